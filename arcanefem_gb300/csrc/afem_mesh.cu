@@ -1,0 +1,328 @@
+// Connectivity and sparsity for P1 meshes.
+//
+// node -> cell adjacency (the transpose of cell -> node):
+//   histogram of incidences, exclusive scan, scatter, then a per-node
+//   segmented sort of (cell, local) keys so that cells come out ascending --
+//   the order of Arcane's nodeCell() connectivity.  The histogram and scatter
+//   use integer atomics on per-node counters; the segmented sort makes the
+//   result independent of their order, so the output is deterministic.
+//
+// node -> node sparsity (rows of the assembled matrix):
+//   one warp per node gathers the nodes of its incident cells into shared
+//   memory, bitonic-sorts them and keeps the distinct values: row length =
+//   1 + number of neighbours (femutils/BSRFormat.cc:445-557, row = deg + 1).
+//   A second pass writes the columns (ascending or self-last) and the slot
+//   map used by the assembly kernels.
+#include <climits>
+
+#include "afem_internal.cuh"
+
+namespace afem {
+
+// ---------------------------------------------------------------------------
+// node -> cell
+
+__global__ void k_nc_count(const int32_t* __restrict__ cn, int64_t total, int nb_node, int32_t* __restrict__ cnt,
+                           int* __restrict__ err) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t n = cn[i];
+    if (n < 0 || n >= nb_node) {
+      atomicOr(err, 1);
+      continue;
+    }
+    atomicAdd(&cnt[n], 1);
+  }
+}
+
+__global__ void k_nc_scatter(const int32_t* __restrict__ cn, int64_t total, int npc, int nb_node,
+                             const int32_t* __restrict__ nc_ptr, int32_t* __restrict__ cursor,
+                             int32_t* __restrict__ key) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t n = cn[i];
+    if (n < 0 || n >= nb_node) continue;
+    int32_t pos = nc_ptr[n] + atomicAdd(&cursor[n], 1);
+    int32_t cell = (int32_t)(i / npc);
+    int32_t local = (int32_t)(i - (int64_t)cell * npc);
+    key[pos] = cell * 4 + local;  // cells < 2^29 checked by the caller
+  }
+}
+
+// Per-node insertion sort of the (cell * 4 + local) keys, then split.
+__global__ void k_nc_sort(int nb_node, const int32_t* __restrict__ nc_ptr, int32_t* __restrict__ key,
+                          int32_t* __restrict__ nc_cell, uint8_t* __restrict__ nc_local) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb_node; n += gridDim.x * blockDim.x) {
+    int32_t b = nc_ptr[n], e = nc_ptr[n + 1];
+    for (int32_t i = b + 1; i < e; ++i) {
+      int32_t v = key[i];
+      int32_t j = i - 1;
+      while (j >= b && key[j] > v) {
+        key[j + 1] = key[j];
+        --j;
+      }
+      key[j + 1] = v;
+    }
+    for (int32_t i = b; i < e; ++i) {
+      int32_t v = key[i];
+      nc_cell[i] = v >> 2;
+      nc_local[i] = (uint8_t)(v & 3);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// node -> node
+
+constexpr int kRowWarps = 8;        // warps per block
+constexpr int kRowCap = 512;        // candidates per node (deg * npc), e.g. 128 tetrahedra
+constexpr int kMaxRowLen = 255;     // slot map entries are uint8
+
+__device__ __forceinline__ void warp_bitonic_sort(int32_t* s, int P) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < P; i += 32) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          int32_t a = s[i], b = s[ixj];
+          bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            s[i] = b;
+            s[ixj] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Gathers, sorts and compacts the distinct candidate nodes of node n into
+// `u` (ascending).  Returns the number of distinct nodes (row length), or -1
+// if the candidate count exceeds kRowCap.
+__device__ int warp_row_unique(int n, int npc, const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_ptr,
+                               const int32_t* __restrict__ nc_cell, int32_t* s, int32_t* u) {
+  const int lane = threadIdx.x & 31;
+  int32_t b = nc_ptr[n], e = nc_ptr[n + 1];
+  int m = (e - b) * npc;
+  if (m > kRowCap) return -1;
+  int P = 32;
+  while (P < m) P <<= 1;
+  for (int i = lane; i < P; i += 32) {
+    int32_t v = INT_MAX;
+    if (i < m) {
+      int k = i / npc, j = i - k * npc;
+      v = cn[(int64_t)nc_cell[b + k] * npc + j];
+    }
+    s[i] = v;
+  }
+  __syncwarp();
+  warp_bitonic_sort(s, P);
+  int count = 0;
+  for (int i0 = 0; i0 < P; i0 += 32) {
+    int i = i0 + lane;
+    int32_t v = s[i];
+    bool keep = v != INT_MAX && (i == 0 || s[i - 1] != v);
+    unsigned mask = __ballot_sync(0xffffffffu, keep);
+    if (keep) u[count + __popc(mask & ((1u << lane) - 1u))] = v;
+    count += __popc(mask);
+  }
+  __syncwarp();
+  return count;
+}
+
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_len(int nb_node, int npc, const int32_t* __restrict__ cn,
+                                                            const int32_t* __restrict__ nc_ptr,
+                                                            const int32_t* __restrict__ nc_cell,
+                                                            int32_t* __restrict__ row_len, int* __restrict__ err) {
+  __shared__ int32_t sh_s[kRowWarps][kRowCap];
+  __shared__ int32_t sh_u[kRowWarps][kRowCap];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int n = blockIdx.x * kRowWarps + w; n < nb_node; n += gridDim.x * kRowWarps) {
+    int len = warp_row_unique(n, npc, cn, nc_ptr, nc_cell, sh_s[w], sh_u[w]);
+    if (lane == 0) {
+      if (len < 0 || len > kMaxRowLen) {
+        atomicOr(err, 2);
+        len = 0;
+      }
+      row_len[n] = len;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(int nb_node, int npc, const int32_t* __restrict__ cn,
+                                                             const int32_t* __restrict__ nc_ptr,
+                                                             const int32_t* __restrict__ nc_cell,
+                                                             const uint8_t* __restrict__ nc_local,
+                                                             const int32_t* __restrict__ row_ptr, int self_last,
+                                                             int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
+                                                             int* __restrict__ err) {
+  __shared__ int32_t sh_s[kRowWarps][kRowCap];
+  __shared__ int32_t sh_u[kRowWarps][kRowCap];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int n = blockIdx.x * kRowWarps + w; n < nb_node; n += gridDim.x * kRowWarps) {
+    int32_t* u = sh_u[w];
+    int len = warp_row_unique(n, npc, cn, nc_ptr, nc_cell, sh_s[w], u);
+    int32_t rb = row_ptr[n];
+    if (len < 0 || len != row_ptr[n + 1] - rb) {
+      if (lane == 0) atomicOr(err, 4);
+      continue;
+    }
+    // position of the diagonal in the ascending list
+    int self_pos = -1;
+    for (int i0 = 0; i0 < len; i0 += 32) {
+      int i = i0 + lane;
+      unsigned m = __ballot_sync(0xffffffffu, i < len && u[i] == n);
+      if (m && self_pos < 0) self_pos = i0 + __ffs(m) - 1;
+    }
+    // columns
+    for (int i = lane; i < len; i += 32) {
+      int dst = i;
+      if (self_last) dst = (i == self_pos) ? len - 1 : (i > self_pos ? i - 1 : i);
+      cols[rb + dst] = u[i];
+    }
+    // slot map: incidence p, cell node j -> position of that column in the row
+    int32_t b = nc_ptr[n], e = nc_ptr[n + 1];
+    int m = (e - b) * npc;
+    for (int i = lane; i < m; i += 32) {
+      int k = i / npc, j = i - k * npc;
+      int32_t v = cn[(int64_t)nc_cell[b + k] * npc + j];
+      int lo = 0, hi = len - 1;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (u[mid] < v) lo = mid + 1; else hi = mid;
+      }
+      int pos = lo;
+      if (self_last) pos = (pos == self_pos) ? len - 1 : (pos > self_pos ? pos - 1 : pos);
+      slot[(int64_t)(b + k) * npc + j] = (uint8_t)pos;
+    }
+    __syncwarp();
+  }
+}
+
+// Block CSR -> scalar CSR structure (BSRMatrix::toCsr, femutils/BSRFormat.cc:110-172).
+__global__ void k_bsr_rows(int nb_brow, int b, const int32_t* __restrict__ brow_ptr, int32_t* __restrict__ row_ptr) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r <= nb_brow * b; r += gridDim.x * blockDim.x) {
+    if (r == nb_brow * b) {
+      row_ptr[r] = brow_ptr[nb_brow] * b * b;
+      continue;
+    }
+    int br = r / b, i = r - br * b;
+    int32_t s = brow_ptr[br], len = brow_ptr[br + 1] - s;
+    row_ptr[r] = s * b * b + i * len * b;
+  }
+}
+
+__global__ void k_bsr_cols(int nb_brow, int b, const int32_t* __restrict__ brow_ptr, const int32_t* __restrict__ bcols,
+                           int32_t* __restrict__ cols) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nb_brow * b; r += gridDim.x * blockDim.x) {
+    int br = r / b, i = r - br * b;
+    int32_t s = brow_ptr[br], len = brow_ptr[br + 1] - s;
+    int64_t o = (int64_t)s * b * b + (int64_t)i * len * b;
+    for (int32_t x = 0; x < len; ++x)
+      for (int k = 0; k < b; ++k) cols[o + (int64_t)x * b + k] = bcols[s + x] * b + k;
+  }
+}
+
+}  // namespace afem
+
+using namespace afem;
+
+extern "C" {
+
+afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int npc, const int32_t* cell_nodes_d,
+                                 int32_t* nc_ptr_d, int32_t* nc_cell_d, uint8_t* nc_local_d) {
+  AFEM_CHECK_ARG(ctx, "afem_node_cell_build: null context");
+  AFEM_CHECK_ARG(nb_node > 0 && nb_cell > 0, "afem_node_cell_build: empty mesh (nb_node=%d nb_cell=%d)", nb_node,
+                 nb_cell);
+  AFEM_CHECK_ARG(npc == 3 || npc == 4, "afem_node_cell_build: nodes_per_cell must be 3 or 4 (got %d)", npc);
+  AFEM_CHECK_ARG(nb_cell < (1 << 29), "afem_node_cell_build: too many cells (%d)", nb_cell);
+  AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && nc_local_d, "afem_node_cell_build: null buffer");
+  int64_t total = (int64_t)nb_cell * npc;
+  AFEM_CHECK_ARG(total < INT_MAX, "afem_node_cell_build: too many incidences");
+  size_t need = 2 * align256(sizeof(int32_t) * ((size_t)nb_node + 1)) + align256(sizeof(int32_t) * total) + 256 +
+                scan_scratch_bytes(nb_node);
+  AFEM_TRY(scratch_reserve(ctx, need));
+  int32_t *cnt, *cursor, *key;
+  int* err;
+  AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &cnt));
+  AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &cursor));
+  AFEM_TRY(scratch_take(ctx, (size_t)total, &key));
+  AFEM_TRY(scratch_take(ctx, 1, &err));
+  AFEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)nb_node + 1), ctx->stream));
+  AFEM_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * ((size_t)nb_node + 1), ctx->stream));
+  AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  AFEM_TRY(launch(ctx, k_nc_count, grid_for(ctx, total, 256), 256, 0, cell_nodes_d, total, nb_node, cnt, err));
+  AFEM_TRY(exclusive_scan_i32(ctx, cnt, nc_ptr_d, nb_node));
+  AFEM_TRY(launch(ctx, k_nc_scatter, grid_for(ctx, total, 256), 256, 0, cell_nodes_d, total, npc, nb_node,
+                  (const int32_t*)nc_ptr_d, cursor, key));
+  AFEM_TRY(launch(ctx, k_nc_sort, grid_for(ctx, nb_node, 128, 16), 128, 0, nb_node, (const int32_t*)nc_ptr_d, key,
+                  nc_cell_d, nc_local_d));
+  int herr = 0;
+  AFEM_TRY(read_scalar(ctx, err, &herr));
+  if (herr) return fail(AFEM_ERR_MESH, "afem_node_cell_build: node id out of range [0, %d) in cell_nodes", nb_node);
+  return AFEM_OK;
+}
+
+afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int32_t* cell_nodes_d,
+                               const int32_t* nc_ptr_d, const int32_t* nc_cell_d, int32_t* row_ptr_d, int64_t* nnz_h) {
+  AFEM_CHECK_ARG(ctx, "afem_sparsity_rows: null context");
+  AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4), "afem_sparsity_rows: bad sizes");
+  AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && row_ptr_d, "afem_sparsity_rows: null buffer");
+  size_t need = align256(sizeof(int32_t) * ((size_t)nb_node + 1)) + 256 + scan_scratch_bytes(nb_node);
+  AFEM_TRY(scratch_reserve(ctx, need));
+  int32_t* len;
+  int* err;
+  AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &len));
+  AFEM_TRY(scratch_take(ctx, 1, &err));
+  AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  unsigned grid = (unsigned)std::min<int64_t>((nb_node + kRowWarps - 1) / kRowWarps, (int64_t)ctx->sm_count * 8);
+  AFEM_TRY(launch(ctx, k_row_len, grid, kRowWarps * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, len, err));
+  AFEM_TRY(exclusive_scan_i32(ctx, len, row_ptr_d, nb_node));
+  int herr = 0;
+  AFEM_TRY(read_scalar(ctx, err, &herr));
+  if (herr)
+    return fail(AFEM_ERR_MESH,
+                "afem_sparsity_rows: a node has more than %d cell-node incidences or more than %d neighbours",
+                kRowCap, kMaxRowLen);
+  if (nnz_h) {
+    int32_t nnz = 0;
+    AFEM_TRY(read_scalar(ctx, row_ptr_d + nb_node, &nnz));
+    *nnz_h = nnz;
+  }
+  return AFEM_OK;
+}
+
+afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int32_t* cell_nodes_d,
+                               const int32_t* nc_ptr_d, const int32_t* nc_cell_d, const uint8_t* nc_local_d,
+                               const int32_t* row_ptr_d, int col_order, int32_t* cols_d, uint8_t* nc_slot_d) {
+  AFEM_CHECK_ARG(ctx, "afem_sparsity_cols: null context");
+  AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4), "afem_sparsity_cols: bad sizes");
+  AFEM_CHECK_ARG(col_order == AFEM_COLS_ASCENDING || col_order == AFEM_COLS_SELF_LAST,
+                 "afem_sparsity_cols: bad col_order %d", col_order);
+  AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && row_ptr_d && cols_d && nc_slot_d,
+                 "afem_sparsity_cols: null buffer");
+  AFEM_TRY(scratch_reserve(ctx, 256));
+  int* err;
+  AFEM_TRY(scratch_take(ctx, 1, &err));
+  AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  unsigned grid = (unsigned)std::min<int64_t>((nb_node + kRowWarps - 1) / kRowWarps, (int64_t)ctx->sm_count * 8);
+  AFEM_TRY(launch(ctx, k_row_fill, grid, kRowWarps * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d,
+                  nc_local_d, row_ptr_d, col_order, cols_d, nc_slot_d, err));
+  int herr = 0;
+  AFEM_TRY(read_scalar(ctx, err, &herr));
+  if (herr) return fail(AFEM_ERR_MESH, "afem_sparsity_cols: row_ptr does not match the mesh");
+  return AFEM_OK;
+}
+
+afem_status afem_bsr_to_csr_structure(afem_context ctx, int nb_brow, int b, const int32_t* brow_ptr_d,
+                                      const int32_t* bcols_d, int32_t* row_ptr_d, int32_t* cols_d) {
+  AFEM_CHECK_ARG(ctx && nb_brow > 0 && b >= 1 && b <= 8, "afem_bsr_to_csr_structure: bad arguments");
+  AFEM_CHECK_ARG(brow_ptr_d && bcols_d && row_ptr_d && cols_d, "afem_bsr_to_csr_structure: null buffer");
+  scratch_reset(ctx);
+  AFEM_TRY(launch(ctx, k_bsr_rows, grid_for(ctx, (int64_t)nb_brow * b + 1, 256), 256, 0, nb_brow, b, brow_ptr_d,
+                  row_ptr_d));
+  return launch(ctx, k_bsr_cols, grid_for(ctx, (int64_t)nb_brow * b, 256), 256, 0, nb_brow, b, brow_ptr_d, bcols_d,
+                cols_d);
+}
+
+}  // extern "C"

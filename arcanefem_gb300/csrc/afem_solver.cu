@@ -1,0 +1,812 @@
+// Krylov solve on the assembled CSR system.
+//
+// Replaces the external HYPRE / PETSc / Aleph / Arcane MatVec solvers behind
+// IDoFLinearSystemImpl::solve (femutils/HypreDoFLinearSystem.cc:596-751,
+// femutils/DoFLinearSystem.cc:151-159).  Diagonal (Jacobi) preconditioned CG
+// with HYPRE's two-norm stop ||r|| <= max(rtol ||b||, atol).
+//
+// Layout of one iteration (3 kernels, captured in a CUDA graph per chunk of
+// iterations):
+//   K1  q = A p, <p, q>           -> alpha        (last-block finalize)
+//   K2  x += alpha p, r -= alpha q, z = D^-1 r, <r, z>, <r, r> -> beta, stop
+//   K3  p = z + beta p
+// Dot products are block partial sums reduced in a fixed order by the last
+// block to finish (threadfence + ticket), so results are deterministic.
+// A device flag stops the remaining kernels of a chunk once converged.
+//
+// MIXED precision: FP64 iterative refinement (r = b - A x with FP64 values,
+// FP64 norms) around an FP32 CG (FP32 matrix values and vectors, FP64 dot
+// product accumulation).
+#include <algorithm>
+#include <cmath>
+
+#include "afem_internal.cuh"
+
+namespace afem {
+
+constexpr int kSolveBlock = 256;
+
+struct CgState {
+  double rz, rr, pq, alpha, beta, bnorm2, tol2, pad0;
+  int done, iter, status, max_iter;
+  unsigned int ticket[4];
+};
+
+// ---------------------------------------------------------------------------
+// SpMV: G lanes per row, fixed-order reduction.
+template <int G, class T, class V>
+__device__ __forceinline__ double row_dot(int row, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                          const T* __restrict__ vals, const V* __restrict__ x, int lane) {
+  double s = 0.0;
+  const int32_t e = __ldg(rp + row + 1);
+  for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s += (double)__ldg(vals + k) * (double)__ldg(x + __ldg(cols + k));
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
+// FP32 row dot product accumulated in FP32 (inner solve).
+template <int G>
+__device__ __forceinline__ float row_dot_f(int row, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                           const float* __restrict__ vals, const float* __restrict__ x, int lane) {
+  float s = 0.f;
+  const int32_t e = __ldg(rp + row + 1);
+  for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s = fmaf(__ldg(vals + k), __ldg(x + __ldg(cols + k)), s);
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_spmv(int n, const int32_t* __restrict__ rp,
+                                                      const int32_t* __restrict__ cols, const double* __restrict__ vals,
+                                                      const double* __restrict__ x, double* __restrict__ y) {
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < n + ((groups - n % groups) % groups);
+       row += groups) {
+    const bool ok = row < n;
+    double s = 0.0;
+    if (ok) s = row_dot<G>(row, rp, cols, vals, x, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (ok && lane == 0) y[row] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Last-block finalize helper: every block publishes partials[blockIdx.x * W + w];
+// returns true in the (single) last block, after which all partials are visible.
+__device__ __forceinline__ bool last_block(unsigned int* ticket) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int t = atomicAdd(ticket, 1u);
+    is_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+// Fixed-order sum of partials[k * W + w], k < nparts (valid in thread 0).
+__device__ __forceinline__ double reduce_partials(const double* partials, int nparts, int W, int w, double* sh) {
+  double s = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += ((volatile const double*)partials)[(int64_t)k * W + w];
+  return block_sum(s, sh);
+}
+
+// r = b - A x ; z = D^-1 r ; p = z ; <r,z>, <r,r>, <b,b> (masked) ; initial stop test
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_cg_init(int n, const int32_t* __restrict__ rp,
+                                                         const int32_t* __restrict__ cols,
+                                                         const double* __restrict__ vals, const double* __restrict__ b,
+                                                         const double* __restrict__ x, const double* __restrict__ dinv,
+                                                         const uint8_t* __restrict__ skip, double* __restrict__ r,
+                                                         double* __restrict__ z, double* __restrict__ p,
+                                                         double* partials, CgState* st, double rtol, double atol) {
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  double rz = 0.0, rr = 0.0, bb = 0.0;
+  const int nr = n + ((groups - n % groups) % groups);
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
+    double s = 0.0;
+    if (row < n) s = row_dot<G>(row, rp, cols, vals, x, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (row < n && lane == 0) {
+      double bi = b[row];
+      double ri = bi - s;
+      double zi = dinv ? dinv[row] * ri : ri;
+      r[row] = ri;
+      z[row] = zi;
+      p[row] = zi;
+      rz += ri * zi;
+      if (!(skip && skip[row])) {
+        rr += ri * ri;
+        bb += bi * bi;
+      }
+    }
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  bb = block_sum(bb, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 3 + 0] = rz;
+    partials[blockIdx.x * 3 + 1] = rr;
+    partials[blockIdx.x * 3 + 2] = bb;
+  }
+  if (last_block(&st->ticket[0])) {
+    double trz = reduce_partials(partials, gridDim.x, 3, 0, sh);
+    double trr = reduce_partials(partials, gridDim.x, 3, 1, sh);
+    double tbb = reduce_partials(partials, gridDim.x, 3, 2, sh);
+    if (threadIdx.x == 0) {
+      st->rz = trz;
+      st->rr = trr;
+      st->bnorm2 = tbb;
+      double t = std::max(rtol * rtol * tbb, atol * atol);
+      st->tol2 = t;
+      st->iter = 0;
+      st->status = AFEM_OK;
+      st->done = (trr <= t) ? 1 : 0;
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// K1: q = A p, <p, q> -> alpha
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_cg_spmv(int n, const int32_t* __restrict__ rp,
+                                                         const int32_t* __restrict__ cols,
+                                                         const double* __restrict__ vals, const double* __restrict__ p,
+                                                         double* __restrict__ q, double* partials, CgState* st) {
+  if (((volatile CgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  const int nr = n + ((groups - n % groups) % groups);
+  double pq = 0.0;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
+    double s = 0.0;
+    if (row < n) s = row_dot<G>(row, rp, cols, vals, p, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (row < n && lane == 0) {
+      q[row] = s;
+      pq += p[row] * s;
+    }
+  }
+  pq = block_sum(pq, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = pq;
+  if (last_block(&st->ticket[1])) {
+    double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
+    if (threadIdx.x == 0) {
+      st->pq = t;
+      if (!(t > 0.0) || !isfinite(t)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+        st->alpha = 0.0;
+      } else {
+        st->alpha = st->rz / t;
+      }
+      st->ticket[1] = 0;
+    }
+  }
+}
+
+// K2: x += alpha p ; r -= alpha q ; z = D^-1 r ; <r,z>, <r,r> -> beta, stop test
+__global__ void __launch_bounds__(kSolveBlock) k_cg_update(int n, double* __restrict__ x, double* __restrict__ r,
+                                                           double* __restrict__ z, const double* __restrict__ p,
+                                                           const double* __restrict__ q,
+                                                           const double* __restrict__ dinv,
+                                                           const uint8_t* __restrict__ skip, double* partials,
+                                                           CgState* st) {
+  if (((volatile CgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const double alpha = ((volatile CgState*)st)->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double pi = p[i];
+    x[i] += alpha * pi;
+    double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    double zi = dinv ? dinv[i] * ri : ri;
+    z[i] = zi;
+    rz += ri * zi;
+    if (!(skip && skip[i])) rr += ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 2 + 0] = rz;
+    partials[blockIdx.x * 2 + 1] = rr;
+  }
+  if (last_block(&st->ticket[2])) {
+    double trz = reduce_partials(partials, gridDim.x, 2, 0, sh);
+    double trr = reduce_partials(partials, gridDim.x, 2, 1, sh);
+    if (threadIdx.x == 0) {
+      st->beta = trz / st->rz;
+      st->rz = trz;
+      st->rr = trr;
+      st->iter += 1;
+      if (!isfinite(trr)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+      } else if (trr <= st->tol2) {
+        st->done = 1;
+      } else if (st->iter >= st->max_iter) {
+        st->status = AFEM_ERR_NOT_CONVERGED;
+        st->done = 1;
+      }
+      st->ticket[2] = 0;
+    }
+  }
+}
+
+// K3: p = z + beta p (skipped once converged: p is not used any more)
+__global__ void __launch_bounds__(kSolveBlock) k_cg_dir(int n, const double* __restrict__ z, double* __restrict__ p,
+                                                        const CgState* st) {
+  if (((volatile const CgState*)st)->done) return;
+  const double beta = ((volatile const CgState*)st)->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
+}
+
+// D^-1 from the diagonal entries (1 where the diagonal is missing or zero).
+__global__ void k_inv_diag(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                           const double* __restrict__ vals, double* __restrict__ dinv, float* __restrict__ dinv32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double d = 0.0;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+      if (cols[k] == i) {
+        d = vals[k];
+        break;
+      }
+    double v = d != 0.0 ? 1.0 / d : 1.0;
+    if (dinv) dinv[i] = v;
+    if (dinv32) dinv32[i] = (float)v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 inner CG (mixed precision).  Same structure, FP32 vectors and values,
+// FP64 dot-product accumulation.
+
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv(int n, const int32_t* __restrict__ rp,
+                                                          const int32_t* __restrict__ cols,
+                                                          const float* __restrict__ vals, const float* __restrict__ p,
+                                                          float* __restrict__ q, double* partials, CgState* st) {
+  if (((volatile CgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  const int nr = n + ((groups - n % groups) % groups);
+  double pq = 0.0;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
+    float s = 0.f;
+    if (row < n) s = row_dot_f<G>(row, rp, cols, vals, p, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (row < n && lane == 0) {
+      q[row] = s;
+      pq += (double)p[row] * (double)s;
+    }
+  }
+  pq = block_sum(pq, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = pq;
+  if (last_block(&st->ticket[1])) {
+    double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
+    if (threadIdx.x == 0) {
+      st->pq = t;
+      if (!(t > 0.0) || !isfinite(t)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+        st->alpha = 0.0;
+      } else {
+        st->alpha = st->rz / t;
+      }
+      st->ticket[1] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveBlock) k_cgf_update(int n, float* __restrict__ x, float* __restrict__ r,
+                                                            float* __restrict__ z, const float* __restrict__ p,
+                                                            const float* __restrict__ q,
+                                                            const float* __restrict__ dinv,
+                                                            const uint8_t* __restrict__ skip, double* partials,
+                                                            CgState* st) {
+  if (((volatile CgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const float alpha = (float)((volatile CgState*)st)->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = fmaf(alpha, p[i], x[i]);
+    float ri = fmaf(-alpha, q[i], r[i]);
+    r[i] = ri;
+    float zi = dinv[i] * ri;
+    z[i] = zi;
+    rz += (double)ri * (double)zi;
+    if (!(skip && skip[i])) rr += (double)ri * (double)ri;
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 2 + 0] = rz;
+    partials[blockIdx.x * 2 + 1] = rr;
+  }
+  if (last_block(&st->ticket[2])) {
+    double trz = reduce_partials(partials, gridDim.x, 2, 0, sh);
+    double trr = reduce_partials(partials, gridDim.x, 2, 1, sh);
+    if (threadIdx.x == 0) {
+      st->beta = trz / st->rz;
+      st->rz = trz;
+      st->rr = trr;
+      st->iter += 1;
+      if (!isfinite(trr)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+      } else if (trr <= st->tol2 || st->iter >= st->max_iter) {
+        st->done = 1;
+      }
+      st->ticket[2] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveBlock) k_cgf_dir(int n, const float* __restrict__ z, float* __restrict__ p,
+                                                         const CgState* st) {
+  if (((volatile const CgState*)st)->done) return;
+  const float beta = (float)((volatile const CgState*)st)->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fmaf(beta, p[i], z[i]);
+}
+
+// Outer step of the refinement: r = b - A x (FP64), r32 = (float) r, x32 = 0,
+// z32 = D^-1 r32, p32 = z32 ; <r32, z32> and FP64 ||r||^2 ; inner state reset.
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
+    int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols, const double* __restrict__ vals,
+    const double* __restrict__ b, const double* __restrict__ x, const float* __restrict__ dinv32,
+    const uint8_t* __restrict__ skip, float* __restrict__ r32, float* __restrict__ x32, float* __restrict__ z32,
+    float* __restrict__ p32, double* partials, CgState* outer, CgState* inner, double inner_rtol, int inner_max) {
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  const int nr = n + ((groups - n % groups) % groups);
+  double rz = 0.0, rr = 0.0, bb = 0.0;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
+    double s = 0.0;
+    if (row < n) s = row_dot<G>(row, rp, cols, vals, x, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (row < n && lane == 0) {
+      double bi = b[row];
+      double ri = bi - s;
+      float rf = (float)ri;
+      float zf = dinv32[row] * rf;
+      r32[row] = rf;
+      x32[row] = 0.f;
+      z32[row] = zf;
+      p32[row] = zf;
+      rz += (double)rf * (double)zf;
+      if (!(skip && skip[row])) {
+        rr += ri * ri;
+        bb += bi * bi;
+      }
+    }
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  bb = block_sum(bb, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 3 + 0] = rz;
+    partials[blockIdx.x * 3 + 1] = rr;
+    partials[blockIdx.x * 3 + 2] = bb;
+  }
+  if (last_block(&outer->ticket[0])) {
+    double trz = reduce_partials(partials, gridDim.x, 3, 0, sh);
+    double trr = reduce_partials(partials, gridDim.x, 3, 1, sh);
+    double tbb = reduce_partials(partials, gridDim.x, 3, 2, sh);
+    if (threadIdx.x == 0) {
+      outer->rr = trr;
+      outer->bnorm2 = tbb;
+      outer->done = (trr <= outer->tol2) ? 1 : 0;
+      outer->ticket[0] = 0;
+      inner->rz = trz;
+      inner->rr = trr;
+      inner->tol2 = inner_rtol * inner_rtol * trr;
+      inner->iter = 0;
+      inner->max_iter = inner_max;
+      inner->status = AFEM_OK;
+      inner->done = outer->done;
+    }
+  }
+}
+
+__global__ void k_ir_correct(int n, double* __restrict__ x, const float* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)d[i];
+}
+
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+__global__ void k_fill_f32(int64_t n, float v, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+int lanes_per_row(int n, int64_t nnz) {
+  double avg = n > 0 ? (double)nnz / n : 1.0;
+  if (avg <= 6) return 4;
+  if (avg <= 20) return 8;
+  if (avg <= 48) return 16;
+  return 32;
+}
+
+template <class F>
+afem_status dispatch_g(int G, F&& f) {
+  switch (G) {
+    case 4: return f(std::integral_constant<int, 4>{});
+    case 8: return f(std::integral_constant<int, 8>{});
+    case 16: return f(std::integral_constant<int, 16>{});
+    default: return f(std::integral_constant<int, 32>{});
+  }
+}
+
+template <class Kernel, class... Args>
+afem_status launch_s(afem_context ctx, cudaStream_t s, Kernel k, unsigned grid, unsigned block, Args... args) {
+  k<<<grid, block, 0, s>>>(args...);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch", __FILE__, __LINE__);
+  ++ctx->launches;
+  return AFEM_OK;
+}
+
+struct GraphChunk {
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  ~GraphChunk() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+// Capture `body(stream)` once into an executable graph.
+template <class Body>
+afem_status capture(afem_context ctx, GraphChunk& g, Body&& body) {
+  cudaStream_t cs;
+  AFEM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(cs);
+    return cuda_fail(e, "cudaStreamBeginCapture", __FILE__, __LINE__);
+  }
+  int64_t before = ctx->launches;
+  afem_status st = body(cs);
+  cudaError_t e2 = cudaStreamEndCapture(cs, &g.graph);
+  cudaStreamDestroy(cs);
+  ctx->launches = before;  // captured kernels are counted when the graph runs
+  if (st != AFEM_OK) return st;
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture", __FILE__, __LINE__);
+  AFEM_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+  return AFEM_OK;
+}
+
+afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals, int64_t nnz,
+                    const double* b, double* x, const uint8_t* skip, const afem_solver_options& opt,
+                    afem_solve_info* info) {
+  const int G = lanes_per_row(n, nnz);
+  const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
+  const unsigned nparts = std::max(grid_rows, grid_vec);
+  size_t need = 5 * align256(sizeof(double) * (size_t)n) + align256(sizeof(double) * 3 * nparts) +
+                align256(sizeof(CgState));
+  AFEM_TRY(scratch_reserve(ctx, need));
+  double *r, *z, *p, *q, *dinv, *partials;
+  CgState* st;
+  AFEM_TRY(scratch_take(ctx, n, &r));
+  AFEM_TRY(scratch_take(ctx, n, &z));
+  AFEM_TRY(scratch_take(ctx, n, &p));
+  AFEM_TRY(scratch_take(ctx, n, &q));
+  AFEM_TRY(scratch_take(ctx, n, &dinv));
+  AFEM_TRY(scratch_take(ctx, 3 * (size_t)nparts, &partials));
+  AFEM_TRY(scratch_take(ctx, 1, &st));
+  AFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), ctx->stream));
+  const int max_iter = opt.max_iter > 0 ? opt.max_iter : 1000;
+  AFEM_CUDA(cudaMemcpyAsync(&st->max_iter, &max_iter, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  const bool jacobi = opt.precond == AFEM_PRECOND_JACOBI;
+  if (jacobi)
+    AFEM_TRY(launch(ctx, k_inv_diag, grid_vec, kSolveBlock, 0, n, rp, cols, vals, dinv, (float*)nullptr));
+  const double* dv = jacobi ? dinv : nullptr;
+  AFEM_TRY(dispatch_g(G, [&](auto g) {
+    return launch(ctx, k_cg_init<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b,
+                  (const double*)x, dv, skip, r, z, p, partials, st, opt.rtol, opt.atol);
+  }));
+  const int chunk = opt.check_every > 0 ? opt.check_every : 16;
+  GraphChunk gc;
+  AFEM_TRY(capture(ctx, gc, [&](cudaStream_t s) -> afem_status {
+    for (int k = 0; k < chunk; ++k) {
+      AFEM_TRY(dispatch_g(G, [&](auto g) {
+        return launch_s(ctx, s, k_cg_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols, vals,
+                        (const double*)p, q, partials, st);
+      }));
+      AFEM_TRY(launch_s(ctx, s, k_cg_update, grid_vec, kSolveBlock, n, x, r, z, (const double*)p, (const double*)q,
+                        dv, skip, partials, st));
+      AFEM_TRY(launch_s(ctx, s, k_cg_dir, grid_vec, kSolveBlock, n, (const double*)z, p, (const CgState*)st));
+    }
+    return AFEM_OK;
+  }));
+  CgState hs{};
+  for (int done_chunks = 0;; ++done_chunks) {
+    AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+    AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+    hs = *reinterpret_cast<CgState*>(ctx->pinned);
+    if (hs.done) break;
+    AFEM_CUDA(cudaGraphLaunch(gc.exec, ctx->stream));
+    ctx->launches += 3 * chunk;
+  }
+  if (info) {
+    info->iterations = hs.iter;
+    info->refinements = 0;
+    info->status = hs.status;
+  }
+  return hs.status;
+}
+
+afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals, int64_t nnz,
+                     const double* b, double* x, const uint8_t* skip, const afem_solver_options& opt,
+                     afem_solve_info* info) {
+  const int G = lanes_per_row(n, nnz);
+  const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
+  const unsigned nparts = std::max(grid_rows, grid_vec);
+  size_t need = align256(sizeof(float) * (size_t)nnz) + 6 * align256(sizeof(float) * (size_t)n) +
+                align256(sizeof(double) * 3 * nparts) + 2 * align256(sizeof(CgState));
+  AFEM_TRY(scratch_reserve(ctx, need));
+  float *v32, *r32, *z32, *p32, *q32, *x32, *dinv32;
+  double* partials;
+  CgState *outer, *inner;
+  AFEM_TRY(scratch_take(ctx, (size_t)nnz, &v32));
+  AFEM_TRY(scratch_take(ctx, n, &r32));
+  AFEM_TRY(scratch_take(ctx, n, &z32));
+  AFEM_TRY(scratch_take(ctx, n, &p32));
+  AFEM_TRY(scratch_take(ctx, n, &q32));
+  AFEM_TRY(scratch_take(ctx, n, &x32));
+  AFEM_TRY(scratch_take(ctx, n, &dinv32));
+  AFEM_TRY(scratch_take(ctx, 3 * (size_t)nparts, &partials));
+  AFEM_TRY(scratch_take(ctx, 1, &outer));
+  AFEM_TRY(scratch_take(ctx, 1, &inner));
+  AFEM_CUDA(cudaMemsetAsync(outer, 0, sizeof(CgState), ctx->stream));
+  AFEM_CUDA(cudaMemsetAsync(inner, 0, sizeof(CgState), ctx->stream));
+  AFEM_TRY(launch(ctx, k_to_f32, grid_for(ctx, nnz, 256), 256, 0, nnz, vals, v32));
+  AFEM_TRY(launch(ctx, k_inv_diag, grid_vec, kSolveBlock, 0, n, rp, cols, vals, (double*)nullptr, dinv32));
+  if (opt.precond != AFEM_PRECOND_JACOBI)  // unpreconditioned inner solve: D^-1 = 1
+    AFEM_TRY(launch(ctx, k_fill_f32, grid_for(ctx, n, 256), 256, 0, (int64_t)n, 1.0f, dinv32));
+  const double inner_rtol = opt.inner_rtol > 0 ? opt.inner_rtol : 1e-4;
+  const int max_iter = opt.max_iter > 0 ? opt.max_iter : 1000;
+  const int chunk = opt.check_every > 0 ? opt.check_every : 16;
+  // outer tolerance: needs ||b||, computed by the first residual pass
+  GraphChunk gc;
+  AFEM_TRY(capture(ctx, gc, [&](cudaStream_t s) -> afem_status {
+    for (int k = 0; k < chunk; ++k) {
+      AFEM_TRY(dispatch_g(G, [&](auto g) {
+        return launch_s(ctx, s, k_cgf_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols,
+                        (const float*)v32, (const float*)p32, q32, partials, inner);
+      }));
+      AFEM_TRY(launch_s(ctx, s, k_cgf_update, grid_vec, kSolveBlock, n, x32, r32, z32, (const float*)p32,
+                        (const float*)q32, (const float*)dinv32, skip, partials, inner));
+      AFEM_TRY(launch_s(ctx, s, k_cgf_dir, grid_vec, kSolveBlock, n, (const float*)z32, p32, (const CgState*)inner));
+    }
+    return AFEM_OK;
+  }));
+  int total_inner = 0, outer_steps = 0;
+  afem_status status = AFEM_OK;
+  const int max_outer = 100;
+  for (;; ++outer_steps) {
+    AFEM_TRY(dispatch_g(G, [&](auto g) {
+      return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b,
+                    (const double*)x, (const float*)dinv32, skip, r32, x32, z32, p32, partials, outer, inner,
+                    inner_rtol, max_iter);
+    }));
+    CgState ho{};
+    AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, outer, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+    AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+    ho = *reinterpret_cast<CgState*>(ctx->pinned);
+    if (outer_steps == 0) {
+      // first pass: set the FP64 outer tolerance from ||b|| and re-test
+      double tol2 = std::max(opt.rtol * opt.rtol * ho.bnorm2, opt.atol * opt.atol);
+      ho.tol2 = tol2;
+      AFEM_CUDA(cudaMemcpyAsync(&outer->tol2, &ho.tol2, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+      if (ho.rr <= tol2) break;
+      int d = 0;
+      AFEM_CUDA(cudaMemcpyAsync(&inner->done, &d, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    } else if (ho.done) {
+      break;
+    }
+    if (outer_steps >= max_outer || total_inner >= 50 * max_iter) {
+      status = AFEM_ERR_NOT_CONVERGED;
+      break;
+    }
+    CgState hi{};
+    for (;;) {
+      AFEM_CUDA(cudaGraphLaunch(gc.exec, ctx->stream));
+      ctx->launches += 3 * chunk;
+      AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, inner, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+      AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+      hi = *reinterpret_cast<CgState*>(ctx->pinned);
+      if (hi.done) break;
+    }
+    total_inner += hi.iter;
+    if (hi.status == AFEM_ERR_BREAKDOWN && hi.iter == 0) {
+      status = AFEM_ERR_BREAKDOWN;
+      break;
+    }
+    AFEM_TRY(launch(ctx, k_ir_correct, grid_vec, 256, 0, n, x, (const float*)x32));
+  }
+  if (info) {
+    info->iterations = total_inner;
+    info->refinements = outer_steps;
+    info->status = status;
+  }
+  return status;
+}
+
+// ||b - A x||^2 and ||b||^2 (masked), FP64, written to out[0], out[1].
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_true_residual(int n, const int32_t* __restrict__ rp,
+                                                               const int32_t* __restrict__ cols,
+                                                               const double* __restrict__ vals,
+                                                               const double* __restrict__ b,
+                                                               const double* __restrict__ x,
+                                                               const uint8_t* __restrict__ skip, double* partials,
+                                                               unsigned int* ticket, double* out) {
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  const int nr = n + ((groups - n % groups) % groups);
+  double rr = 0.0, bb = 0.0;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
+    double s = 0.0;
+    if (row < n) s = row_dot<G>(row, rp, cols, vals, x, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (row < n && lane == 0 && !(skip && skip[row])) {
+      double ri = b[row] - s;
+      rr += ri * ri;
+      bb += b[row] * b[row];
+    }
+  }
+  rr = block_sum(rr, sh);
+  bb = block_sum(bb, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 2] = rr;
+    partials[blockIdx.x * 2 + 1] = bb;
+  }
+  if (last_block(ticket)) {
+    double a = reduce_partials(partials, gridDim.x, 2, 0, sh);
+    double c = reduce_partials(partials, gridDim.x, 2, 1, sh);
+    if (threadIdx.x == 0) {
+      out[0] = a;
+      out[1] = c;
+      *ticket = 0;
+    }
+  }
+}
+
+afem_status true_relres(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                        int64_t nnz, const double* b, const double* x, const uint8_t* skip, double* relres) {
+  const int G = lanes_per_row(n, nnz);
+  const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * 2 * grid_rows) + 512));
+  double *partials, *out;
+  unsigned int* ticket;
+  AFEM_TRY(scratch_take(ctx, 2 * (size_t)grid_rows, &partials));
+  AFEM_TRY(scratch_take(ctx, 2, &out));
+  AFEM_TRY(scratch_take(ctx, 1, &ticket));
+  AFEM_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), ctx->stream));
+  AFEM_TRY(dispatch_g(G, [&](auto g) {
+    return launch(ctx, k_true_residual<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b, x, skip,
+                  partials, ticket, out);
+  }));
+  AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+  const double* h = reinterpret_cast<const double*>(ctx->pinned);
+  *relres = h[1] > 0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
+  return AFEM_OK;
+}
+
+afem_status solve_csr(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                      const double* b, double* x, const uint8_t* forced, const afem_solver_options* opt_in,
+                      afem_solve_info* info) {
+  AFEM_CHECK_ARG(ctx && n > 0 && rp && cols && vals && b && x, "afem_cg_solve_csr: bad arguments");
+  afem_solver_options opt;
+  if (opt_in) opt = *opt_in;
+  else afem_solver_options_default(&opt);
+  AFEM_CHECK_ARG(opt.precond == AFEM_PRECOND_NONE || opt.precond == AFEM_PRECOND_JACOBI,
+                 "afem_cg_solve_csr: precond %d needs the learned-preconditioner entry points", opt.precond);
+  int32_t nnz32 = 0;
+  AFEM_TRY(read_scalar(ctx, rp + n, &nnz32));
+  const int64_t nnz = nnz32;
+  const uint8_t* skip = opt.skip_forced_rows ? forced : nullptr;
+  cudaEvent_t e0, e1;
+  AFEM_CUDA(cudaEventCreate(&e0));
+  AFEM_CUDA(cudaEventCreate(&e1));
+  AFEM_CUDA(cudaEventRecord(e0, ctx->stream));
+  afem_status st = opt.precision == AFEM_PRECISION_MIXED ? cg_mixed(ctx, n, rp, cols, vals, nnz, b, x, skip, opt, info)
+                                                         : cg_fp64(ctx, n, rp, cols, vals, nnz, b, x, skip, opt, info);
+  cudaEventRecord(e1, ctx->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != AFEM_OK && st != AFEM_ERR_NOT_CONVERGED && st != AFEM_ERR_BREAKDOWN) return st;
+  double rel = 0.0;
+  afem_status s2 = true_relres(ctx, n, rp, cols, vals, nnz, b, x, skip, &rel);
+  if (info) {
+    info->solve_ms = ms;
+    info->relres = rel;
+    info->status = st;
+  }
+  if (s2 != AFEM_OK) return s2;
+  if (st == AFEM_ERR_NOT_CONVERGED) return fail(st, "CG did not reach the tolerance (relres %.3e)", rel);
+  if (st == AFEM_ERR_BREAKDOWN) return fail(st, "CG breakdown (<p, A p> <= 0 or non-finite)");
+  return AFEM_OK;
+}
+
+}  // namespace afem
+
+using namespace afem;
+
+extern "C" {
+
+void afem_solver_options_default(afem_solver_options* o) {
+  if (!o) return;
+  o->rtol = 1e-7;
+  o->atol = 0.0;
+  o->max_iter = 1000;
+  o->precond = AFEM_PRECOND_JACOBI;
+  o->precision = AFEM_PRECISION_FP64;
+  o->skip_forced_rows = 0;
+  o->inner_rtol = 1e-4;
+  o->check_every = 16;
+}
+
+afem_status afem_cg_solve_csr(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                              const double* b, double* x, const uint8_t* forced, const afem_solver_options* opt,
+                              afem_solve_info* info) {
+  return solve_csr(ctx, n, rp, cols, vals, b, x, forced, opt, info);
+}
+
+afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                          const double* x, double* y) {
+  AFEM_CHECK_ARG(ctx && n > 0 && rp && cols && vals && x && y, "afem_spmv_csr: bad arguments");
+  int32_t nnz = 0;
+  AFEM_TRY(read_scalar(ctx, rp + n, &nnz));
+  const int G = lanes_per_row(n, nnz);
+  const unsigned grid = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  return dispatch_g(G, [&](auto g) {
+    return launch(ctx, k_spmv<decltype(g)::value>, grid, kSolveBlock, 0, n, rp, cols, vals, x, y);
+  });
+}
+
+}  // extern "C"

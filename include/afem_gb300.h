@@ -1,0 +1,299 @@
+/*
+ * afem_gb300.h -- C ABI of the GB300 (sm_103a) node-wise P1 assembly and
+ * Krylov library.
+ *
+ * This is the drop-in boundary for ArcaneFEM's GPU hot path.  Each entry
+ * point names the reference interface it replaces (paths relative to the
+ * arcanefem source tree).  Conventions:
+ *
+ *   - every pointer argument suffixed _d is device memory; _h is host memory;
+ *   - every call is asynchronous on the stream of its context, except where
+ *     it returns a host value (documented per call);
+ *   - every call returns an afem_status and never aborts; the message of the
+ *     last failure of the calling thread is afem_last_error();
+ *   - coords: double[nb_node][3] (Arcane Real3, z = 0 in 2D);
+ *     cell_nodes: int32[nb_cell][nodes_per_cell] (3 triangle, 4 tetrahedron);
+ *   - DoF numbering: dof = node * nb_dof + component
+ *     (femutils/FemDoFsOnNodes.cc:72-112);
+ *   - row_ptr: int32[nb_row + 1].  The reference CsrFormatMatrixView stores N
+ *     row starts and ends the last row at nbColumn()
+ *     (femutils/CsrFormatMatrixView.h:181-187); row_ptr[N] = nnz is that end.
+ *
+ * Handles are not thread safe: use one context per host thread / stream.
+ */
+#ifndef AFEM_GB300_H
+#define AFEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The library is built with hidden visibility; these are its only exports. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* Status codes.  Replace ARCANE_FATAL / ARCANE_THROW (femutils/BSRFormat.cc:51-55)
+ * and the HYPRE error mapping (femutils/HypreDoFLinearSystem.cc:86-111). */
+typedef int afem_status;
+enum {
+  AFEM_OK = 0,
+  AFEM_ERR_BAD_ARG = 1,          /* ArgumentException */
+  AFEM_ERR_OOM = 2,
+  AFEM_ERR_NOT_CONVERGED = 3,
+  AFEM_ERR_BREAKDOWN = 4,        /* <p, A p> <= 0 or NaN in CG */
+  AFEM_ERR_TIMEOUT = 5,          /* a bounded device wait ran out */
+  AFEM_ERR_CUDA = 6,
+  AFEM_ERR_MESH = 7,             /* bad connectivity, degree above a kernel limit */
+  AFEM_ERR_NOT_IMPLEMENTED = 8,  /* NotImplementedException */
+  AFEM_ERR_NOT_FOUND = 9         /* "Value not found" (BSRFormat.cc:105) */
+};
+
+/* Message of the last failure on this host thread ("" if none). */
+const char* afem_last_error(void);
+/* Library version, e.g. 10000 for 1.0.0. */
+int afem_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* Context: a stream plus a device scratch arena.  Replaces the Arcane
+ * RunQueue and its memory resource (femutils/CsrFormatMatrix.cc:40-47). */
+typedef struct afem_context_s* afem_context;
+
+afem_status afem_context_create(afem_context* ctx, void* cuda_stream);
+afem_status afem_context_destroy(afem_context ctx);
+afem_status afem_context_set_stream(afem_context ctx, void* cuda_stream);
+/* Block the host until the context's stream is idle (RunQueue::barrier). */
+afem_status afem_context_synchronize(afem_context ctx);
+/* Number of kernels this library launched through the context so far. */
+afem_status afem_context_launch_count(afem_context ctx, int64_t* count_h);
+/* Measured FP64 FMA issue rate of the device (G FMA/s), the ceiling of the
+ * FP64-bound element kernels.  No reference counterpart (a roofline helper).
+ * Synchronous, about 10 ms. */
+afem_status afem_device_fp64_fma_rate(afem_context ctx, double* gfma_per_s_h);
+
+/* ---------------------------------------------------------------------- */
+/* Connectivity and sparsity.
+ *
+ * Node -> cell adjacency: Arcane's nodeCell() connectivity
+ * (used at femutils/BSRFormat.h:411,428; NodeWiseCsrBiliAssembly.cc:179,188),
+ * cells ascending per node.  nc_local_d[p] = position of the node inside
+ * cell nc_cell_d[p].  Buffers: nc_ptr_d[nb_node+1], nc_cell_d and
+ * nc_local_d[nb_cell*nodes_per_cell].  Deterministic. */
+afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int nodes_per_cell,
+                                 const int32_t* cell_nodes_d, int32_t* nc_ptr_d, int32_t* nc_cell_d,
+                                 uint8_t* nc_local_d);
+
+/* Column order of a row. */
+enum {
+  AFEM_COLS_ASCENDING = 0,   /* canonical; the DOK/ordered-map order (internal/OrderedRowColumnMap.h:59) */
+  AFEM_COLS_SELF_LAST = 1    /* neighbours ascending, diagonal last (BSRFormat.cc:658-672,758-770) */
+};
+
+/* Node-to-node sparsity, step 1: row_ptr_d[nb_node+1] (row length = 1 +
+ * number of distinct neighbours) and the total in *nnz_h (host, synchronous).
+ * Replaces computeRowIndexAtomicFree / computeRowIndex (BSRFormat.cc:562-573,
+ * 912-924) and _buildOffsetsNodeWiseCsr (NodeWiseCsrBiliAssembly.cc:90-112). */
+afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int nodes_per_cell, const int32_t* cell_nodes_d,
+                               const int32_t* nc_ptr_d, const int32_t* nc_cell_d, int32_t* row_ptr_d,
+                               int64_t* nnz_h);
+/* Step 2: cols_d[nnz] in the requested order, and nc_slot_d[nb_cell *
+ * nodes_per_cell * nodes_per_cell] (uint8): for incidence p of node n and
+ * cell node j, the position inside row n of column cell_nodes[c][j].  The
+ * slot map lets the assembly skip the reference's linear column search
+ * (BSRFormat.h:449-462).  Replaces computeColumnsAtomicFree / computeColumns
+ * (BSRFormat.cc:578-772, 929-971) and _buildMatrixNodeWiseCsr
+ * (NodeWiseCsrBiliAssembly.cc:115-152). */
+afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int nodes_per_cell, const int32_t* cell_nodes_d,
+                               const int32_t* nc_ptr_d, const int32_t* nc_cell_d, const uint8_t* nc_local_d,
+                               const int32_t* row_ptr_d, int col_order, int32_t* cols_d, uint8_t* nc_slot_d);
+
+/* ---------------------------------------------------------------------- */
+/* Node-wise (atomic-free) assembly.
+ *
+ * Value layouts for block size b (BSRFormat.h:514-526, BSRFormat.cc:79-106):
+ *   AFEM_LAYOUT_PER_BLOCK: values[(row_ptr[r] + x) * b*b + i*b + j]
+ *   AFEM_LAYOUT_PER_ROW  : values[row_ptr[r]*b*b + b*(x + i*nnzb_row) + j]
+ *                          (CSR-compatible: scalar row r*b+i is contiguous)
+ * For b = 1 both layouts are plain CSR. */
+enum { AFEM_LAYOUT_PER_BLOCK = 0, AFEM_LAYOUT_PER_ROW = 1 };
+
+typedef struct {
+  int dim;                       /* 2 (triangles) or 3 (tetrahedra) */
+  int nb_node;
+  int nb_cell;
+  const double* coords_d;        /* [nb_node][3] */
+  const int32_t* cell_nodes_d;   /* [nb_cell][dim+1] */
+  const int32_t* nc_ptr_d;       /* [nb_node+1] */
+  const int32_t* nc_cell_d;      /* [nb_cell*(dim+1)] */
+  const uint8_t* nc_local_d;     /* [nb_cell*(dim+1)] */
+  const uint8_t* nc_slot_d;      /* [nb_cell*(dim+1)^2] from afem_sparsity_cols */
+} afem_mesh_view;
+
+/* Scalar Poisson P1 stiffness, -div(k grad u): values_d[nnz] (CSR) receives
+ * sum_cells k_c vol grad N_i . grad N_j.  cell_coeff_d (nullable) holds k_c.
+ * Replaces assembleBilinearAtomicFree with _computeElementVectorTria3Gpu /
+ * _computeElementVectorTetra4Gpu (BSRFormat.h:556-565,
+ * modules/poisson/ElementMatrix.h:54-63,107-118) and the testlab
+ * _assembleNodeWiseCsrBilinearOperatorTria3/Tetra4
+ * (modules/testlab/NodeWiseCsrBiliAssembly.cc:157-297).  Overwrites
+ * values_d (no prior zeroing needed).  Uses scratch from the context. */
+afem_status afem_assemble_poisson_p1(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
+                                     const double* cell_coeff_d, double* values_d);
+
+/* Linear elasticity P1 tetrahedra, 3x3 blocks (b = 3):
+ * values_d[nnzb * 9] in the given layout.  Replaces assembleBilinearAtomicFree
+ * with computeElementVectorTetra4Gpu (modules/elasticity/ElementMatrix.h:216-301,
+ * modules/elasticity/FemModule.cc:257-271).  Uses scratch from the context. */
+afem_status afem_assemble_elasticity_tet4(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
+                                          double lambda, double mu, int layout, double* values_d);
+
+/* The two stages of the assemblies above, for callers that keep the element
+ * matrices themselves (and to time the stages separately).  Stage 1 writes
+ * the element matrices once per cell as planes ke_d[entry * nb_cell + cell]:
+ * Poisson: the packed upper triangle of the (dim+1)^2 matrix (6 planes for
+ * triangles, 10 for tetrahedra); elasticity: 78 planes (6 off-diagonal 3x3
+ * blocks then 4 packed diagonal blocks).  Stage 2 sums, per row, the element
+ * rows of the incident cells in increasing cell order (no atomics). */
+afem_status afem_element_matrices_poisson_p1(afem_context ctx, const afem_mesh_view* mesh,
+                                             const double* cell_coeff_d, double* ke_d);
+afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
+                                   const double* ke_d, double* values_d);
+afem_status afem_element_matrices_elasticity_tet4(afem_context ctx, const afem_mesh_view* mesh, double lambda,
+                                                  double mu, double* ke_d);
+afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
+                                        const double* ke_d, int layout, double* values_d);
+
+/* Expand block-row pointers / block columns of a b x b BSR to scalar CSR
+ * row_ptr_d[nb_node*b+1] and cols_d[nnzb*b*b] (the per-row value layout is
+ * already CSR-ordered).  Replaces the host loops of BSRMatrix::toCsr
+ * (femutils/BSRFormat.cc:110-172). */
+afem_status afem_bsr_to_csr_structure(afem_context ctx, int nb_block_row, int b, const int32_t* brow_ptr_d,
+                                      const int32_t* bcols_d, int32_t* row_ptr_d, int32_t* cols_d);
+
+/* rhs_d[node*nb_dof] = sum_cells qdot * measure / (dim+1), other entries
+ * untouched.  Replaces applyConstantSourceToRhsBase
+ * (femutils/ArcaneFemFunctionsGpu.h:676-708). */
+afem_status afem_rhs_constant_source(afem_context ctx, const afem_mesh_view* mesh, double qdot, int nb_dof,
+                                     double* rhs_d);
+
+/* Body force on tetrahedra, rhs_d[3*node + k] += sum_cells f[k] * vol / 4,
+ * node-wise (no atomics).  Replaces the host loop of
+ * FemModuleElasticity::_applyBodyForce (modules/elasticity/BodyForce.h:148-160). */
+afem_status afem_rhs_body_force_tet4(afem_context ctx, const afem_mesh_view* mesh, double fx, double fy, double fz,
+                                     double* rhs_d);
+
+/* ---------------------------------------------------------------------- */
+/* Linear system: mirrors CsrDoFLinearSystemImpl
+ * (femutils/internal/CsrDoFLinearSystemImpl.h:36-113) behind
+ * IDoFLinearSystemImpl (femutils/internal/IDoFLinearSystemImpl.h:37-70).
+ * It owns the DoF variables (rhs, solution, forced info/value, elimination
+ * info/value) and keeps a NON-owning view of the CSR matrix set by
+ * afem_ls_set_csr_values, which must stay valid until afem_ls_solve
+ * (femutils/DoFLinearSystem.h:318-328). */
+typedef struct afem_linear_system_s* afem_linear_system;
+
+enum { AFEM_ELIMINATE_NONE = 0, AFEM_ELIMINATE_ROW = 1, AFEM_ELIMINATE_ROW_COLUMN = 2 }; /* FemUtilsGlobal.h:51-62 */
+
+/* IDoFLinearSystemFactory::createInstance (femutils/IDoFLinearSystemFactory.h:42-43). */
+afem_status afem_ls_create(afem_context ctx, int nb_dof, afem_linear_system* ls);
+afem_status afem_ls_destroy(afem_linear_system ls);
+/* setCSRValues (CsrDoFLinearSystemImpl.h:98-101). */
+afem_status afem_ls_set_csr_values(afem_linear_system ls, const int32_t* row_ptr_d, const int32_t* cols_d,
+                                   double* values_d, int64_t nnz);
+/* hasSetCSRValues / getCSRValues. */
+afem_status afem_ls_get_csr_values(afem_linear_system ls, const int32_t** row_ptr_d, const int32_t** cols_d,
+                                   double** values_d, int64_t* nnz);
+/* Device pointers to the DoF variables: rhsVariable, solutionVariable,
+ * getForcedInfo (uint8 0/1), getForcedValue, getEliminationInfo,
+ * getEliminationValue (DoFLinearSystemImplBase.cc:27-36). */
+afem_status afem_ls_dof_variables(afem_linear_system ls, double** rhs_d, double** solution_d, uint8_t** forced_info_d,
+                                  double** forced_value_d, uint8_t** elimination_info_d,
+                                  double** elimination_value_d);
+/* clearValues (DoFLinearSystemImplBase.cc:44-50, CsrDoFLinearSystemImpl.h:90-95). */
+afem_status afem_ls_clear_values(afem_linear_system ls);
+/* matrixAddValue / matrixSetValue (CsrDoFLinearSystemImpl.h:55-65): one entry,
+ * linear search in the row; AFEM_ERR_NOT_FOUND if the column is not stored. */
+afem_status afem_ls_matrix_add_value(afem_linear_system ls, int32_t row, int32_t col, double value);
+afem_status afem_ls_matrix_set_value(afem_linear_system ls, int32_t row, int32_t col, double value);
+/* eliminateRow / eliminateRowColumn throw NotImplementedException on the CSR
+ * impl (CsrDoFLinearSystemImpl.h:67-75): AFEM_ERR_NOT_IMPLEMENTED here too. */
+afem_status afem_ls_eliminate_row(afem_linear_system ls, int32_t row, double value);
+afem_status afem_ls_eliminate_row_column(afem_linear_system ls, int32_t row, double value);
+
+/* Dirichlet flagging on a node group (nodes_d[nb_sel]):
+ * applyDirichletToNodeGroupViaPenalty (ArcaneFemFunctionsGpu.cc:54-78):
+ *   forced_info = 1, forced_value = penalty, rhs = penalty * value;
+ * applyDirichletToNodeGroupViaRowOrRowColumnElimination (ArcaneFemFunctionsGpu.cc:83-105):
+ *   elimination_info = type, elimination_value = value. */
+afem_status afem_dirichlet_penalty(afem_linear_system ls, int nb_sel, const int32_t* nodes_d, int nb_dof_per_node,
+                                   int dof_index, double value, double penalty);
+afem_status afem_dirichlet_elimination(afem_linear_system ls, int elimination_type, int nb_sel,
+                                       const int32_t* nodes_d, int nb_dof_per_node, int dof_index, double value);
+
+/* applyMatrixTransformation (CsrDoFLinearSystemImpl.cc:235-242): keeps the
+ * pre-elimination values needed for row-column elimination, applies row
+ * elimination, row-column elimination (with the reference's column_index > 0
+ * test, :111) and forced (penalty) diagonals.  Fully on the device. */
+afem_status afem_ls_apply_matrix_transformation(afem_linear_system ls);
+/* applyRHSTransformation (CsrDoFLinearSystemImpl.cc:247-253 and
+ * DoFLinearSystemImplBase.cc:55-88): rhs_j -= A_ij g_i for row-column
+ * eliminated i in increasing i (the host std::map order of the reference),
+ * then rhs_i = g_i on eliminated rows.  Fully on the device. */
+afem_status afem_ls_apply_rhs_transformation(afem_linear_system ls);
+
+/* ---------------------------------------------------------------------- */
+/* Krylov solve. */
+enum { AFEM_PRECOND_NONE = 0, AFEM_PRECOND_JACOBI = 1, AFEM_PRECOND_LEARNED = 2 };
+enum { AFEM_PRECISION_FP64 = 0, AFEM_PRECISION_MIXED = 1 };
+
+typedef struct {
+  double rtol;            /* stop when ||b - A x|| <= max(rtol ||b||, atol) (two-norm, HypreDoFLinearSystem.cc:596-603) */
+  double atol;
+  int max_iter;           /* default 1000 when 0 (HypreDoFLinearSystem.cc:182) */
+  int precond;            /* AFEM_PRECOND_* */
+  int precision;          /* AFEM_PRECISION_*; MIXED = FP32 inner CG inside FP64 iterative refinement */
+  int skip_forced_rows;   /* leave penalty (forced) rows out of both norms of the stop test */
+  double inner_rtol;      /* MIXED: relative tolerance of each FP32 inner solve (default 1e-4) */
+  int check_every;        /* iterations between host convergence checks (default 16) */
+} afem_solver_options;
+
+typedef struct {
+  int iterations;         /* total (inner) CG iterations */
+  int refinements;        /* outer FP64 refinement steps (MIXED) */
+  int status;             /* afem_status of the solve */
+  double relres;          /* true FP64 ||b - A x|| / ||b|| recomputed at the end */
+  double solve_ms;        /* device time of the solve */
+} afem_solve_info;
+
+void afem_solver_options_default(afem_solver_options* opt);
+
+/* x_d (initial guess in, solution out) for the CSR system (row_ptr, cols, values).
+ * Replaces IDoFLinearSystemImpl::solve of the HYPRE / PETSc / Aleph / Arcane
+ * MatVec backends (HypreDoFLinearSystem.cc:265-858, DoFLinearSystem.cc:146-159).
+ * forced_info_d (nullable) marks rows left out of the stop test when
+ * opt->skip_forced_rows.  Synchronous (returns after convergence). */
+afem_status afem_cg_solve_csr(afem_context ctx, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
+                              const double* values_d, const double* b_d, double* x_d, const uint8_t* forced_info_d,
+                              const afem_solver_options* opt, afem_solve_info* info);
+
+/* IDoFLinearSystemImpl::solve: solves the linear system's matrix view for
+ * its rhs into its solution variable (applyLinearSystemTransformationAndSolve
+ * calls the two transformations first, femutils/DoFLinearSystem.cc:487-493). */
+afem_status afem_ls_solve(afem_linear_system ls, const afem_solver_options* opt, afem_solve_info* info);
+
+/* y = A x, FP64 CSR. */
+afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
+                          const double* values_d, const double* x_d, double* y_d);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFEM_GB300_H */

@@ -1,0 +1,325 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances:
+  * structure (node->cell adjacency, row pointers, columns): bit-exact;
+  * matrix values: |a - b| <= 1e-12 * max(|b|, 1e-3 * max|row of b|) per
+    entry (the element math is regrouped for FP64 throughput, so the last
+    bits may differ; the guard covers entries that cancel to ~0);
+  * Dirichlet transformations on equal inputs: bit-exact;
+  * solutions: true FP64 relative residual below the requested tolerance and
+    the reference check files within their own tolerance.
+"""
+import numpy as np
+import pytest
+import torch
+
+import golden_cases as G
+from arcanefem_gb300 import fem, meshgen
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-12
+
+
+def rel_err_rows(got, ref, rp, b=1):
+    """Max over entries of |got - ref| / max(|ref|, 1e-3 * max|row|)."""
+    ref = np.asarray(ref)
+    got = np.asarray(got)
+    row_of = np.repeat(np.arange(rp.size - 1), np.diff(rp) * b * b)
+    rowmax = np.zeros(rp.size - 1)
+    np.maximum.at(rowmax, row_of, np.abs(ref))
+    denom = np.maximum(np.abs(ref), 1e-3 * rowmax[row_of])
+    return float(np.max(np.abs(got - ref) / denom))
+
+
+def build_format(ctx, mesh, nb_dof=1, use_csr=True, col_order=fem.COLS_ASCENDING):
+    dm = fem.Mesh.from_host(mesh.dim, mesh.coords, mesh.cells)
+    f = fem.BSRFormat(ctx, dm)
+    f.initialize(nb_dof, use_csr, col_order)
+    f.compute_sparsity()
+    return f
+
+
+MESHES = {
+    "tri_4": lambda: meshgen.unit_square_tri(4, seed=1),
+    "tri_33": lambda: meshgen.unit_square_tri(33, seed=2),
+    "tet_3": lambda: meshgen.unit_cube_tet(3, seed=3),
+    "tet_9": lambda: meshgen.unit_cube_tet(9, seed=4),
+}
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+def test_node_cell_adjacency_bit_exact(cuda_ctx, name):
+    m = MESHES[name]()
+    f = build_format(cuda_ctx, m)
+    ptr, nc, loc = O.node_cell(m.nb_node, m.cells)
+    assert np.array_equal(f.nc_ptr.cpu().numpy(), ptr)
+    assert np.array_equal(f.nc_cell.cpu().numpy(), nc)
+    assert np.array_equal(f.nc_local.cpu().numpy(), loc)
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+@pytest.mark.parametrize("self_last", [False, True])
+def test_sparsity_bit_exact(cuda_ctx, name, self_last):
+    m = MESHES[name]()
+    order = fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING
+    f = build_format(cuda_ctx, m, col_order=order)
+    rp, cols = O.sparsity(m.nb_node, m.cells, self_last=self_last)
+    assert np.array_equal(f.row_ptr.cpu().numpy(), rp)
+    assert np.array_equal(f.cols.cpu().numpy(), cols)
+    assert f.nnzb == meshgen.nnz_formula(m)
+    # slot map: column at the slot is the cell node
+    slot = f.nc_slot.cpu().numpy().reshape(-1, m.npc)
+    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    node_of = np.repeat(np.arange(m.nb_node), np.diff(ptr))
+    got_cols = cols[rp[node_of][:, None] + slot]
+    assert np.array_equal(got_cols, m.cells[nc])
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+@pytest.mark.parametrize("self_last", [False, True])
+def test_poisson_values_match_oracle(cuda_ctx, name, self_last):
+    m = MESHES[name]()
+    f = build_format(cuda_ctx, m, col_order=fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING)
+    f.assemble_poisson()
+    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    rp, cols = O.sparsity(m.nb_node, m.cells, self_last=self_last)
+    kind = O.POISSON_TRI3 if m.dim == 2 else O.POISSON_TET4
+    ref = O.assemble(kind, m.coords, m.cells, ptr, nc, rp, cols)
+    got = f.values.cpu().numpy()
+    assert rel_err_rows(got, ref, rp) < REL
+    # the testlab formulation (B matrix, signed measure) agrees too
+    kind_t = O.TESTLAB_TRI3 if m.dim == 2 else O.TESTLAB_TET4
+    ref_t = O.assemble(kind_t, m.coords, m.cells, ptr, nc, rp, cols)
+    assert rel_err_rows(got, ref_t, rp) < REL
+
+
+def test_poisson_variable_coefficient(cuda_ctx):
+    m = meshgen.unit_square_tri(20, seed=9)
+    k = np.exp(np.random.default_rng(0).standard_normal(m.nb_cell))
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson(torch.as_tensor(k, device="cuda"))
+    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    rp, cols = O.sparsity(m.nb_node, m.cells)
+    ref = O.assemble(O.POISSON_TRI3, m.coords, m.cells, ptr, nc, rp, cols, cell_coeff=k)
+    assert rel_err_rows(f.values.cpu().numpy(), ref, rp) < REL
+
+
+@pytest.mark.parametrize("use_csr", [True, False])
+def test_elasticity_values_match_oracle(cuda_ctx, use_csr):
+    m = meshgen.unit_cube_tet(5, seed=6)
+    lam, mu = fem.lame(21e5, 0.28)
+    f = build_format(cuda_ctx, m, nb_dof=3, use_csr=use_csr)
+    f.assemble_elasticity(lam, mu)
+    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    rp, cols = O.sparsity(m.nb_node, m.cells)
+    ref = O.assemble(O.ELASTICITY_TET4, m.coords, m.cells, ptr, nc, rp, cols, per_block_layout=not use_csr,
+                     lam=lam, mu=mu)
+    got = f.values.cpu().numpy()
+    if use_csr:
+        srp, _ = G.scalar_csr_from_block(rp, cols, 3)
+        assert rel_err_rows(got, ref, srp) < REL
+    else:
+        assert rel_err_rows(got, ref, rp, b=3) < REL
+
+
+def test_bsr_to_csr_structure(cuda_ctx):
+    m = meshgen.unit_cube_tet(3, seed=1)
+    f = build_format(cuda_ctx, m, nb_dof=3)
+    srp, scols, _ = f.to_csr()
+    rp, cols = O.sparsity(m.nb_node, m.cells)
+    erp, ecols = G.scalar_csr_from_block(rp, cols, 3)
+    assert np.array_equal(srp.cpu().numpy(), erp) and np.array_equal(scols.cpu().numpy(), ecols)
+
+
+def test_assembly_is_deterministic(cuda_ctx):
+    m = meshgen.unit_cube_tet(8, seed=11)
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson()
+    a = f.values.clone()
+    f.reset_matrix_values()
+    f.assemble_poisson()
+    assert torch.equal(a, f.values)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_rhs_constant_source(cuda_ctx, dim):
+    m = meshgen.unit_square_tri(12, seed=1) if dim == 2 else meshgen.unit_cube_tet(4, seed=1)
+    f = build_format(cuda_ctx, m)
+    rhs = torch.zeros(m.nb_node, dtype=torch.float64, device="cuda")
+    f.rhs_constant_source(-5.5, rhs)
+    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    ref = O.rhs_constant_source(dim, m.coords, m.cells, ptr, nc, -5.5)
+    np.testing.assert_allclose(rhs.cpu().numpy(), ref, rtol=1e-13, atol=0)
+
+
+def test_rhs_body_force(cuda_ctx):
+    m = meshgen.unit_cube_tet(4, seed=2)
+    f = build_format(cuda_ctx, m, nb_dof=3)
+    rhs = torch.zeros(3 * m.nb_node, dtype=torch.float64, device="cuda")
+    f.rhs_body_force([0.0, 0.5, -1.0], rhs)
+    ref = O.rhs_body_force_tet4(m.coords, m.cells, [0.0, 0.5, -1.0])
+    np.testing.assert_allclose(rhs.cpu().numpy(), ref, rtol=1e-13, atol=1e-300)
+
+
+def test_dirichlet_transformations_bit_exact(cuda_ctx):
+    m = meshgen.unit_square_tri(6, seed=3)
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson()
+    rp, cols, vals = (t.cpu().numpy() for t in f.to_csr())
+    n = m.nb_node
+    rng = np.random.default_rng(5)
+    rhs0 = rng.standard_normal(n)
+    ls = fem.DoFLinearSystem(cuda_ctx, n)
+    f.to_linear_system(ls)
+    ls.rhs_variable().copy_(torch.as_tensor(rhs0))
+    dev = lambda a: torch.as_tensor(np.asarray(a, np.int32), device="cuda")  # noqa: E731
+    ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW_COLUMN, dev([0, 5, 9]), 1, 0, 0.25)
+    ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW, dev([14, 15]), 1, 0, -1.5)
+    ls.apply_dirichlet_penalty(dev([30, 31]), 1, 0, 2.0, 1e30)
+    ls.apply_matrix_transformation()
+    ls.apply_rhs_transformation()
+    # oracle on the same inputs
+    fi, fv = np.zeros(n, np.uint8), np.zeros(n)
+    ei, ev = np.zeros(n, np.uint8), np.zeros(n)
+    rr = rhs0.copy()
+    O.dirichlet_elimination(np.array([0, 5, 9]), 1, 0, 0.25, 2, ei, ev)
+    O.dirichlet_elimination(np.array([14, 15]), 1, 0, -1.5, 1, ei, ev)
+    O.dirichlet_penalty(np.array([30, 31]), 1, 0, 2.0, 1e30, fi, fv, rr)
+    vv = vals.copy()
+    O.apply_transformations(rp, cols, vv, rr, fi, fv, ei, ev)
+    assert np.array_equal(f.values.cpu().numpy(), vv)
+    assert np.array_equal(ls.rhs_variable().cpu().numpy(), rr)
+    assert np.array_equal(ls.get_forced_info().cpu().numpy(), fi)
+    assert np.array_equal(ls.get_elimination_info().cpu().numpy(), ei)
+
+
+def test_linear_system_entry_api(cuda_ctx):
+    m = meshgen.unit_square_tri(3, seed=0)
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson()
+    ls = fem.DoFLinearSystem(cuda_ctx, m.nb_node)
+    f.to_linear_system(ls)
+    before = f.values.clone()
+    ls.matrix_add_value(0, 0, 1.5)
+    ls.matrix_set_value(1, 1, 7.0)
+    rp = f.row_ptr.cpu().numpy()
+    cols = f.cols.cpu().numpy()
+    k00 = rp[0] + list(cols[rp[0]:rp[1]]).index(0)
+    k11 = rp[1] + list(cols[rp[1]:rp[2]]).index(1)
+    assert f.values[k00].item() == before[k00].item() + 1.5 and f.values[k11].item() == 7.0
+    with pytest.raises(fem.AfemError) as e:
+        ls.matrix_add_value(0, m.nb_node - 1, 1.0)     # not in the sparsity
+    assert e.value.status == 9
+    with pytest.raises(fem.AfemError) as e:
+        ls.eliminate_row(0, 1.0)
+    assert e.value.status == 8
+
+
+@pytest.mark.parametrize("precision", [fem.PRECISION_FP64, fem.PRECISION_MIXED])
+def test_cg_solution_matches_oracle(cuda_ctx, precision):
+    m = meshgen.unit_cube_tet(10, seed=4)
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson()
+    ls = fem.DoFLinearSystem(cuda_ctx, m.nb_node)
+    f.to_linear_system(ls)
+    f.rhs_constant_source(1.0, ls.rhs_variable())
+    nodes = torch.as_tensor(m.groups["x_faces"], device="cuda")
+    ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW_COLUMN, nodes, 1, 0, 0.0)
+    info = ls.apply_linear_system_transformation_and_solve(
+        fem.solver_options(rtol=1e-10, max_iter=5000, precision=precision))
+    assert info.status == 0 and info.relres < 1e-10
+    # oracle solution of the same transformed system
+    rp, cols, vals = (t.cpu().numpy() for t in f.to_csr())
+    b = ls.rhs_variable().cpu().numpy()
+    x_ref, _, _ = O.pcg_jacobi(rp, cols, vals, b, rtol=1e-13, max_iter=20000)
+    x = ls.solution_variable().cpu().numpy()
+    assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-8
+    if precision == fem.PRECISION_MIXED:
+        assert info.refinements >= 1
+
+
+def test_cg_penalty_with_skipped_forced_rows(cuda_ctx):
+    m = meshgen.unit_square_tri(24, seed=2)
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson()
+    ls = fem.DoFLinearSystem(cuda_ctx, m.nb_node)
+    f.to_linear_system(ls)
+    f.rhs_constant_source(-1.0, ls.rhs_variable())
+    ls.apply_dirichlet_penalty(torch.as_tensor(m.groups["boundary"], device="cuda"), 1, 0, 0.5, 1e30)
+    info = ls.apply_linear_system_transformation_and_solve(
+        fem.solver_options(rtol=1e-12, max_iter=5000, skip_forced_rows=True))
+    assert info.status == 0 and info.relres < 1e-12
+    x = ls.solution_variable().cpu().numpy()
+    assert np.allclose(x[m.groups["boundary"]], 0.5, rtol=0, atol=1e-12)
+
+
+def test_spmv_matches_oracle(cuda_ctx):
+    m = meshgen.unit_cube_tet(6, seed=8)
+    f = build_format(cuda_ctx, m, nb_dof=3)
+    f.assemble_elasticity(*fem.lame(1.0, 0.3))
+    rp, cols, vals = f.to_csr()
+    x = torch.randn(3 * m.nb_node, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    fem.spmv_csr(cuda_ctx, rp, cols, vals, x, y)
+    ref = O.spmv(rp.cpu().numpy(), cols.cpu().numpy(), vals.cpu().numpy(), x.cpu().numpy())
+    np.testing.assert_allclose(y.cpu().numpy(), ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("name", list(G.CASES))
+def test_golden_case_on_gpu(cuda_ctx, name):
+    """The reference test cases end to end on the GPU path, compared with the
+    reference's own check files."""
+    spec = G.CASES[name]
+    d = G.load(name)
+    dim = 2 if d["cells"].shape[1] == 3 else 3
+    mesh = meshgen.Mesh(dim, d["coords"], d["cells"])
+    if spec["kind"] == "elasticity":
+        f = build_format(cuda_ctx, mesh, nb_dof=3)
+        f.assemble_elasticity(*fem.lame(spec["E"], spec["nu"]))
+        ls = fem.DoFLinearSystem(cuda_ctx, 3 * mesh.nb_node)
+        f.to_linear_system(ls)
+        f.rhs_body_force(spec["body_force"], ls.rhs_variable())
+        for g, v3 in spec["dirichlet3"]:
+            for comp, v in enumerate(v3):
+                if v is not None:
+                    ls.apply_dirichlet_penalty(torch.as_tensor(d["group__" + g], device="cuda"), 3, comp, v,
+                                               spec["penalty"])
+    else:
+        f = build_format(cuda_ctx, mesh)
+        f.assemble_poisson()
+        ls = fem.DoFLinearSystem(cuda_ctx, mesh.nb_node)
+        f.to_linear_system(ls)
+        f.rhs_constant_source(spec["f"], ls.rhs_variable())
+        for g, v in spec["dirichlet"]:
+            ls.apply_dirichlet_penalty(torch.as_tensor(d["group__" + g], device="cuda"), 1, 0, v, spec["penalty"])
+    info = ls.apply_linear_system_transformation_and_solve(
+        fem.solver_options(rtol=1e-12, max_iter=20000, skip_forced_rows=True))
+    err = G.compare(name, ls.solution_variable().cpu().numpy(), d)
+    assert err < spec["eps"], f"{name}: {err:.3e} (iters {info.iterations}, relres {info.relres:.2e})"
+
+
+def test_bad_mesh_is_reported(cuda_ctx):
+    m = meshgen.unit_square_tri(2)
+    cells = m.cells.copy()
+    cells[0, 0] = m.nb_node + 5            # out of range: caught by the kernel's own bounds check
+    dm = fem.Mesh.from_host(2, m.coords, cells)
+    f = fem.BSRFormat(cuda_ctx, dm)
+    with pytest.raises(fem.AfemError) as e:
+        f.initialize(1)
+    assert e.value.status == 7
+
+
+def test_single_cell_meshes(cuda_ctx):
+    for dim, coords, cells in ((2, [[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 2]]),
+                               (3, [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], [[0, 1, 2, 3]])):
+        m = meshgen.Mesh(dim, np.array(coords, float), np.array(cells, np.int32))
+        f = build_format(cuda_ctx, m)
+        f.assemble_poisson()
+        n = dim + 1
+        assert f.nnzb == n * n
+        K = f.values.cpu().numpy().reshape(n, n)
+        ref = np.array([O.elem_vec(O.POISSON_TRI3 if dim == 2 else O.POISSON_TET4, m.coords, cells[0], i)
+                        for i in range(n)])
+        np.testing.assert_allclose(K, ref, rtol=1e-14, atol=1e-15)
