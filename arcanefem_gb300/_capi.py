@@ -31,7 +31,7 @@ class AfemError(RuntimeError):
 class MeshView(C.Structure):
     _fields_ = [("dim", C.c_int), ("nb_node", C.c_int), ("nb_cell", C.c_int), ("coords_d", C.c_void_p),
                 ("cell_nodes_d", C.c_void_p), ("nc_ptr_d", C.c_void_p), ("nc_cell_d", C.c_void_p),
-                ("nc_local_d", C.c_void_p), ("nc_slot_d", C.c_void_p)]
+                ("nc_local_d", C.c_void_p), ("nc_slot_d", C.c_void_p), ("nc_inverse_d", C.c_void_p)]
 
 
 class SolverOptions(C.Structure):
@@ -59,7 +59,7 @@ SIGNATURES = {
     "afem_context_synchronize": (C.c_int, [_P]),
     "afem_context_launch_count": (C.c_int, [_P, _I64P]),
     "afem_device_fp64_fma_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
-    "afem_node_cell_build": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P]),
+    "afem_node_cell_build": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P]),
     "afem_sparsity_rows": (C.c_int, [_P, C.c_int, C.c_int, _P, _P, _P, _P, _I64P]),
     "afem_sparsity_cols": (C.c_int, [_P, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P, _P]),
     "afem_assemble_poisson_p1": (C.c_int, [_P, C.POINTER(MeshView), _P, _P, _P]),

@@ -58,9 +58,30 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_examples()
     if verbose:
         print(f"built {LIB}")
     return LIB
+
+
+EXAMPLES = os.path.join(PKG, "examples")
+
+
+def build_examples() -> None:
+    """C++ host programs over include/afem_gb300.hpp, linked to the library."""
+    cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    for src in sorted(glob.glob(os.path.join(EXAMPLES, "*.cpp"))):
+        exe = os.path.join(LIBDIR, os.path.basename(src)[:-4])
+        deps = [src, LIB, os.path.join(ROOT, "include", "afem_gb300.hpp")]
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
+            continue
+        cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I",
+               os.path.join(cuda_home, "include"), src, "-o", exe, "-L", LIBDIR, "-lafem_gb300",
+               "-L", os.path.join(cuda_home, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+               "-Wl,-rpath," + os.path.join(cuda_home, "lib64")]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

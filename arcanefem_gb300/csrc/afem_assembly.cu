@@ -5,11 +5,12 @@
 // count, not by bytes.  The reference recomputes each element once per
 // incident node (femutils/BSRFormat.h:406-537: 3x for triangles, 4x for
 // tetrahedra); here every element matrix is computed ONCE, in a cell-wise
-// kernel with a minimal-operation formulation, and stored as planes
-// ke[entry][cell] (structure of arrays, coalesced).  A node-wise kernel then
-// sums, for each row, the element rows of its incident cells, in increasing
-// cell order, straight into the slots given by the slot map -- no atomics,
-// no column search, deterministic.
+// kernel with a minimal-operation formulation.  Its rows are stored in
+// incidence order: row i of cell c goes to the slot of incidence
+// p = nc_inverse[c][i] of the node -> cell lists, so that a node-wise kernel
+// then STREAMS, for each row, the contiguous element rows of its incident
+// cells (in increasing cell order) and adds them into the slots given by the
+// slot map -- no atomics, no column search, deterministic.
 //
 // Element formulation (same quantities as modules/poisson/ElementMatrix.h:41-118
 // and femutils/ArcaneFemFunctionsGpu.h:76-128,241-281,414-535, regrouped):
@@ -44,19 +45,12 @@ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
 }
 __device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
-// packed upper-triangle index of (i, j) in an n x n symmetric matrix
-__device__ __forceinline__ int sym_index(int i, int j, int n) {
-  int lo = min(i, j), hi = max(i, j);
-  return lo * (2 * n - lo + 1) / 2 + (hi - lo);
-}
-
 // Tetrahedron geometry: cofactor vectors c[0..3] and s = 1 / (6 |det|).
 __device__ __forceinline__ void tet_cofactors(const double* __restrict__ xyz, const int32_t* __restrict__ cn,
                                               int64_t c, d3 cf[4], double* s, double* vol) {
-  const int32_t* q = cn + 4 * c;
-  int32_t n0 = __ldg(q), n1 = __ldg(q + 1), n2 = __ldg(q + 2), n3 = __ldg(q + 3);
-  d3 p0 = ld_node(xyz, n0);
-  d3 v1 = sub(ld_node(xyz, n1), p0), v2 = sub(ld_node(xyz, n2), p0), v3 = sub(ld_node(xyz, n3), p0);
+  const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
+  d3 p0 = ld_node(xyz, q.x);
+  d3 v1 = sub(ld_node(xyz, q.y), p0), v2 = sub(ld_node(xyz, q.z), p0), v3 = sub(ld_node(xyz, q.w), p0);
   cf[1] = cross(v2, v3);
   cf[2] = cross(v3, v1);
   cf[3] = cross(v1, v2);
@@ -66,45 +60,50 @@ __device__ __forceinline__ void tet_cofactors(const double* __restrict__ xyz, co
   *s = 1.0 / (6.0 * det);
 }
 
-// ---------------------------------------------------------------------------
-// Element kernels.
+// 32-byte row stores / loads as two 16-byte vector accesses (rows are 32-byte aligned)
+__device__ __forceinline__ void st4(double* p, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+  reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
+__device__ __forceinline__ void ld4(const double* __restrict__ p, double v[4]) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
 
-// Poisson tetrahedron: 10 planes (packed upper triangle of the 4x4 matrix).
+// ---------------------------------------------------------------------------
+// Element kernels (one thread per cell).
+
+// Poisson tetrahedron: 4 rows of 4 values, row i at er[inv[c][i] * 4].
 __global__ void __launch_bounds__(256) k_elem_poisson_tet(int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
-                                                          const double* __restrict__ coeff, double* __restrict__ ke) {
-  const int64_t C = nb_cell;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+                                                          const int32_t* __restrict__ inv,
+                                                          const double* __restrict__ coeff, double* __restrict__ er) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
     d3 cf[4];
     double s, vol;
     tet_cofactors(xyz, cn, c, cf, &s, &vol);
     if (coeff) s *= __ldg(coeff + c);
-    double k01 = s * dot(cf[0], cf[1]), k02 = s * dot(cf[0], cf[2]), k03 = s * dot(cf[0], cf[3]);
-    double k12 = s * dot(cf[1], cf[2]), k13 = s * dot(cf[1], cf[3]), k23 = s * dot(cf[2], cf[3]);
-    ke[0 * C + c] = -(k01 + k02 + k03);
-    ke[1 * C + c] = k01;
-    ke[2 * C + c] = k02;
-    ke[3 * C + c] = k03;
-    ke[4 * C + c] = -(k01 + k12 + k13);
-    ke[5 * C + c] = k12;
-    ke[6 * C + c] = k13;
-    ke[7 * C + c] = -(k02 + k12 + k23);
-    ke[8 * C + c] = k23;
-    ke[9 * C + c] = -(k03 + k13 + k23);
+    const double k01 = s * dot(cf[0], cf[1]), k02 = s * dot(cf[0], cf[2]), k03 = s * dot(cf[0], cf[3]);
+    const double k12 = s * dot(cf[1], cf[2]), k13 = s * dot(cf[1], cf[3]), k23 = s * dot(cf[2], cf[3]);
+    const int4 p = __ldg(reinterpret_cast<const int4*>(inv) + c);
+    st4(er + 4 * (int64_t)p.x, -(k01 + k02 + k03), k01, k02, k03);
+    st4(er + 4 * (int64_t)p.y, k01, -(k01 + k12 + k13), k12, k13);
+    st4(er + 4 * (int64_t)p.z, k02, k12, -(k02 + k12 + k23), k23);
+    st4(er + 4 * (int64_t)p.w, k03, k13, k23, -(k03 + k13 + k23));
   }
 }
 
-// Poisson triangle: 6 planes.
+// Poisson triangle: 3 rows of 3 values, row i at er[inv[c][i] * 3].
 __global__ void __launch_bounds__(256) k_elem_poisson_tri(int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
-                                                          const double* __restrict__ coeff, double* __restrict__ ke) {
-  const int64_t C = nb_cell;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+                                                          const int32_t* __restrict__ inv,
+                                                          const double* __restrict__ coeff, double* __restrict__ er) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
     const int32_t* q = cn + 3 * c;
-    int32_t n0 = __ldg(q), n1 = __ldg(q + 1), n2 = __ldg(q + 2);
-    const double* a0 = xyz + 3 * (int64_t)n0;
-    const double* a1 = xyz + 3 * (int64_t)n1;
-    const double* a2 = xyz + 3 * (int64_t)n2;
+    const double* a0 = xyz + 3 * (int64_t)__ldg(q);
+    const double* a1 = xyz + 3 * (int64_t)__ldg(q + 1);
+    const double* a2 = xyz + 3 * (int64_t)__ldg(q + 2);
     double x0 = __ldg(a0), y0 = __ldg(a0 + 1);
     double v1x = __ldg(a1) - x0, v1y = __ldg(a1 + 1) - y0;
     double v2x = __ldg(a2) - x0, v2y = __ldg(a2 + 1) - y0;
@@ -113,190 +112,234 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tri(int nb_cell, const dou
     if (coeff) s *= __ldg(coeff + c);
     // c1 = (v2y, -v2x), c2 = (-v1y, v1x), c0 = -(c1 + c2)
     double c0x = v1y - v2y, c0y = v2x - v1x;
-    double k01 = s * (c0x * v2y - c0y * v2x);
-    double k02 = s * (c0y * v1x - c0x * v1y);
-    double k12 = s * (-(v2y * v1y) - v2x * v1x);
-    ke[0 * C + c] = -(k01 + k02);
-    ke[1 * C + c] = k01;
-    ke[2 * C + c] = k02;
-    ke[3 * C + c] = -(k01 + k12);
-    ke[4 * C + c] = k12;
-    ke[5 * C + c] = -(k02 + k12);
+    const double k01 = s * (c0x * v2y - c0y * v2x);
+    const double k02 = s * (c0y * v1x - c0x * v1y);
+    const double k12 = s * (-(v2y * v1y) - v2x * v1x);
+    const int32_t* ip = inv + 3 * c;
+    double* r0 = er + 3 * (int64_t)__ldg(ip);
+    double* r1 = er + 3 * (int64_t)__ldg(ip + 1);
+    double* r2 = er + 3 * (int64_t)__ldg(ip + 2);
+    r0[0] = -(k01 + k02); r0[1] = k01; r0[2] = k02;
+    r1[0] = k01; r1[1] = -(k01 + k12); r1[2] = k12;
+    r2[0] = k02; r2[1] = k12; r2[2] = -(k02 + k12);
   }
 }
 
-// Elasticity tetrahedron: 78 planes = 6 off-diagonal 3x3 blocks (n < m, 9
-// each, row-major) followed by 4 diagonal blocks (6 each, packed upper).
-// Block (n, m) rows a / columns b:
+// Elasticity tetrahedron: for each local node n, its 3x12 row block
+// er[inv[c][n] * 36 + a * 12 + 3 m + b].  Block (n, m) rows a / columns b:
 //   K_ab = V [lambda dN_n/dx_a dN_m/dx_b + mu dN_n/dx_b dN_m/dx_a
 //             + mu delta_ab grad N_n . grad N_m]
 // which is modules/elasticity/ElementMatrix.h:216-301 (normal strain +
 // compressibility + shear) regrouped; diagonal blocks by zero block-row sum.
-__global__ void __launch_bounds__(128) k_elem_elasticity_tet(int nb_cell, const double* __restrict__ xyz,
-                                                             const int32_t* __restrict__ cn, double lambda, double mu,
-                                                             double* __restrict__ ke) {
-  const int64_t C = nb_cell;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
-    d3 cf[4];
-    double s, vol;
-    tet_cofactors(xyz, cn, c, cf, &s, &vol);
-    const double ls = lambda * s, ms = mu * s, lms = (lambda + mu) * s;
-    double dg[4][6];
-#pragma unroll
-    for (int n = 0; n < 4; ++n)
-#pragma unroll
-      for (int k = 0; k < 6; ++k) dg[n][k] = 0.0;
-    int pair = 0;
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-#pragma unroll
-      for (int m = n + 1; m < 4; ++m) {
-        const double cn_[3] = {cf[n].x, cf[n].y, cf[n].z};
-        const double cm_[3] = {cf[m].x, cf[m].y, cf[m].z};
-        double P[3][3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) P[a][b] = cn_[a] * cm_[b];
-        const double msS = ms * (P[0][0] + P[1][1] + P[2][2]);
-        double B[3][3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) B[a][b] = (a == b) ? fma(lms, P[a][a], msS) : fma(ls, P[a][b], ms * P[b][a]);
-        double* out = ke + (int64_t)(pair * 9) * C + c;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) out[(int64_t)(a * 3 + b) * C] = B[a][b];
-        // diagonal blocks: K^nn = -sum_m K^nm, K^mm = -sum_n (K^nm)^T
-        int k = 0;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = a; b < 3; ++b, ++k) {
-            dg[n][k] -= B[a][b];
-            dg[m][k] -= B[b][a];
-          }
-        ++pair;
-      }
-    }
-#pragma unroll
-    for (int n = 0; n < 4; ++n)
-#pragma unroll
-      for (int k = 0; k < 6; ++k) ke[(int64_t)(54 + n * 6 + k) * C + c] = dg[n][k];
-  }
-}
+//
+// Each thread computes the 78 distinct values of its cell (6 off-diagonal
+// 3x3 blocks, 4 symmetric diagonal blocks) into shared memory; the warp then
+// writes the 4 x 32 row blocks (288 B each) with 16-byte stores, 18 lanes per
+// row block, so that every written sector is complete.
+constexpr int kElastElemBlock = 64;
+constexpr int kElastPacked = 78;
 
-// Plane of entry (row node i comp a, column node m comp b) in the 78-plane layout.
-__device__ __forceinline__ int elast_plane(int i, int m, int a, int b) {
+// packed position of entry (row node i comp a, column node m comp b)
+__device__ __forceinline__ int elast_packed(int i, int m, int a, int b) {
   if (i == m) {
-    int lo = min(a, b), hi = max(a, b);
+    const int lo = min(a, b), hi = max(a, b);
     return 54 + i * 6 + lo * (5 - lo) / 2 + hi;
   }
-  int lo = min(i, m), hi = max(i, m);
-  int pair = lo * (7 - lo) / 2 + (hi - lo - 1);
+  const int lo = min(i, m), hi = max(i, m);
+  const int pair = lo * (7 - lo) / 2 + (hi - lo - 1);
   return pair * 9 + (i < m ? a * 3 + b : b * 3 + a);
 }
 
-// ---------------------------------------------------------------------------
-// Node-wise gathers.
+__global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int nb_cell, const double* __restrict__ xyz,
+                                                                         const int32_t* __restrict__ cn,
+                                                                         const int32_t* __restrict__ inv,
+                                                                         double lambda, double mu,
+                                                                         double* __restrict__ er) {
+  __shared__ double stage[kElastElemBlock][kElastPacked + 1];
+  __shared__ int32_t stage_p[kElastElemBlock][4];
+  const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nb_cell; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = base + threadIdx.x;
+    double* my = stage[threadIdx.x];
+    if (c < nb_cell) {
+      d3 cf[4];
+      double s, vol;
+      tet_cofactors(xyz, cn, c, cf, &s, &vol);
+      const double ls = lambda * s, ms = mu * s, lms = (lambda + mu) * s;
+      const int4 p4 = __ldg(reinterpret_cast<const int4*>(inv) + c);
+      stage_p[threadIdx.x][0] = p4.x;
+      stage_p[threadIdx.x][1] = p4.y;
+      stage_p[threadIdx.x][2] = p4.z;
+      stage_p[threadIdx.x][3] = p4.w;
+      double dg[4][6];
+#pragma unroll
+      for (int n = 0; n < 4; ++n)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dg[n][k] = 0.0;
+      int pair = 0;
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+#pragma unroll
+        for (int m = n + 1; m < 4; ++m) {
+          const double cn_[3] = {cf[n].x, cf[n].y, cf[n].z};
+          const double cm_[3] = {cf[m].x, cf[m].y, cf[m].z};
+          double P[3][3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) P[a][b] = cn_[a] * cm_[b];
+          const double msS = ms * (P[0][0] + P[1][1] + P[2][2]);
+          double B[3][3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+              B[a][b] = (a == b) ? fma(lms, P[a][a], msS) : fma(ls, P[a][b], ms * P[b][a]);
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) my[pair * 9 + a * 3 + b] = B[a][b];
+          int k = 0;
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = a; b < 3; ++b, ++k) {
+              dg[n][k] -= B[a][b];
+              dg[m][k] -= B[b][a];
+            }
+          ++pair;
+        }
+      }
+#pragma unroll
+      for (int n = 0; n < 4; ++n)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) my[54 + n * 6 + k] = dg[n][k];
+    }
+    __syncwarp();
+    const int64_t wfirst = base + wbase;
+    const int wcount = wfirst < nb_cell ? (int)(nb_cell - wfirst < 32 ? nb_cell - wfirst : 32) : 0;
+#pragma unroll 1
+    for (int n = 0; n < 4; ++n) {
+      for (int k = lane; k < wcount * 18; k += 32) {
+        const int t = k / 18, q = k - 18 * t;
+        const int pos = 2 * q, a = pos / 12, rem = pos - 12 * a, m = rem / 3, b = rem - 3 * m;
+        const double* src = stage[wbase + t];
+        // pos and pos + 1 share (a, m) except when b == 2 (the pair straddles two column nodes)
+        const double v0 = src[elast_packed(n, m, a, b)];
+        const int pos1 = pos + 1, a1 = pos1 / 12, rem1 = pos1 - 12 * a1, m1 = rem1 / 3, b1 = rem1 - 3 * m1;
+        const double v1 = src[elast_packed(n, m1, a1, b1)];
+        double* dst = er + 36 * (int64_t)stage_p[wbase + t][n] + pos;
+        *reinterpret_cast<double2*>(dst) = make_double2(v0, v1);
+      }
+    }
+    __syncwarp();
+  }
+}
 
-// One thread per (scalar) row: accumulates the element rows of the incident
-// cells in shared memory (row length <= kScalarRmax) or directly in its own
-// row of `values` (longer rows), then writes the row.
+// ---------------------------------------------------------------------------
+// Node-wise gathers: one thread per (scalar) row streams its contiguous
+// element rows and adds them into shared-memory accumulators (row length
+// <= kScalarRmax) or directly into its own row of `values` (longer rows).
+
 template <int NPC>
 __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int nb_node, const int32_t* __restrict__ nc_ptr,
-                                                                const int32_t* __restrict__ nc_cell,
-                                                                const uint8_t* __restrict__ nc_local,
                                                                 const uint8_t* __restrict__ nc_slot,
                                                                 const int32_t* __restrict__ row_ptr,
-                                                                const double* __restrict__ ke, int nb_cell,
+                                                                const double* __restrict__ er,
                                                                 double* __restrict__ values) {
   __shared__ double acc[kScalarRmax * kGatherBlock];
-  const int t = threadIdx.x;
-  const int64_t C = nb_cell;
-  for (int row = blockIdx.x * blockDim.x + t; row < nb_node; row += gridDim.x * blockDim.x) {
-    const int32_t rb = row_ptr[row];
-    const int len = row_ptr[row + 1] - rb;
-    const bool fast = len <= kScalarRmax;
-    if (fast) {
-      for (int s = 0; s < len; ++s) acc[s * kGatherBlock + t] = 0.0;
-    } else {
-      for (int s = 0; s < len; ++s) values[rb + s] = 0.0;
-    }
-    const int32_t pe = nc_ptr[row + 1];
-    for (int32_t p = nc_ptr[row]; p < pe; ++p) {
-      const int64_t c = __ldg(nc_cell + p);
-      const int i = __ldg(nc_local + p);
-      uint8_t sl[NPC];
-      if (NPC == 4) {
-        uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(nc_slot) + p);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) sl[j] = (uint8_t)(w >> (8 * j));
+  double* const my = acc + threadIdx.x;   // this thread's accumulators, stride kGatherBlock
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nb_node; row += gridDim.x * blockDim.x) {
+    const int32_t rb = __ldg(row_ptr + row);
+    const int len = __ldg(row_ptr + row + 1) - rb;
+    const int32_t p0 = __ldg(nc_ptr + row), p1 = __ldg(nc_ptr + row + 1);
+    if (len <= kScalarRmax) {
+      for (int s = 0; s < len; ++s) my[s * kGatherBlock] = 0.0;
+      if constexpr (NPC == 4) {
+        const double2* src = reinterpret_cast<const double2*>(er) + 2 * (int64_t)p0;
+        const uint32_t* sp = reinterpret_cast<const uint32_t*>(nc_slot) + p0;
+#pragma unroll 2
+        for (int32_t p = p0; p < p1; ++p, src += 2, ++sp) {
+          const double2 a = __ldg(src), b = __ldg(src + 1);
+          const uint32_t w = __ldg(sp);
+          my[(w & 0xffu) * kGatherBlock] += a.x;
+          my[((w >> 8) & 0xffu) * kGatherBlock] += a.y;
+          my[((w >> 16) & 0xffu) * kGatherBlock] += b.x;
+          my[(w >> 24) * kGatherBlock] += b.y;
+        }
       } else {
+        const double* src = er + (int64_t)NPC * p0;
+        const uint8_t* sp = nc_slot + (int64_t)NPC * p0;
+#pragma unroll 2
+        for (int32_t p = p0; p < p1; ++p, src += NPC, sp += NPC) {
 #pragma unroll
-        for (int j = 0; j < NPC; ++j) sl[j] = __ldg(nc_slot + (int64_t)p * NPC + j);
+          for (int j = 0; j < NPC; ++j) my[__ldg(sp + j) * kGatherBlock] += __ldg(src + j);
+        }
       }
+      for (int s = 0; s < len; ++s) values[rb + s] = my[s * kGatherBlock];
+    } else {
+      // long row: accumulate in this thread's own row of values
+      for (int s = 0; s < len; ++s) values[rb + s] = 0.0;
+      for (int32_t p = p0; p < p1; ++p)
 #pragma unroll
-      for (int j = 0; j < NPC; ++j) {
-        double v = __ldg(ke + (int64_t)sym_index(i, j, NPC) * C + c);
-        if (fast)
-          acc[sl[j] * kGatherBlock + t] += v;
-        else
-          values[rb + sl[j]] += v;
-      }
+        for (int j = 0; j < NPC; ++j) values[rb + __ldg(nc_slot + (int64_t)NPC * p + j)] += __ldg(er + (int64_t)NPC * p + j);
     }
-    if (fast)
-      for (int s = 0; s < len; ++s) values[rb + s] = acc[s * kGatherBlock + t];
   }
 }
 
 // One thread per scalar row (node, component a) of the 3x3-block matrix.
-__global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(
-    int nb_node, const int32_t* __restrict__ nc_ptr, const int32_t* __restrict__ nc_cell,
-    const uint8_t* __restrict__ nc_local, const uint8_t* __restrict__ nc_slot, const int32_t* __restrict__ row_ptr,
-    const double* __restrict__ ke, int nb_cell, int per_row_layout, double* __restrict__ values) {
+__global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int nb_node, const int32_t* __restrict__ nc_ptr,
+                                                                    const uint8_t* __restrict__ nc_slot,
+                                                                    const int32_t* __restrict__ row_ptr,
+                                                                    const double* __restrict__ er, int per_row_layout,
+                                                                    double* __restrict__ values) {
   __shared__ double acc[3 * kElastRmaxB * kGatherBlock];
-  const int t = threadIdx.x;
-  const int64_t C = nb_cell;
+  double* const my = acc + threadIdx.x;
   const int64_t nrow = 3 * (int64_t)nb_node;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + t; r < nrow; r += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrow; r += (int64_t)gridDim.x * blockDim.x) {
     const int node = (int)(r / 3), a = (int)(r - 3 * (int64_t)node);
-    const int32_t rb = row_ptr[node];
-    const int len = row_ptr[node + 1] - rb;
-    const bool fast = len <= kElastRmaxB;
+    const int32_t rb = __ldg(row_ptr + node);
+    const int len = __ldg(row_ptr + node + 1) - rb;
+    const int32_t p0 = __ldg(nc_ptr + node), p1 = __ldg(nc_ptr + node + 1);
     // value index of (block x, column comp b) of this scalar row
-    auto vidx = [&](int x, int b) -> int64_t {
-      return per_row_layout ? (int64_t)rb * 9 + (int64_t)a * 3 * len + 3 * x + b : ((int64_t)rb + x) * 9 + a * 3 + b;
-    };
-    if (fast) {
-      for (int s = 0; s < 3 * len; ++s) acc[s * kGatherBlock + t] = 0.0;
+    const int64_t row_base = per_row_layout ? (int64_t)rb * 9 + (int64_t)a * 3 * len : (int64_t)rb * 9 + a * 3;
+    const int xstride = per_row_layout ? 3 : 9;
+    if (len <= kElastRmaxB) {
+      for (int s = 0; s < 3 * len; ++s) my[s * kGatherBlock] = 0.0;
+      const double2* src = reinterpret_cast<const double2*>(er + 36 * (int64_t)p0 + 12 * a);
+      const uint32_t* sp = reinterpret_cast<const uint32_t*>(nc_slot) + p0;
+      for (int32_t p = p0; p < p1; ++p, src += 18, ++sp) {
+        const uint32_t w = __ldg(sp);
+        double v[12];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          const double2 q = __ldg(src + k);
+          v[2 * k] = q.x;
+          v[2 * k + 1] = q.y;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          double* d = my + 3 * ((w >> (8 * m)) & 0xffu) * kGatherBlock;
+          d[0] += v[3 * m];
+          d[kGatherBlock] += v[3 * m + 1];
+          d[2 * kGatherBlock] += v[3 * m + 2];
+        }
+      }
+      for (int x = 0; x < len; ++x)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) values[row_base + (int64_t)xstride * x + b] = my[(3 * x + b) * kGatherBlock];
     } else {
       for (int x = 0; x < len; ++x)
-        for (int b = 0; b < 3; ++b) values[vidx(x, b)] = 0.0;
-    }
-    const int32_t pe = nc_ptr[node + 1];
-    for (int32_t p = nc_ptr[node]; p < pe; ++p) {
-      const int64_t c = __ldg(nc_cell + p);
-      const int i = __ldg(nc_local + p);
-      const uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(nc_slot) + p);
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int x = (w >> (8 * m)) & 0xff;
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          double v = __ldg(ke + (int64_t)elast_plane(i, m, a, b) * C + c);
-          if (fast)
-            acc[(3 * x + b) * kGatherBlock + t] += v;
-          else
-            values[vidx(x, b)] += v;
+        for (int b = 0; b < 3; ++b) values[row_base + (int64_t)xstride * x + b] = 0.0;
+      for (int32_t p = p0; p < p1; ++p) {
+        const uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(nc_slot) + p);
+        const double* src = er + 36 * (int64_t)p + 12 * a;
+        for (int m = 0; m < 4; ++m) {
+          const int x = (w >> (8 * m)) & 0xff;
+          for (int b = 0; b < 3; ++b) values[row_base + (int64_t)xstride * x + b] += __ldg(src + 3 * m + b);
         }
       }
     }
-    if (fast)
-      for (int x = 0; x < len; ++x)
-        for (int b = 0; b < 3; ++b) values[vidx(x, b)] = acc[(3 * x + b) * kGatherBlock + t];
   }
 }
 
@@ -358,8 +401,18 @@ static afem_status check_mesh(const afem_mesh_view* m, const char* who) {
   AFEM_CHECK_ARG(m != nullptr, "%s: null mesh view", who);
   AFEM_CHECK_ARG(m->dim == 2 || m->dim == 3, "%s: dim must be 2 or 3 (got %d)", who, m->dim);
   AFEM_CHECK_ARG(m->nb_node > 0 && m->nb_cell > 0, "%s: empty mesh", who);
-  AFEM_CHECK_ARG(m->coords_d && m->cell_nodes_d && m->nc_ptr_d && m->nc_cell_d && m->nc_local_d,
-                 "%s: null mesh buffer", who);
+  AFEM_CHECK_ARG(m->coords_d && m->cell_nodes_d && m->nc_ptr_d && m->nc_cell_d, "%s: null mesh buffer", who);
+  if (m->dim == 3)
+    AFEM_CHECK_ARG(((uintptr_t)m->cell_nodes_d & 15) == 0, "%s: cell_nodes must be 16-byte aligned", who);
+  return AFEM_OK;
+}
+
+static afem_status check_assembly(const afem_mesh_view* m, const char* who) {
+  AFEM_TRY(check_mesh(m, who));
+  AFEM_CHECK_ARG(m->nc_inverse_d && m->nc_slot_d, "%s: null nc_inverse / nc_slot", who);
+  if (m->dim == 3)
+    AFEM_CHECK_ARG(((uintptr_t)m->nc_inverse_d & 15) == 0 && ((uintptr_t)m->nc_slot_d & 3) == 0,
+                   "%s: nc_inverse must be 16-byte and nc_slot 4-byte aligned", who);
   return AFEM_OK;
 }
 
@@ -372,36 +425,38 @@ extern "C" {
 afem_status afem_element_matrices_poisson_p1(afem_context ctx, const afem_mesh_view* m, const double* cell_coeff_d,
                                              double* ke) {
   AFEM_CHECK_ARG(ctx, "afem_element_matrices_poisson_p1: null context");
-  AFEM_TRY(check_mesh(m, "afem_element_matrices_poisson_p1"));
-  AFEM_CHECK_ARG(ke, "afem_element_matrices_poisson_p1: null ke");
+  AFEM_TRY(check_assembly(m, "afem_element_matrices_poisson_p1"));
+  AFEM_CHECK_ARG(ke && ((uintptr_t)ke & 31) == 0, "afem_element_matrices_poisson_p1: ke null or not 32-byte aligned");
   unsigned ge = grid_for(ctx, m->nb_cell, 256, 16);
   if (m->dim == 3)
-    return launch(ctx, k_elem_poisson_tet, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, cell_coeff_d, ke);
-  return launch(ctx, k_elem_poisson_tri, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, cell_coeff_d, ke);
+    return launch(ctx, k_elem_poisson_tet, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                  cell_coeff_d, ke);
+  return launch(ctx, k_elem_poisson_tri, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                cell_coeff_d, ke);
 }
 
 afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                    const double* ke, double* values_d) {
   AFEM_CHECK_ARG(ctx, "afem_gather_poisson_p1: null context");
-  AFEM_TRY(check_mesh(m, "afem_gather_poisson_p1"));
-  AFEM_CHECK_ARG(m->nc_slot_d && row_ptr_d && ke && values_d, "afem_gather_poisson_p1: null buffer");
+  AFEM_TRY(check_assembly(m, "afem_gather_poisson_p1"));
+  AFEM_CHECK_ARG(row_ptr_d && ke && values_d && ((uintptr_t)ke & 31) == 0, "afem_gather_poisson_p1: bad buffer");
   unsigned gg = (unsigned)((m->nb_node + kGatherBlock - 1) / kGatherBlock);
   if (m->dim == 3)
-    return launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_cell_d, m->nc_local_d,
-                  m->nc_slot_d, row_ptr_d, ke, m->nb_cell, values_d);
-  return launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_cell_d, m->nc_local_d,
-                m->nc_slot_d, row_ptr_d, ke, m->nb_cell, values_d);
+    return launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                  values_d);
+  return launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                values_d);
 }
 
 afem_status afem_assemble_poisson_p1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                      const double* cell_coeff_d, double* values_d) {
   AFEM_CHECK_ARG(ctx, "afem_assemble_poisson_p1: null context");
-  AFEM_TRY(check_mesh(m, "afem_assemble_poisson_p1"));
-  AFEM_CHECK_ARG(m->nc_slot_d && row_ptr_d && values_d, "afem_assemble_poisson_p1: null buffer");
-  const int npc = m->dim + 1, nsym = npc * (npc + 1) / 2;
-  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * (size_t)nsym * m->nb_cell)));
+  AFEM_TRY(check_assembly(m, "afem_assemble_poisson_p1"));
+  AFEM_CHECK_ARG(row_ptr_d && values_d, "afem_assemble_poisson_p1: null buffer");
+  const size_t npc = m->dim + 1;
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * npc * npc * m->nb_cell)));
   double* ke;
-  AFEM_TRY(scratch_take(ctx, (size_t)nsym * m->nb_cell, &ke));
+  AFEM_TRY(scratch_take(ctx, npc * npc * m->nb_cell, &ke));
   AFEM_TRY(afem_element_matrices_poisson_p1(ctx, m, cell_coeff_d, ke));
   return afem_gather_poisson_p1(ctx, m, row_ptr_d, ke, values_d);
 }
@@ -409,34 +464,35 @@ afem_status afem_assemble_poisson_p1(afem_context ctx, const afem_mesh_view* m, 
 afem_status afem_element_matrices_elasticity_tet4(afem_context ctx, const afem_mesh_view* m, double lambda,
                                                   double mu, double* ke) {
   AFEM_CHECK_ARG(ctx, "afem_element_matrices_elasticity_tet4: null context");
-  AFEM_TRY(check_mesh(m, "afem_element_matrices_elasticity_tet4"));
+  AFEM_TRY(check_assembly(m, "afem_element_matrices_elasticity_tet4"));
   AFEM_CHECK_ARG(m->dim == 3, "afem_element_matrices_elasticity_tet4: tetrahedra only (dim 3)");
-  AFEM_CHECK_ARG(ke, "afem_element_matrices_elasticity_tet4: null ke");
-  return launch(ctx, k_elem_elasticity_tet, grid_for(ctx, m->nb_cell, 128, 16), 128, 0, m->nb_cell, m->coords_d,
-                m->cell_nodes_d, lambda, mu, ke);
+  AFEM_CHECK_ARG(ke && ((uintptr_t)ke & 31) == 0, "afem_element_matrices_elasticity_tet4: ke null or misaligned");
+  return launch(ctx, k_elem_elasticity_tet, grid_for(ctx, m->nb_cell, kElastElemBlock, 32), kElastElemBlock, 0,
+                m->nb_cell, m->coords_d,
+                m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke);
 }
 
 afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                         const double* ke, int layout, double* values_d) {
   AFEM_CHECK_ARG(ctx, "afem_gather_elasticity_tet4: null context");
-  AFEM_TRY(check_mesh(m, "afem_gather_elasticity_tet4"));
+  AFEM_TRY(check_assembly(m, "afem_gather_elasticity_tet4"));
   AFEM_CHECK_ARG(m->dim == 3, "afem_gather_elasticity_tet4: tetrahedra only (dim 3)");
   AFEM_CHECK_ARG(layout == AFEM_LAYOUT_PER_BLOCK || layout == AFEM_LAYOUT_PER_ROW,
                  "afem_gather_elasticity_tet4: bad layout %d", layout);
-  AFEM_CHECK_ARG(m->nc_slot_d && row_ptr_d && ke && values_d, "afem_gather_elasticity_tet4: null buffer");
+  AFEM_CHECK_ARG(row_ptr_d && ke && values_d && ((uintptr_t)ke & 31) == 0, "afem_gather_elasticity_tet4: bad buffer");
   unsigned gg = (unsigned)((3 * (int64_t)m->nb_node + kGatherBlock - 1) / kGatherBlock);
-  return launch(ctx, k_gather_elasticity, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_cell_d, m->nc_local_d,
-                m->nc_slot_d, row_ptr_d, ke, m->nb_cell, (int)(layout == AFEM_LAYOUT_PER_ROW), values_d);
+  return launch(ctx, k_gather_elasticity, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                (int)(layout == AFEM_LAYOUT_PER_ROW), values_d);
 }
 
 afem_status afem_assemble_elasticity_tet4(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                           double lambda, double mu, int layout, double* values_d) {
   AFEM_CHECK_ARG(ctx, "afem_assemble_elasticity_tet4: null context");
-  AFEM_TRY(check_mesh(m, "afem_assemble_elasticity_tet4"));
-  AFEM_CHECK_ARG(m->nc_slot_d && row_ptr_d && values_d, "afem_assemble_elasticity_tet4: null buffer");
-  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * (size_t)78 * m->nb_cell)));
+  AFEM_TRY(check_assembly(m, "afem_assemble_elasticity_tet4"));
+  AFEM_CHECK_ARG(row_ptr_d && values_d, "afem_assemble_elasticity_tet4: null buffer");
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * (size_t)144 * m->nb_cell)));
   double* ke;
-  AFEM_TRY(scratch_take(ctx, (size_t)78 * m->nb_cell, &ke));
+  AFEM_TRY(scratch_take(ctx, (size_t)144 * m->nb_cell, &ke));
   AFEM_TRY(afem_element_matrices_elasticity_tet4(ctx, m, lambda, mu, ke));
   return afem_gather_elasticity_tet4(ctx, m, row_ptr_d, ke, layout, values_d);
 }

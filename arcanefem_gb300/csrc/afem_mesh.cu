@@ -4,15 +4,18 @@
 //   histogram of incidences, exclusive scan, scatter, then a per-node
 //   segmented sort of (cell, local) keys so that cells come out ascending --
 //   the order of Arcane's nodeCell() connectivity.  The histogram and scatter
-//   use integer atomics on per-node counters; the segmented sort makes the
-//   result independent of their order, so the output is deterministic.
+//   use integer atomics on per-node counters; the segmented sort (a bitonic
+//   network in registers, one warp per node) makes the result independent of
+//   their order, so the output is deterministic.
 //
 // node -> node sparsity (rows of the assembled matrix):
-//   one warp per node gathers the nodes of its incident cells into shared
-//   memory, bitonic-sorts them and keeps the distinct values: row length =
-//   1 + number of neighbours (femutils/BSRFormat.cc:445-557, row = deg + 1).
-//   A second pass writes the columns (ascending or self-last) and the slot
-//   map used by the assembly kernels.
+//   one warp per node stages the nodes of its incident cells in shared memory
+//   and extracts their distinct values in increasing order (one warp-wide
+//   minimum per distinct value): row length = 1 + number of neighbours
+//   (femutils/BSRFormat.cc:445-557, row = deg + 1).  The second pass writes
+//   the columns (ascending or self-last) and, for every cell-node incidence,
+//   its position in the row (the slot map used by the assembly kernels).
+#include <algorithm>
 #include <climits>
 
 #include "afem_internal.cuh"
@@ -47,24 +50,53 @@ __global__ void k_nc_scatter(const int32_t* __restrict__ cn, int64_t total, int 
   }
 }
 
-// Per-node insertion sort of the (cell * 4 + local) keys, then split.
-__global__ void k_nc_sort(int nb_node, const int32_t* __restrict__ nc_ptr, int32_t* __restrict__ key,
-                          int32_t* __restrict__ nc_cell, uint8_t* __restrict__ nc_local) {
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb_node; n += gridDim.x * blockDim.x) {
-    int32_t b = nc_ptr[n], e = nc_ptr[n + 1];
-    for (int32_t i = b + 1; i < e; ++i) {
-      int32_t v = key[i];
-      int32_t j = i - 1;
-      while (j >= b && key[j] > v) {
-        key[j + 1] = key[j];
-        --j;
+constexpr int kWarpsPerBlock = 8;
+
+// Per-node sort of the (cell * 4 + local) keys, then split; the inverse map
+// records, for each (cell, local), its incidence index.  One warp per node:
+// up to 32 keys are sorted by a bitonic network on registers (shuffles);
+// longer lists (rare) by an insertion sort in lane 0.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_nc_sort(int nb_node, int npc,
+                                                                 const int32_t* __restrict__ nc_ptr,
+                                                                 int32_t* __restrict__ key,
+                                                                 int32_t* __restrict__ nc_cell,
+                                                                 uint8_t* __restrict__ nc_local,
+                                                                 int32_t* __restrict__ nc_inverse) {
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int n = wid; n < nb_node; n += nwarps) {
+    const int32_t b = nc_ptr[n], e = nc_ptr[n + 1];
+    const int deg = e - b;
+    if (deg <= 32) {
+      int32_t v = lane < deg ? key[b + lane] : INT_MAX;
+#pragma unroll
+      for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          int32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+          bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+          v = keep_min ? min(v, o) : max(v, o);
+        }
       }
-      key[j + 1] = v;
+      if (lane < deg) key[b + lane] = v;
+    } else if (lane == 0) {
+      for (int32_t i = b + 1; i < e; ++i) {
+        int32_t v = key[i];
+        int32_t j = i - 1;
+        while (j >= b && key[j] > v) {
+          key[j + 1] = key[j];
+          --j;
+        }
+        key[j + 1] = v;
+      }
     }
-    for (int32_t i = b; i < e; ++i) {
+    __syncwarp();
+    for (int32_t i = b + lane; i < e; i += 32) {
       int32_t v = key[i];
       nc_cell[i] = v >> 2;
       nc_local[i] = (uint8_t)(v & 3);
+      if (nc_inverse) nc_inverse[(int64_t)(v >> 2) * npc + (v & 3)] = i;
     }
   }
 }
@@ -72,73 +104,64 @@ __global__ void k_nc_sort(int nb_node, const int32_t* __restrict__ nc_ptr, int32
 // ---------------------------------------------------------------------------
 // node -> node
 
-constexpr int kRowWarps = 8;        // warps per block
 constexpr int kRowCap = 512;        // candidates per node (deg * npc), e.g. 128 tetrahedra
 constexpr int kMaxRowLen = 255;     // slot map entries are uint8
 
-__device__ __forceinline__ void warp_bitonic_sort(int32_t* s, int P) {
+// Stage the candidate nodes of node n (the nodes of its incident cells) in s.
+// Returns the candidate count, or -1 above kRowCap.
+__device__ __forceinline__ int stage_candidates(int n, int npc, const int32_t* __restrict__ cn,
+                                                const int32_t* __restrict__ nc_ptr,
+                                                const int32_t* __restrict__ nc_cell, int32_t* s) {
   const int lane = threadIdx.x & 31;
-  for (int k = 2; k <= P; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = lane; i < P; i += 32) {
-        int ixj = i ^ j;
-        if (ixj > i) {
-          int32_t a = s[i], b = s[ixj];
-          bool up = (i & k) == 0;
-          if ((a > b) == up) {
-            s[i] = b;
-            s[ixj] = a;
-          }
-        }
-      }
-      __syncwarp();
-    }
-  }
-}
-
-// Gathers, sorts and compacts the distinct candidate nodes of node n into
-// `u` (ascending).  Returns the number of distinct nodes (row length), or -1
-// if the candidate count exceeds kRowCap.
-__device__ int warp_row_unique(int n, int npc, const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_ptr,
-                               const int32_t* __restrict__ nc_cell, int32_t* s, int32_t* u) {
-  const int lane = threadIdx.x & 31;
-  int32_t b = nc_ptr[n], e = nc_ptr[n + 1];
-  int m = (e - b) * npc;
+  const int32_t b = nc_ptr[n];
+  const int m = (nc_ptr[n + 1] - b) * npc;
   if (m > kRowCap) return -1;
-  int P = 32;
-  while (P < m) P <<= 1;
-  for (int i = lane; i < P; i += 32) {
-    int32_t v = INT_MAX;
-    if (i < m) {
-      int k = i / npc, j = i - k * npc;
-      v = cn[(int64_t)nc_cell[b + k] * npc + j];
-    }
-    s[i] = v;
+  for (int i = lane; i < m; i += 32) {
+    const int k = i / npc, j = i - k * npc;
+    s[i] = cn[(int64_t)nc_cell[b + k] * npc + j];
   }
   __syncwarp();
-  warp_bitonic_sort(s, P);
-  int count = 0;
-  for (int i0 = 0; i0 < P; i0 += 32) {
-    int i = i0 + lane;
-    int32_t v = s[i];
-    bool keep = v != INT_MAX && (i == 0 || s[i - 1] != v);
-    unsigned mask = __ballot_sync(0xffffffffu, keep);
-    if (keep) u[count + __popc(mask & ((1u << lane) - 1u))] = v;
-    count += __popc(mask);
-  }
-  __syncwarp();
-  return count;
+  return m;
 }
 
-__global__ void __launch_bounds__(kRowWarps * 32) k_row_len(int nb_node, int npc, const int32_t* __restrict__ cn,
-                                                            const int32_t* __restrict__ nc_ptr,
-                                                            const int32_t* __restrict__ nc_cell,
-                                                            int32_t* __restrict__ row_len, int* __restrict__ err) {
-  __shared__ int32_t sh_s[kRowWarps][kRowCap];
-  __shared__ int32_t sh_u[kRowWarps][kRowCap];
+// Distinct candidates in increasing order: returns the row length; when
+// `fill`, also writes the columns (ascending or self-last) at cols[0..len)
+// and, per candidate i, its position in the row at slot[i].
+__device__ __forceinline__ int extract_row(int n, const int32_t* s, int m, bool fill, int len, int self_last,
+                                           int32_t* __restrict__ cols, uint8_t* __restrict__ slot) {
+  const int lane = threadIdx.x & 31;
+  int32_t last = INT_MIN;
+  int it = 0;
+  for (;;) {
+    int32_t loc = INT_MAX;
+    for (int i = lane; i < m; i += 32) {
+      const int32_t v = s[i];
+      if (v > last && v < loc) loc = v;
+    }
+    const int32_t mn = __reduce_min_sync(0xffffffffu, loc);
+    if (mn == INT_MAX) break;
+    if (fill) {
+      const int pos = self_last ? (mn < n ? it : (mn == n ? len - 1 : it - 1)) : it;
+      if (lane == 0 && pos >= 0 && pos < len) cols[pos] = mn;   // a row_ptr that disagrees is reported, not written past
+      for (int i = lane; i < m; i += 32)
+        if (s[i] == mn) slot[i] = (uint8_t)pos;
+    }
+    last = mn;
+    ++it;
+  }
+  return it;
+}
+
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, int npc, const int32_t* __restrict__ cn,
+                                                                 const int32_t* __restrict__ nc_ptr,
+                                                                 const int32_t* __restrict__ nc_cell,
+                                                                 int32_t* __restrict__ row_len,
+                                                                 int* __restrict__ err) {
+  __shared__ int32_t sh[kWarpsPerBlock][kRowCap];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int n = blockIdx.x * kRowWarps + w; n < nb_node; n += gridDim.x * kRowWarps) {
-    int len = warp_row_unique(n, npc, cn, nc_ptr, nc_cell, sh_s[w], sh_u[w]);
+  for (int n = blockIdx.x * kWarpsPerBlock + w; n < nb_node; n += gridDim.x * kWarpsPerBlock) {
+    const int m = stage_candidates(n, npc, cn, nc_ptr, nc_cell, sh[w]);
+    int len = m < 0 ? -1 : extract_row(n, sh[w], m, false, 0, 0, nullptr, nullptr);
     if (lane == 0) {
       if (len < 0 || len > kMaxRowLen) {
         atomicOr(err, 2);
@@ -146,55 +169,26 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_len(int nb_node, int npc
       }
       row_len[n] = len;
     }
+    __syncwarp();
   }
 }
 
-__global__ void __launch_bounds__(kRowWarps * 32) k_row_fill(int nb_node, int npc, const int32_t* __restrict__ cn,
-                                                             const int32_t* __restrict__ nc_ptr,
-                                                             const int32_t* __restrict__ nc_cell,
-                                                             const uint8_t* __restrict__ nc_local,
-                                                             const int32_t* __restrict__ row_ptr, int self_last,
-                                                             int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
-                                                             int* __restrict__ err) {
-  __shared__ int32_t sh_s[kRowWarps][kRowCap];
-  __shared__ int32_t sh_u[kRowWarps][kRowCap];
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, int npc, const int32_t* __restrict__ cn,
+                                                                  const int32_t* __restrict__ nc_ptr,
+                                                                  const int32_t* __restrict__ nc_cell,
+                                                                  const int32_t* __restrict__ row_ptr, int self_last,
+                                                                  int32_t* __restrict__ cols,
+                                                                  uint8_t* __restrict__ slot, int* __restrict__ err) {
+  __shared__ int32_t sh[kWarpsPerBlock][kRowCap];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int n = blockIdx.x * kRowWarps + w; n < nb_node; n += gridDim.x * kRowWarps) {
-    int32_t* u = sh_u[w];
-    int len = warp_row_unique(n, npc, cn, nc_ptr, nc_cell, sh_s[w], u);
-    int32_t rb = row_ptr[n];
-    if (len < 0 || len != row_ptr[n + 1] - rb) {
-      if (lane == 0) atomicOr(err, 4);
-      continue;
-    }
-    // position of the diagonal in the ascending list
-    int self_pos = -1;
-    for (int i0 = 0; i0 < len; i0 += 32) {
-      int i = i0 + lane;
-      unsigned m = __ballot_sync(0xffffffffu, i < len && u[i] == n);
-      if (m && self_pos < 0) self_pos = i0 + __ffs(m) - 1;
-    }
-    // columns
-    for (int i = lane; i < len; i += 32) {
-      int dst = i;
-      if (self_last) dst = (i == self_pos) ? len - 1 : (i > self_pos ? i - 1 : i);
-      cols[rb + dst] = u[i];
-    }
-    // slot map: incidence p, cell node j -> position of that column in the row
-    int32_t b = nc_ptr[n], e = nc_ptr[n + 1];
-    int m = (e - b) * npc;
-    for (int i = lane; i < m; i += 32) {
-      int k = i / npc, j = i - k * npc;
-      int32_t v = cn[(int64_t)nc_cell[b + k] * npc + j];
-      int lo = 0, hi = len - 1;
-      while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (u[mid] < v) lo = mid + 1; else hi = mid;
-      }
-      int pos = lo;
-      if (self_last) pos = (pos == self_pos) ? len - 1 : (pos > self_pos ? pos - 1 : pos);
-      slot[(int64_t)(b + k) * npc + j] = (uint8_t)pos;
-    }
+  for (int n = blockIdx.x * kWarpsPerBlock + w; n < nb_node; n += gridDim.x * kWarpsPerBlock) {
+    const int32_t rb = row_ptr[n];
+    const int len = row_ptr[n + 1] - rb;
+    const int m = stage_candidates(n, npc, cn, nc_ptr, nc_cell, sh[w]);
+    int got = -1;
+    if (m >= 0)
+      got = extract_row(n, sh[w], m, true, len, self_last, cols + rb, slot + (int64_t)nc_ptr[n] * npc);
+    if (lane == 0 && got != len) atomicOr(err, 4);
     __syncwarp();
   }
 }
@@ -230,7 +224,7 @@ using namespace afem;
 extern "C" {
 
 afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int npc, const int32_t* cell_nodes_d,
-                                 int32_t* nc_ptr_d, int32_t* nc_cell_d, uint8_t* nc_local_d) {
+                                 int32_t* nc_ptr_d, int32_t* nc_cell_d, uint8_t* nc_local_d, int32_t* nc_inverse_d) {
   AFEM_CHECK_ARG(ctx, "afem_node_cell_build: null context");
   AFEM_CHECK_ARG(nb_node > 0 && nb_cell > 0, "afem_node_cell_build: empty mesh (nb_node=%d nb_cell=%d)", nb_node,
                  nb_cell);
@@ -255,8 +249,8 @@ afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int
   AFEM_TRY(exclusive_scan_i32(ctx, cnt, nc_ptr_d, nb_node));
   AFEM_TRY(launch(ctx, k_nc_scatter, grid_for(ctx, total, 256), 256, 0, cell_nodes_d, total, npc, nb_node,
                   (const int32_t*)nc_ptr_d, cursor, key));
-  AFEM_TRY(launch(ctx, k_nc_sort, grid_for(ctx, nb_node, 128, 16), 128, 0, nb_node, (const int32_t*)nc_ptr_d, key,
-                  nc_cell_d, nc_local_d));
+  AFEM_TRY(launch(ctx, k_nc_sort, grid_for(ctx, (int64_t)nb_node * 32, kWarpsPerBlock * 32, 8), kWarpsPerBlock * 32, 0,
+                  nb_node, npc, (const int32_t*)nc_ptr_d, key, nc_cell_d, nc_local_d, nc_inverse_d));
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
   if (herr) return fail(AFEM_ERR_MESH, "afem_node_cell_build: node id out of range [0, %d) in cell_nodes", nb_node);
@@ -275,8 +269,10 @@ afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int
   AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &len));
   AFEM_TRY(scratch_take(ctx, 1, &err));
   AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
-  unsigned grid = (unsigned)std::min<int64_t>((nb_node + kRowWarps - 1) / kRowWarps, (int64_t)ctx->sm_count * 8);
-  AFEM_TRY(launch(ctx, k_row_len, grid, kRowWarps * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, len, err));
+  unsigned grid =
+      (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock, (int64_t)ctx->sm_count * 8);
+  AFEM_TRY(launch(ctx, k_row_len, grid, kWarpsPerBlock * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, len,
+                  err));
   AFEM_TRY(exclusive_scan_i32(ctx, len, row_ptr_d, nb_node));
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
@@ -295,6 +291,7 @@ afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int
 afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int32_t* cell_nodes_d,
                                const int32_t* nc_ptr_d, const int32_t* nc_cell_d, const uint8_t* nc_local_d,
                                const int32_t* row_ptr_d, int col_order, int32_t* cols_d, uint8_t* nc_slot_d) {
+  (void)nc_local_d;
   AFEM_CHECK_ARG(ctx, "afem_sparsity_cols: null context");
   AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4), "afem_sparsity_cols: bad sizes");
   AFEM_CHECK_ARG(col_order == AFEM_COLS_ASCENDING || col_order == AFEM_COLS_SELF_LAST,
@@ -305,9 +302,10 @@ afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int
   int* err;
   AFEM_TRY(scratch_take(ctx, 1, &err));
   AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
-  unsigned grid = (unsigned)std::min<int64_t>((nb_node + kRowWarps - 1) / kRowWarps, (int64_t)ctx->sm_count * 8);
-  AFEM_TRY(launch(ctx, k_row_fill, grid, kRowWarps * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d,
-                  nc_local_d, row_ptr_d, col_order, cols_d, nc_slot_d, err));
+  unsigned grid =
+      (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock, (int64_t)ctx->sm_count * 8);
+  AFEM_TRY(launch(ctx, k_row_fill, grid, kWarpsPerBlock * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d,
+                  row_ptr_d, col_order, cols_d, nc_slot_d, err));
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
   if (herr) return fail(AFEM_ERR_MESH, "afem_sparsity_cols: row_ptr does not match the mesh");

@@ -138,8 +138,9 @@ class BSRFormat:
         self.nc_ptr = torch.empty(m.nb_node + 1, dtype=torch.int32, device=dev)
         self.nc_cell = torch.empty(total, dtype=torch.int32, device=dev)
         self.nc_local = torch.empty(total, dtype=torch.uint8, device=dev)
+        self.nc_inverse = torch.empty(total, dtype=torch.int32, device=dev)
         call("afem_node_cell_build", self.ctx.handle, m.nb_node, m.nb_cell, m.npc, _ptr(m.cells), _ptr(self.nc_ptr),
-             _ptr(self.nc_cell), _ptr(self.nc_local))
+             _ptr(self.nc_cell), _ptr(self.nc_local), _ptr(self.nc_inverse))
 
     # BSRFormat::computeSparsity (femutils/BSRFormat.cc:1011-1018)
     def compute_sparsity(self):
@@ -161,7 +162,7 @@ class BSRFormat:
         m = self.mesh
         return MeshView(m.dim, m.nb_node, m.nb_cell, m.coords.data_ptr(), m.cells.data_ptr(), self.nc_ptr.data_ptr(),
                         self.nc_cell.data_ptr(), self.nc_local.data_ptr(),
-                        0 if self.nc_slot is None else self.nc_slot.data_ptr())
+                        0 if self.nc_slot is None else self.nc_slot.data_ptr(), self.nc_inverse.data_ptr())
 
     # assembleBilinearAtomicFree with the Poisson element vectors
     def assemble_poisson(self, cell_coeff: torch.Tensor | None = None):
@@ -176,11 +177,10 @@ class BSRFormat:
         call("afem_assemble_elasticity_tet4", self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), float(lam), float(mu),
              layout, _ptr(self.values))
 
-    def element_planes(self) -> int:
-        if self.nb_dof == 3:
-            return 78
-        npc = self.mesh.npc
-        return npc * (npc + 1) // 2
+    def element_buffer_size(self) -> int:
+        """Doubles of the stage-1 element rows (incidence order): npc^2 per cell, 144 for elasticity."""
+        per_cell = 144 if self.nb_dof == 3 else self.mesh.npc ** 2
+        return per_cell * self.mesh.nb_cell
 
     # the two stages of assemble_poisson / assemble_elasticity, caller-owned element matrices
     def element_matrices(self, ke: torch.Tensor, cell_coeff: torch.Tensor | None = None, lam=0.0, mu=0.0):

@@ -1,13 +1,23 @@
 #!/usr/bin/env python
-"""Benchmark: node-wise P1 CSR assembly on one GB300 (assembled nnz/s).
+"""Benchmark: node-wise P1 assembly on one GB300 (assembled nnz/s), plus the
+time to a relative residual of the Krylov solve on the assembled system.
 
-Workload (default): 3D Poisson P1 on the unit cube, 128^3 hexahedra split in
-6 tetrahedra (12,582,912 tets, 2,146,689 nodes, 31,802,497 nonzeros),
-interior nodes jittered by +-0.15 h (seeded), synthetic data.  A step is one
-full assembly of the matrix values (element matrices + node-wise gather) with
-the sparsity reused, the AF-BSR / node-wise CSR hot loop of the reference.
+Workloads (synthetic, seeded jittered structured meshes):
+  poisson3d    (default) 3D Poisson P1, unit cube 128^3 hexahedra x 6 tets
+               (12,582,912 tets, 2,146,689 nodes, 31,802,497 nnz); f = 1,
+               u = 0 on x = 0 and x = 1; CG to 1e-8.
+  elasticity3d linear elasticity P1, 96^3 x 6 tets, 3x3 blocks
+               (121,188,969 scalar nnz); E = 21e5, nu = 0.28, f = (0,0,-1),
+               clamped at z = 0; mixed-precision CG to 1e-8.
+  poisson2d    2D Poisson P1, 256^2 quads x 2 tris; f = -1, u = 0 on the
+               boundary; CG to 1e-10.
+
+A step is one full assembly of the matrix values (element matrices +
+node-wise gather) with the sparsity reused: the node-wise CSR / AF-BSR hot
+loop of the reference.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload poisson3d|elasticity3d|poisson2d]
 
 One JSON line on rank 0.  ``value`` is device-timed (CUDA events, L2 flushed
 between steps); ``e2e`` is the same metric through the public API with host
@@ -31,9 +41,19 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "assembled nnz/s (node-wise CSR, 3D Poisson P1)"
 UNIT = "nnz/s"
 HBM_FALLBACK_GBS = 6800.0
+
+WORKLOADS = {
+    "poisson3d": dict(dim=3, n=128, jitter=0.15, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 3D Poisson P1)",
+                      dp_elem=74, dp_gather=16, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
+    "elasticity3d": dict(dim=3, n=96, jitter=0.15, nb_dof=3,
+                         metric="assembled nnz/s (node-wise 3x3 BSR, 3D linear elasticity P1)",
+                         dp_elem=276, dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
+                         E=21e5, nu=0.28, body=(0.0, 0.0, -1.0)),
+    "poisson2d": dict(dim=2, n=256, jitter=0.2, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 2D Poisson P1)",
+                      dp_elem=26, dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
+}
 
 
 def parse_args():
@@ -42,26 +62,42 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--n", type=int, default=128, help="hexahedra per cube edge")
+    p.add_argument("--workload", choices=list(WORKLOADS), default="poisson3d")
+    p.add_argument("--n", type=int, default=0, help="elements per edge (default: the workload's)")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    return p.parse_args()
+    p.add_argument("--no-solve", action="store_true")
+    a = p.parse_args()
+    if a.n <= 0:
+        a.n = WORKLOADS[a.workload]["n"]
+    return a
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", 1))
-    local = int(os.environ.get("LOCAL_RANK", 0))
-    return rank, world, local
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def make_mesh(args):
+    from arcanefem_gb300 import meshgen
+    w = WORKLOADS[args.workload]
+    if w["dim"] == 3:
+        return meshgen.unit_cube_tet(args.n, jitter=w["jitter"], seed=args.seed)
+    return meshgen.unit_square_tri(args.n, jitter=w["jitter"], seed=args.seed)
 
 
 def config(args, world):
-    return {"workload": f"poisson3d_p1_tet_{args.n}^3 (unit cube, 6-tet Kuhn split, jitter 0.15h)",
-            "elements": 6 * args.n ** 3, "nodes": (args.n + 1) ** 3, "seed": args.seed,
+    w = WORKLOADS[args.workload]
+    if w["dim"] == 3:
+        desc = f"unit cube {args.n}^3 hexahedra x 6 Kuhn tetrahedra, jitter {w['jitter']}h"
+        elements, nodes = 6 * args.n ** 3, (args.n + 1) ** 3
+    else:
+        desc = f"unit square {args.n}^2 quads x 2 triangles, jitter {w['jitter']}h"
+        elements, nodes = 2 * args.n ** 2, (args.n + 1) ** 2
+    return {"workload": f"{args.workload} ({desc})", "elements": elements, "nodes": nodes,
+            "dof_per_node": w["nb_dof"], "seed": args.seed,
             "step": "values assembly (element matrices + node-wise gather), sparsity reused",
-            "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}",
-            "dirichlet": "none in the timed step (matrix only)"}
+            "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"}
 
 
 # ---------------------------------------------------------------------------
@@ -79,10 +115,11 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            time.sleep(0.3)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -93,6 +130,7 @@ class ClockSampler:
 
     def __exit__(self, *exc):
         if self.proc:
+            time.sleep(0.2)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -119,19 +157,17 @@ class ClockSampler:
 
 
 def read_peaks():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        d = json.load(open(path))
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         return float(d["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return HBM_FALLBACK_GBS, "fallback"
 
 
 def read_traffic(name: str):
-    """Per-launch DRAM bytes from the committed ncu summary (profiles/), or None."""
-    path = os.path.join(ROOT, "profiles", name)
+    """Per-assembly DRAM bytes from the committed ncu summary (profiles/), or None."""
     try:
-        for line in open(path):
+        for line in open(os.path.join(ROOT, "profiles", name)):
             m = re.match(r"\s*traffic_bytes_per_assembly\s*[:=]\s*([0-9.eE+]+)", line)
             if m:
                 return float(m.group(1))
@@ -140,42 +176,44 @@ def read_traffic(name: str):
     return None
 
 
-def algorithmic_bytes(nb_node, nb_cell, nnz, npc=4, dim=3):
-    """Values-only assembly bytes: values + coords + cell->node + node->cell (ptr + list)."""
-    return 8 * nnz + 8 * dim * nb_node + 4 * npc * nb_cell + 4 * npc * nb_cell + 4 * (nb_node + 1)
+def algorithmic_bytes(mesh, nnz_scalar):
+    """Values-only assembly bytes: values + coords + cell->node + node->cell (list + ptr)."""
+    npc, n, c = mesh.npc, mesh.nb_node, mesh.nb_cell
+    return 8 * nnz_scalar + 8 * 3 * n + 4 * npc * c + 4 * npc * c + 4 * (n + 1)
 
 
 # ---------------------------------------------------------------------------
 def run_gpu(args):
-    import numpy as np
     import torch
     import torch.distributed as dist
 
-    from arcanefem_gb300 import fem, meshgen
+    from arcanefem_gb300 import fem
 
+    w = WORKLOADS[args.workload]
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    mesh = meshgen.unit_cube_tet(args.n, jitter=0.15, seed=args.seed)
+    mesh = make_mesh(args)
     ctx = fem.Context()
-    dm = fem.Mesh.from_host(3, mesh.coords, mesh.cells)
+    dm = fem.Mesh.from_host(mesh.dim, mesh.coords, mesh.cells)
     fmt = fem.BSRFormat(ctx, dm)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    fmt.initialize(1)
+    fmt.initialize(w["nb_dof"])
     fmt.compute_sparsity()
     torch.cuda.synchronize()
     structure_ms = (time.perf_counter() - t0) * 1e3
-    nnz = fmt.nnzb
-    ke = torch.empty(fmt.element_planes() * mesh.nb_cell, dtype=torch.float64, device="cuda")
+    nnz = fmt.nnzb * w["nb_dof"] ** 2
+    lam, mu = fem.lame(w["E"], w["nu"]) if w["nb_dof"] == 3 else (0.0, 0.0)
+    ke = torch.empty(fmt.element_buffer_size(), dtype=torch.float64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def step(ev=None):
         if ev:
             ev[0].record()
-        fmt.element_matrices(ke)
+        fmt.element_matrices(ke, lam=lam, mu=mu)
         if ev:
             ev[1].record()
         fmt.gather(ke)
@@ -201,8 +239,7 @@ def run_gpu(args):
     launches = ctx.launches - launches0
     elem_ms = [e[0].elapsed_time(e[1]) for e in events]
     gath_ms = [e[1].elapsed_time(e[2]) for e in events]
-    asm_ms = [a + b for a, b in zip(elem_ms, gath_ms)]
-    total_ms = sum(asm_ms)
+    total_ms = sum(a + b for a, b in zip(elem_ms, gath_ms))
     if world > 1:
         t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -210,33 +247,25 @@ def run_gpu(args):
     ms_per_step = total_ms / args.steps
     value = world * nnz / (ms_per_step * 1e-3)
 
-    # roofline of the assembly (element + gather kernels of one step)
     hbm_peak, peak_kind = read_peaks()
-    alg = algorithmic_bytes(mesh.nb_node, mesh.nb_cell, nnz)
+    alg = algorithmic_bytes(mesh, nnz)
     achieved = alg / (ms_per_step * 1e-3) / 1e9
-    traffic = read_traffic(f"assembly_poisson_tet_n{args.n}.md")
+    traffic = read_traffic(f"assembly_{args.workload}_n{args.n}.md")
     fma_rate = ctx.fp64_fma_rate()
-    dp_per_tet = 74 + 16      # element kernel + gather adds
-    dp_achieved = dp_per_tet * mesh.nb_cell / (ms_per_step * 1e-3) / 1e9
+    dp_cell = w["dp_elem"] + w["dp_gather"]
+    dp_achieved = dp_cell * mesh.nb_cell / (ms_per_step * 1e-3) / 1e9
+    kernel = ("k_elem_elasticity_tet + k_gather_elasticity" if w["nb_dof"] == 3 else
+              f"k_elem_poisson_{'tet' if mesh.dim == 3 else 'tri'} + k_gather_scalar<{mesh.npc}>")
 
-    # e2e: public API, host buffers, transfers inside the timed region
-    e2e = None
-    if not args.no_e2e:
-        e2e = run_e2e(args, mesh, nnz)
-
+    e2e = None if args.no_e2e else run_e2e(args, mesh, fmt, lam, mu)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(mesh, fmt)
-
-    # a cheap correctness guard on the benchmarked output (row sums of a P1 Laplacian vanish)
-    vals = fmt.values
-    rows = torch.repeat_interleave(torch.arange(mesh.nb_node, device="cuda"), torch.diff(fmt.row_ptr.long()))
-    rs = torch.zeros(mesh.nb_node, dtype=torch.float64, device="cuda").index_add_(0, rows, vals)
-    row_sum_rel = float(rs.abs().max() / vals.abs().max())
+        cpu = cpu_baseline(args, mesh, fmt, lam, mu)
+    solve = None if args.no_solve else run_solve(args, ctx, mesh, fmt)
 
     if rank == 0:
         out = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered mesh)",
             "config": config(args, world),
@@ -244,38 +273,42 @@ def run_gpu(args):
             "structure_ms_once": structure_ms, "wall_s_timed_loop": wall_s, "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
-                         "algorithmic_bytes": alg, "kernel": "k_elem_poisson_tet + k_gather_scalar<4>"},
-            "fp64_roofline": {"achieved_gdp_instr_s": dp_achieved, "peak_gfma_s": fma_rate,
-                              "frac": dp_achieved / fma_rate, "dp_instr_per_tet": dp_per_tet},
-            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(), "check": {"row_sum_rel": row_sum_rel},
+                         "algorithmic_bytes": alg, "kernel": kernel},
+            "fp64_roofline": {"achieved_g_fp64_instr_s": dp_achieved, "peak_g_fma_s": fma_rate,
+                              "frac": dp_achieved / fma_rate, "fp64_instr_per_cell": dp_cell,
+                              "note": "FP64 issue rate is the binding limit of the element kernel on GB300"},
+            "e2e": e2e, "cpu_baseline": cpu, "solve": solve, "clocks": clk.summary(),
         }
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
 
-def run_e2e(args, mesh, nnz):
+def run_e2e(args, mesh, fmt0, lam, mu):
+    """Same metric through the public API with host buffers (transfers timed)."""
     import torch
 
     from arcanefem_gb300 import fem
 
+    w = WORKLOADS[args.workload]
+    nnz = fmt0.nnzb * w["nb_dof"] ** 2
     coords_h = torch.from_numpy(mesh.coords).pin_memory()
     cells_h = torch.from_numpy(mesh.cells).pin_memory()
     vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
-    cols_h = torch.empty(nnz, dtype=torch.int32).pin_memory()
+    cols_h = torch.empty(fmt0.nnzb, dtype=torch.int32).pin_memory()
     rp_h = torch.empty(mesh.nb_node + 1, dtype=torch.int32).pin_memory()
     ctx = fem.Context()
     dco = torch.empty_like(coords_h, device="cuda")
     dce = torch.empty_like(cells_h, device="cuda")
-    ke = torch.empty(10 * mesh.nb_cell, dtype=torch.float64, device="cuda")
+    ke = torch.empty(fmt0.element_buffer_size(), dtype=torch.float64, device="cuda")
 
     def one():
         dco.copy_(coords_h, non_blocking=True)
         dce.copy_(cells_h, non_blocking=True)
-        f = fem.BSRFormat(ctx, fem.Mesh(3, dco, dce))
-        f.initialize(1)
+        f = fem.BSRFormat(ctx, fem.Mesh(mesh.dim, dco, dce))
+        f.initialize(w["nb_dof"])
         f.compute_sparsity()
-        f.element_matrices(ke)
+        f.element_matrices(ke, lam=lam, mu=mu)
         f.gather(ke)
         rp_h.copy_(f.row_ptr, non_blocking=True)
         cols_h.copy_(f.cols, non_blocking=True)
@@ -292,67 +325,119 @@ def run_e2e(args, mesh, nnz):
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / steps
     h2d = coords_h.numel() * 8 + cells_h.numel() * 4
-    d2h = nnz * 12 + (mesh.nb_node + 1) * 4
+    d2h = nnz * 8 + fmt0.nnzb * 4 + (mesh.nb_node + 1) * 4
     return {"value": nnz / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "ms_per_step": dt * 1e3, "steps": steps,
-            "includes": "H2D mesh, node->cell, sparsity, element matrices, gather, D2H CSR"}
+            "includes": "H2D mesh, node->cell, sparsity, element matrices, gather, D2H block CSR"}
 
 
-def cpu_baseline(mesh, fmt):
+def oracle_kind(args):
+    from oracle import oracle as O
+    w = WORKLOADS[args.workload]
+    if w["nb_dof"] == 3:
+        return O.ELASTICITY_TET4
+    return O.POISSON_TET4 if w["dim"] == 3 else O.POISSON_TRI3
+
+
+def cpu_baseline(args, mesh, fmt, lam, mu):
     """The oracle's node-wise assembly (CPU restatement of BSRFormat.h:473-537 with
-    _computeElementVectorTetra4Gpu) on all host cores, same mesh and sparsity."""
+    the reference element vectors) on all host cores, same mesh and sparsity."""
     import numpy as np
 
     from oracle import oracle as O
 
     threads = O.max_threads()
-    ptr = fmt.nc_ptr.cpu().numpy()
-    nc = fmt.nc_cell.cpu().numpy()
-    rp = fmt.row_ptr.cpu().numpy()
-    cols = fmt.cols.cpu().numpy()
-    nnz = int(rp[-1])
+    ptr, nc = fmt.nc_ptr.cpu().numpy(), fmt.nc_cell.cpu().numpy()
+    rp, cols = fmt.row_ptr.cpu().numpy(), fmt.cols.cpu().numpy()
+    nnz = fmt.nnzb * WORKLOADS[args.workload]["nb_dof"] ** 2
     t0 = time.perf_counter()
-    v = O.assemble(O.POISSON_TET4, mesh.coords, mesh.cells, ptr, nc, rp, cols, nb_threads=threads)
+    v = O.assemble(oracle_kind(args), mesh.coords, mesh.cells, ptr, nc, rp, cols, lam=lam, mu=mu, nb_threads=threads)
     dt = time.perf_counter() - t0
     gpu = fmt.values.cpu().numpy()
     err = float(np.max(np.abs(gpu - v) / np.maximum(np.abs(v), 1e-3 * np.abs(v).max())))
     return {"value": nnz / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"one full values assembly of the same mesh ({mesh.nb_cell} tets), {dt:.2f} s",
+            "sample": f"one full values assembly of the same mesh ({mesh.nb_cell} cells), {dt:.2f} s",
             "max_rel_diff_vs_gpu": err}
+
+
+def run_solve(args, ctx, mesh, fmt):
+    """Time to the target relative residual on the assembled system (RowColumn
+    elimination Dirichlet, source / body force), FP64 CG and mixed precision."""
+    import torch
+
+    from arcanefem_gb300 import fem
+
+    w = WORKLOADS[args.workload]
+    nd = mesh.nb_node * w["nb_dof"]
+    nodes = torch.as_tensor(mesh.groups[w["dirichlet"]], device="cuda")
+    res = {"target_relres": w["rtol"], "dirichlet": f"row-column elimination on {w['dirichlet']}"}
+    for prec in ("fp64", "mixed"):
+        # re-assemble: the transformation of the previous solve modified the values in place
+        ke = torch.empty(fmt.element_buffer_size(), dtype=torch.float64, device="cuda")
+        lam, mu = fem.lame(w["E"], w["nu"]) if w["nb_dof"] == 3 else (0.0, 0.0)
+        fmt.element_matrices(ke, lam=lam, mu=mu)
+        fmt.gather(ke)
+        del ke
+        ls = fem.DoFLinearSystem(ctx, nd)
+        fmt.to_linear_system(ls)
+        if w["nb_dof"] == 3:
+            fmt.rhs_body_force(w["body"], ls.rhs_variable())
+            for comp in range(3):
+                ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW_COLUMN, nodes, 3, comp, 0.0)
+        else:
+            fmt.rhs_constant_source(w["source"], ls.rhs_variable())
+            ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW_COLUMN, nodes, 1, 0, 0.0)
+        ls.apply_matrix_transformation()
+        ls.apply_rhs_transformation()
+        opt = fem.solver_options(rtol=w["rtol"], max_iter=20000,
+                                 precision=fem.PRECISION_MIXED if prec == "mixed" else fem.PRECISION_FP64,
+                                 inner_rtol=1e-3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        info = ls.solve(opt)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) * 1e3
+        res[prec] = {"solve_ms": info.solve_ms, "wall_ms": wall, "iterations": info.iterations,
+                     "refinements": info.refinements, "true_relres": info.relres, "status": info.status}
+        ls.close()
+    return res
 
 
 # ---------------------------------------------------------------------------
 def run_reference(args):
     """CPU reference arm: the oracle's restatement of the reference node-wise
-    assembly, all host threads, rank 0 only."""
+    assembly on all host threads, rank 0 only."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from arcanefem_gb300 import meshgen
+    from arcanefem_gb300 import fem
     from oracle import oracle as O
 
-    mesh = meshgen.unit_cube_tet(args.n, jitter=0.15, seed=args.seed)
+    w = WORKLOADS[args.workload]
+    mesh = make_mesh(args)
     ptr, nc, _ = O.node_cell(mesh.nb_node, mesh.cells)
     rp, cols = O.sparsity(mesh.nb_node, mesh.cells)
-    nnz = int(rp[-1])
+    nnz = int(rp[-1]) * w["nb_dof"] ** 2
+    lam, mu = fem.lame(w["E"], w["nu"]) if w["nb_dof"] == 3 else (0.0, 0.0)
     threads = O.max_threads()
+    kind = oracle_kind(args)
     for _ in range(args.warmup):
-        O.assemble(O.POISSON_TET4, mesh.coords, mesh.cells, ptr, nc, rp, cols, nb_threads=threads)
+        O.assemble(kind, mesh.coords, mesh.cells, ptr, nc, rp, cols, lam=lam, mu=mu, nb_threads=threads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        O.assemble(O.POISSON_TET4, mesh.coords, mesh.cells, ptr, nc, rp, cols, nb_threads=threads)
+        O.assemble(kind, mesh.coords, mesh.cells, ptr, nc, rp, cols, lam=lam, mu=mu, nb_threads=threads)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * sum(times) / len(times)
     value = nnz / (ms * 1e-3)
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    out = {"metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered mesh)",
            "config": config(args, 1), "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": f"full values assembly of the same mesh per step ({mesh.nb_cell} tets)"},
+                            "sample": f"full values assembly of the same mesh per step ({mesh.nb_cell} cells)"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "note": "reference (Arcane/HYPRE) cannot be built here; CPU restatement of its node-wise assembly"}
+           "note": "ArcaneFEM needs Arcane/.NET/MPI/HYPRE, absent here: CPU restatement of its node-wise assembly"}
     print(json.dumps(out), flush=True)
 
 

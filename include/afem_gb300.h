@@ -81,11 +81,13 @@ afem_status afem_device_fp64_fma_rate(afem_context ctx, double* gfma_per_s_h);
  * Node -> cell adjacency: Arcane's nodeCell() connectivity
  * (used at femutils/BSRFormat.h:411,428; NodeWiseCsrBiliAssembly.cc:179,188),
  * cells ascending per node.  nc_local_d[p] = position of the node inside
- * cell nc_cell_d[p].  Buffers: nc_ptr_d[nb_node+1], nc_cell_d and
- * nc_local_d[nb_cell*nodes_per_cell].  Deterministic. */
+ * cell nc_cell_d[p]; nc_inverse_d[cell*nodes_per_cell + i] = p, the incidence
+ * of (cell, local node i) in that list (nullable).  Buffers:
+ * nc_ptr_d[nb_node+1], nc_cell_d, nc_local_d and
+ * nc_inverse_d[nb_cell*nodes_per_cell].  Deterministic. */
 afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int nodes_per_cell,
                                  const int32_t* cell_nodes_d, int32_t* nc_ptr_d, int32_t* nc_cell_d,
-                                 uint8_t* nc_local_d);
+                                 uint8_t* nc_local_d, int32_t* nc_inverse_d);
 
 /* Column order of a row. */
 enum {
@@ -131,6 +133,7 @@ typedef struct {
   const int32_t* nc_cell_d;      /* [nb_cell*(dim+1)] */
   const uint8_t* nc_local_d;     /* [nb_cell*(dim+1)] */
   const uint8_t* nc_slot_d;      /* [nb_cell*(dim+1)^2] from afem_sparsity_cols */
+  const int32_t* nc_inverse_d;   /* [nb_cell*(dim+1)] from afem_node_cell_build */
 } afem_mesh_view;
 
 /* Scalar Poisson P1 stiffness, -div(k grad u): values_d[nnz] (CSR) receives
@@ -152,12 +155,14 @@ afem_status afem_assemble_elasticity_tet4(afem_context ctx, const afem_mesh_view
                                           double lambda, double mu, int layout, double* values_d);
 
 /* The two stages of the assemblies above, for callers that keep the element
- * matrices themselves (and to time the stages separately).  Stage 1 writes
- * the element matrices once per cell as planes ke_d[entry * nb_cell + cell]:
- * Poisson: the packed upper triangle of the (dim+1)^2 matrix (6 planes for
- * triangles, 10 for tetrahedra); elasticity: 78 planes (6 off-diagonal 3x3
- * blocks then 4 packed diagonal blocks).  Stage 2 sums, per row, the element
- * rows of the incident cells in increasing cell order (no atomics). */
+ * matrices themselves (and to time the stages separately).  Stage 1 computes
+ * each element matrix once per cell and stores its rows in incidence order:
+ * row i of cell c goes to incidence p = nc_inverse[c*npc + i], at
+ * ke_d[p*npc .. p*npc + npc-1] (Poisson, npc = dim+1 values) or
+ * ke_d[p*36 + a*12 + 3*m + b] (elasticity: the 3x12 row block, rows a,
+ * column node m, component b).  Size: nb_cell*npc*npc doubles (Poisson),
+ * nb_cell*144 (elasticity).  Stage 2 streams, per row, the contiguous
+ * element rows of the incident cells in increasing cell order (no atomics). */
 afem_status afem_element_matrices_poisson_p1(afem_context ctx, const afem_mesh_view* mesh,
                                              const double* cell_coeff_d, double* ke_d);
 afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,

@@ -39,7 +39,7 @@ def test_version_and_errors_without_gpu(L):
     assert L.afem_context_create(None, None) == 1
     assert b"null output" in L.afem_last_error()
     assert L.afem_ls_eliminate_row(None, 0, 0.0) == 1
-    assert L.afem_node_cell_build(None, 1, 1, 3, None, None, None, None) == 1
+    assert L.afem_node_cell_build(None, 1, 1, 3, None, None, None, None, None) == 1
     opt = _capi.SolverOptions()
     L.afem_solver_options_default(C.byref(opt))
     assert opt.rtol == 1e-7 and opt.max_iter == 1000 and opt.precond == _capi.PRECOND_JACOBI
