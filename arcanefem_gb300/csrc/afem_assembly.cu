@@ -22,6 +22,7 @@
 //   Diagonals use the zero row sum of a P1 stiffness: K_ii = -sum_{j!=i} K_ij.
 // Results agree with the reference formulas to rounding (tests check 1e-12).
 #include <algorithm>
+#include <mutex>
 
 #include "afem_internal.cuh"
 
@@ -531,3 +532,85 @@ afem_status afem_rhs_body_force_tet4(afem_context ctx, const afem_mesh_view* m, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of afem_assemble_poisson_p1.
+//
+// Some callers cannot let a library allocate device memory while they
+// assemble: a host framework that manages every device allocation through its
+// own pool and forbids any other cudaMalloc, or code that runs while a stream
+// is being captured (where allocating on that stream is not allowed).  This
+// entry point takes no context and calls no cudaMalloc / cudaFree / library
+// routine that allocates: the element rows live in a fixed file-scope device
+// array of kNoAllocRows doubles (32 MiB), which every GPU that loads the
+// library keeps until the process exits.  The caller still passes all inputs
+// and outputs.
+
+namespace afem {
+
+constexpr size_t kNoAllocRows = size_t(1) << 22;   // doubles: 262,144 tetrahedra or 466,033 triangles
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_rows[kNoAllocRows];
+
+// Device address of g_noalloc_rows, looked up once per device (host code
+// must not pass the symbol itself: that is a host-side stand-in).
+static double* g_noalloc_addr[kNoAllocMaxDevices] = {};
+static std::mutex g_noalloc_mutex;
+
+static afem_status noalloc_rows_address(int dev, double** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_rows);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_rows)", __FILE__, __LINE__);
+    g_noalloc_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return AFEM_OK;
+}
+
+template <class Kernel, class... Args>
+static afem_status launch_on(cudaStream_t s, Kernel k, unsigned grid, unsigned block, Args... args) {
+  k<<<grid, block, 0, s>>>(args...);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? AFEM_OK : cuda_fail(e, "kernel launch", __FILE__, __LINE__);
+}
+
+}  // namespace afem
+
+extern "C" afem_status afem_assemble_poisson_p1_noalloc(void* cuda_stream, const afem_mesh_view* m,
+                                                        const int32_t* row_ptr_d, const double* cell_coeff_d,
+                                                        double* values_d) {
+  AFEM_TRY(check_assembly(m, "afem_assemble_poisson_p1_noalloc"));
+  AFEM_CHECK_ARG(row_ptr_d && values_d, "afem_assemble_poisson_p1_noalloc: null buffer");
+  const size_t npc = m->dim + 1;
+  const size_t need = npc * npc * (size_t)m->nb_cell;
+  if (need > kNoAllocRows)
+    return fail(AFEM_ERR_BAD_ARG,
+                "afem_assemble_poisson_p1_noalloc: %d cells need %zu doubles of element rows, above the fixed "
+                "%zu (at most %zu tetrahedra or %zu triangles); use afem_assemble_poisson_p1",
+                m->nb_cell, need, kNoAllocRows, kNoAllocRows / 16, kNoAllocRows / 9);
+  int dev = 0, sms = 0;
+  AFEM_CUDA(cudaGetDevice(&dev));
+  AFEM_CHECK_ARG(dev >= 0 && dev < kNoAllocMaxDevices, "afem_assemble_poisson_p1_noalloc: device %d unsupported", dev);
+  AFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* rows = nullptr;
+  AFEM_TRY(noalloc_rows_address(dev, &rows));
+  // every element row is rewritten by the element kernel before the gather
+  // reads it, so nothing left by a previous call needs clearing
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
+  const int64_t eblocks = ((int64_t)m->nb_cell + 255) / 256;
+  const unsigned ge = (unsigned)std::max<int64_t>(1, std::min<int64_t>(eblocks, (int64_t)sms * 16));
+  const unsigned gg = (unsigned)((m->nb_node + kGatherBlock - 1) / kGatherBlock);
+  if (m->dim == 3) {
+    AFEM_TRY(launch_on(s, k_elem_poisson_tet, ge, 256, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                       cell_coeff_d, rows));
+    return launch_on(s, k_gather_scalar<4>, gg, kGatherBlock, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
+                     (const double*)rows, values_d);
+  }
+  AFEM_TRY(launch_on(s, k_elem_poisson_tri, ge, 256, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                     cell_coeff_d, rows));
+  return launch_on(s, k_gather_scalar<3>, gg, kGatherBlock, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
+                   (const double*)rows, values_d);
+}

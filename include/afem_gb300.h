@@ -172,6 +172,24 @@ afem_status afem_element_matrices_elasticity_tet4(afem_context ctx, const afem_m
 afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
                                         const double* ke_d, int layout, double* values_d);
 
+/* Allocation-free assembly of the scalar Poisson P1 matrix.  No counterpart
+ * in the reference: it serves callers that cannot let a library allocate
+ * device memory (a host framework that owns all device allocations through
+ * its own pool, or code running while a stream is captured into a CUDA
+ * graph).  Same arguments and results as afem_assemble_poisson_p1, but no
+ * context: the work runs on cuda_stream, and the element-row scratch is a
+ * fixed 32 MiB device array inside the library, held by every GPU that loads
+ * the library until the process exits.  Limit: 4,194,304 doubles of scratch,
+ * i.e. at most 262,144 tetrahedra or 466,033 triangles; larger meshes are
+ * rejected with AFEM_ERR_BAD_ARG.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) for that device: make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls that can overlap on the GPU (different streams, or different host
+ * threads without ordering) race and must be serialised by the caller. */
+afem_status afem_assemble_poisson_p1_noalloc(void* cuda_stream, const afem_mesh_view* mesh,
+                                             const int32_t* row_ptr_d, const double* cell_coeff_d,
+                                             double* values_d);
+
 /* Expand block-row pointers / block columns of a b x b BSR to scalar CSR
  * row_ptr_d[nb_node*b+1] and cols_d[nnzb*b*b] (the per-row value layout is
  * already CSR-ordered).  Replaces the host loops of BSRMatrix::toCsr
