@@ -10,7 +10,10 @@
 // p = nc_inverse[c][i] of the node -> cell lists, so that a node-wise kernel
 // then STREAMS, for each row, the contiguous element rows of its incident
 // cells (in increasing cell order) and adds them into the slots given by the
-// slot map -- no atomics, no column search, deterministic.
+// slot map -- no atomics, no column search, deterministic.  Each element row
+// holds the diagonal entry first, then the other cell nodes in increasing
+// local index (the order of the slot map), so that the gather keeps the
+// diagonal -- which every incident cell updates -- in a register.
 //
 // Element formulation (same quantities as modules/poisson/ElementMatrix.h:41-118
 // and femutils/ArcaneFemFunctionsGpu.h:76-128,241-281,414-535, regrouped):
@@ -75,7 +78,8 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double v[4]) {
 // ---------------------------------------------------------------------------
 // Element kernels (one thread per cell).
 
-// Poisson tetrahedron: 4 rows of 4 values, row i at er[inv[c][i] * 4].
+// Poisson tetrahedron: 4 rows of 4 values, row i at er[inv[c][i] * 4] as
+// (K_ii, then K_ij for j != i increasing).
 __global__ void __launch_bounds__(256) k_elem_poisson_tet(int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
                                                           const int32_t* __restrict__ inv,
@@ -89,13 +93,13 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tet(int nb_cell, const dou
     const double k12 = s * dot(cf[1], cf[2]), k13 = s * dot(cf[1], cf[3]), k23 = s * dot(cf[2], cf[3]);
     const int4 p = __ldg(reinterpret_cast<const int4*>(inv) + c);
     st4(er + 4 * (int64_t)p.x, -(k01 + k02 + k03), k01, k02, k03);
-    st4(er + 4 * (int64_t)p.y, k01, -(k01 + k12 + k13), k12, k13);
-    st4(er + 4 * (int64_t)p.z, k02, k12, -(k02 + k12 + k23), k23);
-    st4(er + 4 * (int64_t)p.w, k03, k13, k23, -(k03 + k13 + k23));
+    st4(er + 4 * (int64_t)p.y, -(k01 + k12 + k13), k01, k12, k13);
+    st4(er + 4 * (int64_t)p.z, -(k02 + k12 + k23), k02, k12, k23);
+    st4(er + 4 * (int64_t)p.w, -(k03 + k13 + k23), k03, k13, k23);
   }
 }
 
-// Poisson triangle: 3 rows of 3 values, row i at er[inv[c][i] * 3].
+// Poisson triangle: 3 rows of 3 values, row i at er[inv[c][i] * 3], diagonal first.
 __global__ void __launch_bounds__(256) k_elem_poisson_tri(int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
                                                           const int32_t* __restrict__ inv,
@@ -121,13 +125,14 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tri(int nb_cell, const dou
     double* r1 = er + 3 * (int64_t)__ldg(ip + 1);
     double* r2 = er + 3 * (int64_t)__ldg(ip + 2);
     r0[0] = -(k01 + k02); r0[1] = k01; r0[2] = k02;
-    r1[0] = k01; r1[1] = -(k01 + k12); r1[2] = k12;
-    r2[0] = k02; r2[1] = k12; r2[2] = -(k02 + k12);
+    r1[0] = -(k01 + k12); r1[1] = k01; r1[2] = k12;
+    r2[0] = -(k02 + k12); r2[1] = k02; r2[2] = k12;
   }
 }
 
 // Elasticity tetrahedron: for each local node n, its 3x12 row block
-// er[inv[c][n] * 36 + a * 12 + 3 m + b].  Block (n, m) rows a / columns b:
+// er[inv[c][n] * 36 + a * 12 + 3 q + b], column-node position q = 0 for n
+// itself, then the other local nodes in increasing order.  Block (n, m) rows a / columns b:
 //   K_ab = V [lambda dN_n/dx_a dN_m/dx_b + mu dN_n/dx_b dN_m/dx_a
 //             + mu delta_ab grad N_n . grad N_m]
 // which is modules/elasticity/ElementMatrix.h:216-301 (normal strain +
@@ -223,11 +228,14 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int nb_
     for (int n = 0; n < 4; ++n) {
       for (int k = lane; k < wcount * 18; k += 32) {
         const int t = k / 18, q = k - 18 * t;
-        const int pos = 2 * q, a = pos / 12, rem = pos - 12 * a, m = rem / 3, b = rem - 3 * m;
+        // row-block position pos = a * 12 + 3 * qn + b: column-node position qn is
+        // 0 for the row's own node n, then the other local nodes increasing
+        const int pos = 2 * q, a = pos / 12, rem = pos - 12 * a, qn = rem / 3, b = rem - 3 * qn;
+        const int m = qn == 0 ? n : qn - 1 + (qn - 1 >= n);
         const double* src = stage[wbase + t];
-        // pos and pos + 1 share (a, m) except when b == 2 (the pair straddles two column nodes)
         const double v0 = src[elast_packed(n, m, a, b)];
-        const int pos1 = pos + 1, a1 = pos1 / 12, rem1 = pos1 - 12 * a1, m1 = rem1 / 3, b1 = rem1 - 3 * m1;
+        const int pos1 = pos + 1, a1 = pos1 / 12, rem1 = pos1 - 12 * a1, qn1 = rem1 / 3, b1 = rem1 - 3 * qn1;
+        const int m1 = qn1 == 0 ? n : qn1 - 1 + (qn1 - 1 >= n);
         const double v1 = src[elast_packed(n, m1, a1, b1)];
         double* dst = er + 36 * (int64_t)stage_p[wbase + t][n] + pos;
         *reinterpret_cast<double2*>(dst) = make_double2(v0, v1);
@@ -256,6 +264,8 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int nb_node, con
     const int32_t p0 = __ldg(nc_ptr + row), p1 = __ldg(nc_ptr + row + 1);
     if (len <= kScalarRmax) {
       for (int s = 0; s < len; ++s) my[s * kGatherBlock] = 0.0;
+      // the diagonal (first value and slot byte of every incidence) in a register
+      double diag = 0.0;
       if constexpr (NPC == 4) {
         const double2* src = reinterpret_cast<const double2*>(er) + 2 * (int64_t)p0;
         const uint32_t* sp = reinterpret_cast<const uint32_t*>(nc_slot) + p0;
@@ -263,7 +273,7 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int nb_node, con
         for (int32_t p = p0; p < p1; ++p, src += 2, ++sp) {
           const double2 a = __ldg(src), b = __ldg(src + 1);
           const uint32_t w = __ldg(sp);
-          my[(w & 0xffu) * kGatherBlock] += a.x;
+          diag += a.x;
           my[((w >> 8) & 0xffu) * kGatherBlock] += a.y;
           my[((w >> 16) & 0xffu) * kGatherBlock] += b.x;
           my[(w >> 24) * kGatherBlock] += b.y;
@@ -273,10 +283,12 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int nb_node, con
         const uint8_t* sp = nc_slot + (int64_t)NPC * p0;
 #pragma unroll 2
         for (int32_t p = p0; p < p1; ++p, src += NPC, sp += NPC) {
+          diag += __ldg(src);
 #pragma unroll
-          for (int j = 0; j < NPC; ++j) my[__ldg(sp + j) * kGatherBlock] += __ldg(src + j);
+          for (int j = 1; j < NPC; ++j) my[__ldg(sp + j) * kGatherBlock] += __ldg(src + j);
         }
       }
+      if (p1 > p0) my[__ldg(nc_slot + (int64_t)NPC * p0) * kGatherBlock] = diag;
       for (int s = 0; s < len; ++s) values[rb + s] = my[s * kGatherBlock];
     } else {
       // long row: accumulate in this thread's own row of values
@@ -309,6 +321,7 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int nb_node,
       for (int s = 0; s < 3 * len; ++s) my[s * kGatherBlock] = 0.0;
       const double2* src = reinterpret_cast<const double2*>(er + 36 * (int64_t)p0 + 12 * a);
       const uint32_t* sp = reinterpret_cast<const uint32_t*>(nc_slot) + p0;
+      double self0 = 0.0, self1 = 0.0, self2 = 0.0;   // the row's own 3x3 block, in registers
       for (int32_t p = p0; p < p1; ++p, src += 18, ++sp) {
         const uint32_t w = __ldg(sp);
         double v[12];
@@ -318,13 +331,22 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int nb_node,
           v[2 * k] = q.x;
           v[2 * k + 1] = q.y;
         }
+        self0 += v[0];
+        self1 += v[1];
+        self2 += v[2];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
+        for (int m = 1; m < 4; ++m) {
           double* d = my + 3 * ((w >> (8 * m)) & 0xffu) * kGatherBlock;
           d[0] += v[3 * m];
           d[kGatherBlock] += v[3 * m + 1];
           d[2 * kGatherBlock] += v[3 * m + 2];
         }
+      }
+      if (p1 > p0) {
+        double* d = my + 3 * (__ldg(nc_slot + 4 * (int64_t)p0) & 0xffu) * kGatherBlock;
+        d[0] = self0;
+        d[kGatherBlock] = self1;
+        d[2 * kGatherBlock] = self2;
       }
       for (int x = 0; x < len; ++x)
 #pragma unroll

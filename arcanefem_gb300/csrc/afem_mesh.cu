@@ -126,9 +126,13 @@ __device__ __forceinline__ int stage_candidates(int n, int npc, const int32_t* _
 
 // Distinct candidates in increasing order: returns the row length; when
 // `fill`, also writes the columns (ascending or self-last) at cols[0..len)
-// and, per candidate i, its position in the row at slot[i].
-__device__ __forceinline__ int extract_row(int n, const int32_t* s, int m, bool fill, int len, int self_last,
-                                           int32_t* __restrict__ cols, uint8_t* __restrict__ slot) {
+// and the slot map.  Candidate i is cell node j = i % npc of incidence
+// k = i / npc; its slot byte goes to slot[k * npc + q] with q = 0 for the
+// row's own node (local index li = local[k]) and q = 1.. for the other cell
+// nodes in increasing local index -- the order of the element rows.
+__device__ __forceinline__ int extract_row(int n, const int32_t* s, int m, int npc, bool fill, int len,
+                                           int self_last, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
+                                           const uint8_t* __restrict__ local) {
   const int lane = threadIdx.x & 31;
   int32_t last = INT_MIN;
   int it = 0;
@@ -144,7 +148,11 @@ __device__ __forceinline__ int extract_row(int n, const int32_t* s, int m, bool 
       const int pos = self_last ? (mn < n ? it : (mn == n ? len - 1 : it - 1)) : it;
       if (lane == 0 && pos >= 0 && pos < len) cols[pos] = mn;   // a row_ptr that disagrees is reported, not written past
       for (int i = lane; i < m; i += 32)
-        if (s[i] == mn) slot[i] = (uint8_t)pos;
+        if (s[i] == mn) {
+          const int k = i / npc, j = i - k * npc, li = local[k];
+          const int q = j == li ? 0 : (j < li ? j + 1 : j);
+          slot[k * npc + q] = (uint8_t)pos;
+        }
     }
     last = mn;
     ++it;
@@ -161,7 +169,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, in
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int n = blockIdx.x * kWarpsPerBlock + w; n < nb_node; n += gridDim.x * kWarpsPerBlock) {
     const int m = stage_candidates(n, npc, cn, nc_ptr, nc_cell, sh[w]);
-    int len = m < 0 ? -1 : extract_row(n, sh[w], m, false, 0, 0, nullptr, nullptr);
+    int len = m < 0 ? -1 : extract_row(n, sh[w], m, npc, false, 0, 0, nullptr, nullptr, nullptr);
     if (lane == 0) {
       if (len < 0 || len > kMaxRowLen) {
         atomicOr(err, 2);
@@ -176,6 +184,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, in
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, int npc, const int32_t* __restrict__ cn,
                                                                   const int32_t* __restrict__ nc_ptr,
                                                                   const int32_t* __restrict__ nc_cell,
+                                                                  const uint8_t* __restrict__ nc_local,
                                                                   const int32_t* __restrict__ row_ptr, int self_last,
                                                                   int32_t* __restrict__ cols,
                                                                   uint8_t* __restrict__ slot, int* __restrict__ err) {
@@ -187,7 +196,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, i
     const int m = stage_candidates(n, npc, cn, nc_ptr, nc_cell, sh[w]);
     int got = -1;
     if (m >= 0)
-      got = extract_row(n, sh[w], m, true, len, self_last, cols + rb, slot + (int64_t)nc_ptr[n] * npc);
+      got = extract_row(n, sh[w], m, npc, true, len, self_last, cols + rb, slot + (int64_t)nc_ptr[n] * npc,
+                        nc_local + nc_ptr[n]);
     if (lane == 0 && got != len) atomicOr(err, 4);
     __syncwarp();
   }
@@ -291,12 +301,11 @@ afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int
 afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int32_t* cell_nodes_d,
                                const int32_t* nc_ptr_d, const int32_t* nc_cell_d, const uint8_t* nc_local_d,
                                const int32_t* row_ptr_d, int col_order, int32_t* cols_d, uint8_t* nc_slot_d) {
-  (void)nc_local_d;
   AFEM_CHECK_ARG(ctx, "afem_sparsity_cols: null context");
   AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4), "afem_sparsity_cols: bad sizes");
   AFEM_CHECK_ARG(col_order == AFEM_COLS_ASCENDING || col_order == AFEM_COLS_SELF_LAST,
                  "afem_sparsity_cols: bad col_order %d", col_order);
-  AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && row_ptr_d && cols_d && nc_slot_d,
+  AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && nc_local_d && row_ptr_d && cols_d && nc_slot_d,
                  "afem_sparsity_cols: null buffer");
   AFEM_TRY(scratch_reserve(ctx, 256));
   int* err;
@@ -305,7 +314,7 @@ afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int
   unsigned grid =
       (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock, (int64_t)ctx->sm_count * 8);
   AFEM_TRY(launch(ctx, k_row_fill, grid, kWarpsPerBlock * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d,
-                  row_ptr_d, col_order, cols_d, nc_slot_d, err));
+                  nc_local_d, row_ptr_d, col_order, cols_d, nc_slot_d, err));
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
   if (herr) return fail(AFEM_ERR_MESH, "afem_sparsity_cols: row_ptr does not match the mesh");

@@ -69,12 +69,16 @@ def test_sparsity_bit_exact(cuda_ctx, name, self_last):
     assert np.array_equal(f.row_ptr.cpu().numpy(), rp)
     assert np.array_equal(f.cols.cpu().numpy(), cols)
     assert f.nnzb == meshgen.nnz_formula(m)
-    # slot map: column at the slot is the cell node
+    # slot map: for each incidence, slot byte 0 is the row's own column, then the
+    # other cell nodes in increasing local index (the order of the element rows)
     slot = f.nc_slot.cpu().numpy().reshape(-1, m.npc)
-    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    ptr, nc, loc = O.node_cell(m.nb_node, m.cells)
     node_of = np.repeat(np.arange(m.nb_node), np.diff(ptr))
     got_cols = cols[rp[node_of][:, None] + slot]
-    assert np.array_equal(got_cols, m.cells[nc])
+    cell_nodes = m.cells[nc]
+    others = np.array([np.delete(row, li) for row, li in zip(cell_nodes, loc)])
+    expected = np.concatenate([node_of[:, None], others], axis=1)
+    assert np.array_equal(got_cols, expected)
 
 
 @pytest.mark.parametrize("name", list(MESHES))
