@@ -12,6 +12,7 @@ import os
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libafem_gb300.so")
 
 AFEM_OK = 0
+NOT_CONVERGED = 3
 STATUS_NAMES = {0: "AFEM_OK", 1: "AFEM_ERR_BAD_ARG", 2: "AFEM_ERR_OOM", 3: "AFEM_ERR_NOT_CONVERGED",
                 4: "AFEM_ERR_BREAKDOWN", 5: "AFEM_ERR_TIMEOUT", 6: "AFEM_ERR_CUDA", 7: "AFEM_ERR_MESH",
                 8: "AFEM_ERR_NOT_IMPLEMENTED", 9: "AFEM_ERR_NOT_FOUND"}
@@ -92,6 +93,18 @@ SIGNATURES = {
                                     C.POINTER(SolveInfo)]),
     "afem_ls_solve": (C.c_int, [_P, C.POINTER(SolverOptions), C.POINTER(SolveInfo)]),
     "afem_spmv_csr": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P]),
+    "afem_mpnn_create": (C.c_int, None),
+    "afem_mpnn_destroy": (C.c_int, [_P]),
+    "afem_mpnn_param_count": (C.c_int, [_P]),
+    "afem_mpnn_set_params": (C.c_int, [_P, _P]),
+    "afem_mpnn_get_params": (C.c_int, [_P, _P]),
+    "afem_mpnn_set_operator": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+    "afem_mpnn_forward": (C.c_int, [_P, C.c_int, _P, _P]),
+    "afem_mpnn_scalings": (C.c_int, [_P, C.c_int, _P]),
+    "afem_mpnn_gradients": (C.c_int, [_P, C.c_int, _P, _P, _P, C.POINTER(C.c_double)]),
+    "afem_mpnn_train_step": (C.c_int, [_P, C.c_int, _P, _P, C.c_float, C.POINTER(C.c_double)]),
+    "afem_fcg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.POINTER(SolverOptions),
+                                 C.POINTER(SolveInfo)]),
 }
 
 _lib = None
@@ -108,7 +121,8 @@ def lib():
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)
             fn.restype = res
-            fn.argtypes = args
+            if args is not None:      # None: variadic-looking signatures declared at the call site
+                fn.argtypes = args
         _lib = L
     return _lib
 

@@ -32,9 +32,9 @@ afem_status cuda_fail(cudaError_t e, const char* what, const char* file, int lin
     if (!(cond)) return ::afem::fail(AFEM_ERR_BAD_ARG, __VA_ARGS__);          \
   } while (0)
 
-#define AFEM_TRY(expr)                                                        \
+#define AFEM_TRY(...)                                                         \
   do {                                                                        \
-    afem_status afem_s_ = (expr);                                             \
+    afem_status afem_s_ = (__VA_ARGS__);                                      \
     if (afem_s_ != AFEM_OK) return afem_s_;                                   \
   } while (0)
 
@@ -107,6 +107,10 @@ afem_status read_scalar(afem_context ctx, const T* d, T* h) {
   *h = *reinterpret_cast<T*>(ctx->pinned);
   return AFEM_OK;
 }
+
+// y = A x (FP64 CSR), lanes per row chosen from nnz / n (afem_solver.cu).
+afem_status spmv_fp64(afem_context ctx, int n, int64_t nnz, const int32_t* rp, const int32_t* cols,
+                      const double* vals, const double* x, double* y);
 
 // Exclusive scan of int32 counts into int32 offsets out[0..n] (out[n] = total),
 // three-phase (tile sums, scan of sums, add-back), deterministic.

@@ -1,0 +1,126 @@
+// Shared pieces of the Krylov solvers (CG, mixed-precision CG, flexible CG
+// with the learned preconditioner): G-lanes-per-row CSR dot products,
+// deterministic last-block reductions, the lanes-per-row choice, and CUDA
+// graph capture of a chunk of iterations.
+#pragma once
+#include <type_traits>
+
+#include "afem_internal.cuh"
+
+namespace afem {
+
+constexpr int kSolveBlock = 256;
+
+// ---------------------------------------------------------------------------
+// SpMV: G lanes per row, fixed-order reduction.
+template <int G, class T, class V>
+__device__ __forceinline__ double row_dot(int row, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                          const T* __restrict__ vals, const V* __restrict__ x, int lane) {
+  double s = 0.0;
+  const int32_t e = __ldg(rp + row + 1);
+  for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s += (double)__ldg(vals + k) * (double)__ldg(x + __ldg(cols + k));
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
+// FP32 row dot product accumulated in FP32 (inner solve).
+template <int G>
+__device__ __forceinline__ float row_dot_f(int row, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                           const float* __restrict__ vals, const float* __restrict__ x, int lane) {
+  float s = 0.f;
+  const int32_t e = __ldg(rp + row + 1);
+  for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s = fmaf(__ldg(vals + k), __ldg(x + __ldg(cols + k)), s);
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Last-block finalize helper: every block publishes partials[blockIdx.x * W + w];
+// returns true in the (single) last block, after which all partials are visible.
+__device__ __forceinline__ bool last_block(unsigned int* ticket) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int t = atomicAdd(ticket, 1u);
+    is_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+// Fixed-order sum of partials[k * W + w], k < nparts (valid in thread 0).
+__device__ __forceinline__ double reduce_partials(const double* partials, int nparts, int W, int w, double* sh) {
+  double s = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += ((volatile const double*)partials)[(int64_t)k * W + w];
+  return block_sum(s, sh);
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+inline int lanes_per_row(int n, int64_t nnz) {
+  double avg = n > 0 ? (double)nnz / n : 1.0;
+  if (avg <= 6) return 4;
+  if (avg <= 20) return 8;
+  if (avg <= 48) return 16;
+  return 32;
+}
+
+template <class F>
+afem_status dispatch_g(int G, F&& f) {
+  switch (G) {
+    case 4: return f(std::integral_constant<int, 4>{});
+    case 8: return f(std::integral_constant<int, 8>{});
+    case 16: return f(std::integral_constant<int, 16>{});
+    default: return f(std::integral_constant<int, 32>{});
+  }
+}
+
+template <class Kernel, class... Args>
+inline afem_status launch_s(afem_context ctx, cudaStream_t s, Kernel k, unsigned grid, unsigned block, Args... args) {
+  k<<<grid, block, 0, s>>>(args...);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch", __FILE__, __LINE__);
+  ++ctx->launches;
+  return AFEM_OK;
+}
+
+struct GraphChunk {
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  ~GraphChunk() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+// Capture `body(stream)` once into an executable graph.
+template <class Body>
+inline afem_status capture(afem_context ctx, GraphChunk& g, Body&& body) {
+  cudaStream_t cs;
+  AFEM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(cs);
+    return cuda_fail(e, "cudaStreamBeginCapture", __FILE__, __LINE__);
+  }
+  int64_t before = ctx->launches;
+  afem_status st = body(cs);
+  cudaError_t e2 = cudaStreamEndCapture(cs, &g.graph);
+  cudaStreamDestroy(cs);
+  ctx->launches = before;  // captured kernels are counted when the graph runs
+  if (st != AFEM_OK) return st;
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture", __FILE__, __LINE__);
+  AFEM_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+  return AFEM_OK;
+}
+
+// ||b - A x|| / ||b|| in FP64 (rows with skip[i] != 0 left out; skip may be null).
+afem_status true_relres(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                        int64_t nnz, const double* b, const double* x, const uint8_t* skip, double* relres);
+
+}  // namespace afem

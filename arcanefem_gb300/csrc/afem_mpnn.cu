@@ -1,0 +1,1342 @@
+// Learned preconditioner: an additive multilevel preconditioner whose level
+// scalings are predicted by a message-passing network (MPNN) on the mesh
+// graph, trained on the GPU and applied inside flexible CG.
+//
+// Preconditioner (linear and symmetric positive definite in r):
+//   M r = sum_{l=0}^{L-1} Q_l diag(d_l) Q_l^T r,   Q_0 = I, Q_{l+1} = Q_l P_l,
+// P_l the bilinear prolongation of the structured hierarchy (the additive
+// multilevel / BPX form), evaluated as one down sweep t_{l+1} = P_l^T t_l and
+// one up sweep w_l = d_l t_l + P_l w_{l+1}.  The scalings are
+//   d_l = base_l * exp(c_l),  base_l = (R..R 1) / (R..R diag A),
+// so c = 0 is multilevel diagonal scaling; the network predicts c_l per node.
+// The caller's P_l should vanish on Dirichlet nodes (rows of fine and columns
+// of coarse boundary nodes): coarse functions that violate the boundary
+// condition cost a factor ~2 in condition number per level.
+//
+// Network (message-passing layers of width 64, BF16 weights and activations,
+// FP32 accumulation) on the coefficient features x0 = [1, log(A_ii / mean)]:
+//   a = relu(x0 W_in + b_in)
+//   o_l = relu(h_l W1_l + (S_l h_l) W2_l + b_l),  h_0 = a,  h_{l+1} = R_l o_l
+//   (levels past the last layer: o_l = h_l)
+//   c_l = o_l . w_l + beta_l                      (one head per level)
+// S_0 is the matrix graph with weights -A_ij / sqrt(A_ii A_jj); S_l (l >= 1),
+// R_l, P_l come from the caller (CSR).  It runs once per operator and per
+// training step; the per-iteration application is the two sweeps above.
+//
+// GEMMs (all K = 64): mma.sync m16n8k16 BF16 -> FP32 tensor-core tiles; the
+// weight gradients X^T G use ldmatrix.trans.  Aggregation / transfers: CSR
+// SpMM over 64-wide rows.  Training: the mean relative energy norm of the
+// error propagation, ||(I - M A) e||_A^2 / ||e||_A^2 over (r = A e, e) pairs
+// (A in FP32), Adam on FP32 master weights.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "afem_krylov.cuh"
+
+namespace afem {
+
+constexpr int kF = 64;                 // hidden width
+constexpr int kGemmRows = 128;         // rows per GEMM block (8 warps x 16)
+constexpr int kMaxLevels = 12;
+constexpr int kMaxBatch = 64;
+
+typedef __nv_bfloat16 bf16;
+
+// ---------------------------------------------------------------------------
+// Tensor-core helpers (PTX mma.sync / ldmatrix).
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void ldmatrix_x4_trans(uint32_t r[4], const void* smem_row) {
+  unsigned addr = (unsigned)__cvta_generic_to_shared(smem_row);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// ---------------------------------------------------------------------------
+// Row GEMM: Y[M x 64] = act( X1 B1 + X2 B2 + bias ), X in BF16 (row-major,
+// 64 columns), B given transposed as Bt[n][k] (64 x 64 BF16).  Each warp
+// computes 16 rows x 64 columns (8 n-tiles x 4 k-steps of m16n8k16).
+// Output BF16 (Yb) and/or FP32 (Yf, optionally accumulated).
+template <bool TWO, bool RELU>
+__global__ void __launch_bounds__(256) k_row_gemm(int M, const bf16* __restrict__ X1, const bf16* __restrict__ B1t,
+                                                  const bf16* __restrict__ X2, const bf16* __restrict__ B2t,
+                                                  const float* __restrict__ bias, bf16* __restrict__ Yb,
+                                                  float* __restrict__ Yf, int accumulate) {
+  __shared__ uint32_t sB1[kF * kF / 2];
+  __shared__ uint32_t sB2[TWO ? kF * kF / 2 : 1];
+  for (int i = threadIdx.x; i < kF * kF / 2; i += blockDim.x) {
+    sB1[i] = reinterpret_cast<const uint32_t*>(B1t)[i];
+    if (TWO) sB2[i] = reinterpret_cast<const uint32_t*>(B2t)[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  for (int64_t r0 = (int64_t)blockIdx.x * kGemmRows + warp * 16; r0 < M; r0 += (int64_t)gridDim.x * kGemmRows) {
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      const float b0 = bias ? bias[nt * 8 + 2 * t] : 0.f, b1 = bias ? bias[nt * 8 + 2 * t + 1] : 0.f;
+      acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
+    }
+    const int64_t ra = r0 + g, rb = r0 + g + 8;
+    const bool va = ra < M, vb = rb < M;
+#pragma unroll
+    for (int src = 0; src < (TWO ? 2 : 1); ++src) {
+      const uint32_t* X = reinterpret_cast<const uint32_t*>(src == 0 ? X1 : X2);
+      const uint32_t* sB = src == 0 ? sB1 : sB2;
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+        const int kw = ks * 8 + t;   // 32-bit word index of columns (16 ks + 2 t)
+        uint32_t a[4];
+        a[0] = va ? __ldg(X + ra * 32 + kw) : 0u;
+        a[1] = vb ? __ldg(X + rb * 32 + kw) : 0u;
+        a[2] = va ? __ldg(X + ra * 32 + kw + 4) : 0u;
+        a[3] = vb ? __ldg(X + rb * 32 + kw + 4) : 0u;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+          uint32_t b[2];
+          b[0] = sB[(nt * 8 + g) * 32 + kw];
+          b[1] = sB[(nt * 8 + g) * 32 + kw + 4];
+          mma_bf16(acc[nt], a, b);
+        }
+      }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      float c0 = acc[nt][0], c1 = acc[nt][1], c2 = acc[nt][2], c3 = acc[nt][3];
+      if (RELU) {
+        c0 = fmaxf(c0, 0.f); c1 = fmaxf(c1, 0.f); c2 = fmaxf(c2, 0.f); c3 = fmaxf(c3, 0.f);
+      }
+      const int col = nt * 8 + 2 * t;
+      if (Yb) {
+        if (va) reinterpret_cast<uint32_t*>(Yb)[ra * 32 + col / 2] = pack_bf16(c0, c1);
+        if (vb) reinterpret_cast<uint32_t*>(Yb)[rb * 32 + col / 2] = pack_bf16(c2, c3);
+      }
+      if (Yf) {
+        if (va) {
+          float2* p = reinterpret_cast<float2*>(Yf + ra * kF + col);
+          float2 o = accumulate ? *p : make_float2(0.f, 0.f);
+          *p = make_float2(o.x + c0, o.y + c1);
+        }
+        if (vb) {
+          float2* p = reinterpret_cast<float2*>(Yf + rb * kF + col);
+          float2 o = accumulate ? *p : make_float2(0.f, 0.f);
+          *p = make_float2(o.x + c2, o.y + c3);
+        }
+      }
+    }
+  }
+}
+
+// Weight gradient partials: P_blk[64 x 64] = X[rows of blk]^T G[rows of blk],
+// X and G BF16 [M x 64].  8 warps: warp w owns output rows 16 (w % 4) .. +16
+// and columns 32 (w / 4) .. +32.  A = X^T and B = G fragments come from
+// shared-memory tiles through ldmatrix.trans.
+constexpr int kDwRows = 128;
+constexpr int kDwPitch = kF + 8;   // padded row (bf16) against bank conflicts
+
+__global__ void __launch_bounds__(256) k_dw_partial(int M, const bf16* __restrict__ X, const bf16* __restrict__ G,
+                                                    float* __restrict__ partial) {
+  __shared__ __align__(16) bf16 sX[kDwRows * kDwPitch];
+  __shared__ __align__(16) bf16 sG[kDwRows * kDwPitch];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int i0 = 16 * (warp & 3), j0 = 32 * (warp >> 2);
+  float acc[4][4] = {};
+  for (int64_t base = (int64_t)blockIdx.x * kDwRows; base < M; base += (int64_t)gridDim.x * kDwRows) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kDwRows * (kF / 8); e += blockDim.x) {
+      const int r = e / (kF / 8), c8 = (e % (kF / 8)) * 8;
+      const int64_t gr = base + r;
+      uint4 xv = make_uint4(0, 0, 0, 0), gv = make_uint4(0, 0, 0, 0);
+      if (gr < M) {
+        xv = *reinterpret_cast<const uint4*>(X + gr * kF + c8);
+        gv = *reinterpret_cast<const uint4*>(G + gr * kF + c8);
+      }
+      *reinterpret_cast<uint4*>(sX + r * kDwPitch + c8) = xv;
+      *reinterpret_cast<uint4*>(sG + r * kDwPitch + c8) = gv;
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int k0 = 0; k0 < kDwRows; k0 += 16) {
+      // A = X^T (16 i x 16 k): blocks (i0..+8, k0..+8), (i0+8.., k0..), (i0.., k0+8..), (i0+8.., k0+8..)
+      uint32_t a[4];
+      {
+        const int q = lane >> 3, rr = lane & 7;
+        const int krow = k0 + rr + ((q >> 1) ? 8 : 0), icol = i0 + ((q & 1) ? 8 : 0);
+        ldmatrix_x4_trans(a, sX + krow * kDwPitch + icol);
+      }
+#pragma unroll
+      for (int np = 0; np < 2; ++np) {
+        // B = G (16 k x 16 j) for two n-tiles: blocks (k0.., j), (k0+8.., j), (k0.., j+8), (k0+8.., j+8)
+        uint32_t b4[4];
+        const int q = lane >> 3, rr = lane & 7;
+        const int krow = k0 + rr + ((q & 1) ? 8 : 0), jcol = j0 + 16 * np + ((q >> 1) ? 8 : 0);
+        ldmatrix_x4_trans(b4, sG + krow * kDwPitch + jcol);
+        uint32_t b0[2] = {b4[0], b4[1]}, b1[2] = {b4[2], b4[3]};
+        mma_bf16(acc[2 * np], a, b0);
+        mma_bf16(acc[2 * np + 1], a, b1);
+      }
+    }
+  }
+  float* out = partial + (int64_t)blockIdx.x * kF * kF;
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+    const int col = j0 + nt * 8 + 2 * t;
+    out[(i0 + g) * kF + col] = acc[nt][0];
+    out[(i0 + g) * kF + col + 1] = acc[nt][1];
+    out[(i0 + g + 8) * kF + col] = acc[nt][2];
+    out[(i0 + g + 8) * kF + col + 1] = acc[nt][3];
+  }
+}
+
+// out[e] (+)= sum_b partial[b][e], fixed order (deterministic).
+__global__ void k_sum_partials(int nparts, int nelem, const float* __restrict__ partial, float* __restrict__ out,
+                               int accumulate) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nparts; ++b) s += partial[(int64_t)b * nelem + e];
+    out[e] = accumulate ? out[e] + s : s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CSR SpMM over 64-wide rows, one warp per row, lane = 2 features.
+// Y[b][row] = (acc ? Y : 0) + sum_k w_k X[b][col_k] (+ Z[b][row])  ; batch in grid.y.
+template <class TIn, class TOut>
+__global__ void k_spmm(int nrow, int ncol_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                       const float* __restrict__ w, const TIn* __restrict__ X, const bf16* __restrict__ Z,
+                       TOut* __restrict__ Y, int accumulate) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = blockIdx.y;
+  const TIn* Xb = X + b * (int64_t)ncol_rows * kF;
+  TOut* Yb = Y + b * (int64_t)nrow * kF;
+  const bf16* Zb = Z ? Z + b * (int64_t)nrow * kF : nullptr;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrow; row += (gridDim.x * blockDim.x) >> 5) {
+    float s0 = 0.f, s1 = 0.f;
+    for (int32_t k = rp[row]; k < rp[row + 1]; ++k) {
+      const float wk = w[k];
+      const int64_t c = cols[k];
+      float x0, x1;
+      if constexpr (sizeof(TIn) == 2) {
+        const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(Xb + c * kF)[lane];
+        x0 = __low2float(v);
+        x1 = __high2float(v);
+      } else {
+        const float2 v = reinterpret_cast<const float2*>(Xb + c * kF)[lane];
+        x0 = v.x;
+        x1 = v.y;
+      }
+      s0 = fmaf(wk, x0, s0);
+      s1 = fmaf(wk, x1, s1);
+    }
+    if (Zb) {
+      const __nv_bfloat162 z = reinterpret_cast<const __nv_bfloat162*>(Zb + (int64_t)row * kF)[lane];
+      s0 += __low2float(z);
+      s1 += __high2float(z);
+    }
+    if constexpr (sizeof(TOut) == 2) {
+      reinterpret_cast<__nv_bfloat162*>(Yb + (int64_t)row * kF)[lane] = __floats2bfloat162_rn(s0, s1);
+    } else {
+      float2* p = reinterpret_cast<float2*>(Yb + (int64_t)row * kF) + lane;
+      float2 o = accumulate ? *p : make_float2(0.f, 0.f);
+      *p = make_float2(o.x + s0, o.y + s1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small per-node kernels.
+
+// Level-0 graph weights from A: w_ij = -A_ij / sqrt(A_ii A_jj), 0 on the diagonal.
+__global__ void k_level0_weights(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                 const double* __restrict__ vals, const double* __restrict__ diag,
+                                 float* __restrict__ w) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double di = diag[i];
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+      const int32_t j = cols[k];
+      w[k] = (j == i) ? 0.f : (float)(-vals[k] / sqrt(di * diag[j]));
+    }
+  }
+}
+
+__global__ void k_diag(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                       const double* __restrict__ vals, double* __restrict__ diag, float* __restrict__ diag32,
+                       float* __restrict__ ones) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double d = 1.0;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+      if (cols[k] == i) {
+        d = vals[k];
+        break;
+      }
+    d = d > 0 ? d : 1.0;
+    diag[i] = d;
+    diag32[i] = (float)d;
+    ones[i] = 1.f;
+  }
+}
+
+// coefficient features x0 = [1, log d - mean log d] and the input layer a = relu(x0 W_in + b_in)
+__global__ void k_input_layer(int n, const double* __restrict__ diag, double mean_log, const float* __restrict__ Win,
+                              const float* __restrict__ bin, float* __restrict__ x0, bf16* __restrict__ a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float f0 = 1.f;
+    const float f1 = (float)(log(diag[i]) - mean_log);
+    x0[2 * (int64_t)i] = f0;
+    x0[2 * (int64_t)i + 1] = f1;
+    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(a + (int64_t)i * kF);
+#pragma unroll 8
+    for (int c = 0; c < kF; c += 2) {
+      const float y0 = fmaxf(f0 * Win[c] + f1 * Win[kF + c] + bin[c], 0.f);
+      const float y1 = fmaxf(f0 * Win[c + 1] + f1 * Win[kF + c + 1] + bin[c + 1], 0.f);
+      dst[c / 2] = __floats2bfloat162_rn(y0, y1);
+    }
+  }
+}
+
+// level head: c = o . w + beta ; d = base * exp(clamp(c))
+__global__ void k_head(int n, const bf16* __restrict__ o, const float* __restrict__ w, const float* __restrict__ base,
+                       float* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const __nv_bfloat162* row = reinterpret_cast<const __nv_bfloat162*>(o + (int64_t)i * kF);
+    float acc = w[kF];
+#pragma unroll 8
+    for (int c = 0; c < kF / 2; ++c) {
+      const __nv_bfloat162 v = row[c];
+      acc = fmaf(__low2float(v), w[2 * c], acc);
+      acc = fmaf(__high2float(v), w[2 * c + 1], acc);
+    }
+    d[i] = base[i] * __expf(fminf(fmaxf(acc, -20.f), 20.f));
+  }
+}
+
+// scalar CSR SpMV over a batch (grid.y): y[b][i] = (d ? d[i] t[b][i] : 0) + sum_k w_k x[b][col_k]
+__global__ void k_sweep(int nrow, int ncol, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                        const float* __restrict__ w, const float* __restrict__ x, const float* __restrict__ d,
+                        const float* __restrict__ t, float* __restrict__ y) {
+  const int64_t b = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nrow; i += gridDim.x * blockDim.x) {
+    float s = d ? d[i] * t[b * nrow + i] : 0.f;
+    if (x)
+      for (int32_t k = rp[i]; k < rp[i + 1]; ++k) s = fmaf(w[k], x[b * ncol + cols[k]], s);
+    y[b * nrow + i] = s;
+  }
+}
+
+// y = x / z elementwise (base_l = count_l / diag_l)
+__global__ void k_ratio(int n, const float* __restrict__ x, const float* __restrict__ z, float* __restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = z[i] > 0.f ? x[i] / z[i] : 0.f;
+}
+
+// per-sample energy sums: sums[b*4+0] += e . (A e), sums[b*4+1] += (e - z) . (A (e - z))
+__global__ void k_energy_sums(int n, const float* __restrict__ z, const float* __restrict__ e,
+                              const float* __restrict__ Ae, const float* __restrict__ Av, double* __restrict__ sums) {
+  __shared__ double sh[32];
+  const int64_t b = blockIdx.y;
+  double ee = 0, vv = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int64_t k = b * n + i;
+    const double ei = e[k];
+    ee += ei * (double)Ae[k];
+    vv += (ei - (double)z[k]) * (double)Av[k];
+  }
+  ee = block_sum(ee, sh);
+  vv = block_sum(vv, sh);
+  if (threadIdx.x == 0) {
+    atomicAdd(&sums[b * 4], ee);
+    atomicAdd(&sums[b * 4 + 1], vv);
+  }
+}
+
+// v = e - z
+__global__ void k_sub(int64_t n, const float* __restrict__ e, const float* __restrict__ z, float* __restrict__ v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = e[i] - z[i];
+}
+
+// dL/dz = -2 A (e - z) / (e . A e  B), in place over Av
+__global__ void k_energy_grad(int n, int batch, const double* __restrict__ sums, float* __restrict__ Av) {
+  const int64_t b = blockIdx.y;
+  const double ee = sums[b * 4] > 0 ? sums[b * 4] : 1e-300;
+  const float scale = (float)(-2.0 / (ee * batch));
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) Av[b * n + i] *= scale;
+}
+
+// dc_l[i] = d_l[i] * sum_b t_l[b][i] s_l[b][i]   (dL/dc through d = base exp(c))
+__global__ void k_dc(int n, int batch, const float* __restrict__ t, const float* __restrict__ s,
+                     const float* __restrict__ d, float* __restrict__ dc) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int b = 0; b < batch; ++b) acc = fmaf(t[(int64_t)b * n + i], s[(int64_t)b * n + i], acc);
+    dc[i] = acc * d[i];
+  }
+}
+
+// head backward: d o = dc (x) w (FP32 [n][64]); partials of dw = sum_i dc_i o_i and dbeta = sum_i dc_i
+__global__ void k_head_backward(int n, const float* __restrict__ dc, const bf16* __restrict__ o,
+                                const float* __restrict__ w, float* __restrict__ dO, float* __restrict__ part) {
+  __shared__ float sh[kF + 1][8];
+  float acc[kF + 1];
+#pragma unroll
+  for (int c = 0; c <= kF; ++c) acc[c] = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float g = dc[i];
+    const __nv_bfloat162* row = reinterpret_cast<const __nv_bfloat162*>(o + (int64_t)i * kF);
+    float2* drow = reinterpret_cast<float2*>(dO + (int64_t)i * kF);
+#pragma unroll
+    for (int c = 0; c < kF / 2; ++c) {
+      const __nv_bfloat162 v = row[c];
+      acc[2 * c] = fmaf(g, __low2float(v), acc[2 * c]);
+      acc[2 * c + 1] = fmaf(g, __high2float(v), acc[2 * c + 1]);
+      drow[c] = make_float2(g * w[2 * c], g * w[2 * c + 1]);
+    }
+    acc[kF] += g;
+  }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c <= kF; ++c) {
+    float v = acc[c];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) sh[c][wp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x <= kF) {
+    float s = 0.f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[threadIdx.x][k];
+    part[(int64_t)blockIdx.x * (kF + 1) + threadIdx.x] = s;
+  }
+}
+
+// G = dO (x) [O > 0] in BF16, and per-block column sums (db)
+__global__ void k_relu_grad(int64_t M, const float* __restrict__ dO, const bf16* __restrict__ O,
+                            bf16* __restrict__ G, float* __restrict__ db_part) {
+  __shared__ float sh[kF][8];
+  float acc0 = 0.f, acc1 = 0.f;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < M;
+       row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const __nv_bfloat162 o = reinterpret_cast<const __nv_bfloat162*>(O + row * kF)[lane];
+    const float2 d = reinterpret_cast<const float2*>(dO + row * kF)[lane];
+    const float g0 = __low2float(o) > 0.f ? d.x : 0.f, g1 = __high2float(o) > 0.f ? d.y : 0.f;
+    reinterpret_cast<__nv_bfloat162*>(G + row * kF)[lane] = __floats2bfloat162_rn(g0, g1);
+    acc0 += g0;
+    acc1 += g1;
+  }
+  sh[2 * lane][w] = acc0;
+  sh[2 * lane + 1][w] = acc1;
+  __syncthreads();
+  if (threadIdx.x < kF) {
+    float s = 0.f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[threadIdx.x][k];
+    db_part[(int64_t)blockIdx.x * kF + threadIdx.x] = s;
+  }
+}
+
+// input layer backward: G_in = da (x) [a > 0]; partials of dW_in = x0^T G_in (2 x 64) and db_in
+__global__ void k_input_backward(int64_t M, const float* __restrict__ da, const bf16* __restrict__ a,
+                                 const float* __restrict__ x0, float* __restrict__ part) {
+  __shared__ float sh[3 * kF][8];
+  float acc[3][2] = {};
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < M;
+       row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const __nv_bfloat162 av = reinterpret_cast<const __nv_bfloat162*>(a + row * kF)[lane];
+    const float2 d = reinterpret_cast<const float2*>(da + row * kF)[lane];
+    const float g0 = __low2float(av) > 0.f ? d.x : 0.f, g1 = __high2float(av) > 0.f ? d.y : 0.f;
+    const float f0 = x0[row * 2], f1 = x0[row * 2 + 1];
+    acc[0][0] += f0 * g0; acc[0][1] += f0 * g1;
+    acc[1][0] += f1 * g0; acc[1][1] += f1 * g1;
+    acc[2][0] += g0;      acc[2][1] += g1;
+  }
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    sh[q * kF + 2 * lane][w] = acc[q][0];
+    sh[q * kF + 2 * lane + 1][w] = acc[q][1];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 3 * kF; e += blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[e][k];
+    part[(int64_t)blockIdx.x * 3 * kF + e] = s;
+  }
+}
+
+// Adam on the FP32 master parameters.
+__global__ void k_adam(int n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, float lr, float b1, float b2, float eps, float c1, float c2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float a = b1 * m1[i] + (1 - b1) * gi;
+    const float v = b2 * m2[i] + (1 - b2) * gi * gi;
+    m1[i] = a;
+    m2[i] = v;
+    p[i] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
+  }
+}
+
+// W [k][n] FP32 -> Wt [n][k] and W [k][n] as BF16 (the two GEMM operand forms)
+__global__ void k_weights_bf16(int nmat, const float* __restrict__ W, bf16* __restrict__ Wt, bf16* __restrict__ Wn) {
+  const int total = nmat * kF * kF;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int m = e / (kF * kF), r = e % (kF * kF), k = r / kF, n = r % kF;
+    const bf16 v = __float2bfloat16_rn(W[e]);
+    Wt[m * kF * kF + n * kF + k] = v;
+    Wn[e] = v;
+  }
+}
+
+__global__ void k_f64_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+}  // namespace afem
+
+// ---------------------------------------------------------------------------
+// Network object.
+
+using namespace afem;
+
+namespace afem {
+struct FcgWork;
+}
+
+struct CsrLevel {
+  int nrow = 0, ncol = 0;
+  int32_t* rp = nullptr;
+  int32_t* cols = nullptr;
+  float* w = nullptr;
+  int64_t nnz = 0;
+};
+
+struct afem_mpnn_s {
+  afem_context ctx = nullptr;
+  int L = 0;                     // levels of the hierarchy (one head each)
+  int NL = 0;                    // message-passing layers, on levels 0 .. NL-1
+  int n[kMaxLevels] = {};
+  CsrLevel S[kMaxLevels];        // aggregation graph per level (S[0] weights from A)
+  CsrLevel R[kMaxLevels];        // restriction l -> l+1
+  CsrLevel Rt[kMaxLevels];       // its transpose (backward)
+  CsrLevel P[kMaxLevels];        // prolongation l+1 -> l
+  CsrLevel Pt[kMaxLevels];       // its transpose (down sweep)
+  int max_batch = 1;
+  // parameters (FP32 master, flat): W_in[2][64], b_in[64], per layer W1, W2 [64][64], b[64],
+  // then per level a head w[64], beta.  Levels l >= NL have no layer: o_l = h_l = R o_{l-1}.
+  int nparam = 0;
+  float* params = nullptr;
+  float* grads = nullptr;
+  float* adam_m = nullptr;
+  float* adam_v = nullptr;
+  int adam_t = 0;
+  bf16* Wt = nullptr;   // [2 NL][64][64] transposed BF16 (forward operands)
+  bf16* Wn = nullptr;   // [2 NL][64][64] BF16 (backward dX operands)
+  // operator
+  double* diag = nullptr;
+  float* diag32 = nullptr;
+  float* ones = nullptr;
+  double mean_log = 0;
+  int n0 = 0;
+  bool have_operator = false;
+  bool scalings_valid = false;
+  // network activations (batch 1: the features do not depend on r)
+  float* x0 = nullptr;                       // [n0][2]
+  bf16* a_in = nullptr;                      // [n0][64]
+  bf16* h[kMaxLevels] = {};                  // layer inputs (h[0] = a_in)
+  bf16* m[kMaxLevels] = {};                  // S h
+  bf16* o[kMaxLevels] = {};                  // layer outputs
+  float* dO[kMaxLevels] = {};                // FP32 d o per level [n][64]
+  float* dH[kMaxLevels] = {};                // FP32 d h per level [n][64]
+  bf16* Gb = nullptr;                        // BF16 G [n0][64]
+  float* ftmp = nullptr;                     // FP32 [n0][64]
+  // multilevel preconditioner
+  float* base[kMaxLevels] = {};              // base scaling per level [n_l]
+  float* d[kMaxLevels] = {};                 // learned scaling per level [n_l]
+  float* dc[kMaxLevels] = {};                // dL/dc per level [n_l]
+  float* t[kMaxLevels] = {};                 // down sweep [B][n_l] (level 0: the input r, t0)
+  const float* t0 = nullptr;
+  float* w[kMaxLevels] = {};                 // up sweep [B][n_l] (w[0] = M r)
+  float* s[kMaxLevels] = {};                 // adjoint down sweep [B][n_l]
+  double* sums = nullptr;                    // [B][4]
+  float* part = nullptr;                     // partial sums (dW, db)
+  int64_t part_cap = 0;
+  float* a32 = nullptr;                      // A in FP32 on the level-0 graph (training loss)
+  CsrLevel Aop;
+  float* tmpB = nullptr;                     // [B][n0]
+  float* r32 = nullptr;                      // FCG staging [n0]
+  float* z32 = nullptr;                      // FCG staging [n0]
+  afem::FcgWork* fcg = nullptr;              // FCG buffers and graph (created on first solve)
+  std::vector<void*> owned;
+};
+
+namespace afem {
+
+static afem_status dalloc(afem_mpnn net, size_t bytes, void** out) {
+  AFEM_CUDA(cudaMallocAsync(out, bytes, net->ctx->stream));
+  net->owned.push_back(*out);
+  return AFEM_OK;
+}
+template <class T>
+static afem_status dalloc(afem_mpnn net, size_t count, T** out) {
+  return dalloc(net, count * sizeof(T), reinterpret_cast<void**>(out));
+}
+
+static afem_status copy_csr(afem_mpnn net, CsrLevel& dst, int nrow, int ncol, const int32_t* rp, const int32_t* cols,
+                            const float* w) {
+  dst.nrow = nrow;
+  dst.ncol = ncol;
+  int32_t nnz = 0;
+  AFEM_TRY(read_scalar(net->ctx, rp + nrow, &nnz));
+  dst.nnz = nnz;
+  AFEM_TRY(dalloc(net, (size_t)nrow + 1, &dst.rp));
+  AFEM_TRY(dalloc(net, (size_t)std::max(nnz, 1), &dst.cols));
+  AFEM_TRY(dalloc(net, (size_t)std::max(nnz, 1), &dst.w));
+  cudaStream_t s = net->ctx->stream;
+  AFEM_CUDA(cudaMemcpyAsync(dst.rp, rp, sizeof(int32_t) * (nrow + 1), cudaMemcpyDeviceToDevice, s));
+  if (nnz) {
+    AFEM_CUDA(cudaMemcpyAsync(dst.cols, cols, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, s));
+    if (w) AFEM_CUDA(cudaMemcpyAsync(dst.w, w, sizeof(float) * nnz, cudaMemcpyDeviceToDevice, s));
+  }
+  return AFEM_OK;
+}
+
+// parameter offsets
+static int off_win() { return 0; }
+static int off_bin() { return 2 * kF; }
+static int off_w1(int l) { return 3 * kF + l * (2 * kF * kF + kF); }
+static int off_w2(int l) { return off_w1(l) + kF * kF; }
+static int off_b(int l) { return off_w1(l) + 2 * kF * kF; }
+static int off_head(int NL, int l) { return 3 * kF + NL * (2 * kF * kF + kF) + l * (kF + 1); }
+
+static afem_status refresh_weights(afem_mpnn net) {
+  afem_context ctx = net->ctx;
+  const int L = net->NL;
+  float* Wstack = nullptr;
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(float) * 2 * L * kF * kF)));
+  AFEM_TRY(scratch_take(ctx, (size_t)2 * L * kF * kF, &Wstack));
+  for (int l = 0; l < L; ++l) {
+    AFEM_CUDA(cudaMemcpyAsync(Wstack + (2 * l) * kF * kF, net->params + off_w1(l), sizeof(float) * kF * kF,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+    AFEM_CUDA(cudaMemcpyAsync(Wstack + (2 * l + 1) * kF * kF, net->params + off_w2(l), sizeof(float) * kF * kF,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  net->scalings_valid = false;
+  return launch(ctx, k_weights_bf16, grid_for(ctx, 2 * L * kF * kF, 256), 256, 0, 2 * L, (const float*)Wstack,
+                net->Wt, net->Wn);
+}
+
+template <class TIn, class TOut>
+static afem_status spmm(afem_mpnn net, const CsrLevel& S, const TIn* X, TOut* Y, int acc) {
+  dim3 grid(grid_for(net->ctx, (int64_t)S.nrow * 32, 256, 8), 1);
+  k_spmm<TIn, TOut><<<grid, 256, 0, net->ctx->stream>>>(S.nrow, S.ncol, S.rp, S.cols, S.w, X, (const bf16*)nullptr,
+                                                        Y, acc);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_spmm", __FILE__, __LINE__);
+  ++net->ctx->launches;
+  return AFEM_OK;
+}
+
+static afem_status sweep(afem_mpnn net, const CsrLevel* M, int batch, const float* x, const float* dsc,
+                         const float* tv, float* y, int nrow) {
+  dim3 grid(grid_for(net->ctx, nrow, 256, 8), batch);
+  if (M)
+    k_sweep<<<grid, 256, 0, net->ctx->stream>>>(M->nrow, M->ncol, M->rp, M->cols, M->w, x, dsc, tv, y);
+  else
+    k_sweep<<<grid, 256, 0, net->ctx->stream>>>(nrow, 0, nullptr, nullptr, nullptr, nullptr, dsc, tv, y);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_sweep", __FILE__, __LINE__);
+  ++net->ctx->launches;
+  return AFEM_OK;
+}
+
+static unsigned gemm_grid(afem_context ctx, int64_t M) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((M + kGemmRows - 1) / kGemmRows, (int64_t)ctx->sm_count * 8));
+}
+
+// network forward on the coefficient features -> scalings d_l
+static afem_status features_forward(afem_mpnn net) {
+  afem_context ctx = net->ctx;
+  const int n0 = net->n0, L = net->L;
+  AFEM_TRY(launch(ctx, k_input_layer, grid_for(ctx, n0, 256, 8), 256, 0, n0, (const double*)net->diag, net->mean_log,
+                  (const float*)(net->params + off_win()), (const float*)(net->params + off_bin()), net->x0,
+                  net->a_in));
+  for (int l = 0; l < L; ++l) {
+    const int nl = net->n[l];
+    if (l < net->NL) {
+      AFEM_TRY(spmm<bf16, bf16>(net, net->S[l], net->h[l], net->m[l], 0));
+      AFEM_TRY(launch(ctx, k_row_gemm<true, true>, gemm_grid(ctx, nl), 256, 0, nl, (const bf16*)net->h[l],
+                      (const bf16*)(net->Wt + (2 * l) * kF * kF), (const bf16*)net->m[l],
+                      (const bf16*)(net->Wt + (2 * l + 1) * kF * kF), (const float*)(net->params + off_b(l)),
+                      net->o[l], (float*)nullptr, 0));
+    }
+    if (l + 1 < L) AFEM_TRY(spmm<bf16, bf16>(net, net->R[l], net->o[l], net->h[l + 1], 0));
+    AFEM_TRY(launch(ctx, k_head, grid_for(ctx, nl, 256, 8), 256, 0, nl, (const bf16*)net->o[l],
+                    (const float*)(net->params + off_head(net->NL, l)), (const float*)net->base[l], net->d[l]));
+  }
+  net->scalings_valid = true;
+  return AFEM_OK;
+}
+
+// z = M r for `batch` FP32 vectors (r, z: [batch][n0]); with z == nullptr the
+// result stays in w[0] and the down sweep in t[] (training keeps both)
+static afem_status apply(afem_mpnn net, int batch, const float* r, float* z) {
+  const int L = net->L;
+  if (!net->scalings_valid) AFEM_TRY(features_forward(net));
+  net->t0 = r;
+  const float* tl = r;
+  for (int l = 0; l + 1 < L; ++l) {
+    AFEM_TRY(sweep(net, &net->Pt[l], batch, tl, nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
+    tl = net->t[l + 1];
+  }
+  float* w0 = z ? z : net->w[0];
+  AFEM_TRY(sweep(net, nullptr, batch, nullptr, net->d[L - 1], tl, L == 1 ? w0 : net->w[L - 1], net->n[L - 1]));
+  for (int l = L - 2; l >= 0; --l)
+    AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], net->d[l], l == 0 ? r : net->t[l], l == 0 ? w0 : net->w[l],
+                   net->n[l]));
+  return AFEM_OK;
+}
+
+static afem_status ensure_part(afem_mpnn net, int64_t count) {
+  if (count <= net->part_cap) return AFEM_OK;
+  AFEM_TRY(dalloc(net, (size_t)count, &net->part));
+  net->part_cap = count;
+  return AFEM_OK;
+}
+
+// dW = X^T G summed over M rows into dst (FP32 64x64), deterministic
+static afem_status dw_gemm(afem_mpnn net, int64_t M, const bf16* X, const bf16* G, float* dst) {
+  afem_context ctx = net->ctx;
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>((M + kDwRows - 1) / kDwRows, (int64_t)ctx->sm_count * 2));
+  AFEM_TRY(ensure_part(net, (int64_t)nb * kF * kF));
+  AFEM_TRY(launch(ctx, k_dw_partial, nb, 256, 0, (int)M, X, G, net->part));
+  return launch(ctx, k_sum_partials, grid_for(ctx, kF * kF, 256), 256, 0, nb, kF * kF, (const float*)net->part, dst,
+                0);
+}
+
+// loss and gradients of the mean relative squared error over (r, e)
+static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, const float* e, double* loss_h) {
+  afem_context ctx = net->ctx;
+  cudaStream_t s = ctx->stream;
+  const int n0 = net->n0, L = net->L;
+  if (!net->scalings_valid) AFEM_TRY(features_forward(net));
+  AFEM_TRY(apply(net, batch, r, nullptr));
+  AFEM_CUDA(cudaMemsetAsync(net->sums, 0, sizeof(double) * 4 * batch, s));
+  AFEM_CUDA(cudaMemsetAsync(net->grads, 0, sizeof(float) * net->nparam, s));
+  // energy-norm loss ||(I - M A) e||_A^2 / ||e||_A^2: Av = A (e - z) into s[0], A e into tmpB
+  AFEM_TRY(launch(ctx, k_sub, grid_for(ctx, (int64_t)batch * n0, 256), 256, 0, (int64_t)batch * n0, e,
+                  (const float*)net->w[0], net->tmpB));
+  AFEM_TRY(sweep(net, &net->Aop, batch, net->tmpB, nullptr, nullptr, net->s[0], n0));
+  AFEM_TRY(sweep(net, &net->Aop, batch, e, nullptr, nullptr, net->tmpB, n0));
+  {
+    dim3 g(grid_for(ctx, n0, 256, 2), batch);
+    k_energy_sums<<<g, 256, 0, s>>>(n0, net->w[0], e, net->tmpB, net->s[0], net->sums);
+    k_energy_grad<<<g, 256, 0, s>>>(n0, batch, net->sums, net->s[0]);
+    cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess) return cuda_fail(ce, "k_energy", __FILE__, __LINE__);
+    ctx->launches += 2;
+  }
+  // adjoint down sweep s_{l+1} = P_l^T s_l ; dc_l = d_l sum_b t_l s_l ; heads
+  for (int l = 0; l < L; ++l) {
+    if (l + 1 < L) AFEM_TRY(sweep(net, &net->Pt[l], batch, net->s[l], nullptr, nullptr, net->s[l + 1], net->n[l + 1]));
+    const int nl = net->n[l];
+    AFEM_TRY(launch(ctx, k_dc, grid_for(ctx, nl, 256, 8), 256, 0, nl, batch, l == 0 ? net->t0 : (const float*)net->t[l],
+                    (const float*)net->s[l], (const float*)net->d[l], net->dc[l]));
+    const unsigned nbk = grid_for(ctx, nl, 256, 2);
+    AFEM_TRY(ensure_part(net, (int64_t)nbk * (kF + 1)));
+    AFEM_TRY(launch(ctx, k_head_backward, nbk, 256, 0, nl, (const float*)net->dc[l], (const bf16*)net->o[l],
+                    (const float*)(net->params + off_head(net->NL, l)), net->dO[l], net->part));
+    AFEM_TRY(launch(ctx, k_sum_partials, 1, 96, 0, (int)nbk, kF + 1, (const float*)net->part,
+                    net->grads + off_head(net->NL, l), 0));
+  }
+  // network backward, coarsest level first: o_l gets its head gradient plus R_l^T dh_{l+1}
+  for (int l = L - 1; l >= 0; --l) {
+    const int64_t M = net->n[l];
+    if (l >= net->NL) {   // o_l = h_l = R_{l-1} o_{l-1}: pass the gradient down
+      AFEM_TRY(spmm<float, float>(net, net->Rt[l - 1], net->dO[l], net->dO[l - 1], 1));
+      continue;
+    }
+    const unsigned nbk = grid_for(ctx, M * 32, 256, 4);
+    AFEM_TRY(ensure_part(net, std::max<int64_t>((int64_t)nbk * kF, (int64_t)ctx->sm_count * 2 * kF * kF)));
+    AFEM_TRY(launch(ctx, k_relu_grad, nbk, 256, 0, M, (const float*)net->dO[l], (const bf16*)net->o[l], net->Gb,
+                    net->part));
+    AFEM_TRY(launch(ctx, k_sum_partials, 1, 64, 0, (int)nbk, kF, (const float*)net->part, net->grads + off_b(l), 0));
+    AFEM_TRY(dw_gemm(net, M, net->h[l], net->Gb, net->grads + off_w1(l)));
+    AFEM_TRY(dw_gemm(net, M, net->m[l], net->Gb, net->grads + off_w2(l)));
+    // dh_l = G W1^T + S_l^T (G W2^T)   (S_l symmetric)
+    AFEM_TRY(launch(ctx, k_row_gemm<false, false>, gemm_grid(ctx, M), 256, 0, (int)M, (const bf16*)net->Gb,
+                    (const bf16*)(net->Wn + (2 * l) * kF * kF), (const bf16*)nullptr, (const bf16*)nullptr,
+                    (const float*)nullptr, (bf16*)nullptr, net->dH[l], 0));
+    AFEM_TRY(launch(ctx, k_row_gemm<false, false>, gemm_grid(ctx, M), 256, 0, (int)M, (const bf16*)net->Gb,
+                    (const bf16*)(net->Wn + (2 * l + 1) * kF * kF), (const bf16*)nullptr, (const bf16*)nullptr,
+                    (const float*)nullptr, (bf16*)nullptr, net->ftmp, 0));
+    AFEM_TRY(spmm<float, float>(net, net->S[l], net->ftmp, net->dH[l], 1));
+    if (l > 0) AFEM_TRY(spmm<float, float>(net, net->Rt[l - 1], net->dH[l], net->dO[l - 1], 1));
+  }
+  {
+    const unsigned nbk = grid_for(ctx, (int64_t)n0 * 32, 256, 4);
+    AFEM_TRY(ensure_part(net, (int64_t)nbk * 3 * kF));
+    AFEM_TRY(launch(ctx, k_input_backward, nbk, 256, 0, (int64_t)n0, (const float*)net->dH[0],
+                    (const bf16*)net->a_in, (const float*)net->x0, net->part));
+    AFEM_TRY(launch(ctx, k_sum_partials, 1, 192, 0, (int)nbk, 3 * kF, (const float*)net->part,
+                    net->grads + off_win(), 0));
+  }
+  if (loss_h) {
+    std::vector<double> hs(4 * batch);
+    AFEM_CUDA(cudaMemcpyAsync(hs.data(), net->sums, sizeof(double) * 4 * batch, cudaMemcpyDeviceToHost, s));
+    AFEM_CUDA(cudaStreamSynchronize(s));
+    double l = 0;
+    for (int b = 0; b < batch; ++b) l += hs[b * 4 + 1] / (hs[b * 4] + 1e-300);
+    *loss_h = l / batch;
+  }
+  return AFEM_OK;
+}
+
+}  // namespace afem
+
+extern "C" {
+
+afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, const int* level_rows, const int32_t* const* graph_rp,
+                             const int32_t* const* graph_cols, const float* const* graph_w,
+                             const int32_t* const* restr_rp, const int32_t* const* restr_cols,
+                             const float* const* restr_w, const int32_t* const* restrT_rp,
+                             const int32_t* const* restrT_cols, const float* const* restrT_w,
+                             const int32_t* const* prol_rp, const int32_t* const* prol_cols,
+                             const float* const* prol_w, const int32_t* const* prolT_rp,
+                             const int32_t* const* prolT_cols, const float* const* prolT_w, int max_batch,
+                             afem_mpnn* out) {
+  AFEM_CHECK_ARG(ctx && out && level_rows, "afem_mpnn_create: null argument");
+  AFEM_CHECK_ARG(nb_levels >= 1 && nb_levels <= kMaxLevels, "afem_mpnn_create: 1..%d levels", kMaxLevels);
+  AFEM_CHECK_ARG(max_batch >= 1 && max_batch <= kMaxBatch, "afem_mpnn_create: max_batch 1..%d", kMaxBatch);
+  AFEM_CHECK_ARG(nb_layers >= 1 && nb_layers <= nb_levels, "afem_mpnn_create: 1..%d layers", nb_levels);
+  *out = nullptr;
+  afem_mpnn net = new (std::nothrow) afem_mpnn_s();
+  if (!net) return fail(AFEM_ERR_OOM, "afem_mpnn_create: host allocation");
+  net->ctx = ctx;
+  net->L = nb_levels;
+  net->NL = nb_layers;
+  net->max_batch = max_batch;
+  auto cleanup = [&](afem_status st) {
+    afem_mpnn_destroy(net);
+    return st;
+  };
+  afem_status st;
+  for (int l = 0; l < nb_levels; ++l) {
+    net->n[l] = level_rows[l];
+    if (level_rows[l] <= 0) return cleanup(fail(AFEM_ERR_BAD_ARG, "afem_mpnn_create: empty level %d", l));
+    if ((st = copy_csr(net, net->S[l], level_rows[l], level_rows[l], graph_rp[l], graph_cols[l],
+                       l == 0 ? nullptr : graph_w[l])) != AFEM_OK)
+      return cleanup(st);
+    if (l + 1 < nb_levels) {
+      if ((st = copy_csr(net, net->R[l], level_rows[l + 1], level_rows[l], restr_rp[l], restr_cols[l], restr_w[l])) ||
+          (st = copy_csr(net, net->Rt[l], level_rows[l], level_rows[l + 1], restrT_rp[l], restrT_cols[l],
+                         restrT_w[l])) ||
+          (st = copy_csr(net, net->P[l], level_rows[l], level_rows[l + 1], prol_rp[l], prol_cols[l], prol_w[l])) ||
+          (st = copy_csr(net, net->Pt[l], level_rows[l + 1], level_rows[l], prolT_rp[l], prolT_cols[l], prolT_w[l])))
+        return cleanup(st);
+    }
+  }
+  net->n0 = level_rows[0];
+  net->nparam = off_head(nb_layers, nb_levels);
+  const size_t B = max_batch;
+  const size_t n0 = net->n0;
+  if ((st = dalloc(net, (size_t)net->nparam, &net->params)) || (st = dalloc(net, (size_t)net->nparam, &net->grads)) ||
+      (st = dalloc(net, (size_t)net->nparam, &net->adam_m)) || (st = dalloc(net, (size_t)net->nparam, &net->adam_v)) ||
+      (st = dalloc(net, (size_t)2 * nb_layers * kF * kF, &net->Wt)) ||
+      (st = dalloc(net, (size_t)2 * nb_layers * kF * kF, &net->Wn)) || (st = dalloc(net, n0, &net->diag)) ||
+      (st = dalloc(net, n0, &net->diag32)) || (st = dalloc(net, n0, &net->ones)) ||
+      (st = dalloc(net, n0 * 2, &net->x0)) || (st = dalloc(net, n0 * kF, &net->a_in)) ||
+      (st = dalloc(net, n0 * kF, &net->Gb)) || (st = dalloc(net, n0 * kF, &net->ftmp)) ||
+      (st = dalloc(net, B * 4, &net->sums)) || (st = dalloc(net, n0, &net->r32)) || (st = dalloc(net, n0, &net->z32)) ||
+      (st = dalloc(net, (size_t)std::max<int64_t>(net->S[0].nnz, 1), &net->a32)) || (st = dalloc(net, B * n0, &net->tmpB)))
+    return cleanup(st);
+  net->h[0] = net->a_in;
+  for (int l = 0; l < nb_levels; ++l) {
+    const size_t nl = net->n[l];
+    if (l > 0 && (st = dalloc(net, nl * kF, &net->h[l]))) return cleanup(st);
+    if (l < nb_layers &&
+        ((st = dalloc(net, nl * kF, &net->m[l])) || (st = dalloc(net, nl * kF, &net->o[l])) ||
+         (st = dalloc(net, nl * kF, &net->dH[l]))))
+      return cleanup(st);
+    if (l >= nb_layers) net->o[l] = net->h[l];
+    if ((st = dalloc(net, nl * kF, &net->dO[l])) ||
+        (st = dalloc(net, nl, &net->base[l])) || (st = dalloc(net, nl, &net->d[l])) ||
+        (st = dalloc(net, nl, &net->dc[l])) || (st = dalloc(net, B * nl, &net->t[l])) ||
+        (st = dalloc(net, B * nl, &net->w[l])) || (st = dalloc(net, B * nl, &net->s[l])))
+      return cleanup(st);
+  }
+  cudaStream_t s = ctx->stream;
+  cudaMemsetAsync(net->adam_m, 0, sizeof(float) * net->nparam, s);
+  cudaMemsetAsync(net->adam_v, 0, sizeof(float) * net->nparam, s);
+  cudaMemsetAsync(net->params, 0, sizeof(float) * net->nparam, s);
+  *out = net;
+  return AFEM_OK;
+}
+
+afem_status afem_mpnn_destroy(afem_mpnn net) {
+  if (!net) return AFEM_OK;
+  cudaStream_t s = net->ctx->stream;
+  delete net->fcg;
+  for (void* p : net->owned) cudaFreeAsync(p, s);
+  cudaStreamSynchronize(s);
+  delete net;
+  return AFEM_OK;
+}
+
+int afem_mpnn_param_count(afem_mpnn net) { return net ? net->nparam : 0; }
+
+afem_status afem_mpnn_set_params(afem_mpnn net, const float* params_d) {
+  AFEM_CHECK_ARG(net && params_d, "afem_mpnn_set_params: null argument");
+  AFEM_CUDA(cudaMemcpyAsync(net->params, params_d, sizeof(float) * net->nparam, cudaMemcpyDeviceToDevice,
+                            net->ctx->stream));
+  net->adam_t = 0;
+  AFEM_CUDA(cudaMemsetAsync(net->adam_m, 0, sizeof(float) * net->nparam, net->ctx->stream));
+  AFEM_CUDA(cudaMemsetAsync(net->adam_v, 0, sizeof(float) * net->nparam, net->ctx->stream));
+  return refresh_weights(net);
+}
+
+afem_status afem_mpnn_get_params(afem_mpnn net, float* params_d) {
+  AFEM_CHECK_ARG(net && params_d, "afem_mpnn_get_params: null argument");
+  AFEM_CUDA(cudaMemcpyAsync(params_d, net->params, sizeof(float) * net->nparam, cudaMemcpyDeviceToDevice,
+                            net->ctx->stream));
+  return AFEM_OK;
+}
+
+afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* rp, const int32_t* cols, const double* vals) {
+  AFEM_CHECK_ARG(net && rp && cols && vals, "afem_mpnn_set_operator: null argument");
+  AFEM_CHECK_ARG(n == net->n0, "afem_mpnn_set_operator: %d rows, network level 0 has %d", n, net->n0);
+  int32_t nnz = 0;
+  AFEM_TRY(read_scalar(net->ctx, rp + n, &nnz));
+  AFEM_CHECK_ARG(nnz == net->S[0].nnz, "afem_mpnn_set_operator: matrix graph differs from level 0 (%d vs %lld nnz)",
+                 nnz, (long long)net->S[0].nnz);
+  afem_context ctx = net->ctx;
+  cudaStream_t s = ctx->stream;
+  AFEM_TRY(launch(ctx, k_diag, grid_for(ctx, n, 256), 256, 0, n, rp, cols, vals, net->diag, net->diag32, net->ones));
+  AFEM_TRY(launch(ctx, k_level0_weights, grid_for(ctx, n, 256), 256, 0, n, rp, cols, vals, (const double*)net->diag,
+                  net->S[0].w));
+  AFEM_TRY(launch(ctx, k_f64_to_f32, grid_for(ctx, nnz, 256), 256, 0, (int64_t)nnz, vals, net->a32));
+  net->Aop = net->S[0];
+  net->Aop.w = net->a32;
+  // mean log diag (host, once per operator)
+  {
+    std::vector<double> hd(n);
+    AFEM_CUDA(cudaMemcpyAsync(hd.data(), net->diag, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    AFEM_CUDA(cudaStreamSynchronize(s));
+    double acc = 0;
+    for (int i = 0; i < n; ++i) acc += std::log(hd[i]);
+    net->mean_log = acc / n;
+  }
+  // base scalings: base_l = (R..R 1) / (R..R diag), base_0 = 1 / diag
+  AFEM_TRY(launch(ctx, k_ratio, grid_for(ctx, n, 256), 256, 0, n, (const float*)net->ones,
+                  (const float*)net->diag32, net->base[0]));
+  // numerator (restricted ones) in t[], denominator (restricted diag) in w[]
+  const float* num = net->ones;
+  const float* den = net->diag32;
+  for (int l = 0; l + 1 < net->L; ++l) {
+    AFEM_TRY(sweep(net, &net->R[l], 1, num, nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
+    AFEM_TRY(sweep(net, &net->R[l], 1, den, nullptr, nullptr, net->w[l + 1], net->n[l + 1]));
+    num = net->t[l + 1];
+    den = net->w[l + 1];
+    AFEM_TRY(launch(ctx, k_ratio, grid_for(ctx, net->n[l + 1], 256), 256, 0, net->n[l + 1], num, den,
+                    net->base[l + 1]));
+  }
+  net->have_operator = true;
+  net->scalings_valid = false;
+  return AFEM_OK;
+}
+
+afem_status afem_mpnn_forward(afem_mpnn net, int batch, const float* r_d, float* z_d) {
+  AFEM_CHECK_ARG(net && r_d && z_d && batch >= 1 && batch <= net->max_batch, "afem_mpnn_forward: bad arguments");
+  AFEM_CHECK_ARG(net->have_operator, "afem_mpnn_forward: call afem_mpnn_set_operator first");
+  return apply(net, batch, r_d, z_d);
+}
+
+afem_status afem_mpnn_scalings(afem_mpnn net, int level, float* d_d) {
+  AFEM_CHECK_ARG(net && d_d && level >= 0 && level < net->L, "afem_mpnn_scalings: bad arguments");
+  AFEM_CHECK_ARG(net->have_operator, "afem_mpnn_scalings: call afem_mpnn_set_operator first");
+  if (!net->scalings_valid) AFEM_TRY(features_forward(net));
+  AFEM_CUDA(cudaMemcpyAsync(d_d, net->d[level], sizeof(float) * net->n[level], cudaMemcpyDeviceToDevice,
+                            net->ctx->stream));
+  return AFEM_OK;
+}
+
+afem_status afem_mpnn_gradients(afem_mpnn net, int batch, const float* r_d, const float* e_d, float* grad_d,
+                                double* loss_h) {
+  AFEM_CHECK_ARG(net && r_d && e_d && batch >= 1 && batch <= net->max_batch, "afem_mpnn_gradients: bad arguments");
+  AFEM_CHECK_ARG(net->have_operator, "afem_mpnn_gradients: call afem_mpnn_set_operator first");
+  AFEM_TRY(loss_and_gradients(net, batch, r_d, e_d, loss_h));
+  if (grad_d)
+    AFEM_CUDA(cudaMemcpyAsync(grad_d, net->grads, sizeof(float) * net->nparam, cudaMemcpyDeviceToDevice,
+                              net->ctx->stream));
+  return AFEM_OK;
+}
+
+afem_status afem_mpnn_train_step(afem_mpnn net, int batch, const float* r_d, const float* e_d, float lr,
+                                 double* loss_h) {
+  AFEM_TRY(afem_mpnn_gradients(net, batch, r_d, e_d, nullptr, loss_h));
+  afem_context ctx = net->ctx;
+  net->adam_t += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - powf(b1, (float)net->adam_t), c2 = 1.f - powf(b2, (float)net->adam_t);
+  AFEM_TRY(launch(ctx, k_adam, grid_for(ctx, net->nparam, 256), 256, 0, net->nparam, net->params,
+                  (const float*)net->grads, net->adam_m, net->adam_v, lr, b1, b2, 1e-8f, c1, c2));
+  return refresh_weights(net);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Flexible CG (FCG(1): each new direction A-orthogonalised against the last
+// one) with M as the preconditioner.  FP64 vectors, matrix, dot products and
+// stop test; M runs in FP32 on r converted to FP32.  Scalars stay on the
+// device (last-block reductions in a fixed order, deterministic); one
+// iteration is 4 + (2L - 1) kernels, captured in a CUDA graph per chunk of
+// iterations, and a device flag makes the remaining kernels of a chunk return
+// once converged.
+//   K1  q = A p ; <p, q>, <r, p>            -> alpha = <r, p> / <p, q>
+//   K2  x += alpha p ; r -= alpha q ; r32   -> <r, r>, stop test
+//   M   z32 = M r32 (down and up sweeps)
+//   K3  z = z32 ; <z, q>                    -> beta = -<z, q> / <p, q>
+//   K4  p = z + beta p
+
+namespace afem {
+
+struct FcgState {
+  double pq, rp, alpha, beta, rr, bnorm2, tol2, pad;
+  int done, iter, status, max_iter;
+  unsigned int ticket[4];
+};
+static_assert(sizeof(FcgState) <= 256, "FcgState is read back through the context's 256-byte pinned buffer");
+
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_fcg_init(int n, const int32_t* __restrict__ rp,
+                                                          const int32_t* __restrict__ cols,
+                                                          const double* __restrict__ vals, const double* __restrict__ b,
+                                                          const double* __restrict__ x, double* __restrict__ r,
+                                                          float* __restrict__ r32, double* partials, FcgState* st,
+                                                          double rtol, double atol, int max_iter) {
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  const int nr = n + ((groups - n % groups) % groups);
+  double rr = 0.0, bb = 0.0;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
+    double s = 0.0;
+    if (row < n) s = row_dot<G>(row, rp, cols, vals, x, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (row < n && lane == 0) {
+      const double bi = b[row], ri = bi - s;
+      r[row] = ri;
+      r32[row] = (float)ri;
+      rr += ri * ri;
+      bb += bi * bi;
+    }
+  }
+  rr = block_sum(rr, sh);
+  bb = block_sum(bb, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 2] = rr;
+    partials[blockIdx.x * 2 + 1] = bb;
+  }
+  if (last_block(&st->ticket[0])) {
+    const double trr = reduce_partials(partials, gridDim.x, 2, 0, sh);
+    const double tbb = reduce_partials(partials, gridDim.x, 2, 1, sh);
+    if (threadIdx.x == 0) {
+      st->rr = trr;
+      st->bnorm2 = tbb;
+      st->tol2 = fmax(rtol * rtol * tbb, atol * atol);
+      st->iter = 0;
+      st->max_iter = max_iter;
+      st->status = AFEM_OK;
+      st->done = trr <= st->tol2 ? 1 : 0;
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+template <int G>
+__global__ void __launch_bounds__(kSolveBlock) k_fcg_spmv(int n, const int32_t* __restrict__ rp,
+                                                          const int32_t* __restrict__ cols,
+                                                          const double* __restrict__ vals, const double* __restrict__ p,
+                                                          const double* __restrict__ r, double* __restrict__ q,
+                                                          double* partials, FcgState* st) {
+  if (((volatile FcgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & (G - 1);
+  const int groups = gridDim.x * (blockDim.x / G);
+  const int nr = n + ((groups - n % groups) % groups);
+  double pq = 0.0, rpd = 0.0;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
+    double s = 0.0;
+    if (row < n) s = row_dot<G>(row, rp, cols, vals, p, lane);
+    else {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    }
+    if (row < n && lane == 0) {
+      const double pi = p[row];
+      q[row] = s;
+      pq += pi * s;
+      rpd += r[row] * pi;
+    }
+  }
+  pq = block_sum(pq, sh);
+  rpd = block_sum(rpd, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x * 2] = pq;
+    partials[blockIdx.x * 2 + 1] = rpd;
+  }
+  if (last_block(&st->ticket[1])) {
+    const double tpq = reduce_partials(partials, gridDim.x, 2, 0, sh);
+    const double trp = reduce_partials(partials, gridDim.x, 2, 1, sh);
+    if (threadIdx.x == 0) {
+      st->pq = tpq;
+      st->rp = trp;
+      if (!(tpq > 0.0) || !isfinite(tpq)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+        st->alpha = 0.0;
+      } else {
+        st->alpha = trp / tpq;
+      }
+      st->ticket[1] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveBlock) k_fcg_update(int n, double* __restrict__ x, double* __restrict__ r,
+                                                            float* __restrict__ r32, const double* __restrict__ p,
+                                                            const double* __restrict__ q, double* partials,
+                                                            FcgState* st) {
+  if (((volatile FcgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const double alpha = ((volatile FcgState*)st)->alpha;
+  double rr = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    r32[i] = (float)ri;
+    rr += ri * ri;
+  }
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x * 2] = rr;
+  if (last_block(&st->ticket[2])) {
+    const double trr = reduce_partials(partials, gridDim.x, 2, 0, sh);
+    if (threadIdx.x == 0) {
+      st->rr = trr;
+      st->iter += 1;
+      if (!isfinite(trr)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+      } else if (trr <= st->tol2) {
+        st->done = 1;
+      } else if (st->iter >= st->max_iter) {
+        st->status = AFEM_ERR_NOT_CONVERGED;
+        st->done = 1;
+      }
+      st->ticket[2] = 0;
+    }
+  }
+}
+
+// first != 0: p = z32 (the initial direction).  Otherwise z = z32 and
+// <z, q> -> beta = -<z, q> / <p, q>.
+__global__ void __launch_bounds__(kSolveBlock) k_fcg_widen(int n, const float* __restrict__ z32, double* __restrict__ z,
+                                                           const double* __restrict__ q, double* __restrict__ p,
+                                                           int first, double* partials, FcgState* st) {
+  if (((volatile FcgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  double zq = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double zi = (double)z32[i];
+    if (first) {
+      p[i] = zi;
+    } else {
+      z[i] = zi;
+      zq += zi * q[i];
+    }
+  }
+  if (first) return;
+  zq = block_sum(zq, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x * 2] = zq;
+  if (last_block(&st->ticket[3])) {
+    const double t = reduce_partials(partials, gridDim.x, 2, 0, sh);
+    if (threadIdx.x == 0) {
+      st->beta = -t / st->pq;
+      st->ticket[3] = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveBlock) k_fcg_dir(int n, const double* __restrict__ z, double* __restrict__ p,
+                                                         const FcgState* st) {
+  if (((volatile const FcgState*)st)->done) return;
+  const double beta = ((volatile const FcgState*)st)->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
+}
+
+// Solver buffers and the captured iteration graph, kept with the network and
+// rebuilt when the operator or solution pointers change.
+struct FcgWork {
+  double *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *partials = nullptr;
+  FcgState* st = nullptr;
+  int nparts = 0;
+  const void* key[4] = {};
+  int key_chunk = 0;
+  GraphChunk* graph = nullptr;
+  ~FcgWork() { delete graph; }
+};
+
+static afem_status fcg_work(afem_mpnn net, FcgWork** out) {
+  if (!net->fcg) {
+    FcgWork* w = new (std::nothrow) FcgWork();
+    if (!w) return fail(AFEM_ERR_OOM, "afem_fcg_solve: host allocation");
+    net->fcg = w;
+    const size_t n = net->n0;
+    w->nparts = (int)std::max<unsigned>(grid_for(net->ctx, (int64_t)n * 32, kSolveBlock, 8),
+                                        grid_for(net->ctx, (int64_t)n, kSolveBlock, 8));
+    AFEM_TRY(dalloc(net, n, &w->r));
+    AFEM_TRY(dalloc(net, n, &w->z));
+    AFEM_TRY(dalloc(net, n, &w->p));
+    AFEM_TRY(dalloc(net, n, &w->q));
+    AFEM_TRY(dalloc(net, (size_t)2 * w->nparts, &w->partials));
+    AFEM_TRY(dalloc(net, sizeof(FcgState), reinterpret_cast<void**>(&w->st)));
+    AFEM_CUDA(cudaMemsetAsync(w->st, 0, sizeof(FcgState), net->ctx->stream));
+  }
+  *out = net->fcg;
+  return AFEM_OK;
+}
+
+// z32 = M r32 for one vector, launched on `stream` (the capture stream inside a graph)
+static afem_status apply_on(afem_mpnn net, cudaStream_t stream) {
+  afem_context ctx = net->ctx;
+  cudaStream_t saved = ctx->stream;
+  ctx->stream = stream;
+  afem_status st = apply(net, 1, net->r32, net->z32);
+  ctx->stream = saved;
+  return st;
+}
+
+}  // namespace afem
+
+extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp, const int32_t* cols,
+                                      const double* vals, const double* b, double* x, afem_mpnn net,
+                                      const afem_solver_options* opt_in, afem_solve_info* info) {
+  AFEM_CHECK_ARG(ctx && n > 0 && rp && cols && vals && b && x && net, "afem_fcg_solve: bad arguments");
+  AFEM_CHECK_ARG(net->ctx == ctx, "afem_fcg_solve: the network belongs to another context");
+  AFEM_CHECK_ARG(net->n0 == n && net->have_operator, "afem_fcg_solve: network not set for this operator");
+  afem_solver_options opt;
+  if (opt_in) opt = *opt_in;
+  else afem_solver_options_default(&opt);
+  const int max_iter = opt.max_iter > 0 ? opt.max_iter : 1000;
+  const int chunk = opt.check_every > 0 ? std::min(opt.check_every, 64) : 4;
+  int32_t nnz32 = 0;
+  AFEM_TRY(read_scalar(ctx, rp + n, &nnz32));
+  const int G = lanes_per_row(n, nnz32);
+  const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
+  FcgWork* w = nullptr;
+  AFEM_TRY(fcg_work(net, &w));
+  if (!net->scalings_valid) AFEM_TRY(features_forward(net));
+  const void* key[4] = {rp, cols, vals, x};
+  if (!w->graph || w->key_chunk != chunk || !std::equal(key, key + 4, w->key)) {
+    delete w->graph;
+    w->graph = new (std::nothrow) GraphChunk();
+    if (!w->graph) return fail(AFEM_ERR_OOM, "afem_fcg_solve: host allocation");
+    std::copy(key, key + 4, w->key);
+    w->key_chunk = chunk;
+    afem_status cst = capture(ctx, *w->graph, [&](cudaStream_t s) -> afem_status {
+      for (int k = 0; k < chunk; ++k) {
+        AFEM_TRY(dispatch_g(G, [&](auto g) {
+          return launch_s(ctx, s, k_fcg_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols, vals,
+                          (const double*)w->p, (const double*)w->r, w->q, w->partials, w->st);
+        }));
+        AFEM_TRY(launch_s(ctx, s, k_fcg_update, grid_vec, kSolveBlock, n, x, w->r, net->r32, (const double*)w->p,
+                          (const double*)w->q, w->partials, w->st));
+        AFEM_TRY(apply_on(net, s));
+        AFEM_TRY(launch_s(ctx, s, k_fcg_widen, grid_vec, kSolveBlock, n, (const float*)net->z32, w->z,
+                          (const double*)w->q, w->p, 0, w->partials, w->st));
+        AFEM_TRY(launch_s(ctx, s, k_fcg_dir, grid_vec, kSolveBlock, n, (const double*)w->z, w->p,
+                          (const FcgState*)w->st));
+      }
+      return AFEM_OK;
+    });
+    if (cst != AFEM_OK) {
+      delete w->graph;
+      w->graph = nullptr;
+      return cst;
+    }
+  }
+  cudaEvent_t e0, e1;
+  AFEM_CUDA(cudaEventCreate(&e0));
+  AFEM_CUDA(cudaEventCreate(&e1));
+  AFEM_CUDA(cudaEventRecord(e0, ctx->stream));
+  afem_status st = dispatch_g(G, [&](auto g) {
+    return launch(ctx, k_fcg_init<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b,
+                  (const double*)x, w->r, net->r32, w->partials, w->st, opt.rtol, opt.atol, max_iter);
+  });
+  if (st == AFEM_OK) st = apply(net, 1, net->r32, net->z32);
+  if (st == AFEM_OK)
+    st = launch(ctx, k_fcg_widen, grid_vec, kSolveBlock, 0, n, (const float*)net->z32, w->z, (const double*)w->q,
+                w->p, 1, w->partials, w->st);
+  const int per_iteration = 4 + 2 * net->L - 1;
+  FcgState hs{};
+  while (st == AFEM_OK) {
+    cudaError_t ce = cudaMemcpyAsync(ctx->pinned, w->st, sizeof(FcgState), cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+    if (ce != cudaSuccess) {
+      st = cuda_fail(ce, "afem_fcg_solve state", __FILE__, __LINE__);
+      break;
+    }
+    hs = *reinterpret_cast<FcgState*>(ctx->pinned);
+    if (hs.done) break;
+    ce = cudaGraphLaunch(w->graph->exec, ctx->stream);
+    if (ce != cudaSuccess) {
+      st = cuda_fail(ce, "cudaGraphLaunch", __FILE__, __LINE__);
+      break;
+    }
+    ctx->launches += (int64_t)per_iteration * chunk;
+  }
+  cudaEventRecord(e1, ctx->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != AFEM_OK) return st;
+  double rel = 0.0;
+  AFEM_TRY(true_relres(ctx, n, rp, cols, vals, nnz32, b, x, nullptr, &rel));
+  if (info) {
+    info->iterations = hs.iter;
+    info->refinements = 0;
+    info->status = hs.status;
+    info->relres = rel;
+    info->solve_ms = ms;
+  }
+  if (hs.status == AFEM_ERR_NOT_CONVERGED)
+    return fail(hs.status, "FCG did not reach the tolerance in %d iterations (relres %.3e)", hs.iter, rel);
+  if (hs.status == AFEM_ERR_BREAKDOWN) return fail(hs.status, "FCG breakdown (<p, A p> <= 0 or non-finite)");
+  return AFEM_OK;
+}

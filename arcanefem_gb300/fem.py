@@ -22,6 +22,7 @@ counterpart of the reference's ARCANE_FATAL / ARCANE_THROW.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 from dataclasses import dataclass
 
 import torch
@@ -79,6 +80,9 @@ class Context:
             self.handle = None
 
     def __del__(self):
+        # at interpreter shutdown the CUDA runtime may already be torn down: leak instead
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -333,6 +337,8 @@ class DoFLinearSystem:
             self.handle = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:

@@ -1,0 +1,401 @@
+"""Learned preconditioner: host side of the multilevel message-passing network.
+
+The network, its training kernels and the flexible CG that applies it live in
+libafem_gb300.so (``afem_mpnn_*``, ``afem_fcg_solve``).  This module builds
+what they need on a structured triangle mesh of the unit square
+(``meshgen.unit_square_tri``, node id = i + j (n+1)):
+
+* the level hierarchy: vertex grids of (n/2^l + 1)^2 nodes, 8-neighbour
+  graphs (weights 1/8) on the coarse levels, full-weighting restriction and
+  bilinear prolongation vanishing on the Dirichlet boundary (the grid
+  boundary), all as CSR;
+* the variable-coefficient diffusion problem -div(k grad u) = f of the
+  learned-preconditioner benchmark: k = exp(g), g a Gaussian random field
+  (correlation length 0.05, variance 1, FFT on a 1024^2 periodic grid,
+  bilinearly sampled at the cell centroids), f a sum of Gaussian bumps,
+  u = 0 on the boundary;
+* training pairs (r, e) generated by the FEM solver itself: the errors
+  e_k = x* - x_k of restarted Jacobi CG iterates and their residuals A e_k.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import _capi, fem, meshgen
+from ._capi import call
+
+F = 64
+
+
+def prolongation(R: sp.csr_matrix) -> sp.csr_matrix:
+    """Bilinear interpolation: 4 R^T for full weighting (weight 1 at the
+    coinciding node, 1/2 and 1/4 at the edge and cell midpoints)."""
+    return sp.csr_matrix(4.0 * R.T)
+
+
+def _ptr(t):
+    return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+# ---------------------------------------------------------------------------
+# Structured hierarchy
+
+def grid_graph(m: int) -> sp.csr_matrix:
+    """8-neighbour graph of an m x m vertex grid, weight 1/8, symmetric."""
+    idx = np.arange(m * m).reshape(m, m)
+    rows, cols = [], []
+    for dj in (-1, 0, 1):
+        for di in (-1, 0, 1):
+            if di == 0 and dj == 0:
+                continue
+            a = idx[max(0, -dj):m - max(0, dj), max(0, -di):m - max(0, di)]
+            b = idx[max(0, dj):m - max(0, -dj), max(0, di):m - max(0, -di)]
+            rows.append(a.ravel())
+            cols.append(b.ravel())
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    return sp.csr_matrix((np.full(r.size, 1.0 / 8.0), (r, c)), shape=(m * m, m * m))
+
+
+def restriction(mf: int) -> sp.csr_matrix:
+    """Full weighting from an mf x mf vertex grid to ((mf-1)/2 + 1)^2."""
+    mc = (mf - 1) // 2 + 1
+    w1 = {-1: 0.25, 0: 0.5, 1: 0.25}
+    rows, cols, vals = [], [], []
+    J, I = np.meshgrid(np.arange(mc), np.arange(mc), indexing="ij")
+    for dj in (-1, 0, 1):
+        for di in (-1, 0, 1):
+            fi, fj = 2 * I + di, 2 * J + dj
+            ok = (fi >= 0) & (fi < mf) & (fj >= 0) & (fj < mf)
+            rows.append((I + J * mc)[ok])
+            cols.append((fi + fj * mf)[ok])
+            vals.append(np.full(int(ok.sum()), w1[di] * w1[dj]))
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(mc * mc, mf * mf))
+
+
+def interior_mask(m: int) -> np.ndarray:
+    """1 on the interior nodes of an m x m vertex grid, 0 on its boundary."""
+    b = np.ones((m, m))
+    b[0, :] = b[-1, :] = b[:, 0] = b[:, -1] = 0
+    return b.ravel()
+
+
+def masked_prolongation(R: sp.csr_matrix, mf: int) -> sp.csr_matrix:
+    """Bilinear prolongation with the rows of fine and the columns of coarse
+    boundary nodes removed: the coarse functions satisfy u = 0 there."""
+    mc = (mf - 1) // 2 + 1
+    return sp.csr_matrix(sp.diags(interior_mask(mf)) @ prolongation(R) @ sp.diags(interior_mask(mc)))
+
+
+class Hierarchy:
+    """Device CSR matrices of the level hierarchy (level 0 = the matrix graph)."""
+
+    def __init__(self, n: int, levels: int, row_ptr0: torch.Tensor, cols0: torch.Tensor, dirichlet: bool = True):
+        assert n % (1 << (levels - 1)) == 0, "grid size must be divisible by 2^(levels-1)"
+        self.levels = levels
+        self.sizes = [(n >> l) + 1 for l in range(levels)]
+        self.rows = [m * m for m in self.sizes]
+        self.keep = []
+        dev = "cuda"
+
+        def dcsr(M):
+            M = sp.csr_matrix(M)
+            M.sort_indices()
+            t = (torch.as_tensor(M.indptr.astype(np.int32), device=dev),
+                 torch.as_tensor(M.indices.astype(np.int32), device=dev),
+                 torch.as_tensor(M.data.astype(np.float32), device=dev))
+            self.keep.append(t)
+            return t
+
+        self.graph = [(row_ptr0, cols0, None)] + [dcsr(grid_graph(m)) for m in self.sizes[1:]]
+        self.restr, self.restrT, self.prol, self.prolT = [], [], [], []
+        for l in range(levels - 1):
+            R = restriction(self.sizes[l])
+            P = masked_prolongation(R, self.sizes[l]) if dirichlet else prolongation(R)
+            self.restr.append(dcsr(R))
+            self.restrT.append(dcsr(R.T))
+            self.prol.append(dcsr(P))
+            self.prolT.append(dcsr(P.T))
+
+
+def param_count(layers: int, levels: int) -> int:
+    """W_in[2][64], b_in[64]; per layer W1, W2 [64][64], b[64]; per level head w[64], beta."""
+    return 3 * F + layers * (2 * F * F + F) + levels * (F + 1)
+
+
+def init_params(layers: int, levels: int, seed: int = 0, head_scale: float = 0.01) -> np.ndarray:
+    """He-style hidden weights; heads near zero, so that the initial
+    preconditioner is multilevel diagonal scaling (c_l ~ 0)."""
+    rng = np.random.default_rng(seed)
+    parts = [rng.normal(0, 1.0, (2, F)), np.zeros(F)]
+    for _ in range(layers):
+        parts += [rng.normal(0, np.sqrt(1.0 / F), (F, F)), rng.normal(0, np.sqrt(1.0 / F), (F, F)), np.zeros(F)]
+    for _ in range(levels):
+        parts += [rng.normal(0, head_scale, F), np.zeros(1)]
+    p = np.concatenate([p.ravel() for p in parts]).astype(np.float32)
+    assert p.size == param_count(layers, levels)
+    return p
+
+
+class MPNN:
+    """ctypes wrapper of the afem_mpnn handle."""
+
+    def __init__(self, ctx: fem.Context, hier: Hierarchy, layers: int = 6, max_batch: int = 8):
+        self.ctx = ctx
+        self.hier = hier
+        L = hier.levels
+        layers = min(layers, L)
+        P = C.c_void_p
+
+        def arr(items, k):
+            return (P * L)(*[P(0 if it is None or it[k] is None else it[k].data_ptr()) for it in items] +
+                           [P(0)] * (L - len(items)))
+
+        h = P()
+        sizes = (C.c_int * L)(*hier.rows)
+        args = [arr(hier.graph, 0), arr(hier.graph, 1), arr(hier.graph, 2)]
+        for mats in (hier.restr, hier.restrT, hier.prol, hier.prolT):
+            args += [arr(mats, 0), arr(mats, 1), arr(mats, 2)]
+        L_ = _capi.lib()
+        L_.afem_mpnn_create.restype = C.c_int
+        rc = L_.afem_mpnn_create(ctx.handle, C.c_int(L), C.c_int(layers), sizes, *args, C.c_int(max_batch),
+                                 C.byref(h))
+        _capi.check(rc, "afem_mpnn_create")
+        self.handle = h
+        self.max_batch = max_batch
+        self.nparam = int(_capi.lib().afem_mpnn_param_count(h))
+        self.n0 = hier.rows[0]
+        self.levels = L
+        self.layers = layers
+
+    def set_params(self, p):
+        t = torch.as_tensor(np.asarray(p, np.float32), device="cuda")
+        call("afem_mpnn_set_params", self.handle, _ptr(t))
+
+    def get_params(self) -> np.ndarray:
+        t = torch.empty(self.nparam, dtype=torch.float32, device="cuda")
+        call("afem_mpnn_get_params", self.handle, _ptr(t))
+        return t.cpu().numpy()
+
+    def set_operator(self, row_ptr, cols, values):
+        call("afem_mpnn_set_operator", self.handle, int(row_ptr.numel()) - 1, _ptr(row_ptr), _ptr(cols),
+             _ptr(values))
+
+    def scalings(self, level: int) -> torch.Tensor:
+        d = torch.empty(self.hier.rows[level], dtype=torch.float32, device="cuda")
+        call("afem_mpnn_scalings", self.handle, level, _ptr(d))
+        return d
+
+    def forward(self, r: torch.Tensor) -> torch.Tensor:
+        b = r.numel() // self.n0
+        z = torch.empty_like(r, dtype=torch.float32)
+        call("afem_mpnn_forward", self.handle, b, _ptr(r.contiguous()), _ptr(z))
+        return z
+
+    def gradients(self, r, e):
+        b = r.numel() // self.n0
+        g = torch.empty(self.nparam, dtype=torch.float32, device="cuda")
+        loss = C.c_double()
+        call("afem_mpnn_gradients", self.handle, b, _ptr(r.contiguous()), _ptr(e.contiguous()), _ptr(g),
+             C.byref(loss))
+        return g, float(loss.value)
+
+    def train_step(self, r, e, lr):
+        b = r.numel() // self.n0
+        loss = C.c_double()
+        call("afem_mpnn_train_step", self.handle, b, _ptr(r.contiguous()), _ptr(e.contiguous()), C.c_float(lr),
+             C.byref(loss))
+        return float(loss.value)
+
+    def fcg(self, row_ptr, cols, values, b, x, options=None) -> _capi.SolveInfo:
+        info = _capi.SolveInfo()
+        opt = options or fem.solver_options()
+        call("afem_fcg_solve", self.ctx.handle, int(row_ptr.numel()) - 1, _ptr(row_ptr), _ptr(cols), _ptr(values),
+             _ptr(b), _ptr(x), self.handle, C.byref(opt), C.byref(info))
+        return info
+
+    def close(self):
+        if self.handle:
+            call("afem_mpnn_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# The variable-coefficient diffusion problem
+
+def gaussian_random_field(seed: int, corr: float = 0.05, var: float = 1.0, grid: int = 1024) -> np.ndarray:
+    """Periodic GRF on [0,1)^2 with Gaussian covariance exp(-d^2 / (2 corr^2)), unit variance."""
+    rng = np.random.default_rng(seed)
+    k = np.fft.fftfreq(grid, d=1.0 / grid)
+    kx, ky = np.meshgrid(k, k, indexing="ij")
+    spec = np.exp(-0.5 * (2 * np.pi * corr) ** 2 * (kx ** 2 + ky ** 2))
+    noise = rng.standard_normal((grid, grid)) + 1j * rng.standard_normal((grid, grid))
+    g = np.real(np.fft.ifft2(np.sqrt(spec) * noise))
+    g = (g - g.mean()) / g.std() * np.sqrt(var)
+    return g
+
+
+def sample_bilinear(field: np.ndarray, x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    n = field.shape[0]
+    fx, fy = (x % 1.0) * n, (y % 1.0) * n
+    i0, j0 = np.floor(fx).astype(int) % n, np.floor(fy).astype(int) % n
+    i1, j1 = (i0 + 1) % n, (j0 + 1) % n
+    tx, ty = fx - np.floor(fx), fy - np.floor(fy)
+    return ((1 - tx) * (1 - ty) * field[i0, j0] + tx * (1 - ty) * field[i1, j0] + (1 - tx) * ty * field[i0, j1] +
+            tx * ty * field[i1, j1])
+
+
+def bumps(rng, x, y, count=8):
+    """sum of `count` Gaussian bumps: amplitudes N(0,1), centres U[0,1]^2, widths U[0.02, 0.1]."""
+    f = np.zeros_like(x)
+    for _ in range(count):
+        a, cx, cy, w = rng.standard_normal(), rng.uniform(), rng.uniform(), rng.uniform(0.02, 0.1)
+        f += a * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * w * w))
+    return f
+
+
+class DiffusionProblem:
+    """Assembled -div(k grad u) = f on the unit square, u = 0 on the boundary."""
+
+    def __init__(self, ctx: fem.Context, n: int = 512, seed: int = 7, jitter: float = 0.2):
+        self.ctx = ctx
+        self.n = n
+        self.mesh = meshgen.unit_square_tri(n, jitter=jitter, seed=seed)
+        m = self.mesh
+        cent = m.coords[m.cells].mean(axis=1)
+        g = gaussian_random_field(seed + 1)
+        self.k = np.exp(sample_bilinear(g, cent[:, 0], cent[:, 1]))
+        self.fmt = fem.BSRFormat(ctx, fem.Mesh.from_host(2, m.coords, m.cells))
+        self.fmt.initialize(1)
+        self.fmt.compute_sparsity()
+        self.fmt.assemble_poisson(torch.as_tensor(self.k, device="cuda"))
+        self.boundary = torch.as_tensor(m.groups["boundary"], device="cuda")
+        ls = fem.DoFLinearSystem(ctx, m.nb_node)
+        self.fmt.to_linear_system(ls)
+        ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW_COLUMN, self.boundary, 1, 0, 0.0)
+        ls.apply_matrix_transformation()
+        self.ls = ls
+        self.row_ptr, self.cols, self.values = self.fmt.to_csr()
+        # lumped load weights: sum of area / 3 over the incident cells
+        w = torch.zeros(m.nb_node, dtype=torch.float64, device="cuda")
+        self.fmt.rhs_constant_source(1.0, w)
+        self.lumped = w
+        self.interior = torch.ones(m.nb_node, dtype=torch.float64, device="cuda")
+        self.interior[self.boundary.long()] = 0.0
+
+    def rhs(self, rng) -> torch.Tensor:
+        f = bumps(rng, self.mesh.coords[:, 0], self.mesh.coords[:, 1])
+        return self.lumped * torch.as_tensor(f, device="cuda") * self.interior
+
+    def apply(self, x: torch.Tensor) -> torch.Tensor:
+        y = torch.empty_like(x)
+        fem.spmv_csr(self.ctx, self.row_ptr, self.cols, self.values, x, y)
+        return y
+
+    def cg(self, b, rtol=1e-8, max_iter=20000, precision=fem.PRECISION_FP64):
+        x = torch.zeros_like(b)
+        info = fem.cg_solve_csr(self.ctx, self.row_ptr, self.cols, self.values, b, x,
+                                options=fem.solver_options(rtol=rtol, max_iter=max_iter, precision=precision))
+        return x, info
+
+
+def cg_steps(prob: DiffusionProblem, b: torch.Tensor, x: torch.Tensor, iters: int) -> None:
+    """`iters` iterations of Jacobi FP64 CG from the current x (a restart)."""
+    info = _capi.SolveInfo()
+    opt = fem.solver_options(rtol=1e-300, max_iter=iters)
+    rc = _capi.lib().afem_cg_solve_csr(prob.ctx.handle, int(prob.row_ptr.numel()) - 1, _ptr(prob.row_ptr),
+                                       _ptr(prob.cols), _ptr(prob.values), _ptr(b), _ptr(x), _ptr(None),
+                                       C.byref(opt), C.byref(info))
+    if rc not in (0, _capi.NOT_CONVERGED):
+        _capi.check(rc, "afem_cg_solve_csr")
+
+
+def make_training_pairs(prob: DiffusionProblem, count: int, solves: int, every: int = 25, seed: int = 11):
+    """`count` (residual, error) pairs generated by the solver: for each of
+    `solves` bump right-hand sides b, the converged solution x* (CG to 1e-10)
+    and the iterates x_k of Jacobi CG restarted every `every` iterations from
+    x_0 = 0; the pair is (r_k = A e_k, e_k = x* - x_k), so early pairs carry
+    rough errors and late ones the smooth errors CG leaves behind."""
+    rng = np.random.default_rng(seed)
+    n = prob.mesh.nb_node
+    R = torch.empty((count, n), dtype=torch.float32, device="cuda")
+    E = torch.empty((count, n), dtype=torch.float32, device="cuda")
+    per = -(-count // solves)
+    s = 0
+    while s < count:
+        b = prob.rhs(rng)
+        xs, _ = prob.cg(b, rtol=1e-10)
+        x = torch.zeros_like(b)
+        for k in range(per):
+            if s >= count:
+                break
+            if k:
+                cg_steps(prob, b, x, every)
+            e = xs - x
+            R[s] = prob.apply(e).float()
+            E[s] = e.float()
+            s += 1
+    return R, E
+
+
+def train(net: MPNN, R, E, epochs=6, batch=8, lr=2e-3, seed=0, log=None):
+    """Adam on the mean relative squared error; returns the per-epoch mean loss."""
+    rng = np.random.default_rng(seed)
+    count = R.shape[0]
+    hist = []
+    step = 0
+    total = epochs * (count // batch)
+    for ep in range(epochs):
+        perm = rng.permutation(count)
+        losses = []
+        for i in range(0, count - batch + 1, batch):
+            idx = torch.as_tensor(perm[i:i + batch], device="cuda")
+            cur = lr * 0.5 * (1 + np.cos(np.pi * step / max(total, 1)))   # cosine decay
+            losses.append(net.train_step(R[idx], E[idx], cur))
+            step += 1
+        hist.append(float(np.mean(losses)))
+        if log:
+            log(f"epoch {ep}: loss {hist[-1]:.4f}")
+    return hist
+
+
+def train_validated(net: MPNN, prob: DiffusionProblem, R, E, b_val, epochs=6, batch=16, lr=2e-3, rtol=1e-8,
+                    log=None):
+    """Train, then let the solver judge: FCG on the held-out right-hand side
+    b_val with the parameters before and after training; the ones that reach
+    rtol in fewer iterations stay in the network.  Returns the loss history
+    and both iteration counts."""
+    opt = fem.solver_options(rtol=rtol, max_iter=20000)
+    before = net.get_params()
+    x = torch.zeros_like(b_val)
+    it_before = net.fcg(prob.row_ptr, prob.cols, prob.values, b_val, x, opt).iterations
+    hist = train(net, R, E, epochs=epochs, batch=batch, lr=lr, log=log)
+    x = torch.zeros_like(b_val)
+    it_after = net.fcg(prob.row_ptr, prob.cols, prob.values, b_val, x, opt).iterations
+    kept = "trained"
+    if it_after > it_before:
+        net.set_params(before)
+        kept = "untrained"
+    return {"loss": hist, "iterations_untrained": it_before, "iterations_trained": it_after, "kept": kept}
+
+
+def setup(ctx: fem.Context, n=512, levels=9, layers=6, seed=7, max_batch=8):
+    prob = DiffusionProblem(ctx, n=n, seed=seed)
+    hier = Hierarchy(n, levels, prob.row_ptr, prob.cols)
+    net = MPNN(ctx, hier, layers=layers, max_batch=max_batch)
+    net.set_params(init_params(net.layers, levels, seed))
+    net.set_operator(prob.row_ptr, prob.cols, prob.values)
+    return prob, hier, net

@@ -312,6 +312,64 @@ afem_status afem_ls_solve(afem_linear_system ls, const afem_solver_options* opt,
 afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
                           const double* values_d, const double* x_d, double* y_d);
 
+/* ---------------------------------------------------------------------- */
+/* Learned preconditioner.  No counterpart in the reference (it delegates to
+ * HYPRE BoomerAMG / PETSc / Aleph): an additive multilevel preconditioner
+ *   M r = sum_l Q_l diag(d_l) Q_l^T r,  Q_0 = I,  Q_{l+1} = Q_l P_l,
+ * linear and symmetric positive definite in r, whose per-node level scalings
+ *   d_l = base_l * exp(c_l),  base_l = (R..R 1) / (R..R diag A)
+ * come from a message-passing network on the mesh graph (6 layers, width 64,
+ * BF16 tensor-core GEMMs with FP32 accumulation), trained on the GPU with this
+ * library's forward and backward kernels and applied inside flexible CG.
+ * With c = 0 the preconditioner is multilevel diagonal scaling.
+ *
+ * The caller provides the level hierarchy as device CSR matrices (FP32
+ * weights): graph[l] (level l adjacency, symmetric; level 0 = the matrix
+ * graph, its weights are set from A by afem_mpnn_set_operator and graph_w[0]
+ * is ignored), restr[l] (level l -> l+1), prol[l] (level l+1 -> l) and their
+ * transposes.  The pointer arrays are host arrays of device pointers. */
+typedef struct afem_mpnn_s* afem_mpnn;
+
+afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, const int* level_rows_h,
+                             const int32_t* const* graph_rp_h, const int32_t* const* graph_cols_h,
+                             const float* const* graph_w_h, const int32_t* const* restr_rp_h,
+                             const int32_t* const* restr_cols_h, const float* const* restr_w_h,
+                             const int32_t* const* restrT_rp_h, const int32_t* const* restrT_cols_h,
+                             const float* const* restrT_w_h, const int32_t* const* prol_rp_h,
+                             const int32_t* const* prol_cols_h, const float* const* prol_w_h,
+                             const int32_t* const* prolT_rp_h, const int32_t* const* prolT_cols_h,
+                             const float* const* prolT_w_h, int max_batch, afem_mpnn* net);
+afem_status afem_mpnn_destroy(afem_mpnn net);
+/* nb_layers (1..nb_levels) message-passing layers run on levels
+ * 0..nb_layers-1; deeper levels take the restricted output of the last layer.
+ * Number of FP32 parameters.  Flat layout: W_in[2][64], b_in[64]; per layer
+ * W1[64][64], W2[64][64], b[64]; then per level a head w[64], beta. */
+int afem_mpnn_param_count(afem_mpnn net);
+afem_status afem_mpnn_set_params(afem_mpnn net, const float* params_d);
+afem_status afem_mpnn_get_params(afem_mpnn net, float* params_d);
+/* Diagonal, level-0 edge weights -A_ij / sqrt(A_ii A_jj), coefficient
+ * features and base scalings from the FP64 CSR operator (same graph as level
+ * 0).  Synchronous (one host reduction of log diag A). */
+afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
+                                   const double* values_d);
+/* z = M r for `batch` FP32 vectors stored one after the other. */
+afem_status afem_mpnn_forward(afem_mpnn net, int batch, const float* r_d, float* z_d);
+/* The level-l scalings d_l (level_rows[l] floats). */
+afem_status afem_mpnn_scalings(afem_mpnn net, int level, float* d_d);
+/* Gradient of the mean relative squared error ||M r - e||^2 / ||e||^2 over
+ * the batch (grad_d: param_count floats, nullable) and the loss (host,
+ * nullable; non-null makes the call synchronous). */
+afem_status afem_mpnn_gradients(afem_mpnn net, int batch, const float* r_d, const float* e_d, float* grad_d,
+                                double* loss_h);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss. */
+afem_status afem_mpnn_train_step(afem_mpnn net, int batch, const float* r_d, const float* e_d, float lr,
+                                 double* loss_h);
+/* Flexible CG (FCG(1)) on the FP64 CSR system with M as the preconditioner;
+ * FP64 vectors, dots and true residual, M applied in FP32.  Synchronous. */
+afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
+                           const double* values_d, const double* b_d, double* x_d, afem_mpnn net,
+                           const afem_solver_options* opt, afem_solve_info* info);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -1,0 +1,89 @@
+"""Learned preconditioner on the GPU: scalings, forward and gradients against
+the CPU oracle, training reduces the loss, and what the trained network gains
+in flexible CG over the same multilevel form untrained and over Jacobi CG
+(the method without it)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from arcanefem_gb300 import fem, learned
+from oracle import mpnn_oracle as MO
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_net(prob, hier, layers):
+    rp = prob.row_ptr.cpu().numpy()
+    cols = prob.cols.cpu().numpy()
+    vals = prob.values.cpu().numpy()
+    A = sp.csr_matrix((vals, cols, rp), shape=(rp.size - 1, rp.size - 1))
+    graphs = [None] + [learned.grid_graph(s) for s in hier.sizes[1:]]
+    R = [learned.restriction(hier.sizes[l]) for l in range(hier.levels - 1)]
+    P = [learned.masked_prolongation(R[l], hier.sizes[l]) for l in range(hier.levels - 1)]
+    return MO.Net(A, graphs, R, P, layers=layers, bf16_round=True)
+
+
+def test_zero_heads_give_multilevel_diagonal_scaling(cuda_ctx):
+    prob, hier, net = learned.setup(cuda_ctx, n=32, levels=4, layers=2, seed=2, max_batch=1)
+    net.set_params(np.zeros(net.nparam, np.float32))
+    onet = oracle_net(prob, hier, 2)
+    for l in range(hier.levels):
+        d = net.scalings(l).cpu().numpy()
+        assert np.allclose(d, onet.base[l], rtol=1e-5, atol=0), l
+    net.close()
+
+
+@pytest.mark.parametrize("layers", [5, 3])
+def test_forward_and_gradients_match_oracle(cuda_ctx, layers):
+    prob, hier, net = learned.setup(cuda_ctx, n=32, levels=5, layers=layers, seed=5, max_batch=2)
+    rng = np.random.default_rng(0)
+    params = learned.init_params(layers, 5, seed=9, head_scale=0.1)
+    params[2 * 64:3 * 64] = 0.05
+    net.set_params(params)
+    n = prob.mesh.nb_node
+    e = torch.as_tensor(rng.standard_normal((2, n)), device="cuda") * prob.interior
+    r = torch.stack([prob.apply(e[0].contiguous()), prob.apply(e[1].contiguous())])
+    R, E = r.float().contiguous(), e.float().contiguous()
+    z = net.forward(R).cpu().numpy()
+    g, loss = net.gradients(R, E)
+    g = g.cpu().numpy()
+    onet = oracle_net(prob, hier, layers)
+    p64 = net.get_params().astype(np.float64)
+    rs = [R[i].cpu().numpy().astype(np.float64) for i in range(2)]
+    es = [E[i].cpu().numpy().astype(np.float64) for i in range(2)]
+    zo = np.stack([onet.forward(p64, rs[i]) for i in range(2)])
+    assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 1e-2
+    lo, go = onet.loss_and_grad(p64, rs, es)
+    assert abs(loss - lo) / lo < 1e-2
+    cos = float(np.dot(g, go) / (np.linalg.norm(g) * np.linalg.norm(go)))
+    rel = float(np.linalg.norm(g - go) / np.linalg.norm(go))
+    assert cos > 0.998 and rel < 6e-2, (cos, rel)
+    net.close()
+
+
+def test_training_and_learned_fcg(cuda_ctx):
+    prob, hier, net = learned.setup(cuda_ctx, n=128, levels=7, layers=6, seed=3, max_batch=16)
+    R, E = learned.make_training_pairs(prob, count=384, solves=6, every=20, seed=4)
+    b_val = prob.rhs(np.random.default_rng(98))
+    rep = learned.train_validated(net, prob, R, E, b_val, epochs=8, batch=16, lr=2e-3)
+    hist = rep["loss"]
+    assert hist[-1] < 0.9 * hist[0], hist
+    b = prob.rhs(np.random.default_rng(99))
+    _, info_cg = prob.cg(b, rtol=1e-8)
+    x = torch.zeros_like(b)
+    info = net.fcg(prob.row_ptr, prob.cols, prob.values, b, x, fem.solver_options(rtol=1e-8, max_iter=2000))
+    assert info.status == 0 and info.relres < 1e-8
+    print(f"FCG untrained {rep['iterations_untrained']}, trained {rep['iterations_trained']} "
+          f"(kept {rep['kept']}), test rhs {info.iterations}, Jacobi CG {info_cg.iterations}")
+    # what the learned preconditioner gains over the method without it (Jacobi CG)
+    assert info.iterations * 3 < info_cg.iterations, (info.iterations, info_cg.iterations)
+    # the solver's judgement keeps the better parameter set
+    xv = torch.zeros_like(b_val)
+    kept = net.fcg(prob.row_ptr, prob.cols, prob.values, b_val, xv, fem.solver_options(rtol=1e-8, max_iter=2000))
+    assert kept.iterations == min(rep["iterations_untrained"], rep["iterations_trained"])
+    # the device-side FCG graph is reused on a second solve with the same pointers
+    x.zero_()
+    info2 = net.fcg(prob.row_ptr, prob.cols, prob.values, b, x, fem.solver_options(rtol=1e-8, max_iter=2000))
+    assert info2.iterations == info.iterations and info2.relres < 1e-8
+    net.close()
