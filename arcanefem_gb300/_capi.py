@@ -105,6 +105,15 @@ SIGNATURES = {
     "afem_mpnn_train_step": (C.c_int, [_P, C.c_int, _P, _P, C.c_float, C.POINTER(C.c_double)]),
     "afem_fcg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.POINTER(SolverOptions),
                                  C.POINTER(SolveInfo)]),
+    "afem_batch_create": (C.c_int, None),
+    "afem_batch_destroy": (C.c_int, [_P]),
+    "afem_batch_set_config": (C.c_int, None),
+    "afem_batch_get_config": (C.c_int, None),
+    "afem_batch_team": (C.c_int, None),
+    "afem_batch_set_weights": (C.c_int, None),
+    "afem_batch_solve": (C.c_int, None),
+    "afem_batch_autotune": (C.c_int, None),
+    "afem_batch_failure_test": (C.c_int, [_P, C.c_int, C.c_longlong]),
 }
 
 _lib = None

@@ -370,6 +370,76 @@ afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* row_ptr_d, co
                            const double* values_d, const double* b_d, double* x_d, afem_mpnn net,
                            const afem_solver_options* opt, afem_solve_info* info);
 
+/* ---------------------------------------------------------------------- */
+/* Batched 2D Poisson P1: many independent instances (the Poisson module's
+ * assemble + Dirichlet elimination + solve, modules/poisson/FemModule.cc:
+ * 163-196, once per instance) with 4 right-hand sides each, assembled and
+ * solved in ONE persistent cooperative launch captured in a CUDA graph.
+ * Each instance is solved by its own team of CTAs (sized by a cost model);
+ * FP64 iterative refinement around FP32 Jacobi CG.  No counterpart in the
+ * reference, which runs one system per module execution. */
+typedef struct afem_batch_s* afem_batch;
+
+typedef struct {
+  int nb_node, nb_cell;
+  const double* coords_d;       /* [nb_node][3] */
+  const int32_t* cells_d;       /* [nb_cell][3] triangles */
+  const int32_t* nc_ptr_d;      /* node -> cell incidence (afem_node_cell_build) */
+  const int32_t* nc_cell_d;
+  const uint8_t* nc_local_d;
+  const uint8_t* nc_slot_d;     /* slot map (afem_sparsity_cols) */
+  const int32_t* row_ptr_d;     /* CSR structure (afem_sparsity_rows / _cols) */
+  const int32_t* cols_d;
+  const uint8_t* dirichlet_d;   /* [nb_node]: 1 = u = 0 there (row-column elimination) */
+  const float* sources_d;       /* [4][8][4]: per right-hand side 8 Gaussian bumps
+                                   (amplitude, centre x, centre y, width); f_k(x) =
+                                   sum a exp(-|x - c|^2 / (2 w^2)), b_i = m_i f_k(x_i)
+                                   with m_i the lumped area (sum of |T| / 3) */
+  double* values_d;             /* out: FP64 CSR values after elimination [nnz] */
+  double* rhs_d;                /* out: right-hand sides [nb_node][4] */
+  double* x_d;                  /* out: solutions [nb_node][4] (16-byte aligned) */
+} afem_batch_instance;
+
+typedef struct {
+  int block;                    /* threads per CTA: 128, 256 or 512 */
+  int blocks_per_sm;            /* CTAs per SM (clamped to the occupancy) */
+  float cost_exponent;          /* team size ~ rows^(cost_exponent / 2) */
+} afem_batch_config;
+
+typedef struct {
+  int inner_iterations;         /* FP32 CG iterations, all refinement steps */
+  int refinements;              /* FP64 refinement steps */
+  int status;
+  float finish_ms;              /* time from the launch's start to this instance's finish */
+  double relres[4];             /* final FP64 ||b - A x|| / ||b|| per right-hand side */
+} afem_batch_result;
+
+afem_status afem_batch_create(afem_context ctx, int nb_inst, const afem_batch_instance* inst_h, afem_batch* batch);
+afem_status afem_batch_destroy(afem_batch batch);
+afem_status afem_batch_set_config(afem_batch batch, const afem_batch_config* cfg);
+afem_status afem_batch_get_config(afem_batch batch, afem_batch_config* cfg, int* grid);
+/* Team sizes in proportion to explicit per-instance weights (nb_inst
+ * positive values; null returns to the cost model), e.g. measured
+ * finish_ms x CTAs of a previous run. */
+afem_status afem_batch_set_weights(afem_batch batch, const double* weights_h);
+/* The CTA range of instance `inst` in the persistent grid. */
+afem_status afem_batch_team(afem_batch batch, int inst, int* cta0, int* ncta);
+/* Assemble and solve every instance (opt: rtol on the FP64 residual,
+ * inner_rtol of the FP32 CG, max_iter per inner solve).  results_h: nb_inst
+ * entries (nullable); ms: device time of the graph launch (nullable).
+ * Synchronous. */
+afem_status afem_batch_solve(afem_batch batch, const afem_solver_options* opt, afem_batch_result* results_h,
+                             float* ms);
+/* Time every candidate configuration (reps timed runs after one warm-up,
+ * minimum kept; times_ms[c] = -1 for a candidate that cannot run), keep the
+ * fastest (*best = its index). */
+afem_status afem_batch_autotune(afem_batch batch, const afem_solver_options* opt, const afem_batch_config* cands,
+                                int nb_cands, int reps, float* times_ms, int* best);
+/* Failure-detection test: CTA `stall_cta` leaves before its first team
+ * barrier, so its teammates' waits run out after `spin_limit` polls and the
+ * call returns AFEM_ERR_TIMEOUT with the context still usable. */
+afem_status afem_batch_failure_test(afem_batch batch, int stall_cta, long long spin_limit);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif
