@@ -16,6 +16,12 @@ A step is one full assembly of the matrix values (element matrices +
 node-wise gather) with the sparsity reused: the node-wise CSR / AF-BSR hot
 loop of the reference.
 
+Two more sections ride on the same line (rank 0):
+  learned  512^2 variable-coefficient diffusion: time to 1e-8 of plain FP64
+           CG against flexible CG with the learned multilevel preconditioner;
+  batched  64 Poisson instances (N ~ U{64..512}) x 4 right-hand sides,
+           assembled and solved to 1e-8 in one persistent launch.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--workload poisson3d|elasticity3d|poisson2d]
 
@@ -68,6 +74,10 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner section")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched-solve section")
+    p.add_argument("--learned-n", type=int, default=512)
+    p.add_argument("--batched-count", type=int, default=64)
     a = p.parse_args()
     if a.n <= 0:
         a.n = WORKLOADS[a.workload]["n"]
@@ -262,6 +272,8 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, mesh, fmt, lam, mu)
     solve = None if args.no_solve else run_solve(args, ctx, mesh, fmt)
+    learned = None if (args.no_learned or rank != 0) else run_learned(args)
+    batched = None if (args.no_batched or rank != 0) else run_batched(args)
 
     if rank == 0:
         out = {
@@ -277,7 +289,8 @@ def run_gpu(args):
             "fp64_roofline": {"achieved_g_fp64_instr_s": dp_achieved, "peak_g_fma_s": fma_rate,
                               "frac": dp_achieved / fma_rate, "fp64_instr_per_cell": dp_cell,
                               "note": "FP64 issue rate is the binding limit of the element kernel on GB300"},
-            "e2e": e2e, "cpu_baseline": cpu, "solve": solve, "clocks": clk.summary(),
+            "e2e": e2e, "cpu_baseline": cpu, "solve": solve, "learned": learned, "batched": batched,
+            "clocks": clk.summary(),
         }
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -401,6 +414,128 @@ def run_solve(args, ctx, mesh, fmt):
                      "refinements": info.refinements, "true_relres": info.relres, "status": info.status}
         ls.close()
     return res
+
+
+def run_learned(args):
+    """Variable-coefficient diffusion on a 512^2 triangle grid (k = exp(GRF),
+    correlation 0.05, variance 1; bump source; u = 0 on the boundary): time to
+    a 1e-8 FP64 relative residual of plain FP64 CG (Jacobi and none) against
+    flexible CG with the learned multilevel preconditioner (M in FP32, network
+    BF16), trained on 2000 solver-generated pairs.  Device time per solve
+    (CUDA events); training and pair generation reported separately."""
+    import numpy as np
+    import torch
+
+    from arcanefem_gb300 import fem, learned
+
+    n = args.learned_n
+    levels = int(np.log2(n)) if n >= 8 else 3
+    ctx = fem.Context()
+    t0 = time.perf_counter()
+    prob, hier, net = learned.setup(ctx, n=n, levels=levels, layers=6, seed=7, max_batch=16)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    b = prob.rhs(np.random.default_rng(123))
+
+    def best(fn, reps=3):
+        out = [fn() for _ in range(reps)]
+        return min(out, key=lambda i: i.solve_ms)
+
+    def cg(precond):
+        x = torch.zeros_like(b)
+        return fem.cg_solve_csr(ctx, prob.row_ptr, prob.cols, prob.values, b, x,
+                                options=fem.solver_options(rtol=1e-8, max_iter=50000, precond=precond))
+
+    def fcg():
+        x = torch.zeros_like(b)
+        return net.fcg(prob.row_ptr, prob.cols, prob.values, b, x, fem.solver_options(rtol=1e-8, max_iter=5000))
+
+    cg_jac = best(lambda: cg(fem.PRECOND_JACOBI), 2)
+    cg_none = best(lambda: cg(fem.PRECOND_NONE), 1)
+    untrained = best(fcg)
+    t0 = time.perf_counter()
+    R, E = learned.make_training_pairs(prob, count=2000, solves=20, every=25, seed=4)
+    torch.cuda.synchronize()
+    pairs_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rep = learned.train_validated(net, prob, R, E, prob.rhs(np.random.default_rng(77)), epochs=4, batch=16, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    kept = best(fcg)
+    net.close()
+
+    def d(info):
+        return {"solve_ms": info.solve_ms, "iterations": info.iterations, "true_relres": info.relres,
+                "status": info.status}
+    return {
+        "problem": f"-div(k grad u) = f, {n}^2 quads x 2 triangles ({2 * n * n} tris), k = exp(GRF 0.05, var 1)",
+        "target_relres": 1e-8,
+        "plain_fp64_cg_jacobi": d(cg_jac), "plain_fp64_cg_none": d(cg_none),
+        "fcg_multilevel_untrained": d(untrained), "fcg_learned": d(kept),
+        "speedup_vs_plain_fp64_cg_jacobi": cg_jac.solve_ms / kept.solve_ms,
+        "speedup_vs_plain_fp64_cg_none": cg_none.solve_ms / kept.solve_ms,
+        "network": "6 message-passing layers, width 64, BF16 mma.sync GEMMs, FP32 accumulate; 9-level hierarchy",
+        "training": {"pairs": 2000, "pair_generation_s": pairs_s, "train_s": train_s, "loss": rep["loss"],
+                     "fcg_iterations_untrained": rep["iterations_untrained"],
+                     "fcg_iterations_trained": rep["iterations_trained"], "kept": rep["kept"]},
+        "setup_s": setup_s,
+    }
+
+
+def run_batched(args):
+    """64 Poisson instances (sides N ~ U{64..512}, seeded), 4 bump right-hand
+    sides each, assembled and solved to a 1e-8 FP64 relative residual in one
+    persistent cooperative launch (CUDA graph), autotuned; against the same
+    systems solved one right-hand side at a time through the single-system
+    FP64 CG."""
+    import numpy as np
+    import torch
+
+    from arcanefem_gb300 import batch as B
+    from arcanefem_gb300 import fem
+
+    ctx = fem.Context()
+    sizes = B.instance_sizes(args.batched_count, 64, 512, seed=2024)
+    t0 = time.perf_counter()
+    bt = B.Batch(ctx, sizes, seed=7)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    opt = fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000)
+    t0 = time.perf_counter()
+    cands = [(128, 8, 3.0), (128, 8, 3.5), (256, 4, 3.0), (256, 4, 3.5), (256, 3, 3.5), (512, 2, 3.5)]
+    tune = bt.autotune(candidates=cands, options=opt, reps=1)
+    tune_s = time.perf_counter() - t0
+    runs = [bt.solve(opt) for _ in range(3)]
+    res, ms = min(runs, key=lambda r: r[1])
+    # the same systems through the single-system API: FP64 CG, first right-hand side of every instance
+    single_ms = 0.0
+    for i in range(len(sizes)):
+        f = bt.fmts[i]
+        bi = bt.rhs[i][:, 0].contiguous()
+        x = torch.zeros_like(bi)
+        info = fem.cg_solve_csr(ctx, f.row_ptr, f.cols, f.values, bi, x,
+                                options=fem.solver_options(rtol=1e-8, max_iter=50000))
+        single_ms += info.solve_ms
+    cfg, grid = bt.config()
+    dofs = bt.nb_node * B.RHS
+    fin = [r.finish_ms for r in res]
+    out = {
+        "instances": len(sizes), "sides": [min(sizes), max(sizes)], "nodes": bt.nb_node, "nnz": bt.nnz,
+        "rhs_per_instance": B.RHS, "target_relres": 1e-8,
+        "batch_ms": ms, "dof_rhs_per_s": dofs / (ms * 1e-3),
+        "max_relres": max(max(r.relres) for r in res),
+        "inner_iterations_max": max(r.inner_iterations for r in res),
+        "refinements_max": max(r.refinements for r in res),
+        "team_finish_ms": {"min": min(fin), "median": float(np.median(fin)), "max": max(fin)},
+        "config": {**cfg.as_dict(), "grid_ctas": grid, "rebalanced": tune["config"].get("weights") is not None,
+                   "from_cache": tune["cached"]},
+        "autotune_s": tune_s, "setup_s": setup_s,
+        "single_system_fp64_cg_ms_one_rhs": single_ms,
+        "speedup_vs_single_system_4_rhs": 4 * single_ms / ms,
+        "launches_per_batch": 1,
+    }
+    bt.close()
+    return out
 
 
 # ---------------------------------------------------------------------------
