@@ -120,17 +120,20 @@ __device__ __forceinline__ bool team_sync(TeamBar* bar, int T, unsigned* gen_sh,
 // Sum v[0..M) over the block and then over the team (fixed order); the
 // results land in out[0..M) for every thread of every CTA of the team.
 // `region` (0..3) selects the partials slot (see the phase notes below).
-template <int BLOCK, int M>
-__device__ __forceinline__ bool team_reduce(const double (&v)[M], double (&out)[M], const BatchInst& I, int rank,
+// T = float for the inner-solve dot products: per-thread and per-warp sums
+// stay on the FP32 pipe (GB300 issues FP64 at 1/74 of FP32, and the per-row
+// FP64 accumulation bound this kernel), only warp totals go to FP64.
+template <int BLOCK, int M, class T>
+__device__ __forceinline__ bool team_reduce(const T (&v)[M], double (&out)[M], const BatchInst& I, int rank,
                                             int region, double (*red)[8], double* tres, unsigned* gen_sh, int* err,
                                             long long limit) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < M; ++j) {
-    double s = v[j];
+    T s = v[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) red[warp][j] = s;
+    if (lane == 0) red[warp][j] = (double)s;
   }
   __syncthreads();
   if (threadIdx.x < M) {
@@ -309,8 +312,10 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
     // direction p = D^-1 r + beta p_old of every entry it gathers (and writes
     // its own row), so the direction update needs no pass and no barrier of
     // its own; p is double-buffered (p_old is read while p is written).
+    // Every refinement restarts the FP32 CG (a kept direction loses
+    // conjugacy: the FP32 recursive residual drifts from the true one).
     {
-      double lrz[kBatchRhs] = {};
+      float lrz[kBatchRhs] = {};
       const bool a0 = S.active[0], a1 = S.active[1], a2 = S.active[2], a3 = S.active[3];
       for (int row = tid; row < I.n; row += nthr) {
         const double* rr = I.r64 + (int64_t)row * kBatchRhs;
@@ -320,15 +325,15 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
         I.r[row] = rv;
         I.z[row] = make_float4(0.f, 0.f, 0.f, 0.f);   // p_old of the first iteration
         I.d[row] = make_float4(0.f, 0.f, 0.f, 0.f);
-        lrz[0] += (double)rv.x * (di * rv.x); lrz[1] += (double)rv.y * (di * rv.y);
-        lrz[2] += (double)rv.z * (di * rv.z); lrz[3] += (double)rv.w * (di * rv.w);
+        lrz[0] = fmaf(rv.x, di * rv.x, lrz[0]); lrz[1] = fmaf(rv.y, di * rv.y, lrz[1]);
+        lrz[2] = fmaf(rv.z, di * rv.z, lrz[2]); lrz[3] = fmaf(rv.w, di * rv.w, lrz[3]);
       }
       double trz[kBatchRhs];
       if (!team_reduce<BLOCK, kBatchRhs>(lrz, trz, I, rank, 3, red, tres, &gen_sh, err, lim)) return;
       if (threadIdx.x == 0)
         for (int j = 0; j < kBatchRhs; ++j) {
-          S.rz[j] = trz[j];
           S.beta[j] = 0.f;
+          S.rz[j] = trz[j];
         }
       __syncthreads();
     }
@@ -339,7 +344,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
       // row; the row's column and value loads are issued together, then its gathers.
       {
         const float b0 = S.beta[0], b1 = S.beta[1], b2 = S.beta[2], b3 = S.beta[3];
-        double lpq[kBatchRhs] = {};
+        float lpq[kBatchRhs] = {};
         for (int row = tid; row < I.n; row += nthr) {
           const int32_t rb = I.rp[row], e = I.rp[row + 1];
           const int len = e - rb;
@@ -375,8 +380,8 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
                                         fmaf(b2, po.z, di * rv.z), fmaf(b3, po.w, di * rv.w));
           pnew[row] = pr;
           I.q[row] = s;
-          lpq[0] += (double)pr.x * s.x; lpq[1] += (double)pr.y * s.y;
-          lpq[2] += (double)pr.z * s.z; lpq[3] += (double)pr.w * s.w;
+          lpq[0] = fmaf(pr.x, s.x, lpq[0]); lpq[1] = fmaf(pr.y, s.y, lpq[1]);
+          lpq[2] = fmaf(pr.z, s.z, lpq[2]); lpq[3] = fmaf(pr.w, s.w, lpq[3]);
         }
         double pq[kBatchRhs];
         if (!team_reduce<BLOCK, kBatchRhs>(lpq, pq, I, rank, 0, red, tres, &gen_sh, err, lim)) return;
@@ -394,7 +399,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
       // d += alpha p ; r -= alpha q ; <r, D^-1 r>, <r, r>
       {
         const float al0 = S.alpha[0], al1 = S.alpha[1], al2 = S.alpha[2], al3 = S.alpha[3];
-        double lrr[2 * kBatchRhs] = {};
+        float lrr[2 * kBatchRhs] = {};
         for (int row = tid; row < I.n; row += nthr) {
           const float4 pv = pnew[row], qv = I.q[row];
           float4 dv = I.d[row], rv = I.r[row];
@@ -405,10 +410,10 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
           const float di = I.dinv[row];
           I.d[row] = dv;
           I.r[row] = rv;
-          lrr[0] += (double)rv.x * (di * rv.x); lrr[1] += (double)rv.y * (di * rv.y);
-          lrr[2] += (double)rv.z * (di * rv.z); lrr[3] += (double)rv.w * (di * rv.w);
-          lrr[4] += (double)rv.x * rv.x; lrr[5] += (double)rv.y * rv.y;
-          lrr[6] += (double)rv.z * rv.z; lrr[7] += (double)rv.w * rv.w;
+          lrr[0] = fmaf(rv.x, di * rv.x, lrr[0]); lrr[1] = fmaf(rv.y, di * rv.y, lrr[1]);
+          lrr[2] = fmaf(rv.z, di * rv.z, lrr[2]); lrr[3] = fmaf(rv.w, di * rv.w, lrr[3]);
+          lrr[4] = fmaf(rv.x, rv.x, lrr[4]); lrr[5] = fmaf(rv.y, rv.y, lrr[5]);
+          lrr[6] = fmaf(rv.z, rv.z, lrr[6]); lrr[7] = fmaf(rv.w, rv.w, lrr[7]);
         }
         double trr[2 * kBatchRhs];
         if (!team_reduce<BLOCK, 2 * kBatchRhs>(lrr, trr, I, rank, 1, red, tres, &gen_sh, err, lim)) return;

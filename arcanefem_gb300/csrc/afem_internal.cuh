@@ -139,4 +139,20 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return v;
 }
 
+// Block-wide sum of FP32 per-thread partials: warp sums in FP32, warp totals
+// summed in FP64 (result valid in thread 0).  Keeps per-element dot-product
+// work off GB300's narrow FP64 pipe.
+__device__ __forceinline__ double block_sum_f(float v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = (double)v;
+  __syncthreads();
+  int nw = blockDim.x >> 5;
+  double d = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) d = warp_sum(d);
+  __syncthreads();
+  return d;
+}
+
 }  // namespace afem

@@ -13,9 +13,37 @@ constexpr int kSolveBlock = 256;
 
 // ---------------------------------------------------------------------------
 // SpMV: G lanes per row, fixed-order reduction.
+// Thread-per-row form: the row is read in chunks of kRowChunk entries whose
+// column and value loads are all issued before their gathers (predicated past
+// the row end with a zero weight on the row's own entry), so a thread keeps
+// kRowChunk loads in flight.  Entries are summed in increasing k order.
+constexpr int kRowChunk = 8;
+
+template <class Acc, class T, class V>
+__device__ __forceinline__ Acc row_dot_chunked(int row, const int32_t* __restrict__ rp,
+                                               const int32_t* __restrict__ cols, const T* __restrict__ vals,
+                                               const V* __restrict__ x) {
+  Acc s = Acc(0);
+  const int32_t e = __ldg(rp + row + 1);
+  for (int32_t k = __ldg(rp + row); k < e; k += kRowChunk) {
+    int32_t c[kRowChunk];
+    T a[kRowChunk];
+#pragma unroll
+    for (int u = 0; u < kRowChunk; ++u) {
+      const bool in = k + u < e;
+      c[u] = in ? __ldg(cols + k + u) : row;
+      a[u] = in ? __ldg(vals + k + u) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kRowChunk; ++u) s += (Acc)a[u] * (Acc)__ldg(x + c[u]);
+  }
+  return s;
+}
+
 template <int G, class T, class V>
 __device__ __forceinline__ double row_dot(int row, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                           const T* __restrict__ vals, const V* __restrict__ x, int lane) {
+  if constexpr (G == 1) return row_dot_chunked<double>(row, rp, cols, vals, x);
   double s = 0.0;
   const int32_t e = __ldg(rp + row + 1);
   for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s += (double)__ldg(vals + k) * (double)__ldg(x + __ldg(cols + k));
@@ -28,6 +56,23 @@ __device__ __forceinline__ double row_dot(int row, const int32_t* __restrict__ r
 template <int G>
 __device__ __forceinline__ float row_dot_f(int row, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                            const float* __restrict__ vals, const float* __restrict__ x, int lane) {
+  if constexpr (G == 1) {
+    float s = 0.f;
+    const int32_t e = __ldg(rp + row + 1);
+    for (int32_t k = __ldg(rp + row); k < e; k += kRowChunk) {
+      int32_t c[kRowChunk];
+      float a[kRowChunk];
+#pragma unroll
+      for (int u = 0; u < kRowChunk; ++u) {
+        const bool in = k + u < e;
+        c[u] = in ? __ldg(cols + k + u) : row;
+        a[u] = in ? __ldg(vals + k + u) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < kRowChunk; ++u) s = fmaf(a[u], __ldg(x + c[u]), s);
+    }
+    return s;
+  }
   float s = 0.f;
   const int32_t e = __ldg(rp + row + 1);
   for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s = fmaf(__ldg(vals + k), __ldg(x + __ldg(cols + k)), s);
@@ -64,15 +109,30 @@ __device__ __forceinline__ double reduce_partials(const double* partials, int np
 
 inline int lanes_per_row(int n, int64_t nnz) {
   double avg = n > 0 ? (double)nnz / n : 1.0;
+  if (avg <= 24) return 1;   // chunked thread-per-row keeps more loads in flight
   if (avg <= 6) return 4;
   if (avg <= 20) return 8;
   if (avg <= 48) return 16;
   return 32;
 }
 
+// FP64 rows: on GB300 a warp FP64 instruction costs the same whatever its
+// active lanes, so the shuffle-tree reduction and the lane-0 dot-product
+// updates of a lanes-per-row layout multiply the FP64 issue count (measured:
+// the FP64 pipe, not HBM, bound an 8-lane FP64 SpMV).  Short FP64 rows are
+// therefore processed one thread per row, longer ones with few lanes.
+inline int lanes_per_row_fp64(int n, int64_t nnz) {
+  const double avg = n > 0 ? (double)nnz / n : 1.0;
+  if (avg <= 24) return 1;
+  if (avg <= 96) return 4;
+  return 8;
+}
+
 template <class F>
 afem_status dispatch_g(int G, F&& f) {
   switch (G) {
+    case 1: return f(std::integral_constant<int, 1>{});
+    case 2: return f(std::integral_constant<int, 2>{});
     case 4: return f(std::integral_constant<int, 4>{});
     case 8: return f(std::integral_constant<int, 8>{});
     case 16: return f(std::integral_constant<int, 16>{});

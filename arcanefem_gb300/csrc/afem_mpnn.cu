@@ -341,6 +341,62 @@ __global__ void k_sweep(int nrow, int ncol, const int32_t* __restrict__ rp, cons
   }
 }
 
+// The coarse end of the multilevel application in ONE block per vector:
+// levels lo..L-1 are small (<= kCoarseRows rows each), so their down sweep,
+// coarsest scaling and up sweep run back to back with block barriers instead
+// of one launch per level.  In: t_lo ([b][n_lo]); out: w_lo; t_l (l > lo)
+// are kept for the training backward.
+constexpr int kCoarseRows = 8192;
+constexpr int kCoarseBlock = 1024;
+
+struct CoarseLevel {
+  int n;
+  const int32_t *pt_rp, *pt_cols, *p_rp, *p_cols;   // P_l^T (n_{l+1} rows), P_l (n_l rows)
+  const float *pt_w, *p_w, *d;
+  float *t, *w;
+};
+struct CoarsePlan {
+  int lo, L;
+  CoarseLevel lev[kMaxLevels];
+};
+
+__global__ void __launch_bounds__(kCoarseBlock) k_coarse_apply(CoarsePlan plan, const float* __restrict__ t_lo,
+                                                               float* __restrict__ w_lo) {
+  const int64_t b = blockIdx.y;
+  const int lo = plan.lo, L = plan.L;
+  for (int l = lo; l + 1 < L; ++l) {   // t_{l+1} = P_l^T t_l
+    const CoarseLevel& A = plan.lev[l];
+    const CoarseLevel& C = plan.lev[l + 1];
+    const float* tl = (l == lo ? t_lo : A.t) + b * A.n;
+    float* tn = C.t + b * C.n;
+    for (int i = threadIdx.x; i < C.n; i += blockDim.x) {
+      float s = 0.f;
+      for (int32_t k = A.pt_rp[i]; k < A.pt_rp[i + 1]; ++k) s = fmaf(A.pt_w[k], tl[A.pt_cols[k]], s);
+      tn[i] = s;
+    }
+    __syncthreads();
+  }
+  {
+    const CoarseLevel& C = plan.lev[L - 1];
+    const float* tc = (L - 1 == lo ? t_lo : C.t) + b * C.n;
+    float* wc = (L - 1 == lo ? w_lo : C.w) + b * C.n;
+    for (int i = threadIdx.x; i < C.n; i += blockDim.x) wc[i] = C.d[i] * tc[i];
+    __syncthreads();
+  }
+  for (int l = L - 2; l >= lo; --l) {   // w_l = d_l t_l + P_l w_{l+1}
+    const CoarseLevel& A = plan.lev[l];
+    const float* tl = (l == lo ? t_lo : A.t) + b * A.n;
+    const float* wn = plan.lev[l + 1].w + b * plan.lev[l + 1].n;
+    float* wl = (l == lo ? w_lo : A.w) + b * A.n;
+    for (int i = threadIdx.x; i < A.n; i += blockDim.x) {
+      float s = A.d[i] * tl[i];
+      for (int32_t k = A.p_rp[i]; k < A.p_rp[i + 1]; ++k) s = fmaf(A.p_w[k], wn[A.p_cols[k]], s);
+      wl[i] = s;
+    }
+    __syncthreads();
+  }
+}
+
 // y = x / z elementwise (base_l = count_l / diag_l)
 __global__ void k_ratio(int n, const float* __restrict__ x, const float* __restrict__ z, float* __restrict__ y) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -574,6 +630,7 @@ struct afem_mpnn_s {
   float* dc[kMaxLevels] = {};                // dL/dc per level [n_l]
   float* t[kMaxLevels] = {};                 // down sweep [B][n_l] (level 0: the input r, t0)
   const float* t0 = nullptr;
+  int coarse_lo = 0;                         // levels coarse_lo..L-1 run in k_coarse_apply
   float* w[kMaxLevels] = {};                 // up sweep [B][n_l] (w[0] = M r)
   float* s[kMaxLevels] = {};                 // adjoint down sweep [B][n_l]
   double* sums = nullptr;                    // [B][4]
@@ -699,17 +756,40 @@ static afem_status features_forward(afem_mpnn net) {
 // z = M r for `batch` FP32 vectors (r, z: [batch][n0]); with z == nullptr the
 // result stays in w[0] and the down sweep in t[] (training keeps both)
 static afem_status apply(afem_mpnn net, int batch, const float* r, float* z) {
-  const int L = net->L;
+  const int L = net->L, lo = net->coarse_lo;
   if (!net->scalings_valid) AFEM_TRY(features_forward(net));
   net->t0 = r;
   const float* tl = r;
-  for (int l = 0; l + 1 < L; ++l) {
+  for (int l = 0; l < lo; ++l) {   // fine levels: one sweep per level
     AFEM_TRY(sweep(net, &net->Pt[l], batch, tl, nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
     tl = net->t[l + 1];
   }
   float* w0 = z ? z : net->w[0];
-  AFEM_TRY(sweep(net, nullptr, batch, nullptr, net->d[L - 1], tl, L == 1 ? w0 : net->w[L - 1], net->n[L - 1]));
-  for (int l = L - 2; l >= 0; --l)
+  {
+    CoarsePlan plan{};
+    plan.lo = lo;
+    plan.L = L;
+    for (int l = lo; l < L; ++l) {
+      CoarseLevel& c = plan.lev[l];
+      c.n = net->n[l];
+      c.d = net->d[l];
+      c.t = net->t[l];
+      c.w = net->w[l];
+      if (l + 1 < L) {
+        c.pt_rp = net->Pt[l].rp;
+        c.pt_cols = net->Pt[l].cols;
+        c.pt_w = net->Pt[l].w;
+        c.p_rp = net->P[l].rp;
+        c.p_cols = net->P[l].cols;
+        c.p_w = net->P[l].w;
+      }
+    }
+    k_coarse_apply<<<dim3(1, batch), kCoarseBlock, 0, net->ctx->stream>>>(plan, tl, lo == 0 ? w0 : net->w[lo]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "k_coarse_apply", __FILE__, __LINE__);
+    ++net->ctx->launches;
+  }
+  for (int l = lo - 1; l >= 0; --l)   // fine levels back up
     AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], net->d[l], l == 0 ? r : net->t[l], l == 0 ? w0 : net->w[l],
                    net->n[l]));
   return AFEM_OK;
@@ -855,6 +935,8 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
     }
   }
   net->n0 = level_rows[0];
+  net->coarse_lo = nb_levels - 1;
+  while (net->coarse_lo > 0 && level_rows[net->coarse_lo - 1] <= kCoarseRows) --net->coarse_lo;
   net->nparam = off_head(nb_layers, nb_levels);
   const size_t B = max_batch;
   const size_t n0 = net->n0;
@@ -1008,7 +1090,8 @@ afem_status afem_mpnn_train_step(afem_mpnn net, int batch, const float* r_d, con
 // one) with M as the preconditioner.  FP64 vectors, matrix, dot products and
 // stop test; M runs in FP32 on r converted to FP32.  Scalars stay on the
 // device (last-block reductions in a fixed order, deterministic); one
-// iteration is 4 + (2L - 1) kernels, captured in a CUDA graph per chunk of
+// iteration is 4 + (2 lo + 1) kernels (lo fine levels each way, one coarse
+// kernel), captured in a CUDA graph per chunk of
 // iterations, and a device flag makes the remaining kernels of a chunk return
 // once converged.
 //   K1  q = A p ; <p, q>, <r, p>            -> alpha = <r, p> / <p, q>
@@ -1254,7 +1337,7 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
   const int chunk = opt.check_every > 0 ? std::min(opt.check_every, 64) : 4;
   int32_t nnz32 = 0;
   AFEM_TRY(read_scalar(ctx, rp + n, &nnz32));
-  const int G = lanes_per_row(n, nnz32);
+  const int G = lanes_per_row_fp64(n, nnz32);
   const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
   FcgWork* w = nullptr;
@@ -1301,7 +1384,7 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
   if (st == AFEM_OK)
     st = launch(ctx, k_fcg_widen, grid_vec, kSolveBlock, 0, n, (const float*)net->z32, w->z, (const double*)w->q,
                 w->p, 1, w->partials, w->st);
-  const int per_iteration = 4 + 2 * net->L - 1;
+  const int per_iteration = 4 + 2 * net->coarse_lo + 1;
   FcgState hs{};
   while (st == AFEM_OK) {
     cudaError_t ce = cudaMemcpyAsync(ctx->pinned, w->st, sizeof(FcgState), cudaMemcpyDeviceToHost, ctx->stream);

@@ -15,8 +15,12 @@
 // A device flag stops the remaining kernels of a chunk once converged.
 //
 // MIXED precision: FP64 iterative refinement (r = b - A x with FP64 values,
-// FP64 norms) around an FP32 CG (FP32 matrix values and vectors, FP64 dot
-// product accumulation).
+// FP64 norms) around an FP32 CG (FP32 matrix values and vectors; dot products
+// in FP32 per thread and warp, FP64 across warps and blocks), restarted at
+// every refinement.  (Keeping the direction across refinements -- reliable
+// updates -- stalled: after a 1e-4 inner reduction the FP32 recursive
+// residual has drifted too far from the true one for the old direction to
+// stay conjugate.)
 #include <algorithm>
 #include <cmath>
 
@@ -226,8 +230,9 @@ __global__ void k_inv_diag(int n, const int32_t* __restrict__ rp, const int32_t*
 }
 
 // ---------------------------------------------------------------------------
-// FP32 inner CG (mixed precision).  Same structure, FP32 vectors and values,
-// FP64 dot-product accumulation.
+// FP32 inner CG (mixed precision).  Same structure, FP32 vectors and values;
+// dot products accumulate in FP32 per thread and warp, in FP64 across warps
+// and blocks.
 
 template <int G>
 __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv(int n, const int32_t* __restrict__ rp,
@@ -239,7 +244,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv(int n, const int32_t* 
   const int lane = threadIdx.x & (G - 1);
   const int groups = gridDim.x * (blockDim.x / G);
   const int nr = n + ((groups - n % groups) % groups);
-  double pq = 0.0;
+  float pqf = 0.f;
   for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
     float s = 0.f;
     if (row < n) s = row_dot_f<G>(row, rp, cols, vals, p, lane);
@@ -249,10 +254,10 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv(int n, const int32_t* 
     }
     if (row < n && lane == 0) {
       q[row] = s;
-      pq += (double)p[row] * (double)s;
+      pqf = fmaf(p[row], s, pqf);
     }
   }
-  pq = block_sum(pq, sh);
+  const double pq = block_sum_f(pqf, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = pq;
   if (last_block(&st->ticket[1])) {
     double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
@@ -279,18 +284,18 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_update(int n, float* __rest
   if (((volatile CgState*)st)->done) return;
   __shared__ double sh[kSolveBlock / 32];
   const float alpha = (float)((volatile CgState*)st)->alpha;
-  double rz = 0.0, rr = 0.0;
+  float rzf = 0.f, rrf = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] = fmaf(alpha, p[i], x[i]);
     float ri = fmaf(-alpha, q[i], r[i]);
     r[i] = ri;
     float zi = dinv[i] * ri;
     z[i] = zi;
-    rz += (double)ri * (double)zi;
-    if (!(skip && skip[i])) rr += (double)ri * (double)ri;
+    rzf = fmaf(ri, zi, rzf);
+    if (!(skip && skip[i])) rrf = fmaf(ri, ri, rrf);
   }
-  rz = block_sum(rz, sh);
-  rr = block_sum(rr, sh);
+  const double rz = block_sum_f(rzf, sh);
+  const double rr = block_sum_f(rrf, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x * 2 + 0] = rz;
     partials[blockIdx.x * 2 + 1] = rr;
@@ -405,7 +410,7 @@ __global__ void k_fill_f32(int64_t n, float v, float* __restrict__ b) {
 afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals, int64_t nnz,
                     const double* b, double* x, const uint8_t* skip, const afem_solver_options& opt,
                     afem_solve_info* info) {
-  const int G = lanes_per_row(n, nnz);
+  const int G = lanes_per_row_fp64(n, nnz);
   const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned nparts = std::max(grid_rows, grid_vec);
@@ -466,10 +471,12 @@ afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* c
 afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals, int64_t nnz,
                      const double* b, double* x, const uint8_t* skip, const afem_solver_options& opt,
                      afem_solve_info* info) {
-  const int G = lanes_per_row(n, nnz);
+  const int G = lanes_per_row(n, nnz);          // FP32 inner SpMV
+  const int G64 = lanes_per_row_fp64(n, nnz);   // FP64 outer residual
   const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  const unsigned grid_rows64 = grid_for(ctx, (int64_t)n * G64, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
-  const unsigned nparts = std::max(grid_rows, grid_vec);
+  const unsigned nparts = std::max(std::max(grid_rows, grid_rows64), grid_vec);
   size_t need = align256(sizeof(float) * (size_t)nnz) + 6 * align256(sizeof(float) * (size_t)n) +
                 align256(sizeof(double) * 3 * nparts) + 2 * align256(sizeof(CgState));
   AFEM_TRY(scratch_reserve(ctx, need));
@@ -513,8 +520,8 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   afem_status status = AFEM_OK;
   const int max_outer = 100;
   for (;; ++outer_steps) {
-    AFEM_TRY(dispatch_g(G, [&](auto g) {
-      return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b,
+    AFEM_TRY(dispatch_g(G64, [&](auto g) {
+      return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows64, kSolveBlock, 0, n, rp, cols, vals, b,
                     (const double*)x, (const float*)dinv32, skip, r32, x32, z32, p32, partials, outer, inner,
                     inner_rtol, max_iter);
     }));
@@ -607,7 +614,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_true_residual(int n, const int3
 
 afem_status true_relres(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
                         int64_t nnz, const double* b, const double* x, const uint8_t* skip, double* relres) {
-  const int G = lanes_per_row(n, nnz);
+  const int G = lanes_per_row_fp64(n, nnz);
   const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
   AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * 2 * grid_rows) + 512));
   double *partials, *out;
@@ -668,7 +675,7 @@ afem_status solve_csr(afem_context ctx, int n, const int32_t* rp, const int32_t*
 
 afem_status spmv_fp64(afem_context ctx, int n, int64_t nnz, const int32_t* rp, const int32_t* cols,
                       const double* vals, const double* x, double* y) {
-  const int G = lanes_per_row(n, nnz);
+  const int G = lanes_per_row_fp64(n, nnz);
   const unsigned grid = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
   return dispatch_g(G, [&](auto g) {
     return launch(ctx, k_spmv<decltype(g)::value>, grid, kSolveBlock, 0, n, rp, cols, vals, x, y);
@@ -704,7 +711,7 @@ afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* rp, const int3
   AFEM_CHECK_ARG(ctx && n > 0 && rp && cols && vals && x && y, "afem_spmv_csr: bad arguments");
   int32_t nnz = 0;
   AFEM_TRY(read_scalar(ctx, rp + n, &nnz));
-  const int G = lanes_per_row(n, nnz);
+  const int G = lanes_per_row_fp64(n, nnz);
   const unsigned grid = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
   return dispatch_g(G, [&](auto g) {
     return launch(ctx, k_spmv<decltype(g)::value>, grid, kSolveBlock, 0, n, rp, cols, vals, x, y);

@@ -78,6 +78,9 @@ def parse_args():
     p.add_argument("--no-batched", action="store_true", help="skip the batched-solve section")
     p.add_argument("--learned-n", type=int, default=512)
     p.add_argument("--batched-count", type=int, default=64)
+    p.add_argument("--batched-sides", type=int, nargs=2, default=(64, 512), metavar=("MIN", "MAX"))
+    p.add_argument("--batched-tune", choices=["auto", "none"], default="auto",
+                   help="auto: autotune (JSON cache); none: the library's default configuration")
     a = p.parse_args()
     if a.n <= 0:
         a.n = WORKLOADS[a.workload]["n"]
@@ -86,6 +89,19 @@ def parse_args():
 
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def replica_value(total_ms: float, world: int, units_per_rank: int, steps: int, device: str):
+    """Replicas: every rank assembled its own copy; the job time is the max
+    over ranks and the value is all ranks' units over that time."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / steps
+    return ms_per_step, world * units_per_rank / (ms_per_step * 1e-3)
 
 
 def make_mesh(args):
@@ -250,12 +266,7 @@ def run_gpu(args):
     elem_ms = [e[0].elapsed_time(e[1]) for e in events]
     gath_ms = [e[1].elapsed_time(e[2]) for e in events]
     total_ms = sum(a + b for a, b in zip(elem_ms, gath_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms_per_step = total_ms / args.steps
-    value = world * nnz / (ms_per_step * 1e-3)
+    ms_per_step, value = replica_value(total_ms, world, nnz, args.steps, "cuda")
 
     hbm_peak, peak_kind = read_peaks()
     alg = algorithmic_bytes(mesh, nnz)
@@ -495,7 +506,7 @@ def run_batched(args):
     from arcanefem_gb300 import fem
 
     ctx = fem.Context()
-    sizes = B.instance_sizes(args.batched_count, 64, 512, seed=2024)
+    sizes = B.instance_sizes(args.batched_count, args.batched_sides[0], args.batched_sides[1], seed=2024)
     t0 = time.perf_counter()
     bt = B.Batch(ctx, sizes, seed=7)
     torch.cuda.synchronize()
@@ -503,7 +514,8 @@ def run_batched(args):
     opt = fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000)
     t0 = time.perf_counter()
     cands = [(128, 8, 3.0), (128, 8, 3.5), (256, 4, 3.0), (256, 4, 3.5), (256, 3, 3.5), (512, 2, 3.5)]
-    tune = bt.autotune(candidates=cands, options=opt, reps=1)
+    tune = (bt.autotune(candidates=cands, options=opt, reps=1) if args.batched_tune == "auto"
+            else {"cached": False, "config": {}})
     tune_s = time.perf_counter() - t0
     runs = [bt.solve(opt) for _ in range(3)]
     res, ms = min(runs, key=lambda r: r[1])

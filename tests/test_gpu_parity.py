@@ -244,6 +244,33 @@ def test_cg_solution_matches_oracle(cuda_ctx, precision):
         assert info.refinements >= 1
 
 
+def test_mixed_precision_iterations_stay_close_to_fp64(cuda_ctx):
+    """Mixed precision may restart its FP32 CG at each refinement but must not
+    stall: on a 128^2 Poisson problem to 1e-8 its total FP32 iterations stay
+    within 2.5x of the FP64 CG's."""
+    m = meshgen.unit_square_tri(128, seed=5)
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson()
+    rp, cols, vals = f.to_csr()
+    ls = fem.DoFLinearSystem(cuda_ctx, m.nb_node)
+    f.to_linear_system(ls)
+    f.rhs_constant_source(-1.0, ls.rhs_variable())
+    nodes = torch.as_tensor(m.groups["boundary"], device="cuda")
+    ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW_COLUMN, nodes, 1, 0, 0.0)
+    ls.apply_matrix_transformation()
+    ls.apply_rhs_transformation()
+    b = ls.rhs_variable().clone()
+    its = {}
+    for prec in (fem.PRECISION_FP64, fem.PRECISION_MIXED):
+        x = torch.zeros_like(b)
+        info = fem.cg_solve_csr(cuda_ctx, rp, cols, vals, b, x,
+                                options=fem.solver_options(rtol=1e-8, max_iter=20000, precision=prec,
+                                                           inner_rtol=1e-3))
+        assert info.status == 0 and info.relres < 1e-8
+        its[prec] = info.iterations
+    assert its[fem.PRECISION_MIXED] <= 2.5 * its[fem.PRECISION_FP64], its
+
+
 def test_cg_penalty_with_skipped_forced_rows(cuda_ctx):
     m = meshgen.unit_square_tri(24, seed=2)
     f = build_format(cuda_ctx, m)
