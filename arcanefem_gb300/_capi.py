@@ -105,6 +105,8 @@ SIGNATURES = {
     "afem_mpnn_train_step": (C.c_int, [_P, C.c_int, _P, _P, C.c_float, C.POINTER(C.c_double)]),
     "afem_fcg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.POINTER(SolverOptions),
                                  C.POINTER(SolveInfo)]),
+    "afem_rhs_boundary_faces": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, C.c_int,
+                                          C.POINTER(C.c_double), C.c_int, _P]),
     "afem_batch_create": (C.c_int, None),
     "afem_batch_destroy": (C.c_int, [_P]),
     "afem_batch_set_config": (C.c_int, None),

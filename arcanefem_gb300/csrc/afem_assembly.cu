@@ -370,6 +370,77 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int nb_node,
 // Right-hand sides.
 
 // w_c = qdot * measure / npc (ArcaneFemFunctionsGpu.h:703: sum += qdot * domain / nbItem)
+// Boundary-face terms (Neumann flux, traction), per face g * |f| / nf, in
+// the oracle's operation order with no contraction (applyNeumannToRhsTria3 /
+// Tetra4, femutils/ArcaneFemFunctionsGpu.cc:679-735,1082-1140; traction
+// femutils/ArcaneFemFunctions.h:2188-2220,2854-2885).  term[f][c].
+__global__ void k_face_terms(int dim, int nb_face, const double* __restrict__ xyz, const int32_t* __restrict__ fn,
+                             const uint8_t* __restrict__ outward, int mode, double g0, double g1, double g2,
+                             double* __restrict__ term) {
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nb_face; f += gridDim.x * blockDim.x) {
+    const int32_t* q = fn + (int64_t)f * dim;
+    const double* a0 = xyz + 3 * (int64_t)q[0];
+    const double* a1 = xyz + 3 * (int64_t)q[1];
+    const bool out = outward ? outward[f] != 0 : true;
+    const double* b0 = out ? a0 : a1;
+    const double* b1 = out ? a1 : a0;
+    double measure, n0 = 0.0, n1 = 0.0, n2 = 0.0;
+    if (dim == 2) {
+      const double dx = __dsub_rn(a1[0], a0[0]), dy = __dsub_rn(a1[1], a0[1]);
+      measure = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+      const double ex = __dsub_rn(b1[0], b0[0]), ey = __dsub_rn(b1[1], b0[1]);
+      const double nn = __dsqrt_rn(__dadd_rn(__dmul_rn(ey, ey), __dmul_rn(ex, ex)));
+      n0 = __ddiv_rn(ey, nn);
+      n1 = __ddiv_rn(__dsub_rn(b0[0], b1[0]), nn);
+    } else {
+      const double* a2 = xyz + 3 * (int64_t)q[2];
+      const double u0 = __dsub_rn(a1[0], a0[0]), u1 = __dsub_rn(a1[1], a0[1]), u2 = __dsub_rn(a1[2], a0[2]);
+      const double v0 = __dsub_rn(a2[0], a0[0]), v1 = __dsub_rn(a2[1], a0[1]), v2 = __dsub_rn(a2[2], a0[2]);
+      const double c0 = __dsub_rn(__dmul_rn(u1, v2), __dmul_rn(u2, v1));
+      const double c1 = __dsub_rn(__dmul_rn(u2, v0), __dmul_rn(u0, v2));
+      const double c2 = __dsub_rn(__dmul_rn(u0, v1), __dmul_rn(u1, v0));
+      measure = __ddiv_rn(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(c0, c0), __dmul_rn(c1, c1)), __dmul_rn(c2, c2))),
+                          2.0);
+      const double e10 = __dsub_rn(b1[0], b0[0]), e11 = __dsub_rn(b1[1], b0[1]), e12 = __dsub_rn(b1[2], b0[2]);
+      const double e20 = __dsub_rn(a2[0], b0[0]), e21 = __dsub_rn(a2[1], b0[1]), e22 = __dsub_rn(a2[2], b0[2]);
+      const double m0 = __dsub_rn(__dmul_rn(e11, e22), __dmul_rn(e12, e21));
+      const double m1 = __dsub_rn(__dmul_rn(e12, e20), __dmul_rn(e10, e22));
+      const double m2 = __dsub_rn(__dmul_rn(e10, e21), __dmul_rn(e11, e20));
+      const double nn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(m0, m0), __dmul_rn(m1, m1)), __dmul_rn(m2, m2)));
+      n0 = __ddiv_rn(m0, nn);
+      n1 = __ddiv_rn(m1, nn);
+      n2 = __ddiv_rn(m2, nn);
+    }
+    const double nf = (double)dim;
+    double* t = term + 3 * (int64_t)f;
+    if (mode == AFEM_FACE_SCALAR) {
+      t[0] = __ddiv_rn(__dmul_rn(g0, measure), nf);
+    } else if (mode == AFEM_FACE_NORMAL) {
+      double flux = __dadd_rn(__dmul_rn(n0, g0), __dmul_rn(n1, g1));
+      if (dim == 3) flux = __dadd_rn(flux, __dmul_rn(n2, g2));
+      t[0] = __ddiv_rn(__dmul_rn(flux, measure), nf);
+    } else {
+      t[0] = __ddiv_rn(__dmul_rn(g0, measure), nf);
+      t[1] = __ddiv_rn(__dmul_rn(g1, measure), nf);
+      if (dim == 3) t[2] = __ddiv_rn(__dmul_rn(g2, measure), nf);
+    }
+  }
+}
+
+// rhs[n][c] += term of every incident face, in increasing face order.
+__global__ void k_face_gather(int nb_node, const int32_t* __restrict__ ptr, const int32_t* __restrict__ face,
+                              const double* __restrict__ term, int ncomp, int nb_dof, double* __restrict__ rhs) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb_node; n += gridDim.x * blockDim.x) {
+    const int32_t p0 = ptr[n], p1 = ptr[n + 1];
+    if (p0 == p1) continue;
+    for (int c = 0; c < ncomp; ++c) {
+      double acc = rhs[(int64_t)n * nb_dof + c];
+      for (int32_t p = p0; p < p1; ++p) acc = __dadd_rn(acc, term[3 * (int64_t)face[p] + c]);
+      rhs[(int64_t)n * nb_dof + c] = acc;
+    }
+  }
+}
+
 __global__ void k_cell_source_weight(int nb_cell, int dim, const double* __restrict__ xyz,
                                      const int32_t* __restrict__ cn, double qdot, double* __restrict__ w) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
@@ -551,6 +622,53 @@ afem_status afem_rhs_body_force_tet4(afem_context ctx, const afem_mesh_view* m, 
                     (const double*)vol, 3, k, f[k], 1, rhs_d));
   }
   return AFEM_OK;
+}
+
+afem_status afem_rhs_boundary_faces(afem_context ctx, int dim, int nb_node, int nb_face, const double* coords_d,
+                                    const int32_t* face_nodes_d, const uint8_t* outward_d, int mode,
+                                    const double* g_h, int nb_dof, double* rhs_d) {
+  AFEM_CHECK_ARG(ctx, "afem_rhs_boundary_faces: null context");
+  AFEM_CHECK_ARG(dim == 2 || dim == 3, "afem_rhs_boundary_faces: dim must be 2 or 3");
+  AFEM_CHECK_ARG(mode >= AFEM_FACE_SCALAR && mode <= AFEM_FACE_VECTOR, "afem_rhs_boundary_faces: bad mode %d", mode);
+  AFEM_CHECK_ARG(nb_node > 0 && nb_face >= 0 && g_h && rhs_d, "afem_rhs_boundary_faces: bad arguments");
+  AFEM_CHECK_ARG(nb_dof >= (mode == AFEM_FACE_VECTOR ? dim : 1), "afem_rhs_boundary_faces: nb_dof too small");
+  if (nb_face == 0) return AFEM_OK;
+  AFEM_CHECK_ARG(coords_d && face_nodes_d, "afem_rhs_boundary_faces: null mesh arrays");
+  cudaStream_t s = ctx->stream;
+  const size_t total = (size_t)nb_face * dim;
+  int32_t *ptr = nullptr, *face = nullptr, *inv = nullptr;
+  uint8_t* local = nullptr;
+  double* term = nullptr;
+  auto release = [&]() {
+    if (ptr) cudaFreeAsync(ptr, s);
+    if (face) cudaFreeAsync(face, s);
+    if (inv) cudaFreeAsync(inv, s);
+    if (local) cudaFreeAsync(local, s);
+    if (term) cudaFreeAsync(term, s);
+  };
+  cudaError_t e = cudaMallocAsync((void**)&ptr, sizeof(int32_t) * (nb_node + 1), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&face, sizeof(int32_t) * total, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&inv, sizeof(int32_t) * total, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&local, total, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&term, sizeof(double) * 3 * nb_face, s);
+  if (e != cudaSuccess) {
+    release();
+    return cuda_fail(e, "afem_rhs_boundary_faces allocation", __FILE__, __LINE__);
+  }
+  // node -> face incidence in increasing face order (the faces' sequential order)
+  afem_status st = afem_node_cell_build(ctx, nb_node, nb_face, dim, face_nodes_d, ptr, face, local, inv);
+  // the scalar mode reads g_h[0] only, the others dim components
+  const double g0 = g_h[0];
+  const double g1 = mode == AFEM_FACE_SCALAR ? 0.0 : g_h[1];
+  const double g2 = (mode == AFEM_FACE_SCALAR || dim == 2) ? 0.0 : g_h[2];
+  if (st == AFEM_OK)
+    st = launch(ctx, k_face_terms, grid_for(ctx, nb_face, 256), 256, 0, dim, nb_face, coords_d, face_nodes_d,
+                outward_d, mode, g0, g1, g2, term);
+  if (st == AFEM_OK)
+    st = launch(ctx, k_face_gather, grid_for(ctx, nb_node, 256), 256, 0, nb_node, (const int32_t*)ptr,
+                (const int32_t*)face, (const double*)term, mode == AFEM_FACE_VECTOR ? dim : 1, nb_dof, rhs_d);
+  release();
+  return st;
 }
 
 }  // extern "C"

@@ -238,7 +238,7 @@ afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int
   AFEM_CHECK_ARG(ctx, "afem_node_cell_build: null context");
   AFEM_CHECK_ARG(nb_node > 0 && nb_cell > 0, "afem_node_cell_build: empty mesh (nb_node=%d nb_cell=%d)", nb_node,
                  nb_cell);
-  AFEM_CHECK_ARG(npc == 3 || npc == 4, "afem_node_cell_build: nodes_per_cell must be 3 or 4 (got %d)", npc);
+  AFEM_CHECK_ARG(npc >= 2 && npc <= 4, "afem_node_cell_build: nodes_per_cell must be 2, 3 or 4 (got %d)", npc);
   AFEM_CHECK_ARG(nb_cell < (1 << 29), "afem_node_cell_build: too many cells (%d)", nb_cell);
   AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && nc_local_d, "afem_node_cell_build: null buffer");
   int64_t total = (int64_t)nb_cell * npc;

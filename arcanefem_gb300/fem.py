@@ -354,6 +354,18 @@ def cg_solve_csr(ctx: Context, row_ptr, cols, values, b, x, forced_info=None, op
     return info
 
 
+FACE_SCALAR, FACE_NORMAL, FACE_VECTOR = 0, 1, 2
+
+
+def rhs_boundary_faces(ctx: Context, dim: int, coords, face_nodes, outward, mode: int, g, nb_dof: int, rhs):
+    """Neumann flux (scalar or normal) or traction of boundary faces added into
+    rhs: applyNeumannToRhsTria3/Tetra4 and applyTractionToRhsTria3/Tetra4 with
+    a deterministic node-wise gather (see afem_rhs_boundary_faces)."""
+    gv = (C.c_double * 3)(*([float(v) for v in g] + [0.0] * (3 - len(g))))
+    call("afem_rhs_boundary_faces", ctx.handle, dim, int(coords.shape[0]), int(face_nodes.shape[0]), _ptr(coords),
+         _ptr(face_nodes), _ptr(outward), mode, gv, nb_dof, _ptr(rhs))
+
+
 def spmv_csr(ctx: Context, row_ptr, cols, values, x, y):
     call("afem_spmv_csr", ctx.handle, int(row_ptr.numel()) - 1, _ptr(row_ptr), _ptr(cols), _ptr(values), _ptr(x),
          _ptr(y))

@@ -154,3 +154,42 @@ def nnz_formula(mesh: Mesh) -> int:
             pairs.append(lo << 32 | hi)
     nb_edge = np.unique(np.concatenate(pairs)).size
     return mesh.nb_node + 2 * nb_edge
+
+
+def boundary_faces(mesh: Mesh, seed: int = 0):
+    """Boundary faces of a P1 mesh (edges of triangles, triangles of tets),
+    each in a random node order, with its orientation flag: 1 when the order
+    gives the outward normal (edge: (dy, -dx); triangle: (n1-n0) x (n2-n0)),
+    0 when the first two nodes must be swapped for it (Arcane's
+    isSubDomainBoundaryOutside).  Faces come sorted by their node set."""
+    rng = np.random.default_rng(seed)
+    c = mesh.cells
+    if mesh.dim == 2:
+        loc = [(0, 1, 2), (1, 2, 0), (2, 0, 1)]   # edge (a, b), opposite vertex
+    else:
+        loc = [(1, 2, 3, 0), (0, 2, 3, 1), (0, 1, 3, 2), (0, 1, 2, 3)]
+    faces, opp = [], []
+    for t in loc:
+        faces.append(c[:, list(t[:-1])])
+        opp.append(c[:, t[-1]])
+    faces = np.concatenate(faces)
+    opp = np.concatenate(opp)
+    key = np.sort(faces, axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    bnd = cnt[inv.ravel()] == 1
+    f, o = faces[bnd], opp[bnd]
+    order = np.lexsort(np.sort(f, axis=1).T[::-1])
+    f, o = f[order], o[order]
+    # random node order per face
+    perm = np.array([rng.permutation(f.shape[1]) for _ in range(f.shape[0])]) if f.shape[0] else np.zeros((0, f.shape[1]), int)
+    f = np.take_along_axis(f, perm, axis=1).astype(np.int32)
+    X = mesh.coords
+    if mesh.dim == 2:
+        d = X[f[:, 1], :2] - X[f[:, 0], :2]
+        nrm = np.stack([d[:, 1], -d[:, 0]], 1)
+        away = X[o, :2] - X[f[:, 0], :2]
+    else:
+        nrm = np.cross(X[f[:, 1]] - X[f[:, 0]], X[f[:, 2]] - X[f[:, 0]])
+        away = X[o] - X[f[:, 0]]
+    outward = (np.einsum("ij,ij->i", nrm, away) < 0).astype(np.uint8)
+    return f, outward

@@ -84,7 +84,8 @@ afem_status afem_device_fp64_fma_rate(afem_context ctx, double* gfma_per_s_h);
  * cell nc_cell_d[p]; nc_inverse_d[cell*nodes_per_cell + i] = p, the incidence
  * of (cell, local node i) in that list (nullable).  Buffers:
  * nc_ptr_d[nb_node+1], nc_cell_d, nc_local_d and
- * nc_inverse_d[nb_cell*nodes_per_cell].  Deterministic. */
+ * nc_inverse_d[nb_cell*nodes_per_cell].  Deterministic.  nodes_per_cell:
+ * 3 or 4 for cells; 2 also serves boundary edges (node -> face lists). */
 afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int nodes_per_cell,
                                  const int32_t* cell_nodes_d, int32_t* nc_ptr_d, int32_t* nc_cell_d,
                                  uint8_t* nc_local_d, int32_t* nc_inverse_d);
@@ -208,6 +209,28 @@ afem_status afem_rhs_constant_source(afem_context ctx, const afem_mesh_view* mes
  * FemModuleElasticity::_applyBodyForce (modules/elasticity/BodyForce.h:148-160). */
 afem_status afem_rhs_body_force_tet4(afem_context ctx, const afem_mesh_view* mesh, double fx, double fy, double fz,
                                      double* rhs_d);
+
+/* Boundary-face right-hand-side terms on P1 meshes (boundary edges in 2D,
+ * triangles in 3D), added into rhs:
+ *   AFEM_FACE_SCALAR  scalar Neumann flux:  rhs[dof(n, 0)] += g[0] |f| / nf
+ *   AFEM_FACE_NORMAL  vector Neumann flux:  rhs[dof(n, 0)] += (nrm . g) |f| / nf
+ *   AFEM_FACE_VECTOR  traction:             rhs[dof(n, c)] += g[c] |f| / nf, c < dim
+ * |f| = edge length or triangle area, nf = dim nodes per face, dof(n, c) =
+ * n nb_dof + c, nrm = unit outward normal: the face's node order as given
+ * when outward_d[f] != 0 (Arcane's isSubDomainBoundaryOutside), its first two
+ * nodes swapped otherwise (outward_d null: all outward).  g_h: host array of
+ * dim values ("NULL" components = 0).  Replaces applyNeumannToRhsTria3 /
+ * Tetra4 (femutils/ArcaneFemFunctionsGpu.cc:679-735,1082-1140, atomic adds)
+ * and applyTractionToRhsTria3 / Tetra4 (femutils/ArcaneFemFunctions.h:
+ * 2854-2885,2188-2220): contributions are gathered node-wise in increasing
+ * face order, so the result is deterministic and equals the sequential
+ * face-loop order. */
+#define AFEM_FACE_SCALAR 0
+#define AFEM_FACE_NORMAL 1
+#define AFEM_FACE_VECTOR 2
+afem_status afem_rhs_boundary_faces(afem_context ctx, int dim, int nb_node, int nb_face, const double* coords_d,
+                                    const int32_t* face_nodes_d, const uint8_t* outward_d, int mode,
+                                    const double* g_h, int nb_dof, double* rhs_d);
 
 /* ---------------------------------------------------------------------- */
 /* Linear system: mirrors CsrDoFLinearSystemImpl

@@ -406,6 +406,66 @@ void afo_rhs_body_force_tet4(int nb_cell, const double* coords, const int32_t* c
   }
 }
 
+/* Boundary-face terms on P1 meshes, faces in the order given, nodes in face
+ * order, += into the right-hand side (the CPU paths' sequential order):
+ *   mode 0, scalar Neumann:  rhs[dof(n, 0)] += g0 * |f| / nf
+ *     (applyNeumannToRhsTria3 / Tetra4, femutils/ArcaneFemFunctionsGpu.cc:679-735,1082-1140)
+ *   mode 1, normal Neumann:  rhs[dof(n, 0)] += (nrm . g) * |f| / nf   (same functions, vector branch)
+ *   mode 2, traction:        rhs[dof(n, c)] += g_c * |f| / nf, c < dim
+ *     (applyTractionToRhsTria3 / Tetra4, femutils/ArcaneFemFunctions.h:2854-2885,2188-2220)
+ * |f|: edge length sqrt(dx dx + dy dy) (ArcaneFemFunctionsGpu.h:139-147) or
+ * triangle area |(n1 - n0) x (n2 - n0)| / 2 (:92-102); nrm: the unit outward
+ * normal (:159-178, :190-213), the face's first two nodes swapped when the
+ * face is not oriented outward (outward[f] == 0).  Arcane's Real3::normL2 is
+ * sqrt(x x + y y + z z). */
+void afo_rhs_boundary_faces(int dim, int nb_face, const double* coords, const int32_t* face_nodes,
+                            const uint8_t* outward, int mode, const double g[3], int nb_dof, double* rhs) {
+  const int nf = dim;
+  for (int f = 0; f < nb_face; ++f) {
+    const int32_t* fn = face_nodes + (int64_t)f * nf;
+    const double* a0 = coords + 3 * (int64_t)fn[0];
+    const double* a1 = coords + 3 * (int64_t)fn[1];
+    double measure, nrm[3] = {0.0, 0.0, 0.0};
+    const int out = outward ? outward[f] : 1;
+    if (dim == 2) {
+      const double dx = a1[0] - a0[0], dy = a1[1] - a0[1];
+      measure = sqrt(dx * dx + dy * dy);
+      const double* b0 = out ? a0 : a1;
+      const double* b1 = out ? a1 : a0;
+      const double ex = b1[0] - b0[0], ey = b1[1] - b0[1];
+      const double nn = sqrt(ey * ey + ex * ex);
+      nrm[0] = ey / nn;
+      nrm[1] = (b0[0] - b1[0]) / nn;
+    } else {
+      const double* a2 = coords + 3 * (int64_t)fn[2];
+      const double u[3] = {a1[0] - a0[0], a1[1] - a0[1], a1[2] - a0[2]};
+      const double v[3] = {a2[0] - a0[0], a2[1] - a0[1], a2[2] - a0[2]};
+      const double c[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+      measure = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) / 2.0;
+      const double* b0 = out ? a0 : a1;
+      const double* b1 = out ? a1 : a0;
+      const double e1[3] = {b1[0] - b0[0], b1[1] - b0[1], b1[2] - b0[2]};
+      const double e2[3] = {a2[0] - b0[0], a2[1] - b0[1], a2[2] - b0[2]};
+      const double m[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+      const double nn = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+      nrm[0] = m[0] / nn;
+      nrm[1] = m[1] / nn;
+      nrm[2] = m[2] / nn;
+    }
+    for (int k = 0; k < nf; ++k) {
+      const int64_t d = (int64_t)fn[k] * nb_dof;
+      if (mode == 0) {
+        rhs[d] += g[0] * measure / nf;
+      } else if (mode == 1) {
+        const double flux = dim == 2 ? nrm[0] * g[0] + nrm[1] * g[1] : nrm[0] * g[0] + nrm[1] * g[1] + nrm[2] * g[2];
+        rhs[d] += flux * measure / nf;
+      } else {
+        for (int c = 0; c < dim; ++c) rhs[d + c] += g[c] * measure / nf;
+      }
+    }
+  }
+}
+
 /* applyDirichletToNodeGroupViaPenalty (femutils/ArcaneFemFunctionsGpu.cc:54-78) */
 void afo_dirichlet_penalty(int nb_sel, const int32_t* nodes, int nb_dof, int dof_index, double value,
                            double penalty, uint8_t* forced_info, double* forced_value, double* rhs) {

@@ -77,6 +77,8 @@ void afo_rhs_constant_source(int dim, int nb_node, const double* coords, const i
 /* Body force on tetrahedra, cell loop with += (modules/elasticity/BodyForce.h:148-160). */
 void afo_rhs_body_force_tet4(int nb_cell, const double* coords, const int32_t* cell_nodes, const double f[3],
                              double* rhs);
+void afo_rhs_boundary_faces(int dim, int nb_face, const double* coords, const int32_t* face_nodes,
+                            const uint8_t* outward, int mode, const double g[3], int nb_dof, double* rhs);
 
 /* Penalty flagging (femutils/ArcaneFemFunctionsGpu.cc:54-78). */
 void afo_dirichlet_penalty(int nb_sel, const int32_t* nodes, int nb_dof, int dof_index, double value,

@@ -58,6 +58,8 @@ def _declare(L):
     L.afo_rhs_constant_source.restype = None
     L.afo_rhs_body_force_tet4.argtypes = [C.c_int, _P, _P, _P, _P]
     L.afo_rhs_body_force_tet4.restype = None
+    L.afo_rhs_boundary_faces.argtypes = [C.c_int, C.c_int, _P, _P, _P, C.c_int, _P, C.c_int, _P]
+    L.afo_rhs_boundary_faces.restype = None
     L.afo_dirichlet_penalty.argtypes = [C.c_int, _P, C.c_int, C.c_int, C.c_double, C.c_double, _P, _P, _P]
     L.afo_dirichlet_penalty.restype = None
     L.afo_dirichlet_elimination.argtypes = [C.c_int, _P, C.c_int, C.c_int, C.c_double, C.c_uint8, _P, _P]
@@ -160,6 +162,20 @@ def rhs_body_force_tet4(coords, cell_nodes, f, rhs=None):
         rhs = np.zeros(coords.shape[0] * 3)
     fv = _c(f, np.float64)
     lib().afo_rhs_body_force_tet4(cell_nodes.shape[0], _p(coords), _p(cell_nodes), _p(fv), _p(rhs))
+    return rhs
+
+
+FACE_SCALAR, FACE_NORMAL, FACE_VECTOR = 0, 1, 2
+
+
+def rhs_boundary_faces(dim, coords, face_nodes, outward, mode, g, nb_dof, rhs):
+    """Neumann (scalar / normal flux) or traction terms of boundary faces, += into rhs."""
+    coords = _c(coords, np.float64)
+    face_nodes = _c(face_nodes, np.int32)
+    out = None if outward is None else _c(outward, np.uint8)
+    gv = _c(np.resize(np.asarray(g, np.float64), 3), np.float64)
+    lib().afo_rhs_boundary_faces(dim, face_nodes.shape[0], _p(coords), _p(face_nodes), _p(out), mode, _p(gv),
+                                 nb_dof, _p(rhs))
     return rhs
 
 

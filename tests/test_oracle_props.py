@@ -1,5 +1,6 @@
 """Known answers and properties of the oracle (CPU only)."""
 import numpy as np
+import pytest
 import scipy.sparse as sp
 
 from arcanefem_gb300 import meshgen
@@ -134,3 +135,35 @@ def test_dirichlet_transformations_match_reference_semantics():
     # the quirk: the diagonal of row 0 is not reset to 1
     k0 = rp[0] + list(cols[rp[0]:rp[1]]).index(0)
     assert vv[k0] == v[k0] and v[k0] != 1.0
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_boundary_face_terms_integrate_the_boundary(dim):
+    """Neumann / traction terms of the oracle: a scalar flux integrates to
+    g x |boundary|, a constant vector's normal flux to 0 (divergence theorem),
+    a traction to g x |boundary| per component; the face orientation flags
+    are honoured (a flipped face with its flag flipped gives the same sum)."""
+    from arcanefem_gb300 import meshgen
+    m = meshgen.unit_square_tri(6, seed=3) if dim == 2 else meshgen.unit_cube_tet(4, seed=3)
+    f, out = meshgen.boundary_faces(m, seed=5)
+    size = 4.0 if dim == 2 else 6.0
+    r = O.rhs_boundary_faces(dim, m.coords, f, out, O.FACE_SCALAR, [2.5], 1, np.zeros(m.nb_node))
+    assert abs(r.sum() - 2.5 * size) < 1e-12
+    g = [1.0, -2.0, 0.5][:dim]
+    r = O.rhs_boundary_faces(dim, m.coords, f, out, O.FACE_NORMAL, g, 1, np.zeros(m.nb_node))
+    assert abs(r.sum()) < 1e-12
+    # outward normal flux of the position field x integrates to dim x volume: use g = e_x on the x = 1 face only
+    r = O.rhs_boundary_faces(dim, m.coords, f, out, O.FACE_VECTOR, g, dim, np.zeros(m.nb_node * dim))
+    assert np.allclose(r.reshape(-1, dim).sum(0), np.array(g) * size, atol=1e-12)
+    # flipping a face's first two nodes together with its flag leaves the normal flux unchanged
+    f2, out2 = f.copy(), out.copy()
+    f2[:, [0, 1]] = f2[:, [1, 0]]
+    out2 = 1 - out2
+    ra = O.rhs_boundary_faces(dim, m.coords, f, out, O.FACE_NORMAL, g, 1, np.zeros(m.nb_node))
+    rb = O.rhs_boundary_faces(dim, m.coords, f2, out2, O.FACE_NORMAL, g, 1, np.zeros(m.nb_node))
+    assert np.allclose(ra, rb, atol=1e-14)
+    # the x = 1 face carries flux +|face| for g = e_x
+    on = np.all(np.isclose(m.coords[f, 0], 1.0), axis=1)
+    r = O.rhs_boundary_faces(dim, m.coords, f[on], out[on], O.FACE_NORMAL, [1.0, 0.0, 0.0][:dim], 1,
+                             np.zeros(m.nb_node))
+    assert abs(r.sum() - 1.0) < 1e-12
