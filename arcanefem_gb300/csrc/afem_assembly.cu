@@ -370,6 +370,158 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int nb_node,
 // Right-hand sides.
 
 // w_c = qdot * measure / npc (ArcaneFemFunctionsGpu.h:703: sum += qdot * domain / nbItem)
+// ---------------------------------------------------------------------------
+// Bilinear / trilinear Lagrange elements (Quad4, Hexa8), 2 x 2 (x 2) Gauss
+// points: _computeElementVectorQuad4Gpu / _computeElementVectorHexa8Gpu
+// (modules/poisson/ElementMatrixHexQuad.h:63-91,239-266) with the Jacobian of
+// _computeQuadGradientsAndJacobian / _computeHexaGradientsAndJacobian
+// (femutils/ArcaneFemFunctionsGpu.h:298-350,554-586) and the reference
+// gradients of femutils/ShapeFunctions.h:123-129,314-345.  The element
+// matrix is computed once per cell (the reference recomputes it for each of
+// the 4 / 8 incident nodes); row a goes to incidence inv[c][a], diagonal
+// first, then the other nodes in increasing local index.
+
+constexpr double kGauss = 0.57735026918962576451;   // 1 / sqrt(3)
+
+template <int N>
+__device__ __forceinline__ void write_rows_q1(const double (&K)[N][N], const int32_t* ip, double* er) {
+#pragma unroll
+  for (int a = 0; a < N; ++a) {
+    double* r = er + (int64_t)N * __ldg(ip + a);
+    r[0] = K[a][a];
+    int q = 1;
+#pragma unroll
+    for (int b = 0; b < N; ++b)
+      if (b != a) r[q++] = K[a < b ? a : b][a < b ? b : a];
+  }
+}
+
+__global__ void __launch_bounds__(128) k_elem_poisson_quad4(int nb_cell, const double* __restrict__ xyz,
+                                                            const int32_t* __restrict__ cn,
+                                                            const int32_t* __restrict__ inv,
+                                                            const double* __restrict__ coeff, double* __restrict__ er) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+    double x[4], y[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const double* p = xyz + 3 * (int64_t)__ldg(cn + 4 * c + a);
+      x[a] = __ldg(p);
+      y[a] = __ldg(p + 1);
+    }
+    double K[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) K[a][b] = 0.0;
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const double xi = (g >> 1) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
+      const double dxi[4] = {-0.25 * (1.0 - eta), 0.25 * (1.0 - eta), 0.25 * (1.0 + eta), -0.25 * (1.0 + eta)};
+      const double deta[4] = {-0.25 * (1.0 - xi), -0.25 * (1.0 + xi), 0.25 * (1.0 + xi), 0.25 * (1.0 - xi)};
+      double j00 = 0.0, j01 = 0.0, j10 = 0.0, j11 = 0.0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        j00 += dxi[a] * x[a];
+        j01 += dxi[a] * y[a];
+        j10 += deta[a] * x[a];
+        j11 += deta[a] * y[a];
+      }
+      const double det = j00 * j11 - j01 * j10;
+      const double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
+      double dx[4], dy[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        dx[a] = i00 * dxi[a] + i01 * deta[a];
+        dy[a] = i10 * dxi[a] + i11 * deta[a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = a; b < 4; ++b) K[a][b] += (dx[a] * dx[b]) * det + (dy[a] * dy[b]) * det;
+    }
+    if (coeff) {
+      const double k = __ldg(coeff + c);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = a; b < 4; ++b) K[a][b] *= k;
+    }
+    write_rows_q1<4>(K, inv + 4 * c, er);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int nb_cell, const double* __restrict__ xyz,
+                                                            const int32_t* __restrict__ cn,
+                                                            const int32_t* __restrict__ inv,
+                                                            const double* __restrict__ coeff, double* __restrict__ er) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+    double x[8], y[8], z[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const double* p = xyz + 3 * (int64_t)__ldg(cn + 8 * c + a);
+      x[a] = __ldg(p);
+      y[a] = __ldg(p + 1);
+      z[a] = __ldg(p + 2);
+    }
+    double K[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) K[a][b] = 0.0;
+#pragma unroll 1
+    for (int g = 0; g < 8; ++g) {
+      const double xi = (g >> 2) ? kGauss : -kGauss, eta = ((g >> 1) & 1) ? kGauss : -kGauss,
+                   zeta = (g & 1) ? kGauss : -kGauss;
+      const double mx = 1.0 - xi, px = 1.0 + xi, me = 1.0 - eta, pe = 1.0 + eta, mz = 1.0 - zeta, pz = 1.0 + zeta;
+      const double dxi[8] = {-0.125 * me * mz, 0.125 * me * mz, 0.125 * pe * mz, -0.125 * pe * mz,
+                             -0.125 * me * pz, 0.125 * me * pz, 0.125 * pe * pz, -0.125 * pe * pz};
+      const double deta[8] = {-0.125 * mx * mz, -0.125 * px * mz, 0.125 * px * mz, 0.125 * mx * mz,
+                              -0.125 * mx * pz, -0.125 * px * pz, 0.125 * px * pz, 0.125 * mx * pz};
+      const double dzeta[8] = {-0.125 * mx * me, -0.125 * px * me, -0.125 * px * pe, -0.125 * mx * pe,
+                               0.125 * mx * me, 0.125 * px * me, 0.125 * px * pe, 0.125 * mx * pe};
+      double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        J[0][0] += dxi[a] * x[a]; J[0][1] += dxi[a] * y[a]; J[0][2] += dxi[a] * z[a];
+        J[1][0] += deta[a] * x[a]; J[1][1] += deta[a] * y[a]; J[1][2] += deta[a] * z[a];
+        J[2][0] += dzeta[a] * x[a]; J[2][1] += dzeta[a] * y[a]; J[2][2] += dzeta[a] * z[a];
+      }
+      // determinant by the first row, inverse = adjugate / det
+      const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+      const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+      const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+      const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+      const double id = 1.0 / det;
+      const double v00 = c00 * id, v10 = c01 * id, v20 = c02 * id;
+      const double v01 = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+      const double v11 = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+      const double v21 = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+      const double v02 = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+      const double v12 = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+      const double v22 = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+      double dx[8], dy[8], dz[8];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        dx[a] = v00 * dxi[a] + v01 * deta[a] + v02 * dzeta[a];
+        dy[a] = v10 * dxi[a] + v11 * deta[a] + v12 * dzeta[a];
+        dz[a] = v20 * dxi[a] + v21 * deta[a] + v22 * dzeta[a];
+      }
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = a; b < 8; ++b) K[a][b] += (dx[a] * dx[b] + dy[a] * dy[b] + dz[a] * dz[b]) * det;
+    }
+    if (coeff) {
+      const double k = __ldg(coeff + c);
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = a; b < 8; ++b) K[a][b] *= k;
+    }
+    write_rows_q1<8>(K, inv + 8 * c, er);
+  }
+}
+
 // Boundary-face terms (Neumann flux, traction), per face g * |f| / nf, in
 // the oracle's operation order with no contraction (applyNeumannToRhsTria3 /
 // Tetra4, femutils/ArcaneFemFunctionsGpu.cc:679-735,1082-1140; traction
@@ -540,6 +692,45 @@ afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, co
                   values_d);
   return launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                 values_d);
+}
+
+afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_view* m, const double* cell_coeff_d,
+                                             double* ke) {
+  AFEM_CHECK_ARG(ctx, "afem_element_matrices_poisson_q1: null context");
+  AFEM_TRY(check_mesh(m, "afem_element_matrices_poisson_q1"));
+  AFEM_CHECK_ARG(m->nc_inverse_d && ke, "afem_element_matrices_poisson_q1: null nc_inverse / element buffer");
+  const unsigned ge = grid_for(ctx, m->nb_cell, 128, 16);
+  if (m->dim == 3)
+    return launch(ctx, k_elem_poisson_hexa8, ge, 128, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                  cell_coeff_d, ke);
+  return launch(ctx, k_elem_poisson_quad4, ge, 128, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                cell_coeff_d, ke);
+}
+
+afem_status afem_gather_poisson_q1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
+                                   const double* ke, double* values_d) {
+  AFEM_CHECK_ARG(ctx, "afem_gather_poisson_q1: null context");
+  AFEM_TRY(check_mesh(m, "afem_gather_poisson_q1"));
+  AFEM_CHECK_ARG(m->nc_slot_d && row_ptr_d && ke && values_d, "afem_gather_poisson_q1: null buffer");
+  unsigned gg = (unsigned)((m->nb_node + kGatherBlock - 1) / kGatherBlock);
+  if (m->dim == 3)
+    return launch(ctx, k_gather_scalar<8>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                  values_d);
+  return launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                values_d);
+}
+
+afem_status afem_assemble_poisson_q1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
+                                     const double* cell_coeff_d, double* values_d) {
+  AFEM_CHECK_ARG(ctx, "afem_assemble_poisson_q1: null context");
+  AFEM_TRY(check_mesh(m, "afem_assemble_poisson_q1"));
+  AFEM_CHECK_ARG(row_ptr_d && values_d, "afem_assemble_poisson_q1: null buffer");
+  const size_t npc = (size_t)1 << m->dim;
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * npc * npc * m->nb_cell)));
+  double* ke;
+  AFEM_TRY(scratch_take(ctx, npc * npc * m->nb_cell, &ke));
+  AFEM_TRY(afem_element_matrices_poisson_q1(ctx, m, cell_coeff_d, ke));
+  return afem_gather_poisson_q1(ctx, m, row_ptr_d, ke, values_d);
 }
 
 afem_status afem_assemble_poisson_p1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,

@@ -46,13 +46,13 @@ __global__ void k_nc_scatter(const int32_t* __restrict__ cn, int64_t total, int 
     int32_t pos = nc_ptr[n] + atomicAdd(&cursor[n], 1);
     int32_t cell = (int32_t)(i / npc);
     int32_t local = (int32_t)(i - (int64_t)cell * npc);
-    key[pos] = cell * 4 + local;  // cells < 2^29 checked by the caller
+    key[pos] = (cell << 3) | local;  // cells < 2^28 checked by the caller; local < 8
   }
 }
 
 constexpr int kWarpsPerBlock = 8;
 
-// Per-node sort of the (cell * 4 + local) keys, then split; the inverse map
+// Per-node sort of the (cell << 3 | local) keys, then split; the inverse map
 // records, for each (cell, local), its incidence index.  One warp per node:
 // up to 32 keys are sorted by a bitonic network on registers (shuffles);
 // longer lists (rare) by an insertion sort in lane 0.
@@ -94,9 +94,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_nc_sort(int nb_node, in
     __syncwarp();
     for (int32_t i = b + lane; i < e; i += 32) {
       int32_t v = key[i];
-      nc_cell[i] = v >> 2;
-      nc_local[i] = (uint8_t)(v & 3);
-      if (nc_inverse) nc_inverse[(int64_t)(v >> 2) * npc + (v & 3)] = i;
+      nc_cell[i] = v >> 3;
+      nc_local[i] = (uint8_t)(v & 7);
+      if (nc_inverse) nc_inverse[(int64_t)(v >> 3) * npc + (v & 7)] = i;
     }
   }
 }
@@ -238,8 +238,9 @@ afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int
   AFEM_CHECK_ARG(ctx, "afem_node_cell_build: null context");
   AFEM_CHECK_ARG(nb_node > 0 && nb_cell > 0, "afem_node_cell_build: empty mesh (nb_node=%d nb_cell=%d)", nb_node,
                  nb_cell);
-  AFEM_CHECK_ARG(npc >= 2 && npc <= 4, "afem_node_cell_build: nodes_per_cell must be 2, 3 or 4 (got %d)", npc);
-  AFEM_CHECK_ARG(nb_cell < (1 << 29), "afem_node_cell_build: too many cells (%d)", nb_cell);
+  AFEM_CHECK_ARG(npc >= 2 && npc <= 8 && npc != 5 && npc != 6 && npc != 7,
+                 "afem_node_cell_build: nodes_per_cell must be 2, 3, 4 or 8 (got %d)", npc);
+  AFEM_CHECK_ARG(nb_cell < (1 << 28), "afem_node_cell_build: too many cells (%d)", nb_cell);
   AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && nc_local_d, "afem_node_cell_build: null buffer");
   int64_t total = (int64_t)nb_cell * npc;
   AFEM_CHECK_ARG(total < INT_MAX, "afem_node_cell_build: too many incidences");
@@ -270,7 +271,7 @@ afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int
 afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int32_t* cell_nodes_d,
                                const int32_t* nc_ptr_d, const int32_t* nc_cell_d, int32_t* row_ptr_d, int64_t* nnz_h) {
   AFEM_CHECK_ARG(ctx, "afem_sparsity_rows: null context");
-  AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4), "afem_sparsity_rows: bad sizes");
+  AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4 || npc == 8), "afem_sparsity_rows: bad sizes");
   AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && row_ptr_d, "afem_sparsity_rows: null buffer");
   size_t need = align256(sizeof(int32_t) * ((size_t)nb_node + 1)) + 256 + scan_scratch_bytes(nb_node);
   AFEM_TRY(scratch_reserve(ctx, need));
@@ -302,7 +303,7 @@ afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int
                                const int32_t* nc_ptr_d, const int32_t* nc_cell_d, const uint8_t* nc_local_d,
                                const int32_t* row_ptr_d, int col_order, int32_t* cols_d, uint8_t* nc_slot_d) {
   AFEM_CHECK_ARG(ctx, "afem_sparsity_cols: null context");
-  AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4), "afem_sparsity_cols: bad sizes");
+  AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4 || npc == 8), "afem_sparsity_cols: bad sizes");
   AFEM_CHECK_ARG(col_order == AFEM_COLS_ASCENDING || col_order == AFEM_COLS_SELF_LAST,
                  "afem_sparsity_cols: bad col_order %d", col_order);
   AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && nc_local_d && row_ptr_d && cols_d && nc_slot_d,

@@ -169,10 +169,14 @@ class BSRFormat:
                         0 if self.nc_slot is None else self.nc_slot.data_ptr(), self.nc_inverse.data_ptr())
 
     # assembleBilinearAtomicFree with the Poisson element vectors
+    def is_q1(self) -> bool:
+        """Quad4 / Hexa8 cells (2^dim nodes) rather than P1 simplices."""
+        return self.mesh.npc == 1 << self.mesh.dim
+
     def assemble_poisson(self, cell_coeff: torch.Tensor | None = None):
         mv = self.mesh_view()
-        call("afem_assemble_poisson_p1", self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), _ptr(cell_coeff),
-             _ptr(self.values))
+        fn = "afem_assemble_poisson_q1" if self.is_q1() else "afem_assemble_poisson_p1"
+        call(fn, self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), _ptr(cell_coeff), _ptr(self.values))
 
     # assembleBilinearAtomicFree with the elasticity element vectors (Lame lambda, mu)
     def assemble_elasticity(self, lam: float, mu: float):
@@ -192,7 +196,8 @@ class BSRFormat:
         if self.nb_dof == 3:
             call("afem_element_matrices_elasticity_tet4", self.ctx.handle, C.byref(mv), float(lam), float(mu), _ptr(ke))
         else:
-            call("afem_element_matrices_poisson_p1", self.ctx.handle, C.byref(mv), _ptr(cell_coeff), _ptr(ke))
+            fn = "afem_element_matrices_poisson_q1" if self.is_q1() else "afem_element_matrices_poisson_p1"
+            call(fn, self.ctx.handle, C.byref(mv), _ptr(cell_coeff), _ptr(ke))
 
     def gather(self, ke: torch.Tensor):
         mv = self.mesh_view()
@@ -201,8 +206,8 @@ class BSRFormat:
             call("afem_gather_elasticity_tet4", self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), _ptr(ke), layout,
                  _ptr(self.values))
         else:
-            call("afem_gather_poisson_p1", self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), _ptr(ke),
-                 _ptr(self.values))
+            fn = "afem_gather_poisson_q1" if self.is_q1() else "afem_gather_poisson_p1"
+            call(fn, self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), _ptr(ke), _ptr(self.values))
 
     def reset_matrix_values(self):
         self.values.zero_()

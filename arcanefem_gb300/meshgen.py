@@ -193,3 +193,26 @@ def boundary_faces(mesh: Mesh, seed: int = 0):
         away = X[o] - X[f[:, 0]]
     outward = (np.einsum("ij,ij->i", nrm, away) < 0).astype(np.uint8)
     return f, outward
+
+
+def unit_square_quad(n: int, jitter: float = 0.2, seed: int = 0) -> Mesh:
+    """n x n bilinear quadrilaterals of the unit square, counter-clockwise
+    (the Quad4 reference order), node id = i + j (n+1), interior nodes jittered."""
+    tri = unit_square_tri(n, jitter=jitter, seed=seed)
+    m = n + 1
+    ids = np.arange(m * m).reshape(m, m)
+    q = np.stack([ids[:-1, :-1], ids[:-1, 1:], ids[1:, 1:], ids[1:, :-1]], axis=-1).reshape(-1, 4)
+    return Mesh(2, tri.coords, q.astype(np.int32), dict(tri.groups))
+
+
+def unit_cube_hex(n: int, jitter: float = 0.15, seed: int = 0) -> Mesh:
+    """n^3 trilinear hexahedra of the unit cube in the Hexa8 reference order
+    (bottom face counter-clockwise, then the top face), node id =
+    i + j (n+1) + k (n+1)^2, interior nodes jittered."""
+    tet = unit_cube_tet(n, jitter=jitter, seed=seed)
+    m = n + 1
+    ids = np.arange(m ** 3).reshape(m, m, m)   # [k][j][i]
+    b = [ids[:-1, :-1, :-1], ids[:-1, :-1, 1:], ids[:-1, 1:, 1:], ids[:-1, 1:, :-1]]
+    t = [ids[1:, :-1, :-1], ids[1:, :-1, 1:], ids[1:, 1:, 1:], ids[1:, 1:, :-1]]
+    h = np.stack(b + t, axis=-1).reshape(-1, 8)
+    return Mesh(3, tet.coords, h.astype(np.int32), dict(tet.groups))

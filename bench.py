@@ -59,6 +59,10 @@ WORKLOADS = {
                          E=21e5, nu=0.28, body=(0.0, 0.0, -1.0)),
     "poisson2d": dict(dim=2, n=256, jitter=0.2, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 2D Poisson P1)",
                       dp_elem=26, dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
+    # Q1 widening: trilinear hexahedra (2x2x2 Gauss points); assembly only (no Q1 source term yet)
+    "poisson3d_hex": dict(dim=3, cell="hex", n=96, jitter=0.15, nb_dof=1,
+                          metric="assembled nnz/s (node-wise CSR, 3D Poisson Q1 Hexa8)",
+                          dp_elem=3000, dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
 }
 
 
@@ -107,6 +111,8 @@ def replica_value(total_ms: float, world: int, units_per_rank: int, steps: int, 
 def make_mesh(args):
     from arcanefem_gb300 import meshgen
     w = WORKLOADS[args.workload]
+    if w.get("cell") == "hex":
+        return meshgen.unit_cube_hex(args.n, jitter=w["jitter"], seed=args.seed)
     if w["dim"] == 3:
         return meshgen.unit_cube_tet(args.n, jitter=w["jitter"], seed=args.seed)
     return meshgen.unit_square_tri(args.n, jitter=w["jitter"], seed=args.seed)
@@ -114,7 +120,10 @@ def make_mesh(args):
 
 def config(args, world):
     w = WORKLOADS[args.workload]
-    if w["dim"] == 3:
+    if w.get("cell") == "hex":
+        desc = f"unit cube {args.n}^3 trilinear hexahedra, jitter {w['jitter']}h"
+        elements, nodes = args.n ** 3, (args.n + 1) ** 3
+    elif w["dim"] == 3:
         desc = f"unit cube {args.n}^3 hexahedra x 6 Kuhn tetrahedra, jitter {w['jitter']}h"
         elements, nodes = 6 * args.n ** 3, (args.n + 1) ** 3
     else:
@@ -276,13 +285,14 @@ def run_gpu(args):
     dp_cell = w["dp_elem"] + w["dp_gather"]
     dp_achieved = dp_cell * mesh.nb_cell / (ms_per_step * 1e-3) / 1e9
     kernel = ("k_elem_elasticity_tet + k_gather_elasticity" if w["nb_dof"] == 3 else
+              f"k_elem_poisson_hexa8 + k_gather_scalar<8>" if w.get("cell") == "hex" else
               f"k_elem_poisson_{'tet' if mesh.dim == 3 else 'tri'} + k_gather_scalar<{mesh.npc}>")
 
     e2e = None if args.no_e2e else run_e2e(args, mesh, fmt, lam, mu)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, mesh, fmt, lam, mu)
-    solve = None if args.no_solve else run_solve(args, ctx, mesh, fmt)
+    solve = None if (args.no_solve or w.get("cell") == "hex") else run_solve(args, ctx, mesh, fmt)
     learned = None if (args.no_learned or rank != 0) else run_learned(args)
     batched = None if (args.no_batched or rank != 0) else run_batched(args)
 
@@ -360,6 +370,8 @@ def oracle_kind(args):
     w = WORKLOADS[args.workload]
     if w["nb_dof"] == 3:
         return O.ELASTICITY_TET4
+    if w.get("cell") == "hex":
+        return O.POISSON_HEXA8
     return O.POISSON_TET4 if w["dim"] == 3 else O.POISSON_TRI3
 
 

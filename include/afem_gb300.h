@@ -148,6 +148,24 @@ typedef struct {
 afem_status afem_assemble_poisson_p1(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
                                      const double* cell_coeff_d, double* values_d);
 
+/* Bilinear / trilinear Lagrange Poisson stiffness (Quad4 for dim 2, Hexa8 for
+ * dim 3: the view's cell arrays hold 2^dim nodes per cell in the reference
+ * element's order -- quads counter-clockwise, hexahedra the bottom face
+ * counter-clockwise then the top face), 2 x 2 (x 2) Gauss points:
+ * _computeElementVectorQuad4Gpu / _computeElementVectorHexa8Gpu
+ * (modules/poisson/ElementMatrixHexQuad.h:63-91,239-266).  The node -> cell
+ * incidence, slot map and CSR structure come from afem_node_cell_build /
+ * afem_sparsity_* with nodes_per_cell = 2^dim.  Element matrices are computed
+ * once per cell into ke[npc * npc * nb_cell] (afem_element_matrices_poisson_q1),
+ * then gathered node-wise (afem_gather_poisson_q1); afem_assemble_poisson_q1
+ * does both with library scratch. */
+afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_view* mesh, const double* cell_coeff_d,
+                                             double* ke_d);
+afem_status afem_gather_poisson_q1(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
+                                   const double* ke_d, double* values_d);
+afem_status afem_assemble_poisson_q1(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
+                                     const double* cell_coeff_d, double* values_d);
+
 /* Linear elasticity P1 tetrahedra, 3x3 blocks (b = 3):
  * values_d[nnzb * 9] in the given layout.  Replaces assembleBilinearAtomicFree
  * with computeElementVectorTetra4Gpu (modules/elasticity/ElementMatrix.h:216-301,

@@ -307,11 +307,107 @@ void afo_elem_vec_elasticity_tet4(const double* coords, const int32_t* cn, doubl
   }
 }
 
+/* _computeElementVectorQuad4Gpu (modules/poisson/ElementMatrixHexQuad.h:63-91)
+ * with computeGradientsAndJacobianQuad4Gpu (femutils/ArcaneFemFunctionsGpu.h:
+ * 298-360) and computeReferenceGradientsQuad4 (femutils/ShapeFunctions.h:123-129). */
+static const double kGp = 0.57735026918962576451;
+void afo_elem_vec_poisson_quad4(const double* coords, const int32_t* cn, int i, double out[4]) {
+  const double gp[2] = {-kGp, kGp};
+  for (int k = 0; k < 4; ++k) out[k] = 0.0;
+  for (int ixi = 0; ixi < 2; ++ixi)
+    for (int ieta = 0; ieta < 2; ++ieta) {
+      const double xi = gp[ixi], eta = gp[ieta];
+      const double dxi[4] = {-0.25 * (1.0 - eta), 0.25 * (1.0 - eta), 0.25 * (1.0 + eta), -0.25 * (1.0 + eta)};
+      const double deta[4] = {-0.25 * (1.0 - xi), -0.25 * (1.0 + xi), 0.25 * (1.0 + xi), 0.25 * (1.0 - xi)};
+      double J00 = 0.0, J01 = 0.0, J10 = 0.0, J11 = 0.0;
+      for (int a = 0; a < 4; ++a) {
+        const double* c = coords + 3 * (int64_t)cn[a];
+        J00 += dxi[a] * c[0];
+        J01 += dxi[a] * c[1];
+        J10 += deta[a] * c[0];
+        J11 += deta[a] * c[1];
+      }
+      const double detJ = J00 * J11 - J01 * J10;
+      const double invJ00 = J11 / detJ, invJ01 = -J01 / detJ, invJ10 = -J10 / detJ, invJ11 = J00 / detJ;
+      double dx[4], dy[4];
+      for (int a = 0; a < 4; ++a) {
+        dx[a] = invJ00 * dxi[a] + invJ01 * deta[a];
+        dy[a] = invJ10 * dxi[a] + invJ11 * deta[a];
+      }
+      const double w = detJ * 1.0 * 1.0;
+      for (int k = 0; k < 4; ++k) out[k] += (dx[i] * dx[k]) * w + (dy[i] * dy[k]) * w;
+    }
+}
+
+/* _computeElementVectorHexa8Gpu (modules/poisson/ElementMatrixHexQuad.h:239-266)
+ * with _computeHexaGradientsAndJacobian (femutils/ArcaneFemFunctionsGpu.h:
+ * 554-586) and computeReferenceGradientsHexa8 (femutils/ShapeFunctions.h:
+ * 314-345).  Arcane's math::matrixDeterminant / inverseMatrix (not in the
+ * reference tree) are restated as the expansion along the first row and the
+ * adjugate divided by the determinant. */
+void afo_elem_vec_poisson_hexa8(const double* coords, const int32_t* cn, int i, double out[8]) {
+  const double gp[2] = {-kGp, kGp};
+  for (int k = 0; k < 8; ++k) out[k] = 0.0;
+  for (int ixi = 0; ixi < 2; ++ixi)
+    for (int ieta = 0; ieta < 2; ++ieta)
+      for (int izeta = 0; izeta < 2; ++izeta) {
+        const double xi = gp[ixi], eta = gp[ieta], zeta = gp[izeta];
+        const double dxi[8] = {-0.125 * (1.0 - eta) * (1.0 - zeta), 0.125 * (1.0 - eta) * (1.0 - zeta),
+                               0.125 * (1.0 + eta) * (1.0 - zeta),  -0.125 * (1.0 + eta) * (1.0 - zeta),
+                               -0.125 * (1.0 - eta) * (1.0 + zeta), 0.125 * (1.0 - eta) * (1.0 + zeta),
+                               0.125 * (1.0 + eta) * (1.0 + zeta),  -0.125 * (1.0 + eta) * (1.0 + zeta)};
+        const double deta[8] = {-0.125 * (1.0 - xi) * (1.0 - zeta), -0.125 * (1.0 + xi) * (1.0 - zeta),
+                                0.125 * (1.0 + xi) * (1.0 - zeta),  0.125 * (1.0 - xi) * (1.0 - zeta),
+                                -0.125 * (1.0 - xi) * (1.0 + zeta), -0.125 * (1.0 + xi) * (1.0 + zeta),
+                                0.125 * (1.0 + xi) * (1.0 + zeta),  0.125 * (1.0 - xi) * (1.0 + zeta)};
+        const double dzeta[8] = {-0.125 * (1.0 - xi) * (1.0 - eta), -0.125 * (1.0 + xi) * (1.0 - eta),
+                                 -0.125 * (1.0 + xi) * (1.0 + eta), -0.125 * (1.0 - xi) * (1.0 + eta),
+                                 0.125 * (1.0 - xi) * (1.0 - eta),  0.125 * (1.0 + xi) * (1.0 - eta),
+                                 0.125 * (1.0 + xi) * (1.0 + eta),  0.125 * (1.0 - xi) * (1.0 + eta)};
+        double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+        for (int a = 0; a < 8; ++a) {
+          const double* c = coords + 3 * (int64_t)cn[a];
+          for (int d = 0; d < 3; ++d) {
+            J[0][d] += dxi[a] * c[d];
+            J[1][d] += deta[a] * c[d];
+            J[2][d] += dzeta[a] * c[d];
+          }
+        }
+        const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        double inv[3][3];
+        inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        double dx[8], dy[8], dz[8];
+        for (int a = 0; a < 8; ++a) {
+          dx[a] = inv[0][0] * dxi[a] + inv[0][1] * deta[a] + inv[0][2] * dzeta[a];
+          dy[a] = inv[1][0] * dxi[a] + inv[1][1] * deta[a] + inv[1][2] * dzeta[a];
+          dz[a] = inv[2][0] * dxi[a] + inv[2][1] * deta[a] + inv[2][2] * dzeta[a];
+        }
+        for (int k = 0; k < 8; ++k) {
+          const double grad_dot = dx[i] * dx[k] + dy[i] * dy[k] + dz[i] * dz[k];
+          out[k] += grad_dot * det;
+        }
+      }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Node-wise assembly                                                        */
 /* ------------------------------------------------------------------------ */
 
-static int kind_npc(int kind) { return (kind == AFO_POISSON_TRI3 || kind == AFO_TESTLAB_TRI3) ? 3 : 4; }
+static int kind_npc(int kind) {
+  if (kind == AFO_POISSON_QUAD4) return 4;
+  if (kind == AFO_POISSON_HEXA8) return 8;
+  return (kind == AFO_POISSON_TRI3 || kind == AFO_TESTLAB_TRI3) ? 3 : 4;
+}
 static int kind_block(int kind) { return kind == AFO_ELASTICITY_TET4 ? 3 : 1; }
 
 /* assembleBilinearOrderedPerBlockAtomicFree (femutils/BSRFormat.h:406-470) and
@@ -343,6 +439,8 @@ int afo_assemble_nodewise(int kind, int nb_node, int nb_cell, const double* coor
         case AFO_POISSON_TET4: afo_elem_vec_poisson_tet4(coords, cn, li, ev); break;
         case AFO_TESTLAB_TRI3: afo_elem_vec_testlab_tri3(coords, cn, li, ev); break;
         case AFO_TESTLAB_TET4: afo_elem_vec_testlab_tet4(coords, cn, li, ev); break;
+        case AFO_POISSON_QUAD4: afo_elem_vec_poisson_quad4(coords, cn, li, ev); break;
+        case AFO_POISSON_HEXA8: afo_elem_vec_poisson_hexa8(coords, cn, li, ev); break;
         default: afo_elem_vec_elasticity_tet4(coords, cn, lambda, mu, li, ev); break;
       }
       double coeff = cell_coeff ? cell_coeff[cell] : 1.0;

@@ -32,7 +32,9 @@ enum {
   AFO_POISSON_TET4 = 1,       /* modules/poisson/ElementMatrix.h:107-118 */
   AFO_ELASTICITY_TET4 = 2,    /* modules/elasticity/ElementMatrix.h:216-301 */
   AFO_TESTLAB_TRI3 = 3,       /* modules/testlab/FemModule.h:471-495 + NodeWiseCsrBiliAssembly.cc:194-211 */
-  AFO_TESTLAB_TET4 = 4        /* modules/testlab/FemModule.h:499-538 + NodeWiseCsrBiliAssembly.cc:269-290 */
+  AFO_TESTLAB_TET4 = 4,       /* modules/testlab/FemModule.h:499-538 + NodeWiseCsrBiliAssembly.cc:269-290 */
+  AFO_POISSON_QUAD4 = 5,      /* modules/poisson/ElementMatrixHexQuad.h:63-91 */
+  AFO_POISSON_HEXA8 = 6       /* modules/poisson/ElementMatrixHexQuad.h:239-266 */
 };
 
 /* node -> cell adjacency, cells ascending per node, plus the local index of

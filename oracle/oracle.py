@@ -18,6 +18,7 @@ _LIB_PATH = os.path.join(_HERE, "liboracle_afem.so")
 _lib = None
 
 POISSON_TRI3, POISSON_TET4, ELASTICITY_TET4, TESTLAB_TRI3, TESTLAB_TET4 = 0, 1, 2, 3, 4
+POISSON_QUAD4, POISSON_HEXA8 = 5, 6
 ELIM_NONE, ELIM_ROW, ELIM_ROW_COLUMN = 0, 1, 2
 
 
