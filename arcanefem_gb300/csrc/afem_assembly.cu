@@ -522,6 +522,87 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int nb_cell, const d
   }
 }
 
+// Constant source on Quad4 / Hexa8 cells, 2 x 2 (x 2) Gauss points: each
+// (cell, local node) term sum_gp N_i qdot w detJ goes to its incidence slot
+// (applyConstantSourceToRhsQuad4 / Hexa8, femutils/ArcaneFemFunctionsGpu.cc:
+// 393-458,875-960, which adds per Gauss point with atomics).
+template <int N>
+__global__ void __launch_bounds__(128) k_cell_source_q1(int nb_cell, const double* __restrict__ xyz,
+                                                        const int32_t* __restrict__ cn,
+                                                        const int32_t* __restrict__ inv, double qdot,
+                                                        double* __restrict__ term) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+    double x[N], y[N], z[N], acc[N];
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+      const double* p = xyz + 3 * (int64_t)__ldg(cn + N * c + a);
+      x[a] = __ldg(p);
+      y[a] = __ldg(p + 1);
+      z[a] = __ldg(p + 2);
+      acc[a] = 0.0;
+    }
+#pragma unroll 1
+    for (int g = 0; g < (N == 4 ? 4 : 8); ++g) {
+      double det, Nf[N];
+      if constexpr (N == 4) {
+        const double xi = (g >> 1) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
+        Nf[0] = 0.25 * (1.0 - xi) * (1.0 - eta);
+        Nf[1] = 0.25 * (1.0 + xi) * (1.0 - eta);
+        Nf[2] = 0.25 * (1.0 + xi) * (1.0 + eta);
+        Nf[3] = 0.25 * (1.0 - xi) * (1.0 + eta);
+        const double dxi[4] = {-0.25 * (1.0 - eta), 0.25 * (1.0 - eta), 0.25 * (1.0 + eta), -0.25 * (1.0 + eta)};
+        const double deta[4] = {-0.25 * (1.0 - xi), -0.25 * (1.0 + xi), 0.25 * (1.0 + xi), 0.25 * (1.0 - xi)};
+        double j00 = 0.0, j01 = 0.0, j10 = 0.0, j11 = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          j00 += dxi[a] * x[a];
+          j01 += dxi[a] * y[a];
+          j10 += deta[a] * x[a];
+          j11 += deta[a] * y[a];
+        }
+        det = j00 * j11 - j01 * j10;
+      } else {
+        const double xi = (g >> 2) ? kGauss : -kGauss, eta = ((g >> 1) & 1) ? kGauss : -kGauss,
+                     zeta = (g & 1) ? kGauss : -kGauss;
+        const double mx = 1.0 - xi, px = 1.0 + xi, me = 1.0 - eta, pe = 1.0 + eta, mz = 1.0 - zeta, pz = 1.0 + zeta;
+        Nf[0] = 0.125 * mx * me * mz; Nf[1] = 0.125 * px * me * mz; Nf[2] = 0.125 * px * pe * mz;
+        Nf[3] = 0.125 * mx * pe * mz; Nf[4] = 0.125 * mx * me * pz; Nf[5] = 0.125 * px * me * pz;
+        Nf[6] = 0.125 * px * pe * pz; Nf[7] = 0.125 * mx * pe * pz;
+        const double dxi[8] = {-0.125 * me * mz, 0.125 * me * mz, 0.125 * pe * mz, -0.125 * pe * mz,
+                               -0.125 * me * pz, 0.125 * me * pz, 0.125 * pe * pz, -0.125 * pe * pz};
+        const double deta[8] = {-0.125 * mx * mz, -0.125 * px * mz, 0.125 * px * mz, 0.125 * mx * mz,
+                                -0.125 * mx * pz, -0.125 * px * pz, 0.125 * px * pz, 0.125 * mx * pz};
+        const double dzeta[8] = {-0.125 * mx * me, -0.125 * px * me, -0.125 * px * pe, -0.125 * mx * pe,
+                                 0.125 * mx * me, 0.125 * px * me, 0.125 * px * pe, 0.125 * mx * pe};
+        double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          J[0][0] += dxi[a] * x[a]; J[0][1] += dxi[a] * y[a]; J[0][2] += dxi[a] * z[a];
+          J[1][0] += deta[a] * x[a]; J[1][1] += deta[a] * y[a]; J[1][2] += deta[a] * z[a];
+          J[2][0] += dzeta[a] * x[a]; J[2][1] += dzeta[a] * y[a]; J[2][2] += dzeta[a] * z[a];
+        }
+        det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+              J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      }
+#pragma unroll
+      for (int a = 0; a < N; ++a) acc[a] += Nf[a] * qdot * det;
+    }
+    const int32_t* ip = inv + N * c;
+#pragma unroll
+    for (int a = 0; a < N; ++a) term[__ldg(ip + a)] = acc[a];
+  }
+}
+
+// rhs[n * nb_dof] = sum of the node's incidence terms (increasing cell order)
+__global__ void k_incidence_sum(int nb_node, const int32_t* __restrict__ nc_ptr, const double* __restrict__ term,
+                                int nb_dof, double* __restrict__ rhs) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb_node; n += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int32_t p = nc_ptr[n]; p < nc_ptr[n + 1]; ++p) s += term[p];
+    rhs[(int64_t)n * nb_dof] = s;
+  }
+}
+
 // Boundary-face terms (Neumann flux, traction), per face g * |f| / nf, in
 // the oracle's operation order with no contraction (applyNeumannToRhsTria3 /
 // Tetra4, femutils/ArcaneFemFunctionsGpu.cc:679-735,1082-1140; traction
@@ -794,6 +875,25 @@ afem_status afem_rhs_constant_source(afem_context ctx, const afem_mesh_view* m, 
                   m->coords_d, m->cell_nodes_d, qdot, w));
   return launch(ctx, k_node_sum, grid_for(ctx, m->nb_node, 256), 256, 0, m->nb_node, m->nc_ptr_d, m->nc_cell_d,
                 (const double*)w, nb_dof, 0, 0.0, 0, rhs_d);
+}
+
+afem_status afem_rhs_constant_source_q1(afem_context ctx, const afem_mesh_view* m, double qdot, int nb_dof,
+                                        double* rhs_d) {
+  AFEM_CHECK_ARG(ctx, "afem_rhs_constant_source_q1: null context");
+  AFEM_TRY(check_mesh(m, "afem_rhs_constant_source_q1"));
+  AFEM_CHECK_ARG(m->nc_inverse_d && nb_dof >= 1 && rhs_d, "afem_rhs_constant_source_q1: bad arguments");
+  const size_t npc = (size_t)1 << m->dim;
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * npc * (size_t)m->nb_cell)));
+  double* term;
+  AFEM_TRY(scratch_take(ctx, npc * (size_t)m->nb_cell, &term));
+  if (m->dim == 3)
+    AFEM_TRY(launch(ctx, k_cell_source_q1<8>, grid_for(ctx, m->nb_cell, 128, 16), 128, 0, m->nb_cell, m->coords_d,
+                    m->cell_nodes_d, m->nc_inverse_d, qdot, term));
+  else
+    AFEM_TRY(launch(ctx, k_cell_source_q1<4>, grid_for(ctx, m->nb_cell, 128, 16), 128, 0, m->nb_cell, m->coords_d,
+                    m->cell_nodes_d, m->nc_inverse_d, qdot, term));
+  return launch(ctx, k_incidence_sum, grid_for(ctx, m->nb_node, 256), 256, 0, m->nb_node, m->nc_ptr_d,
+                (const double*)term, nb_dof, rhs_d);
 }
 
 afem_status afem_rhs_body_force_tet4(afem_context ctx, const afem_mesh_view* m, double fx, double fy, double fz,

@@ -234,7 +234,8 @@ class BSRFormat:
 
     def rhs_constant_source(self, qdot: float, rhs: torch.Tensor):
         mv = self.mesh_view()
-        call("afem_rhs_constant_source", self.ctx.handle, C.byref(mv), float(qdot), self.nb_dof, _ptr(rhs))
+        fn = "afem_rhs_constant_source_q1" if self.is_q1() else "afem_rhs_constant_source"
+        call(fn, self.ctx.handle, C.byref(mv), float(qdot), self.nb_dof, _ptr(rhs))
 
     def rhs_body_force(self, f, rhs: torch.Tensor):
         mv = self.mesh_view()

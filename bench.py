@@ -59,7 +59,7 @@ WORKLOADS = {
                          E=21e5, nu=0.28, body=(0.0, 0.0, -1.0)),
     "poisson2d": dict(dim=2, n=256, jitter=0.2, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 2D Poisson P1)",
                       dp_elem=26, dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
-    # Q1 widening: trilinear hexahedra (2x2x2 Gauss points); assembly only (no Q1 source term yet)
+    # Q1 widening: trilinear hexahedra (2x2x2 Gauss points), Q1 source, FP64 / mixed CG
     "poisson3d_hex": dict(dim=3, cell="hex", n=96, jitter=0.15, nb_dof=1,
                           metric="assembled nnz/s (node-wise CSR, 3D Poisson Q1 Hexa8)",
                           dp_elem=3000, dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
@@ -292,7 +292,7 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, mesh, fmt, lam, mu)
-    solve = None if (args.no_solve or w.get("cell") == "hex") else run_solve(args, ctx, mesh, fmt)
+    solve = None if args.no_solve else run_solve(args, ctx, mesh, fmt)
     learned = None if (args.no_learned or rank != 0) else run_learned(args)
     batched = None if (args.no_batched or rank != 0) else run_batched(args)
 

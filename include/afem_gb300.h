@@ -225,6 +225,14 @@ afem_status afem_rhs_constant_source(afem_context ctx, const afem_mesh_view* mes
 /* Body force on tetrahedra, rhs_d[3*node + k] += sum_cells f[k] * vol / 4,
  * node-wise (no atomics).  Replaces the host loop of
  * FemModuleElasticity::_applyBodyForce (modules/elasticity/BodyForce.h:148-160). */
+/* Constant source on Quad4 / Hexa8 cells (2^dim nodes, as
+ * afem_assemble_poisson_q1): rhs[n nb_dof] = sum over the incident cells of
+ * sum_gp N_n qdot w detJ, 2 x 2 (x 2) Gauss points
+ * (applyConstantSourceToRhsQuad4 / Hexa8, femutils/ArcaneFemFunctionsGpu.cc:
+ * 393-458,875-960, which adds with atomics; here per (cell, node) then per
+ * node in increasing cell order). */
+afem_status afem_rhs_constant_source_q1(afem_context ctx, const afem_mesh_view* mesh, double qdot, int nb_dof,
+                                        double* rhs_d);
 afem_status afem_rhs_body_force_tet4(afem_context ctx, const afem_mesh_view* mesh, double fx, double fy, double fz,
                                      double* rhs_d);
 

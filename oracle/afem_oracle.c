@@ -489,6 +489,72 @@ void afo_rhs_constant_source(int dim, int nb_node, const double* coords, const i
   }
 }
 
+/* applyConstantSourceToRhsQuad4 / Hexa8 (femutils/ArcaneFemFunctionsGpu.cc:
+ * 393-458,875-960): N_i qdot (w detJ) per Gauss point, summed per node over
+ * its cells in increasing order (the reference's atomics have no fixed order). */
+void afo_rhs_constant_source_q1(int dim, int nb_node, const double* coords, const int32_t* cell_nodes,
+                                const int32_t* nc_ptr, const int32_t* nc_cell, double qdot, int nb_dof,
+                                double* rhs) {
+  const int npc = 1 << dim;
+  const double gp[2] = {-kGp, kGp};
+  for (int n = 0; n < nb_node; ++n) {
+    double sum = 0.0;
+    for (int32_t p = nc_ptr[n]; p < nc_ptr[n + 1]; ++p) {
+      const int32_t* cn = cell_nodes + (int64_t)nc_cell[p] * npc;
+      int li = 0;
+      while (cn[li] != n) ++li;
+      for (int ixi = 0; ixi < 2; ++ixi)
+        for (int ieta = 0; ieta < 2; ++ieta)
+          for (int izeta = 0; izeta < (dim == 3 ? 2 : 1); ++izeta) {
+            const double xi = gp[ixi], eta = gp[ieta], zeta = gp[izeta];
+            double Ni, detJ;
+            if (dim == 2) {
+              const double Nq[4] = {0.25 * (1.0 - xi) * (1.0 - eta), 0.25 * (1.0 + xi) * (1.0 - eta),
+                                    0.25 * (1.0 + xi) * (1.0 + eta), 0.25 * (1.0 - xi) * (1.0 + eta)};
+              const double dxi[4] = {-0.25 * (1.0 - eta), 0.25 * (1.0 - eta), 0.25 * (1.0 + eta), -0.25 * (1.0 + eta)};
+              const double deta[4] = {-0.25 * (1.0 - xi), -0.25 * (1.0 + xi), 0.25 * (1.0 + xi), 0.25 * (1.0 - xi)};
+              double J00 = 0.0, J01 = 0.0, J10 = 0.0, J11 = 0.0;
+              for (int a = 0; a < 4; ++a) {
+                const double* c = coords + 3 * (int64_t)cn[a];
+                J00 += dxi[a] * c[0];
+                J01 += dxi[a] * c[1];
+                J10 += deta[a] * c[0];
+                J11 += deta[a] * c[1];
+              }
+              detJ = J00 * J11 - J01 * J10;
+              Ni = Nq[li];
+            } else {
+              const double mx = 1.0 - xi, px = 1.0 + xi, me = 1.0 - eta, pe = 1.0 + eta, mz = 1.0 - zeta,
+                           pz = 1.0 + zeta;
+              const double Nh[8] = {0.125 * mx * me * mz, 0.125 * px * me * mz, 0.125 * px * pe * mz,
+                                    0.125 * mx * pe * mz, 0.125 * mx * me * pz, 0.125 * px * me * pz,
+                                    0.125 * px * pe * pz, 0.125 * mx * pe * pz};
+              const double dxi[8] = {-0.125 * me * mz, 0.125 * me * mz, 0.125 * pe * mz, -0.125 * pe * mz,
+                                     -0.125 * me * pz, 0.125 * me * pz, 0.125 * pe * pz, -0.125 * pe * pz};
+              const double deta[8] = {-0.125 * mx * mz, -0.125 * px * mz, 0.125 * px * mz, 0.125 * mx * mz,
+                                      -0.125 * mx * pz, -0.125 * px * pz, 0.125 * px * pz, 0.125 * mx * pz};
+              const double dzeta[8] = {-0.125 * mx * me, -0.125 * px * me, -0.125 * px * pe, -0.125 * mx * pe,
+                                       0.125 * mx * me, 0.125 * px * me, 0.125 * px * pe, 0.125 * mx * pe};
+              double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+              for (int a = 0; a < 8; ++a) {
+                const double* c = coords + 3 * (int64_t)cn[a];
+                for (int d = 0; d < 3; ++d) {
+                  J[0][d] += dxi[a] * c[d];
+                  J[1][d] += deta[a] * c[d];
+                  J[2][d] += dzeta[a] * c[d];
+                }
+              }
+              detJ = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                     J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+              Ni = Nh[li];
+            }
+            sum += Ni * qdot * (1.0 * detJ);
+          }
+    }
+    rhs[(int64_t)n * nb_dof] = sum;
+  }
+}
+
 /* FemModuleElasticity::_applyBodyForce, tetrahedra (modules/elasticity/BodyForce.h:148-160) */
 void afo_rhs_body_force_tet4(int nb_cell, const double* coords, const int32_t* cell_nodes, const double f[3],
                              double* rhs) {

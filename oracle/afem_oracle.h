@@ -77,6 +77,9 @@ void afo_rhs_constant_source(int dim, int nb_node, const double* coords, const i
                              double* rhs);
 
 /* Body force on tetrahedra, cell loop with += (modules/elasticity/BodyForce.h:148-160). */
+void afo_rhs_constant_source_q1(int dim, int nb_node, const double* coords, const int32_t* cell_nodes,
+                                const int32_t* nc_ptr, const int32_t* nc_cell, double qdot, int nb_dof,
+                                double* rhs);
 void afo_rhs_body_force_tet4(int nb_cell, const double* coords, const int32_t* cell_nodes, const double f[3],
                              double* rhs);
 void afo_rhs_boundary_faces(int dim, int nb_face, const double* coords, const int32_t* face_nodes,

@@ -61,6 +61,8 @@ def _declare(L):
     L.afo_rhs_body_force_tet4.restype = None
     L.afo_rhs_boundary_faces.argtypes = [C.c_int, C.c_int, _P, _P, _P, C.c_int, _P, C.c_int, _P]
     L.afo_rhs_boundary_faces.restype = None
+    L.afo_rhs_constant_source_q1.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, C.c_double, C.c_int, _P]
+    L.afo_rhs_constant_source_q1.restype = None
     L.afo_dirichlet_penalty.argtypes = [C.c_int, _P, C.c_int, C.c_int, C.c_double, C.c_double, _P, _P, _P]
     L.afo_dirichlet_penalty.restype = None
     L.afo_dirichlet_elimination.argtypes = [C.c_int, _P, C.c_int, C.c_int, C.c_double, C.c_uint8, _P, _P]
@@ -163,6 +165,15 @@ def rhs_body_force_tet4(coords, cell_nodes, f, rhs=None):
         rhs = np.zeros(coords.shape[0] * 3)
     fv = _c(f, np.float64)
     lib().afo_rhs_body_force_tet4(cell_nodes.shape[0], _p(coords), _p(cell_nodes), _p(fv), _p(rhs))
+    return rhs
+
+
+def rhs_constant_source_q1(dim, coords, cell_nodes, nc_ptr, nc_cell, qdot, nb_dof=1):
+    coords = _c(coords, np.float64)
+    cell_nodes = _c(cell_nodes, np.int32)
+    rhs = np.zeros(coords.shape[0] * nb_dof)
+    lib().afo_rhs_constant_source_q1(dim, coords.shape[0], _p(coords), _p(cell_nodes), _p(_c(nc_ptr, np.int32)),
+                                     _p(_c(nc_cell, np.int32)), float(qdot), nb_dof, _p(rhs))
     return rhs
 
 

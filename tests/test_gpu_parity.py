@@ -401,3 +401,33 @@ def test_q1_structure_and_values_match_oracle(cuda_ctx, name):
     kind = O.POISSON_QUAD4 if m.dim == 2 else O.POISSON_HEXA8
     ref = O.assemble(kind, m.coords, m.cells, ptr, nc, rp, cols, cell_coeff=k.cpu().numpy())
     assert rel_err_rows(f.values.cpu().numpy(), ref, rp) < REL
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_q1_constant_source(cuda_ctx, dim):
+    m = meshgen.unit_square_quad(17, seed=3) if dim == 2 else meshgen.unit_cube_hex(6, seed=3)
+    f = build_format(cuda_ctx, m)
+    rhs = torch.zeros(m.nb_node, dtype=torch.float64, device="cuda")
+    f.rhs_constant_source(-5.5, rhs)
+    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    ref = O.rhs_constant_source_q1(dim, m.coords, m.cells, ptr, nc, -5.5)
+    np.testing.assert_allclose(rhs.cpu().numpy(), ref, rtol=1e-13, atol=0)
+
+
+def test_q1_poisson_solve(cuda_ctx):
+    """Hexa8 assembly + Q1 source + row-column elimination + CG to 1e-10,
+    against the oracle's CG on the oracle's system."""
+    m = meshgen.unit_cube_hex(8, seed=4)
+    f = build_format(cuda_ctx, m)
+    f.assemble_poisson()
+    ls = fem.DoFLinearSystem(cuda_ctx, m.nb_node)
+    f.to_linear_system(ls)
+    f.rhs_constant_source(1.0, ls.rhs_variable())
+    nodes = torch.as_tensor(m.groups["x_faces"], device="cuda")
+    ls.apply_dirichlet_elimination(fem.ELIMINATE_ROW_COLUMN, nodes, 1, 0, 0.0)
+    info = ls.apply_linear_system_transformation_and_solve(fem.solver_options(rtol=1e-10, max_iter=5000))
+    assert info.status == 0 and info.relres < 1e-10
+    rp, cols, vals = (t.cpu().numpy() for t in f.to_csr())
+    x_ref, _, _ = O.pcg_jacobi(rp, cols, vals, ls.rhs_variable().cpu().numpy(), rtol=1e-13, max_iter=20000)
+    x = ls.solution_variable().cpu().numpy()
+    assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) < 1e-8

@@ -167,3 +167,14 @@ def test_boundary_face_terms_integrate_the_boundary(dim):
     r = O.rhs_boundary_faces(dim, m.coords, f[on], out[on], O.FACE_NORMAL, [1.0, 0.0, 0.0][:dim], 1,
                              np.zeros(m.nb_node))
     assert abs(r.sum() - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_q1_source_integrates_the_domain(dim):
+    """The Quad4 / Hexa8 constant source sums to qdot x |domain| (2x2(x2) Gauss
+    points integrate the shape functions exactly)."""
+    from arcanefem_gb300 import meshgen
+    m = meshgen.unit_square_quad(9, seed=2) if dim == 2 else meshgen.unit_cube_hex(4, seed=2)
+    ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+    r = O.rhs_constant_source_q1(dim, m.coords, m.cells, ptr, nc, 2.5)
+    assert abs(r.sum() - 2.5) < 1e-12
