@@ -14,10 +14,12 @@ the case parameters taken from the reference's ``.arc`` input.
 from __future__ import annotations
 
 import os
-import struct
 import sys
 
 import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+from arcanefem_gb300 import meshio  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -51,128 +53,11 @@ CASES = {
         penalty=1e30, eps=1e-3, min_value=1e-10),
 }
 
-ELEM_NODES = {1: 2, 2: 3, 3: 4, 4: 4, 5: 8, 15: 1}
-
-
-class Reader:
-    def __init__(self, data: bytes):
-        self.d = data
-        self.p = 0
-
-    def line(self) -> str:
-        e = self.d.index(b"\n", self.p)
-        s = self.d[self.p:e].decode()
-        self.p = e + 1
-        return s.strip()
-
-    def take(self, fmt: str):
-        n = struct.calcsize(fmt)
-        v = struct.unpack_from(fmt, self.d, self.p)
-        self.p += n
-        return v
-
-    def arr(self, dtype, count):
-        a = np.frombuffer(self.d, dtype=dtype, count=count, offset=self.p)
-        self.p += a.nbytes
-        return a
-
-
-def read_msh41(path: str):
-    """Minimal reader of binary gmsh 4.1 (public format specification):
-    physical names, entities, nodes and elements."""
-    r = Reader(open(path, "rb").read())
-    names = {}
-    ent_phys = {}
-    nodes_tag = []
-    nodes_xyz = []
-    elems = []   # (dim, entity_tag, type, tags[n], node_tags[n, k])
-    while r.p < len(r.d):
-        head = r.line()
-        if head == "$MeshFormat":
-            ver, ftype, dsize = r.line().split()
-            assert ver == "4.1" and ftype == "1" and dsize == "8", (ver, ftype, dsize)
-            one, = r.take("<i")
-            assert one == 1
-            r.line()
-            assert r.line() == "$EndMeshFormat"
-        elif head == "$PhysicalNames":
-            n = int(r.line())
-            for _ in range(n):
-                s = r.line()
-                dim, tag, rest = s.split(" ", 2)
-                names[(int(dim), int(tag))] = rest.strip().strip('"')
-            assert r.line() == "$EndPhysicalNames"
-        elif head == "$Entities":
-            npt, ncu, nsu, nvo = r.take("<4Q")
-            for _ in range(npt):
-                tag, = r.take("<i")
-                r.take("<3d")
-                nph, = r.take("<Q")
-                ent_phys[(0, tag)] = list(r.take(f"<{nph}i"))
-            for dim, cnt in ((1, ncu), (2, nsu), (3, nvo)):
-                for _ in range(cnt):
-                    tag, = r.take("<i")
-                    r.take("<6d")
-                    nph, = r.take("<Q")
-                    ent_phys[(dim, tag)] = list(r.take(f"<{nph}i"))
-                    nb, = r.take("<Q")
-                    r.take(f"<{nb}i")
-            r.line()
-            assert r.line() == "$EndEntities"
-        elif head == "$Nodes":
-            nblk, nnod, _, _ = r.take("<4Q")
-            for _ in range(nblk):
-                edim, etag, param = r.take("<3i")
-                n, = r.take("<Q")
-                tags = r.arr("<u8", n).astype(np.int64)
-                xyz = r.arr("<f8", n * 3).reshape(n, 3)
-                assert param == 0
-                nodes_tag.append(tags)
-                nodes_xyz.append(xyz)
-            r.line()
-            assert r.line() == "$EndNodes"
-        elif head == "$Elements":
-            nblk, nel, _, _ = r.take("<4Q")
-            for _ in range(nblk):
-                edim, etag, etype = r.take("<3i")
-                n, = r.take("<Q")
-                k = ELEM_NODES[etype]
-                data = r.arr("<u8", n * (k + 1)).reshape(n, k + 1).astype(np.int64)
-                elems.append((edim, etag, etype, data[:, 0], data[:, 1:]))
-            r.line()
-            assert r.line() == "$EndElements"
-        elif head.startswith("$"):
-            end = "$End" + head[1:]
-            idx = r.d.index(end.encode(), r.p)
-            r.p = idx
-            r.line()
-        else:
-            continue
-    tags = np.concatenate(nodes_tag)
-    xyz = np.concatenate(nodes_xyz)
-    return names, ent_phys, tags, xyz, elems
-
-
 def build_case(root: str, name: str, spec: dict) -> dict:
-    names, ent_phys, tags, xyz, elems = read_msh41(os.path.join(root, spec["mesh"]))
-    cell_dim = max(e[0] for e in elems)
-    order = np.argsort(tags)
-    tags_sorted = tags[order]
-    # node local ids follow increasing gmsh node tag
-    coords = xyz[order]
-    tag_to_lid = {int(t): i for i, t in enumerate(tags_sorted)}
-    cells = [e[4] for e in elems if e[0] == cell_dim]
-    cells = np.concatenate(cells)
-    cells = np.vectorize(tag_to_lid.__getitem__)(cells).astype(np.int32)
-    groups = {}
-    for (pdim, ptag), pname in names.items():
-        sel = []
-        for edim, etag, etype, etags, enodes in elems:
-            if edim == pdim and ptag in ent_phys.get((edim, etag), []):
-                sel.append(enodes.ravel())
-        if sel:
-            ids = np.unique(np.concatenate(sel))
-            groups[pname] = np.array([tag_to_lid[int(t)] for t in ids], np.int32)
+    """Mesh through the library's gmsh MSH 4.1 reader (node local ids in
+    increasing gmsh tag order), check file as given."""
+    d = meshio.read_msh(os.path.join(root, spec["mesh"]))
+    coords, cells, tags_sorted, groups = d.mesh.coords, d.mesh.cells, d.node_tags, d.mesh.groups
     check = np.loadtxt(os.path.join(root, spec["check"]))
     out = dict(coords=coords.astype(np.float64), cells=cells, node_tags=tags_sorted.astype(np.int64),
                check_uid=check[:, 0].astype(np.int64), check_val=check[:, 1:].astype(np.float64))
