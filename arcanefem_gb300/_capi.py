@@ -105,6 +105,7 @@ SIGNATURES = {
     "afem_mpnn_set_operator": (C.c_int, [_P, C.c_int, _P, _P, _P]),
     "afem_mpnn_forward": (C.c_int, [_P, C.c_int, _P, _P]),
     "afem_mpnn_scalings": (C.c_int, [_P, C.c_int, _P]),
+    "afem_mpnn_set_coarse_rows": (C.c_int, [_P, C.c_int]),
     "afem_mpnn_gradients": (C.c_int, [_P, C.c_int, _P, _P, _P, C.POINTER(C.c_double)]),
     "afem_mpnn_train_step": (C.c_int, [_P, C.c_int, _P, _P, C.c_float, C.POINTER(C.c_double)]),
     "afem_fcg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.POINTER(SolverOptions),

@@ -1,17 +1,23 @@
-// Learned preconditioner: an additive multilevel preconditioner whose level
-// scalings are predicted by a message-passing network (MPNN) on the mesh
-// graph, trained on the GPU and applied inside flexible CG.
+// Learned preconditioner: a geometric multigrid V-cycle whose per-node
+// smoother weights are predicted by a message-passing network (MPNN) on the
+// mesh graph, trained on the GPU and applied inside flexible CG.
 //
-// Preconditioner (linear and symmetric positive definite in r):
-//   M r = sum_{l=0}^{L-1} Q_l diag(d_l) Q_l^T r,   Q_0 = I, Q_{l+1} = Q_l P_l,
-// P_l the bilinear prolongation of the structured hierarchy (the additive
-// multilevel / BPX form), evaluated as one down sweep t_{l+1} = P_l^T t_l and
-// one up sweep w_l = d_l t_l + P_l w_{l+1}.  The scalings are
-//   d_l = base_l * exp(c_l),  base_l = (R..R 1) / (R..R diag A),
-// so c = 0 is multilevel diagonal scaling; the network predicts c_l per node.
-// The caller's P_l should vanish on Dirichlet nodes (rows of fine and columns
-// of coarse boundary nodes): coarse functions that violate the boundary
-// condition cost a factor ~2 in condition number per level.
+// Preconditioner: one symmetric V(1,1)-cycle from a zero initial guess on the
+// Galerkin hierarchy A_0 = A, A_{l+1} = P_l^T A_l P_l (P_l the caller's
+// prolongation, computed here in FP64 on the caller's coarse patterns):
+//   V_l(r):  x1 = d_l .* r ;  s = r - A_l x1
+//            x2 = x1 + P_l V_{l+1}(P_l^T s)
+//            u  = r - A_l x2 ;  return x2 + d_l .* u
+//   V_{L-1}(r) = d_{L-1} .* r
+// Weighted-Jacobi smoothers with per-node weights
+//   d_l = cap_l * sigmoid(c_l + logit(0.8)),  cap_l = 2 / sum_j |A_l,ij|
+// (0 on empty rows): 2 diag(d_l)^-1 - A_l is strictly diagonally dominant, so
+// the V-cycle is symmetric positive definite whatever the network predicts;
+// c = 0 is l1-Jacobi smoothing at 0.8 of the cap.  The caller's P_l should
+// vanish on Dirichlet nodes (rows of fine and columns of coarse boundary
+// nodes), so that the coarse spaces satisfy the boundary condition.
+// Fine levels run one kernel per step; the levels of <= kCoarseRows rows run
+// in ONE block per vector with block barriers.
 //
 // Network (message-passing layers of width 64, BF16 weights and activations,
 // FP32 accumulation) on the coefficient features x0 = [1, log(A_ii / mean)]:
@@ -21,13 +27,14 @@
 //   c_l = o_l . w_l + beta_l                      (one head per level)
 // S_0 is the matrix graph with weights -A_ij / sqrt(A_ii A_jj); S_l (l >= 1),
 // R_l, P_l come from the caller (CSR).  It runs once per operator and per
-// training step; the per-iteration application is the two sweeps above.
+// training step; the per-iteration application is the V-cycle above.
 //
 // GEMMs (all K = 64): mma.sync m16n8k16 BF16 -> FP32 tensor-core tiles; the
 // weight gradients X^T G use ldmatrix.trans.  Aggregation / transfers: CSR
 // SpMM over 64-wide rows.  Training: the mean relative energy norm of the
 // error propagation, ||(I - M A) e||_A^2 / ||e||_A^2 over (r = A e, e) pairs
-// (A in FP32), Adam on FP32 master weights.
+// (A in FP32), back-propagated through the adjoint V-cycle; Adam on FP32
+// master weights.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -42,6 +49,7 @@ constexpr int kF = 64;                 // hidden width
 constexpr int kGemmRows = 128;         // rows per GEMM block (8 warps x 16)
 constexpr int kMaxLevels = 12;
 constexpr int kMaxBatch = 64;
+constexpr float kLogitTheta = 1.38629436f;   // log(0.8 / 0.2): untrained weight = 0.8 of the l1 cap
 
 typedef __nv_bfloat16 bf16;
 
@@ -278,8 +286,7 @@ __global__ void k_level0_weights(int n, const int32_t* __restrict__ rp, const in
 }
 
 __global__ void k_diag(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
-                       const double* __restrict__ vals, double* __restrict__ diag, float* __restrict__ diag32,
-                       float* __restrict__ ones) {
+                       const double* __restrict__ vals, double* __restrict__ diag) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double d = 1.0;
     for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
@@ -289,8 +296,6 @@ __global__ void k_diag(int n, const int32_t* __restrict__ rp, const int32_t* __r
       }
     d = d > 0 ? d : 1.0;
     diag[i] = d;
-    diag32[i] = (float)d;
-    ones[i] = 1.f;
   }
 }
 
@@ -312,7 +317,7 @@ __global__ void k_input_layer(int n, const double* __restrict__ diag, double mea
   }
 }
 
-// level head: c = o . w + beta ; d = base * exp(clamp(c))
+// level head: c = o . w + beta ; d = cap * sigmoid(clamp(c + logit(0.8)))
 __global__ void k_head(int n, const bf16* __restrict__ o, const float* __restrict__ w, const float* __restrict__ base,
                        float* __restrict__ d) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -324,7 +329,7 @@ __global__ void k_head(int n, const bf16* __restrict__ o, const float* __restric
       acc = fmaf(__low2float(v), w[2 * c], acc);
       acc = fmaf(__high2float(v), w[2 * c + 1], acc);
     }
-    d[i] = base[i] * __expf(fminf(fmaxf(acc, -20.f), 20.f));
+    d[i] = base[i] / (1.f + __expf(-fminf(fmaxf(acc + kLogitTheta, -30.f), 30.f)));
   }
 }
 
@@ -341,66 +346,229 @@ __global__ void k_sweep(int nrow, int ncol, const int32_t* __restrict__ rp, cons
   }
 }
 
-// The coarse end of the multilevel application in ONE block per vector:
-// levels lo..L-1 are small (<= kCoarseRows rows each), so their down sweep,
-// coarsest scaling and up sweep run back to back with block barriers instead
-// of one launch per level.  In: t_lo ([b][n_lo]); out: w_lo; t_l (l > lo)
-// are kept for the training backward.
-constexpr int kCoarseRows = 8192;
+// ---------------------------------------------------------------------------
+// V-cycle kernels (FP32).  The row operations below are shared by the
+// per-level kernels (grid-stride over the rows of one vector, the vector in
+// grid.y) and the coarse-levels kernels (block-stride, one block per vector).
+// Pointers are already offset to the vector.
+
+// s = r - A (d .* r)     (forward pre-smoothing residual; backward x2b = g - A (d .* g))
+__device__ __forceinline__ void vc_smooth_res(int i0, int st, int n, const int32_t* __restrict__ rp,
+                                              const int32_t* __restrict__ cols, const float* __restrict__ w,
+                                              const float* __restrict__ d, const float* __restrict__ r,
+                                              float* __restrict__ s) {
+  for (int i = i0; i < n; i += st) {
+    float acc = r[i];
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+      const int32_t j = cols[k];
+      acc = fmaf(-w[k], d[j] * r[j], acc);
+    }
+    s[i] = acc;
+  }
+}
+
+// y = (d ? d .* t : 0) + M x
+__device__ __forceinline__ void vc_spmv(int i0, int st, int n, const int32_t* __restrict__ rp,
+                                        const int32_t* __restrict__ cols, const float* __restrict__ w,
+                                        const float* __restrict__ x, const float* __restrict__ d,
+                                        const float* __restrict__ t, float* __restrict__ y) {
+  for (int i = i0; i < n; i += st) {
+    float acc = d ? d[i] * t[i] : 0.f;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) acc = fmaf(w[k], x[cols[k]], acc);
+    y[i] = acc;
+  }
+}
+
+// u = r - A x2 ; y = x2 + d .* u   (post-smoothing; u kept for the backward when non-null)
+__device__ __forceinline__ void vc_post(int i0, int st, int n, const int32_t* __restrict__ rp,
+                                        const int32_t* __restrict__ cols, const float* __restrict__ w,
+                                        const float* __restrict__ d, const float* __restrict__ r,
+                                        const float* __restrict__ x2, float* __restrict__ u, float* __restrict__ y) {
+  for (int i = i0; i < n; i += st) {
+    float acc = r[i];
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) acc = fmaf(-w[k], x2[cols[k]], acc);
+    if (u) u[i] = acc;
+    y[i] = fmaf(d[i], acc, x2[i]);
+  }
+}
+
+// adjoint of the pre-smoothing: x1b = x2b - A sb ; rb = d .* (g + x1b) + sb
+__device__ __forceinline__ void vc_pre_adjoint(int i0, int st, int n, const int32_t* __restrict__ rp,
+                                               const int32_t* __restrict__ cols, const float* __restrict__ w,
+                                               const float* __restrict__ d, const float* __restrict__ g,
+                                               const float* __restrict__ x2b, const float* __restrict__ sb,
+                                               float* __restrict__ x1b, float* __restrict__ rb) {
+  for (int i = i0; i < n; i += st) {
+    float acc = x2b[i];
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) acc = fmaf(-w[k], sb[cols[k]], acc);
+    x1b[i] = acc;
+    if (rb) rb[i] = fmaf(d[i], g[i] + acc, sb[i]);
+  }
+}
+
+__global__ void k_vc_smooth_res(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                const float* __restrict__ w, const float* __restrict__ d, const float* __restrict__ r,
+                                float* __restrict__ s) {
+  const int64_t o = (int64_t)blockIdx.y * n;
+  vc_smooth_res(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, rp, cols, w, d, r + o, s + o);
+}
+
+__global__ void k_vc_post(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                          const float* __restrict__ w, const float* __restrict__ d, const float* __restrict__ r,
+                          const float* __restrict__ x2, float* __restrict__ u, float* __restrict__ y) {
+  const int64_t o = (int64_t)blockIdx.y * n;
+  vc_post(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, rp, cols, w, d, r + o, x2 + o,
+          u ? u + o : nullptr, y + o);
+}
+
+__global__ void k_vc_pre_adjoint(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                 const float* __restrict__ w, const float* __restrict__ d, const float* __restrict__ g,
+                                 const float* __restrict__ x2b, const float* __restrict__ sb, float* __restrict__ x1b,
+                                 float* __restrict__ rb) {
+  const int64_t o = (int64_t)blockIdx.y * n;
+  vc_pre_adjoint(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, rp, cols, w, d, g + o, x2b + o,
+                 sb + o, x1b + o, rb ? rb + o : nullptr);
+}
+
+// The coarse end of the V-cycle in ONE block per vector: levels lo..L-1 are
+// small (<= kCoarseRows rows each), so their steps run back to back with
+// block barriers instead of one launch each.
+constexpr int kCoarseRows = 2048;
 constexpr int kCoarseBlock = 1024;
 
 struct CoarseLevel {
   int n;
-  const int32_t *pt_rp, *pt_cols, *p_rp, *p_cols;   // P_l^T (n_{l+1} rows), P_l (n_l rows)
-  const float *pt_w, *p_w, *d;
-  float *t, *w;
+  const int32_t *a_rp, *a_cols, *pt_rp, *pt_cols, *p_rp, *p_cols;   // A_l, P_l^T (n_{l+1} rows), P_l (n_l rows)
+  const float *a_w, *pt_w, *p_w, *d;
+  // [B][n] buffers: t = the level's input r (l > lo), vs = s / sb, x2 = x2 / x2b,
+  // u, w = the level's output x / rb (l > lo), g = the adjoint input, x1b
+  float *t, *vs, *x2, *u, *w, *g, *x1b;
 };
 struct CoarsePlan {
   int lo, L;
   CoarseLevel lev[kMaxLevels];
 };
 
-__global__ void __launch_bounds__(kCoarseBlock) k_coarse_apply(CoarsePlan plan, const float* __restrict__ t_lo,
-                                                               float* __restrict__ w_lo) {
+// forward: x_lo = V_lo(r_lo), keeping t, u per level for the backward
+__global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse(CoarsePlan plan, const float* __restrict__ r_lo,
+                                                            float* __restrict__ x_lo) {
   const int64_t b = blockIdx.y;
-  const int lo = plan.lo, L = plan.L;
-  for (int l = lo; l + 1 < L; ++l) {   // t_{l+1} = P_l^T t_l
+  const int lo = plan.lo, L = plan.L, i0 = threadIdx.x, st = blockDim.x;
+  for (int l = lo; l + 1 < L; ++l) {   // pre-smoothing residual, restriction
     const CoarseLevel& A = plan.lev[l];
     const CoarseLevel& C = plan.lev[l + 1];
-    const float* tl = (l == lo ? t_lo : A.t) + b * A.n;
-    float* tn = C.t + b * C.n;
-    for (int i = threadIdx.x; i < C.n; i += blockDim.x) {
-      float s = 0.f;
-      for (int32_t k = A.pt_rp[i]; k < A.pt_rp[i + 1]; ++k) s = fmaf(A.pt_w[k], tl[A.pt_cols[k]], s);
-      tn[i] = s;
-    }
+    const float* r = (l == lo ? r_lo : A.t) + b * A.n;
+    float* s = A.vs + b * A.n;
+    vc_smooth_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, r, s);
+    __syncthreads();
+    vc_spmv(i0, st, C.n, A.pt_rp, A.pt_cols, A.pt_w, s, nullptr, nullptr, C.t + b * C.n);
     __syncthreads();
   }
   {
     const CoarseLevel& C = plan.lev[L - 1];
-    const float* tc = (L - 1 == lo ? t_lo : C.t) + b * C.n;
-    float* wc = (L - 1 == lo ? w_lo : C.w) + b * C.n;
-    for (int i = threadIdx.x; i < C.n; i += blockDim.x) wc[i] = C.d[i] * tc[i];
+    const float* r = (L - 1 == lo ? r_lo : C.t) + b * C.n;
+    float* x = (L - 1 == lo ? x_lo : C.w) + b * C.n;
+    for (int i = i0; i < C.n; i += st) x[i] = C.d[i] * r[i];
     __syncthreads();
   }
-  for (int l = L - 2; l >= lo; --l) {   // w_l = d_l t_l + P_l w_{l+1}
+  for (int l = L - 2; l >= lo; --l) {   // prolongation + d r, post-smoothing
     const CoarseLevel& A = plan.lev[l];
-    const float* tl = (l == lo ? t_lo : A.t) + b * A.n;
-    const float* wn = plan.lev[l + 1].w + b * plan.lev[l + 1].n;
-    float* wl = (l == lo ? w_lo : A.w) + b * A.n;
-    for (int i = threadIdx.x; i < A.n; i += blockDim.x) {
-      float s = A.d[i] * tl[i];
-      for (int32_t k = A.p_rp[i]; k < A.p_rp[i + 1]; ++k) s = fmaf(A.p_w[k], wn[A.p_cols[k]], s);
-      wl[i] = s;
-    }
+    const CoarseLevel& C = plan.lev[l + 1];
+    const float* r = (l == lo ? r_lo : A.t) + b * A.n;
+    float* x2 = A.x2 + b * A.n;
+    vc_spmv(i0, st, A.n, A.p_rp, A.p_cols, A.p_w, C.w + b * C.n, A.d, r, x2);
+    __syncthreads();
+    vc_post(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, r, x2, A.u + b * A.n, (l == lo ? x_lo : A.w) + b * A.n);
     __syncthreads();
   }
 }
 
-// y = x / z elementwise (base_l = count_l / diag_l)
-__global__ void k_ratio(int n, const float* __restrict__ x, const float* __restrict__ z, float* __restrict__ y) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    y[i] = z[i] > 0.f ? x[i] / z[i] : 0.f;
+// backward: from the adjoint g_lo of x_lo, rb_lo (the adjoint of r_lo), and
+// per level g (the adjoint of the level's output) and x1b for the weights
+__global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse_adjoint(CoarsePlan plan, const float* __restrict__ g_lo,
+                                                                    float* __restrict__ rb_lo) {
+  const int64_t b = blockIdx.y;
+  const int lo = plan.lo, L = plan.L, i0 = threadIdx.x, st = blockDim.x;
+  for (int l = lo; l + 1 < L; ++l) {   // adjoint of the post-smoothing, then of the prolongation
+    const CoarseLevel& A = plan.lev[l];
+    const CoarseLevel& C = plan.lev[l + 1];
+    const float* g = (l == lo ? g_lo : A.g) + b * A.n;
+    float* x2b = A.x2 + b * A.n;
+    vc_smooth_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, g, x2b);
+    __syncthreads();
+    vc_spmv(i0, st, C.n, A.pt_rp, A.pt_cols, A.pt_w, x2b, nullptr, nullptr, C.g + b * C.n);
+    __syncthreads();
+  }
+  {
+    const CoarseLevel& C = plan.lev[L - 1];
+    const float* g = (L - 1 == lo ? g_lo : C.g) + b * C.n;
+    float* rb = (L - 1 == lo ? rb_lo : C.w) + b * C.n;
+    for (int i = i0; i < C.n; i += st) rb[i] = C.d[i] * g[i];
+    __syncthreads();
+  }
+  for (int l = L - 2; l >= lo; --l) {   // adjoint of the restriction, then of the pre-smoothing
+    const CoarseLevel& A = plan.lev[l];
+    const CoarseLevel& C = plan.lev[l + 1];
+    const float* g = (l == lo ? g_lo : A.g) + b * A.n;
+    float* sb = A.vs + b * A.n;
+    vc_spmv(i0, st, A.n, A.p_rp, A.p_cols, A.p_w, C.w + b * C.n, nullptr, nullptr, sb);
+    __syncthreads();
+    vc_pre_adjoint(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, g, A.x2 + b * A.n, sb, A.x1b + b * A.n,
+                   (l == lo ? rb_lo : A.w) + b * A.n);
+    __syncthreads();
+  }
+}
+
+// Galerkin product C = P^T A P, one thread per coarse row I, on the caller's
+// pattern of C: sum over the children i of I (row I of P^T), the entries
+// A_ij of row i and the parents J of j (row j of P), in that fixed order, in
+// FP64.  Also the FP32 copy and the l1 cap 2 / sum_J |C_IJ|.  An entry
+// outside the pattern sets *missing.
+__global__ void k_rap(int nc, const int32_t* __restrict__ pt_rp, const int32_t* __restrict__ pt_cols,
+                      const float* __restrict__ pt_w, const int32_t* __restrict__ a_rp,
+                      const int32_t* __restrict__ a_cols, const double* __restrict__ a_v,
+                      const int32_t* __restrict__ p_rp, const int32_t* __restrict__ p_cols,
+                      const float* __restrict__ p_w, const int32_t* __restrict__ c_rp,
+                      const int32_t* __restrict__ c_cols, double* __restrict__ c_v, float* __restrict__ c_w,
+                      float* __restrict__ cap, int* __restrict__ missing) {
+  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nc; I += gridDim.x * blockDim.x) {
+    const int32_t cb = c_rp[I], ce = c_rp[I + 1];
+    for (int32_t k = cb; k < ce; ++k) c_v[k] = 0.0;
+    for (int32_t kk = pt_rp[I]; kk < pt_rp[I + 1]; ++kk) {
+      const int32_t i = pt_cols[kk];
+      const double wi = pt_w[kk];
+      for (int32_t ka = a_rp[i]; ka < a_rp[i + 1]; ++ka) {
+        const int32_t j = a_cols[ka];
+        const double aij = wi * a_v[ka];
+        for (int32_t kp = p_rp[j]; kp < p_rp[j + 1]; ++kp) {
+          const int32_t J = p_cols[kp];
+          int32_t pos = cb;
+          while (pos < ce && c_cols[pos] != J) ++pos;
+          if (pos == ce) {
+            atomicOr(missing, 1);
+            continue;
+          }
+          c_v[pos] += aij * (double)p_w[kp];
+        }
+      }
+    }
+    double l1 = 0.0;
+    for (int32_t k = cb; k < ce; ++k) {
+      c_w[k] = (float)c_v[k];
+      l1 += fabs(c_v[k]);
+    }
+    cap[I] = l1 > 0.0 ? (float)(2.0 / l1) : 0.f;
+  }
+}
+
+// cap = 2 / sum_j |A_ij| for the level-0 matrix (0 on an empty row)
+__global__ void k_l1cap(int n, const int32_t* __restrict__ rp, const double* __restrict__ vals,
+                        float* __restrict__ cap) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double l1 = 0.0;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) l1 += fabs(vals[k]);
+    cap[i] = l1 > 0.0 ? (float)(2.0 / l1) : 0.f;
+  }
 }
 
 // per-sample energy sums: sums[b*4+0] += e . (A e), sums[b*4+1] += (e - z) . (A (e - z))
@@ -437,13 +605,20 @@ __global__ void k_energy_grad(int n, int batch, const double* __restrict__ sums,
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) Av[b * n + i] *= scale;
 }
 
-// dc_l[i] = d_l[i] * sum_b t_l[b][i] s_l[b][i]   (dL/dc through d = base exp(c))
-__global__ void k_dc(int n, int batch, const float* __restrict__ t, const float* __restrict__ s,
-                     const float* __restrict__ d, float* __restrict__ dc) {
+// dL/dc_l through d = cap sigmoid(c + logit 0.8):
+//   dc_i = d_i (1 - d_i / cap_i) sum_b (g u + x1b r)   (coarsest level: sum_b g r)
+__global__ void k_dc_vcycle(int n, int batch, const float* __restrict__ d, const float* __restrict__ cap,
+                            const float* __restrict__ g, const float* __restrict__ u, const float* __restrict__ x1b,
+                            const float* __restrict__ r, float* __restrict__ dc) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float acc = 0.f;
-    for (int b = 0; b < batch; ++b) acc = fmaf(t[(int64_t)b * n + i], s[(int64_t)b * n + i], acc);
-    dc[i] = acc * d[i];
+    for (int b = 0; b < batch; ++b) {
+      const int64_t k = (int64_t)b * n + i;
+      if (u) acc = fmaf(x1b[k], r[k], fmaf(g[k], u[k], acc));
+      else acc = fmaf(g[k], r[k], acc);
+    }
+    const float di = d[i], ci = cap[i];
+    dc[i] = ci > 0.f ? acc * di * (1.f - di / ci) : 0.f;
   }
 }
 
@@ -594,7 +769,10 @@ struct afem_mpnn_s {
   CsrLevel R[kMaxLevels];        // restriction l -> l+1
   CsrLevel Rt[kMaxLevels];       // its transpose (backward)
   CsrLevel P[kMaxLevels];        // prolongation l+1 -> l
-  CsrLevel Pt[kMaxLevels];       // its transpose (down sweep)
+  CsrLevel Pt[kMaxLevels];       // its transpose (restriction of residuals)
+  CsrLevel Ac[kMaxLevels];       // Galerkin operators A_l, FP32 values (Ac[0]: the matrix on the level-0 graph)
+  double* ac64[kMaxLevels] = {};  // FP64 values of A_l, l >= 1
+  int* missing = nullptr;        // set by k_rap when a product entry falls outside the caller's pattern
   int max_batch = 1;
   // parameters (FP32 master, flat): W_in[2][64], b_in[64], per layer W1, W2 [64][64], b[64],
   // then per level a head w[64], beta.  Levels l >= NL have no layer: o_l = h_l = R o_{l-1}.
@@ -608,8 +786,6 @@ struct afem_mpnn_s {
   bf16* Wn = nullptr;   // [2 NL][64][64] BF16 (backward dX operands)
   // operator
   double* diag = nullptr;
-  float* diag32 = nullptr;
-  float* ones = nullptr;
   double mean_log = 0;
   int n0 = 0;
   bool have_operator = false;
@@ -624,15 +800,19 @@ struct afem_mpnn_s {
   float* dH[kMaxLevels] = {};                // FP32 d h per level [n][64]
   bf16* Gb = nullptr;                        // BF16 G [n0][64]
   float* ftmp = nullptr;                     // FP32 [n0][64]
-  // multilevel preconditioner
-  float* base[kMaxLevels] = {};              // base scaling per level [n_l]
-  float* d[kMaxLevels] = {};                 // learned scaling per level [n_l]
+  // V-cycle
+  float* base[kMaxLevels] = {};              // l1 cap 2 / ||row||_1 per level [n_l]
+  float* d[kMaxLevels] = {};                 // learned smoother weights per level [n_l]
   float* dc[kMaxLevels] = {};                // dL/dc per level [n_l]
-  float* t[kMaxLevels] = {};                 // down sweep [B][n_l] (level 0: the input r, t0)
+  float* t[kMaxLevels] = {};                 // level input r_l [B][n_l] (level 0: the caller's r, t0)
   const float* t0 = nullptr;
-  int coarse_lo = 0;                         // levels coarse_lo..L-1 run in k_coarse_apply
-  float* w[kMaxLevels] = {};                 // up sweep [B][n_l] (w[0] = M r)
-  float* s[kMaxLevels] = {};                 // adjoint down sweep [B][n_l]
+  int coarse_lo = 0;                         // levels coarse_lo..L-1 run in the coarse-levels kernels
+  float* w[kMaxLevels] = {};                 // level output x_l (w[0] = M r in training); backward: rb_l
+  float* s[kMaxLevels] = {};                 // adjoint g_l of the level output (s[0] = dL/dz)
+  float* vs[kMaxLevels] = {};                // pre-smoothing residual s_l; backward: sb_l
+  float* x2[kMaxLevels] = {};                // x1 + P x_{l+1}; backward: x2b_l
+  float* u[kMaxLevels] = {};                 // post-smoothing residual (kept for the backward)
+  float* x1b[kMaxLevels] = {};               // adjoint of the pre-smoothed x1
   double* sums = nullptr;                    // [B][4]
   float* part = nullptr;                     // partial sums (dW, db)
   int64_t part_cap = 0;
@@ -753,45 +933,117 @@ static afem_status features_forward(afem_mpnn net) {
   return AFEM_OK;
 }
 
-// z = M r for `batch` FP32 vectors (r, z: [batch][n0]); with z == nullptr the
-// result stays in w[0] and the down sweep in t[] (training keeps both)
+template <class Kernel, class... Args>
+static afem_status launch_batch(afem_mpnn net, Kernel k, const char* name, int nrow, int batch, Args... args) {
+  dim3 grid(grid_for(net->ctx, nrow, 256, 8), batch);
+  k<<<grid, 256, 0, net->ctx->stream>>>(args...);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, name, __FILE__, __LINE__);
+  ++net->ctx->launches;
+  return AFEM_OK;
+}
+
+static CoarsePlan coarse_plan(afem_mpnn net) {
+  CoarsePlan plan{};
+  plan.lo = net->coarse_lo;
+  plan.L = net->L;
+  for (int l = plan.lo; l < net->L; ++l) {
+    CoarseLevel& c = plan.lev[l];
+    c.n = net->n[l];
+    c.a_rp = net->Ac[l].rp;
+    c.a_cols = net->Ac[l].cols;
+    c.a_w = net->Ac[l].w;
+    c.d = net->d[l];
+    c.t = net->t[l];
+    c.vs = net->vs[l];
+    c.x2 = net->x2[l];
+    c.u = net->u[l];
+    c.w = net->w[l];
+    c.g = net->s[l];
+    c.x1b = net->x1b[l];
+    if (l + 1 < net->L) {
+      c.pt_rp = net->Pt[l].rp;
+      c.pt_cols = net->Pt[l].cols;
+      c.pt_w = net->Pt[l].w;
+      c.p_rp = net->P[l].rp;
+      c.p_cols = net->P[l].cols;
+      c.p_w = net->P[l].w;
+    }
+  }
+  return plan;
+}
+
+// z = M r (one V-cycle) for `batch` FP32 vectors (r, z: [batch][n0]); with
+// z == nullptr the result stays in w[0] and the states the backward needs
+// (t, u per level) are kept
 static afem_status apply(afem_mpnn net, int batch, const float* r, float* z) {
-  const int L = net->L, lo = net->coarse_lo;
+  const int lo = net->coarse_lo;
+  const bool keep = z == nullptr;
   if (!net->scalings_valid) AFEM_TRY(features_forward(net));
   net->t0 = r;
-  const float* tl = r;
-  for (int l = 0; l < lo; ++l) {   // fine levels: one sweep per level
-    AFEM_TRY(sweep(net, &net->Pt[l], batch, tl, nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
-    tl = net->t[l + 1];
+  for (int l = 0; l < lo; ++l) {   // fine levels down: s = r - A (d r), r_{l+1} = P^T s
+    const CsrLevel& A = net->Ac[l];
+    const int nl = net->n[l];
+    const float* rl = l == 0 ? r : net->t[l];
+    AFEM_TRY(launch_batch(net, k_vc_smooth_res, "k_vc_smooth_res", nl, batch, nl, (const int32_t*)A.rp,
+                          (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], rl, net->vs[l]));
+    AFEM_TRY(sweep(net, &net->Pt[l], batch, net->vs[l], nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
   }
-  float* w0 = z ? z : net->w[0];
+  float* x0 = z ? z : net->w[0];
   {
-    CoarsePlan plan{};
-    plan.lo = lo;
-    plan.L = L;
-    for (int l = lo; l < L; ++l) {
-      CoarseLevel& c = plan.lev[l];
-      c.n = net->n[l];
-      c.d = net->d[l];
-      c.t = net->t[l];
-      c.w = net->w[l];
-      if (l + 1 < L) {
-        c.pt_rp = net->Pt[l].rp;
-        c.pt_cols = net->Pt[l].cols;
-        c.pt_w = net->Pt[l].w;
-        c.p_rp = net->P[l].rp;
-        c.p_cols = net->P[l].cols;
-        c.p_w = net->P[l].w;
-      }
-    }
-    k_coarse_apply<<<dim3(1, batch), kCoarseBlock, 0, net->ctx->stream>>>(plan, tl, lo == 0 ? w0 : net->w[lo]);
+    k_vc_coarse<<<dim3(1, batch), kCoarseBlock, 0, net->ctx->stream>>>(coarse_plan(net), lo == 0 ? r : net->t[lo],
+                                                                      lo == 0 ? x0 : net->w[lo]);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "k_coarse_apply", __FILE__, __LINE__);
+    if (e != cudaSuccess) return cuda_fail(e, "k_vc_coarse", __FILE__, __LINE__);
     ++net->ctx->launches;
   }
-  for (int l = lo - 1; l >= 0; --l)   // fine levels back up
-    AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], net->d[l], l == 0 ? r : net->t[l], l == 0 ? w0 : net->w[l],
-                   net->n[l]));
+  for (int l = lo - 1; l >= 0; --l) {   // fine levels up: x2 = d r + P x_{l+1}, post-smoothing
+    const CsrLevel& A = net->Ac[l];
+    const int nl = net->n[l];
+    const float* rl = l == 0 ? r : net->t[l];
+    AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], net->d[l], rl, net->x2[l], nl));
+    AFEM_TRY(launch_batch(net, k_vc_post, "k_vc_post", nl, batch, nl, (const int32_t*)A.rp, (const int32_t*)A.cols,
+                          (const float*)A.w, (const float*)net->d[l], rl, (const float*)net->x2[l],
+                          keep ? net->u[l] : (float*)nullptr, l == 0 ? x0 : net->w[l]));
+  }
+  return AFEM_OK;
+}
+
+// dL/dc per level from the adjoint s[0] = dL/dz of the last training apply()
+static afem_status apply_adjoint(afem_mpnn net, int batch) {
+  afem_context ctx = net->ctx;
+  const int lo = net->coarse_lo, L = net->L;
+  for (int l = 0; l < lo; ++l) {   // adjoint of the post-smoothing, then of the prolongation
+    const CsrLevel& A = net->Ac[l];
+    const int nl = net->n[l];
+    AFEM_TRY(launch_batch(net, k_vc_smooth_res, "k_vc_smooth_res", nl, batch, nl, (const int32_t*)A.rp,
+                          (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], (const float*)net->s[l],
+                          net->x2[l]));
+    AFEM_TRY(sweep(net, &net->Pt[l], batch, net->x2[l], nullptr, nullptr, net->s[l + 1], net->n[l + 1]));
+  }
+  {
+    k_vc_coarse_adjoint<<<dim3(1, batch), kCoarseBlock, 0, ctx->stream>>>(coarse_plan(net), net->s[lo], net->w[lo]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "k_vc_coarse_adjoint", __FILE__, __LINE__);
+    ++ctx->launches;
+  }
+  for (int l = lo - 1; l >= 0; --l) {   // adjoint of the restriction, then of the pre-smoothing
+    const CsrLevel& A = net->Ac[l];
+    const int nl = net->n[l];
+    AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], nullptr, nullptr, net->vs[l], nl));
+    AFEM_TRY(launch_batch(net, k_vc_pre_adjoint, "k_vc_pre_adjoint", nl, batch, nl, (const int32_t*)A.rp,
+                          (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], (const float*)net->s[l],
+                          (const float*)net->x2[l], (const float*)net->vs[l], net->x1b[l],
+                          l == 0 ? (float*)nullptr : net->w[l]));
+  }
+  for (int l = 0; l < L; ++l) {
+    const int nl = net->n[l];
+    const bool last = l == L - 1;
+    AFEM_TRY(launch(ctx, k_dc_vcycle, grid_for(ctx, nl, 256, 8), 256, 0, nl, batch, (const float*)net->d[l],
+                    (const float*)net->base[l], (const float*)net->s[l], last ? (const float*)nullptr : net->u[l],
+                    last ? (const float*)nullptr : net->x1b[l], l == 0 ? net->t0 : (const float*)net->t[l],
+                    net->dc[l]));
+  }
   return AFEM_OK;
 }
 
@@ -834,12 +1086,10 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
     if (ce != cudaSuccess) return cuda_fail(ce, "k_energy", __FILE__, __LINE__);
     ctx->launches += 2;
   }
-  // adjoint down sweep s_{l+1} = P_l^T s_l ; dc_l = d_l sum_b t_l s_l ; heads
+  // adjoint V-cycle -> dL/dc_l per level ; heads
+  AFEM_TRY(apply_adjoint(net, batch));
   for (int l = 0; l < L; ++l) {
-    if (l + 1 < L) AFEM_TRY(sweep(net, &net->Pt[l], batch, net->s[l], nullptr, nullptr, net->s[l + 1], net->n[l + 1]));
     const int nl = net->n[l];
-    AFEM_TRY(launch(ctx, k_dc, grid_for(ctx, nl, 256, 8), 256, 0, nl, batch, l == 0 ? net->t0 : (const float*)net->t[l],
-                    (const float*)net->s[l], (const float*)net->d[l], net->dc[l]));
     const unsigned nbk = grid_for(ctx, nl, 256, 2);
     AFEM_TRY(ensure_part(net, (int64_t)nbk * (kF + 1)));
     AFEM_TRY(launch(ctx, k_head_backward, nbk, 256, 0, nl, (const float*)net->dc[l], (const bf16*)net->o[l],
@@ -901,7 +1151,8 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
                              const int32_t* const* restrT_cols, const float* const* restrT_w,
                              const int32_t* const* prol_rp, const int32_t* const* prol_cols,
                              const float* const* prol_w, const int32_t* const* prolT_rp,
-                             const int32_t* const* prolT_cols, const float* const* prolT_w, int max_batch,
+                             const int32_t* const* prolT_cols, const float* const* prolT_w,
+                             const int32_t* const* coarse_rp, const int32_t* const* coarse_cols, int max_batch,
                              afem_mpnn* out) {
   AFEM_CHECK_ARG(ctx && out && level_rows, "afem_mpnn_create: null argument");
   AFEM_CHECK_ARG(nb_levels >= 1 && nb_levels <= kMaxLevels, "afem_mpnn_create: 1..%d levels", kMaxLevels);
@@ -933,6 +1184,13 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
           (st = copy_csr(net, net->Pt[l], level_rows[l + 1], level_rows[l], prolT_rp[l], prolT_cols[l], prolT_w[l])))
         return cleanup(st);
     }
+    if (l > 0) {   // Galerkin pattern of A_l
+      if (!coarse_rp || !coarse_cols || !coarse_rp[l] || !coarse_cols[l])
+        return cleanup(fail(AFEM_ERR_BAD_ARG, "afem_mpnn_create: no coarse operator pattern for level %d", l));
+      if ((st = copy_csr(net, net->Ac[l], level_rows[l], level_rows[l], coarse_rp[l], coarse_cols[l], nullptr)) ||
+          (st = dalloc(net, (size_t)std::max<int64_t>(net->Ac[l].nnz, 1), &net->ac64[l])))
+        return cleanup(st);
+    }
   }
   net->n0 = level_rows[0];
   net->coarse_lo = nb_levels - 1;
@@ -944,11 +1202,11 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
       (st = dalloc(net, (size_t)net->nparam, &net->adam_m)) || (st = dalloc(net, (size_t)net->nparam, &net->adam_v)) ||
       (st = dalloc(net, (size_t)2 * nb_layers * kF * kF, &net->Wt)) ||
       (st = dalloc(net, (size_t)2 * nb_layers * kF * kF, &net->Wn)) || (st = dalloc(net, n0, &net->diag)) ||
-      (st = dalloc(net, n0, &net->diag32)) || (st = dalloc(net, n0, &net->ones)) ||
       (st = dalloc(net, n0 * 2, &net->x0)) || (st = dalloc(net, n0 * kF, &net->a_in)) ||
       (st = dalloc(net, n0 * kF, &net->Gb)) || (st = dalloc(net, n0 * kF, &net->ftmp)) ||
       (st = dalloc(net, B * 4, &net->sums)) || (st = dalloc(net, n0, &net->r32)) || (st = dalloc(net, n0, &net->z32)) ||
-      (st = dalloc(net, (size_t)std::max<int64_t>(net->S[0].nnz, 1), &net->a32)) || (st = dalloc(net, B * n0, &net->tmpB)))
+      (st = dalloc(net, (size_t)std::max<int64_t>(net->S[0].nnz, 1), &net->a32)) || (st = dalloc(net, B * n0, &net->tmpB)) ||
+      (st = dalloc(net, 1, &net->missing)))
     return cleanup(st);
   net->h[0] = net->a_in;
   for (int l = 0; l < nb_levels; ++l) {
@@ -962,7 +1220,9 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
     if ((st = dalloc(net, nl * kF, &net->dO[l])) ||
         (st = dalloc(net, nl, &net->base[l])) || (st = dalloc(net, nl, &net->d[l])) ||
         (st = dalloc(net, nl, &net->dc[l])) || (st = dalloc(net, B * nl, &net->t[l])) ||
-        (st = dalloc(net, B * nl, &net->w[l])) || (st = dalloc(net, B * nl, &net->s[l])))
+        (st = dalloc(net, B * nl, &net->w[l])) || (st = dalloc(net, B * nl, &net->s[l])) ||
+        (st = dalloc(net, B * nl, &net->vs[l])) || (st = dalloc(net, B * nl, &net->x2[l])) ||
+        (st = dalloc(net, B * nl, &net->u[l])) || (st = dalloc(net, B * nl, &net->x1b[l])))
       return cleanup(st);
   }
   cudaStream_t s = ctx->stream;
@@ -1011,7 +1271,7 @@ afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* rp, cons
                  nnz, (long long)net->S[0].nnz);
   afem_context ctx = net->ctx;
   cudaStream_t s = ctx->stream;
-  AFEM_TRY(launch(ctx, k_diag, grid_for(ctx, n, 256), 256, 0, n, rp, cols, vals, net->diag, net->diag32, net->ones));
+  AFEM_TRY(launch(ctx, k_diag, grid_for(ctx, n, 256), 256, 0, n, rp, cols, vals, net->diag));
   AFEM_TRY(launch(ctx, k_level0_weights, grid_for(ctx, n, 256), 256, 0, n, rp, cols, vals, (const double*)net->diag,
                   net->S[0].w));
   AFEM_TRY(launch(ctx, k_f64_to_f32, grid_for(ctx, nnz, 256), 256, 0, (int64_t)nnz, vals, net->a32));
@@ -1026,19 +1286,25 @@ afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* rp, cons
     for (int i = 0; i < n; ++i) acc += std::log(hd[i]);
     net->mean_log = acc / n;
   }
-  // base scalings: base_l = (R..R 1) / (R..R diag), base_0 = 1 / diag
-  AFEM_TRY(launch(ctx, k_ratio, grid_for(ctx, n, 256), 256, 0, n, (const float*)net->ones,
-                  (const float*)net->diag32, net->base[0]));
-  // numerator (restricted ones) in t[], denominator (restricted diag) in w[]
-  const float* num = net->ones;
-  const float* den = net->diag32;
-  for (int l = 0; l + 1 < net->L; ++l) {
-    AFEM_TRY(sweep(net, &net->R[l], 1, num, nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
-    AFEM_TRY(sweep(net, &net->R[l], 1, den, nullptr, nullptr, net->w[l + 1], net->n[l + 1]));
-    num = net->t[l + 1];
-    den = net->w[l + 1];
-    AFEM_TRY(launch(ctx, k_ratio, grid_for(ctx, net->n[l + 1], 256), 256, 0, net->n[l + 1], num, den,
-                    net->base[l + 1]));
+  // l1 caps and the Galerkin hierarchy A_{l+1} = P_l^T A_l P_l (FP64, FP32 copies)
+  net->Ac[0] = net->Aop;
+  AFEM_TRY(launch(ctx, k_l1cap, grid_for(ctx, n, 256), 256, 0, n, rp, vals, net->base[0]));
+  AFEM_CUDA(cudaMemsetAsync(net->missing, 0, sizeof(int), s));
+  for (int l = 1; l < net->L; ++l) {
+    const CsrLevel& Pt = net->Pt[l - 1];
+    const CsrLevel& P = net->P[l - 1];
+    const CsrLevel& Af = net->Ac[l - 1];
+    const double* af = l == 1 ? vals : net->ac64[l - 1];
+    AFEM_TRY(launch(ctx, k_rap, grid_for(ctx, net->n[l], 128), 128, 0, net->n[l], (const int32_t*)Pt.rp,
+                    (const int32_t*)Pt.cols, (const float*)Pt.w, (const int32_t*)Af.rp, (const int32_t*)Af.cols, af,
+                    (const int32_t*)P.rp, (const int32_t*)P.cols, (const float*)P.w, (const int32_t*)net->Ac[l].rp,
+                    (const int32_t*)net->Ac[l].cols, net->ac64[l], net->Ac[l].w, net->base[l], net->missing));
+  }
+  {
+    int missing = 0;
+    AFEM_CUDA(cudaMemcpyAsync(&missing, net->missing, sizeof(int), cudaMemcpyDeviceToHost, s));
+    AFEM_CUDA(cudaStreamSynchronize(s));
+    AFEM_CHECK_ARG(!missing, "afem_mpnn_set_operator: a coarse operator pattern misses entries of P^T A P");
   }
   net->have_operator = true;
   net->scalings_valid = false;
@@ -1090,13 +1356,13 @@ afem_status afem_mpnn_train_step(afem_mpnn net, int batch, const float* r_d, con
 // one) with M as the preconditioner.  FP64 vectors, matrix, dot products and
 // stop test; M runs in FP32 on r converted to FP32.  Scalars stay on the
 // device (last-block reductions in a fixed order, deterministic); one
-// iteration is 4 + (2 lo + 1) kernels (lo fine levels each way, one coarse
-// kernel), captured in a CUDA graph per chunk of
+// iteration is 4 + (4 lo + 1) kernels (two per fine level each way, one
+// coarse-levels kernel), captured in a CUDA graph per chunk of
 // iterations, and a device flag makes the remaining kernels of a chunk return
 // once converged.
 //   K1  q = A p ; <p, q>, <r, p>            -> alpha = <r, p> / <p, q>
 //   K2  x += alpha p ; r -= alpha q ; r32   -> <r, r>, stop test
-//   M   z32 = M r32 (down and up sweeps)
+//   M   z32 = M r32 (one V-cycle)
 //   K3  z = z32 ; <z, q>                    -> beta = -<z, q> / <p, q>
 //   K4  p = z + beta p
 
@@ -1384,7 +1650,7 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
   if (st == AFEM_OK)
     st = launch(ctx, k_fcg_widen, grid_vec, kSolveBlock, 0, n, (const float*)net->z32, w->z, (const double*)w->q,
                 w->p, 1, w->partials, w->st);
-  const int per_iteration = 4 + 2 * net->coarse_lo + 1;
+  const int per_iteration = 4 + 4 * net->coarse_lo + 1;
   FcgState hs{};
   while (st == AFEM_OK) {
     cudaError_t ce = cudaMemcpyAsync(ctx->pinned, w->st, sizeof(FcgState), cudaMemcpyDeviceToHost, ctx->stream);
@@ -1421,5 +1687,18 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
   if (hs.status == AFEM_ERR_NOT_CONVERGED)
     return fail(hs.status, "FCG did not reach the tolerance in %d iterations (relres %.3e)", hs.iter, rel);
   if (hs.status == AFEM_ERR_BREAKDOWN) return fail(hs.status, "FCG breakdown (<p, A p> <= 0 or non-finite)");
+  return AFEM_OK;
+}
+
+// Levels of at most `rows` rows run in the coarse-levels kernel (one block
+// per vector); the others one launch per V-cycle step.
+extern "C" afem_status afem_mpnn_set_coarse_rows(afem_mpnn net, int rows) {
+  AFEM_CHECK_ARG(net && rows >= 0, "afem_mpnn_set_coarse_rows: bad arguments");
+  net->coarse_lo = net->L - 1;
+  while (net->coarse_lo > 0 && net->n[net->coarse_lo - 1] <= rows) --net->coarse_lo;
+  if (net->fcg) {   // the captured FCG iteration depends on the split
+    delete net->fcg->graph;
+    net->fcg->graph = nullptr;
+  }
   return AFEM_OK;
 }

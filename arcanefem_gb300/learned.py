@@ -6,16 +6,17 @@ what they need on a structured triangle mesh of the unit square
 (``meshgen.unit_square_tri``, node id = i + j (n+1)):
 
 * the level hierarchy: vertex grids of (n/2^l + 1)^2 nodes, 8-neighbour
-  graphs (weights 1/8) on the coarse levels, full-weighting restriction and
-  bilinear prolongation vanishing on the Dirichlet boundary (the grid
-  boundary), all as CSR;
+  graphs (weights 1/8) on the coarse levels for the network, full-weighting
+  restriction of its features, the multigrid's bilinear prolongation
+  vanishing on the Dirichlet boundary (the grid boundary), and the sparsity
+  pattern of each Galerkin coarse operator P^T A P, all as CSR;
 * the variable-coefficient diffusion problem -div(k grad u) = f of the
   learned-preconditioner benchmark: k = exp(g), g a Gaussian random field
   (correlation length 0.05, variance 1, FFT on a 1024^2 periodic grid,
   bilinearly sampled at the cell centroids), f a sum of Gaussian bumps,
   u = 0 on the boundary;
 * training pairs (r, e) generated by the FEM solver itself: the errors
-  e_k = x* - x_k of restarted Jacobi CG iterates and their residuals A e_k.
+  e_k = x* - x_k of restarted solver iterates and their residuals A e_k.
 """
 from __future__ import annotations
 
@@ -93,7 +94,9 @@ def masked_prolongation(R: sp.csr_matrix, mf: int) -> sp.csr_matrix:
 
 
 class Hierarchy:
-    """Device CSR matrices of the level hierarchy (level 0 = the matrix graph)."""
+    """Device CSR matrices of the level hierarchy (level 0 = the matrix graph),
+    and the sparsity pattern of each Galerkin coarse operator (structure
+    only: the values are computed on the device from the matrix)."""
 
     def __init__(self, n: int, levels: int, row_ptr0: torch.Tensor, cols0: torch.Tensor, dirichlet: bool = True):
         assert n % (1 << (levels - 1)) == 0, "grid size must be divisible by 2^(levels-1)"
@@ -121,6 +124,17 @@ class Hierarchy:
             self.restrT.append(dcsr(R.T))
             self.prol.append(dcsr(P))
             self.prolT.append(dcsr(P.T))
+        rp0, c0 = row_ptr0.cpu().numpy(), cols0.cpu().numpy()
+        G = sp.csr_matrix((np.ones(c0.size), c0, rp0), shape=(self.rows[0], self.rows[0]))
+        self.coarse = [None]
+        for l in range(levels - 1):
+            P = sp.csr_matrix(abs(sp.csr_matrix((self.prol[l][2].cpu().numpy(), self.prol[l][1].cpu().numpy(),
+                                                 self.prol[l][0].cpu().numpy()),
+                                                shape=(self.rows[l], self.rows[l + 1]))))
+            G = sp.csr_matrix(P.T @ G @ P)
+            G.data[:] = 1.0
+            G.sort_indices()
+            self.coarse.append(dcsr(G))
 
 
 def param_count(layers: int, levels: int) -> int:
@@ -130,7 +144,7 @@ def param_count(layers: int, levels: int) -> int:
 
 def init_params(layers: int, levels: int, seed: int = 0, head_scale: float = 0.01) -> np.ndarray:
     """He-style hidden weights; heads near zero, so that the initial
-    preconditioner is multilevel diagonal scaling (c_l ~ 0)."""
+    preconditioner is the V-cycle with l1-Jacobi smoothing (c_l ~ 0)."""
     rng = np.random.default_rng(seed)
     parts = [rng.normal(0, 1.0, (2, F)), np.zeros(F)]
     for _ in range(layers):
@@ -161,6 +175,7 @@ class MPNN:
         args = [arr(hier.graph, 0), arr(hier.graph, 1), arr(hier.graph, 2)]
         for mats in (hier.restr, hier.restrT, hier.prol, hier.prolT):
             args += [arr(mats, 0), arr(mats, 1), arr(mats, 2)]
+        args += [arr(hier.coarse, 0), arr(hier.coarse, 1)]
         L_ = _capi.lib()
         L_.afem_mpnn_create.restype = C.c_int
         rc = L_.afem_mpnn_create(ctx.handle, C.c_int(L), C.c_int(layers), sizes, *args, C.c_int(max_batch),
@@ -185,6 +200,9 @@ class MPNN:
     def set_operator(self, row_ptr, cols, values):
         call("afem_mpnn_set_operator", self.handle, int(row_ptr.numel()) - 1, _ptr(row_ptr), _ptr(cols),
              _ptr(values))
+
+    def set_coarse_rows(self, rows: int):
+        call("afem_mpnn_set_coarse_rows", self.handle, int(rows))
 
     def scalings(self, level: int) -> torch.Tensor:
         d = torch.empty(self.hier.rows[level], dtype=torch.float32, device="cuda")
@@ -323,12 +341,26 @@ def cg_steps(prob: DiffusionProblem, b: torch.Tensor, x: torch.Tensor, iters: in
         _capi.check(rc, "afem_cg_solve_csr")
 
 
-def make_training_pairs(prob: DiffusionProblem, count: int, solves: int, every: int = 25, seed: int = 11):
+def fcg_steps(net: MPNN, prob: DiffusionProblem, b: torch.Tensor, x: torch.Tensor, iters: int) -> None:
+    """`iters` iterations of flexible CG preconditioned by the network, from
+    the current x (a restart)."""
+    info = _capi.SolveInfo()
+    opt = fem.solver_options(rtol=1e-300, max_iter=iters)
+    rc = _capi.lib().afem_fcg_solve(prob.ctx.handle, int(prob.row_ptr.numel()) - 1, _ptr(prob.row_ptr),
+                                    _ptr(prob.cols), _ptr(prob.values), _ptr(b), _ptr(x), net.handle,
+                                    C.byref(opt), C.byref(info))
+    if rc not in (0, _capi.NOT_CONVERGED):
+        _capi.check(rc, "afem_fcg_solve")
+
+
+def make_training_pairs(prob: DiffusionProblem, count: int, solves: int, every: int = 25, seed: int = 11,
+                        net: MPNN = None):
     """`count` (residual, error) pairs generated by the solver: for each of
-    `solves` bump right-hand sides b, the converged solution x* (CG to 1e-10)
-    and the iterates x_k of Jacobi CG restarted every `every` iterations from
-    x_0 = 0; the pair is (r_k = A e_k, e_k = x* - x_k), so early pairs carry
-    rough errors and late ones the smooth errors CG leaves behind."""
+    `solves` bump right-hand sides b, the converged solution x* (to 1e-10)
+    and the iterates x_k of a solver restarted every `every` iterations from
+    x_0 = 0 -- Jacobi CG, or flexible CG preconditioned by `net` when given;
+    the pair is (r_k = A e_k, e_k = x* - x_k), so early pairs carry the
+    initial errors and late ones the errors the solver is slow to remove."""
     rng = np.random.default_rng(seed)
     n = prob.mesh.nb_node
     R = torch.empty((count, n), dtype=torch.float32, device="cuda")
@@ -337,13 +369,20 @@ def make_training_pairs(prob: DiffusionProblem, count: int, solves: int, every: 
     s = 0
     while s < count:
         b = prob.rhs(rng)
-        xs, _ = prob.cg(b, rtol=1e-10)
+        if net is None:
+            xs, _ = prob.cg(b, rtol=1e-10)
+        else:
+            xs = torch.zeros_like(b)
+            net.fcg(prob.row_ptr, prob.cols, prob.values, b, xs, fem.solver_options(rtol=1e-10, max_iter=5000))
         x = torch.zeros_like(b)
         for k in range(per):
             if s >= count:
                 break
             if k:
-                cg_steps(prob, b, x, every)
+                if net is None:
+                    cg_steps(prob, b, x, every)
+                else:
+                    fcg_steps(net, prob, b, x, every)
             e = xs - x
             R[s] = prob.apply(e).float()
             E[s] = e.float()

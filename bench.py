@@ -18,7 +18,7 @@ loop of the reference.
 
 Two more sections ride on the same line (rank 0):
   learned  512^2 variable-coefficient diffusion: time to 1e-8 of plain FP64
-           CG against flexible CG with the learned multilevel preconditioner;
+           CG against flexible CG with the learned V-cycle preconditioner;
   batched  64 Poisson instances (N ~ U{64..512}) x 4 right-hand sides,
            assembled and solved to 1e-8 in one persistent launch.
 
@@ -443,7 +443,7 @@ def run_learned(args):
     """Variable-coefficient diffusion on a 512^2 triangle grid (k = exp(GRF),
     correlation 0.05, variance 1; bump source; u = 0 on the boundary): time to
     a 1e-8 FP64 relative residual of plain FP64 CG (Jacobi and none) against
-    flexible CG with the learned multilevel preconditioner (M in FP32, network
+    flexible CG with the learned V-cycle preconditioner (M in FP32, network
     BF16), trained on 2000 solver-generated pairs.  Device time per solve
     (CUDA events); training and pair generation reported separately."""
     import numpy as np
@@ -494,10 +494,11 @@ def run_learned(args):
         "problem": f"-div(k grad u) = f, {n}^2 quads x 2 triangles ({2 * n * n} tris), k = exp(GRF 0.05, var 1)",
         "target_relres": 1e-8,
         "plain_fp64_cg_jacobi": d(cg_jac), "plain_fp64_cg_none": d(cg_none),
-        "fcg_multilevel_untrained": d(untrained), "fcg_learned": d(kept),
+        "fcg_vcycle_untrained": d(untrained), "fcg_learned": d(kept),
         "speedup_vs_plain_fp64_cg_jacobi": cg_jac.solve_ms / kept.solve_ms,
         "speedup_vs_plain_fp64_cg_none": cg_none.solve_ms / kept.solve_ms,
-        "network": "6 message-passing layers, width 64, BF16 mma.sync GEMMs, FP32 accumulate; 9-level hierarchy",
+        "network": ("6 message-passing layers, width 64, BF16 mma.sync GEMMs, FP32 accumulate; predicts the "
+                    "per-node smoother weights of a V(1,1)-cycle on a 9-level Galerkin hierarchy"),
         "training": {"pairs": 2000, "pair_generation_s": pairs_s, "train_s": train_s, "loss": rep["loss"],
                      "fcg_iterations_untrained": rep["iterations_untrained"],
                      "fcg_iterations_trained": rep["iterations_trained"], "kept": rep["kept"]},

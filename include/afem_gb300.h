@@ -363,20 +363,25 @@ afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* row_ptr_d, con
 
 /* ---------------------------------------------------------------------- */
 /* Learned preconditioner.  No counterpart in the reference (it delegates to
- * HYPRE BoomerAMG / PETSc / Aleph): an additive multilevel preconditioner
- *   M r = sum_l Q_l diag(d_l) Q_l^T r,  Q_0 = I,  Q_{l+1} = Q_l P_l,
- * linear and symmetric positive definite in r, whose per-node level scalings
- *   d_l = base_l * exp(c_l),  base_l = (R..R 1) / (R..R diag A)
+ * HYPRE BoomerAMG / PETSc / Aleph): one symmetric V(1,1)-cycle of geometric
+ * multigrid on the Galerkin hierarchy A_{l+1} = P_l^T A_l P_l, with
+ * weighted-Jacobi smoothers whose per-node weights
+ *   d_l = cap_l * sigmoid(c_l + logit 0.8),  cap_l = 2 / sum_j |A_l,ij|
  * come from a message-passing network on the mesh graph (6 layers, width 64,
  * BF16 tensor-core GEMMs with FP32 accumulation), trained on the GPU with this
  * library's forward and backward kernels and applied inside flexible CG.
- * With c = 0 the preconditioner is multilevel diagonal scaling.
+ * The cap keeps the V-cycle symmetric positive definite for any network
+ * output; with c = 0 the smoother is l1-Jacobi at 0.8 of the cap.
  *
  * The caller provides the level hierarchy as device CSR matrices (FP32
  * weights): graph[l] (level l adjacency, symmetric; level 0 = the matrix
  * graph, its weights are set from A by afem_mpnn_set_operator and graph_w[0]
- * is ignored), restr[l] (level l -> l+1), prol[l] (level l+1 -> l) and their
- * transposes.  The pointer arrays are host arrays of device pointers. */
+ * is ignored), restr[l] (level l -> l+1, feature restriction), prol[l]
+ * (level l+1 -> l, the multigrid prolongation), their transposes, and the
+ * sparsity pattern of every coarse operator (coarse_rp[l], coarse_cols[l]
+ * for l >= 1; entry 0 is ignored) that must hold all entries of
+ * P_{l-1}^T A_{l-1} P_{l-1}.  The pointer arrays are host arrays of device
+ * pointers. */
 typedef struct afem_mpnn_s* afem_mpnn;
 
 afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, const int* level_rows_h,
@@ -387,7 +392,8 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
                              const float* const* restrT_w_h, const int32_t* const* prol_rp_h,
                              const int32_t* const* prol_cols_h, const float* const* prol_w_h,
                              const int32_t* const* prolT_rp_h, const int32_t* const* prolT_cols_h,
-                             const float* const* prolT_w_h, int max_batch, afem_mpnn* net);
+                             const float* const* prolT_w_h, const int32_t* const* coarse_rp_h,
+                             const int32_t* const* coarse_cols_h, int max_batch, afem_mpnn* net);
 afem_status afem_mpnn_destroy(afem_mpnn net);
 /* nb_layers (1..nb_levels) message-passing layers run on levels
  * 0..nb_layers-1; deeper levels take the restricted output of the last layer.
@@ -397,17 +403,24 @@ int afem_mpnn_param_count(afem_mpnn net);
 afem_status afem_mpnn_set_params(afem_mpnn net, const float* params_d);
 afem_status afem_mpnn_get_params(afem_mpnn net, float* params_d);
 /* Diagonal, level-0 edge weights -A_ij / sqrt(A_ii A_jj), coefficient
- * features and base scalings from the FP64 CSR operator (same graph as level
- * 0).  Synchronous (one host reduction of log diag A). */
+ * features, the Galerkin coarse operators and the smoother caps from the
+ * FP64 CSR operator (same graph as level 0).  Synchronous (one host
+ * reduction of log diag A); AFEM_ERR_BAD_ARG when a coarse pattern misses
+ * entries. */
 afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
                                    const double* values_d);
 /* z = M r for `batch` FP32 vectors stored one after the other. */
 afem_status afem_mpnn_forward(afem_mpnn net, int batch, const float* r_d, float* z_d);
-/* The level-l scalings d_l (level_rows[l] floats). */
+/* Levels of at most `rows` rows (default 2048) run their V-cycle steps in
+ * one block per vector with block barriers; larger levels one grid-wide
+ * launch per step. */
+afem_status afem_mpnn_set_coarse_rows(afem_mpnn net, int rows);
+/* The level-l smoother weights d_l (level_rows[l] floats). */
 afem_status afem_mpnn_scalings(afem_mpnn net, int level, float* d_d);
-/* Gradient of the mean relative squared error ||M r - e||^2 / ||e||^2 over
- * the batch (grad_d: param_count floats, nullable) and the loss (host,
- * nullable; non-null makes the call synchronous). */
+/* Gradient of the mean relative energy norm of the error propagation,
+ * ||e - M r||_A^2 / ||e||_A^2 over the batch of (r = A e, e) pairs (grad_d:
+ * param_count floats, nullable) and the loss (host, nullable; non-null makes
+ * the call synchronous). */
 afem_status afem_mpnn_gradients(afem_mpnn net, int batch, const float* r_d, const float* e_d, float* grad_d,
                                 double* loss_h);
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss. */

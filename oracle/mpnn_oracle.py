@@ -1,19 +1,30 @@
-"""CPU oracle of the learned preconditioner (network, multilevel application,
+"""CPU oracle of the learned preconditioner (network, multigrid V-cycle,
 loss and gradients).
 
 TEST INFRASTRUCTURE ONLY: the checker for the GPU kernels of afem_mpnn_*.
 The reference has no learned preconditioner (it hands the solve to HYPRE /
 PETSc / Aleph); this restates the preconditioner the library documents in
-include/afem_gb300.h:
+include/afem_gb300.h: one symmetric V(1,1)-cycle from a zero initial guess
+on the Galerkin hierarchy A_0 = A, A_{l+1} = P_l^T A_l P_l,
 
-    M r = sum_l Q_l diag(d_l) Q_l^T r,   Q_0 = I,  Q_{l+1} = Q_l P_l
-    d_l = base_l * exp(c_l),  base_l = (R..R 1) / (R..R diag A)
+    V_l(r):  x1 = d_l * r
+             s  = r - A_l x1
+             x2 = x1 + P_l V_{l+1}(P_l^T s)
+             u  = r - A_l x2
+             return x2 + d_l * u           (V_{L-1}(r) = d_{L-1} * r)
+
+with weighted-Jacobi smoothers whose per-node weights come from the network:
+    d_l = cap_l * sigmoid(c_l + logit(THETA)),  cap_l = 2 / sum_j |A_l,ij|
+    (0 on empty rows), so that 2 diag(d_l)^-1 - A_l is strictly diagonally
+    dominant and the V-cycle is symmetric positive definite for any c;
+    c = 0 is l1-Jacobi at THETA of the cap;
     c_l = o_l . w_l + beta_l  (o_l the level-l output of the message-passing
     network on the coefficient features x0 = [1, log A_ii - mean log A_ii])
 
 trained on the relative energy norm of the error propagation
 ||(I - M A) e||_A^2 / ||e||_A^2, with the gradient -2 A (e - M r) of a
-symmetric A (as the GPU computes it).
+symmetric A (as the GPU computes it); the backward pass is the adjoint of
+the V-cycle.
 
 Float64 numpy; with ``bf16_round=True`` the values the GPU keeps in BF16
 (the 64x64 weights, the activations a, m, o, h and the ReLU-masked
@@ -26,6 +37,7 @@ import numpy as np
 import scipy.sparse as sp
 
 F = 64
+THETA = 0.8          # untrained smoother weight, as a fraction of the l1-Jacobi cap
 
 
 def bf16(x):
@@ -76,11 +88,14 @@ class Net:
         self.L = len(self.S)
         self.NL = self.L if layers is None else min(layers, self.L)
         self.q = bf16 if bf16_round else (lambda x: np.asarray(x, np.float64))
-        num, den = np.ones_like(self.d), self.d.copy()
-        self.base = [1.0 / self.d]
+        # Galerkin hierarchy A_{l+1} = P_l^T A_l P_l and the smoother base weights
+        self.Al = [self.A]
         for l in range(self.L - 1):
-            num, den = self.R[l] @ num, self.R[l] @ den
-            self.base.append(np.where(den > 0, num / np.where(den > 0, den, 1.0), 0.0))
+            self.Al.append(sp.csr_matrix(self.P[l].T @ self.Al[-1] @ self.P[l]))
+        self.base = []          # the caps 2 / ||row||_1
+        for Al in self.Al:
+            l1 = np.asarray(abs(Al).sum(axis=1)).ravel()
+            self.base.append(np.where(l1 > 0, 2.0 / np.where(l1 > 0, l1, 1.0), 0.0))
         logd = np.log(self.d)
         self.x0 = np.stack([np.ones_like(logd), (logd - logd.mean()).astype(np.float32).astype(np.float64)], 1)
 
@@ -101,21 +116,53 @@ class Net:
                 o = h
             c["o"].append(o)
             w, beta = heads[l]
-            c["d"].append(self.base[l] * np.exp(np.clip(o @ w + beta, -20, 20)))
+            z = np.clip(o @ w + beta + np.log(THETA / (1 - THETA)), -30, 30)
+            c["d"].append(self.base[l] / (1 + np.exp(-z)))
             if l + 1 < self.L:
                 h = q(self.R[l] @ o)
                 c["h"].append(h)
         return c
 
     def apply(self, d, r):
-        """z = M r and the down sweep t_l = Q_l^T r."""
-        t = [r]
-        for l in range(self.L - 1):
-            t.append(self.P[l].T @ t[l])
-        w = d[-1] * t[-1]
-        for l in range(self.L - 2, -1, -1):
-            w = d[l] * t[l] + self.P[l] @ w
-        return w, t
+        """z = M r (one V(1,1)-cycle) and the per-level states (r_l, u_l) the
+        backward pass needs."""
+        L = self.L
+        st = [None] * L
+
+        def V(l, r):
+            if l == L - 1:
+                st[l] = (r, None)
+                return d[l] * r
+            A = self.Al[l]
+            x1 = d[l] * r
+            s = r - A @ x1
+            x2 = x1 + self.P[l] @ V(l + 1, self.P[l].T @ s)
+            u = r - A @ x2
+            st[l] = (r, u)
+            return x2 + d[l] * u
+
+        return V(0, r), st
+
+    def adjoint(self, d, st, g):
+        """dL/dd_l for dL/dz = g through the V-cycle with states st."""
+        L = self.L
+        dd = [np.zeros_like(x) for x in d]
+
+        def B(l, g):
+            r, u = st[l]
+            if l == L - 1:
+                dd[l] += g * r
+                return d[l] * g
+            A = self.Al[l]
+            dd[l] += g * u                       # post-smoothing weight
+            x2b = g - A @ (d[l] * g)
+            sb = self.P[l] @ B(l + 1, self.P[l].T @ x2b)
+            x1b = x2b - A @ sb
+            dd[l] += x1b * r                     # pre-smoothing weight
+            return d[l] * g + sb + d[l] * x1b
+
+        B(0, g)
+        return dd
 
     def forward(self, params, r):
         c = self.features(params)
@@ -138,20 +185,19 @@ class Net:
         return loss, self.backward(params, c, ts, seeds)
 
     def backward(self, params, c, ts, seeds):
-        """Parameter gradient from dL/dz_b (seeds) for z_b = M r_b with down sweeps ts."""
+        """Parameter gradient from dL/dz_b (seeds) for z_b = M r_b with V-cycle states ts."""
         q = self.q
         Win, bin_, layers, heads = unpack(params, self.NL, self.L)
         L = self.L
         dd = [np.zeros_like(x) for x in c["d"]]
         for t, s in zip(ts, seeds):
-            for l in range(L):
-                dd[l] += t[l] * s
-                if l + 1 < L:
-                    s = self.P[l].T @ s
+            for l, x in enumerate(self.adjoint(c["d"], t, s)):
+                dd[l] += x
         gheads = []
         dO = [None] * L
         for l in range(L):
-            dc = dd[l] * c["d"][l]
+            dl, cap = c["d"][l], self.base[l]
+            dc = dd[l] * dl * (1 - np.where(cap > 0, dl / np.where(cap > 0, cap, 1.0), 0.0))
             w, _ = heads[l]
             gheads.append((c["o"][l].T @ dc, dc.sum()))
             dO[l] = np.outer(dc, w)

@@ -24,13 +24,21 @@ def oracle_net(prob, hier, layers):
     return MO.Net(A, graphs, R, P, layers=layers, bf16_round=True)
 
 
-def test_zero_heads_give_multilevel_diagonal_scaling(cuda_ctx):
+def test_zero_heads_give_l1_jacobi_vcycle(cuda_ctx):
+    """Zero parameters: every smoother weight is 0.8 of its l1 cap (the caps
+    come from the Galerkin operators the library computes), and one
+    application is the plain V-cycle of the oracle."""
     prob, hier, net = learned.setup(cuda_ctx, n=32, levels=4, layers=2, seed=2, max_batch=1)
     net.set_params(np.zeros(net.nparam, np.float32))
     onet = oracle_net(prob, hier, 2)
     for l in range(hier.levels):
         d = net.scalings(l).cpu().numpy()
-        assert np.allclose(d, onet.base[l], rtol=1e-5, atol=0), l
+        assert np.allclose(d, MO.THETA * onet.base[l], rtol=1e-5, atol=0), l
+    e = torch.as_tensor(np.random.default_rng(4).standard_normal(prob.mesh.nb_node), device="cuda") * prob.interior
+    r = prob.apply(e).float().contiguous()
+    z = net.forward(r).cpu().numpy()
+    zo = onet.forward(np.zeros(net.nparam), r.cpu().numpy().astype(np.float64))
+    assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 1e-5
     net.close()
 
 
