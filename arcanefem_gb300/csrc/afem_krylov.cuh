@@ -149,6 +149,35 @@ inline afem_status launch_s(afem_context ctx, cudaStream_t s, Kernel k, unsigned
   return AFEM_OK;
 }
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl may
+// start while its predecessor in the stream is still running; it must call
+// pdl_wait() before touching anything the predecessor writes (the wait
+// returns once that grid has completed and its memory is visible).
+// pdl_trigger() lets the next such kernel begin launching early.  Both are
+// no-ops for a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+inline afem_status launch_pdl(afem_context ctx, cudaStream_t s, void (*k)(KArgs...), dim3 grid, unsigned block,
+                              Args... args) {
+  if (grid.x == 0) return AFEM_OK;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch (PDL)", __FILE__, __LINE__);
+  ++ctx->launches;
+  return AFEM_OK;
+}
+
 struct GraphChunk {
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;

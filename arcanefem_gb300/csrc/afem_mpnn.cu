@@ -337,6 +337,8 @@ __global__ void k_head(int n, const bf16* __restrict__ o, const float* __restric
 __global__ void k_sweep(int nrow, int ncol, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                         const float* __restrict__ w, const float* __restrict__ x, const float* __restrict__ d,
                         const float* __restrict__ t, float* __restrict__ y) {
+  pdl_trigger();
+  pdl_wait();
   const int64_t b = blockIdx.y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nrow; i += gridDim.x * blockDim.x) {
     float s = d ? d[i] * t[b * nrow + i] : 0.f;
@@ -409,6 +411,8 @@ __device__ __forceinline__ void vc_pre_adjoint(int i0, int st, int n, const int3
 __global__ void k_vc_smooth_res(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                                 const float* __restrict__ w, const float* __restrict__ d, const float* __restrict__ r,
                                 float* __restrict__ s) {
+  pdl_trigger();
+  pdl_wait();
   const int64_t o = (int64_t)blockIdx.y * n;
   vc_smooth_res(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, rp, cols, w, d, r + o, s + o);
 }
@@ -416,6 +420,8 @@ __global__ void k_vc_smooth_res(int n, const int32_t* __restrict__ rp, const int
 __global__ void k_vc_post(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                           const float* __restrict__ w, const float* __restrict__ d, const float* __restrict__ r,
                           const float* __restrict__ x2, float* __restrict__ u, float* __restrict__ y) {
+  pdl_trigger();
+  pdl_wait();
   const int64_t o = (int64_t)blockIdx.y * n;
   vc_post(blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, rp, cols, w, d, r + o, x2 + o,
           u ? u + o : nullptr, y + o);
@@ -452,6 +458,8 @@ struct CoarsePlan {
 // forward: x_lo = V_lo(r_lo), keeping t, u per level for the backward
 __global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse(CoarsePlan plan, const float* __restrict__ r_lo,
                                                             float* __restrict__ x_lo) {
+  pdl_trigger();
+  pdl_wait();
   const int64_t b = blockIdx.y;
   const int lo = plan.lo, L = plan.L, i0 = threadIdx.x, st = blockDim.x;
   for (int l = lo; l + 1 < L; ++l) {   // pre-smoothing residual, restriction
@@ -822,6 +830,7 @@ struct afem_mpnn_s {
   float* r32 = nullptr;                      // FCG staging [n0]
   float* z32 = nullptr;                      // FCG staging [n0]
   afem::FcgWork* fcg = nullptr;              // FCG buffers and graph (created on first solve)
+  bool pdl = false;                          // V-cycle kernels launched with programmatic dependent launch
   std::vector<void*> owned;
 };
 
@@ -895,6 +904,11 @@ static afem_status spmm(afem_mpnn net, const CsrLevel& S, const TIn* X, TOut* Y,
 static afem_status sweep(afem_mpnn net, const CsrLevel* M, int batch, const float* x, const float* dsc,
                          const float* tv, float* y, int nrow) {
   dim3 grid(grid_for(net->ctx, nrow, 256, 8), batch);
+  if (net->pdl)
+    return M ? launch_pdl(net->ctx, net->ctx->stream, k_sweep, grid, 256, M->nrow, M->ncol, M->rp, M->cols, M->w, x,
+                          dsc, tv, y)
+             : launch_pdl(net->ctx, net->ctx->stream, k_sweep, grid, 256, nrow, 0, nullptr, nullptr, nullptr,
+                          nullptr, dsc, tv, y);
   if (M)
     k_sweep<<<grid, 256, 0, net->ctx->stream>>>(M->nrow, M->ncol, M->rp, M->cols, M->w, x, dsc, tv, y);
   else
@@ -936,6 +950,7 @@ static afem_status features_forward(afem_mpnn net) {
 template <class Kernel, class... Args>
 static afem_status launch_batch(afem_mpnn net, Kernel k, const char* name, int nrow, int batch, Args... args) {
   dim3 grid(grid_for(net->ctx, nrow, 256, 8), batch);
+  if (net->pdl) return launch_pdl(net->ctx, net->ctx->stream, k, grid, 256, args...);
   k<<<grid, 256, 0, net->ctx->stream>>>(args...);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, name, __FILE__, __LINE__);
@@ -990,7 +1005,10 @@ static afem_status apply(afem_mpnn net, int batch, const float* r, float* z) {
     AFEM_TRY(sweep(net, &net->Pt[l], batch, net->vs[l], nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
   }
   float* x0 = z ? z : net->w[0];
-  {
+  if (net->pdl) {
+    AFEM_TRY(launch_pdl(net->ctx, net->ctx->stream, k_vc_coarse, dim3(1, batch), kCoarseBlock, coarse_plan(net),
+                        lo == 0 ? r : (const float*)net->t[lo], lo == 0 ? x0 : net->w[lo]));
+  } else {
     k_vc_coarse<<<dim3(1, batch), kCoarseBlock, 0, net->ctx->stream>>>(coarse_plan(net), lo == 0 ? r : net->t[lo],
                                                                       lo == 0 ? x0 : net->w[lo]);
     cudaError_t e = cudaGetLastError();
@@ -1430,6 +1448,8 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_spmv(int n, const int32_t* 
                                                           const double* __restrict__ vals, const double* __restrict__ p,
                                                           const double* __restrict__ r, double* __restrict__ q,
                                                           double* partials, FcgState* st) {
+  pdl_trigger();
+  pdl_wait();
   if (((volatile FcgState*)st)->done) return;
   __shared__ double sh[kSolveBlock / 32];
   const int lane = threadIdx.x & (G - 1);
@@ -1478,6 +1498,8 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_update(int n, double* __res
                                                             float* __restrict__ r32, const double* __restrict__ p,
                                                             const double* __restrict__ q, double* partials,
                                                             FcgState* st) {
+  pdl_trigger();
+  pdl_wait();
   if (((volatile FcgState*)st)->done) return;
   __shared__ double sh[kSolveBlock / 32];
   const double alpha = ((volatile FcgState*)st)->alpha;
@@ -1515,6 +1537,8 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_update(int n, double* __res
 __global__ void __launch_bounds__(kSolveBlock) k_fcg_widen(int n, const float* __restrict__ z32, double* __restrict__ z,
                                                            const double* __restrict__ q, double* __restrict__ p,
                                                            int first, double* partials, FcgState* st) {
+  pdl_trigger();
+  pdl_wait();
   if (((volatile FcgState*)st)->done) return;
   __shared__ double sh[kSolveBlock / 32];
   double zq = 0.0;
@@ -1541,6 +1565,8 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_widen(int n, const float* _
 
 __global__ void __launch_bounds__(kSolveBlock) k_fcg_dir(int n, const double* __restrict__ z, double* __restrict__ p,
                                                          const FcgState* st) {
+  pdl_trigger();
+  pdl_wait();
   if (((volatile const FcgState*)st)->done) return;
   const double beta = ((volatile const FcgState*)st)->beta;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
@@ -1583,7 +1609,9 @@ static afem_status apply_on(afem_mpnn net, cudaStream_t stream) {
   afem_context ctx = net->ctx;
   cudaStream_t saved = ctx->stream;
   ctx->stream = stream;
+  net->pdl = true;
   afem_status st = apply(net, 1, net->r32, net->z32);
+  net->pdl = false;
   ctx->stream = saved;
   return st;
 }
@@ -1619,16 +1647,16 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
     afem_status cst = capture(ctx, *w->graph, [&](cudaStream_t s) -> afem_status {
       for (int k = 0; k < chunk; ++k) {
         AFEM_TRY(dispatch_g(G, [&](auto g) {
-          return launch_s(ctx, s, k_fcg_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols, vals,
-                          (const double*)w->p, (const double*)w->r, w->q, w->partials, w->st);
+          return launch_pdl(ctx, s, k_fcg_spmv<decltype(g)::value>, dim3(grid_rows), kSolveBlock, n, rp, cols, vals,
+                            (const double*)w->p, (const double*)w->r, w->q, w->partials, w->st);
         }));
-        AFEM_TRY(launch_s(ctx, s, k_fcg_update, grid_vec, kSolveBlock, n, x, w->r, net->r32, (const double*)w->p,
-                          (const double*)w->q, w->partials, w->st));
+        AFEM_TRY(launch_pdl(ctx, s, k_fcg_update, dim3(grid_vec), kSolveBlock, n, x, w->r, net->r32,
+                            (const double*)w->p, (const double*)w->q, w->partials, w->st));
         AFEM_TRY(apply_on(net, s));
-        AFEM_TRY(launch_s(ctx, s, k_fcg_widen, grid_vec, kSolveBlock, n, (const float*)net->z32, w->z,
-                          (const double*)w->q, w->p, 0, w->partials, w->st));
-        AFEM_TRY(launch_s(ctx, s, k_fcg_dir, grid_vec, kSolveBlock, n, (const double*)w->z, w->p,
-                          (const FcgState*)w->st));
+        AFEM_TRY(launch_pdl(ctx, s, k_fcg_widen, dim3(grid_vec), kSolveBlock, n, (const float*)net->z32, w->z,
+                            (const double*)w->q, w->p, 0, w->partials, w->st));
+        AFEM_TRY(launch_pdl(ctx, s, k_fcg_dir, dim3(grid_vec), kSolveBlock, n, (const double*)w->z, w->p,
+                            (const FcgState*)w->st));
       }
       return AFEM_OK;
     });

@@ -14,13 +14,18 @@
 // block to finish (threadfence + ticket), so results are deterministic.
 // A device flag stops the remaining kernels of a chunk once converged.
 //
-// MIXED precision: FP64 iterative refinement (r = b - A x with FP64 values,
-// FP64 norms) around an FP32 CG (FP32 matrix values and vectors; dot products
-// in FP32 per thread and warp, FP64 across warps and blocks), restarted at
-// every refinement.  (Keeping the direction across refinements -- reliable
-// updates -- stalled: after a 1e-4 inner reduction the FP32 recursive
-// residual has drifted too far from the true one for the old direction to
-// stay conjugate.)
+// MIXED precision: FP32 CG (FP32 matrix values and vectors; dot products in
+// FP32 per thread and warp, FP64 across warps and blocks) with reliable
+// updates: each time the recursive residual has fallen by inner_rtol (default
+// 0.1) the FP32 correction is added to the FP64 solution, the residual is
+// replaced by the true FP64 residual b - A x, and the search direction is
+// KEPT (p = z + beta p with beta from the replaced residual), so the Krylov
+// recurrence is not restarted.  A refinement that does not halve the true
+// residual restarts the direction (p = z).  Each FP32 cycle can gain at most
+// ~1 / (eps32 kappa) before the FP32 operator error floors it, which is why
+// larger reductions per cycle are wasted; and with a kept direction the
+// drift between recursive and true residual must stay well below the
+// residual (a 1e-3 - 1e-4 reduction per cycle lost conjugacy and stalled).
 #include <algorithm>
 #include <cmath>
 
@@ -305,6 +310,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_update(int n, float* __rest
     double trr = reduce_partials(partials, gridDim.x, 2, 1, sh);
     if (threadIdx.x == 0) {
       st->beta = trz / st->rz;
+      st->pad0 = st->rz;   // <r, z> before this step, for a reliable update that keeps p
       st->rz = trz;
       st->rr = trr;
       st->iter += 1;
@@ -326,14 +332,17 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_dir(int n, const float* __r
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fmaf(beta, p[i], z[i]);
 }
 
-// Outer step of the refinement: r = b - A x (FP64), r32 = (float) r, x32 = 0,
-// z32 = D^-1 r32, p32 = z32 ; <r32, z32> and FP64 ||r||^2 ; inner state reset.
+// Reliable update: r = b - A x (FP64), r32 = (float) r, x32 = 0,
+// z32 = D^-1 r32 ; <r32, z32> and FP64 ||r||^2 ; inner state reset.  With
+// `restart` p32 = z32; otherwise beta = <r32, z32> / <r, z>_prev is left in
+// the inner state for k_ir_dir.
 template <int G>
 __global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
     int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols, const double* __restrict__ vals,
     const double* __restrict__ b, const double* __restrict__ x, const float* __restrict__ dinv32,
     const uint8_t* __restrict__ skip, float* __restrict__ r32, float* __restrict__ x32, float* __restrict__ z32,
-    float* __restrict__ p32, double* partials, CgState* outer, CgState* inner, double inner_rtol, int inner_max) {
+    float* __restrict__ p32, double* partials, CgState* outer, CgState* inner, double inner_rtol, int inner_max,
+    int restart) {
   __shared__ double sh[kSolveBlock / 32];
   const int lane = threadIdx.x & (G - 1);
   const int groups = gridDim.x * (blockDim.x / G);
@@ -354,7 +363,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
       r32[row] = rf;
       x32[row] = 0.f;
       z32[row] = zf;
-      p32[row] = zf;
+      if (restart) p32[row] = zf;
       rz += (double)rf * (double)zf;
       if (!(skip && skip[row])) {
         rr += ri * ri;
@@ -379,6 +388,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
       outer->bnorm2 = tbb;
       outer->done = (trr <= outer->tol2) ? 1 : 0;
       outer->ticket[0] = 0;
+      inner->beta = restart ? 0.0 : trz / inner->pad0;
       inner->rz = trz;
       inner->rr = trr;
       inner->tol2 = inner_rtol * inner_rtol * trr;
@@ -388,6 +398,12 @@ __global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
       inner->done = outer->done;
     }
   }
+}
+
+// p32 = z32 + beta p32 after a reliable update that keeps the direction
+__global__ void k_ir_dir(int n, const float* __restrict__ z, float* __restrict__ p, const CgState* inner) {
+  const float beta = (float)((volatile const CgState*)inner)->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fmaf(beta, p[i], z[i]);
 }
 
 __global__ void k_ir_correct(int n, double* __restrict__ x, const float* __restrict__ d) {
@@ -499,7 +515,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   AFEM_TRY(launch(ctx, k_inv_diag, grid_vec, kSolveBlock, 0, n, rp, cols, vals, (double*)nullptr, dinv32));
   if (opt.precond != AFEM_PRECOND_JACOBI)  // unpreconditioned inner solve: D^-1 = 1
     AFEM_TRY(launch(ctx, k_fill_f32, grid_for(ctx, n, 256), 256, 0, (int64_t)n, 1.0f, dinv32));
-  const double inner_rtol = opt.inner_rtol > 0 ? opt.inner_rtol : 1e-4;
+  const double inner_rtol = opt.inner_rtol > 0 ? opt.inner_rtol : 0.1;
   const int max_iter = opt.max_iter > 0 ? opt.max_iter : 1000;
   const int chunk = opt.check_every > 0 ? opt.check_every : 16;
   // outer tolerance: needs ||b||, computed by the first residual pass
@@ -518,17 +534,34 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   }));
   int total_inner = 0, outer_steps = 0;
   afem_status status = AFEM_OK;
-  const int max_outer = 100;
+  const int max_outer = 1000;
+  double rr_prev = 0.0;      // true ||r||^2 at the previous update
+  bool restart = true;
   for (;; ++outer_steps) {
     AFEM_TRY(dispatch_g(G64, [&](auto g) {
       return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows64, kSolveBlock, 0, n, rp, cols, vals, b,
                     (const double*)x, (const float*)dinv32, skip, r32, x32, z32, p32, partials, outer, inner,
-                    inner_rtol, max_iter);
+                    inner_rtol, max_iter, restart ? 1 : 0);
     }));
     CgState ho{};
     AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, outer, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
     AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
     ho = *reinterpret_cast<CgState*>(ctx->pinned);
+    if (!restart && !(ho.rr <= 0.25 * rr_prev)) {
+      // the true residual did not halve: redo this update with a fresh direction
+      restart = true;
+      AFEM_TRY(dispatch_g(G64, [&](auto g) {
+        return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows64, kSolveBlock, 0, n, rp, cols, vals, b,
+                      (const double*)x, (const float*)dinv32, skip, r32, x32, z32, p32, partials, outer, inner,
+                      inner_rtol, max_iter, 1);
+      }));
+      AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, outer, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+      AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+      ho = *reinterpret_cast<CgState*>(ctx->pinned);
+    }
+    if (!restart) AFEM_TRY(launch(ctx, k_ir_dir, grid_vec, 256, 0, n, (const float*)z32, p32, (const CgState*)inner));
+    rr_prev = ho.rr;
+    restart = false;
     if (outer_steps == 0) {
       // first pass: set the FP64 outer tolerance from ||b|| and re-test
       double tol2 = std::max(opt.rtol * opt.rtol * ho.bnorm2, opt.atol * opt.atol);
@@ -696,7 +729,7 @@ void afem_solver_options_default(afem_solver_options* o) {
   o->precond = AFEM_PRECOND_JACOBI;
   o->precision = AFEM_PRECISION_FP64;
   o->skip_forced_rows = 0;
-  o->inner_rtol = 1e-4;
+  o->inner_rtol = 0.0;   // library default: 0.1 (mixed CG), 1e-4 (batch)
   o->check_every = 16;
 }
 

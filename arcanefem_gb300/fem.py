@@ -244,7 +244,7 @@ class BSRFormat:
 
 
 def solver_options(rtol=1e-7, atol=0.0, max_iter=1000, precond=PRECOND_JACOBI, precision=PRECISION_FP64,
-                   skip_forced_rows=False, inner_rtol=1e-4, check_every=16) -> SolverOptions:
+                   skip_forced_rows=False, inner_rtol=0.0, check_every=16) -> SolverOptions:
     return SolverOptions(rtol, atol, max_iter, precond, precision, int(skip_forced_rows), inner_rtol, check_every)
 
 

@@ -78,6 +78,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-solve", action="store_true")
+    p.add_argument("--inner-rtol", type=float, default=0.1,
+                   help="mixed precision: FP32 CG residual reduction between reliable updates")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner section")
     p.add_argument("--no-batched", action="store_true", help="skip the batched-solve section")
     p.add_argument("--learned-n", type=int, default=512)
@@ -427,7 +429,7 @@ def run_solve(args, ctx, mesh, fmt):
         ls.apply_rhs_transformation()
         opt = fem.solver_options(rtol=w["rtol"], max_iter=20000,
                                  precision=fem.PRECISION_MIXED if prec == "mixed" else fem.PRECISION_FP64,
-                                 inner_rtol=1e-3)
+                                 inner_rtol=args.inner_rtol)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         info = ls.solve(opt)

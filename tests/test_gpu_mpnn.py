@@ -1,7 +1,7 @@
-"""Learned preconditioner on the GPU: scalings, forward and gradients against
-the CPU oracle, training reduces the loss, and what the trained network gains
-in flexible CG over the same multilevel form untrained and over Jacobi CG
-(the method without it)."""
+"""Learned preconditioner on the GPU: smoother weights, V-cycle forward and
+gradients against the CPU oracle, training reduces the loss on held-out
+pairs, and what the trained network gains in flexible CG over the same
+V-cycle untrained (the method without it) and over Jacobi CG."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -73,10 +73,23 @@ def test_forward_and_gradients_match_oracle(cuda_ctx, layers):
 def test_training_and_learned_fcg(cuda_ctx):
     prob, hier, net = learned.setup(cuda_ctx, n=128, levels=7, layers=6, seed=3, max_batch=16)
     R, E = learned.make_training_pairs(prob, count=384, solves=6, every=20, seed=4)
+    Rv, Ev = learned.make_training_pairs(prob, count=32, solves=2, every=20, seed=40)   # held out
+
+    def held_out_loss():
+        return np.mean([net.gradients(Rv[i:i + 16], Ev[i:i + 16])[1] for i in range(0, 32, 16)])
+
+    val_before = held_out_loss()
     b_val = prob.rhs(np.random.default_rng(98))
     rep = learned.train_validated(net, prob, R, E, b_val, epochs=8, batch=16, lr=2e-3)
     hist = rep["loss"]
     assert hist[-1] < 0.9 * hist[0], hist
+    val_after = held_out_loss()
+    print(f"held-out energy loss {val_before:.4f} -> {val_after:.4f}")
+    # what training gains over the same V-cycle untrained: a lower error-propagation
+    # energy on pairs it never saw, and no more FCG iterations
+    assert val_after < 0.9 * val_before, (val_before, val_after)
+    assert rep["iterations_trained"] <= rep["iterations_untrained"], rep
+    assert rep["kept"] == "trained"
     b = prob.rhs(np.random.default_rng(99))
     _, info_cg = prob.cg(b, rtol=1e-8)
     x = torch.zeros_like(b)
@@ -84,8 +97,8 @@ def test_training_and_learned_fcg(cuda_ctx):
     assert info.status == 0 and info.relres < 1e-8
     print(f"FCG untrained {rep['iterations_untrained']}, trained {rep['iterations_trained']} "
           f"(kept {rep['kept']}), test rhs {info.iterations}, Jacobi CG {info_cg.iterations}")
-    # what the learned preconditioner gains over the method without it (Jacobi CG)
-    assert info.iterations * 3 < info_cg.iterations, (info.iterations, info_cg.iterations)
+    # against plain Jacobi CG
+    assert info.iterations * 10 < info_cg.iterations, (info.iterations, info_cg.iterations)
     # the solver's judgement keeps the better parameter set
     xv = torch.zeros_like(b_val)
     kept = net.fcg(prob.row_ptr, prob.cols, prob.values, b_val, xv, fem.solver_options(rtol=1e-8, max_iter=2000))

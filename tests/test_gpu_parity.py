@@ -245,9 +245,10 @@ def test_cg_solution_matches_oracle(cuda_ctx, precision):
 
 
 def test_mixed_precision_iterations_stay_close_to_fp64(cuda_ctx):
-    """Mixed precision may restart its FP32 CG at each refinement but must not
-    stall: on a 128^2 Poisson problem to 1e-8 its total FP32 iterations stay
-    within 2.5x of the FP64 CG's."""
+    """Mixed precision keeps its FP32 CG direction across the reliable updates
+    (true FP64 residual every decade), so on a 128^2 Poisson problem to 1e-8
+    its FP32 iterations stay close to the FP64 CG's instead of growing with
+    every restart."""
     m = meshgen.unit_square_tri(128, seed=5)
     f = build_format(cuda_ctx, m)
     f.assemble_poisson()
@@ -265,10 +266,12 @@ def test_mixed_precision_iterations_stay_close_to_fp64(cuda_ctx):
         x = torch.zeros_like(b)
         info = fem.cg_solve_csr(cuda_ctx, rp, cols, vals, b, x,
                                 options=fem.solver_options(rtol=1e-8, max_iter=20000, precision=prec,
-                                                           inner_rtol=1e-3))
+                                                           inner_rtol=0.1))
         assert info.status == 0 and info.relres < 1e-8
-        its[prec] = info.iterations
-    assert its[fem.PRECISION_MIXED] <= 2.5 * its[fem.PRECISION_FP64], its
+        its[prec] = (info.iterations, info.refinements)
+    print("iterations (FP32 CG, reliable updates) vs FP64 CG", its)
+    assert its[fem.PRECISION_MIXED][1] >= 6, its         # one update per decade
+    assert its[fem.PRECISION_MIXED][0] <= 1.3 * its[fem.PRECISION_FP64][0], its
 
 
 def test_cg_penalty_with_skipped_forced_rows(cuda_ctx):
