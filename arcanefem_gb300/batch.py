@@ -125,7 +125,7 @@ class Batch:
     def rebalance(self, options=None, rounds: int = 3):
         """Feedback partitioning: weight each instance by its measured work
         (finish time x CTAs) and resize the teams; keep the fastest split."""
-        opt = options or fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000)
+        opt = options or fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000)
         res, best_ms = self.solve(opt)
         best_w = None
         for _ in range(rounds):
@@ -147,7 +147,7 @@ class Batch:
     def solve(self, options: _capi.SolverOptions | None = None):
         res = (BatchResult * len(self.sizes))()
         ms = C.c_float()
-        opt = options or fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000)
+        opt = options or fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000)
         call("afem_batch_solve", self.handle, C.byref(opt), res, C.byref(ms))
         return list(res), float(ms.value)
 
@@ -175,7 +175,7 @@ class Batch:
         arr = (BatchConfig * len(cands))(*[BatchConfig(*c) for c in cands])
         times = (C.c_float * len(cands))()
         best = C.c_int()
-        opt = options or fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000)
+        opt = options or fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000)
         call("afem_batch_autotune", self.handle, C.byref(opt), arr, len(cands), reps, times, C.byref(best))
         chosen = arr[best.value].as_dict()
         if rebalance:

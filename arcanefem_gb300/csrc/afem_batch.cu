@@ -24,10 +24,12 @@
 //    CsrDoFLinearSystemImpl does (femutils/CsrDoFLinearSystemImpl.cc:88-121,
 //    column_index > 0 test included), and builds the lumped source
 //    b_i = m_i f_k(x_i), f_k a sum of 8 Gaussian bumps;
-//  * phase B solves the 4 systems together: FP64 iterative refinement
-//    (r = b - A x with FP64 values and vectors) around a Jacobi-preconditioned
-//    FP32 CG on the FP32 copy of A; the 4 right-hand sides are interleaved
-//    (float4 per node), so each matrix entry is read once for all four.
+//  * phase B solves the 4 systems together: a Jacobi-preconditioned FP32 CG
+//    on the FP32 copy of A with reliable updates (every inner_rtol reduction
+//    the correction goes into the FP64 solution and the residual is replaced
+//    by the true r = b - A x, FP64 values and vectors, keeping the search
+//    direction); the 4 right-hand sides are interleaved (float4 per node), so
+//    each matrix entry is read once for all four.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -228,9 +230,9 @@ constexpr int kRowUnroll = 8;   // entries of a row loaded together in the FP32 
 
 // Per-CTA copy of the team's solver scalars (identical in every CTA of a team).
 struct SolveState {
-  double bnorm2[kBatchRhs], tol2[kBatchRhs], rr64[kBatchRhs], itol2[kBatchRhs], rz[kBatchRhs];
-  float alpha[kBatchRhs], beta[kBatchRhs];
-  int active[kBatchRhs];
+  double bnorm2[kBatchRhs], tol2[kBatchRhs], rr64[kBatchRhs], itol2[kBatchRhs], rz[kBatchRhs], rzprev[kBatchRhs];
+  float alpha[kBatchRhs], beta[kBatchRhs], zc[kBatchRhs];
+  int active[kBatchRhs], keep[kBatchRhs];
   int any, all_done;
 };
 
@@ -292,6 +294,10 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
             S.bnorm2[j] = tot[kBatchRhs + j];
             S.tol2[j] = fmax(prm.rtol * prm.rtol * S.bnorm2[j], prm.atol * prm.atol);
           }
+          // keep the direction when the last cycle at least halved the true
+          // residual and cycles are short enough for the FP32 recursive
+          // residual to stay close to the true one (inner_rtol >= 0.01)
+          S.keep[j] = outer > 0 && prm.inner_rtol >= 0.01 && tot[j] <= 0.25 * S.rr64[j];
           S.rr64[j] = tot[j];
           const int dn = !(tot[j] > S.tol2[j]);
           S.active[j] = !dn;
@@ -307,13 +313,17 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
       status = AFEM_ERR_NOT_CONVERGED;
       break;
     }
-    // inner solve A32 d = r32 from d = 0 for the unconverged right-hand sides.
-    // z = D^-1 r is never stored: the SpMV of iteration `it` forms the new
-    // direction p = D^-1 r + beta p_old of every entry it gathers (and writes
-    // its own row), so the direction update needs no pass and no barrier of
-    // its own; p is double-buffered (p_old is read while p is written).
-    // Every refinement restarts the FP32 CG (a kept direction loses
-    // conjugacy: the FP32 recursive residual drifts from the true one).
+    // FP32 CG on A32 d = r32 from d = 0 for the unconverged right-hand sides.
+    // z = D^-1 r is never stored: the SpMV of each iteration forms the new
+    // direction p = zc D^-1 r + beta p_old of every entry it gathers (and
+    // writes its own row), so the direction update needs no pass and no
+    // barrier of its own; p is double-buffered (p_old is read while p is
+    // written), with the parity of the running iteration count so that a
+    // direction survives from one cycle to the next.  A right-hand side that
+    // has reached its cycle tolerance keeps its direction (zc = 0, beta = 1).
+    // Reliable updates: the cycle's residual is the true FP64 one, and the
+    // direction is kept (beta = <r,z>_new / <r,z>_prev) unless the last cycle
+    // failed to halve the true residual.
     {
       float lrz[kBatchRhs] = {};
       const bool a0 = S.active[0], a1 = S.active[1], a2 = S.active[2], a3 = S.active[3];
@@ -323,7 +333,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
         const float4 rv = make_float4(a0 ? (float)rr[0] : 0.f, a1 ? (float)rr[1] : 0.f, a2 ? (float)rr[2] : 0.f,
                                       a3 ? (float)rr[3] : 0.f);
         I.r[row] = rv;
-        I.z[row] = make_float4(0.f, 0.f, 0.f, 0.f);   // p_old of the first iteration
+        if (outer == 0) I.z[row] = make_float4(0.f, 0.f, 0.f, 0.f);   // p_old of the first iteration
         I.d[row] = make_float4(0.f, 0.f, 0.f, 0.f);
         lrz[0] = fmaf(rv.x, di * rv.x, lrz[0]); lrz[1] = fmaf(rv.y, di * rv.y, lrz[1]);
         lrz[2] = fmaf(rv.z, di * rv.z, lrz[2]); lrz[3] = fmaf(rv.w, di * rv.w, lrz[3]);
@@ -332,18 +342,20 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
       if (!team_reduce<BLOCK, kBatchRhs>(lrz, trz, I, rank, 3, red, tres, &gen_sh, err, lim)) return;
       if (threadIdx.x == 0)
         for (int j = 0; j < kBatchRhs; ++j) {
-          S.beta[j] = 0.f;
+          S.beta[j] = S.keep[j] && S.active[j] ? (float)(trz[j] / S.rzprev[j]) : 0.f;
+          S.zc[j] = 1.f;
           S.rz[j] = trz[j];
         }
       __syncthreads();
     }
     for (int it = 0; it < prm.max_inner; ++it) {
-      float4* const pold = (it & 1) ? I.p : I.z;
-      float4* const pnew = (it & 1) ? I.z : I.p;
+      float4* const pold = (inner_total & 1) ? I.p : I.z;
+      float4* const pnew = (inner_total & 1) ? I.z : I.p;
       // p = D^-1 r + beta p_old (on the fly), q = A32 p ; <p, q>.  Thread per
       // row; the row's column and value loads are issued together, then its gathers.
       {
         const float b0 = S.beta[0], b1 = S.beta[1], b2 = S.beta[2], b3 = S.beta[3];
+        const float z0 = S.zc[0], z1 = S.zc[1], z2 = S.zc[2], z3 = S.zc[3];
         float lpq[kBatchRhs] = {};
         for (int row = tid; row < I.n; row += nthr) {
           const int32_t rb = I.rp[row], e = I.rp[row + 1];
@@ -360,8 +372,8 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
           for (int u = 0; u < kRowUnroll; ++u) {
             const float4 rv = I.r[c[u]], po = pold[c[u]];
             const float di = I.dinv[c[u]];
-            const float4 pv = make_float4(fmaf(b0, po.x, di * rv.x), fmaf(b1, po.y, di * rv.y),
-                                          fmaf(b2, po.z, di * rv.z), fmaf(b3, po.w, di * rv.w));
+            const float4 pv = make_float4(fmaf(b0, po.x, z0 * di * rv.x), fmaf(b1, po.y, z1 * di * rv.y),
+                                          fmaf(b2, po.z, z2 * di * rv.z), fmaf(b3, po.w, z3 * di * rv.w));
             s.x = fmaf(a[u], pv.x, s.x); s.y = fmaf(a[u], pv.y, s.y);
             s.z = fmaf(a[u], pv.z, s.z); s.w = fmaf(a[u], pv.w, s.w);
           }
@@ -370,14 +382,14 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
             const float av = I.vals32[k];
             const float4 rv = I.r[ck], po = pold[ck];
             const float di = I.dinv[ck];
-            const float4 pv = make_float4(fmaf(b0, po.x, di * rv.x), fmaf(b1, po.y, di * rv.y),
-                                          fmaf(b2, po.z, di * rv.z), fmaf(b3, po.w, di * rv.w));
+            const float4 pv = make_float4(fmaf(b0, po.x, z0 * di * rv.x), fmaf(b1, po.y, z1 * di * rv.y),
+                                          fmaf(b2, po.z, z2 * di * rv.z), fmaf(b3, po.w, z3 * di * rv.w));
             s.x = fmaf(av, pv.x, s.x); s.y = fmaf(av, pv.y, s.y); s.z = fmaf(av, pv.z, s.z); s.w = fmaf(av, pv.w, s.w);
           }
           const float4 rv = I.r[row], po = pold[row];
           const float di = I.dinv[row];
-          const float4 pr = make_float4(fmaf(b0, po.x, di * rv.x), fmaf(b1, po.y, di * rv.y),
-                                        fmaf(b2, po.z, di * rv.z), fmaf(b3, po.w, di * rv.w));
+          const float4 pr = make_float4(fmaf(b0, po.x, z0 * di * rv.x), fmaf(b1, po.y, z1 * di * rv.y),
+                                        fmaf(b2, po.z, z2 * di * rv.z), fmaf(b3, po.w, z3 * di * rv.w));
           pnew[row] = pr;
           I.q[row] = s;
           lpq[0] = fmaf(pr.x, s.x, lpq[0]); lpq[1] = fmaf(pr.y, s.y, lpq[1]);
@@ -422,10 +434,14 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchInst* 
           for (int j = 0; j < kBatchRhs; ++j) {
             if (S.active[j]) {
               S.beta[j] = (float)(trr[j] / S.rz[j]);
+              S.rzprev[j] = S.rz[j];
               S.rz[j] = trr[j];
               if (!(trr[kBatchRhs + j] > S.itol2[j])) S.active[j] = 0;
             }
-            if (!S.active[j]) S.beta[j] = 0.f;
+            if (!S.active[j]) {   // keep the direction for the next cycle
+              S.beta[j] = 1.f;
+              S.zc[j] = 0.f;
+            }
             any = any || S.active[j];
           }
           S.any = any;
@@ -599,7 +615,7 @@ static BatchParams batch_params(const afem_solver_options& opt) {
   BatchParams prm{};
   prm.rtol = opt.rtol;
   prm.atol = opt.atol;
-  prm.inner_rtol = opt.inner_rtol > 0 ? opt.inner_rtol : 1e-4;
+  prm.inner_rtol = opt.inner_rtol > 0 ? opt.inner_rtol : 0.1;
   prm.max_inner = opt.max_iter > 0 ? opt.max_iter : 1000;
   prm.max_outer = 30;
   prm.spin_limit = 20000000LL;   // ~2.5 s of 128 ns sleeps

@@ -21,10 +21,11 @@
 // replaced by the true FP64 residual b - A x, and the search direction is
 // KEPT (p = z + beta p with beta from the replaced residual), so the Krylov
 // recurrence is not restarted.  A refinement that does not halve the true
-// residual restarts the direction (p = z).  Each FP32 cycle can gain at most
-// ~1 / (eps32 kappa) before the FP32 operator error floors it, which is why
-// larger reductions per cycle are wasted; and with a kept direction the
-// drift between recursive and true residual must stay well below the
+// residual restarts the direction (p = z), and so does every refinement when
+// inner_rtol < 0.01 (plain restarted refinement).  Each FP32 cycle can gain
+// at most ~1 / (eps32 kappa) before the FP32 operator error floors it, which
+// is why larger reductions per cycle are wasted; and with a kept direction
+// the drift between recursive and true residual must stay well below the
 // residual (a 1e-3 - 1e-4 reduction per cycle lost conjugacy and stalled).
 #include <algorithm>
 #include <cmath>
@@ -547,7 +548,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, outer, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
     AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
     ho = *reinterpret_cast<CgState*>(ctx->pinned);
-    if (!restart && !(ho.rr <= 0.25 * rr_prev)) {
+    if (!restart && !(ho.rr <= 0.25 * rr_prev && inner_rtol >= 0.01)) {
       // the true residual did not halve: redo this update with a fresh direction
       restart = true;
       AFEM_TRY(dispatch_g(G64, [&](auto g) {
@@ -729,7 +730,7 @@ void afem_solver_options_default(afem_solver_options* o) {
   o->precond = AFEM_PRECOND_JACOBI;
   o->precision = AFEM_PRECISION_FP64;
   o->skip_forced_rows = 0;
-  o->inner_rtol = 0.0;   // library default: 0.1 (mixed CG), 1e-4 (batch)
+  o->inner_rtol = 0.0;   // library default: 0.1
   o->check_every = 16;
 }
 

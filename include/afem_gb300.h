@@ -329,8 +329,8 @@ typedef struct {
   int precond;            /* AFEM_PRECOND_* */
   int precision;          /* AFEM_PRECISION_*; MIXED = FP32 inner CG inside FP64 iterative refinement */
   int skip_forced_rows;   /* leave penalty (forced) rows out of both norms of the stop test */
-  double inner_rtol;      /* MIXED: FP32 residual reduction between reliable updates (<= 0: 0.1);
-                             batch: per FP64 refinement (<= 0: 1e-4) */
+  double inner_rtol;      /* MIXED and batch: FP32 residual reduction between reliable updates
+                             (<= 0: 0.1) */
   int check_every;        /* iterations between host convergence checks (default 16) */
 } afem_solver_options;
 

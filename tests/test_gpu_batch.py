@@ -57,7 +57,7 @@ def small_batch():
 def test_batch_assembly_rhs_and_solutions_match_oracle(small_batch):
     ctx, bt = small_batch
     rtol = 1e-10
-    res, ms = bt.solve(fem.solver_options(rtol=rtol, inner_rtol=1e-4, max_iter=20000))
+    res, ms = bt.solve(fem.solver_options(rtol=rtol, inner_rtol=0.1, max_iter=20000))
     assert ms > 0
     for i, n in enumerate(SIZES):
         rp, cols, v, b = oracle_instance(bt, i)
@@ -80,7 +80,7 @@ def test_batch_assembly_rhs_and_solutions_match_oracle(small_batch):
 
 def test_batch_is_deterministic_and_reusable(small_batch):
     ctx, bt = small_batch
-    opt = fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000)
+    opt = fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000)
     bt.solve(opt)
     x1 = [x.clone() for x in bt.x]
     res, _ = bt.solve(opt)
@@ -102,7 +102,7 @@ def test_team_partition_covers_the_grid(small_batch):
         order = np.argsort(SIZES)
         counts = [bt.team(int(i))[1] for i in order]
         assert counts == sorted(counts)
-        res, _ = bt.solve(fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000))
+        res, _ = bt.solve(fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000))
         assert all(r.status == 0 for r in res)
     bt.set_config(256, 1, 3.0)
 
@@ -147,5 +147,5 @@ def test_barrier_wait_runs_out_and_context_survives(small_batch):
     assert ncta >= 2
     status = bt.failure_test(cta0 + 1, spin_limit=200000)
     assert status == 5   # AFEM_ERR_TIMEOUT
-    res, _ = bt.solve(fem.solver_options(rtol=1e-8, inner_rtol=1e-4, max_iter=20000))
+    res, _ = bt.solve(fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000))
     assert all(r.status == 0 for r in res)
