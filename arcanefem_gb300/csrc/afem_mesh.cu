@@ -107,52 +107,55 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_nc_sort(int nb_node, in
 constexpr int kRowCap = 512;        // candidates per node (deg * npc), e.g. 128 tetrahedra
 constexpr int kMaxRowLen = 255;     // slot map entries are uint8
 
-// Stage the candidate nodes of node n (the nodes of its incident cells) in s.
-// Returns the candidate count, or -1 above kRowCap.
-__device__ __forceinline__ int stage_candidates(int n, int npc, const int32_t* __restrict__ cn,
-                                                const int32_t* __restrict__ nc_ptr,
-                                                const int32_t* __restrict__ nc_cell, int32_t* s) {
+// One warp per node.  The candidates (the nodes of the node's incident
+// cells, m = deg * npc of them) are held in registers, R per lane (candidate
+// i in lane i % 32, register i / 32), with, for the column pass, the slot-map
+// index of each: k * npc + q for candidate i = cell node j of incidence
+// k = i / npc, q = 0 for the row's own node (local index li) and q = 1.. for
+// the other cell nodes in increasing local index -- the order of the element
+// rows.  The distinct candidates come out in increasing order, one warp-wide
+// minimum per distinct value; the sweep that finds value t + 1 also writes
+// the slot bytes of value t, so each distinct value costs one sweep of R
+// registers.  Returns the row length; with `fill`, writes the columns
+// (ascending or self-last) at cols[0..len) and the slot map.
+template <int R, bool FILL>
+__device__ __forceinline__ int row_select(int n, int npc, int m, const int32_t* __restrict__ cn,
+                                          const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ local,
+                                          int len, int self_last, int32_t* __restrict__ cols,
+                                          uint8_t* __restrict__ slot) {
   const int lane = threadIdx.x & 31;
-  const int32_t b = nc_ptr[n];
-  const int m = (nc_ptr[n + 1] - b) * npc;
-  if (m > kRowCap) return -1;
-  for (int i = lane; i < m; i += 32) {
-    const int k = i / npc, j = i - k * npc;
-    s[i] = cn[(int64_t)nc_cell[b + k] * npc + j];
+  int32_t v[R];
+  int16_t si[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int i = r * 32 + lane;
+    v[r] = INT_MAX;
+    si[r] = 0;
+    if (i < m) {
+      const int k = i / npc, j = i - k * npc;
+      v[r] = __ldg(cn + (int64_t)__ldg(nc_cell + k) * npc + j);
+      if (FILL) {
+        const int li = __ldg(local + k);
+        si[r] = (int16_t)(k * npc + (j == li ? 0 : (j < li ? j + 1 : j)));
+      }
+    }
   }
-  __syncwarp();
-  return m;
-}
-
-// Distinct candidates in increasing order: returns the row length; when
-// `fill`, also writes the columns (ascending or self-last) at cols[0..len)
-// and the slot map.  Candidate i is cell node j = i % npc of incidence
-// k = i / npc; its slot byte goes to slot[k * npc + q] with q = 0 for the
-// row's own node (local index li = local[k]) and q = 1.. for the other cell
-// nodes in increasing local index -- the order of the element rows.
-__device__ __forceinline__ int extract_row(int n, const int32_t* s, int m, int npc, bool fill, int len,
-                                           int self_last, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
-                                           const uint8_t* __restrict__ local) {
-  const int lane = threadIdx.x & 31;
   int32_t last = INT_MIN;
-  int it = 0;
+  int pos_last = -1, it = 0;
   for (;;) {
     int32_t loc = INT_MAX;
-    for (int i = lane; i < m; i += 32) {
-      const int32_t v = s[i];
-      if (v > last && v < loc) loc = v;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (FILL && v[r] == last && pos_last >= 0) slot[si[r]] = (uint8_t)pos_last;
+      if (v[r] > last && v[r] < loc) loc = v[r];
     }
     const int32_t mn = __reduce_min_sync(0xffffffffu, loc);
     if (mn == INT_MAX) break;
-    if (fill) {
+    if (FILL) {
       const int pos = self_last ? (mn < n ? it : (mn == n ? len - 1 : it - 1)) : it;
-      if (lane == 0 && pos >= 0 && pos < len) cols[pos] = mn;   // a row_ptr that disagrees is reported, not written past
-      for (int i = lane; i < m; i += 32)
-        if (s[i] == mn) {
-          const int k = i / npc, j = i - k * npc, li = local[k];
-          const int q = j == li ? 0 : (j < li ? j + 1 : j);
-          slot[k * npc + q] = (uint8_t)pos;
-        }
+      // a row_ptr that disagrees is reported by the caller, not written past
+      pos_last = (pos >= 0 && pos < len) ? pos : -1;
+      if (lane == 0 && pos_last >= 0) cols[pos_last] = mn;
     }
     last = mn;
     ++it;
@@ -160,16 +163,29 @@ __device__ __forceinline__ int extract_row(int n, const int32_t* s, int m, int n
   return it;
 }
 
+template <bool FILL>
+__device__ __forceinline__ int row_dispatch(int n, int npc, int m, const int32_t* cn, const int32_t* nc_cell,
+                                            const uint8_t* local, int len, int self_last, int32_t* cols,
+                                            uint8_t* slot) {
+  if (m <= 32) return row_select<1, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
+  if (m <= 64) return row_select<2, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
+  if (m <= 128) return row_select<4, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
+  if (m <= 256) return row_select<8, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
+  return row_select<16, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
+}
+
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, int npc, const int32_t* __restrict__ cn,
                                                                  const int32_t* __restrict__ nc_ptr,
                                                                  const int32_t* __restrict__ nc_cell,
                                                                  int32_t* __restrict__ row_len,
                                                                  int* __restrict__ err) {
-  __shared__ int32_t sh[kWarpsPerBlock][kRowCap];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int n = blockIdx.x * kWarpsPerBlock + w; n < nb_node; n += gridDim.x * kWarpsPerBlock) {
-    const int m = stage_candidates(n, npc, cn, nc_ptr, nc_cell, sh[w]);
-    int len = m < 0 ? -1 : extract_row(n, sh[w], m, npc, false, 0, 0, nullptr, nullptr, nullptr);
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int n = wid; n < nb_node; n += nwarps) {
+    const int32_t b = __ldg(nc_ptr + n);
+    const int m = (__ldg(nc_ptr + n + 1) - b) * npc;
+    int len = m > kRowCap ? -1 : row_dispatch<false>(n, npc, m, cn, nc_cell + b, nullptr, 0, 0, nullptr, nullptr);
     if (lane == 0) {
       if (len < 0 || len > kMaxRowLen) {
         atomicOr(err, 2);
@@ -177,7 +193,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, in
       }
       row_len[n] = len;
     }
-    __syncwarp();
   }
 }
 
@@ -188,18 +203,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, i
                                                                   const int32_t* __restrict__ row_ptr, int self_last,
                                                                   int32_t* __restrict__ cols,
                                                                   uint8_t* __restrict__ slot, int* __restrict__ err) {
-  __shared__ int32_t sh[kWarpsPerBlock][kRowCap];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int n = blockIdx.x * kWarpsPerBlock + w; n < nb_node; n += gridDim.x * kWarpsPerBlock) {
-    const int32_t rb = row_ptr[n];
-    const int len = row_ptr[n + 1] - rb;
-    const int m = stage_candidates(n, npc, cn, nc_ptr, nc_cell, sh[w]);
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int n = wid; n < nb_node; n += nwarps) {
+    const int32_t rb = __ldg(row_ptr + n);
+    const int len = __ldg(row_ptr + n + 1) - rb;
+    const int32_t b = __ldg(nc_ptr + n);
+    const int m = (__ldg(nc_ptr + n + 1) - b) * npc;
     int got = -1;
-    if (m >= 0)
-      got = extract_row(n, sh[w], m, npc, true, len, self_last, cols + rb, slot + (int64_t)nc_ptr[n] * npc,
-                        nc_local + nc_ptr[n]);
+    if (m <= kRowCap)
+      got = row_dispatch<true>(n, npc, m, cn, nc_cell + b, nc_local + b, len, self_last, cols + rb,
+                               slot + (int64_t)b * npc);
     if (lane == 0 && got != len) atomicOr(err, 4);
-    __syncwarp();
   }
 }
 
