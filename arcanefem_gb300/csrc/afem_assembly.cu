@@ -251,14 +251,15 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int nb_
 // <= kScalarRmax) or directly into its own row of `values` (longer rows).
 
 template <int NPC>
-__global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int nb_node, const int32_t* __restrict__ nc_ptr,
+__global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int row0, int nb_node,
+                                                                const int32_t* __restrict__ nc_ptr,
                                                                 const uint8_t* __restrict__ nc_slot,
                                                                 const int32_t* __restrict__ row_ptr,
                                                                 const double* __restrict__ er,
                                                                 double* __restrict__ values) {
   __shared__ double acc[kScalarRmax * kGatherBlock];
   double* const my = acc + threadIdx.x;   // this thread's accumulators, stride kGatherBlock
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nb_node; row += gridDim.x * blockDim.x) {
+  for (int row = row0 + blockIdx.x * blockDim.x + threadIdx.x; row < nb_node; row += gridDim.x * blockDim.x) {
     const int32_t rb = __ldg(row_ptr + row);
     const int len = __ldg(row_ptr + row + 1) - rb;
     const int32_t p0 = __ldg(nc_ptr + row), p1 = __ldg(nc_ptr + row + 1);
@@ -301,7 +302,8 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int nb_node, con
 }
 
 // One thread per scalar row (node, component a) of the 3x3-block matrix.
-__global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int nb_node, const int32_t* __restrict__ nc_ptr,
+__global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int node0, int nb_node,
+                                                                    const int32_t* __restrict__ nc_ptr,
                                                                     const uint8_t* __restrict__ nc_slot,
                                                                     const int32_t* __restrict__ row_ptr,
                                                                     const double* __restrict__ er, int per_row_layout,
@@ -309,7 +311,8 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int nb_node,
   __shared__ double acc[3 * kElastRmaxB * kGatherBlock];
   double* const my = acc + threadIdx.x;
   const int64_t nrow = 3 * (int64_t)nb_node;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrow; r += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t r = 3 * (int64_t)node0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrow;
+       r += (int64_t)gridDim.x * blockDim.x) {
     const int node = (int)(r / 3), a = (int)(r - 3 * (int64_t)node);
     const int32_t rb = __ldg(row_ptr + node);
     const int len = __ldg(row_ptr + node + 1) - rb;
@@ -769,10 +772,64 @@ afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, co
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && ((uintptr_t)ke & 31) == 0, "afem_gather_poisson_p1: bad buffer");
   unsigned gg = (unsigned)((m->nb_node + kGatherBlock - 1) / kGatherBlock);
   if (m->dim == 3)
-    return launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+    return launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                   values_d);
-  return launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+  return launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                 values_d);
+}
+
+afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* m, int kind, const int32_t* row_ptr_d,
+                                const double* ke, int layout, double* values_d, double* values_h, int chunks) {
+  AFEM_CHECK_ARG(ctx, "afem_gather_to_host: null context");
+  AFEM_TRY(check_assembly(m, "afem_gather_to_host"));
+  AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
+                 "afem_gather_to_host: bad buffer");
+  AFEM_CHECK_ARG(chunks >= 1 && chunks <= 16, "afem_gather_to_host: chunks 1..16");
+  AFEM_CHECK_ARG(kind == AFEM_GATHER_POISSON_P1 || kind == AFEM_GATHER_POISSON_Q1 ||
+                     (kind == AFEM_GATHER_ELASTICITY_TET4 && m->dim == 3),
+                 "afem_gather_to_host: bad kind %d", kind);
+  AFEM_CHECK_ARG(kind != AFEM_GATHER_ELASTICITY_TET4 || layout == AFEM_LAYOUT_PER_BLOCK ||
+                     layout == AFEM_LAYOUT_PER_ROW,
+                 "afem_gather_to_host: bad layout %d", layout);
+  if (!ctx->copy_stream) AFEM_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  for (int k = 0; k <= chunks; ++k)
+    if (!ctx->chunk_ev[k]) AFEM_CUDA(cudaEventCreateWithFlags(&ctx->chunk_ev[k], cudaEventDisableTiming));
+  cudaStream_t s = ctx->stream, cs = ctx->copy_stream;
+  // chunk boundaries (nodes) and their value offsets; the copy stream waits for
+  // everything queued so far on the context stream (row_ptr may be fresh)
+  const int n = m->nb_node;
+  const int per = (n + chunks - 1) / chunks;
+  int32_t* hb = reinterpret_cast<int32_t*>(ctx->pinned);   // 256 bytes: up to 64 entries
+  AFEM_CUDA(cudaEventRecord(ctx->chunk_ev[0], s));
+  AFEM_CUDA(cudaStreamWaitEvent(cs, ctx->chunk_ev[0], 0));
+  for (int k = 0; k <= chunks; ++k)
+    AFEM_CUDA(cudaMemcpyAsync(hb + k, row_ptr_d + std::min(k * per, n), sizeof(int32_t), cudaMemcpyDeviceToHost, cs));
+  AFEM_CUDA(cudaStreamSynchronize(cs));
+  int64_t off[17];
+  for (int k = 0; k <= chunks; ++k) off[k] = hb[k];
+  const int64_t scale = kind == AFEM_GATHER_ELASTICITY_TET4 ? 9 : 1;   // values per block entry
+  const int npc = kind == AFEM_GATHER_POISSON_Q1 ? (1 << m->dim) : m->dim + 1;
+  for (int k = 0; k < chunks; ++k) {
+    const int n0 = std::min(k * per, n), n1 = std::min((k + 1) * per, n);
+    if (n1 <= n0) continue;
+    if (kind == AFEM_GATHER_ELASTICITY_TET4) {
+      const unsigned gg = (unsigned)((3 * (int64_t)(n1 - n0) + kGatherBlock - 1) / kGatherBlock);
+      AFEM_TRY(launch(ctx, k_gather_elasticity, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
+                      ke, (int)(layout == AFEM_LAYOUT_PER_ROW), values_d));
+    } else {
+      const unsigned gg = (unsigned)((n1 - n0 + kGatherBlock - 1) / kGatherBlock);
+      auto kern = npc == 8 ? k_gather_scalar<8> : npc == 4 ? k_gather_scalar<4> : k_gather_scalar<3>;
+      AFEM_TRY(launch(ctx, kern, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke, values_d));
+    }
+    AFEM_CUDA(cudaEventRecord(ctx->chunk_ev[k + 1], s));
+    AFEM_CUDA(cudaStreamWaitEvent(cs, ctx->chunk_ev[k + 1], 0));
+    const int64_t v0 = off[k] * scale, v1 = off[k + 1] * scale;
+    if (v1 > v0)
+      AFEM_CUDA(cudaMemcpyAsync(values_h + v0, values_d + v0, sizeof(double) * (size_t)(v1 - v0),
+                                cudaMemcpyDeviceToHost, cs));
+  }
+  AFEM_CUDA(cudaStreamSynchronize(cs));
+  return AFEM_OK;
 }
 
 afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_view* m, const double* cell_coeff_d,
@@ -795,9 +852,9 @@ afem_status afem_gather_poisson_q1(afem_context ctx, const afem_mesh_view* m, co
   AFEM_CHECK_ARG(m->nc_slot_d && row_ptr_d && ke && values_d, "afem_gather_poisson_q1: null buffer");
   unsigned gg = (unsigned)((m->nb_node + kGatherBlock - 1) / kGatherBlock);
   if (m->dim == 3)
-    return launch(ctx, k_gather_scalar<8>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+    return launch(ctx, k_gather_scalar<8>, gg, kGatherBlock, 0, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                   values_d);
-  return launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+  return launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                 values_d);
 }
 
@@ -847,7 +904,7 @@ afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* 
                  "afem_gather_elasticity_tet4: bad layout %d", layout);
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && ((uintptr_t)ke & 31) == 0, "afem_gather_elasticity_tet4: bad buffer");
   unsigned gg = (unsigned)((3 * (int64_t)m->nb_node + kGatherBlock - 1) / kGatherBlock);
-  return launch(ctx, k_gather_elasticity, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+  return launch(ctx, k_gather_elasticity, gg, kGatherBlock, 0, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                 (int)(layout == AFEM_LAYOUT_PER_ROW), values_d);
 }
 
@@ -1037,11 +1094,11 @@ extern "C" afem_status afem_assemble_poisson_p1_noalloc(void* cuda_stream, const
   if (m->dim == 3) {
     AFEM_TRY(launch_on(s, k_elem_poisson_tet, ge, 256, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                        cell_coeff_d, rows));
-    return launch_on(s, k_gather_scalar<4>, gg, kGatherBlock, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
+    return launch_on(s, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
                      (const double*)rows, values_d);
   }
   AFEM_TRY(launch_on(s, k_elem_poisson_tri, ge, 256, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                      cell_coeff_d, rows));
-  return launch_on(s, k_gather_scalar<3>, gg, kGatherBlock, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
+  return launch_on(s, k_gather_scalar<3>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
                    (const double*)rows, values_d);
 }

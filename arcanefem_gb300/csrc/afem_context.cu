@@ -165,6 +165,12 @@ afem_status afem_context_destroy(afem_context ctx) {
   cudaError_t e = cudaSuccess;
   if (ctx->scratch) e = cudaFreeAsync(ctx->scratch, ctx->stream);
   cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
+  for (cudaEvent_t ev : ctx->chunk_ev)
+    if (ev) cudaEventDestroy(ev);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   delete ctx;
   if (e != cudaSuccess) return cuda_fail(e, "afem_context_destroy", __FILE__, __LINE__);

@@ -55,6 +55,10 @@ struct afem_context_s {
   // pinned host staging for scalar read-backs
   void* pinned = nullptr;
   int64_t launches = 0;
+  // device -> host copies overlapped with kernels (afem_gather_to_host),
+  // created on first use
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t chunk_ev[17] = {};
 };
 
 namespace afem {

@@ -209,6 +209,22 @@ class BSRFormat:
             fn = "afem_gather_poisson_q1" if self.is_q1() else "afem_gather_poisson_p1"
             call(fn, self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), _ptr(ke), _ptr(self.values))
 
+    def gather_to_host(self, ke: torch.Tensor, values_h: torch.Tensor, chunks: int = 4):
+        """gather() with the values copied into the host tensor values_h
+        (pinned for overlap) range by range while the next range is gathered;
+        returns when values_h is complete."""
+        assert values_h.device.type == "cpu" and values_h.dtype == torch.float64
+        assert values_h.numel() == self.values.numel() and values_h.is_contiguous()
+        mv = self.mesh_view()
+        layout = 0
+        if self.nb_dof == 3:
+            kind = GATHER_ELASTICITY_TET4
+            layout = LAYOUT_PER_BLOCK if self.order_values_per_block else LAYOUT_PER_ROW
+        else:
+            kind = GATHER_POISSON_Q1 if self.is_q1() else GATHER_POISSON_P1
+        call("afem_gather_to_host", self.ctx.handle, C.byref(mv), kind, _ptr(self.row_ptr), _ptr(ke), layout,
+             _ptr(self.values), C.c_void_p(values_h.data_ptr()), int(chunks))
+
     def reset_matrix_values(self):
         self.values.zero_()
 
@@ -241,6 +257,9 @@ class BSRFormat:
         mv = self.mesh_view()
         call("afem_rhs_body_force_tet4", self.ctx.handle, C.byref(mv), float(f[0]), float(f[1]), float(f[2]),
              _ptr(rhs))
+
+
+GATHER_POISSON_P1, GATHER_POISSON_Q1, GATHER_ELASTICITY_TET4 = 0, 1, 2
 
 
 def solver_options(rtol=1e-7, atol=0.0, max_iter=1000, precond=PRECOND_JACOBI, precision=PRECISION_FP64,

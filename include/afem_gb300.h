@@ -191,6 +191,21 @@ afem_status afem_element_matrices_elasticity_tet4(afem_context ctx, const afem_m
 afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* mesh, const int32_t* row_ptr_d,
                                         const double* ke_d, int layout, double* values_d);
 
+/* Gather and copy back in one call: the node-wise gather runs in `chunks`
+ * (1..16) node ranges on the context stream, and each finished range of
+ * values_d goes to the host buffer values_h on a second stream while the next
+ * range is gathered (pinned values_h for a real overlap).  kind selects the
+ * gather of afem_gather_poisson_p1, afem_gather_poisson_q1 or
+ * afem_gather_elasticity_tet4 (layout used by the latter only).  Returns when
+ * values_h holds the whole matrix.  For callers that need the values on the
+ * host, as the reference's CPU-side linear systems do
+ * (femutils/CsrDoFLinearSystemImpl.cc, HypreDoFLinearSystem.cc:596-751). */
+#define AFEM_GATHER_POISSON_P1 0
+#define AFEM_GATHER_POISSON_Q1 1
+#define AFEM_GATHER_ELASTICITY_TET4 2
+afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* mesh, int kind, const int32_t* row_ptr_d,
+                                const double* ke_d, int layout, double* values_d, double* values_h, int chunks);
+
 /* Allocation-free assembly of the scalar Poisson P1 matrix.  No counterpart
  * in the reference: it serves callers that cannot let a library allocate
  * device memory (a host framework that owns all device allocations through

@@ -463,3 +463,25 @@ def test_msh_to_vtu_end_to_end(cuda_ctx, tmp_path):
     ls.apply_linear_system_transformation_and_solve(
         fem.solver_options(rtol=1e-10, max_iter=100000, skip_forced_rows=True))
     assert np.allclose(ls.solution_variable().cpu().numpy(), u, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("case", ["tri", "tet", "quad", "hex", "elast_block", "elast_row"])
+@pytest.mark.parametrize("chunks", [1, 3, 16])
+def test_gather_to_host_matches_device_gather(cuda_ctx, case, chunks):
+    """The chunked gather with overlapped copies back to a host buffer gives
+    exactly the values of the one-shot device gather."""
+    mesh = {"tri": lambda: meshgen.unit_square_tri(20, seed=1), "tet": lambda: meshgen.unit_cube_tet(7, seed=2),
+            "quad": lambda: meshgen.unit_square_quad(13, seed=3), "hex": lambda: meshgen.unit_cube_hex(5, seed=4),
+            "elast_block": lambda: meshgen.unit_cube_tet(5, seed=5),
+            "elast_row": lambda: meshgen.unit_cube_tet(5, seed=6)}[case]()
+    nb_dof = 3 if case.startswith("elast") else 1
+    f = build_format(cuda_ctx, mesh, nb_dof=nb_dof, use_csr=(case != "elast_block"))
+    ke = torch.empty(f.element_buffer_size(), dtype=torch.float64, device="cuda")
+    f.element_matrices(ke, lam=1.3, mu=0.7)
+    f.gather(ke)
+    ref = f.values.cpu().clone()
+    f.values.fill_(float("nan"))
+    host = torch.full((f.values.numel(),), float("nan"), dtype=torch.float64).pin_memory()
+    f.gather_to_host(ke, host, chunks=chunks)
+    assert torch.equal(host, ref)
+    assert torch.equal(f.values.cpu(), ref)
