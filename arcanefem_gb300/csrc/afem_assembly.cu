@@ -79,23 +79,33 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double v[4]) {
 // Element kernels (one thread per cell).
 
 // Poisson tetrahedron: 4 rows of 4 values, row i at er[inv[c][i] * 4] as
-// (K_ii, then K_ij for j != i increasing).
+// (K_ii, then K_ij for j != i increasing).  FP64 issue is the binding limit
+// on GB300, so the element is computed with few FP64 instructions (72 per
+// cell measured: 21 DADD, 28 DFMA, 23 DMUL): with the cofactor vectors
+// c_1..c_3 of the edges from node 0 (c_0 = -(c_1 + c_2 + c_3) is never
+// formed), the rows sum to zero, so K_0j = -(K_1j + K_2j + K_3j) and K_00 =
+// -(K_01 + K_02 + K_03) follow from the 3x3 block; 1 / (6 |det|) is the
+// correctly rounded reciprocal __drcp_rn (an FP32 seed with two FP64 Newton
+// steps issued more FP64-pipe work: its conversions run there too).
 __global__ void __launch_bounds__(256) k_elem_poisson_tet(int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
                                                           const int32_t* __restrict__ inv,
                                                           const double* __restrict__ coeff, double* __restrict__ er) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
-    d3 cf[4];
-    double s, vol;
-    tet_cofactors(xyz, cn, c, cf, &s, &vol);
+    const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
+    const d3 p0 = ld_node(xyz, q.x);
+    const d3 v1 = sub(ld_node(xyz, q.y), p0), v2 = sub(ld_node(xyz, q.z), p0), v3 = sub(ld_node(xyz, q.w), p0);
+    const d3 c1 = cross(v2, v3), c2 = cross(v3, v1), c3 = cross(v1, v2);
+    double s = __drcp_rn(6.0 * fabs(dot(v1, c1)));
     if (coeff) s *= __ldg(coeff + c);
-    const double k01 = s * dot(cf[0], cf[1]), k02 = s * dot(cf[0], cf[2]), k03 = s * dot(cf[0], cf[3]);
-    const double k12 = s * dot(cf[1], cf[2]), k13 = s * dot(cf[1], cf[3]), k23 = s * dot(cf[2], cf[3]);
+    const double k11 = s * dot(c1, c1), k22 = s * dot(c2, c2), k33 = s * dot(c3, c3);
+    const double k12 = s * dot(c1, c2), k13 = s * dot(c1, c3), k23 = s * dot(c2, c3);
+    const double k01 = -(k11 + k12 + k13), k02 = -(k12 + k22 + k23), k03 = -(k13 + k23 + k33);
     const int4 p = __ldg(reinterpret_cast<const int4*>(inv) + c);
     st4(er + 4 * (int64_t)p.x, -(k01 + k02 + k03), k01, k02, k03);
-    st4(er + 4 * (int64_t)p.y, -(k01 + k12 + k13), k01, k12, k13);
-    st4(er + 4 * (int64_t)p.z, -(k02 + k12 + k23), k02, k12, k23);
-    st4(er + 4 * (int64_t)p.w, -(k03 + k13 + k23), k03, k13, k23);
+    st4(er + 4 * (int64_t)p.y, k11, k01, k12, k13);
+    st4(er + 4 * (int64_t)p.z, k22, k02, k12, k23);
+    st4(er + 4 * (int64_t)p.w, k33, k03, k13, k23);
   }
 }
 

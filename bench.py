@@ -52,7 +52,7 @@ HBM_FALLBACK_GBS = 6800.0
 
 WORKLOADS = {
     "poisson3d": dict(dim=3, n=128, jitter=0.15, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 3D Poisson P1)",
-                      dp_elem=74, dp_gather=16, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
+                      dp_elem=72, dp_gather=16, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
     "elasticity3d": dict(dim=3, n=96, jitter=0.15, nb_dof=3,
                          metric="assembled nnz/s (node-wise 3x3 BSR, 3D linear elasticity P1)",
                          dp_elem=276, dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
