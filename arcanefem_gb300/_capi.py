@@ -38,7 +38,7 @@ class MeshView(C.Structure):
 class SolverOptions(C.Structure):
     _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("max_iter", C.c_int), ("precond", C.c_int),
                 ("precision", C.c_int), ("skip_forced_rows", C.c_int), ("inner_rtol", C.c_double),
-                ("check_every", C.c_int)]
+                ("check_every", C.c_int), ("block_size", C.c_int)]
 
 
 class SolveInfo(C.Structure):

@@ -281,6 +281,91 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv(int n, const int32_t* 
   }
 }
 
+// FP32 BSR SpMV of the mixed solver for a CSR whose scalar rows come in 3x3
+// blocks (the per-row layout of a 3-DoF BSR matrix, femutils/BSRFormat.h:
+// block row I = scalar rows 3I..3I+2 with one pattern, columns 3J..3J+2 per
+// block).  One thread per scalar row, as the scalar SpMV, but with ONE
+// column index per block (bcols, shared by the block row's three threads
+// through L1): 4 B/nnz of FP32 values + 4/3 B/nnz of indices instead of
+// 4 + 4.  The row's blocks are read in chunks of kB3Chunk (indices and
+// values first, then the gathers).  <p, q> -> alpha as k_cgf_spmv.
+constexpr int kB3Chunk = 3;
+
+__global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_b3(int n, const int32_t* __restrict__ rp,
+                                                             const int32_t* __restrict__ bcols,
+                                                             const float* __restrict__ vals,
+                                                             const float* __restrict__ p, float* __restrict__ q,
+                                                             double* partials, CgState* st) {
+  if (((volatile CgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  float pqf = 0.f;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+    const int I = row / 3;
+    const int32_t r0 = __ldg(rp + 3 * I);
+    const int32_t nbk = (__ldg(rp + 3 * I + 1) - r0) / 3;
+    const int32_t* bc = bcols + r0 / 9;
+    const float* v = vals + __ldg(rp + row);
+    float s = 0.f;
+    for (int32_t k = 0; k < nbk; k += kB3Chunk) {
+      int32_t j[kB3Chunk];
+      float a[3 * kB3Chunk];
+#pragma unroll
+      for (int u = 0; u < kB3Chunk; ++u) {
+        const bool in = k + u < nbk;
+        j[u] = in ? 3 * __ldg(bc + k + u) : 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a[3 * u + c] = in ? __ldg(v + 3 * (k + u) + c) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < kB3Chunk; ++u)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) s = fmaf(a[3 * u + c], __ldg(p + j[u] + c), s);
+    }
+    q[row] = s;
+    pqf = fmaf(p[row], s, pqf);
+  }
+  const double pq = block_sum_f(pqf, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = pq;
+  if (last_block(&st->ticket[1])) {
+    double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
+    if (threadIdx.x == 0) {
+      st->pq = t;
+      if (!(t > 0.0) || !isfinite(t)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+        st->alpha = 0.0;
+      } else {
+        st->alpha = st->rz / t;
+      }
+      st->ticket[1] = 0;
+    }
+  }
+}
+
+// Block columns of a 3x3-blocked CSR: bcols[rp[3I] / 9 + k] = J for the k-th
+// block of block row I; a pattern without that shape sets *bad.
+__global__ void k_block_cols3(int nb, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                              int32_t* __restrict__ bcols, int* __restrict__ bad) {
+  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nb; I += gridDim.x * blockDim.x) {
+    const int32_t r0 = rp[3 * I], len = rp[3 * I + 1] - r0;
+    if (len % 3 != 0 || r0 % 9 != 0 || rp[3 * I + 2] - rp[3 * I + 1] != len || rp[3 * I + 3] - rp[3 * I + 2] != len) {
+      atomicOr(bad, 1);
+      continue;
+    }
+    for (int32_t k = 0; k < len; k += 3) {
+      const int32_t c = cols[r0 + k];
+      bool ok = c % 3 == 0;
+      for (int a = 0; a < 3 && ok; ++a)
+        for (int b = 0; b < 3 && ok; ++b) ok = cols[r0 + a * len + k + b] == c + b;
+      if (!ok) {
+        atomicOr(bad, 1);
+        break;
+      }
+      bcols[r0 / 9 + k / 3] = c / 3;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kSolveBlock) k_cgf_update(int n, float* __restrict__ x, float* __restrict__ r,
                                                             float* __restrict__ z, const float* __restrict__ p,
                                                             const float* __restrict__ q,
@@ -490,12 +575,15 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
                      afem_solve_info* info) {
   const int G = lanes_per_row(n, nnz);          // FP32 inner SpMV
   const int G64 = lanes_per_row_fp64(n, nnz);   // FP64 outer residual
-  const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  const bool b3 = opt.block_size == 3;          // FP32 3x3-block SpMV
+  AFEM_CHECK_ARG(!b3 || n % 3 == 0, "block_size 3 needs a multiple of 3 rows (%d)", n);
+  const unsigned grid_rows = b3 ? grid_for(ctx, n, kSolveBlock, 8) : grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
   const unsigned grid_rows64 = grid_for(ctx, (int64_t)n * G64, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned nparts = std::max(std::max(grid_rows, grid_rows64), grid_vec);
   size_t need = align256(sizeof(float) * (size_t)nnz) + 6 * align256(sizeof(float) * (size_t)n) +
-                align256(sizeof(double) * 3 * nparts) + 2 * align256(sizeof(CgState));
+                align256(sizeof(double) * 3 * nparts) + 2 * align256(sizeof(CgState)) +
+                (b3 ? align256(sizeof(int32_t) * (size_t)(nnz / 9 + 1)) + 256 : 0);
   AFEM_TRY(scratch_reserve(ctx, need));
   float *v32, *r32, *z32, *p32, *q32, *x32, *dinv32;
   double* partials;
@@ -512,6 +600,17 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   AFEM_TRY(scratch_take(ctx, 1, &inner));
   AFEM_CUDA(cudaMemsetAsync(outer, 0, sizeof(CgState), ctx->stream));
   AFEM_CUDA(cudaMemsetAsync(inner, 0, sizeof(CgState), ctx->stream));
+  int32_t* bcols = nullptr;
+  if (b3) {
+    int* bad;
+    AFEM_TRY(scratch_take(ctx, (size_t)(nnz / 9 + 1), &bcols));
+    AFEM_TRY(scratch_take(ctx, 1, &bad));
+    AFEM_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+    AFEM_TRY(launch(ctx, k_block_cols3, grid_for(ctx, n / 3, 256), 256, 0, n / 3, rp, cols, bcols, bad));
+    int hbad = 0;
+    AFEM_TRY(read_scalar(ctx, bad, &hbad));
+    AFEM_CHECK_ARG(!hbad, "block_size 3: the CSR pattern is not made of 3x3 blocks");
+  }
   AFEM_TRY(launch(ctx, k_to_f32, grid_for(ctx, nnz, 256), 256, 0, nnz, vals, v32));
   AFEM_TRY(launch(ctx, k_inv_diag, grid_vec, kSolveBlock, 0, n, rp, cols, vals, (double*)nullptr, dinv32));
   if (opt.precond != AFEM_PRECOND_JACOBI)  // unpreconditioned inner solve: D^-1 = 1
@@ -523,10 +622,14 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   GraphChunk gc;
   AFEM_TRY(capture(ctx, gc, [&](cudaStream_t s) -> afem_status {
     for (int k = 0; k < chunk; ++k) {
-      AFEM_TRY(dispatch_g(G, [&](auto g) {
-        return launch_s(ctx, s, k_cgf_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols,
-                        (const float*)v32, (const float*)p32, q32, partials, inner);
-      }));
+      if (b3)
+        AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_b3, grid_rows, kSolveBlock, n, rp, (const int32_t*)bcols,
+                          (const float*)v32, (const float*)p32, q32, partials, inner));
+      else
+        AFEM_TRY(dispatch_g(G, [&](auto g) {
+          return launch_s(ctx, s, k_cgf_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols,
+                          (const float*)v32, (const float*)p32, q32, partials, inner);
+        }));
       AFEM_TRY(launch_s(ctx, s, k_cgf_update, grid_vec, kSolveBlock, n, x32, r32, z32, (const float*)p32,
                         (const float*)q32, (const float*)dinv32, skip, partials, inner));
       AFEM_TRY(launch_s(ctx, s, k_cgf_dir, grid_vec, kSolveBlock, n, (const float*)z32, p32, (const CgState*)inner));
@@ -732,6 +835,7 @@ void afem_solver_options_default(afem_solver_options* o) {
   o->skip_forced_rows = 0;
   o->inner_rtol = 0.0;   // library default: 0.1
   o->check_every = 16;
+  o->block_size = 0;
 }
 
 afem_status afem_cg_solve_csr(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,

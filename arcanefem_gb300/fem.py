@@ -246,6 +246,7 @@ class BSRFormat:
     def to_linear_system(self, ls: "DoFLinearSystem"):
         rp, cl, v = self.to_csr()
         ls.set_csr_values(rp, cl, v)
+        ls.block_size = self.nb_dof   # the scalar rows come in nb_dof x nb_dof blocks
         return rp, cl, v
 
     def rhs_constant_source(self, qdot: float, rhs: torch.Tensor):
@@ -263,8 +264,9 @@ GATHER_POISSON_P1, GATHER_POISSON_Q1, GATHER_ELASTICITY_TET4 = 0, 1, 2
 
 
 def solver_options(rtol=1e-7, atol=0.0, max_iter=1000, precond=PRECOND_JACOBI, precision=PRECISION_FP64,
-                   skip_forced_rows=False, inner_rtol=0.0, check_every=16) -> SolverOptions:
-    return SolverOptions(rtol, atol, max_iter, precond, precision, int(skip_forced_rows), inner_rtol, check_every)
+                   skip_forced_rows=False, inner_rtol=0.0, check_every=16, block_size=0) -> SolverOptions:
+    return SolverOptions(rtol, atol, max_iter, precond, precision, int(skip_forced_rows), inner_rtol, check_every,
+                         block_size)
 
 
 class DoFLinearSystem:
@@ -334,8 +336,13 @@ class DoFLinearSystem:
         call("afem_ls_apply_rhs_transformation", self.handle)
 
     def solve(self, options: SolverOptions | None = None) -> SolveInfo:
+        """Solve; a system filled from a 3-DoF BSRFormat passes its block size
+        to the mixed-precision solver (FP32 BSR SpMV) unless the options set one."""
         info = SolveInfo()
         opt = options or solver_options()
+        if opt.block_size == 0 and getattr(self, "block_size", 1) == 3:
+            opt = SolverOptions.from_buffer_copy(opt)
+            opt.block_size = 3
         call("afem_ls_solve", self.handle, C.byref(opt), C.byref(info))
         return info
 

@@ -347,6 +347,9 @@ typedef struct {
   double inner_rtol;      /* MIXED and batch: FP32 residual reduction between reliable updates
                              (<= 0: 0.1) */
   int check_every;        /* iterations between host convergence checks (default 16) */
+  int block_size;         /* MIXED: 3 = the CSR holds 3x3 blocks (the per-row layout of a 3-DoF
+                             BSR matrix): the FP32 SpMV then reads one column index per block
+                             (the FP32 BSR SpMV); 0 or 1: scalar rows */
 } afem_solver_options;
 
 typedef struct {
