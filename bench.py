@@ -55,14 +55,14 @@ WORKLOADS = {
                       dp_elem=72, dp_gather=16, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
     "elasticity3d": dict(dim=3, n=96, jitter=0.15, nb_dof=3,
                          metric="assembled nnz/s (node-wise 3x3 BSR, 3D linear elasticity P1)",
-                         dp_elem=276, dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
+                         dp_elem=277, dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
                          E=21e5, nu=0.28, body=(0.0, 0.0, -1.0)),
     "poisson2d": dict(dim=2, n=256, jitter=0.2, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 2D Poisson P1)",
-                      dp_elem=26, dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
+                      dp_elem=29, dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
     # Q1 widening: trilinear hexahedra (2x2x2 Gauss points), Q1 source, FP64 / mixed CG
     "poisson3d_hex": dict(dim=3, cell="hex", n=96, jitter=0.15, nb_dof=1,
                           metric="assembled nnz/s (node-wise CSR, 3D Poisson Q1 Hexa8)",
-                          dp_elem=3000, dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
+                          dp_elem=2888, dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
 }
 
 
@@ -471,8 +471,30 @@ def run_solve(args, ctx, mesh, fmt):
         wall = (time.perf_counter() - t0) * 1e3
         res[prec] = {"solve_ms": info.solve_ms, "wall_ms": wall, "iterations": info.iterations,
                      "refinements": info.refinements, "true_relres": info.relres, "status": info.status}
+        if prec == "fp64" and not args.no_cpu_baseline:
+            res["cpu_fp64_cg"] = cpu_solve_baseline(fmt, ls, info.iterations)
         ls.close()
     return res
+
+
+def cpu_solve_baseline(fmt, ls, gpu_iterations, cap=300):
+    """The oracle's Jacobi PCG (CPU restatement of the reference's diagonal-
+    preconditioned CG) on the same transformed system, all host cores, for at
+    most `cap` iterations; the time to the target is that rate times the GPU
+    solver's iteration count (the two run the same iteration)."""
+    from oracle import oracle as O
+
+    rp, cols, vals = (t.cpu().numpy() for t in fmt.to_csr())
+    b = ls.rhs_variable().cpu().numpy()
+    threads = O.max_threads()
+    iters = int(min(gpu_iterations, cap))
+    t0 = time.perf_counter()
+    _, it, rel = O.pcg_jacobi(rp, cols, vals, b, rtol=1e-300, max_iter=iters, nb_threads=threads)
+    dt = time.perf_counter() - t0
+    per_it = dt / max(it, 1)
+    return {"ms_per_iteration": per_it * 1e3, "iterations_sampled": it, "cores": threads, "kind": "port",
+            "estimated_solve_ms": per_it * gpu_iterations * 1e3,
+            "sample": f"{it} Jacobi-PCG iterations on the same system, {dt:.2f} s"}
 
 
 def run_learned(args):
