@@ -178,58 +178,78 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int nb_
     const int64_t c = base + threadIdx.x;
     double* my = stage[threadIdx.x];
     if (c < nb_cell) {
-      d3 cf[4];
-      double s, vol;
-      tet_cofactors(xyz, cn, c, cf, &s, &vol);
+      // cofactors c_1..c_3 of the edges from node 0 and s = 1 / (6 |det|);
+      // with G_n = s c_n the block of nodes (n, m) is
+      //   K_nm = lambda G_n G_m^T + mu G_m G_n^T + mu (G_n . G_m) I  (times 6 |det| s = 1 here)
+      // computed directly for 1 <= n <= m <= 3; the blocks of node 0 follow from the
+      // zero column sums (rigid translations): K_0m = -(K_1m + K_2m + K_3m), K_00 = -sum_m K_0m
+      const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
+      const d3 p0 = ld_node(xyz, q.x);
+      const d3 v1 = sub(ld_node(xyz, q.y), p0), v2 = sub(ld_node(xyz, q.z), p0), v3 = sub(ld_node(xyz, q.w), p0);
+      const d3 c1 = cross(v2, v3), c2 = cross(v3, v1), c3 = cross(v1, v2);
+      const double s = __drcp_rn(6.0 * fabs(dot(v1, c1)));
       const double ls = lambda * s, ms = mu * s, lms = (lambda + mu) * s;
       const int4 p4 = __ldg(reinterpret_cast<const int4*>(inv) + c);
       stage_p[threadIdx.x][0] = p4.x;
       stage_p[threadIdx.x][1] = p4.y;
       stage_p[threadIdx.x][2] = p4.z;
       stage_p[threadIdx.x][3] = p4.w;
-      double dg[4][6];
+      const double cv[3][3] = {{c1.x, c1.y, c1.z}, {c2.x, c2.y, c2.z}, {c3.x, c3.y, c3.z}};
+      // K0[m] accumulates K_0,m+1 = -(sum over n = 1..3 of K_n,m+1); it starts as -K_m+1,m+1
+      double K0[3][3][3];
 #pragma unroll
-      for (int n = 0; n < 4; ++n)
+      for (int n = 0; n < 3; ++n) {   // diagonal blocks of nodes 1..3: (lambda + mu) c c^T + mu |c|^2 I
+        double P[3][3];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) dg[n][k] = 0.0;
-      int pair = 0;
+        for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int n = 0; n < 4; ++n) {
+          for (int b = a; b < 3; ++b) P[a][b] = cv[n][a] * cv[n][b];
+        const double msS = ms * (P[0][0] + P[1][1] + P[2][2]);
+        int k = 0;
 #pragma unroll
-        for (int m = n + 1; m < 4; ++m) {
-          const double cn_[3] = {cf[n].x, cf[n].y, cf[n].z};
-          const double cm_[3] = {cf[m].x, cf[m].y, cf[m].z};
-          double P[3][3];
+        for (int a = 0; a < 3; ++a)
 #pragma unroll
-          for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b) P[a][b] = cn_[a] * cm_[b];
-          const double msS = ms * (P[0][0] + P[1][1] + P[2][2]);
-          double B[3][3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b)
-              B[a][b] = (a == b) ? fma(lms, P[a][a], msS) : fma(ls, P[a][b], ms * P[b][a]);
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b) my[pair * 9 + a * 3 + b] = B[a][b];
-          int k = 0;
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = a; b < 3; ++b, ++k) {
-              dg[n][k] -= B[a][b];
-              dg[m][k] -= B[b][a];
-            }
-          ++pair;
-        }
+          for (int b = a; b < 3; ++b, ++k) {
+            const double v = a == b ? fma(lms, P[a][a], msS) : lms * P[a][b];
+            my[54 + (n + 1) * 6 + k] = v;
+            K0[n][a][b] = -v;
+            K0[n][b][a] = -v;
+          }
       }
+      int pair = 3;
 #pragma unroll
-      for (int n = 0; n < 4; ++n)
+      for (int n = 0; n < 3; ++n)   // off-diagonal blocks of nodes 1..3, pairs (1,2) (1,3) (2,3)
 #pragma unroll
-        for (int k = 0; k < 6; ++k) my[54 + n * 6 + k] = dg[n][k];
+        for (int m = n + 1; m < 3; ++m, ++pair) {
+          double Q[3][3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Q[a][b] = cv[n][a] * cv[m][b];
+          const double mS = ms * (Q[0][0] + Q[1][1] + Q[2][2]);
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              const double v = (a == b) ? fma(lms, Q[a][a], mS) : fma(ls, Q[a][b], ms * Q[b][a]);
+              my[pair * 9 + a * 3 + b] = v;
+              K0[m][a][b] -= v;   // K_nm is in column block m
+              K0[n][b][a] -= v;   // K_mn = K_nm^T is in column block n
+            }
+        }
+#pragma unroll
+      for (int m = 0; m < 3; ++m)   // pairs (0,1) (0,2) (0,3)
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) my[m * 9 + a * 3 + b] = K0[m][a][b];
+      {
+        int k = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)   // K_00 = -(K_01 + K_02 + K_03), upper triangle
+#pragma unroll
+          for (int b = a; b < 3; ++b, ++k) my[54 + k] = -(K0[0][a][b] + K0[1][a][b] + K0[2][a][b]);
+      }
     }
     __syncwarp();
     const int64_t wfirst = base + wbase;

@@ -55,7 +55,7 @@ WORKLOADS = {
                       dp_elem=72, dp_gather=16, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
     "elasticity3d": dict(dim=3, n=96, jitter=0.15, nb_dof=3,
                          metric="assembled nnz/s (node-wise 3x3 BSR, 3D linear elasticity P1)",
-                         dp_elem=277, dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
+                         dp_elem=238, dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
                          E=21e5, nu=0.28, body=(0.0, 0.0, -1.0)),
     "poisson2d": dict(dim=2, n=256, jitter=0.2, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 2D Poisson P1)",
                       dp_elem=29, dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
