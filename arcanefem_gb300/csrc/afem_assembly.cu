@@ -87,11 +87,11 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double v[4]) {
 // -(K_01 + K_02 + K_03) follow from the 3x3 block; 1 / (6 |det|) is the
 // correctly rounded reciprocal __drcp_rn (an FP32 seed with two FP64 Newton
 // steps issued more FP64-pipe work: its conversions run there too).
-__global__ void __launch_bounds__(256) k_elem_poisson_tet(int nb_cell, const double* __restrict__ xyz,
+__global__ void __launch_bounds__(256) k_elem_poisson_tet(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
                                                           const int32_t* __restrict__ inv,
                                                           const double* __restrict__ coeff, double* __restrict__ er) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
     const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
     const d3 p0 = ld_node(xyz, q.x);
     const d3 v1 = sub(ld_node(xyz, q.y), p0), v2 = sub(ld_node(xyz, q.z), p0), v3 = sub(ld_node(xyz, q.w), p0);
@@ -110,11 +110,11 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tet(int nb_cell, const dou
 }
 
 // Poisson triangle: 3 rows of 3 values, row i at er[inv[c][i] * 3], diagonal first.
-__global__ void __launch_bounds__(256) k_elem_poisson_tri(int nb_cell, const double* __restrict__ xyz,
+__global__ void __launch_bounds__(256) k_elem_poisson_tri(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
                                                           const int32_t* __restrict__ inv,
                                                           const double* __restrict__ coeff, double* __restrict__ er) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
     const int32_t* q = cn + 3 * c;
     const double* a0 = xyz + 3 * (int64_t)__ldg(q);
     const double* a1 = xyz + 3 * (int64_t)__ldg(q + 1);
@@ -166,7 +166,7 @@ __device__ __forceinline__ int elast_packed(int i, int m, int a, int b) {
   return pair * 9 + (i < m ? a * 3 + b : b * 3 + a);
 }
 
-__global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int nb_cell, const double* __restrict__ xyz,
+__global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                                          const int32_t* __restrict__ cn,
                                                                          const int32_t* __restrict__ inv,
                                                                          double lambda, double mu,
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int nb_
   __shared__ double stage[kElastElemBlock][kElastPacked + 1];
   __shared__ int32_t stage_p[kElastElemBlock][4];
   const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < nb_cell; base += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t base = cell0 + blockIdx.x * (int64_t)blockDim.x; base < nb_cell; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = base + threadIdx.x;
     double* my = stage[threadIdx.x];
     if (c < nb_cell) {
@@ -272,6 +272,35 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int nb_
       }
     }
     __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined assembly (afem_assemble_to_host): the first node whose last
+// incident cell (the last entry of its ascending incidence list) is at or
+// after each cell bound, so that nodes [0, first[k]) are complete once the
+// cells below bound[k] are.  Warp minimum, one atomic per warp and bound.
+constexpr int kMaxAsmChunks = 16;
+struct CellBounds {
+  int32_t b[kMaxAsmChunks + 1];
+};
+
+__global__ void k_node_bounds(int nb_node, const int32_t* __restrict__ nc_ptr, const int32_t* __restrict__ nc_cell,
+                              int nbound, CellBounds cb, int32_t* __restrict__ first) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nr = ((int64_t)nb_node + stride - 1) / stride * stride;   // whole warps in every pass
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nr; n += stride) {
+    int32_t last = -1;
+    if (n < nb_node) {
+      const int32_t e = __ldg(nc_ptr + n + 1);
+      last = e > __ldg(nc_ptr + n) ? __ldg(nc_cell + e - 1) : -1;
+    }
+    for (int k = 0; k < nbound; ++k) {
+      const int32_t v = (n < nb_node && last >= cb.b[k]) ? (int32_t)n : INT_MAX;
+      const int32_t m = __reduce_min_sync(0xffffffffu, v);
+      if (lane == 0 && m != INT_MAX) atomicMin(first + k, m);
+    }
   }
 }
 
@@ -789,9 +818,9 @@ afem_status afem_element_matrices_poisson_p1(afem_context ctx, const afem_mesh_v
   AFEM_CHECK_ARG(ke && ((uintptr_t)ke & 31) == 0, "afem_element_matrices_poisson_p1: ke null or not 32-byte aligned");
   unsigned ge = grid_for(ctx, m->nb_cell, 256, 16);
   if (m->dim == 3)
-    return launch(ctx, k_elem_poisson_tet, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+    return launch(ctx, k_elem_poisson_tet, ge, 256, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                   cell_coeff_d, ke);
-  return launch(ctx, k_elem_poisson_tri, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+  return launch(ctx, k_elem_poisson_tri, ge, 256, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                 cell_coeff_d, ke);
 }
 
@@ -862,6 +891,92 @@ afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* m, int k
   return AFEM_OK;
 }
 
+afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int kind, const int32_t* row_ptr_d,
+                                  const double* cell_coeff_d, double lambda, double mu, int layout, double* ke,
+                                  double* values_d, double* values_h, int chunks) {
+  AFEM_CHECK_ARG(ctx, "afem_assemble_to_host: null context");
+  AFEM_TRY(check_assembly(m, "afem_assemble_to_host"));
+  AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
+                 "afem_assemble_to_host: bad buffer");
+  AFEM_CHECK_ARG(chunks >= 1 && chunks <= kMaxAsmChunks, "afem_assemble_to_host: chunks 1..%d", kMaxAsmChunks);
+  AFEM_CHECK_ARG(kind == AFEM_GATHER_POISSON_P1 || (kind == AFEM_GATHER_ELASTICITY_TET4 && m->dim == 3),
+                 "afem_assemble_to_host: kind must be AFEM_GATHER_POISSON_P1 or AFEM_GATHER_ELASTICITY_TET4");
+  AFEM_CHECK_ARG(kind != AFEM_GATHER_ELASTICITY_TET4 || layout == AFEM_LAYOUT_PER_BLOCK ||
+                     layout == AFEM_LAYOUT_PER_ROW,
+                 "afem_assemble_to_host: bad layout %d", layout);
+  AFEM_CHECK_ARG(m->nc_ptr_d && m->nc_cell_d, "afem_assemble_to_host: null node->cell lists");
+  if (!ctx->copy_stream) AFEM_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  for (int k = 0; k <= chunks; ++k)
+    if (!ctx->chunk_ev[k]) AFEM_CUDA(cudaEventCreateWithFlags(&ctx->chunk_ev[k], cudaEventDisableTiming));
+  cudaStream_t s = ctx->stream, cs = ctx->copy_stream;
+  const int nc = m->nb_cell, nn = m->nb_node;
+  // cell chunks and the node prefixes they complete
+  CellBounds cb{};
+  int64_t cbound[kMaxAsmChunks + 1];
+  for (int k = 0; k <= chunks; ++k) cbound[k] = (int64_t)nc * k / chunks;
+  for (int k = 1; k < chunks; ++k) cb.b[k - 1] = (int32_t)cbound[k];
+  AFEM_TRY(scratch_reserve(ctx, 512));
+  int32_t* first;
+  AFEM_TRY(scratch_take(ctx, kMaxAsmChunks + 1, &first));
+  int32_t* hb = reinterpret_cast<int32_t*>(ctx->pinned);   // 64 ints: node bounds, then their row starts
+  int32_t nb[kMaxAsmChunks + 1];
+  nb[0] = 0;
+  nb[chunks] = nn;
+  if (chunks > 1) {
+    AFEM_CUDA(cudaMemsetAsync(first, 0x7f, sizeof(int32_t) * (chunks - 1), s));
+    AFEM_TRY(launch(ctx, k_node_bounds, grid_for(ctx, nn, 256), 256, 0, nn, m->nc_ptr_d, m->nc_cell_d, chunks - 1, cb,
+                    first));
+    AFEM_CUDA(cudaMemcpyAsync(hb, first, sizeof(int32_t) * (chunks - 1), cudaMemcpyDeviceToHost, s));
+    AFEM_CUDA(cudaStreamSynchronize(s));
+    for (int k = 1; k < chunks; ++k) nb[k] = std::min(std::max(hb[k - 1], nb[k - 1]), nn);   // monotone
+  }
+  for (int k = 0; k <= chunks; ++k)
+    AFEM_CUDA(cudaMemcpyAsync(hb + 32 + k, row_ptr_d + nb[k], sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  AFEM_CUDA(cudaStreamSynchronize(s));
+  int64_t off[kMaxAsmChunks + 1];
+  const int64_t scale = kind == AFEM_GATHER_ELASTICITY_TET4 ? 9 : 1;
+  for (int k = 0; k <= chunks; ++k) off[k] = (int64_t)hb[32 + k] * scale;
+  const int per_row = kind == AFEM_GATHER_ELASTICITY_TET4 ? 3 : 1;
+  for (int k = 0; k < chunks; ++k) {
+    const int c0 = (int)cbound[k], c1 = (int)cbound[k + 1];
+    if (c1 > c0) {
+      if (kind == AFEM_GATHER_ELASTICITY_TET4) {
+        AFEM_TRY(launch(ctx, k_elem_elasticity_tet, grid_for(ctx, c1 - c0, kElastElemBlock, 32), kElastElemBlock, 0,
+                        c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke));
+      } else {
+        const unsigned ge = grid_for(ctx, c1 - c0, 256, 16);
+        if (m->dim == 3)
+          AFEM_TRY(launch(ctx, k_elem_poisson_tet, ge, 256, 0, c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                          cell_coeff_d, ke));
+        else
+          AFEM_TRY(launch(ctx, k_elem_poisson_tri, ge, 256, 0, c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+                          cell_coeff_d, ke));
+      }
+    }
+    const int n0 = nb[k], n1 = nb[k + 1];
+    if (n1 > n0) {
+      const unsigned gg = (unsigned)(((int64_t)(n1 - n0) * per_row + kGatherBlock - 1) / kGatherBlock);
+      if (kind == AFEM_GATHER_ELASTICITY_TET4)
+        AFEM_TRY(launch(ctx, k_gather_elasticity, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                        (int)(layout == AFEM_LAYOUT_PER_ROW), values_d));
+      else if (m->dim == 3)
+        AFEM_TRY(launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                        values_d));
+      else
+        AFEM_TRY(launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
+                        values_d));
+      AFEM_CUDA(cudaEventRecord(ctx->chunk_ev[k + 1], s));
+      AFEM_CUDA(cudaStreamWaitEvent(cs, ctx->chunk_ev[k + 1], 0));
+      if (off[k + 1] > off[k])
+        AFEM_CUDA(cudaMemcpyAsync(values_h + off[k], values_d + off[k], sizeof(double) * (size_t)(off[k + 1] - off[k]),
+                                  cudaMemcpyDeviceToHost, cs));
+    }
+  }
+  AFEM_CUDA(cudaStreamSynchronize(cs));
+  AFEM_CUDA(cudaStreamSynchronize(s));
+  return AFEM_OK;
+}
+
 afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_view* m, const double* cell_coeff_d,
                                              double* ke) {
   AFEM_CHECK_ARG(ctx, "afem_element_matrices_poisson_q1: null context");
@@ -920,7 +1035,7 @@ afem_status afem_element_matrices_elasticity_tet4(afem_context ctx, const afem_m
   AFEM_TRY(check_assembly(m, "afem_element_matrices_elasticity_tet4"));
   AFEM_CHECK_ARG(m->dim == 3, "afem_element_matrices_elasticity_tet4: tetrahedra only (dim 3)");
   AFEM_CHECK_ARG(ke && ((uintptr_t)ke & 31) == 0, "afem_element_matrices_elasticity_tet4: ke null or misaligned");
-  return launch(ctx, k_elem_elasticity_tet, grid_for(ctx, m->nb_cell, kElastElemBlock, 32), kElastElemBlock, 0,
+  return launch(ctx, k_elem_elasticity_tet, grid_for(ctx, m->nb_cell, kElastElemBlock, 32), kElastElemBlock, 0, 0,
                 m->nb_cell, m->coords_d,
                 m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke);
 }
@@ -1122,12 +1237,12 @@ extern "C" afem_status afem_assemble_poisson_p1_noalloc(void* cuda_stream, const
   const unsigned ge = (unsigned)std::max<int64_t>(1, std::min<int64_t>(eblocks, (int64_t)sms * 16));
   const unsigned gg = (unsigned)((m->nb_node + kGatherBlock - 1) / kGatherBlock);
   if (m->dim == 3) {
-    AFEM_TRY(launch_on(s, k_elem_poisson_tet, ge, 256, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+    AFEM_TRY(launch_on(s, k_elem_poisson_tet, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                        cell_coeff_d, rows));
     return launch_on(s, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
                      (const double*)rows, values_d);
   }
-  AFEM_TRY(launch_on(s, k_elem_poisson_tri, ge, 256, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+  AFEM_TRY(launch_on(s, k_elem_poisson_tri, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                      cell_coeff_d, rows));
   return launch_on(s, k_gather_scalar<3>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
                    (const double*)rows, values_d);

@@ -205,6 +205,18 @@ afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* 
 #define AFEM_GATHER_ELASTICITY_TET4 2
 afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* mesh, int kind, const int32_t* row_ptr_d,
                                 const double* ke_d, int layout, double* values_d, double* values_h, int chunks);
+/* The whole values assembly with the copy back pipelined: the cells are
+ * split into `chunks` (1..16) ranges; after the element matrices of each
+ * range, the nodes it completes (a prefix of the node numbering: every
+ * incident cell done) are gathered and their values copied to values_h on a
+ * second stream while the next range computes.  kind: AFEM_GATHER_POISSON_P1
+ * (cell_coeff_d nullable) or AFEM_GATHER_ELASTICITY_TET4 (lambda, mu,
+ * layout).  ke_d is the caller's element buffer (afem_element_matrices_*
+ * sizes).  Returns when values_h holds the whole matrix; values_d holds it
+ * too.  Meshes numbered so that nodes complete late overlap less. */
+afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* mesh, int kind, const int32_t* row_ptr_d,
+                                  const double* cell_coeff_d, double lambda, double mu, int layout, double* ke_d,
+                                  double* values_d, double* values_h, int chunks);
 
 /* Allocation-free assembly of the scalar Poisson P1 matrix.  No counterpart
  * in the reference: it serves callers that cannot let a library allocate

@@ -527,3 +527,28 @@ def test_mixed_bsr_rejects_a_scalar_pattern(cuda_ctx):
         fem.cg_solve_csr(cuda_ctx, rp3, cols, vals, b, x,
                          options=fem.solver_options(precision=fem.PRECISION_MIXED, block_size=3))
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("case", ["tri", "tet", "elast_block", "elast_row"])
+@pytest.mark.parametrize("chunks", [1, 4, 16])
+def test_assemble_to_host_matches_two_stage_assembly(cuda_ctx, case, chunks):
+    """The pipelined assembly (cell ranges, the node prefixes they complete
+    gathered and copied back behind them) gives exactly the values of the
+    element kernel followed by the one-shot gather."""
+    mesh = {"tri": lambda: meshgen.unit_square_tri(21, seed=1), "tet": lambda: meshgen.unit_cube_tet(7, seed=2),
+            "elast_block": lambda: meshgen.unit_cube_tet(5, seed=5),
+            "elast_row": lambda: meshgen.unit_cube_tet(6, seed=6)}[case]()
+    nb_dof = 3 if case.startswith("elast") else 1
+    f = build_format(cuda_ctx, mesh, nb_dof=nb_dof, use_csr=(case != "elast_block"))
+    coeff = None if nb_dof == 3 else torch.as_tensor(np.exp(np.random.default_rng(3).standard_normal(mesh.nb_cell)),
+                                                      device="cuda")
+    ke = torch.empty(f.element_buffer_size(), dtype=torch.float64, device="cuda")
+    f.element_matrices(ke, cell_coeff=coeff, lam=1.3, mu=0.7)
+    f.gather(ke)
+    ref = f.values.cpu().clone()
+    f.values.fill_(float("nan"))
+    ke.fill_(float("nan"))
+    host = torch.full((f.values.numel(),), float("nan"), dtype=torch.float64).pin_memory()
+    f.assemble_to_host(ke, host, chunks=chunks, cell_coeff=coeff, lam=1.3, mu=0.7)
+    assert torch.equal(host, ref)
+    assert torch.equal(f.values.cpu(), ref)
