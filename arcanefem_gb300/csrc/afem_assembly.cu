@@ -512,6 +512,23 @@ __global__ void __launch_bounds__(128) k_elem_poisson_quad4(int nb_cell, const d
   }
 }
 
+// Trilinear shape-function derivatives (d/dxi, d/deta, d/dzeta of N_0..N_7) at
+// the 2x2x2 Gauss points g = 4 i + 2 j + k, (xi, eta, zeta) = (+-1/sqrt 3)
+// with sign (i, j, k): each is +-0.125 (1 +- g)(1 +- g'), three magnitudes,
+// written exactly as the double products 0.125 * (1 + g) * (1 + g) etc. round.
+constexpr double kHpp = 0.3110042339640731;     // 0.125 (1 + 1/sqrt3)^2
+constexpr double kHpm = 0.08333333333333334;    // 0.125 (1 + 1/sqrt3)(1 - 1/sqrt3) = 1/12
+constexpr double kHmm = 0.022329099369260228;   // 0.125 (1 - 1/sqrt3)^2
+__constant__ double kHexDN[8][3][8] = {
+    {{-kHpp, kHpp, kHpm, -kHpm, -kHpm, kHpm, kHmm, -kHmm}, {-kHpp, -kHpm, kHpm, kHpp, -kHpm, -kHmm, kHmm, kHpm}, {-kHpp, -kHpm, -kHmm, -kHpm, kHpp, kHpm, kHmm, kHpm}},
+    {{-kHpm, kHpm, kHmm, -kHmm, -kHpp, kHpp, kHpm, -kHpm}, {-kHpm, -kHmm, kHmm, kHpm, -kHpp, -kHpm, kHpm, kHpp}, {-kHpp, -kHpm, -kHmm, -kHpm, kHpp, kHpm, kHmm, kHpm}},
+    {{-kHpm, kHpm, kHpp, -kHpp, -kHmm, kHmm, kHpm, -kHpm}, {-kHpp, -kHpm, kHpm, kHpp, -kHpm, -kHmm, kHmm, kHpm}, {-kHpm, -kHmm, -kHpm, -kHpp, kHpm, kHmm, kHpm, kHpp}},
+    {{-kHmm, kHmm, kHpm, -kHpm, -kHpm, kHpm, kHpp, -kHpp}, {-kHpm, -kHmm, kHmm, kHpm, -kHpp, -kHpm, kHpm, kHpp}, {-kHpm, -kHmm, -kHpm, -kHpp, kHpm, kHmm, kHpm, kHpp}},
+    {{-kHpp, kHpp, kHpm, -kHpm, -kHpm, kHpm, kHmm, -kHmm}, {-kHpm, -kHpp, kHpp, kHpm, -kHmm, -kHpm, kHpm, kHmm}, {-kHpm, -kHpp, -kHpm, -kHmm, kHpm, kHpp, kHpm, kHmm}},
+    {{-kHpm, kHpm, kHmm, -kHmm, -kHpp, kHpp, kHpm, -kHpm}, {-kHmm, -kHpm, kHpm, kHmm, -kHpm, -kHpp, kHpp, kHpm}, {-kHpm, -kHpp, -kHpm, -kHmm, kHpm, kHpp, kHpm, kHmm}},
+    {{-kHpm, kHpm, kHpp, -kHpp, -kHmm, kHmm, kHpm, -kHpm}, {-kHpm, -kHpp, kHpp, kHpm, -kHmm, -kHpm, kHpm, kHmm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}},
+    {{-kHmm, kHmm, kHpm, -kHpm, -kHpm, kHpm, kHpp, -kHpp}, {-kHmm, -kHpm, kHpm, kHmm, -kHpm, -kHpp, kHpp, kHpm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}}};
+
 __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int nb_cell, const double* __restrict__ xyz,
                                                             const int32_t* __restrict__ cn,
                                                             const int32_t* __restrict__ inv,
@@ -532,15 +549,9 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int nb_cell, const d
       for (int b = 0; b < 8; ++b) K[a][b] = 0.0;
 #pragma unroll 1
     for (int g = 0; g < 8; ++g) {
-      const double xi = (g >> 2) ? kGauss : -kGauss, eta = ((g >> 1) & 1) ? kGauss : -kGauss,
-                   zeta = (g & 1) ? kGauss : -kGauss;
-      const double mx = 1.0 - xi, px = 1.0 + xi, me = 1.0 - eta, pe = 1.0 + eta, mz = 1.0 - zeta, pz = 1.0 + zeta;
-      const double dxi[8] = {-0.125 * me * mz, 0.125 * me * mz, 0.125 * pe * mz, -0.125 * pe * mz,
-                             -0.125 * me * pz, 0.125 * me * pz, 0.125 * pe * pz, -0.125 * pe * pz};
-      const double deta[8] = {-0.125 * mx * mz, -0.125 * px * mz, 0.125 * px * mz, 0.125 * mx * mz,
-                              -0.125 * mx * pz, -0.125 * px * pz, 0.125 * px * pz, 0.125 * mx * pz};
-      const double dzeta[8] = {-0.125 * mx * me, -0.125 * px * me, -0.125 * px * pe, -0.125 * mx * pe,
-                               0.125 * mx * me, 0.125 * px * me, 0.125 * px * pe, 0.125 * mx * pe};
+      const double* dxi = kHexDN[g][0];
+      const double* deta = kHexDN[g][1];
+      const double* dzeta = kHexDN[g][2];
       double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
@@ -561,17 +572,21 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int nb_cell, const d
       const double v02 = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
       const double v12 = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
       const double v22 = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-      double dx[8], dy[8], dz[8];
+      // physical gradients, and the same scaled by det for the weighted products
+      double dx[8], dy[8], dz[8], sx[8], sy[8], sz[8];
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
         dx[a] = v00 * dxi[a] + v01 * deta[a] + v02 * dzeta[a];
         dy[a] = v10 * dxi[a] + v11 * deta[a] + v12 * dzeta[a];
         dz[a] = v20 * dxi[a] + v21 * deta[a] + v22 * dzeta[a];
+        sx[a] = dx[a] * det;
+        sy[a] = dy[a] * det;
+        sz[a] = dz[a] * det;
       }
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = a; b < 8; ++b) K[a][b] += (dx[a] * dx[b] + dy[a] * dy[b] + dz[a] * dz[b]) * det;
+        for (int b = a; b < 8; ++b) K[a][b] = fma(sx[a], dx[b], fma(sy[a], dy[b], fma(sz[a], dz[b], K[a][b])));
     }
     if (coeff) {
       const double k = __ldg(coeff + c);
