@@ -185,7 +185,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, in
   for (int n = wid; n < nb_node; n += nwarps) {
     const int32_t b = __ldg(nc_ptr + n);
     const int m = (__ldg(nc_ptr + n + 1) - b) * npc;
-    int len = m > kRowCap ? -1 : row_dispatch<false>(n, npc, m, cn, nc_cell + b, nullptr, 0, 0, nullptr, nullptr);
+    // a node in no cell keeps its diagonal (the reference's rows hold deg + 1 entries)
+    int len = m > kRowCap ? -1
+              : m == 0    ? 1
+                          : row_dispatch<false>(n, npc, m, cn, nc_cell + b, nullptr, 0, 0, nullptr, nullptr);
     if (lane == 0) {
       if (len < 0 || len > kMaxRowLen) {
         atomicOr(err, 2);
@@ -212,9 +215,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, i
     const int32_t b = __ldg(nc_ptr + n);
     const int m = (__ldg(nc_ptr + n + 1) - b) * npc;
     int got = -1;
-    if (m <= kRowCap)
+    if (m == 0) {   // a node in no cell: its diagonal only
+      got = 1;
+      if (lane == 0 && len == 1) cols[rb] = n;
+    } else if (m <= kRowCap) {
       got = row_dispatch<true>(n, npc, m, cn, nc_cell + b, nc_local + b, len, self_last, cols + rb,
                                slot + (int64_t)b * npc);
+    }
     if (lane == 0 && got != len) atomicOr(err, 4);
   }
 }

@@ -23,14 +23,15 @@ REL = 1e-12
 
 
 def rel_err_rows(got, ref, rp, b=1):
-    """Max over entries of |got - ref| / max(|ref|, 1e-3 * max|row|)."""
+    """Max over entries of |got - ref| / max(|ref|, 1e-3 * max|row|); an
+    all-zero row (a node in no cell) is compared absolutely."""
     ref = np.asarray(ref)
     got = np.asarray(got)
     row_of = np.repeat(np.arange(rp.size - 1), np.diff(rp) * b * b)
     rowmax = np.zeros(rp.size - 1)
     np.maximum.at(rowmax, row_of, np.abs(ref))
     denom = np.maximum(np.abs(ref), 1e-3 * rowmax[row_of])
-    return float(np.max(np.abs(got - ref) / denom))
+    return float(np.max(np.abs(got - ref) / np.where(denom > 0, denom, 1.0)))
 
 
 def build_format(ctx, mesh, nb_dof=1, use_csr=True, col_order=fem.COLS_ASCENDING):
@@ -552,3 +553,43 @@ def test_assemble_to_host_matches_two_stage_assembly(cuda_ctx, case, chunks):
     f.assemble_to_host(ke, host, chunks=chunks, cell_coeff=coeff, lam=1.3, mu=0.7)
     assert torch.equal(host, ref)
     assert torch.equal(f.values.cpu(), ref)
+
+
+def fan_mesh(k, isolated=0):
+    """k triangles around node 0 (a row of k + 1 entries), plus `isolated`
+    nodes that belong to no cell."""
+    t = np.linspace(0.0, 2 * np.pi, k, endpoint=False)
+    ring = np.stack([np.cos(t), np.sin(t), np.zeros(k)], 1)
+    coords = np.concatenate([np.zeros((1, 3)), ring, np.full((isolated, 3), 2.0)], 0)
+    cells = np.array([[0, 1 + i, 1 + (i + 1) % k] for i in range(k)], np.int32)
+    return coords, cells
+
+
+@pytest.mark.parametrize("k,isolated", [(12, 0), (40, 0), (100, 2)])
+def test_fan_rows_and_isolated_nodes_match_oracle(cuda_ctx, k, isolated):
+    """Rows longer than the gather's shared-memory accumulators (the direct
+    path: 41 and 101 entries) and nodes in no cell (a diagonal-only row, as
+    the reference's deg + 1 rows): structure bit-exact, values 1e-12."""
+    coords, cells = fan_mesh(k, isolated)
+    n = coords.shape[0]
+    f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
+    f.initialize(1)
+    f.compute_sparsity()
+    rp, cols = O.sparsity(n, cells)
+    assert np.array_equal(f.row_ptr.cpu().numpy(), rp) and np.array_equal(f.cols.cpu().numpy(), cols)
+    f.assemble_poisson()
+    ptr, nc, _ = O.node_cell(n, cells)
+    ref = O.assemble(O.POISSON_TRI3, coords, cells, ptr, nc, rp, cols)
+    assert rel_err_rows(f.values.cpu().numpy(), ref, rp) < REL
+
+
+def test_row_above_the_candidate_capacity_is_reported(cuda_ctx):
+    """A node in 200 triangles (600 candidate entries, above the per-node
+    capacity of the sparsity kernels) is reported as a mesh error, not
+    truncated."""
+    coords, cells = fan_mesh(200)
+    f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
+    f.initialize(1)
+    with pytest.raises(fem.AfemError) as e:
+        f.compute_sparsity()
+    assert e.value.status == 7
