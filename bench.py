@@ -480,8 +480,13 @@ def run_solve(args, ctx, mesh, fmt):
         wall = (time.perf_counter() - t0) * 1e3
         res[prec] = {"solve_ms": info.solve_ms, "wall_ms": wall, "iterations": info.iterations,
                      "refinements": info.refinements, "true_relres": info.relres, "status": info.status}
-        if prec == "fp64" and not args.no_cpu_baseline:
-            res["cpu_fp64_cg"] = cpu_solve_baseline(fmt, ls, info.iterations)
+        x = ls.solution_variable()
+        if prec == "fp64":
+            x_fp64 = x.clone()
+            if not args.no_cpu_baseline:
+                res["cpu_fp64_cg"] = cpu_solve_baseline(fmt, ls, info.iterations)
+        else:   # error against the FP64 CG solution of the same system
+            res[prec]["error_vs_fp64_cg"] = float(torch.linalg.norm(x - x_fp64) / torch.linalg.norm(x_fp64))
         ls.close()
     return res
 
