@@ -532,22 +532,28 @@ def run_learned(args):
     setup_s = time.perf_counter() - t0
     b = prob.rhs(np.random.default_rng(123))
 
-    def best(fn, reps=3):
+    sols = {}
+
+    def best(fn, reps=3, tag=None):
         out = [fn() for _ in range(reps)]
-        return min(out, key=lambda i: i.solve_ms)
+        info, x = min(out, key=lambda o: o[0].solve_ms)
+        if tag:
+            sols[tag] = x
+        return info
 
     def cg(precond):
         x = torch.zeros_like(b)
-        return fem.cg_solve_csr(ctx, prob.row_ptr, prob.cols, prob.values, b, x,
+        info = fem.cg_solve_csr(ctx, prob.row_ptr, prob.cols, prob.values, b, x,
                                 options=fem.solver_options(rtol=1e-8, max_iter=50000, precond=precond))
+        return info, x
 
     def fcg():
         x = torch.zeros_like(b)
-        return net.fcg(prob.row_ptr, prob.cols, prob.values, b, x, fem.solver_options(rtol=1e-8, max_iter=5000))
+        return net.fcg(prob.row_ptr, prob.cols, prob.values, b, x, fem.solver_options(rtol=1e-8, max_iter=5000)), x
 
-    cg_jac = best(lambda: cg(fem.PRECOND_JACOBI), 2)
+    cg_jac = best(lambda: cg(fem.PRECOND_JACOBI), 2, tag="fp64")
     cg_none = best(lambda: cg(fem.PRECOND_NONE), 1)
-    untrained = best(fcg)
+    untrained = best(fcg, tag="untrained")
     t0 = time.perf_counter()
     R, E = learned.make_training_pairs(prob, count=2000, solves=20, every=25, seed=4)
     torch.cuda.synchronize()
@@ -556,8 +562,12 @@ def run_learned(args):
     rep = learned.train_validated(net, prob, R, E, prob.rhs(np.random.default_rng(77)), epochs=4, batch=16, lr=2e-3)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
-    kept = best(fcg)
+    kept = best(fcg, tag="learned")
     net.close()
+
+    def err(tag):   # relative error against the FP64 Jacobi-CG solution of the same system
+        return float(torch.linalg.norm(sols[tag] - sols["fp64"]) / torch.linalg.norm(sols["fp64"]))
+
 
     def d(info):
         return {"solve_ms": info.solve_ms, "iterations": info.iterations, "true_relres": info.relres,
@@ -566,7 +576,8 @@ def run_learned(args):
         "problem": f"-div(k grad u) = f, {n}^2 quads x 2 triangles ({2 * n * n} tris), k = exp(GRF 0.05, var 1)",
         "target_relres": 1e-8,
         "plain_fp64_cg_jacobi": d(cg_jac), "plain_fp64_cg_none": d(cg_none),
-        "fcg_vcycle_untrained": d(untrained), "fcg_learned": d(kept),
+        "fcg_vcycle_untrained": dict(d(untrained), error_vs_fp64_cg=err("untrained")),
+        "fcg_learned": dict(d(kept), error_vs_fp64_cg=err("learned")),
         "speedup_vs_plain_fp64_cg_jacobi": cg_jac.solve_ms / kept.solve_ms,
         "speedup_vs_plain_fp64_cg_none": cg_none.solve_ms / kept.solve_ms,
         "network": ("6 message-passing layers, width 64, BF16 mma.sync GEMMs, FP32 accumulate; predicts the "
