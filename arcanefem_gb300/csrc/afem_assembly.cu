@@ -547,17 +547,50 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int nb_cell, const d
     for (int a = 0; a < 8; ++a)
 #pragma unroll
       for (int b = 0; b < 8; ++b) K[a][b] = 0.0;
+    // The trilinear map's derivatives are bilinear in the other two reference
+    // coordinates: d x / d xi = m_xi + eta m_xieta + zeta m_xizeta + eta zeta m_xietazeta,
+    // and so on, with the moments m (signed sums of the 8 nodal coordinates, / 8)
+    // formed once per cell by a Walsh-Hadamard butterfly: 3 FMAs per Jacobian
+    // entry per Gauss point instead of 8.  Node a has reference signs
+    // (s_xi, s_eta, s_zeta) = (-,-,-) (+,-,-) (+,+,-) (-,+,-) (-,-,+) (+,-,+) (+,+,+) (-,+,+).
+    double mo[3][8];   // per component: [1, xi, eta, xi eta, zeta, xi zeta, eta zeta, xi eta zeta]
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double* v = q == 0 ? x : (q == 1 ? y : z);
+      // reorder to the binary order (xi bit 0, eta bit 1, zeta bit 2): nodes 0 1 3 2 4 5 7 6
+      const double u0 = v[0], u1 = v[1], u2 = v[3], u3 = v[2], u4 = v[4], u5 = v[5], u6 = v[7], u7 = v[6];
+      // stage xi
+      const double a0 = u1 + u0, a1 = u1 - u0, a2 = u3 + u2, a3 = u3 - u2;
+      const double a4 = u5 + u4, a5 = u5 - u4, a6 = u7 + u6, a7 = u7 - u6;
+      // stage eta
+      const double b0 = a2 + a0, b1 = a3 + a1, b2 = a2 - a0, b3 = a3 - a1;
+      const double b4 = a6 + a4, b5 = a7 + a5, b6 = a6 - a4, b7 = a7 - a5;
+      // stage zeta
+      mo[q][0] = 0.125 * (b4 + b0);
+      mo[q][1] = 0.125 * (b5 + b1);
+      mo[q][2] = 0.125 * (b6 + b2);
+      mo[q][3] = 0.125 * (b7 + b3);
+      mo[q][4] = 0.125 * (b4 - b0);
+      mo[q][5] = 0.125 * (b5 - b1);
+      mo[q][6] = 0.125 * (b6 - b2);
+      mo[q][7] = 0.125 * (b7 - b3);
+    }
 #pragma unroll 1
     for (int g = 0; g < 8; ++g) {
       const double* dxi = kHexDN[g][0];
       const double* deta = kHexDN[g][1];
       const double* dzeta = kHexDN[g][2];
-      double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+      const double xi = (g >> 2) ? kGauss : -kGauss, eta = ((g >> 1) & 1) ? kGauss : -kGauss,
+                   zeta = (g & 1) ? kGauss : -kGauss;
+      const double xe = (g >> 2) == ((g >> 1) & 1) ? kGauss * kGauss : -(kGauss * kGauss);
+      const double xz = (g >> 2) == (g & 1) ? kGauss * kGauss : -(kGauss * kGauss);
+      const double ez = ((g >> 1) & 1) == (g & 1) ? kGauss * kGauss : -(kGauss * kGauss);
+      double J[3][3];
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
-        J[0][0] += dxi[a] * x[a]; J[0][1] += dxi[a] * y[a]; J[0][2] += dxi[a] * z[a];
-        J[1][0] += deta[a] * x[a]; J[1][1] += deta[a] * y[a]; J[1][2] += deta[a] * z[a];
-        J[2][0] += dzeta[a] * x[a]; J[2][1] += dzeta[a] * y[a]; J[2][2] += dzeta[a] * z[a];
+      for (int q = 0; q < 3; ++q) {
+        J[0][q] = fma(ez, mo[q][7], fma(zeta, mo[q][5], fma(eta, mo[q][3], mo[q][1])));
+        J[1][q] = fma(xz, mo[q][7], fma(zeta, mo[q][6], fma(xi, mo[q][3], mo[q][2])));
+        J[2][q] = fma(xe, mo[q][7], fma(eta, mo[q][6], fma(xi, mo[q][5], mo[q][4])));
       }
       // determinant by the first row, inverse = adjugate / det
       const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];

@@ -62,7 +62,7 @@ WORKLOADS = {
     # Q1 widening: trilinear hexahedra (2x2x2 Gauss points), Q1 source, FP64 / mixed CG
     "poisson3d_hex": dict(dim=3, cell="hex", n=96, jitter=0.15, nb_dof=1,
                           metric="assembled nnz/s (node-wise CSR, 3D Poisson Q1 Hexa8)",
-                          dp_elem=2488, dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
+                          dp_elem=2218, dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
 }
 
 
