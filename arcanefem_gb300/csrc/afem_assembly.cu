@@ -151,7 +151,9 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tri(int cell0, int nb_cell
 // Each thread computes the 78 distinct values of its cell (6 off-diagonal
 // 3x3 blocks, 4 symmetric diagonal blocks) into shared memory; the warp then
 // writes the 4 x 32 row blocks (288 B each) with 16-byte stores, 18 lanes per
-// row block, so that every written sector is complete.
+// row block, so that every written sector is complete.  The packed source
+// positions of each 16-byte chunk come from a per-block table, and a lane's
+// (cell, chunk) position advances by 32 chunks per pass without a division.
 constexpr int kElastElemBlock = 64;
 constexpr int kElastPacked = 78;
 
@@ -172,7 +174,23 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
                                                                          double lambda, double mu,
                                                                          double* __restrict__ er) {
   __shared__ double stage[kElastElemBlock][kElastPacked + 1];
-  __shared__ int32_t stage_p[kElastElemBlock][4];
+  __shared__ int4 stage_p[kElastElemBlock];
+  // src_tab[n][q]: packed positions of entries 2q and 2q + 1 of node n's row block
+  __shared__ uint32_t src_tab[4][18];
+  for (int i = threadIdx.x; i < 72; i += blockDim.x) {
+    const int n = i / 18, q = i - 18 * n;
+    uint32_t two = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      // row-block position pos = a * 12 + 3 * qn + b: column-node position qn is
+      // 0 for the row's own node n, then the other local nodes increasing
+      const int pos = 2 * q + h, a = pos / 12, rem = pos - 12 * a, qn = rem / 3, bb = rem - 3 * qn;
+      const int m = qn == 0 ? n : qn - 1 + (qn - 1 >= n);
+      two |= (uint32_t)elast_packed(n, m, a, bb) << (16 * h);
+    }
+    src_tab[n][q] = two;
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
   for (int64_t base = cell0 + blockIdx.x * (int64_t)blockDim.x; base < nb_cell; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = base + threadIdx.x;
@@ -189,11 +207,7 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
       const d3 c1 = cross(v2, v3), c2 = cross(v3, v1), c3 = cross(v1, v2);
       const double s = __drcp_rn(6.0 * fabs(dot(v1, c1)));
       const double ls = lambda * s, ms = mu * s, lms = (lambda + mu) * s;
-      const int4 p4 = __ldg(reinterpret_cast<const int4*>(inv) + c);
-      stage_p[threadIdx.x][0] = p4.x;
-      stage_p[threadIdx.x][1] = p4.y;
-      stage_p[threadIdx.x][2] = p4.z;
-      stage_p[threadIdx.x][3] = p4.w;
+      stage_p[threadIdx.x] = __ldg(reinterpret_cast<const int4*>(inv) + c);
       const double cv[3][3] = {{c1.x, c1.y, c1.z}, {c2.x, c2.y, c2.z}, {c3.x, c3.y, c3.z}};
       // K0[m] accumulates K_0,m+1 = -(sum over n = 1..3 of K_n,m+1); it starts as -K_m+1,m+1
       double K0[3][3][3];
@@ -254,22 +268,22 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
     __syncwarp();
     const int64_t wfirst = base + wbase;
     const int wcount = wfirst < nb_cell ? (int)(nb_cell - wfirst < 32 ? nb_cell - wfirst : 32) : 0;
-#pragma unroll 1
-    for (int n = 0; n < 4; ++n) {
-      for (int k = lane; k < wcount * 18; k += 32) {
-        const int t = k / 18, q = k - 18 * t;
-        // row-block position pos = a * 12 + 3 * qn + b: column-node position qn is
-        // 0 for the row's own node n, then the other local nodes increasing
-        const int pos = 2 * q, a = pos / 12, rem = pos - 12 * a, qn = rem / 3, b = rem - 3 * qn;
-        const int m = qn == 0 ? n : qn - 1 + (qn - 1 >= n);
-        const double* src = stage[wbase + t];
-        const double v0 = src[elast_packed(n, m, a, b)];
-        const int pos1 = pos + 1, a1 = pos1 / 12, rem1 = pos1 - 12 * a1, qn1 = rem1 / 3, b1 = rem1 - 3 * qn1;
-        const int m1 = qn1 == 0 ? n : qn1 - 1 + (qn1 - 1 >= n);
-        const double v1 = src[elast_packed(n, m1, a1, b1)];
-        double* dst = er + 36 * (int64_t)stage_p[wbase + t][n] + pos;
-        *reinterpret_cast<double2*>(dst) = make_double2(v0, v1);
+    // chunk k = 18 t + q of the warp's cells: lane k starts at t = k / 18 and
+    // every pass adds 32 = 18 + 14 chunks
+    int t = lane >= 18, q = lane - 18 * (lane >= 18);
+    for (int k = lane; k < wcount * 18; k += 32) {
+      const double* src = stage[wbase + t];
+      const int4 p4 = stage_p[wbase + t];
+      const int pr[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        const uint32_t two = src_tab[n][q];
+        double* dst = er + 36 * (int64_t)pr[n] + 2 * q;
+        *reinterpret_cast<double2*>(dst) = make_double2(src[two & 0xffffu], src[two >> 16]);
       }
+      q += 14;
+      t += 1 + (q >= 18);
+      q -= 18 * (q >= 18);
     }
     __syncwarp();
   }
