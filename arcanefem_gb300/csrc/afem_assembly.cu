@@ -25,6 +25,7 @@
 //   Diagonals use the zero row sum of a P1 stiffness: K_ii = -sum_{j!=i} K_ij.
 // Results agree with the reference formulas to rounding (tests check 1e-12).
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "afem_internal.cuh"
@@ -322,6 +323,11 @@ __global__ void k_node_bounds(int nb_node, const int32_t* __restrict__ nc_ptr, c
 // Node-wise gathers: one thread per (scalar) row streams its contiguous
 // element rows and adds them into shared-memory accumulators (row length
 // <= kScalarRmax) or directly into its own row of `values` (longer rows).
+// The columns of one incidence are distinct nodes of one cell, hence distinct
+// accumulator slots: each incidence loads all of its accumulators, adds, then
+// stores them, so its read-modify-writes overlap instead of queuing behind
+// one another (the compiler cannot prove the slots distinct by itself).  Every
+// accumulator still receives its terms in increasing incidence order.
 
 template <int NPC>
 __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int row0, int nb_node,
@@ -348,9 +354,13 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int row0, int nb
           const double2 a = __ldg(src), b = __ldg(src + 1);
           const uint32_t w = __ldg(sp);
           diag += a.x;
-          my[((w >> 8) & 0xffu) * kGatherBlock] += a.y;
-          my[((w >> 16) & 0xffu) * kGatherBlock] += b.x;
-          my[(w >> 24) * kGatherBlock] += b.y;
+          double* const d1 = my + ((w >> 8) & 0xffu) * kGatherBlock;
+          double* const d2 = my + ((w >> 16) & 0xffu) * kGatherBlock;
+          double* const d3 = my + (w >> 24) * kGatherBlock;
+          const double o1 = *d1, o2 = *d2, o3 = *d3;
+          *d1 = o1 + a.y;
+          *d2 = o2 + b.x;
+          *d3 = o3 + b.y;
         }
       } else {
         const double* src = er + (int64_t)NPC * p0;
@@ -358,8 +368,14 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_scalar(int row0, int nb
 #pragma unroll 2
         for (int32_t p = p0; p < p1; ++p, src += NPC, sp += NPC) {
           diag += __ldg(src);
+          double* d[NPC];
+          double o[NPC];
 #pragma unroll
-          for (int j = 1; j < NPC; ++j) my[__ldg(sp + j) * kGatherBlock] += __ldg(src + j);
+          for (int j = 1; j < NPC; ++j) d[j] = my + __ldg(sp + j) * kGatherBlock;
+#pragma unroll
+          for (int j = 1; j < NPC; ++j) o[j] = *d[j];
+#pragma unroll
+          for (int j = 1; j < NPC; ++j) *d[j] = o[j] + __ldg(src + j);
         }
       }
       if (p1 > p0) my[__ldg(nc_slot + (int64_t)NPC * p0) * kGatherBlock] = diag;
@@ -410,13 +426,18 @@ __global__ void __launch_bounds__(kGatherBlock) k_gather_elasticity(int node0, i
         self0 += v[0];
         self1 += v[1];
         self2 += v[2];
+        double* d[4];
+        double o[12];
 #pragma unroll
-        for (int m = 1; m < 4; ++m) {
-          double* d = my + 3 * ((w >> (8 * m)) & 0xffu) * kGatherBlock;
-          d[0] += v[3 * m];
-          d[kGatherBlock] += v[3 * m + 1];
-          d[2 * kGatherBlock] += v[3 * m + 2];
-        }
+        for (int m = 1; m < 4; ++m) d[m] = my + 3 * ((w >> (8 * m)) & 0xffu) * kGatherBlock;
+#pragma unroll
+        for (int m = 1; m < 4; ++m)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) o[3 * m + b] = d[m][b * kGatherBlock];
+#pragma unroll
+        for (int m = 1; m < 4; ++m)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) d[m][b * kGatherBlock] = o[3 * m + b] + v[3 * m + b];
       }
       if (p1 > p0) {
         double* d = my + 3 * (__ldg(nc_slot + 4 * (int64_t)p0) & 0xffu) * kGatherBlock;
@@ -899,19 +920,38 @@ afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, co
                 values_d);
 }
 
+// Range count for chunks == 0: one range per ~80 MB of values, at most 12.
+// Measured on GB300 at ~193 GB/s device -> host: fewer ranges leave a longer
+// copy of the last range after the compute; more ranges add per-range launch
+// and synchronisation cost (3D Poisson, 254 MB: best at 4; elasticity,
+// 970 MB: best at 12, slower at 16).
+constexpr double kAutoRangeBytes = 80e6;
+constexpr int kAutoMaxRanges = 12;
+
+static afem_status auto_ranges(afem_context ctx, const int32_t* row_ptr_d, int n, int64_t scale, int* chunks) {
+  int32_t* hb = reinterpret_cast<int32_t*>(ctx->pinned);
+  AFEM_CUDA(cudaMemcpyAsync(hb, row_ptr_d + n, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+  const double bytes = (double)hb[0] * (double)scale * sizeof(double);
+  *chunks = (int)std::min<double>(kAutoMaxRanges, std::max(1.0, std::ceil(bytes / kAutoRangeBytes)));
+  return AFEM_OK;
+}
+
 afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* m, int kind, const int32_t* row_ptr_d,
                                 const double* ke, int layout, double* values_d, double* values_h, int chunks) {
   AFEM_CHECK_ARG(ctx, "afem_gather_to_host: null context");
   AFEM_TRY(check_assembly(m, "afem_gather_to_host"));
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
                  "afem_gather_to_host: bad buffer");
-  AFEM_CHECK_ARG(chunks >= 1 && chunks <= 16, "afem_gather_to_host: chunks 1..16");
+  AFEM_CHECK_ARG(chunks >= 0 && chunks <= 16, "afem_gather_to_host: chunks 0..16");
   AFEM_CHECK_ARG(kind == AFEM_GATHER_POISSON_P1 || kind == AFEM_GATHER_POISSON_Q1 ||
                      (kind == AFEM_GATHER_ELASTICITY_TET4 && m->dim == 3),
                  "afem_gather_to_host: bad kind %d", kind);
   AFEM_CHECK_ARG(kind != AFEM_GATHER_ELASTICITY_TET4 || layout == AFEM_LAYOUT_PER_BLOCK ||
                      layout == AFEM_LAYOUT_PER_ROW,
                  "afem_gather_to_host: bad layout %d", layout);
+  if (chunks == 0)
+    AFEM_TRY(auto_ranges(ctx, row_ptr_d, m->nb_node, kind == AFEM_GATHER_ELASTICITY_TET4 ? 9 : 1, &chunks));
   if (!ctx->copy_stream) AFEM_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
   for (int k = 0; k <= chunks; ++k)
     if (!ctx->chunk_ev[k]) AFEM_CUDA(cudaEventCreateWithFlags(&ctx->chunk_ev[k], cudaEventDisableTiming));
@@ -960,13 +1000,15 @@ afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int
   AFEM_TRY(check_assembly(m, "afem_assemble_to_host"));
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
                  "afem_assemble_to_host: bad buffer");
-  AFEM_CHECK_ARG(chunks >= 1 && chunks <= kMaxAsmChunks, "afem_assemble_to_host: chunks 1..%d", kMaxAsmChunks);
+  AFEM_CHECK_ARG(chunks >= 0 && chunks <= kMaxAsmChunks, "afem_assemble_to_host: chunks 0..%d", kMaxAsmChunks);
   AFEM_CHECK_ARG(kind == AFEM_GATHER_POISSON_P1 || (kind == AFEM_GATHER_ELASTICITY_TET4 && m->dim == 3),
                  "afem_assemble_to_host: kind must be AFEM_GATHER_POISSON_P1 or AFEM_GATHER_ELASTICITY_TET4");
   AFEM_CHECK_ARG(kind != AFEM_GATHER_ELASTICITY_TET4 || layout == AFEM_LAYOUT_PER_BLOCK ||
                      layout == AFEM_LAYOUT_PER_ROW,
                  "afem_assemble_to_host: bad layout %d", layout);
   AFEM_CHECK_ARG(m->nc_ptr_d && m->nc_cell_d, "afem_assemble_to_host: null node->cell lists");
+  if (chunks == 0)
+    AFEM_TRY(auto_ranges(ctx, row_ptr_d, m->nb_node, kind == AFEM_GATHER_ELASTICITY_TET4 ? 9 : 1, &chunks));
   if (!ctx->copy_stream) AFEM_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
   for (int k = 0; k <= chunks; ++k)
     if (!ctx->chunk_ev[k]) AFEM_CUDA(cudaEventCreateWithFlags(&ctx->chunk_ev[k], cudaEventDisableTiming));

@@ -209,10 +209,11 @@ class BSRFormat:
             fn = "afem_gather_poisson_q1" if self.is_q1() else "afem_gather_poisson_p1"
             call(fn, self.ctx.handle, C.byref(mv), _ptr(self.row_ptr), _ptr(ke), _ptr(self.values))
 
-    def gather_to_host(self, ke: torch.Tensor, values_h: torch.Tensor, chunks: int = 4):
+    def gather_to_host(self, ke: torch.Tensor, values_h: torch.Tensor, chunks: int = 0):
         """gather() with the values copied into the host tensor values_h
         (pinned for overlap) range by range while the next range is gathered;
-        returns when values_h is complete."""
+        returns when values_h is complete.  chunks = 0: one range per ~80 MB
+        of values (at most 12)."""
         assert values_h.device.type == "cpu" and values_h.dtype == torch.float64
         assert values_h.numel() == self.values.numel() and values_h.is_contiguous()
         mv = self.mesh_view()
@@ -225,11 +226,12 @@ class BSRFormat:
         call("afem_gather_to_host", self.ctx.handle, C.byref(mv), kind, _ptr(self.row_ptr), _ptr(ke), layout,
              _ptr(self.values), C.c_void_p(values_h.data_ptr()), int(chunks))
 
-    def assemble_to_host(self, ke: torch.Tensor, values_h: torch.Tensor, chunks: int = 8,
+    def assemble_to_host(self, ke: torch.Tensor, values_h: torch.Tensor, chunks: int = 0,
                          cell_coeff: torch.Tensor | None = None, lam=0.0, mu=0.0):
         """element_matrices + gather with the values copied into the host
         tensor values_h (pinned for overlap), the copies overlapping the
-        element computation of later cell ranges (P1 Poisson, P1 elasticity)."""
+        element computation of later cell ranges (P1 Poisson, P1 elasticity).
+        chunks = 0: one range per ~80 MB of values (at most 12)."""
         assert values_h.device.type == "cpu" and values_h.dtype == torch.float64
         assert values_h.numel() == self.values.numel() and values_h.is_contiguous()
         mv = self.mesh_view()

@@ -78,7 +78,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--e2e-chunks", type=int, default=0,
-                   help="cell ranges of the e2e assembly / copy-back overlap (0: one per 8 M values, 1..4)")
+                   help="cell ranges of the e2e assembly / copy-back overlap (0: the library's choice, "
+                        "one per ~80 MB of values, at most 12; 1..16)")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--inner-rtol", type=float, default=0.1,
                    help="mixed precision: FP32 CG residual reduction between reliable updates")
@@ -347,7 +348,7 @@ def run_e2e(args, mesh, fmt0, lam, mu):
     dce = torch.empty_like(cells_h, device="cuda")
     ke = torch.empty(fmt0.element_buffer_size(), dtype=torch.float64, device="cuda")
     steps = max(3, args.steps // 2)
-    chunks = args.e2e_chunks if args.e2e_chunks > 0 else int(min(4, max(1, nnz // 8_000_000)))
+    chunks = args.e2e_chunks   # 0: the library's choice, one range per ~80 MB of values
 
     def timed(one):
         for _ in range(2):
@@ -397,7 +398,8 @@ def run_e2e(args, mesh, fmt0, lam, mu):
     return {"value": nnz / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "ms_per_step": dt * 1e3, "steps": steps,
             "includes": ("H2D node coordinates, element matrices and gather in cell ranges, each completed node "
-                         f"range's values D2H behind it ({chunks} ranges; sparsity reused)"),
+                         f"range's values D2H behind it ({chunks or 'auto: one per ~80 MB of values, max 12'} "
+                         "ranges; sparsity reused)"),
             "rebuild": {"value": nnz / dt_r, "unit": UNIT, "ms_per_step": dt_r * 1e3,
                         "h2d_bytes_per_step": h2d + cells_h.numel() * 4,
                         "d2h_bytes_per_step": d2h + fmt0.nnzb * 4 + (mesh.nb_node + 1) * 4,

@@ -192,7 +192,8 @@ afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* 
                                         const double* ke_d, int layout, double* values_d);
 
 /* Gather and copy back in one call: the node-wise gather runs in `chunks`
- * (1..16) node ranges on the context stream, and each finished range of
+ * (1..16; 0 = one range per ~80 MB of values, at most 12) node ranges on
+ * the context stream, and each finished range of
  * values_d goes to the host buffer values_h on a second stream while the next
  * range is gathered (pinned values_h for a real overlap).  kind selects the
  * gather of afem_gather_poisson_p1, afem_gather_poisson_q1 or
@@ -206,7 +207,8 @@ afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* 
 afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* mesh, int kind, const int32_t* row_ptr_d,
                                 const double* ke_d, int layout, double* values_d, double* values_h, int chunks);
 /* The whole values assembly with the copy back pipelined: the cells are
- * split into `chunks` (1..16) ranges; after the element matrices of each
+ * split into `chunks` (1..16; 0 = one range per ~80 MB of values, at most
+ * 12) ranges; after the element matrices of each
  * range, the nodes it completes (a prefix of the node numbering: every
  * incident cell done) are gathered and their values copied to values_h on a
  * second stream while the next range computes.  kind: AFEM_GATHER_POISSON_P1

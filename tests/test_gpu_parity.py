@@ -467,7 +467,7 @@ def test_msh_to_vtu_end_to_end(cuda_ctx, tmp_path):
 
 
 @pytest.mark.parametrize("case", ["tri", "tet", "quad", "hex", "elast_block", "elast_row"])
-@pytest.mark.parametrize("chunks", [1, 3, 16])
+@pytest.mark.parametrize("chunks", [0, 1, 3, 16])
 def test_gather_to_host_matches_device_gather(cuda_ctx, case, chunks):
     """The chunked gather with overlapped copies back to a host buffer gives
     exactly the values of the one-shot device gather."""
@@ -531,7 +531,7 @@ def test_mixed_bsr_rejects_a_scalar_pattern(cuda_ctx):
 
 
 @pytest.mark.parametrize("case", ["tri", "tet", "elast_block", "elast_row"])
-@pytest.mark.parametrize("chunks", [1, 4, 16])
+@pytest.mark.parametrize("chunks", [0, 1, 4, 16])
 def test_assemble_to_host_matches_two_stage_assembly(cuda_ctx, case, chunks):
     """The pipelined assembly (cell ranges, the node prefixes they complete
     gathered and copied back behind them) gives exactly the values of the
