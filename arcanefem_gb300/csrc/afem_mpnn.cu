@@ -214,13 +214,39 @@ __global__ void __launch_bounds__(256) k_dw_partial(int M, const bf16* __restric
   }
 }
 
-// out[e] (+)= sum_b partial[b][e], fixed order (deterministic).
-__global__ void k_sum_partials(int nparts, int nelem, const float* __restrict__ partial, float* __restrict__ out,
-                               int accumulate) {
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nelem; e += gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (int b = 0; b < nparts; ++b) s += partial[(int64_t)b * nelem + e];
-    out[e] = accumulate ? out[e] + s : s;
+// out[e] (+)= sum_b partial[b][e] in a fixed order (deterministic).  A block
+// covers 32 consecutive elements, one per lane, so that every warp load is
+// one coalesced 128-byte row segment; its kSumWarps warps split the partials
+// (warp w takes b = w, w + kSumWarps, ..., four loads in flight), and warp 0
+// adds the warp sums in warp order.
+constexpr int kSumWarps = 32;
+__global__ void __launch_bounds__(32 * kSumWarps) k_sum_partials(int nparts, int nelem,
+                                                                 const float* __restrict__ partial,
+                                                                 float* __restrict__ out, int accumulate) {
+  __shared__ float sh[kSumWarps][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int e = blockIdx.x * 32 + lane;
+  float s = 0.f;
+  if (e < nelem) {
+    int b = w;
+    for (; b + 3 * kSumWarps < nparts; b += 4 * kSumWarps) {
+      const float a0 = partial[(int64_t)b * nelem + e];
+      const float a1 = partial[(int64_t)(b + kSumWarps) * nelem + e];
+      const float a2 = partial[(int64_t)(b + 2 * kSumWarps) * nelem + e];
+      const float a3 = partial[(int64_t)(b + 3 * kSumWarps) * nelem + e];
+      s += a0;
+      s += a1;
+      s += a2;
+      s += a3;
+    }
+    for (; b < nparts; b += kSumWarps) s += partial[(int64_t)b * nelem + e];
+  }
+  sh[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && e < nelem) {
+    float t = 0.f;
+    for (int k = 0; k < kSumWarps; ++k) t += sh[k][lane];
+    out[e] = accumulate ? out[e] + t : t;
   }
 }
 
@@ -1072,14 +1098,19 @@ static afem_status ensure_part(afem_mpnn net, int64_t count) {
   return AFEM_OK;
 }
 
+static afem_status sum_partials(afem_context ctx, int nparts, int nelem, const float* part, float* dst,
+                                int accumulate) {
+  return launch(ctx, k_sum_partials, (unsigned)((nelem + 31) / 32), 32 * kSumWarps, 0, nparts, nelem, part, dst,
+                accumulate);
+}
+
 // dW = X^T G summed over M rows into dst (FP32 64x64), deterministic
 static afem_status dw_gemm(afem_mpnn net, int64_t M, const bf16* X, const bf16* G, float* dst) {
   afem_context ctx = net->ctx;
   const int nb = (int)std::max<int64_t>(1, std::min<int64_t>((M + kDwRows - 1) / kDwRows, (int64_t)ctx->sm_count * 2));
   AFEM_TRY(ensure_part(net, (int64_t)nb * kF * kF));
   AFEM_TRY(launch(ctx, k_dw_partial, nb, 256, 0, (int)M, X, G, net->part));
-  return launch(ctx, k_sum_partials, grid_for(ctx, kF * kF, 256), 256, 0, nb, kF * kF, (const float*)net->part, dst,
-                0);
+  return sum_partials(ctx, nb, kF * kF, (const float*)net->part, dst, 0);
 }
 
 // loss and gradients of the mean relative squared error over (r, e)
@@ -1112,7 +1143,7 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
     AFEM_TRY(ensure_part(net, (int64_t)nbk * (kF + 1)));
     AFEM_TRY(launch(ctx, k_head_backward, nbk, 256, 0, nl, (const float*)net->dc[l], (const bf16*)net->o[l],
                     (const float*)(net->params + off_head(net->NL, l)), net->dO[l], net->part));
-    AFEM_TRY(launch(ctx, k_sum_partials, 1, 96, 0, (int)nbk, kF + 1, (const float*)net->part,
+    AFEM_TRY(sum_partials(ctx, (int)nbk, kF + 1, (const float*)net->part,
                     net->grads + off_head(net->NL, l), 0));
   }
   // network backward, coarsest level first: o_l gets its head gradient plus R_l^T dh_{l+1}
@@ -1126,7 +1157,7 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
     AFEM_TRY(ensure_part(net, std::max<int64_t>((int64_t)nbk * kF, (int64_t)ctx->sm_count * 2 * kF * kF)));
     AFEM_TRY(launch(ctx, k_relu_grad, nbk, 256, 0, M, (const float*)net->dO[l], (const bf16*)net->o[l], net->Gb,
                     net->part));
-    AFEM_TRY(launch(ctx, k_sum_partials, 1, 64, 0, (int)nbk, kF, (const float*)net->part, net->grads + off_b(l), 0));
+    AFEM_TRY(sum_partials(ctx, (int)nbk, kF, (const float*)net->part, net->grads + off_b(l), 0));
     AFEM_TRY(dw_gemm(net, M, net->h[l], net->Gb, net->grads + off_w1(l)));
     AFEM_TRY(dw_gemm(net, M, net->m[l], net->Gb, net->grads + off_w2(l)));
     // dh_l = G W1^T + S_l^T (G W2^T)   (S_l symmetric)
@@ -1144,7 +1175,7 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
     AFEM_TRY(ensure_part(net, (int64_t)nbk * 3 * kF));
     AFEM_TRY(launch(ctx, k_input_backward, nbk, 256, 0, (int64_t)n0, (const float*)net->dH[0],
                     (const bf16*)net->a_in, (const float*)net->x0, net->part));
-    AFEM_TRY(launch(ctx, k_sum_partials, 1, 192, 0, (int)nbk, 3 * kF, (const float*)net->part,
+    AFEM_TRY(sum_partials(ctx, (int)nbk, 3 * kF, (const float*)net->part,
                     net->grads + off_win(), 0));
   }
   if (loss_h) {
