@@ -29,13 +29,17 @@
 // R_l, P_l come from the caller (CSR).  It runs once per operator and per
 // training step; the per-iteration application is the V-cycle above.
 //
-// GEMMs (all K = 64): mma.sync m16n8k16 BF16 -> FP32 tensor-core tiles; the
-// weight gradients X^T G use ldmatrix.trans.  Aggregation / transfers: CSR
+// GEMMs on the 5th-generation tensor cores (tcgen05.mma, BF16 -> FP32 in
+// TMEM, operand tiles by TMA): the row GEMMs of the forward pass and of the
+// backward dX (K = 64), and the weight gradients X^T G (64 x 64 results
+// summed over all rows, MN-major operands).  Aggregation / transfers: CSR
 // SpMM over 64-wide rows.  Training: the mean relative energy norm of the
 // error propagation, ||(I - M A) e||_A^2 / ||e||_A^2 over (r = A e, e) pairs
 // (A in FP32), back-propagated through the adjoint V-cycle; Adam on FP32
 // master weights.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -46,7 +50,6 @@
 namespace afem {
 
 constexpr int kF = 64;                 // hidden width
-constexpr int kGemmRows = 128;         // rows per GEMM block (8 warps x 16)
 constexpr int kMaxLevels = 12;
 constexpr int kMaxBatch = 64;
 constexpr float kLogitTheta = 1.38629436f;   // log(0.8 / 0.2): untrained weight = 0.8 of the l1 cap
@@ -54,164 +57,371 @@ constexpr float kLogitTheta = 1.38629436f;   // log(0.8 / 0.2): untrained weight
 typedef __nv_bfloat16 bf16;
 
 // ---------------------------------------------------------------------------
-// Tensor-core helpers (PTX mma.sync / ldmatrix).
-
-__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ void ldmatrix_x4_trans(uint32_t r[4], const void* smem_row) {
-  unsigned addr = (unsigned)__cvta_generic_to_shared(smem_row);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(addr));
-}
-
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t*>(&v);
 }
 
 // ---------------------------------------------------------------------------
-// Row GEMM: Y[M x 64] = act( X1 B1 + X2 B2 + bias ), X in BF16 (row-major,
-// 64 columns), B given transposed as Bt[n][k] (64 x 64 BF16).  Each warp
-// computes 16 rows x 64 columns (8 n-tiles x 4 k-steps of m16n8k16).
-// Output BF16 (Yb) and/or FP32 (Yf, optionally accumulated).
-template <bool TWO, bool RELU>
-__global__ void __launch_bounds__(256) k_row_gemm(int M, const bf16* __restrict__ X1, const bf16* __restrict__ B1t,
-                                                  const bf16* __restrict__ X2, const bf16* __restrict__ B2t,
-                                                  const float* __restrict__ bias, bf16* __restrict__ Yb,
-                                                  float* __restrict__ Yf, int accumulate) {
-  __shared__ uint32_t sB1[kF * kF / 2];
-  __shared__ uint32_t sB2[TWO ? kF * kF / 2 : 1];
-  for (int i = threadIdx.x; i < kF * kF / 2; i += blockDim.x) {
-    sB1[i] = reinterpret_cast<const uint32_t*>(B1t)[i];
-    if (TWO) sB2[i] = reinterpret_cast<const uint32_t*>(B2t)[i];
-  }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  for (int64_t r0 = (int64_t)blockIdx.x * kGemmRows + warp * 16; r0 < M; r0 += (int64_t)gridDim.x * kGemmRows) {
-    float acc[8][4];
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-      const float b0 = bias ? bias[nt * 8 + 2 * t] : 0.f, b1 = bias ? bias[nt * 8 + 2 * t + 1] : 0.f;
-      acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
-    }
-    const int64_t ra = r0 + g, rb = r0 + g + 8;
-    const bool va = ra < M, vb = rb < M;
-#pragma unroll
-    for (int src = 0; src < (TWO ? 2 : 1); ++src) {
-      const uint32_t* X = reinterpret_cast<const uint32_t*>(src == 0 ? X1 : X2);
-      const uint32_t* sB = src == 0 ? sB1 : sB2;
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-        const int kw = ks * 8 + t;   // 32-bit word index of columns (16 ks + 2 t)
-        uint32_t a[4];
-        a[0] = va ? __ldg(X + ra * 32 + kw) : 0u;
-        a[1] = vb ? __ldg(X + rb * 32 + kw) : 0u;
-        a[2] = va ? __ldg(X + ra * 32 + kw + 4) : 0u;
-        a[3] = vb ? __ldg(X + rb * 32 + kw + 4) : 0u;
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-          uint32_t b[2];
-          b[0] = sB[(nt * 8 + g) * 32 + kw];
-          b[1] = sB[(nt * 8 + g) * 32 + kw + 4];
-          mma_bf16(acc[nt], a, b);
-        }
-      }
-    }
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-      float c0 = acc[nt][0], c1 = acc[nt][1], c2 = acc[nt][2], c3 = acc[nt][3];
-      if (RELU) {
-        c0 = fmaxf(c0, 0.f); c1 = fmaxf(c1, 0.f); c2 = fmaxf(c2, 0.f); c3 = fmaxf(c3, 0.f);
-      }
-      const int col = nt * 8 + 2 * t;
-      if (Yb) {
-        if (va) reinterpret_cast<uint32_t*>(Yb)[ra * 32 + col / 2] = pack_bf16(c0, c1);
-        if (vb) reinterpret_cast<uint32_t*>(Yb)[rb * 32 + col / 2] = pack_bf16(c2, c3);
-      }
-      if (Yf) {
-        if (va) {
-          float2* p = reinterpret_cast<float2*>(Yf + ra * kF + col);
-          float2 o = accumulate ? *p : make_float2(0.f, 0.f);
-          *p = make_float2(o.x + c0, o.y + c1);
-        }
-        if (vb) {
-          float2* p = reinterpret_cast<float2*>(Yf + rb * kF + col);
-          float2 o = accumulate ? *p : make_float2(0.f, 0.f);
-          *p = make_float2(o.x + c2, o.y + c3);
-        }
-      }
-    }
+// Row GEMM on the 5th-generation tensor cores:
+//   Y[M x 64] = act( X1 B1 + X2 B2 + bias ),  X in BF16 (row-major, 64 columns),
+// B given transposed as Bt[n][k] (64 x 64 BF16, i.e. K-major), FP32 accumulate;
+// output BF16 (Yb) and/or FP32 (Yf, optionally accumulated).
+//
+// Persistent CTAs of 128 threads walk 128-row tiles.  Bt1/Bt2 are staged once
+// into shared memory in the 128-byte-swizzled K-major layout (16-byte chunk c
+// of row r at r * 128 + ((c ^ (r & 7)) << 4), tile base 1024-byte aligned).
+// The X tiles arrive by TMA (cp.async.bulk.tensor.2d, SWIZZLE_128B, the same
+// layout; rows past M read as zero) into a two-stage ring completed on an
+// mbarrier transaction count: the next tile's copy is in flight while the
+// current tile is multiplied and written out.  Thread 0 issues the
+// tcgen05.mma (M = 128, N = 64, K = 16; 4 per product) into a 64-column TMEM
+// accumulator and commits them to a second mbarrier; warp w then reads TMEM
+// lanes 32 w .. 32 w + 31 (its tile rows) with tcgen05.ld and applies bias,
+// ReLU and the stores.  Every mbarrier wait is bounded: on timeout the kernel
+// sets *err, waits (bounded) for its own copy in flight, frees its TMEM and
+// returns.
+constexpr int kTcRows = 128;                 // rows per tile (MMA M)
+constexpr int kTcTileBytes = kTcRows * 128;  // one BF16 X tile
+constexpr long long kTcWaitCycles = 2000000000ll;
+// kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17,
+// M >> 4 at bit 24.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kF >> 3) << 17) |
+                              ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, 128-byte swizzle, K-major: start address
+// >> 4 (bits 0-13), leading byte offset 16 B (unused for this layout), stride
+// byte offset 1024 B between 8-row groups (bits 32-45), descriptor version 1
+// (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63).  K steps of 16 elements
+// advance the start address by 32 B inside the swizzle atom.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// bounded wait for phase `parity` of an mbarrier; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > kTcWaitCycles) return false;
   }
 }
 
-// Weight gradient partials: P_blk[64 x 64] = X[rows of blk]^T G[rows of blk],
-// X and G BF16 [M x 64].  8 warps: warp w owns output rows 16 (w % 4) .. +16
-// and columns 32 (w / 4) .. +32.  A = X^T and B = G fragments come from
-// shared-memory tiles through ldmatrix.trans.
-constexpr int kDwRows = 128;
-constexpr int kDwPitch = kF + 8;   // padded row (bf16) against bank conflicts
+template <bool TWO>
+__device__ __forceinline__ void tc_load_tile(uint32_t bar, uint32_t dst1, const CUtensorMap* m1, uint32_t dst2,
+                                             const CUtensorMap* m2, int row) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+               "r"((uint32_t)(TWO ? 2 : 1) * kTcTileBytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst1),
+      "l"(reinterpret_cast<uint64_t>(m1)), "r"(0), "r"(row), "r"(bar)
+      : "memory");
+  if (TWO)
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst2),
+        "l"(reinterpret_cast<uint64_t>(m2)), "r"(0), "r"(row), "r"(bar)
+        : "memory");
+}
 
-__global__ void __launch_bounds__(256) k_dw_partial(int M, const bf16* __restrict__ X, const bf16* __restrict__ G,
-                                                    float* __restrict__ partial) {
-  __shared__ __align__(16) bf16 sX[kDwRows * kDwPitch];
-  __shared__ __align__(16) bf16 sG[kDwRows * kDwPitch];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const int i0 = 16 * (warp & 3), j0 = 32 * (warp >> 2);
-  float acc[4][4] = {};
-  for (int64_t base = (int64_t)blockIdx.x * kDwRows; base < M; base += (int64_t)gridDim.x * kDwRows) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < kDwRows * (kF / 8); e += blockDim.x) {
-      const int r = e / (kF / 8), c8 = (e % (kF / 8)) * 8;
-      const int64_t gr = base + r;
-      uint4 xv = make_uint4(0, 0, 0, 0), gv = make_uint4(0, 0, 0, 0);
-      if (gr < M) {
-        xv = *reinterpret_cast<const uint4*>(X + gr * kF + c8);
-        gv = *reinterpret_cast<const uint4*>(G + gr * kF + c8);
+__device__ __forceinline__ void tc_stage_weights(const bf16* __restrict__ Bt, uint8_t* sB) {
+  for (int e = threadIdx.x; e < kF * 8; e += blockDim.x) {
+    const int r = e >> 3, c = e & 7;
+    const uint4 v = *reinterpret_cast<const uint4*>(Bt + r * kF + c * 8);
+    *reinterpret_cast<uint4*>(sB + r * 128 + ((c ^ (r & 7)) << 4)) = v;
+  }
+}
+
+template <bool TWO>
+constexpr int tc_smem_bytes() {
+  // weights, two X stages, barriers + TMEM slot, bias; plus 1024 for the alignment of the base
+  return (TWO ? 2 : 1) * kF * 128 + 2 * (TWO ? 2 : 1) * kTcTileBytes + 64 + kF * 4 + 1024;
+}
+
+template <bool TWO, bool RELU>
+__global__ void __launch_bounds__(128) k_row_gemm(const __grid_constant__ CUtensorMap mX1,
+                                                  const __grid_constant__ CUtensorMap mX2, int M,
+                                                  const bf16* __restrict__ B1t, const bf16* __restrict__ B2t,
+                                                  const float* __restrict__ bias, bf16* __restrict__ Yb,
+                                                  float* __restrict__ Yf, int accumulate, int* __restrict__ err) {
+  extern __shared__ uint8_t tc_dyn[];
+  uint8_t* const base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_dyn) + 1023) & ~(uintptr_t)1023);
+  constexpr int NP = TWO ? 2 : 1;
+  uint8_t* const sB = base;                                   // NP x 8 KB
+  uint8_t* const sX = base + NP * kF * 128;                   // [stage][product] 16 KB tiles
+  uint64_t* const bars = reinterpret_cast<uint64_t*>(sX + 2 * NP * kTcTileBytes);   // full[2], mma
+  uint32_t* const tslot = reinterpret_cast<uint32_t*>(bars + 3);
+  float* const sbias = reinterpret_cast<float*>(bars + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntiles = (M + kTcRows - 1) / kTcRows;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(tslot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 3; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + b)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_stage_weights(B1t, sB);
+  if (TWO) tc_stage_weights(B2t, sB + kF * 128);
+  if (tid < kF) sbias[tid] = bias ? bias[tid] : 0.f;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t full0 = smem_u32(bars), mma_bar = smem_u32(bars + 2);
+  auto stage_x = [&](int st, int p) { return smem_u32(sX + (st * NP + p) * kTcTileBytes); };
+
+  // per stage (thread 0): a copy issued and not yet waited for, and the completed waits (phase parity)
+  bool outstanding[2] = {false, false};
+  uint32_t uses[2] = {0u, 0u};
+  if (tid == 0 && (int)blockIdx.x < ntiles) {
+    tc_load_tile<TWO>(full0, stage_x(0, 0), &mX1, stage_x(0, 1), &mX2, blockIdx.x * kTcRows);
+    outstanding[0] = true;
+  }
+  bool failed = false;
+  int it = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int st = it & 1;
+    bool ok = true;
+    if (tid == 0) {
+      const int next = tile + gridDim.x;
+      // stage st ^ 1 was last read by the previous tile's MMAs, complete before the barrier that ended it
+      if (next < ntiles) {
+        tc_load_tile<TWO>(full0 + 8 * (st ^ 1), stage_x(st ^ 1, 0), &mX1, stage_x(st ^ 1, 1), &mX2, next * kTcRows);
+        outstanding[st ^ 1] = true;
       }
-      *reinterpret_cast<uint4*>(sX + r * kDwPitch + c8) = xv;
-      *reinterpret_cast<uint4*>(sG + r * kDwPitch + c8) = gv;
-    }
-    __syncthreads();
-#pragma unroll 2
-    for (int k0 = 0; k0 < kDwRows; k0 += 16) {
-      // A = X^T (16 i x 16 k): blocks (i0..+8, k0..+8), (i0+8.., k0..), (i0.., k0+8..), (i0+8.., k0+8..)
-      uint32_t a[4];
-      {
-        const int q = lane >> 3, rr = lane & 7;
-        const int krow = k0 + rr + ((q >> 1) ? 8 : 0), icol = i0 + ((q & 1) ? 8 : 0);
-        ldmatrix_x4_trans(a, sX + krow * kDwPitch + icol);
-      }
+      ok = mbar_wait(full0 + 8 * st, uses[st] & 1u);
+      if (ok) {
+        ++uses[st];
+        outstanding[st] = false;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-      for (int np = 0; np < 2; ++np) {
-        // B = G (16 k x 16 j) for two n-tiles: blocks (k0.., j), (k0+8.., j), (k0.., j+8), (k0+8.., j+8)
-        uint32_t b4[4];
-        const int q = lane >> 3, rr = lane & 7;
-        const int krow = k0 + rr + ((q & 1) ? 8 : 0), jcol = j0 + 16 * np + ((q >> 1) ? 8 : 0);
-        ldmatrix_x4_trans(b4, sG + krow * kDwPitch + jcol);
-        uint32_t b0[2] = {b4[0], b4[1]}, b1[2] = {b4[2], b4[3]};
-        mma_bf16(acc[2 * np], a, b0);
-        mma_bf16(acc[2 * np + 1], a, b1);
+        for (int p = 0; p < NP; ++p)
+#pragma unroll
+          for (int kk = 0; kk < kF / 16; ++kk) {
+            const uint64_t ad = sw128_desc(stage_x(st, p) + 32 * kk);
+            const uint64_t bd = sw128_desc(smem_u32(sB + p * kF * 128) + 32 * kk);
+            const uint32_t acc = (p | kk) != 0;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc)
+                : "memory");
+          }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_bar)
+                     : "memory");
       }
+    }
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    ok = __all_sync(0xffffffffu, mbar_wait(mma_bar, it & 1));
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    float v[kF];
+#pragma unroll
+    for (int q = 0; q < kF / 16; ++q) {
+      uint32_t r[16];
+      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + 16 * q;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(ta));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[16 * q + j] = __uint_as_float(r[j]) + sbias[16 * q + j];
+    }
+    const int64_t row = (int64_t)tile * kTcRows + 32 * warp + lane;
+    if (row < M) {
+      if (RELU)
+#pragma unroll
+        for (int j = 0; j < kF; ++j) v[j] = fmaxf(v[j], 0.f);
+      if (Yb) {
+        uint4* dst = reinterpret_cast<uint4*>(Yb + row * kF);
+#pragma unroll
+        for (int c = 0; c < kF / 8; ++c)
+          dst[c] = make_uint4(pack_bf16(v[8 * c], v[8 * c + 1]), pack_bf16(v[8 * c + 2], v[8 * c + 3]),
+                              pack_bf16(v[8 * c + 4], v[8 * c + 5]), pack_bf16(v[8 * c + 6], v[8 * c + 7]));
+      }
+      if (Yf) {
+        float4* dst = reinterpret_cast<float4*>(Yf + row * kF);
+#pragma unroll
+        for (int c = 0; c < kF / 4; ++c) {
+          float4 o = accumulate ? dst[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+          dst[c] = make_float4(o.x + v[4 * c], o.y + v[4 * c + 1], o.z + v[4 * c + 2], o.w + v[4 * c + 3]);
+        }
+      }
+    }
+    // TMEM is overwritten by the next tile's MMAs only after every warp has read it
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (failed) {
+    if (tid == 0) {
+      atomicExch(err, 1);
+      for (int b = 0; b < 2; ++b)   // our own copies still in flight
+        if (outstanding[b]) (void)mbar_wait(full0 + 8 * b, uses[b] & 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+}
+
+// Weight-gradient partials on the tensor cores: per CTA
+//   P[128 x 64] = [X1^T ; X2^T] G   summed over its 128-row tiles,
+// X1, X2, G BF16 [M x 64] row-major (P rows 0..63: X1^T G, rows 64..127: X2^T G,
+// FP32 out at partial[blockIdx.x]).  The reduction runs over rows, so both
+// operands are MN-major: a 128-row TMA tile with the 128-byte swizzle is one
+// MN-major swizzle atom (64 elements along M or N, 8-row K groups 1024 B
+// apart), and A stacks the X1 and X2 tiles as two atoms along M (leading byte
+// offset = one tile).  Each K step of 16 rows advances the start addresses by
+// 2048 B.  A two-stage TMA ring (full / empty mbarriers): the next tile's
+// copy runs while the current tile is multiplied, and a stage is refilled
+// once the MMAs that read it have committed.  The accumulator stays in TMEM
+// across the CTA's tiles; bounded waits as in k_row_gemm.
+constexpr int kDwSmem = 2 * 3 * kTcTileBytes + 64 + 1024;
+// kind::f16, D FP32, A and B BF16 and MN-major (bits 15, 16), N = 64, M = 128
+constexpr uint32_t kDwIdesc = kTcIdesc | (1u << 15) | (1u << 16);
+
+__device__ __forceinline__ uint64_t mn128_desc(uint32_t addr, uint32_t atom_stride) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((atom_stride >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__global__ void __launch_bounds__(128) k_dw_grad(const __grid_constant__ CUtensorMap mX1,
+                                                 const __grid_constant__ CUtensorMap mX2,
+                                                 const __grid_constant__ CUtensorMap mG, int M,
+                                                 float* __restrict__ partial, int* __restrict__ err) {
+  extern __shared__ uint8_t tc_dyn[];
+  uint8_t* const base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_dyn) + 1023) & ~(uintptr_t)1023);
+  // stage s: X1 tile, X2 tile (the two A atoms, adjacent), G tile
+  uint64_t* const bars = reinterpret_cast<uint64_t*>(base + 2 * 3 * kTcTileBytes);   // full[2], empty[2]
+  uint32_t* const tslot = reinterpret_cast<uint32_t*>(bars + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntiles = (M + kTcRows - 1) / kTcRows;
+  const int nlocal = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;   // >= 1 (grid <= ntiles)
+  auto tile_at = [&](int st, int p) { return smem_u32(base + (st * 3 + p) * kTcTileBytes); };
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(tslot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 4; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + b)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 2);
+
+  bool ok = true;
+  if (tid == 0) {
+    bool loaded[2] = {false, false}, committed[2] = {false, false};
+    uint32_t full_uses[2] = {0u, 0u}, empty_uses[2] = {0u, 0u};
+    auto load = [&](int st, int local) {
+      const int row = (blockIdx.x + local * gridDim.x) * kTcRows;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full0 + 8 * st),
+                   "r"((uint32_t)3 * kTcTileBytes)
+                   : "memory");
+      const CUtensorMap* maps[3] = {&mX1, &mX2, &mG};
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+                "r"(tile_at(st, p)),
+            "l"(reinterpret_cast<uint64_t>(maps[p])), "r"(0), "r"(row), "r"(full0 + 8 * st)
+            : "memory");
+      loaded[st] = true;
+    };
+    load(0, 0);
+    for (int it = 0; it < nlocal && ok; ++it) {
+      const int st = it & 1;
+      if (it + 1 < nlocal) {   // refill the other stage once the MMAs of tile it - 1 are done with it
+        if (committed[st ^ 1]) {
+          ok = mbar_wait(empty0 + 8 * (st ^ 1), empty_uses[st ^ 1] & 1u);
+          if (!ok) break;
+          ++empty_uses[st ^ 1];
+          committed[st ^ 1] = false;
+        }
+        load(st ^ 1, it + 1);
+      }
+      ok = mbar_wait(full0 + 8 * st, full_uses[st] & 1u);
+      if (!ok) break;
+      ++full_uses[st];
+      loaded[st] = false;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < kTcRows / 16; ++kk) {
+        const uint64_t ad = mn128_desc(tile_at(st, 0) + 2048 * kk, kTcTileBytes);
+        const uint64_t bd = mn128_desc(tile_at(st, 2) + 2048 * kk, 1024);   // one atom along N
+        const uint32_t acc = (it | kk) != 0;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(kDwIdesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * st)
+                   : "memory");
+      committed[st] = true;
+    }
+    // the last MMAs (and, after a failure, our own copies in flight)
+    for (int b = 0; b < 2; ++b) {
+      if (committed[b]) ok = mbar_wait(empty0 + 8 * b, empty_uses[b] & 1u) && ok;
+      if (loaded[b]) (void)mbar_wait(full0 + 8 * b, full_uses[b] & 1u);
+    }
+    if (!ok) atomicExch(err, 1);
+  }
+  ok = __syncthreads_and(tid == 0 ? ok : 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    float* out = partial + (int64_t)blockIdx.x * 2 * kF * kF + (32 * warp + lane) * kF;
+#pragma unroll
+    for (int q = 0; q < kF / 16; ++q) {
+      uint32_t r[16];
+      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + 16 * q;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(ta));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      float4* o4 = reinterpret_cast<float4*>(out + 16 * q);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        o4[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]), __uint_as_float(r[4 * j + 2]),
+                            __uint_as_float(r[4 * j + 3]));
     }
   }
-  float* out = partial + (int64_t)blockIdx.x * kF * kF;
-#pragma unroll
-  for (int nt = 0; nt < 4; ++nt) {
-    const int col = j0 + nt * 8 + 2 * t;
-    out[(i0 + g) * kF + col] = acc[nt][0];
-    out[(i0 + g) * kF + col + 1] = acc[nt][1];
-    out[(i0 + g + 8) * kF + col] = acc[nt][2];
-    out[(i0 + g + 8) * kF + col + 1] = acc[nt][3];
-  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
 
 // out[e] (+)= sum_b partial[b][e] in a fixed order (deterministic).  A block
@@ -784,6 +994,7 @@ using namespace afem;
 
 namespace afem {
 struct FcgWork;
+static void free_fcg_work(FcgWork* w);   // defined with FcgWork (its destructor frees the captured graph)
 }
 
 struct CsrLevel {
@@ -807,6 +1018,7 @@ struct afem_mpnn_s {
   CsrLevel Ac[kMaxLevels];       // Galerkin operators A_l, FP32 values (Ac[0]: the matrix on the level-0 graph)
   double* ac64[kMaxLevels] = {};  // FP64 values of A_l, l >= 1
   int* missing = nullptr;        // set by k_rap when a product entry falls outside the caller's pattern
+  int* tc_err = nullptr;         // set by k_row_gemm when one of its bounded mbarrier waits runs out
   int max_batch = 1;
   // parameters (FP32 master, flat): W_in[2][64], b_in[64], per layer W1, W2 [64][64], b[64],
   // then per level a head w[64], beta.  Levels l >= NL have no layer: o_l = h_l = R o_{l-1}.
@@ -945,8 +1157,64 @@ static afem_status sweep(afem_mpnn net, const CsrLevel* M, int batch, const floa
   return AFEM_OK;
 }
 
-static unsigned gemm_grid(afem_context ctx, int64_t M) {
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((M + kGemmRows - 1) / kGemmRows, (int64_t)ctx->sm_count * 8));
+// TMA descriptor of a row-major [rows x 64] BF16 matrix: 128-row boxes, 128-byte swizzle (the layout k_row_gemm's
+// MMAs read); rows past the end read as zero.  cuTensorMapEncodeTiled comes from the driver through the runtime.
+static afem_status rows64_map(const bf16* base, int64_t rows, CUtensorMap* map) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return fail(AFEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const cuuint64_t dims[2] = {(cuuint64_t)kF, (cuuint64_t)std::max<int64_t>(rows, 1)};
+  const cuuint64_t strides[1] = {(cuuint64_t)kF * sizeof(bf16)};
+  const cuuint32_t box[2] = {(cuuint32_t)kF, (cuuint32_t)kTcRows};
+  const cuuint32_t estride[2] = {1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(base), dims, strides, box,
+                            estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(AFEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return AFEM_OK;
+}
+
+// Y = act(X1 B1 [+ X2 B2] + bias) over M rows on the tensor cores (k_row_gemm); at most 4 CTAs per SM
+// (4 x 64 TMEM columns of the 512).
+template <bool TWO, bool RELU>
+static afem_status row_gemm(afem_mpnn net, int64_t M, const bf16* X1, const bf16* B1t, const bf16* X2,
+                            const bf16* B2t, const float* bias, bf16* Yb, float* Yf, int accumulate) {
+  afem_context ctx = net->ctx;
+  if (M <= 0) return AFEM_OK;
+  CUtensorMap m1, m2;
+  AFEM_TRY(rows64_map(X1, M, &m1));
+  if (TWO) AFEM_TRY(rows64_map(X2, M, &m2));
+  else m2 = m1;
+  constexpr int smem = tc_smem_bytes<TWO>();
+  static const cudaError_t attr = cudaFuncSetAttribute(k_row_gemm<TWO, RELU>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(k_row_gemm)", __FILE__, __LINE__);
+  const int64_t tiles = (M + kTcRows - 1) / kTcRows;
+  const unsigned grid = (unsigned)std::min<int64_t>(tiles, (int64_t)ctx->sm_count * (TWO ? 2 : 4));
+  k_row_gemm<TWO, RELU><<<grid, 128, smem, ctx->stream>>>(m1, m2, (int)M, B1t, B2t, bias, Yb, Yf, accumulate,
+                                                          net->tc_err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_row_gemm", __FILE__, __LINE__);
+  ++ctx->launches;
+  return AFEM_OK;
+}
+
+// Reports a timed-out tensor-core wait (k_row_gemm) as AFEM_ERR_TIMEOUT.  Reads the flag back (one small
+// synchronous copy), except while the stream is being captured.
+static afem_status check_tc(afem_mpnn net) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  AFEM_CUDA(cudaStreamIsCapturing(net->ctx->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return AFEM_OK;
+  int e = 0;
+  AFEM_TRY(read_scalar(net->ctx, net->tc_err, &e));
+  if (e) return fail(AFEM_ERR_TIMEOUT, "k_row_gemm: a tensor-core mbarrier wait ran out");
+  return AFEM_OK;
 }
 
 // network forward on the coefficient features -> scalings d_l
@@ -960,15 +1228,14 @@ static afem_status features_forward(afem_mpnn net) {
     const int nl = net->n[l];
     if (l < net->NL) {
       AFEM_TRY(spmm<bf16, bf16>(net, net->S[l], net->h[l], net->m[l], 0));
-      AFEM_TRY(launch(ctx, k_row_gemm<true, true>, gemm_grid(ctx, nl), 256, 0, nl, (const bf16*)net->h[l],
-                      (const bf16*)(net->Wt + (2 * l) * kF * kF), (const bf16*)net->m[l],
-                      (const bf16*)(net->Wt + (2 * l + 1) * kF * kF), (const float*)(net->params + off_b(l)),
-                      net->o[l], (float*)nullptr, 0));
+      AFEM_TRY((row_gemm<true, true>(net, nl, net->h[l], net->Wt + (2 * l) * kF * kF, net->m[l],
+                                     net->Wt + (2 * l + 1) * kF * kF, net->params + off_b(l), net->o[l], nullptr, 0)));
     }
     if (l + 1 < L) AFEM_TRY(spmm<bf16, bf16>(net, net->R[l], net->o[l], net->h[l + 1], 0));
     AFEM_TRY(launch(ctx, k_head, grid_for(ctx, nl, 256, 8), 256, 0, nl, (const bf16*)net->o[l],
                     (const float*)(net->params + off_head(net->NL, l)), (const float*)net->base[l], net->d[l]));
   }
+  AFEM_TRY(check_tc(net));
   net->scalings_valid = true;
   return AFEM_OK;
 }
@@ -1104,13 +1371,25 @@ static afem_status sum_partials(afem_context ctx, int nparts, int nelem, const f
                 accumulate);
 }
 
-// dW = X^T G summed over M rows into dst (FP32 64x64), deterministic
-static afem_status dw_gemm(afem_mpnn net, int64_t M, const bf16* X, const bf16* G, float* dst) {
+// [dW1 ; dW2] = [X1^T G ; X2^T G] summed over M rows into dst (FP32 2 x 64 x 64, dW2 right after dW1),
+// deterministic: per-CTA partials on the tensor cores (k_dw_grad), then a fixed-order sum
+static afem_status dw_gemm2(afem_mpnn net, int64_t M, const bf16* X1, const bf16* X2, const bf16* G, float* dst) {
   afem_context ctx = net->ctx;
-  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>((M + kDwRows - 1) / kDwRows, (int64_t)ctx->sm_count * 2));
-  AFEM_TRY(ensure_part(net, (int64_t)nb * kF * kF));
-  AFEM_TRY(launch(ctx, k_dw_partial, nb, 256, 0, (int)M, X, G, net->part));
-  return sum_partials(ctx, nb, kF * kF, (const float*)net->part, dst, 0);
+  if (M <= 0) return AFEM_OK;
+  const int nb = (int)std::min<int64_t>((M + kTcRows - 1) / kTcRows, (int64_t)ctx->sm_count * 2);
+  AFEM_TRY(ensure_part(net, (int64_t)nb * 2 * kF * kF));
+  CUtensorMap m1, m2, mg;
+  AFEM_TRY(rows64_map(X1, M, &m1));
+  AFEM_TRY(rows64_map(X2, M, &m2));
+  AFEM_TRY(rows64_map(G, M, &mg));
+  static const cudaError_t attr = cudaFuncSetAttribute(k_dw_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       kDwSmem);
+  if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(k_dw_grad)", __FILE__, __LINE__);
+  k_dw_grad<<<nb, 128, kDwSmem, ctx->stream>>>(m1, m2, mg, (int)M, net->part, net->tc_err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "k_dw_grad", __FILE__, __LINE__);
+  ++ctx->launches;
+  return sum_partials(ctx, nb, 2 * kF * kF, (const float*)net->part, dst, 0);
 }
 
 // loss and gradients of the mean relative squared error over (r, e)
@@ -1158,15 +1437,12 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
     AFEM_TRY(launch(ctx, k_relu_grad, nbk, 256, 0, M, (const float*)net->dO[l], (const bf16*)net->o[l], net->Gb,
                     net->part));
     AFEM_TRY(sum_partials(ctx, (int)nbk, kF, (const float*)net->part, net->grads + off_b(l), 0));
-    AFEM_TRY(dw_gemm(net, M, net->h[l], net->Gb, net->grads + off_w1(l)));
-    AFEM_TRY(dw_gemm(net, M, net->m[l], net->Gb, net->grads + off_w2(l)));
+    AFEM_TRY(dw_gemm2(net, M, net->h[l], net->m[l], net->Gb, net->grads + off_w1(l)));   // dW2 at off_w2 = off_w1 + 64^2
     // dh_l = G W1^T + S_l^T (G W2^T)   (S_l symmetric)
-    AFEM_TRY(launch(ctx, k_row_gemm<false, false>, gemm_grid(ctx, M), 256, 0, (int)M, (const bf16*)net->Gb,
-                    (const bf16*)(net->Wn + (2 * l) * kF * kF), (const bf16*)nullptr, (const bf16*)nullptr,
-                    (const float*)nullptr, (bf16*)nullptr, net->dH[l], 0));
-    AFEM_TRY(launch(ctx, k_row_gemm<false, false>, gemm_grid(ctx, M), 256, 0, (int)M, (const bf16*)net->Gb,
-                    (const bf16*)(net->Wn + (2 * l + 1) * kF * kF), (const bf16*)nullptr, (const bf16*)nullptr,
-                    (const float*)nullptr, (bf16*)nullptr, net->ftmp, 0));
+    AFEM_TRY((row_gemm<false, false>(net, M, net->Gb, net->Wn + (2 * l) * kF * kF, nullptr, nullptr, nullptr,
+                                     nullptr, net->dH[l], 0)));
+    AFEM_TRY((row_gemm<false, false>(net, M, net->Gb, net->Wn + (2 * l + 1) * kF * kF, nullptr, nullptr, nullptr,
+                                     nullptr, net->ftmp, 0)));
     AFEM_TRY(spmm<float, float>(net, net->S[l], net->ftmp, net->dH[l], 1));
     if (l > 0) AFEM_TRY(spmm<float, float>(net, net->Rt[l - 1], net->dH[l], net->dO[l - 1], 1));
   }
@@ -1186,7 +1462,7 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
     for (int b = 0; b < batch; ++b) l += hs[b * 4 + 1] / (hs[b * 4] + 1e-300);
     *loss_h = l / batch;
   }
-  return AFEM_OK;
+  return check_tc(net);
 }
 
 }  // namespace afem
@@ -1255,8 +1531,10 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
       (st = dalloc(net, n0 * kF, &net->Gb)) || (st = dalloc(net, n0 * kF, &net->ftmp)) ||
       (st = dalloc(net, B * 4, &net->sums)) || (st = dalloc(net, n0, &net->r32)) || (st = dalloc(net, n0, &net->z32)) ||
       (st = dalloc(net, (size_t)std::max<int64_t>(net->S[0].nnz, 1), &net->a32)) || (st = dalloc(net, B * n0, &net->tmpB)) ||
-      (st = dalloc(net, 1, &net->missing)))
+      (st = dalloc(net, 1, &net->missing)) || (st = dalloc(net, 1, &net->tc_err)))
     return cleanup(st);
+  if (cudaMemsetAsync(net->tc_err, 0, sizeof(int), net->ctx->stream) != cudaSuccess)
+    return cleanup(fail(AFEM_ERR_CUDA, "afem_mpnn_create: cudaMemsetAsync"));
   net->h[0] = net->a_in;
   for (int l = 0; l < nb_levels; ++l) {
     const size_t nl = net->n[l];
@@ -1285,7 +1563,7 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
 afem_status afem_mpnn_destroy(afem_mpnn net) {
   if (!net) return AFEM_OK;
   cudaStream_t s = net->ctx->stream;
-  delete net->fcg;
+  free_fcg_work(net->fcg);
   for (void* p : net->owned) cudaFreeAsync(p, s);
   cudaStreamSynchronize(s);
   delete net;
@@ -1614,6 +1892,8 @@ struct FcgWork {
   GraphChunk* graph = nullptr;
   ~FcgWork() { delete graph; }
 };
+
+static void free_fcg_work(FcgWork* w) { delete w; }
 
 static afem_status fcg_work(afem_mpnn net, FcgWork** out) {
   if (!net->fcg) {

@@ -608,7 +608,7 @@ def run_learned(args):
         "cpu_oracle_fp64_cg_jacobi": oracle_solve,
         "speedup_vs_plain_fp64_cg_jacobi": cg_jac.solve_ms / kept.solve_ms,
         "speedup_vs_plain_fp64_cg_none": cg_none.solve_ms / kept.solve_ms,
-        "network": ("6 message-passing layers, width 64, BF16 mma.sync GEMMs, FP32 accumulate; predicts the "
+        "network": ("6 message-passing layers, width 64, BF16 tcgen05 GEMMs (TMA-fed, FP32 accumulate in TMEM); predicts the "
                     "per-node smoother weights of a V(1,1)-cycle on a 9-level Galerkin hierarchy"),
         "training": {"pairs": 2000, "pair_generation_s": pairs_s, "train_s": train_s, "loss": rep["loss"],
                      "fcg_iterations_untrained": rep["iterations_untrained"],
