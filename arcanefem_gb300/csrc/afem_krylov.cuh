@@ -52,35 +52,6 @@ __device__ __forceinline__ double row_dot(int row, const int32_t* __restrict__ r
   return s;
 }
 
-// FP32 row dot product accumulated in FP32 (inner solve).
-template <int G>
-__device__ __forceinline__ float row_dot_f(int row, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
-                                           const float* __restrict__ vals, const float* __restrict__ x, int lane) {
-  if constexpr (G == 1) {
-    float s = 0.f;
-    const int32_t e = __ldg(rp + row + 1);
-    for (int32_t k = __ldg(rp + row); k < e; k += kRowChunk) {
-      int32_t c[kRowChunk];
-      float a[kRowChunk];
-#pragma unroll
-      for (int u = 0; u < kRowChunk; ++u) {
-        const bool in = k + u < e;
-        c[u] = in ? __ldg(cols + k + u) : row;
-        a[u] = in ? __ldg(vals + k + u) : 0.f;
-      }
-#pragma unroll
-      for (int u = 0; u < kRowChunk; ++u) s = fmaf(a[u], __ldg(x + c[u]), s);
-    }
-    return s;
-  }
-  float s = 0.f;
-  const int32_t e = __ldg(rp + row + 1);
-  for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s = fmaf(__ldg(vals + k), __ldg(x + __ldg(cols + k)), s);
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
-  return s;
-}
-
 // ---------------------------------------------------------------------------
 // Last-block finalize helper: every block publishes partials[blockIdx.x * W + w];
 // returns true in the (single) last block, after which all partials are visible.
@@ -106,15 +77,6 @@ __device__ __forceinline__ double reduce_partials(const double* partials, int np
 
 // ---------------------------------------------------------------------------
 // Host side.
-
-inline int lanes_per_row(int n, int64_t nnz) {
-  double avg = n > 0 ? (double)nnz / n : 1.0;
-  if (avg <= 24) return 1;   // chunked thread-per-row keeps more loads in flight
-  if (avg <= 6) return 4;
-  if (avg <= 20) return 8;
-  if (avg <= 48) return 16;
-  return 32;
-}
 
 // FP64 rows: on GB300 a warp FP64 instruction costs the same whatever its
 // active lanes, so the shuffle-tree reduction and the lane-0 dot-product

@@ -173,7 +173,31 @@ __global__ void __launch_bounds__(kSolveBlock) k_cg_update(int n, double* __rest
   __shared__ double sh[kSolveBlock / 32];
   const double alpha = ((volatile CgState*)st)->alpha;
   double rz = 0.0, rr = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // two elements per thread and pass (16-byte accesses: every vector here is
+  // one of the solver's own 256-byte-aligned buffers), then the odd tail
+  const int n2 = n >> 1;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int i = tid; i < n2; i += stride) {
+    const double2 pv = reinterpret_cast<const double2*>(p)[i], qv = reinterpret_cast<const double2*>(q)[i];
+    double2 xv = reinterpret_cast<double2*>(x)[i], rv = reinterpret_cast<double2*>(r)[i];
+    xv.x += alpha * pv.x;
+    xv.y += alpha * pv.y;
+    rv.x = rv.x - alpha * qv.x;
+    rv.y = rv.y - alpha * qv.y;
+    double2 zv = rv;
+    if (dinv) {
+      const double2 dv = reinterpret_cast<const double2*>(dinv)[i];
+      zv = make_double2(dv.x * rv.x, dv.y * rv.y);
+    }
+    reinterpret_cast<double2*>(x)[i] = xv;
+    reinterpret_cast<double2*>(r)[i] = rv;
+    reinterpret_cast<double2*>(z)[i] = zv;
+    rz += rv.x * zv.x;
+    rz += rv.y * zv.y;
+    if (!(skip && skip[2 * i])) rr += rv.x * rv.x;
+    if (!(skip && skip[2 * i + 1])) rr += rv.y * rv.y;
+  }
+  for (int i = 2 * n2 + tid; i < n; i += stride) {
     double pi = p[i];
     x[i] += alpha * pi;
     double ri = r[i] - alpha * q[i];
@@ -216,7 +240,15 @@ __global__ void __launch_bounds__(kSolveBlock) k_cg_dir(int n, const double* __r
                                                         const CgState* st) {
   if (((volatile const CgState*)st)->done) return;
   const double beta = ((volatile const CgState*)st)->beta;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
+  const int n2 = n >> 1;   // 16-byte accesses (solver-owned aligned buffers), then the tail
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int i = tid; i < n2; i += stride) {
+    const double2 zv = reinterpret_cast<const double2*>(z)[i];
+    double2 pv = reinterpret_cast<double2*>(p)[i];
+    pv = make_double2(zv.x + beta * pv.x, zv.y + beta * pv.y);
+    reinterpret_cast<double2*>(p)[i] = pv;
+  }
+  for (int i = 2 * n2 + tid; i < n; i += stride) p[i] = z[i] + beta * p[i];
 }
 
 // D^-1 from the diagonal entries (1 where the diagonal is missing or zero).
@@ -240,27 +272,78 @@ __global__ void k_inv_diag(int n, const int32_t* __restrict__ rp, const int32_t*
 // dot products accumulate in FP32 per thread and warp, in FP64 across warps
 // and blocks.
 
-template <int G>
-__global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv(int n, const int32_t* __restrict__ rp,
-                                                          const int32_t* __restrict__ cols,
-                                                          const float* __restrict__ vals, const float* __restrict__ p,
-                                                          float* __restrict__ q, double* partials, CgState* st) {
+// Sliced-ELL copy of the FP32 matrix for the inner SpMV of the mixed solver:
+// 32 consecutive rows per slice, padded to the slice's longest row; entry k
+// of row 32 s + l sits at 32 soff[s] + 32 k + l, so that a warp reads step k
+// of its 32 rows as one coalesced 128-byte segment of columns and one of
+// values, where the thread-per-row CSR walk reads 32 scattered streams.
+// Padding entries carry a zero weight on the row's own column.  Each row's
+// terms are summed in CSR order (fmaf of a zero weight leaves the sum
+// unchanged), the same order as a thread-per-row walk of the CSR rows.
+constexpr int kSlice = 32;
+
+// slen[s] = the longest row of slice s (one warp per slice)
+__global__ void k_slice_len(int n, const int32_t* __restrict__ rp, int32_t* __restrict__ slen) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
+    const int len = row < n ? __ldg(rp + row + 1) - __ldg(rp + row) : 0;
+    const int m = __reduce_max_sync(0xffffffffu, len);
+    if ((row & (kSlice - 1)) == 0) slen[row / kSlice] = m;
+  }
+}
+
+__global__ void k_slice_fill(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                             const double* __restrict__ vals, const int32_t* __restrict__ soff,
+                             int32_t* __restrict__ scols, float* __restrict__ svals) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
+    const int64_t sl = row / kSlice;
+    const int m = soff[sl + 1] - soff[sl];
+    const int64_t base = (int64_t)kSlice * soff[sl] + (row & (kSlice - 1));
+    const int32_t b = row < n ? rp[row] : 0, e = row < n ? rp[row + 1] : 0;
+    for (int k = 0; k < m; ++k) {
+      const bool in = b + k < e;
+      scols[base + (int64_t)kSlice * k] = in ? cols[b + k] : (row < n ? (int32_t)row : 0);
+      svals[base + (int64_t)kSlice * k] = in ? (float)vals[b + k] : 0.f;
+    }
+  }
+}
+
+// q = A p over the sliced copy ; <p, q> -> alpha (as k_cgf_spmv)
+__global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_sl(int n, const int32_t* __restrict__ soff,
+                                                             const int32_t* __restrict__ scols,
+                                                             const float* __restrict__ svals,
+                                                             const float* __restrict__ p, float* __restrict__ q,
+                                                             double* partials, CgState* st) {
   if (((volatile CgState*)st)->done) return;
   __shared__ double sh[kSolveBlock / 32];
-  const int lane = threadIdx.x & (G - 1);
-  const int groups = gridDim.x * (blockDim.x / G);
-  const int nr = n + ((groups - n % groups) % groups);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;   // a multiple of 32: a warp is one slice
+  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
   float pqf = 0.f;
-  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
-    float s = 0.f;
-    if (row < n) s = row_dot_f<G>(row, rp, cols, vals, p, lane);
-    else {
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
+    const int64_t sl = row / kSlice;
+    const int m = __ldg(soff + sl + 1) - __ldg(soff + sl);
+    const int32_t* c = scols + (int64_t)kSlice * __ldg(soff + sl) + (row & (kSlice - 1));
+    const float* a = svals + (c - scols);
+    float acc = 0.f;
+    int k = 0;
+    for (; k + kRowChunk <= m; k += kRowChunk) {
+      int32_t cc[kRowChunk];
+      float aa[kRowChunk];
 #pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+      for (int u = 0; u < kRowChunk; ++u) {
+        cc[u] = __ldg(c + (int64_t)kSlice * (k + u));
+        aa[u] = __ldg(a + (int64_t)kSlice * (k + u));
+      }
+#pragma unroll
+      for (int u = 0; u < kRowChunk; ++u) acc = fmaf(aa[u], __ldg(p + cc[u]), acc);
     }
-    if (row < n && lane == 0) {
-      q[row] = s;
-      pqf = fmaf(p[row], s, pqf);
+    for (; k < m; ++k) acc = fmaf(__ldg(a + (int64_t)kSlice * k), __ldg(p + __ldg(c + (int64_t)kSlice * k)), acc);
+    if (row < n) {
+      q[row] = acc;
+      pqf = fmaf(p[row], acc, pqf);
     }
   }
   const double pq = block_sum_f(pqf, sh);
@@ -376,7 +459,37 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_update(int n, float* __rest
   __shared__ double sh[kSolveBlock / 32];
   const float alpha = (float)((volatile CgState*)st)->alpha;
   float rzf = 0.f, rrf = 0.f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // four elements per thread and pass (16-byte accesses: the vectors are the
+  // solver's own 256-byte-aligned buffers), then the n % 4 tail
+  const int n4 = n >> 2;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int i = tid; i < n4; i += stride) {
+    const float4 pv = reinterpret_cast<const float4*>(p)[i], qv = reinterpret_cast<const float4*>(q)[i];
+    const float4 dv = reinterpret_cast<const float4*>(dinv)[i];
+    float4 xv = reinterpret_cast<float4*>(x)[i], rv = reinterpret_cast<float4*>(r)[i];
+    xv.x = fmaf(alpha, pv.x, xv.x);
+    xv.y = fmaf(alpha, pv.y, xv.y);
+    xv.z = fmaf(alpha, pv.z, xv.z);
+    xv.w = fmaf(alpha, pv.w, xv.w);
+    rv.x = fmaf(-alpha, qv.x, rv.x);
+    rv.y = fmaf(-alpha, qv.y, rv.y);
+    rv.z = fmaf(-alpha, qv.z, rv.z);
+    rv.w = fmaf(-alpha, qv.w, rv.w);
+    const float4 zv = make_float4(dv.x * rv.x, dv.y * rv.y, dv.z * rv.z, dv.w * rv.w);
+    reinterpret_cast<float4*>(x)[i] = xv;
+    reinterpret_cast<float4*>(r)[i] = rv;
+    reinterpret_cast<float4*>(z)[i] = zv;
+    rzf = fmaf(rv.x, zv.x, rzf);
+    rzf = fmaf(rv.y, zv.y, rzf);
+    rzf = fmaf(rv.z, zv.z, rzf);
+    rzf = fmaf(rv.w, zv.w, rzf);
+    const int e = 4 * i;
+    if (!(skip && skip[e])) rrf = fmaf(rv.x, rv.x, rrf);
+    if (!(skip && skip[e + 1])) rrf = fmaf(rv.y, rv.y, rrf);
+    if (!(skip && skip[e + 2])) rrf = fmaf(rv.z, rv.z, rrf);
+    if (!(skip && skip[e + 3])) rrf = fmaf(rv.w, rv.w, rrf);
+  }
+  for (int i = 4 * n4 + tid; i < n; i += stride) {
     x[i] = fmaf(alpha, p[i], x[i]);
     float ri = fmaf(-alpha, q[i], r[i]);
     r[i] = ri;
@@ -415,7 +528,15 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_dir(int n, const float* __r
                                                          const CgState* st) {
   if (((volatile const CgState*)st)->done) return;
   const float beta = (float)((volatile const CgState*)st)->beta;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fmaf(beta, p[i], z[i]);
+  const int n4 = n >> 2;   // 16-byte accesses (solver-owned aligned buffers), then the tail
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int i = tid; i < n4; i += stride) {
+    const float4 zv = reinterpret_cast<const float4*>(z)[i];
+    float4 pv = reinterpret_cast<float4*>(p)[i];
+    pv = make_float4(fmaf(beta, pv.x, zv.x), fmaf(beta, pv.y, zv.y), fmaf(beta, pv.z, zv.z), fmaf(beta, pv.w, zv.w));
+    reinterpret_cast<float4*>(p)[i] = pv;
+  }
+  for (int i = 4 * n4 + tid; i < n; i += stride) p[i] = fmaf(beta, p[i], z[i]);
 }
 
 // Reliable update: r = b - A x (FP64), r32 = (float) r, x32 = 0,
@@ -516,11 +637,16 @@ afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* c
   const unsigned grid_rows = grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned nparts = std::max(grid_rows, grid_vec);
-  size_t need = 5 * align256(sizeof(double) * (size_t)n) + align256(sizeof(double) * 3 * nparts) +
+  size_t need = 6 * align256(sizeof(double) * (size_t)n) + align256(sizeof(double) * 3 * nparts) +
                 align256(sizeof(CgState));
   AFEM_TRY(scratch_reserve(ctx, need));
   double *r, *z, *p, *q, *dinv, *partials;
   CgState* st;
+  // the iterate lives in an aligned scratch copy (16-byte vector accesses in
+  // k_cg_update), copied in here and back to the caller's x at the end
+  double* const x_user = x;
+  AFEM_TRY(scratch_take(ctx, n, &x));
+  AFEM_CUDA(cudaMemcpyAsync(x, x_user, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
   AFEM_TRY(scratch_take(ctx, n, &r));
   AFEM_TRY(scratch_take(ctx, n, &z));
   AFEM_TRY(scratch_take(ctx, n, &p));
@@ -562,6 +688,7 @@ afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* c
     AFEM_CUDA(cudaGraphLaunch(gc.exec, ctx->stream));
     ctx->launches += 3 * chunk;
   }
+  AFEM_CUDA(cudaMemcpyAsync(x_user, x, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
   if (info) {
     info->iterations = hs.iter;
     info->refinements = 0;
@@ -573,22 +700,23 @@ afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* c
 afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals, int64_t nnz,
                      const double* b, double* x, const uint8_t* skip, const afem_solver_options& opt,
                      afem_solve_info* info) {
-  const int G = lanes_per_row(n, nnz);          // FP32 inner SpMV
   const int G64 = lanes_per_row_fp64(n, nnz);   // FP64 outer residual
-  const bool b3 = opt.block_size == 3;          // FP32 3x3-block SpMV
+  const bool b3 = opt.block_size == 3;          // FP32 3x3-block SpMV, else the sliced-ELL scalar SpMV
   AFEM_CHECK_ARG(!b3 || n % 3 == 0, "block_size 3 needs a multiple of 3 rows (%d)", n);
-  const unsigned grid_rows = b3 ? grid_for(ctx, n, kSolveBlock, 8) : grid_for(ctx, (int64_t)n * G, kSolveBlock, 8);
+  const unsigned grid_rows = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned grid_rows64 = grid_for(ctx, (int64_t)n * G64, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned nparts = std::max(std::max(grid_rows, grid_rows64), grid_vec);
-  size_t need = align256(sizeof(float) * (size_t)nnz) + 6 * align256(sizeof(float) * (size_t)n) +
-                align256(sizeof(double) * 3 * nparts) + 2 * align256(sizeof(CgState)) +
-                (b3 ? align256(sizeof(int32_t) * (size_t)(nnz / 9 + 1)) + 256 : 0);
+  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
+  size_t need = 6 * align256(sizeof(float) * (size_t)n) + align256(sizeof(double) * 3 * nparts) +
+                2 * align256(sizeof(CgState)) +
+                (b3 ? align256(sizeof(float) * (size_t)nnz) + align256(sizeof(int32_t) * (size_t)(nnz / 9 + 1)) + 256
+                    : 2 * align256(sizeof(int32_t) * (size_t)(nslice + 1)) + scan_scratch_bytes(nslice));
   AFEM_TRY(scratch_reserve(ctx, need));
-  float *v32, *r32, *z32, *p32, *q32, *x32, *dinv32;
+  float *v32 = nullptr, *r32, *z32, *p32, *q32, *x32, *dinv32;
   double* partials;
   CgState *outer, *inner;
-  AFEM_TRY(scratch_take(ctx, (size_t)nnz, &v32));
+  if (b3) AFEM_TRY(scratch_take(ctx, (size_t)nnz, &v32));
   AFEM_TRY(scratch_take(ctx, n, &r32));
   AFEM_TRY(scratch_take(ctx, n, &z32));
   AFEM_TRY(scratch_take(ctx, n, &p32));
@@ -611,7 +739,34 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     AFEM_TRY(read_scalar(ctx, bad, &hbad));
     AFEM_CHECK_ARG(!hbad, "block_size 3: the CSR pattern is not made of 3x3 blocks");
   }
-  AFEM_TRY(launch(ctx, k_to_f32, grid_for(ctx, nnz, 256), 256, 0, nnz, vals, v32));
+  // the FP32 matrix: values in CSR order for the 3x3-block SpMV, else the sliced-ELL copy (device memory held
+  // for this solve only)
+  struct SlicedCopy {
+    cudaStream_t s;
+    int32_t* cols = nullptr;
+    float* vals = nullptr;
+    ~SlicedCopy() {
+      if (cols) cudaFreeAsync(cols, s);
+      if (vals) cudaFreeAsync(vals, s);
+    }
+  } sliced{ctx->stream};
+  int32_t* soff = nullptr;
+  if (b3) {
+    AFEM_TRY(launch(ctx, k_to_f32, grid_for(ctx, nnz, 256), 256, 0, nnz, vals, v32));
+  } else {
+    int32_t* slen;
+    AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &slen));
+    AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &soff));
+    AFEM_TRY(launch(ctx, k_slice_len, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, slen));
+    AFEM_TRY(exclusive_scan_i32(ctx, slen, soff, nslice));
+    int32_t slots = 0;   // sum of the slice lengths (<= nnz); the copy holds 32 x that many entries
+    AFEM_TRY(read_scalar(ctx, soff + nslice, &slots));
+    const size_t entries = (size_t)kSlice * (size_t)std::max(slots, 1);
+    AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sliced.cols), sizeof(int32_t) * entries, ctx->stream));
+    AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sliced.vals), sizeof(float) * entries, ctx->stream));
+    AFEM_TRY(launch(ctx, k_slice_fill, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, cols, vals,
+                    (const int32_t*)soff, sliced.cols, sliced.vals));
+  }
   AFEM_TRY(launch(ctx, k_inv_diag, grid_vec, kSolveBlock, 0, n, rp, cols, vals, (double*)nullptr, dinv32));
   if (opt.precond != AFEM_PRECOND_JACOBI)  // unpreconditioned inner solve: D^-1 = 1
     AFEM_TRY(launch(ctx, k_fill_f32, grid_for(ctx, n, 256), 256, 0, (int64_t)n, 1.0f, dinv32));
@@ -626,10 +781,9 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
         AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_b3, grid_rows, kSolveBlock, n, rp, (const int32_t*)bcols,
                           (const float*)v32, (const float*)p32, q32, partials, inner));
       else
-        AFEM_TRY(dispatch_g(G, [&](auto g) {
-          return launch_s(ctx, s, k_cgf_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols,
-                          (const float*)v32, (const float*)p32, q32, partials, inner);
-        }));
+        AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_sl, grid_rows, kSolveBlock, n, (const int32_t*)soff,
+                          (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)p32, q32, partials,
+                          inner));
       AFEM_TRY(launch_s(ctx, s, k_cgf_update, grid_vec, kSolveBlock, n, x32, r32, z32, (const float*)p32,
                         (const float*)q32, (const float*)dinv32, skip, partials, inner));
       AFEM_TRY(launch_s(ctx, s, k_cgf_dir, grid_vec, kSolveBlock, n, (const float*)z32, p32, (const CgState*)inner));
