@@ -120,47 +120,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_cg_init(int n, const int32_t* _
   }
 }
 
-// K1: q = A p, <p, q> -> alpha
-template <int G>
-__global__ void __launch_bounds__(kSolveBlock) k_cg_spmv(int n, const int32_t* __restrict__ rp,
-                                                         const int32_t* __restrict__ cols,
-                                                         const double* __restrict__ vals, const double* __restrict__ p,
-                                                         double* __restrict__ q, double* partials, CgState* st) {
-  if (((volatile CgState*)st)->done) return;
-  __shared__ double sh[kSolveBlock / 32];
-  const int lane = threadIdx.x & (G - 1);
-  const int groups = gridDim.x * (blockDim.x / G);
-  const int nr = n + ((groups - n % groups) % groups);
-  double pq = 0.0;
-  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) / G; row < nr; row += groups) {
-    double s = 0.0;
-    if (row < n) s = row_dot<G>(row, rp, cols, vals, p, lane);
-    else {
-#pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
-    }
-    if (row < n && lane == 0) {
-      q[row] = s;
-      pq += p[row] * s;
-    }
-  }
-  pq = block_sum(pq, sh);
-  if (threadIdx.x == 0) partials[blockIdx.x] = pq;
-  if (last_block(&st->ticket[1])) {
-    double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
-    if (threadIdx.x == 0) {
-      st->pq = t;
-      if (!(t > 0.0) || !isfinite(t)) {
-        st->status = AFEM_ERR_BREAKDOWN;
-        st->done = 1;
-        st->alpha = 0.0;
-      } else {
-        st->alpha = st->rz / t;
-      }
-      st->ticket[1] = 0;
-    }
-  }
-}
+// K1 (q = A p, <p, q> -> alpha) is k_cg_spmv_sl, over the sliced-ELL copy below.
 
 // K2: x += alpha p ; r -= alpha q ; z = D^-1 r ; <r,z>, <r,r> -> beta, stop test
 __global__ void __launch_bounds__(kSolveBlock) k_cg_update(int n, double* __restrict__ x, double* __restrict__ r,
@@ -272,7 +232,8 @@ __global__ void k_inv_diag(int n, const int32_t* __restrict__ rp, const int32_t*
 // dot products accumulate in FP32 per thread and warp, in FP64 across warps
 // and blocks.
 
-// Sliced-ELL copy of the FP32 matrix for the inner SpMV of the mixed solver:
+// Sliced-ELL copies of the matrix for the CG SpMVs (FP64 values for the FP64
+// CG, FP32 for the inner CG of the mixed solver):
 // 32 consecutive rows per slice, padded to the slice's longest row; entry k
 // of row 32 s + l sits at 32 soff[s] + 32 k + l, so that a warp reads step k
 // of its 32 rows as one coalesced 128-byte segment of columns and one of
@@ -293,9 +254,10 @@ __global__ void k_slice_len(int n, const int32_t* __restrict__ rp, int32_t* __re
   }
 }
 
+template <class T>
 __global__ void k_slice_fill(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                              const double* __restrict__ vals, const int32_t* __restrict__ soff,
-                             int32_t* __restrict__ scols, float* __restrict__ svals) {
+                             int32_t* __restrict__ scols, T* __restrict__ svals) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
   for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
@@ -306,7 +268,61 @@ __global__ void k_slice_fill(int n, const int32_t* __restrict__ rp, const int32_
     for (int k = 0; k < m; ++k) {
       const bool in = b + k < e;
       scols[base + (int64_t)kSlice * k] = in ? cols[b + k] : (row < n ? (int32_t)row : 0);
-      svals[base + (int64_t)kSlice * k] = in ? (float)vals[b + k] : 0.f;
+      svals[base + (int64_t)kSlice * k] = in ? (T)vals[b + k] : T(0);
+    }
+  }
+}
+
+// FP64 CG K1 over the sliced copy: q = A p, <p, q> -> alpha (the breakdown test as k_cgf_spmv_sl;
+// each row's products are added in CSR order, as in row_dot_chunked)
+__global__ void __launch_bounds__(kSolveBlock) k_cg_spmv_sl(int n, const int32_t* __restrict__ soff,
+                                                            const int32_t* __restrict__ scols,
+                                                            const double* __restrict__ svals,
+                                                            const double* __restrict__ p, double* __restrict__ q,
+                                                            double* partials, CgState* st) {
+  if (((volatile CgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;   // a multiple of 32: a warp is one slice
+  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
+  double pq = 0.0;
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
+    const int64_t sl = row / kSlice;
+    const int m = __ldg(soff + sl + 1) - __ldg(soff + sl);
+    const int32_t* c = scols + (int64_t)kSlice * __ldg(soff + sl) + (row & (kSlice - 1));
+    const double* a = svals + (c - scols);
+    double acc = 0.0;
+    int k = 0;
+    for (; k + kRowChunk <= m; k += kRowChunk) {
+      int32_t cc[kRowChunk];
+      double aa[kRowChunk];
+#pragma unroll
+      for (int u = 0; u < kRowChunk; ++u) {
+        cc[u] = __ldg(c + (int64_t)kSlice * (k + u));
+        aa[u] = __ldg(a + (int64_t)kSlice * (k + u));
+      }
+#pragma unroll
+      for (int u = 0; u < kRowChunk; ++u) acc += aa[u] * __ldg(p + cc[u]);
+    }
+    for (; k < m; ++k) acc += __ldg(a + (int64_t)kSlice * k) * __ldg(p + __ldg(c + (int64_t)kSlice * k));
+    if (row < n) {
+      q[row] = acc;
+      pq += p[row] * acc;
+    }
+  }
+  pq = block_sum(pq, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = pq;
+  if (last_block(&st->ticket[1])) {
+    double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
+    if (threadIdx.x == 0) {
+      st->pq = t;
+      if (!(t > 0.0) || !isfinite(t)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+        st->alpha = 0.0;
+      } else {
+        st->alpha = st->rz / t;
+      }
+      st->ticket[1] = 0;
     }
   }
 }
@@ -630,6 +646,44 @@ __global__ void k_fill_f32(int64_t n, float v, float* __restrict__ b) {
 // ---------------------------------------------------------------------------
 // Host side.
 
+// Sliced-ELL copy of a CSR matrix: slice offsets in the call's scratch arena
+// (slices_scratch_bytes), columns and values in device memory held for the
+// solve (freed, stream-ordered, when the copy goes out of scope).
+template <class T>
+struct SlicedCopy {
+  cudaStream_t s;
+  int32_t* soff = nullptr;
+  int32_t* cols = nullptr;
+  T* vals = nullptr;
+  ~SlicedCopy() {
+    if (cols) cudaFreeAsync(cols, s);
+    if (vals) cudaFreeAsync(vals, s);
+  }
+};
+
+static size_t slices_scratch_bytes(int n) {
+  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
+  return 2 * align256(sizeof(int32_t) * (size_t)(nslice + 1)) + scan_scratch_bytes(nslice);
+}
+
+template <class T>
+static afem_status build_slices(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                                SlicedCopy<T>& out) {
+  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
+  int32_t* slen;
+  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &slen));
+  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &out.soff));
+  AFEM_TRY(launch(ctx, k_slice_len, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, slen));
+  AFEM_TRY(exclusive_scan_i32(ctx, slen, out.soff, nslice));
+  int32_t slots = 0;   // sum of the slice lengths (<= nnz); the copy holds 32 x that many entries
+  AFEM_TRY(read_scalar(ctx, out.soff + nslice, &slots));
+  const size_t entries = (size_t)kSlice * (size_t)std::max(slots, 1);
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.cols), sizeof(int32_t) * entries, ctx->stream));
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.vals), sizeof(T) * entries, ctx->stream));
+  return launch(ctx, k_slice_fill<T>, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, cols, vals,
+                (const int32_t*)out.soff, out.cols, out.vals);
+}
+
 afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals, int64_t nnz,
                     const double* b, double* x, const uint8_t* skip, const afem_solver_options& opt,
                     afem_solve_info* info) {
@@ -638,7 +692,7 @@ afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* c
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned nparts = std::max(grid_rows, grid_vec);
   size_t need = 6 * align256(sizeof(double) * (size_t)n) + align256(sizeof(double) * 3 * nparts) +
-                align256(sizeof(CgState));
+                align256(sizeof(CgState)) + slices_scratch_bytes(n);
   AFEM_TRY(scratch_reserve(ctx, need));
   double *r, *z, *p, *q, *dinv, *partials;
   CgState* st;
@@ -665,14 +719,15 @@ afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* c
     return launch(ctx, k_cg_init<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b,
                   (const double*)x, dv, skip, r, z, p, partials, st, opt.rtol, opt.atol);
   }));
+  SlicedCopy<double> sliced{ctx->stream};   // the iteration's SpMV reads the sliced-ELL copy
+  AFEM_TRY(build_slices(ctx, n, rp, cols, vals, sliced));
+  const unsigned grid_sl = grid_for(ctx, n, kSolveBlock, 8);
   const int chunk = opt.check_every > 0 ? opt.check_every : 16;
   GraphChunk gc;
   AFEM_TRY(capture(ctx, gc, [&](cudaStream_t s) -> afem_status {
     for (int k = 0; k < chunk; ++k) {
-      AFEM_TRY(dispatch_g(G, [&](auto g) {
-        return launch_s(ctx, s, k_cg_spmv<decltype(g)::value>, grid_rows, kSolveBlock, n, rp, cols, vals,
-                        (const double*)p, q, partials, st);
-      }));
+      AFEM_TRY(launch_s(ctx, s, k_cg_spmv_sl, grid_sl, kSolveBlock, n, (const int32_t*)sliced.soff,
+                        (const int32_t*)sliced.cols, (const double*)sliced.vals, (const double*)p, q, partials, st));
       AFEM_TRY(launch_s(ctx, s, k_cg_update, grid_vec, kSolveBlock, n, x, r, z, (const double*)p, (const double*)q,
                         dv, skip, partials, st));
       AFEM_TRY(launch_s(ctx, s, k_cg_dir, grid_vec, kSolveBlock, n, (const double*)z, p, (const CgState*)st));
@@ -707,11 +762,10 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   const unsigned grid_rows64 = grid_for(ctx, (int64_t)n * G64, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned nparts = std::max(std::max(grid_rows, grid_rows64), grid_vec);
-  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
   size_t need = 6 * align256(sizeof(float) * (size_t)n) + align256(sizeof(double) * 3 * nparts) +
                 2 * align256(sizeof(CgState)) +
                 (b3 ? align256(sizeof(float) * (size_t)nnz) + align256(sizeof(int32_t) * (size_t)(nnz / 9 + 1)) + 256
-                    : 2 * align256(sizeof(int32_t) * (size_t)(nslice + 1)) + scan_scratch_bytes(nslice));
+                    : slices_scratch_bytes(n));
   AFEM_TRY(scratch_reserve(ctx, need));
   float *v32 = nullptr, *r32, *z32, *p32, *q32, *x32, *dinv32;
   double* partials;
@@ -739,34 +793,12 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     AFEM_TRY(read_scalar(ctx, bad, &hbad));
     AFEM_CHECK_ARG(!hbad, "block_size 3: the CSR pattern is not made of 3x3 blocks");
   }
-  // the FP32 matrix: values in CSR order for the 3x3-block SpMV, else the sliced-ELL copy (device memory held
-  // for this solve only)
-  struct SlicedCopy {
-    cudaStream_t s;
-    int32_t* cols = nullptr;
-    float* vals = nullptr;
-    ~SlicedCopy() {
-      if (cols) cudaFreeAsync(cols, s);
-      if (vals) cudaFreeAsync(vals, s);
-    }
-  } sliced{ctx->stream};
-  int32_t* soff = nullptr;
-  if (b3) {
+  // the FP32 matrix: values in CSR order for the 3x3-block SpMV, else the sliced-ELL copy
+  SlicedCopy<float> sliced{ctx->stream};
+  if (b3)
     AFEM_TRY(launch(ctx, k_to_f32, grid_for(ctx, nnz, 256), 256, 0, nnz, vals, v32));
-  } else {
-    int32_t* slen;
-    AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &slen));
-    AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &soff));
-    AFEM_TRY(launch(ctx, k_slice_len, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, slen));
-    AFEM_TRY(exclusive_scan_i32(ctx, slen, soff, nslice));
-    int32_t slots = 0;   // sum of the slice lengths (<= nnz); the copy holds 32 x that many entries
-    AFEM_TRY(read_scalar(ctx, soff + nslice, &slots));
-    const size_t entries = (size_t)kSlice * (size_t)std::max(slots, 1);
-    AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sliced.cols), sizeof(int32_t) * entries, ctx->stream));
-    AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sliced.vals), sizeof(float) * entries, ctx->stream));
-    AFEM_TRY(launch(ctx, k_slice_fill, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, cols, vals,
-                    (const int32_t*)soff, sliced.cols, sliced.vals));
-  }
+  else
+    AFEM_TRY(build_slices(ctx, n, rp, cols, vals, sliced));
   AFEM_TRY(launch(ctx, k_inv_diag, grid_vec, kSolveBlock, 0, n, rp, cols, vals, (double*)nullptr, dinv32));
   if (opt.precond != AFEM_PRECOND_JACOBI)  // unpreconditioned inner solve: D^-1 = 1
     AFEM_TRY(launch(ctx, k_fill_f32, grid_for(ctx, n, 256), 256, 0, (int64_t)n, 1.0f, dinv32));
@@ -781,7 +813,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
         AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_b3, grid_rows, kSolveBlock, n, rp, (const int32_t*)bcols,
                           (const float*)v32, (const float*)p32, q32, partials, inner));
       else
-        AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_sl, grid_rows, kSolveBlock, n, (const int32_t*)soff,
+        AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_sl, grid_rows, kSolveBlock, n, (const int32_t*)sliced.soff,
                           (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)p32, q32, partials,
                           inner));
       AFEM_TRY(launch_s(ctx, s, k_cgf_update, grid_vec, kSolveBlock, n, x32, r32, z32, (const float*)p32,
