@@ -380,69 +380,10 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_sl(int n, const int32_
   }
 }
 
-// FP32 BSR SpMV of the mixed solver for a CSR whose scalar rows come in 3x3
-// blocks (the per-row layout of a 3-DoF BSR matrix, femutils/BSRFormat.h:
-// block row I = scalar rows 3I..3I+2 with one pattern, columns 3J..3J+2 per
-// block).  One thread per scalar row, as the scalar SpMV, but with ONE
-// column index per block (bcols, shared by the block row's three threads
-// through L1): 4 B/nnz of FP32 values + 4/3 B/nnz of indices instead of
-// 4 + 4.  The row's blocks are read in chunks of kB3Chunk (indices and
-// values first, then the gathers).  <p, q> -> alpha as k_cgf_spmv.
-constexpr int kB3Chunk = 3;
-
-__global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_b3(int n, const int32_t* __restrict__ rp,
-                                                             const int32_t* __restrict__ bcols,
-                                                             const float* __restrict__ vals,
-                                                             const float* __restrict__ p, float* __restrict__ q,
-                                                             double* partials, CgState* st) {
-  if (((volatile CgState*)st)->done) return;
-  __shared__ double sh[kSolveBlock / 32];
-  float pqf = 0.f;
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
-    const int I = row / 3;
-    const int32_t r0 = __ldg(rp + 3 * I);
-    const int32_t nbk = (__ldg(rp + 3 * I + 1) - r0) / 3;
-    const int32_t* bc = bcols + r0 / 9;
-    const float* v = vals + __ldg(rp + row);
-    float s = 0.f;
-    for (int32_t k = 0; k < nbk; k += kB3Chunk) {
-      int32_t j[kB3Chunk];
-      float a[3 * kB3Chunk];
-#pragma unroll
-      for (int u = 0; u < kB3Chunk; ++u) {
-        const bool in = k + u < nbk;
-        j[u] = in ? 3 * __ldg(bc + k + u) : 0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) a[3 * u + c] = in ? __ldg(v + 3 * (k + u) + c) : 0.f;
-      }
-#pragma unroll
-      for (int u = 0; u < kB3Chunk; ++u)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) s = fmaf(a[3 * u + c], __ldg(p + j[u] + c), s);
-    }
-    q[row] = s;
-    pqf = fmaf(p[row], s, pqf);
-  }
-  const double pq = block_sum_f(pqf, sh);
-  if (threadIdx.x == 0) partials[blockIdx.x] = pq;
-  if (last_block(&st->ticket[1])) {
-    double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
-    if (threadIdx.x == 0) {
-      st->pq = t;
-      if (!(t > 0.0) || !isfinite(t)) {
-        st->status = AFEM_ERR_BREAKDOWN;
-        st->done = 1;
-        st->alpha = 0.0;
-      } else {
-        st->alpha = st->rz / t;
-      }
-      st->ticket[1] = 0;
-    }
-  }
-}
-
-// Block columns of a 3x3-blocked CSR: bcols[rp[3I] / 9 + k] = J for the k-th
-// block of block row I; a pattern without that shape sets *bad.
+// Block columns of a CSR whose scalar rows come in 3x3 blocks (the per-row
+// layout of a 3-DoF BSR matrix, femutils/BSRFormat.h: block row I = scalar
+// rows 3I..3I+2 with one pattern, columns 3J..3J+2 per block): one index per
+// block, and *bad set if the pattern is not of that form.
 __global__ void k_block_cols3(int nb, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                               int32_t* __restrict__ bcols, int* __restrict__ bad) {
   for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nb; I += gridDim.x * blockDim.x) {
@@ -461,6 +402,115 @@ __global__ void k_block_cols3(int nb, const int32_t* __restrict__ rp, const int3
         break;
       }
       bcols[r0 / 9 + k / 3] = c / 3;
+    }
+  }
+}
+
+// Sliced copy of a 3x3-block matrix for the FP32 SpMV: 32 block rows per
+// slice, padded to the slice's longest block row; block kb of block row
+// 32 s + l has its column index at 32 bsoff[s] + 32 kb + l and its value
+// (a, b) at (32 bsoff[s] + 32 kb) * 9 + (3 a + b) * 32 + l.  Warp (s, a)
+// computes the scalar rows 3 (32 s + l) + a: per block one coalesced
+// 128-byte segment of block columns (shared by the slice's three warps) and
+// three of values.  Padding blocks are zero blocks on the row's own block
+// column.  Each scalar row adds its products block by block, b inner, the
+// order of a thread-per-row walk of the block CSR rows, so q is unchanged;
+// <p, q> accumulates its rows in another order (warps own slices).
+constexpr int kB3Chunk = 3;   // blocks per chunk of loads issued before their products
+
+__global__ void k_slice_len3(int nb, const int32_t* __restrict__ rp, int32_t* __restrict__ slen) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nr = ((int64_t)nb + kSlice - 1) / kSlice * kSlice;
+  for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nr; I += stride) {
+    const int len = I < nb ? (__ldg(rp + 3 * I + 1) - __ldg(rp + 3 * I)) / 3 : 0;
+    const int m = __reduce_max_sync(0xffffffffu, len);
+    if ((I & (kSlice - 1)) == 0) slen[I / kSlice] = m;
+  }
+}
+
+__global__ void k_slice_fill3(int nb, const int32_t* __restrict__ rp, const int32_t* __restrict__ bcols,
+                              const double* __restrict__ vals, const int32_t* __restrict__ soff,
+                              int32_t* __restrict__ scols, float* __restrict__ svals) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nr = ((int64_t)nb + kSlice - 1) / kSlice * kSlice;
+  for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nr; I += stride) {
+    const int64_t sl = I / kSlice, l = I & (kSlice - 1);
+    const int m = soff[sl + 1] - soff[sl];
+    const int32_t r0 = I < nb ? rp[3 * I] : 0;
+    const int nbk = I < nb ? (rp[3 * I + 1] - r0) / 3 : 0;
+    for (int kb = 0; kb < m; ++kb) {
+      const bool in = kb < nbk;
+      const int64_t e = (int64_t)kSlice * soff[sl] + (int64_t)kSlice * kb;
+      scols[e + l] = in ? bcols[r0 / 9 + kb] : (I < nb ? (int32_t)I : 0);
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+          svals[e * 9 + (3 * a + b) * kSlice + l] = in ? (float)vals[rp[3 * I + a] + 3 * kb + b] : 0.f;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_b3s(int nb, const int32_t* __restrict__ soff,
+                                                              const int32_t* __restrict__ scols,
+                                                              const float* __restrict__ svals,
+                                                              const float* __restrict__ p, float* __restrict__ q,
+                                                              double* partials, CgState* st) {
+  if (((volatile CgState*)st)->done) return;
+  __shared__ double sh[kSolveBlock / 32];
+  const int lane = threadIdx.x & 31;
+  const int64_t nslice = ((int64_t)nb + kSlice - 1) / kSlice;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
+  float pqf = 0.f;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32; w < 3 * nslice; w += warps) {
+    const int64_t sl = w / 3;
+    const int a = (int)(w - 3 * sl);
+    const int m = __ldg(soff + sl + 1) - __ldg(soff + sl);
+    const int64_t e0 = (int64_t)kSlice * __ldg(soff + sl);
+    const int32_t* c = scols + e0 + lane;
+    const float* v = svals + e0 * 9 + 3 * a * kSlice + lane;
+    float acc = 0.f;
+    int kb = 0;
+    for (; kb + kB3Chunk <= m; kb += kB3Chunk) {
+      int32_t j[kB3Chunk];
+      float x[3 * kB3Chunk];
+#pragma unroll
+      for (int u = 0; u < kB3Chunk; ++u) {
+        j[u] = 3 * __ldg(c + (int64_t)kSlice * (kb + u));
+#pragma unroll
+        for (int b = 0; b < 3; ++b) x[3 * u + b] = __ldg(v + (int64_t)kSlice * 9 * (kb + u) + b * kSlice);
+      }
+#pragma unroll
+      for (int u = 0; u < kB3Chunk; ++u)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) acc = fmaf(x[3 * u + b], __ldg(p + j[u] + b), acc);
+    }
+    for (; kb < m; ++kb) {
+      const int32_t jj = 3 * __ldg(c + (int64_t)kSlice * kb);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) acc = fmaf(__ldg(v + (int64_t)kSlice * 9 * kb + b * kSlice), __ldg(p + jj + b), acc);
+    }
+    const int64_t I = kSlice * sl + lane;
+    if (I < nb) {
+      const int64_t row = 3 * I + a;
+      q[row] = acc;
+      pqf = fmaf(p[row], acc, pqf);
+    }
+  }
+  const double pq = block_sum_f(pqf, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = pq;
+  if (last_block(&st->ticket[1])) {
+    double t = reduce_partials(partials, gridDim.x, 1, 0, sh);
+    if (threadIdx.x == 0) {
+      st->pq = t;
+      if (!(t > 0.0) || !isfinite(t)) {
+        st->status = AFEM_ERR_BREAKDOWN;
+        st->done = 1;
+        st->alpha = 0.0;
+      } else {
+        st->alpha = st->rz / t;
+      }
+      st->ticket[1] = 0;
     }
   }
 }
@@ -633,10 +683,6 @@ __global__ void k_ir_correct(int n, double* __restrict__ x, const float* __restr
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)d[i];
 }
 
-__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
-}
 
 __global__ void k_fill_f32(int64_t n, float v, float* __restrict__ b) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -681,6 +727,24 @@ static afem_status build_slices(afem_context ctx, int n, const int32_t* rp, cons
   AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.cols), sizeof(int32_t) * entries, ctx->stream));
   AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.vals), sizeof(T) * entries, ctx->stream));
   return launch(ctx, k_slice_fill<T>, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, cols, vals,
+                (const int32_t*)out.soff, out.cols, out.vals);
+}
+
+// Sliced copy of a validated 3x3-block matrix (block columns from k_block_cols3)
+static afem_status build_slices3(afem_context ctx, int nb, const int32_t* rp, const int32_t* bcols,
+                                 const double* vals, SlicedCopy<float>& out) {
+  const int64_t nslice = ((int64_t)nb + kSlice - 1) / kSlice;
+  int32_t* slen;
+  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &slen));
+  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &out.soff));
+  AFEM_TRY(launch(ctx, k_slice_len3, grid_for(ctx, nslice * kSlice, 256), 256, 0, nb, rp, slen));
+  AFEM_TRY(exclusive_scan_i32(ctx, slen, out.soff, nslice));
+  int32_t slots = 0;   // sum of the slice lengths in blocks (<= nnz / 9)
+  AFEM_TRY(read_scalar(ctx, out.soff + nslice, &slots));
+  const size_t entries = (size_t)kSlice * (size_t)std::max(slots, 1);
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.cols), sizeof(int32_t) * entries, ctx->stream));
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.vals), sizeof(float) * 9 * entries, ctx->stream));
+  return launch(ctx, k_slice_fill3, grid_for(ctx, nslice * kSlice, 256), 256, 0, nb, rp, bcols, vals,
                 (const int32_t*)out.soff, out.cols, out.vals);
 }
 
@@ -761,16 +825,17 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   const unsigned grid_rows = grid_for(ctx, n, kSolveBlock, 8);
   const unsigned grid_rows64 = grid_for(ctx, (int64_t)n * G64, kSolveBlock, 8);
   const unsigned grid_vec = grid_for(ctx, n, kSolveBlock, 8);
-  const unsigned nparts = std::max(std::max(grid_rows, grid_rows64), grid_vec);
+  // 3x3-block SpMV: one warp per (slice of 32 block rows, component)
+  const unsigned grid_b3 = grid_for(ctx, 3 * (((int64_t)n / 3 + kSlice - 1) / kSlice) * kSlice, kSolveBlock, 8);
+  const unsigned nparts = std::max(std::max(std::max(grid_rows, grid_rows64), grid_vec), grid_b3);
   size_t need = 6 * align256(sizeof(float) * (size_t)n) + align256(sizeof(double) * 3 * nparts) +
                 2 * align256(sizeof(CgState)) +
-                (b3 ? align256(sizeof(float) * (size_t)nnz) + align256(sizeof(int32_t) * (size_t)(nnz / 9 + 1)) + 256
+                (b3 ? align256(sizeof(int32_t) * (size_t)(nnz / 9 + 1)) + 256 + slices_scratch_bytes(n / 3)
                     : slices_scratch_bytes(n));
   AFEM_TRY(scratch_reserve(ctx, need));
-  float *v32 = nullptr, *r32, *z32, *p32, *q32, *x32, *dinv32;
+  float *r32, *z32, *p32, *q32, *x32, *dinv32;
   double* partials;
   CgState *outer, *inner;
-  if (b3) AFEM_TRY(scratch_take(ctx, (size_t)nnz, &v32));
   AFEM_TRY(scratch_take(ctx, n, &r32));
   AFEM_TRY(scratch_take(ctx, n, &z32));
   AFEM_TRY(scratch_take(ctx, n, &p32));
@@ -793,10 +858,10 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     AFEM_TRY(read_scalar(ctx, bad, &hbad));
     AFEM_CHECK_ARG(!hbad, "block_size 3: the CSR pattern is not made of 3x3 blocks");
   }
-  // the FP32 matrix: values in CSR order for the 3x3-block SpMV, else the sliced-ELL copy
+  // the FP32 matrix: the sliced copy, by 3x3 blocks or by scalar rows
   SlicedCopy<float> sliced{ctx->stream};
   if (b3)
-    AFEM_TRY(launch(ctx, k_to_f32, grid_for(ctx, nnz, 256), 256, 0, nnz, vals, v32));
+    AFEM_TRY(build_slices3(ctx, n / 3, rp, (const int32_t*)bcols, vals, sliced));
   else
     AFEM_TRY(build_slices(ctx, n, rp, cols, vals, sliced));
   AFEM_TRY(launch(ctx, k_inv_diag, grid_vec, kSolveBlock, 0, n, rp, cols, vals, (double*)nullptr, dinv32));
@@ -810,8 +875,9 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   AFEM_TRY(capture(ctx, gc, [&](cudaStream_t s) -> afem_status {
     for (int k = 0; k < chunk; ++k) {
       if (b3)
-        AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_b3, grid_rows, kSolveBlock, n, rp, (const int32_t*)bcols,
-                          (const float*)v32, (const float*)p32, q32, partials, inner));
+        AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_b3s, grid_b3, kSolveBlock, n / 3, (const int32_t*)sliced.soff,
+                          (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)p32, q32, partials,
+                          inner));
       else
         AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_sl, grid_rows, kSolveBlock, n, (const int32_t*)sliced.soff,
                           (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)p32, q32, partials,
