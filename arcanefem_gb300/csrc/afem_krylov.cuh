@@ -1,7 +1,7 @@
 // Shared pieces of the Krylov solvers (CG, mixed-precision CG, flexible CG
 // with the learned preconditioner): G-lanes-per-row CSR dot products,
-// deterministic last-block reductions, the lanes-per-row choice, and CUDA
-// graph capture of a chunk of iterations.
+// deterministic last-block reductions, the lanes-per-row choice, sliced-ELL
+// matrix copies, and CUDA graph capture of a chunk of iterations.
 #pragma once
 #include <type_traits>
 
@@ -168,6 +168,104 @@ inline afem_status capture(afem_context ctx, GraphChunk& g, Body&& body) {
   if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture", __FILE__, __LINE__);
   AFEM_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
   return AFEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Sliced-ELL copies of a CSR matrix for the iteration SpMVs (FP64 CG, FCG,
+// and the FP32 inner CG of the mixed solver): 32 consecutive rows per slice,
+// padded to the slice's longest row; entry k of row 32 s + l sits at
+// 32 soff[s] + 32 k + l, so that a warp reads step k of its 32 rows as one
+// coalesced 128-byte segment of columns and one of values, where the
+// thread-per-row CSR walk reads 32 scattered streams.  Padding entries carry a
+// zero weight on the row's own column.  Each row's terms are summed in CSR
+// order (a zero weight leaves the sum unchanged), the order of a
+// thread-per-row walk of the CSR rows.
+constexpr int kSlice = 32;
+
+// slen[s] = the longest row of slice s (one warp per slice)
+static __global__ void k_slice_len(int n, const int32_t* __restrict__ rp, int32_t* __restrict__ slen) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
+    const int len = row < n ? __ldg(rp + row + 1) - __ldg(rp + row) : 0;
+    const int m = __reduce_max_sync(0xffffffffu, len);
+    if ((row & (kSlice - 1)) == 0) slen[row / kSlice] = m;
+  }
+}
+
+template <class T>
+__global__ void k_slice_fill(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                             const double* __restrict__ vals, const int32_t* __restrict__ soff,
+                             int32_t* __restrict__ scols, T* __restrict__ svals) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
+    const int64_t sl = row / kSlice;
+    const int m = soff[sl + 1] - soff[sl];
+    const int64_t base = (int64_t)kSlice * soff[sl] + (row & (kSlice - 1));
+    const int32_t b = row < n ? rp[row] : 0, e = row < n ? rp[row + 1] : 0;
+    for (int k = 0; k < m; ++k) {
+      const bool in = b + k < e;
+      if (scols) scols[base + (int64_t)kSlice * k] = in ? cols[b + k] : (row < n ? (int32_t)row : 0);
+      svals[base + (int64_t)kSlice * k] = in ? (T)vals[b + k] : T(0);
+    }
+  }
+}
+
+// The copy's device memory (offsets, columns, values), freed stream-ordered
+// by release() or the destructor.
+template <class T>
+struct SlicedCopy {
+  cudaStream_t s = nullptr;
+  int n = 0;
+  int32_t* soff = nullptr;
+  int32_t* cols = nullptr;
+  T* vals = nullptr;
+  void release() {
+    if (soff) cudaFreeAsync(soff, s);
+    if (cols) cudaFreeAsync(cols, s);
+    if (vals) cudaFreeAsync(vals, s);
+    soff = cols = nullptr;
+    vals = nullptr;
+  }
+  ~SlicedCopy() { release(); }
+};
+
+// scratch of build_slices (slice lengths and the scan's tiles)
+inline size_t slices_scratch_bytes(int n) {
+  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
+  return align256(sizeof(int32_t) * (size_t)(nslice + 1)) + scan_scratch_bytes(nslice);
+}
+
+// Builds the sliced copy of (rp, cols, vals) on the context stream (one
+// synchronising read of the copy's size).
+template <class T>
+afem_status build_slices(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                         SlicedCopy<T>& out) {
+  out.release();
+  out.s = ctx->stream;
+  out.n = n;
+  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
+  int32_t* slen;
+  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &slen));
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.soff), sizeof(int32_t) * (size_t)(nslice + 1), ctx->stream));
+  AFEM_TRY(launch(ctx, k_slice_len, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, slen));
+  AFEM_TRY(exclusive_scan_i32(ctx, slen, out.soff, nslice));
+  int32_t slots = 0;   // sum of the slice lengths (<= nnz); the copy holds 32 x that many entries
+  AFEM_TRY(read_scalar(ctx, out.soff + nslice, &slots));
+  const size_t entries = (size_t)kSlice * (size_t)std::max(slots, 1);
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.cols), sizeof(int32_t) * entries, ctx->stream));
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.vals), sizeof(T) * entries, ctx->stream));
+  return launch(ctx, k_slice_fill<T>, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, cols, vals,
+                (const int32_t*)out.soff, out.cols, out.vals);
+}
+
+// Re-reads the values of a matrix whose pattern the copy already holds.
+template <class T>
+afem_status refill_slice_values(afem_context ctx, const int32_t* rp, const double* vals, const SlicedCopy<T>& sc) {
+  const int64_t nslice = ((int64_t)sc.n + kSlice - 1) / kSlice;
+  return launch(ctx, k_slice_fill<T>, grid_for(ctx, nslice * kSlice, 256), 256, 0, sc.n, rp,
+                (const int32_t*)nullptr, vals, (const int32_t*)sc.soff, (int32_t*)nullptr, sc.vals);
 }
 
 // ||b - A x|| / ||b|| in FP64 (rows with skip[i] != 0 left out; skip may be null).

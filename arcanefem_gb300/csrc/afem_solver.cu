@@ -232,47 +232,6 @@ __global__ void k_inv_diag(int n, const int32_t* __restrict__ rp, const int32_t*
 // dot products accumulate in FP32 per thread and warp, in FP64 across warps
 // and blocks.
 
-// Sliced-ELL copies of the matrix for the CG SpMVs (FP64 values for the FP64
-// CG, FP32 for the inner CG of the mixed solver):
-// 32 consecutive rows per slice, padded to the slice's longest row; entry k
-// of row 32 s + l sits at 32 soff[s] + 32 k + l, so that a warp reads step k
-// of its 32 rows as one coalesced 128-byte segment of columns and one of
-// values, where the thread-per-row CSR walk reads 32 scattered streams.
-// Padding entries carry a zero weight on the row's own column.  Each row's
-// terms are summed in CSR order (fmaf of a zero weight leaves the sum
-// unchanged), the same order as a thread-per-row walk of the CSR rows.
-constexpr int kSlice = 32;
-
-// slen[s] = the longest row of slice s (one warp per slice)
-__global__ void k_slice_len(int n, const int32_t* __restrict__ rp, int32_t* __restrict__ slen) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
-  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
-    const int len = row < n ? __ldg(rp + row + 1) - __ldg(rp + row) : 0;
-    const int m = __reduce_max_sync(0xffffffffu, len);
-    if ((row & (kSlice - 1)) == 0) slen[row / kSlice] = m;
-  }
-}
-
-template <class T>
-__global__ void k_slice_fill(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
-                             const double* __restrict__ vals, const int32_t* __restrict__ soff,
-                             int32_t* __restrict__ scols, T* __restrict__ svals) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
-  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < nr; row += stride) {
-    const int64_t sl = row / kSlice;
-    const int m = soff[sl + 1] - soff[sl];
-    const int64_t base = (int64_t)kSlice * soff[sl] + (row & (kSlice - 1));
-    const int32_t b = row < n ? rp[row] : 0, e = row < n ? rp[row + 1] : 0;
-    for (int k = 0; k < m; ++k) {
-      const bool in = b + k < e;
-      scols[base + (int64_t)kSlice * k] = in ? cols[b + k] : (row < n ? (int32_t)row : 0);
-      svals[base + (int64_t)kSlice * k] = in ? (T)vals[b + k] : T(0);
-    }
-  }
-}
-
 // FP64 CG K1 over the sliced copy: q = A p, <p, q> -> alpha (the breakdown test as k_cgf_spmv_sl;
 // each row's products are added in CSR order, as in row_dot_chunked)
 __global__ void __launch_bounds__(kSolveBlock) k_cg_spmv_sl(int n, const int32_t* __restrict__ soff,
@@ -692,51 +651,16 @@ __global__ void k_fill_f32(int64_t n, float v, float* __restrict__ b) {
 // ---------------------------------------------------------------------------
 // Host side.
 
-// Sliced-ELL copy of a CSR matrix: slice offsets in the call's scratch arena
-// (slices_scratch_bytes), columns and values in device memory held for the
-// solve (freed, stream-ordered, when the copy goes out of scope).
-template <class T>
-struct SlicedCopy {
-  cudaStream_t s;
-  int32_t* soff = nullptr;
-  int32_t* cols = nullptr;
-  T* vals = nullptr;
-  ~SlicedCopy() {
-    if (cols) cudaFreeAsync(cols, s);
-    if (vals) cudaFreeAsync(vals, s);
-  }
-};
-
-static size_t slices_scratch_bytes(int n) {
-  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
-  return 2 * align256(sizeof(int32_t) * (size_t)(nslice + 1)) + scan_scratch_bytes(nslice);
-}
-
-template <class T>
-static afem_status build_slices(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
-                                SlicedCopy<T>& out) {
-  const int64_t nslice = ((int64_t)n + kSlice - 1) / kSlice;
-  int32_t* slen;
-  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &slen));
-  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &out.soff));
-  AFEM_TRY(launch(ctx, k_slice_len, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, slen));
-  AFEM_TRY(exclusive_scan_i32(ctx, slen, out.soff, nslice));
-  int32_t slots = 0;   // sum of the slice lengths (<= nnz); the copy holds 32 x that many entries
-  AFEM_TRY(read_scalar(ctx, out.soff + nslice, &slots));
-  const size_t entries = (size_t)kSlice * (size_t)std::max(slots, 1);
-  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.cols), sizeof(int32_t) * entries, ctx->stream));
-  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.vals), sizeof(T) * entries, ctx->stream));
-  return launch(ctx, k_slice_fill<T>, grid_for(ctx, nslice * kSlice, 256), 256, 0, n, rp, cols, vals,
-                (const int32_t*)out.soff, out.cols, out.vals);
-}
-
 // Sliced copy of a validated 3x3-block matrix (block columns from k_block_cols3)
 static afem_status build_slices3(afem_context ctx, int nb, const int32_t* rp, const int32_t* bcols,
                                  const double* vals, SlicedCopy<float>& out) {
+  out.release();
+  out.s = ctx->stream;
+  out.n = nb;
   const int64_t nslice = ((int64_t)nb + kSlice - 1) / kSlice;
   int32_t* slen;
   AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &slen));
-  AFEM_TRY(scratch_take(ctx, (size_t)nslice + 1, &out.soff));
+  AFEM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&out.soff), sizeof(int32_t) * (size_t)(nslice + 1), ctx->stream));
   AFEM_TRY(launch(ctx, k_slice_len3, grid_for(ctx, nslice * kSlice, 256), 256, 0, nb, rp, slen));
   AFEM_TRY(exclusive_scan_i32(ctx, slen, out.soff, nslice));
   int32_t slots = 0;   // sum of the slice lengths in blocks (<= nnz / 9)
@@ -783,7 +707,7 @@ afem_status cg_fp64(afem_context ctx, int n, const int32_t* rp, const int32_t* c
     return launch(ctx, k_cg_init<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b,
                   (const double*)x, dv, skip, r, z, p, partials, st, opt.rtol, opt.atol);
   }));
-  SlicedCopy<double> sliced{ctx->stream};   // the iteration's SpMV reads the sliced-ELL copy
+  SlicedCopy<double> sliced;   // the iteration's SpMV reads the sliced-ELL copy
   AFEM_TRY(build_slices(ctx, n, rp, cols, vals, sliced));
   const unsigned grid_sl = grid_for(ctx, n, kSolveBlock, 8);
   const int chunk = opt.check_every > 0 ? opt.check_every : 16;
@@ -859,7 +783,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     AFEM_CHECK_ARG(!hbad, "block_size 3: the CSR pattern is not made of 3x3 blocks");
   }
   // the FP32 matrix: the sliced copy, by 3x3 blocks or by scalar rows
-  SlicedCopy<float> sliced{ctx->stream};
+  SlicedCopy<float> sliced;
   if (b3)
     AFEM_TRY(build_slices3(ctx, n / 3, rp, (const int32_t*)bcols, vals, sliced));
   else
