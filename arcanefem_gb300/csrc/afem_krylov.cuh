@@ -212,6 +212,32 @@ __global__ void k_slice_fill(int n, const int32_t* __restrict__ rp, const int32_
   }
 }
 
+// Dot product of one sliced row (c, a: the row's first column index and
+// value; entries 32 apart) with x, accumulated in Acc in entry order.  Every
+// chunk issues all of its loads first (past the row's end they read the
+// row's own entry), and the products past the end are skipped by a branch
+// that is uniform across the warp (a slice shares its length m), so there is
+// neither a serial tail nor a wasted FP64 instruction.
+template <class Acc, class T, class V>
+__device__ __forceinline__ Acc sliced_row_dot(const int32_t* __restrict__ c, const T* __restrict__ a, int m,
+                                              const V* __restrict__ x) {
+  Acc acc = Acc(0);
+  for (int k = 0; k < m; k += kRowChunk) {
+    int32_t cc[kRowChunk];
+    T aa[kRowChunk];
+#pragma unroll
+    for (int u = 0; u < kRowChunk; ++u) {
+      const int e = k + u < m ? k + u : 0;
+      cc[u] = __ldg(c + (int64_t)kSlice * e);
+      aa[u] = __ldg(a + (int64_t)kSlice * e);
+    }
+#pragma unroll
+    for (int u = 0; u < kRowChunk; ++u)
+      if (k + u < m) acc = fma((Acc)aa[u], (Acc)__ldg(x + cc[u]), acc);
+  }
+  return acc;
+}
+
 // The copy's device memory (offsets, columns, values), freed stream-ordered
 // by release() or the destructor.
 template <class T>

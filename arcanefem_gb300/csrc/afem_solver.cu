@@ -248,21 +248,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_cg_spmv_sl(int n, const int32_t
     const int64_t sl = row / kSlice;
     const int m = __ldg(soff + sl + 1) - __ldg(soff + sl);
     const int32_t* c = scols + (int64_t)kSlice * __ldg(soff + sl) + (row & (kSlice - 1));
-    const double* a = svals + (c - scols);
-    double acc = 0.0;
-    int k = 0;
-    for (; k + kRowChunk <= m; k += kRowChunk) {
-      int32_t cc[kRowChunk];
-      double aa[kRowChunk];
-#pragma unroll
-      for (int u = 0; u < kRowChunk; ++u) {
-        cc[u] = __ldg(c + (int64_t)kSlice * (k + u));
-        aa[u] = __ldg(a + (int64_t)kSlice * (k + u));
-      }
-#pragma unroll
-      for (int u = 0; u < kRowChunk; ++u) acc += aa[u] * __ldg(p + cc[u]);
-    }
-    for (; k < m; ++k) acc += __ldg(a + (int64_t)kSlice * k) * __ldg(p + __ldg(c + (int64_t)kSlice * k));
+    const double acc = sliced_row_dot<double>(c, svals + (c - scols), m, p);
     if (row < n) {
       q[row] = acc;
       pq += p[row] * acc;
@@ -301,21 +287,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_sl(int n, const int32_
     const int64_t sl = row / kSlice;
     const int m = __ldg(soff + sl + 1) - __ldg(soff + sl);
     const int32_t* c = scols + (int64_t)kSlice * __ldg(soff + sl) + (row & (kSlice - 1));
-    const float* a = svals + (c - scols);
-    float acc = 0.f;
-    int k = 0;
-    for (; k + kRowChunk <= m; k += kRowChunk) {
-      int32_t cc[kRowChunk];
-      float aa[kRowChunk];
-#pragma unroll
-      for (int u = 0; u < kRowChunk; ++u) {
-        cc[u] = __ldg(c + (int64_t)kSlice * (k + u));
-        aa[u] = __ldg(a + (int64_t)kSlice * (k + u));
-      }
-#pragma unroll
-      for (int u = 0; u < kRowChunk; ++u) acc = fmaf(aa[u], __ldg(p + cc[u]), acc);
-    }
-    for (; k < m; ++k) acc = fmaf(__ldg(a + (int64_t)kSlice * k), __ldg(p + __ldg(c + (int64_t)kSlice * k)), acc);
+    const float acc = sliced_row_dot<float>(c, svals + (c - scols), m, p);
     if (row < n) {
       q[row] = acc;
       pqf = fmaf(p[row], acc, pqf);
@@ -428,26 +400,24 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_b3s(int nb, const int3
     const int64_t e0 = (int64_t)kSlice * __ldg(soff + sl);
     const int32_t* c = scols + e0 + lane;
     const float* v = svals + e0 * 9 + 3 * a * kSlice + lane;
+    // chunks of kB3Chunk blocks, all loads first (past the row's end they read its first block), products past
+    // the end skipped by a warp-uniform branch
     float acc = 0.f;
-    int kb = 0;
-    for (; kb + kB3Chunk <= m; kb += kB3Chunk) {
+    for (int kb = 0; kb < m; kb += kB3Chunk) {
       int32_t j[kB3Chunk];
       float x[3 * kB3Chunk];
 #pragma unroll
       for (int u = 0; u < kB3Chunk; ++u) {
-        j[u] = 3 * __ldg(c + (int64_t)kSlice * (kb + u));
+        const int e = kb + u < m ? kb + u : 0;
+        j[u] = 3 * __ldg(c + (int64_t)kSlice * e);
 #pragma unroll
-        for (int b = 0; b < 3; ++b) x[3 * u + b] = __ldg(v + (int64_t)kSlice * 9 * (kb + u) + b * kSlice);
+        for (int b = 0; b < 3; ++b) x[3 * u + b] = __ldg(v + (int64_t)kSlice * 9 * e + b * kSlice);
       }
 #pragma unroll
       for (int u = 0; u < kB3Chunk; ++u)
+        if (kb + u < m)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) acc = fmaf(x[3 * u + b], __ldg(p + j[u] + b), acc);
-    }
-    for (; kb < m; ++kb) {
-      const int32_t jj = 3 * __ldg(c + (int64_t)kSlice * kb);
-#pragma unroll
-      for (int b = 0; b < 3; ++b) acc = fmaf(__ldg(v + (int64_t)kSlice * 9 * kb + b * kSlice), __ldg(p + jj + b), acc);
+          for (int b = 0; b < 3; ++b) acc = fmaf(x[3 * u + b], __ldg(p + j[u] + b), acc);
     }
     const int64_t I = kSlice * sl + lane;
     if (I < nb) {

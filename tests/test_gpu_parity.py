@@ -593,3 +593,47 @@ def test_row_above_the_candidate_capacity_is_reported(cuda_ctx):
     with pytest.raises(fem.AfemError) as e:
         f.compute_sparsity()
     assert e.value.status == 7
+
+
+def hub_laplacian(n, hubs, seed):
+    """SPD CSR with very uneven rows: a random sparse graph Laplacian (weights
+    in [0.5, 1.5]) plus hub nodes joined to a third of the graph, shifted by
+    0.1 I; rows from 2 to ~n/3 + 2 entries, n not a multiple of 32."""
+    rng = np.random.default_rng(seed)
+    edges = {(min(i, j), max(i, j)) for i, j in rng.integers(0, n, (3 * n, 2)) if i != j}
+    for h in hubs:
+        edges |= {(min(h, j), max(h, j)) for j in rng.choice(n, n // 3, replace=False) if j != h}
+    A = np.zeros((n, n))
+    for i, j in edges:
+        w = rng.uniform(0.5, 1.5)
+        A[i, j] = A[j, i] = -w
+    A[np.arange(n), np.arange(n)] = -A.sum(1) + 0.1
+    return A
+
+
+def dense_to_csr(A):
+    rows, cols = np.nonzero(A)
+    rp = np.zeros(A.shape[0] + 1, np.int32)
+    np.add.at(rp, rows + 1, 1)
+    return np.cumsum(rp).astype(np.int32), cols.astype(np.int32), A[rows, cols]
+
+
+@pytest.mark.parametrize("precision,block", [(fem.PRECISION_FP64, 0), (fem.PRECISION_MIXED, 0),
+                                             (fem.PRECISION_MIXED, 3)])
+def test_cg_on_uneven_rows_matches_oracle(cuda_ctx, precision, block):
+    """The iteration SpMVs read sliced-ELL copies (32 rows, or 32 block rows,
+    per slice, padded to the slice's longest row): rows of 2 to ~340 entries,
+    a last slice cut short (1001 rows, or 3 x 1001 scalar rows for the 3x3
+    blocks), FP64 CG and mixed precision against the oracle's solution."""
+    L = hub_laplacian(1001, hubs=[5, 500, 999], seed=3)
+    A = np.kron(L, np.array([[4.0, 1.0, 0.5], [1.0, 3.0, 0.2], [0.5, 0.2, 2.0]])) if block == 3 else L
+    rp, cols, vals = dense_to_csr(A)
+    b = np.random.default_rng(4).standard_normal(A.shape[0])
+    dev = lambda a: torch.as_tensor(a, device="cuda")
+    x = torch.zeros(A.shape[0], dtype=torch.float64, device="cuda")
+    opt = fem.solver_options(rtol=1e-10, max_iter=20000, precision=precision)
+    opt.block_size = block
+    info = fem.cg_solve_csr(cuda_ctx, dev(rp), dev(cols), dev(vals), dev(b), x, options=opt)
+    assert info.status == 0 and info.relres < 1e-10
+    x_ref, _, _ = O.pcg_jacobi(rp, cols, vals, b, rtol=1e-13, max_iter=50000)
+    assert np.linalg.norm(x.cpu().numpy() - x_ref) / np.linalg.norm(x_ref) < 1e-8
