@@ -493,11 +493,12 @@ __device__ __forceinline__ void write_rows_q1(const double (&K)[N][N], const int
   }
 }
 
-__global__ void __launch_bounds__(128) k_elem_poisson_quad4(int nb_cell, const double* __restrict__ xyz,
+__global__ void __launch_bounds__(128) k_elem_poisson_quad4(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                             const int32_t* __restrict__ cn,
                                                             const int32_t* __restrict__ inv,
                                                             const double* __restrict__ coeff, double* __restrict__ er) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell;
+       c += (int64_t)gridDim.x * blockDim.x) {
     double x[4], y[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -564,11 +565,12 @@ __constant__ double kHexDN[8][3][8] = {
     {{-kHpm, kHpm, kHpp, -kHpp, -kHmm, kHmm, kHpm, -kHpm}, {-kHpm, -kHpp, kHpp, kHpm, -kHmm, -kHpm, kHpm, kHmm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}},
     {{-kHmm, kHmm, kHpm, -kHpm, -kHpm, kHpm, kHpp, -kHpp}, {-kHmm, -kHpm, kHpm, kHmm, -kHpm, -kHpp, kHpp, kHpm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}}};
 
-__global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int nb_cell, const double* __restrict__ xyz,
+__global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                             const int32_t* __restrict__ cn,
                                                             const int32_t* __restrict__ inv,
                                                             const double* __restrict__ coeff, double* __restrict__ er) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell;
+       c += (int64_t)gridDim.x * blockDim.x) {
     double x[8], y[8], z[8];
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -1001,8 +1003,9 @@ afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
                  "afem_assemble_to_host: bad buffer");
   AFEM_CHECK_ARG(chunks >= 0 && chunks <= kMaxAsmChunks, "afem_assemble_to_host: chunks 0..%d", kMaxAsmChunks);
-  AFEM_CHECK_ARG(kind == AFEM_GATHER_POISSON_P1 || (kind == AFEM_GATHER_ELASTICITY_TET4 && m->dim == 3),
-                 "afem_assemble_to_host: kind must be AFEM_GATHER_POISSON_P1 or AFEM_GATHER_ELASTICITY_TET4");
+  AFEM_CHECK_ARG(kind == AFEM_GATHER_POISSON_P1 || kind == AFEM_GATHER_POISSON_Q1 ||
+                     (kind == AFEM_GATHER_ELASTICITY_TET4 && m->dim == 3),
+                 "afem_assemble_to_host: bad kind %d", kind);
   AFEM_CHECK_ARG(kind != AFEM_GATHER_ELASTICITY_TET4 || layout == AFEM_LAYOUT_PER_BLOCK ||
                      layout == AFEM_LAYOUT_PER_ROW,
                  "afem_assemble_to_host: bad layout %d", layout);
@@ -1047,6 +1050,14 @@ afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int
       if (kind == AFEM_GATHER_ELASTICITY_TET4) {
         AFEM_TRY(launch(ctx, k_elem_elasticity_tet, grid_for(ctx, c1 - c0, kElastElemBlock, 32), kElastElemBlock, 0,
                         c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke));
+      } else if (kind == AFEM_GATHER_POISSON_Q1) {
+        const unsigned ge = grid_for(ctx, c1 - c0, 128, 16);
+        if (m->dim == 3)
+          AFEM_TRY(launch(ctx, k_elem_poisson_hexa8, ge, 128, 0, c0, c1, m->coords_d, m->cell_nodes_d,
+                          m->nc_inverse_d, cell_coeff_d, ke));
+        else
+          AFEM_TRY(launch(ctx, k_elem_poisson_quad4, ge, 128, 0, c0, c1, m->coords_d, m->cell_nodes_d,
+                          m->nc_inverse_d, cell_coeff_d, ke));
       } else {
         const unsigned ge = grid_for(ctx, c1 - c0, 256, 16);
         if (m->dim == 3)
@@ -1063,12 +1074,12 @@ afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int
       if (kind == AFEM_GATHER_ELASTICITY_TET4)
         AFEM_TRY(launch(ctx, k_gather_elasticity, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                         (int)(layout == AFEM_LAYOUT_PER_ROW), values_d));
-      else if (m->dim == 3)
-        AFEM_TRY(launch(ctx, k_gather_scalar<4>, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
-                        values_d));
-      else
-        AFEM_TRY(launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
-                        values_d));
+      else {
+        // incidences per cell: 3 / 4 (P1 triangle / tetrahedron), 4 / 8 (Quad4 / Hexa8)
+        const int npc = kind == AFEM_GATHER_POISSON_Q1 ? (1 << m->dim) : m->dim + 1;
+        auto kern = npc == 8 ? k_gather_scalar<8> : npc == 4 ? k_gather_scalar<4> : k_gather_scalar<3>;
+        AFEM_TRY(launch(ctx, kern, gg, kGatherBlock, 0, n0, n1, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke, values_d));
+      }
       AFEM_CUDA(cudaEventRecord(ctx->chunk_ev[k + 1], s));
       AFEM_CUDA(cudaStreamWaitEvent(cs, ctx->chunk_ev[k + 1], 0));
       if (off[k + 1] > off[k])
@@ -1088,9 +1099,9 @@ afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_v
   AFEM_CHECK_ARG(m->nc_inverse_d && ke, "afem_element_matrices_poisson_q1: null nc_inverse / element buffer");
   const unsigned ge = grid_for(ctx, m->nb_cell, 128, 16);
   if (m->dim == 3)
-    return launch(ctx, k_elem_poisson_hexa8, ge, 128, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+    return launch(ctx, k_elem_poisson_hexa8, ge, 128, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                   cell_coeff_d, ke);
-  return launch(ctx, k_elem_poisson_quad4, ge, 128, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
+  return launch(ctx, k_elem_poisson_quad4, ge, 128, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
                 cell_coeff_d, ke);
 }
 

@@ -230,8 +230,8 @@ class BSRFormat:
                          cell_coeff: torch.Tensor | None = None, lam=0.0, mu=0.0):
         """element_matrices + gather with the values copied into the host
         tensor values_h (pinned for overlap), the copies overlapping the
-        element computation of later cell ranges (P1 Poisson, P1 elasticity).
-        chunks = 0: one range per ~80 MB of values (at most 12)."""
+        element computation of later cell ranges (P1 and Q1 Poisson, P1
+        elasticity).  chunks = 0: one range per ~80 MB of values (at most 12)."""
         assert values_h.device.type == "cpu" and values_h.dtype == torch.float64
         assert values_h.numel() == self.values.numel() and values_h.is_contiguous()
         mv = self.mesh_view()
@@ -239,9 +239,7 @@ class BSRFormat:
             kind = GATHER_ELASTICITY_TET4
             layout = LAYOUT_PER_BLOCK if self.order_values_per_block else LAYOUT_PER_ROW
         else:
-            if self.is_q1():
-                raise AfemError(8, "assemble_to_host: P1 cells only")
-            kind, layout = GATHER_POISSON_P1, 0
+            kind, layout = (GATHER_POISSON_Q1 if self.is_q1() else GATHER_POISSON_P1), 0
         call("afem_assemble_to_host", self.ctx.handle, C.byref(mv), kind, _ptr(self.row_ptr), _ptr(cell_coeff),
              float(lam), float(mu), layout, _ptr(ke), _ptr(self.values), C.c_void_p(values_h.data_ptr()), int(chunks))
 

@@ -367,13 +367,9 @@ def run_e2e(args, mesh, fmt0, lam, mu):
     fs.initialize(w["nb_dof"])
     fs.compute_sparsity()
 
-    def values_step():
+    def values_step():   # cell ranges: each completed node prefix is gathered and copied back behind them
         dco.copy_(coords_h, non_blocking=True)
-        if fs.is_q1():
-            fs.element_matrices(ke, lam=lam, mu=mu)
-            fs.gather_to_host(ke, vals_h, chunks=chunks)   # gather ranges overlap their copies back
-        else:   # cell ranges: each completed node prefix is gathered and copied back behind them
-            fs.assemble_to_host(ke, vals_h, chunks=chunks, lam=lam, mu=mu)
+        fs.assemble_to_host(ke, vals_h, chunks=chunks, lam=lam, mu=mu)
 
 
 

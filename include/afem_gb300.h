@@ -212,8 +212,8 @@ afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* mesh, in
  * range, the nodes it completes (a prefix of the node numbering: every
  * incident cell done) are gathered and their values copied to values_h on a
  * second stream while the next range computes.  kind: AFEM_GATHER_POISSON_P1
- * (cell_coeff_d nullable) or AFEM_GATHER_ELASTICITY_TET4 (lambda, mu,
- * layout).  ke_d is the caller's element buffer (afem_element_matrices_*
+ * or AFEM_GATHER_POISSON_Q1 (cell_coeff_d nullable) or
+ * AFEM_GATHER_ELASTICITY_TET4 (lambda, mu, layout).  ke_d is the caller's element buffer (afem_element_matrices_*
  * sizes).  Returns when values_h holds the whole matrix; values_d holds it
  * too.  Meshes numbered so that nodes complete late overlap less. */
 afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* mesh, int kind, const int32_t* row_ptr_d,

@@ -530,13 +530,14 @@ def test_mixed_bsr_rejects_a_scalar_pattern(cuda_ctx):
     assert e.value.status == 1
 
 
-@pytest.mark.parametrize("case", ["tri", "tet", "elast_block", "elast_row"])
+@pytest.mark.parametrize("case", ["tri", "tet", "quad", "hex", "elast_block", "elast_row"])
 @pytest.mark.parametrize("chunks", [0, 1, 4, 16])
 def test_assemble_to_host_matches_two_stage_assembly(cuda_ctx, case, chunks):
     """The pipelined assembly (cell ranges, the node prefixes they complete
     gathered and copied back behind them) gives exactly the values of the
     element kernel followed by the one-shot gather."""
     mesh = {"tri": lambda: meshgen.unit_square_tri(21, seed=1), "tet": lambda: meshgen.unit_cube_tet(7, seed=2),
+            "quad": lambda: meshgen.unit_square_quad(13, seed=3), "hex": lambda: meshgen.unit_cube_hex(5, seed=4),
             "elast_block": lambda: meshgen.unit_cube_tet(5, seed=5),
             "elast_row": lambda: meshgen.unit_cube_tet(6, seed=6)}[case]()
     nb_dof = 3 if case.startswith("elast") else 1
