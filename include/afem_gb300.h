@@ -401,8 +401,11 @@ afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* row_ptr_d, con
  * weighted-Jacobi smoothers whose per-node weights
  *   d_l = cap_l * sigmoid(c_l + logit 0.8),  cap_l = 2 / sum_j |A_l,ij|
  * come from a message-passing network on the mesh graph (6 layers, width 64,
- * BF16 tensor-core GEMMs with FP32 accumulation), trained on the GPU with this
- * library's forward and backward kernels and applied inside flexible CG.
+ * BF16 GEMMs on the tcgen05 tensor cores with FP32 accumulation in TMEM and
+ * TMA-loaded operand tiles), trained on the GPU with this library's forward
+ * and backward kernels and applied inside flexible CG.  The GEMMs' mbarrier
+ * waits are bounded: a wait that runs out is reported as AFEM_ERR_TIMEOUT by
+ * the call that ran the network.
  * The cap keeps the V-cycle symmetric positive definite for any network
  * output; with c = 0 the smoother is l1-Jacobi at 0.8 of the cap.
  *
@@ -452,8 +455,8 @@ afem_status afem_mpnn_set_coarse_rows(afem_mpnn net, int rows);
 afem_status afem_mpnn_scalings(afem_mpnn net, int level, float* d_d);
 /* Gradient of the mean relative energy norm of the error propagation,
  * ||e - M r||_A^2 / ||e||_A^2 over the batch of (r = A e, e) pairs (grad_d:
- * param_count floats, nullable) and the loss (host, nullable; non-null makes
- * the call synchronous). */
+ * param_count floats, nullable) and the loss (host, nullable).  Returns once
+ * the device work is done (it reads back the GEMMs' error word). */
 afem_status afem_mpnn_gradients(afem_mpnn net, int batch, const float* r_d, const float* e_d, float* grad_d,
                                 double* loss_h);
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss. */
