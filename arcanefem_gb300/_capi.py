@@ -111,6 +111,8 @@ SIGNATURES = {
     "afem_mpnn_set_coarse_rows": (C.c_int, [_P, C.c_int]),
     "afem_mpnn_gradients": (C.c_int, [_P, C.c_int, _P, _P, _P, C.POINTER(C.c_double)]),
     "afem_mpnn_train_step": (C.c_int, [_P, C.c_int, _P, _P, C.c_float, C.POINTER(C.c_double)]),
+    "afem_tc_row_gemm": (C.c_int, [_P, C.c_int64, _P, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int]),
+    "afem_tc_weight_grad": (C.c_int, [_P, C.c_int64, _P, _P, _P, _P]),
     "afem_fcg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.POINTER(SolverOptions),
                                  C.POINTER(SolveInfo)]),
     "afem_rhs_boundary_faces": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, C.c_int,

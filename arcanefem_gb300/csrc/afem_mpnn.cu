@@ -1183,9 +1183,9 @@ static afem_status rows64_map(const bf16* base, int64_t rows, CUtensorMap* map) 
 // Y = act(X1 B1 [+ X2 B2] + bias) over M rows on the tensor cores (k_row_gemm); at most 4 CTAs per SM
 // (4 x 64 TMEM columns of the 512).
 template <bool TWO, bool RELU>
-static afem_status row_gemm(afem_mpnn net, int64_t M, const bf16* X1, const bf16* B1t, const bf16* X2,
-                            const bf16* B2t, const float* bias, bf16* Yb, float* Yf, int accumulate) {
-  afem_context ctx = net->ctx;
+static afem_status row_gemm_launch(afem_context ctx, int* err, int64_t M, const bf16* X1, const bf16* B1t,
+                                   const bf16* X2, const bf16* B2t, const float* bias, bf16* Yb, float* Yf,
+                                   int accumulate) {
   if (M <= 0) return AFEM_OK;
   CUtensorMap m1, m2;
   AFEM_TRY(rows64_map(X1, M, &m1));
@@ -1197,12 +1197,17 @@ static afem_status row_gemm(afem_mpnn net, int64_t M, const bf16* X1, const bf16
   if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(k_row_gemm)", __FILE__, __LINE__);
   const int64_t tiles = (M + kTcRows - 1) / kTcRows;
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, (int64_t)ctx->sm_count * (TWO ? 2 : 4));
-  k_row_gemm<TWO, RELU><<<grid, 128, smem, ctx->stream>>>(m1, m2, (int)M, B1t, B2t, bias, Yb, Yf, accumulate,
-                                                          net->tc_err);
+  k_row_gemm<TWO, RELU><<<grid, 128, smem, ctx->stream>>>(m1, m2, (int)M, B1t, B2t, bias, Yb, Yf, accumulate, err);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "k_row_gemm", __FILE__, __LINE__);
   ++ctx->launches;
   return AFEM_OK;
+}
+
+template <bool TWO, bool RELU>
+static afem_status row_gemm(afem_mpnn net, int64_t M, const bf16* X1, const bf16* B1t, const bf16* X2,
+                            const bf16* B2t, const float* bias, bf16* Yb, float* Yf, int accumulate) {
+  return row_gemm_launch<TWO, RELU>(net->ctx, net->tc_err, M, X1, B1t, X2, B2t, bias, Yb, Yf, accumulate);
 }
 
 // Reports a timed-out tensor-core wait (k_row_gemm) as AFEM_ERR_TIMEOUT.  Reads the flag back (one small
@@ -1373,11 +1378,15 @@ static afem_status sum_partials(afem_context ctx, int nparts, int nelem, const f
 
 // [dW1 ; dW2] = [X1^T G ; X2^T G] summed over M rows into dst (FP32 2 x 64 x 64, dW2 right after dW1),
 // deterministic: per-CTA partials on the tensor cores (k_dw_grad), then a fixed-order sum
-static afem_status dw_gemm2(afem_mpnn net, int64_t M, const bf16* X1, const bf16* X2, const bf16* G, float* dst) {
-  afem_context ctx = net->ctx;
+static int dw_grad_parts(afem_context ctx, int64_t M) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((M + kTcRows - 1) / kTcRows, (int64_t)ctx->sm_count * 2));
+}
+
+// part: dw_grad_parts(ctx, M) x 2 x 64 x 64 floats
+static afem_status dw_grad_launch(afem_context ctx, int* err, float* part, int64_t M, const bf16* X1,
+                                  const bf16* X2, const bf16* G, float* dst) {
   if (M <= 0) return AFEM_OK;
-  const int nb = (int)std::min<int64_t>((M + kTcRows - 1) / kTcRows, (int64_t)ctx->sm_count * 2);
-  AFEM_TRY(ensure_part(net, (int64_t)nb * 2 * kF * kF));
+  const int nb = dw_grad_parts(ctx, M);
   CUtensorMap m1, m2, mg;
   AFEM_TRY(rows64_map(X1, M, &m1));
   AFEM_TRY(rows64_map(X2, M, &m2));
@@ -1385,11 +1394,16 @@ static afem_status dw_gemm2(afem_mpnn net, int64_t M, const bf16* X1, const bf16
   static const cudaError_t attr = cudaFuncSetAttribute(k_dw_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                        kDwSmem);
   if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(k_dw_grad)", __FILE__, __LINE__);
-  k_dw_grad<<<nb, 128, kDwSmem, ctx->stream>>>(m1, m2, mg, (int)M, net->part, net->tc_err);
+  k_dw_grad<<<nb, 128, kDwSmem, ctx->stream>>>(m1, m2, mg, (int)M, part, err);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "k_dw_grad", __FILE__, __LINE__);
   ++ctx->launches;
-  return sum_partials(ctx, nb, 2 * kF * kF, (const float*)net->part, dst, 0);
+  return sum_partials(ctx, nb, 2 * kF * kF, (const float*)part, dst, 0);
+}
+
+static afem_status dw_gemm2(afem_mpnn net, int64_t M, const bf16* X1, const bf16* X2, const bf16* G, float* dst) {
+  AFEM_TRY(ensure_part(net, (int64_t)dw_grad_parts(net->ctx, M) * 2 * kF * kF));
+  return dw_grad_launch(net->ctx, net->tc_err, net->part, M, X1, X2, G, dst);
 }
 
 // loss and gradients of the mean relative squared error over (r, e)
@@ -1674,6 +1688,49 @@ afem_status afem_mpnn_train_step(afem_mpnn net, int batch, const float* r_d, con
   AFEM_TRY(launch(ctx, k_adam, grid_for(ctx, net->nparam, 256), 256, 0, net->nparam, net->params,
                   (const float*)net->grads, net->adam_m, net->adam_v, lr, b1, b2, 1e-8f, c1, c2));
   return refresh_weights(net);
+}
+
+// The layer GEMMs on their own (testing, reuse).  Synchronous: they read back
+// the kernels' error word.
+afem_status afem_tc_row_gemm(afem_context ctx, int64_t M, const void* X1, const void* W1t, const void* X2,
+                             const void* W2t, const float* bias, int relu, void* Yb, float* Yf, int accumulate) {
+  AFEM_CHECK_ARG(ctx && M >= 0 && X1 && W1t && (Yb || Yf) && (!X2 == !W2t), "afem_tc_row_gemm: bad arguments");
+  scratch_reset(ctx);
+  AFEM_TRY(scratch_reserve(ctx, 256));
+  int* err;
+  AFEM_TRY(scratch_take(ctx, 1, &err));
+  AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  const bf16 *x1 = static_cast<const bf16*>(X1), *w1 = static_cast<const bf16*>(W1t);
+  const bf16 *x2 = static_cast<const bf16*>(X2), *w2 = static_cast<const bf16*>(W2t);
+  bf16* yb = static_cast<bf16*>(Yb);
+  if (X2 && relu) AFEM_TRY((row_gemm_launch<true, true>(ctx, err, M, x1, w1, x2, w2, bias, yb, Yf, accumulate)));
+  else if (X2) AFEM_TRY((row_gemm_launch<true, false>(ctx, err, M, x1, w1, x2, w2, bias, yb, Yf, accumulate)));
+  else if (relu) AFEM_TRY((row_gemm_launch<false, true>(ctx, err, M, x1, w1, x2, w2, bias, yb, Yf, accumulate)));
+  else AFEM_TRY((row_gemm_launch<false, false>(ctx, err, M, x1, w1, x2, w2, bias, yb, Yf, accumulate)));
+  int h = 0;
+  AFEM_TRY(read_scalar(ctx, err, &h));
+  if (h) return fail(AFEM_ERR_TIMEOUT, "afem_tc_row_gemm: a tensor-core mbarrier wait ran out");
+  return AFEM_OK;
+}
+
+afem_status afem_tc_weight_grad(afem_context ctx, int64_t M, const void* X1, const void* X2, const void* G,
+                                float* dW) {
+  AFEM_CHECK_ARG(ctx && M >= 0 && X1 && X2 && G && dW, "afem_tc_weight_grad: bad arguments");
+  const int nb = dw_grad_parts(ctx, M);
+  scratch_reset(ctx);
+  AFEM_TRY(scratch_reserve(ctx, 256 + align256(sizeof(float) * (size_t)nb * 2 * kF * kF)));
+  int* err;
+  float* part;
+  AFEM_TRY(scratch_take(ctx, 1, &err));
+  AFEM_TRY(scratch_take(ctx, (size_t)nb * 2 * kF * kF, &part));
+  AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  if (M == 0) AFEM_CUDA(cudaMemsetAsync(dW, 0, sizeof(float) * 2 * kF * kF, ctx->stream));
+  AFEM_TRY(dw_grad_launch(ctx, err, part, M, static_cast<const bf16*>(X1), static_cast<const bf16*>(X2),
+                          static_cast<const bf16*>(G), dW));
+  int h = 0;
+  AFEM_TRY(read_scalar(ctx, err, &h));
+  if (h) return fail(AFEM_ERR_TIMEOUT, "afem_tc_weight_grad: a tensor-core mbarrier wait ran out");
+  return AFEM_OK;
 }
 
 }  // extern "C"

@@ -43,6 +43,27 @@ def _ptr(t):
     return C.c_void_p(0 if t is None else t.data_ptr())
 
 
+def tc_row_gemm(ctx: fem.Context, X1, W1t, X2=None, W2t=None, bias=None, relu=False, out_bf16=True,
+                out_f32=False, Yf=None, accumulate=False):
+    """The network's layer GEMM on the tcgen05 tensor cores: act(X1 W1 + X2 W2
+    + bias) for BF16 X [M, 64] and transposed weights Wt [64, 64] (BF16); returns
+    (Yb BF16 or None, Yf FP32 or None)."""
+    M = X1.shape[0]
+    Yb = torch.empty((M, 64), dtype=torch.bfloat16, device=X1.device) if out_bf16 else None
+    if out_f32 and Yf is None:
+        Yf = torch.zeros((M, 64), dtype=torch.float32, device=X1.device)
+    call("afem_tc_row_gemm", ctx.handle, int(M), _ptr(X1), _ptr(W1t), _ptr(X2), _ptr(W2t), _ptr(bias), int(relu),
+         _ptr(Yb), _ptr(Yf), int(accumulate))
+    return Yb, Yf
+
+
+def tc_weight_grad(ctx: fem.Context, X1, X2, G):
+    """[X1^T G ; X2^T G] (FP32 [2, 64, 64]) for BF16 [M, 64] inputs, on the tensor cores."""
+    dW = torch.empty((2, 64, 64), dtype=torch.float32, device=X1.device)
+    call("afem_tc_weight_grad", ctx.handle, int(X1.shape[0]), _ptr(X1), _ptr(X2), _ptr(G), _ptr(dW))
+    return dW
+
+
 # ---------------------------------------------------------------------------
 # Structured hierarchy
 

@@ -462,6 +462,19 @@ afem_status afem_mpnn_gradients(afem_mpnn net, int batch, const float* r_d, cons
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss. */
 afem_status afem_mpnn_train_step(afem_mpnn net, int batch, const float* r_d, const float* e_d, float lr,
                                  double* loss_h);
+/* The network's layer GEMMs on their own (the tcgen05 kernels; testing and
+ * reuse).  Y[M x 64] = act(X1 W1 + X2 W2 + bias): X1, X2 BF16 [M][64]
+ * row-major (X2 and W2t null: one product), W given transposed, Wt[n][k]
+ * BF16 64 x 64, bias FP32 [64] nullable, relu 0/1; outputs Yb BF16 [M][64]
+ * and/or Yf FP32 [M][64] (accumulate: Yf += ...).  Device pointers, 16-byte
+ * aligned.  Synchronous. */
+afem_status afem_tc_row_gemm(afem_context ctx, int64_t M, const void* X1_d, const void* W1t_d, const void* X2_d,
+                             const void* W2t_d, const float* bias_d, int relu, void* Yb_d, float* Yf_d,
+                             int accumulate);
+/* dW = [X1^T G ; X2^T G] summed over the M rows: FP32 [2][64][64], fixed
+ * summation order (deterministic).  Synchronous. */
+afem_status afem_tc_weight_grad(afem_context ctx, int64_t M, const void* X1_d, const void* X2_d, const void* G_d,
+                                float* dW_d);
 /* Flexible CG (FCG(1)) on the FP64 CSR system with M as the preconditioner;
  * FP64 vectors, dots and true residual, M applied in FP32.  Synchronous. */
 afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
