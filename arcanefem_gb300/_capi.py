@@ -78,6 +78,8 @@ SIGNATURES = {
     "afem_gather_to_host": (C.c_int, [_P, C.POINTER(MeshView), C.c_int, _P, _P, C.c_int, _P, _P, C.c_int]),
     "afem_assemble_to_host": (C.c_int, [_P, C.POINTER(MeshView), C.c_int, _P, _P, C.c_double, C.c_double, C.c_int,
                                         _P, _P, _P, C.c_int]),
+    "afem_assemble_host_io": (C.c_int, [_P, C.POINTER(MeshView), _P, C.c_int, _P, _P, C.c_double, C.c_double,
+                                        C.c_int, _P, _P, _P, C.c_int]),
     "afem_bsr_to_csr_structure": (C.c_int, [_P, C.c_int, C.c_int, _P, _P, _P, _P]),
     "afem_rhs_constant_source": (C.c_int, [_P, C.POINTER(MeshView), C.c_double, C.c_int, _P]),
     "afem_rhs_body_force_tet4": (C.c_int, [_P, C.POINTER(MeshView), C.c_double, C.c_double, C.c_double, _P]),

@@ -300,21 +300,33 @@ struct CellBounds {
   int32_t b[kMaxAsmChunks + 1];
 };
 
+// With `need` (nullable): need[k] = the last node whose first incident cell
+// (the head of its ascending list) lies below bound[k], so that the cells
+// below bound[k] use only nodes [0, need[k]] (warp maximum, one atomic per
+// warp and bound; -1 when there is none).
 __global__ void k_node_bounds(int nb_node, const int32_t* __restrict__ nc_ptr, const int32_t* __restrict__ nc_cell,
-                              int nbound, CellBounds cb, int32_t* __restrict__ first) {
+                              int nbound, CellBounds cb, int32_t* __restrict__ first, int32_t* __restrict__ need) {
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t nr = ((int64_t)nb_node + stride - 1) / stride * stride;   // whole warps in every pass
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nr; n += stride) {
-    int32_t last = -1;
+    int32_t last = -1, head = INT_MAX;
     if (n < nb_node) {
-      const int32_t e = __ldg(nc_ptr + n + 1);
-      last = e > __ldg(nc_ptr + n) ? __ldg(nc_cell + e - 1) : -1;
+      const int32_t b = __ldg(nc_ptr + n), e = __ldg(nc_ptr + n + 1);
+      if (e > b) {
+        last = __ldg(nc_cell + e - 1);
+        head = __ldg(nc_cell + b);
+      }
     }
     for (int k = 0; k < nbound; ++k) {
       const int32_t v = (n < nb_node && last >= cb.b[k]) ? (int32_t)n : INT_MAX;
       const int32_t m = __reduce_min_sync(0xffffffffu, v);
       if (lane == 0 && m != INT_MAX) atomicMin(first + k, m);
+      if (need) {
+        const int32_t u = (n < nb_node && head < cb.b[k]) ? (int32_t)n : -1;
+        const int32_t mx = __reduce_max_sync(0xffffffffu, u);
+        if (lane == 0 && mx >= 0) atomicMax(need + k, mx);
+      }
     }
   }
 }
@@ -995,9 +1007,18 @@ afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* m, int k
   return AFEM_OK;
 }
 
-afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int kind, const int32_t* row_ptr_d,
-                                  const double* cell_coeff_d, double lambda, double mu, int layout, double* ke,
-                                  double* values_d, double* values_h, int chunks) {
+}  // extern "C"
+
+// afem_assemble_to_host, and with coords_h (afem_assemble_host_io) the node
+// coordinates uploaded into mesh->coords_d in node prefixes on a third stream:
+// the cells below a range's end use only nodes up to the last one whose first
+// incident cell lies below it (k_node_bounds' `need`), so each prefix is
+// copied ahead of the first cell range that needs it while earlier ranges
+// compute.
+static afem_status assemble_to_host_impl(afem_context ctx, const afem_mesh_view* m, int kind,
+                                         const int32_t* row_ptr_d, const double* cell_coeff_d, double lambda,
+                                         double mu, int layout, double* ke, double* values_d, double* values_h,
+                                         int chunks, const double* coords_h) {
   AFEM_CHECK_ARG(ctx, "afem_assemble_to_host: null context");
   AFEM_TRY(check_assembly(m, "afem_assemble_to_host"));
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
@@ -1023,19 +1044,50 @@ afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int
   for (int k = 0; k <= chunks; ++k) cbound[k] = (int64_t)nc * k / chunks;
   for (int k = 1; k < chunks; ++k) cb.b[k - 1] = (int32_t)cbound[k];
   AFEM_TRY(scratch_reserve(ctx, 512));
-  int32_t* first;
+  int32_t *first, *need;
   AFEM_TRY(scratch_take(ctx, kMaxAsmChunks + 1, &first));
-  int32_t* hb = reinterpret_cast<int32_t*>(ctx->pinned);   // 64 ints: node bounds, then their row starts
-  int32_t nb[kMaxAsmChunks + 1];
+  AFEM_TRY(scratch_take(ctx, kMaxAsmChunks + 1, &need));
+  // 64 pinned ints: node bounds at 0, coordinate needs at 16, row starts at 32
+  int32_t* hb = reinterpret_cast<int32_t*>(ctx->pinned);
+  int32_t nb[kMaxAsmChunks + 1], upto[kMaxAsmChunks + 1];
   nb[0] = 0;
   nb[chunks] = nn;
+  upto[chunks - 1] = nn;   // the last range: every node
   if (chunks > 1) {
     AFEM_CUDA(cudaMemsetAsync(first, 0x7f, sizeof(int32_t) * (chunks - 1), s));
+    if (coords_h) AFEM_CUDA(cudaMemsetAsync(need, 0xff, sizeof(int32_t) * (chunks - 1), s));
     AFEM_TRY(launch(ctx, k_node_bounds, grid_for(ctx, nn, 256), 256, 0, nn, m->nc_ptr_d, m->nc_cell_d, chunks - 1, cb,
-                    first));
+                    first, coords_h ? need : (int32_t*)nullptr));
     AFEM_CUDA(cudaMemcpyAsync(hb, first, sizeof(int32_t) * (chunks - 1), cudaMemcpyDeviceToHost, s));
+    if (coords_h)
+      AFEM_CUDA(cudaMemcpyAsync(hb + 16, need, sizeof(int32_t) * (chunks - 1), cudaMemcpyDeviceToHost, s));
     AFEM_CUDA(cudaStreamSynchronize(s));
     for (int k = 1; k < chunks; ++k) nb[k] = std::min(std::max(hb[k - 1], nb[k - 1]), nn);   // monotone
+    if (coords_h)
+      for (int k = 0; k + 1 < chunks; ++k) upto[k] = std::min(std::max(hb[16 + k] + 1, k ? upto[k - 1] : 0), nn);
+  }
+  // coordinate uploads, each ahead of the first range that needs it (h2d_at[k]: the event range k waits for)
+  int h2d_at[kMaxAsmChunks];
+  if (coords_h) {
+    if (!ctx->h2d_stream) AFEM_CUDA(cudaStreamCreateWithFlags(&ctx->h2d_stream, cudaStreamNonBlocking));
+    for (int k = 0; k <= chunks; ++k)
+      if (!ctx->h2d_ev[k]) AFEM_CUDA(cudaEventCreateWithFlags(&ctx->h2d_ev[k], cudaEventDisableTiming));
+    // earlier work of the context stream may still read the coordinates
+    AFEM_CUDA(cudaEventRecord(ctx->h2d_ev[chunks], s));
+    AFEM_CUDA(cudaStreamWaitEvent(ctx->h2d_stream, ctx->h2d_ev[chunks], 0));
+    double* coords_d = const_cast<double*>(m->coords_d);
+    int uploaded = 0, last = -1;
+    for (int k = 0; k < chunks; ++k) {
+      if (upto[k] > uploaded) {
+        AFEM_CUDA(cudaMemcpyAsync(coords_d + 3 * (int64_t)uploaded, coords_h + 3 * (int64_t)uploaded,
+                                  sizeof(double) * 3 * (size_t)(upto[k] - uploaded), cudaMemcpyHostToDevice,
+                                  ctx->h2d_stream));
+        AFEM_CUDA(cudaEventRecord(ctx->h2d_ev[k], ctx->h2d_stream));
+        uploaded = upto[k];
+        last = k;
+      }
+      h2d_at[k] = last;
+    }
   }
   for (int k = 0; k <= chunks; ++k)
     AFEM_CUDA(cudaMemcpyAsync(hb + 32 + k, row_ptr_d + nb[k], sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -1046,6 +1098,8 @@ afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int
   const int per_row = kind == AFEM_GATHER_ELASTICITY_TET4 ? 3 : 1;
   for (int k = 0; k < chunks; ++k) {
     const int c0 = (int)cbound[k], c1 = (int)cbound[k + 1];
+    if (coords_h && h2d_at[k] >= 0 && (k == 0 || h2d_at[k] != h2d_at[k - 1]))
+      AFEM_CUDA(cudaStreamWaitEvent(s, ctx->h2d_ev[h2d_at[k]], 0));
     if (c1 > c0) {
       if (kind == AFEM_GATHER_ELASTICITY_TET4) {
         AFEM_TRY(launch(ctx, k_elem_elasticity_tet, grid_for(ctx, c1 - c0, kElastElemBlock, 32), kElastElemBlock, 0,
@@ -1090,6 +1144,23 @@ afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int
   AFEM_CUDA(cudaStreamSynchronize(cs));
   AFEM_CUDA(cudaStreamSynchronize(s));
   return AFEM_OK;
+}
+
+extern "C" {
+
+afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* m, int kind, const int32_t* row_ptr_d,
+                                  const double* cell_coeff_d, double lambda, double mu, int layout, double* ke,
+                                  double* values_d, double* values_h, int chunks) {
+  return assemble_to_host_impl(ctx, m, kind, row_ptr_d, cell_coeff_d, lambda, mu, layout, ke, values_d, values_h,
+                               chunks, nullptr);
+}
+
+afem_status afem_assemble_host_io(afem_context ctx, const afem_mesh_view* m, const double* coords_h, int kind,
+                                  const int32_t* row_ptr_d, const double* cell_coeff_d, double lambda, double mu,
+                                  int layout, double* ke, double* values_d, double* values_h, int chunks) {
+  AFEM_CHECK_ARG(coords_h, "afem_assemble_host_io: null host coordinates");
+  return assemble_to_host_impl(ctx, m, kind, row_ptr_d, cell_coeff_d, lambda, mu, layout, ke, values_d, values_h,
+                               chunks, coords_h);
 }
 
 afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_view* m, const double* cell_coeff_d,

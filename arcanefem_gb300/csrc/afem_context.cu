@@ -171,6 +171,12 @@ afem_status afem_context_destroy(afem_context ctx) {
   }
   for (cudaEvent_t ev : ctx->chunk_ev)
     if (ev) cudaEventDestroy(ev);
+  if (ctx->h2d_stream) {
+    cudaStreamSynchronize(ctx->h2d_stream);
+    cudaStreamDestroy(ctx->h2d_stream);
+  }
+  for (cudaEvent_t ev : ctx->h2d_ev)
+    if (ev) cudaEventDestroy(ev);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   delete ctx;
   if (e != cudaSuccess) return cuda_fail(e, "afem_context_destroy", __FILE__, __LINE__);

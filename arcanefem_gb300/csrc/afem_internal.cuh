@@ -59,6 +59,9 @@ struct afem_context_s {
   // created on first use
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t chunk_ev[17] = {};
+  // host -> device coordinate uploads overlapped with kernels (afem_assemble_host_io), created on first use
+  cudaStream_t h2d_stream = nullptr;
+  cudaEvent_t h2d_ev[17] = {};
 };
 
 namespace afem {

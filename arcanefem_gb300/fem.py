@@ -227,11 +227,14 @@ class BSRFormat:
              _ptr(self.values), C.c_void_p(values_h.data_ptr()), int(chunks))
 
     def assemble_to_host(self, ke: torch.Tensor, values_h: torch.Tensor, chunks: int = 0,
-                         cell_coeff: torch.Tensor | None = None, lam=0.0, mu=0.0):
+                         cell_coeff: torch.Tensor | None = None, lam=0.0, mu=0.0, coords_h: torch.Tensor | None = None):
         """element_matrices + gather with the values copied into the host
         tensor values_h (pinned for overlap), the copies overlapping the
         element computation of later cell ranges (P1 and Q1 Poisson, P1
-        elasticity).  chunks = 0: one range per ~80 MB of values (at most 12)."""
+        elasticity).  chunks = 0: one range per ~80 MB of values (at most 12).
+        With coords_h (host [nb_node, 3] float64, pinned for overlap) the node
+        coordinates are uploaded into the mesh's device coordinates in node
+        prefixes, each ahead of the first cell range that uses it."""
         assert values_h.device.type == "cpu" and values_h.dtype == torch.float64
         assert values_h.numel() == self.values.numel() and values_h.is_contiguous()
         mv = self.mesh_view()
@@ -240,6 +243,13 @@ class BSRFormat:
             layout = LAYOUT_PER_BLOCK if self.order_values_per_block else LAYOUT_PER_ROW
         else:
             kind, layout = (GATHER_POISSON_Q1 if self.is_q1() else GATHER_POISSON_P1), 0
+        if coords_h is not None:
+            assert coords_h.device.type == "cpu" and coords_h.dtype == torch.float64 and coords_h.is_contiguous()
+            assert coords_h.numel() == 3 * self.mesh.nb_node
+            call("afem_assemble_host_io", self.ctx.handle, C.byref(mv), C.c_void_p(coords_h.data_ptr()), kind,
+                 _ptr(self.row_ptr), _ptr(cell_coeff), float(lam), float(mu), layout, _ptr(ke), _ptr(self.values),
+                 C.c_void_p(values_h.data_ptr()), int(chunks))
+            return
         call("afem_assemble_to_host", self.ctx.handle, C.byref(mv), kind, _ptr(self.row_ptr), _ptr(cell_coeff),
              float(lam), float(mu), layout, _ptr(ke), _ptr(self.values), C.c_void_p(values_h.data_ptr()), int(chunks))
 

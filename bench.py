@@ -367,9 +367,8 @@ def run_e2e(args, mesh, fmt0, lam, mu):
     fs.initialize(w["nb_dof"])
     fs.compute_sparsity()
 
-    def values_step():   # cell ranges: each completed node prefix is gathered and copied back behind them
-        dco.copy_(coords_h, non_blocking=True)
-        fs.assemble_to_host(ke, vals_h, chunks=chunks, lam=lam, mu=mu)
+    def values_step():   # host coordinates in, in node prefixes; cell ranges; values back behind them
+        fs.assemble_to_host(ke, vals_h, chunks=chunks, lam=lam, mu=mu, coords_h=coords_h)
 
 
 
@@ -393,9 +392,9 @@ def run_e2e(args, mesh, fmt0, lam, mu):
     d2h = nnz * 8
     return {"value": nnz / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "ms_per_step": dt * 1e3, "steps": steps,
-            "includes": ("H2D node coordinates, element matrices and gather in cell ranges, each completed node "
-                         f"range's values D2H behind it ({chunks or 'auto: one per ~80 MB of values, max 12'} "
-                         "ranges; sparsity reused)"),
+            "includes": ("H2D node coordinates in node prefixes, each ahead of the cell range that first uses it, "
+                         "element matrices and gather in cell ranges, each completed node range's values D2H behind "
+                         f"it ({chunks or 'auto: one per ~80 MB of values, max 12'} ranges; sparsity reused)"),
             "rebuild": {"value": nnz / dt_r, "unit": UNIT, "ms_per_step": dt_r * 1e3,
                         "h2d_bytes_per_step": h2d + cells_h.numel() * 4,
                         "d2h_bytes_per_step": d2h + fmt0.nnzb * 4 + (mesh.nb_node + 1) * 4,

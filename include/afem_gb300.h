@@ -219,6 +219,15 @@ afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* mesh, in
 afem_status afem_assemble_to_host(afem_context ctx, const afem_mesh_view* mesh, int kind, const int32_t* row_ptr_d,
                                   const double* cell_coeff_d, double lambda, double mu, int layout, double* ke_d,
                                   double* values_d, double* values_h, int chunks);
+/* afem_assemble_to_host with the node coordinates coming from the host too:
+ * coords_h [nb_node][3] (pinned for overlap) is copied into mesh->coords_d
+ * in node prefixes on a third stream, each prefix ahead of the first cell
+ * range whose cells use it (a node is needed from the range of its first
+ * incident cell on), while earlier ranges compute.  Host coordinates in, host
+ * values out; meshes numbered so that cells use nodes in order overlap most. */
+afem_status afem_assemble_host_io(afem_context ctx, const afem_mesh_view* mesh, const double* coords_h, int kind,
+                                  const int32_t* row_ptr_d, const double* cell_coeff_d, double lambda, double mu,
+                                  int layout, double* ke_d, double* values_d, double* values_h, int chunks);
 
 /* Allocation-free assembly of the scalar Poisson P1 matrix.  No counterpart
  * in the reference: it serves callers that cannot let a library allocate

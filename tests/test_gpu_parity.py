@@ -532,10 +532,13 @@ def test_mixed_bsr_rejects_a_scalar_pattern(cuda_ctx):
 
 @pytest.mark.parametrize("case", ["tri", "tet", "quad", "hex", "elast_block", "elast_row"])
 @pytest.mark.parametrize("chunks", [0, 1, 4, 16])
-def test_assemble_to_host_matches_two_stage_assembly(cuda_ctx, case, chunks):
+@pytest.mark.parametrize("host_coords", [False, True])
+def test_assemble_to_host_matches_two_stage_assembly(cuda_ctx, case, chunks, host_coords):
     """The pipelined assembly (cell ranges, the node prefixes they complete
     gathered and copied back behind them) gives exactly the values of the
-    element kernel followed by the one-shot gather."""
+    element kernel followed by the one-shot gather; with host coordinates
+    (afem_assemble_host_io) the device coordinates start as NaN and every
+    range must wait for the upload of the nodes its cells use."""
     mesh = {"tri": lambda: meshgen.unit_square_tri(21, seed=1), "tet": lambda: meshgen.unit_cube_tet(7, seed=2),
             "quad": lambda: meshgen.unit_square_quad(13, seed=3), "hex": lambda: meshgen.unit_cube_hex(5, seed=4),
             "elast_block": lambda: meshgen.unit_cube_tet(5, seed=5),
@@ -551,9 +554,15 @@ def test_assemble_to_host_matches_two_stage_assembly(cuda_ctx, case, chunks):
     f.values.fill_(float("nan"))
     ke.fill_(float("nan"))
     host = torch.full((f.values.numel(),), float("nan"), dtype=torch.float64).pin_memory()
-    f.assemble_to_host(ke, host, chunks=chunks, cell_coeff=coeff, lam=1.3, mu=0.7)
+    coords_h = None
+    if host_coords:
+        coords_h = f.mesh.coords.cpu().pin_memory()
+        f.mesh.coords.fill_(float("nan"))
+    f.assemble_to_host(ke, host, chunks=chunks, cell_coeff=coeff, lam=1.3, mu=0.7, coords_h=coords_h)
     assert torch.equal(host, ref)
     assert torch.equal(f.values.cpu(), ref)
+    if host_coords:
+        assert torch.equal(f.mesh.coords.cpu(), coords_h)
 
 
 def fan_mesh(k, isolated=0):
