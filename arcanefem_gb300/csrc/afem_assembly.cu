@@ -940,6 +940,7 @@ afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, co
 // and synchronisation cost (3D Poisson, 254 MB: best at 4; elasticity,
 // 970 MB: best at 12, slower at 16).
 constexpr double kAutoRangeBytes = 80e6;
+constexpr double kRangeRatio = 0.6;   // successive cell-range sizes of the scalar pipelined assembly
 constexpr int kAutoMaxRanges = 12;
 
 static afem_status auto_ranges(afem_context ctx, const int32_t* row_ptr_d, int n, int64_t scale, int* chunks) {
@@ -1041,7 +1042,20 @@ static afem_status assemble_to_host_impl(afem_context ctx, const afem_mesh_view*
   // cell chunks and the node prefixes they complete
   CellBounds cb{};
   int64_t cbound[kMaxAsmChunks + 1];
-  for (int k = 0; k <= chunks; ++k) cbound[k] = (int64_t)nc * k / chunks;
+  // Scalar kinds produce values more slowly than the link copies them back, so only the last range's copy is
+  // exposed: range sizes shrink geometrically (ratio kRangeRatio) to keep it short.  Elasticity's copy is longer
+  // than its compute: equal ranges start the copies earliest.
+  if (kind == AFEM_GATHER_ELASTICITY_TET4) {
+    for (int k = 0; k <= chunks; ++k) cbound[k] = (int64_t)nc * k / chunks;
+  } else {
+    double w[kMaxAsmChunks + 1], tot = 0.0, acc = 0.0;
+    for (int k = 0; k < chunks; ++k) tot += (w[k] = std::pow(kRangeRatio, k));
+    cbound[0] = 0;
+    for (int k = 0; k < chunks; ++k) {
+      acc += w[k];
+      cbound[k + 1] = k + 1 == chunks ? nc : std::min<int64_t>(nc, (int64_t)(nc * (acc / tot)));
+    }
+  }
   for (int k = 1; k < chunks; ++k) cb.b[k - 1] = (int32_t)cbound[k];
   AFEM_TRY(scratch_reserve(ctx, 512));
   int32_t *first, *need;
