@@ -350,15 +350,20 @@ def run_e2e(args, mesh, fmt0, lam, mu):
     steps = max(3, args.steps // 2)
     chunks = args.e2e_chunks   # 0: the library's choice, one range per ~80 MB of values
 
-    def timed(one):
+    def timed(one, blocks=3):
+        """Median over `blocks` timed blocks of `steps` steps (host-synchronised
+        steps: the median keeps one disturbed block from setting the figure)."""
         for _ in range(2):
             one()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            one()
-        torch.cuda.synchronize()
-        return (time.perf_counter() - t0) / steps
+        per = []
+        for _ in range(blocks):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                one()
+            torch.cuda.synchronize()
+            per.append((time.perf_counter() - t0) / steps)
+        return statistics.median(per)
 
     # values step: structure built once, as the reference module does at init
     dco.copy_(coords_h)
@@ -391,7 +396,7 @@ def run_e2e(args, mesh, fmt0, lam, mu):
     h2d = coords_h.numel() * 8
     d2h = nnz * 8
     return {"value": nnz / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "ms_per_step": dt * 1e3, "steps": steps,
+            "ms_per_step": dt * 1e3, "steps": steps, "timing": f"median of 3 wall-clock blocks of {steps} steps",
             "includes": ("H2D node coordinates in node prefixes, each ahead of the cell range that first uses it, "
                          "element matrices and gather in cell ranges, each completed node range's values D2H behind "
                          f"it ({chunks or 'auto: one per ~80 MB of values, max 12'} ranges; sparsity reused)"),
