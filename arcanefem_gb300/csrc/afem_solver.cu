@@ -272,14 +272,21 @@ __global__ void __launch_bounds__(kSolveBlock) k_cg_spmv_sl(int n, const int32_t
   }
 }
 
-// q = A p over the sliced copy ; <p, q> -> alpha (as k_cgf_spmv)
+// Inner CG step K1, fused with the direction update of the previous step:
+//   w = A z ; p = z + beta p ; q = w + beta q (= A p) ; <p, q> -> alpha
+// over the sliced copy.  The SpMV reads z only, so p and q are updated in
+// place for the thread's own rows.  beta = 0 (first step of a cycle, or a
+// restarted direction) gives p = z, q = A z without reading the old p and q.
+// q follows the recurrence A z + beta q instead of a product with p; the
+// reliable FP64 updates every cycle bound the drift of both.
 __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_sl(int n, const int32_t* __restrict__ soff,
                                                              const int32_t* __restrict__ scols,
                                                              const float* __restrict__ svals,
-                                                             const float* __restrict__ p, float* __restrict__ q,
-                                                             double* partials, CgState* st) {
+                                                             const float* __restrict__ z, float* __restrict__ p,
+                                                             float* __restrict__ q, double* partials, CgState* st) {
   if (((volatile CgState*)st)->done) return;
   __shared__ double sh[kSolveBlock / 32];
+  const float beta = (float)((volatile CgState*)st)->beta;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;   // a multiple of 32: a warp is one slice
   const int64_t nr = ((int64_t)n + kSlice - 1) / kSlice * kSlice;
   float pqf = 0.f;
@@ -287,10 +294,14 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_sl(int n, const int32_
     const int64_t sl = row / kSlice;
     const int m = __ldg(soff + sl + 1) - __ldg(soff + sl);
     const int32_t* c = scols + (int64_t)kSlice * __ldg(soff + sl) + (row & (kSlice - 1));
-    const float acc = sliced_row_dot<float>(c, svals + (c - scols), m, p);
+    const float w = sliced_row_dot<float>(c, svals + (c - scols), m, z);
     if (row < n) {
-      q[row] = acc;
-      pqf = fmaf(p[row], acc, pqf);
+      const float zi = z[row];
+      const float pi = beta != 0.f ? fmaf(beta, p[row], zi) : zi;
+      const float qi = beta != 0.f ? fmaf(beta, q[row], w) : w;
+      p[row] = pi;
+      q[row] = qi;
+      pqf = fmaf(pi, qi, pqf);
     }
   }
   const double pq = block_sum_f(pqf, sh);
@@ -382,13 +393,16 @@ __global__ void k_slice_fill3(int nb, const int32_t* __restrict__ rp, const int3
   }
 }
 
+// K1 of the inner CG over the block slices, fused with the direction update
+// as k_cgf_spmv_sl: w = A z gathered by blocks, then p and q in place.
 __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_b3s(int nb, const int32_t* __restrict__ soff,
                                                               const int32_t* __restrict__ scols,
                                                               const float* __restrict__ svals,
-                                                              const float* __restrict__ p, float* __restrict__ q,
-                                                              double* partials, CgState* st) {
+                                                              const float* __restrict__ z, float* __restrict__ p,
+                                                              float* __restrict__ q, double* partials, CgState* st) {
   if (((volatile CgState*)st)->done) return;
   __shared__ double sh[kSolveBlock / 32];
+  const float beta = (float)((volatile CgState*)st)->beta;
   const int lane = threadIdx.x & 31;
   const int64_t nslice = ((int64_t)nb + kSlice - 1) / kSlice;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
@@ -417,13 +431,17 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_spmv_b3s(int nb, const int3
       for (int u = 0; u < kB3Chunk; ++u)
         if (kb + u < m)
 #pragma unroll
-          for (int b = 0; b < 3; ++b) acc = fmaf(x[3 * u + b], __ldg(p + j[u] + b), acc);
+          for (int b = 0; b < 3; ++b) acc = fmaf(x[3 * u + b], __ldg(z + j[u] + b), acc);
     }
     const int64_t I = kSlice * sl + lane;
     if (I < nb) {
       const int64_t row = 3 * I + a;
-      q[row] = acc;
-      pqf = fmaf(p[row], acc, pqf);
+      const float zi = z[row];
+      const float pi = beta != 0.f ? fmaf(beta, p[row], zi) : zi;
+      const float qi = beta != 0.f ? fmaf(beta, q[row], acc) : acc;
+      p[row] = pi;
+      q[row] = qi;
+      pqf = fmaf(pi, qi, pqf);
     }
   }
   const double pq = block_sum_f(pqf, sh);
@@ -519,32 +537,17 @@ __global__ void __launch_bounds__(kSolveBlock) k_cgf_update(int n, float* __rest
   }
 }
 
-__global__ void __launch_bounds__(kSolveBlock) k_cgf_dir(int n, const float* __restrict__ z, float* __restrict__ p,
-                                                         const CgState* st) {
-  if (((volatile const CgState*)st)->done) return;
-  const float beta = (float)((volatile const CgState*)st)->beta;
-  const int n4 = n >> 2;   // 16-byte accesses (solver-owned aligned buffers), then the tail
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-  for (int i = tid; i < n4; i += stride) {
-    const float4 zv = reinterpret_cast<const float4*>(z)[i];
-    float4 pv = reinterpret_cast<float4*>(p)[i];
-    pv = make_float4(fmaf(beta, pv.x, zv.x), fmaf(beta, pv.y, zv.y), fmaf(beta, pv.z, zv.z), fmaf(beta, pv.w, zv.w));
-    reinterpret_cast<float4*>(p)[i] = pv;
-  }
-  for (int i = 4 * n4 + tid; i < n; i += stride) p[i] = fmaf(beta, p[i], z[i]);
-}
 
 // Reliable update: r = b - A x (FP64), r32 = (float) r, x32 = 0,
-// z32 = D^-1 r32 ; <r32, z32> and FP64 ||r||^2 ; inner state reset.  With
-// `restart` p32 = z32; otherwise beta = <r32, z32> / <r, z>_prev is left in
-// the inner state for k_ir_dir.
+// z32 = D^-1 r32 ; <r32, z32> and FP64 ||r||^2 ; inner state reset.  The
+// inner state's beta is 0 with `restart` (the next K1 starts p = z), else
+// <r32, z32> / <r, z>_prev (the next K1 keeps the direction: p = z + beta p).
 template <int G>
 __global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
     int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols, const double* __restrict__ vals,
     const double* __restrict__ b, const double* __restrict__ x, const float* __restrict__ dinv32,
     const uint8_t* __restrict__ skip, float* __restrict__ r32, float* __restrict__ x32, float* __restrict__ z32,
-    float* __restrict__ p32, double* partials, CgState* outer, CgState* inner, double inner_rtol, int inner_max,
-    int restart) {
+    double* partials, CgState* outer, CgState* inner, double inner_rtol, int inner_max, int restart) {
   __shared__ double sh[kSolveBlock / 32];
   const int lane = threadIdx.x & (G - 1);
   const int groups = gridDim.x * (blockDim.x / G);
@@ -565,7 +568,6 @@ __global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
       r32[row] = rf;
       x32[row] = 0.f;
       z32[row] = zf;
-      if (restart) p32[row] = zf;
       rz += (double)rf * (double)zf;
       if (!(skip && skip[row])) {
         rr += ri * ri;
@@ -602,11 +604,6 @@ __global__ void __launch_bounds__(kSolveBlock) k_ir_residual(
   }
 }
 
-// p32 = z32 + beta p32 after a reliable update that keeps the direction
-__global__ void k_ir_dir(int n, const float* __restrict__ z, float* __restrict__ p, const CgState* inner) {
-  const float beta = (float)((volatile const CgState*)inner)->beta;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fmaf(beta, p[i], z[i]);
-}
 
 __global__ void k_ir_correct(int n, double* __restrict__ x, const float* __restrict__ d) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)d[i];
@@ -770,15 +767,14 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     for (int k = 0; k < chunk; ++k) {
       if (b3)
         AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_b3s, grid_b3, kSolveBlock, n / 3, (const int32_t*)sliced.soff,
-                          (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)p32, q32, partials,
-                          inner));
+                          (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)z32, p32, q32,
+                          partials, inner));
       else
         AFEM_TRY(launch_s(ctx, s, k_cgf_spmv_sl, grid_rows, kSolveBlock, n, (const int32_t*)sliced.soff,
-                          (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)p32, q32, partials,
-                          inner));
+                          (const int32_t*)sliced.cols, (const float*)sliced.vals, (const float*)z32, p32, q32,
+                          partials, inner));
       AFEM_TRY(launch_s(ctx, s, k_cgf_update, grid_vec, kSolveBlock, n, x32, r32, z32, (const float*)p32,
                         (const float*)q32, (const float*)dinv32, skip, partials, inner));
-      AFEM_TRY(launch_s(ctx, s, k_cgf_dir, grid_vec, kSolveBlock, n, (const float*)z32, p32, (const CgState*)inner));
     }
     return AFEM_OK;
   }));
@@ -790,7 +786,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   for (;; ++outer_steps) {
     AFEM_TRY(dispatch_g(G64, [&](auto g) {
       return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows64, kSolveBlock, 0, n, rp, cols, vals, b,
-                    (const double*)x, (const float*)dinv32, skip, r32, x32, z32, p32, partials, outer, inner,
+                    (const double*)x, (const float*)dinv32, skip, r32, x32, z32, partials, outer, inner,
                     inner_rtol, max_iter, restart ? 1 : 0);
     }));
     CgState ho{};
@@ -802,14 +798,13 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
       restart = true;
       AFEM_TRY(dispatch_g(G64, [&](auto g) {
         return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows64, kSolveBlock, 0, n, rp, cols, vals, b,
-                      (const double*)x, (const float*)dinv32, skip, r32, x32, z32, p32, partials, outer, inner,
+                      (const double*)x, (const float*)dinv32, skip, r32, x32, z32, partials, outer, inner,
                       inner_rtol, max_iter, 1);
       }));
       AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, outer, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
       AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
       ho = *reinterpret_cast<CgState*>(ctx->pinned);
     }
-    if (!restart) AFEM_TRY(launch(ctx, k_ir_dir, grid_vec, 256, 0, n, (const float*)z32, p32, (const CgState*)inner));
     rr_prev = ho.rr;
     restart = false;
     if (outer_steps == 0) {
@@ -830,7 +825,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     CgState hi{};
     for (;;) {
       AFEM_CUDA(cudaGraphLaunch(gc.exec, ctx->stream));
-      ctx->launches += 3 * chunk;
+      ctx->launches += 2 * chunk;
       AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, inner, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
       AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
       hi = *reinterpret_cast<CgState*>(ctx->pinned);
