@@ -904,6 +904,28 @@ static afem_status check_assembly(const afem_mesh_view* m, const char* who) {
 
 }  // namespace afem
 
+namespace afem {
+// L1 for the scalar gathers.  Each thread streams its own row's element rows
+// (32 B per incidence), so a warp's loads touch 32 separate lines that are
+// re-read over the next incidences; with the default carveout nearly all of
+// the SM's 256 KB go to the shared-memory accumulators (7 blocks x 32 KB) and
+// the lines are evicted before their reuse.  A 50 % shared-memory carveout
+// keeps 4 blocks (16 warps) resident and leaves ~120 KB of L1.  Measured at
+// 128^3 / 96^3 (gather ms, carveout 25 / 40 / 50 / 60 / 75 / 100 %):
+// tetrahedra 1.28 / 0.59 / 0.56 / 0.57 / 0.62 / 1.02 (default 1.00), Hexa8
+// 0.50 / 0.38 / 0.37 / 0.36 / 0.37 / 0.50 (default 0.50).  The elasticity
+// gather is best at its default (1.90 ms; 1.92 at 75 %, 2.48 at 50 %).
+static void gather_attrs() {
+  static const bool done = [] {
+    cudaFuncSetAttribute(k_gather_scalar<3>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
+    cudaFuncSetAttribute(k_gather_scalar<4>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
+    cudaFuncSetAttribute(k_gather_scalar<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
+    return true;
+  }();
+  (void)done;
+}
+}  // namespace afem
+
 using namespace afem;
 
 extern "C" {
@@ -923,6 +945,7 @@ afem_status afem_element_matrices_poisson_p1(afem_context ctx, const afem_mesh_v
 
 afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                    const double* ke, double* values_d) {
+  gather_attrs();
   AFEM_CHECK_ARG(ctx, "afem_gather_poisson_p1: null context");
   AFEM_TRY(check_assembly(m, "afem_gather_poisson_p1"));
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && ((uintptr_t)ke & 31) == 0, "afem_gather_poisson_p1: bad buffer");
@@ -933,6 +956,7 @@ afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, co
   return launch(ctx, k_gather_scalar<3>, gg, kGatherBlock, 0, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d, ke,
                 values_d);
 }
+
 
 // Range count for chunks == 0: one range per ~80 MB of values, at most 12.
 // Measured on GB300 at ~193 GB/s device -> host: fewer ranges leave a longer
@@ -954,6 +978,7 @@ static afem_status auto_ranges(afem_context ctx, const int32_t* row_ptr_d, int n
 
 afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* m, int kind, const int32_t* row_ptr_d,
                                 const double* ke, int layout, double* values_d, double* values_h, int chunks) {
+  gather_attrs();
   AFEM_CHECK_ARG(ctx, "afem_gather_to_host: null context");
   AFEM_TRY(check_assembly(m, "afem_gather_to_host"));
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
@@ -1020,6 +1045,7 @@ static afem_status assemble_to_host_impl(afem_context ctx, const afem_mesh_view*
                                          const int32_t* row_ptr_d, const double* cell_coeff_d, double lambda,
                                          double mu, int layout, double* ke, double* values_d, double* values_h,
                                          int chunks, const double* coords_h) {
+  gather_attrs();
   AFEM_CHECK_ARG(ctx, "afem_assemble_to_host: null context");
   AFEM_TRY(check_assembly(m, "afem_assemble_to_host"));
   AFEM_CHECK_ARG(row_ptr_d && ke && values_d && values_h && ((uintptr_t)ke & 31) == 0,
@@ -1192,6 +1218,7 @@ afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_v
 
 afem_status afem_gather_poisson_q1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                    const double* ke, double* values_d) {
+  gather_attrs();
   AFEM_CHECK_ARG(ctx, "afem_gather_poisson_q1: null context");
   AFEM_TRY(check_mesh(m, "afem_gather_poisson_q1"));
   AFEM_CHECK_ARG(m->nc_slot_d && row_ptr_d && ke && values_d, "afem_gather_poisson_q1: null buffer");
@@ -1205,6 +1232,7 @@ afem_status afem_gather_poisson_q1(afem_context ctx, const afem_mesh_view* m, co
 
 afem_status afem_assemble_poisson_q1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                      const double* cell_coeff_d, double* values_d) {
+  gather_attrs();
   AFEM_CHECK_ARG(ctx, "afem_assemble_poisson_q1: null context");
   AFEM_TRY(check_mesh(m, "afem_assemble_poisson_q1"));
   AFEM_CHECK_ARG(row_ptr_d && values_d, "afem_assemble_poisson_q1: null buffer");
@@ -1218,6 +1246,7 @@ afem_status afem_assemble_poisson_q1(afem_context ctx, const afem_mesh_view* m, 
 
 afem_status afem_assemble_poisson_p1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                      const double* cell_coeff_d, double* values_d) {
+  gather_attrs();
   AFEM_CHECK_ARG(ctx, "afem_assemble_poisson_p1: null context");
   AFEM_TRY(check_assembly(m, "afem_assemble_poisson_p1"));
   AFEM_CHECK_ARG(row_ptr_d && values_d, "afem_assemble_poisson_p1: null buffer");
@@ -1242,6 +1271,7 @@ afem_status afem_element_matrices_elasticity_tet4(afem_context ctx, const afem_m
 
 afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
                                         const double* ke, int layout, double* values_d) {
+  gather_attrs();
   AFEM_CHECK_ARG(ctx, "afem_gather_elasticity_tet4: null context");
   AFEM_TRY(check_assembly(m, "afem_gather_elasticity_tet4"));
   AFEM_CHECK_ARG(m->dim == 3, "afem_gather_elasticity_tet4: tetrahedra only (dim 3)");
@@ -1415,6 +1445,7 @@ static afem_status launch_on(cudaStream_t s, Kernel k, unsigned grid, unsigned b
 extern "C" afem_status afem_assemble_poisson_p1_noalloc(void* cuda_stream, const afem_mesh_view* m,
                                                         const int32_t* row_ptr_d, const double* cell_coeff_d,
                                                         double* values_d) {
+  gather_attrs();
   AFEM_TRY(check_assembly(m, "afem_assemble_poisson_p1_noalloc"));
   AFEM_CHECK_ARG(row_ptr_d && values_d, "afem_assemble_poisson_p1_noalloc: null buffer");
   const size_t npc = m->dim + 1;
