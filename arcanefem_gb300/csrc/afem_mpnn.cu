@@ -1158,7 +1158,8 @@ static afem_status sweep(afem_mpnn net, const CsrLevel* M, int batch, const floa
 }
 
 // TMA descriptor of a row-major [rows x 64] BF16 matrix: 128-row boxes, 128-byte swizzle (the layout k_row_gemm's
-// MMAs read); rows past the end read as zero.  cuTensorMapEncodeTiled comes from the driver through the runtime.
+// MMAs read); rows past the end read as zero.  cuTensorMapEncodeTiled comes from the CUDA driver through the
+// runtime (cudaGetDriverEntryPointByVersion).
 static afem_status rows64_map(const bf16* base, int64_t rows, CUtensorMap* map) {
   static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
     void* fn = nullptr;
@@ -1168,7 +1169,7 @@ static afem_status rows64_map(const bf16* base, int64_t rows, CUtensorMap* map) 
       fn = nullptr;
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
-  if (!encode) return fail(AFEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  if (!encode) return fail(AFEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the CUDA driver");
   const cuuint64_t dims[2] = {(cuuint64_t)kF, (cuuint64_t)std::max<int64_t>(rows, 1)};
   const cuuint64_t strides[1] = {(cuuint64_t)kF * sizeof(bf16)};
   const cuuint32_t box[2] = {(cuuint32_t)kF, (cuuint32_t)kTcRows};
