@@ -21,6 +21,7 @@ LAYOUT_PER_BLOCK, LAYOUT_PER_ROW = 0, 1
 ELIMINATE_NONE, ELIMINATE_ROW, ELIMINATE_ROW_COLUMN = 0, 1, 2
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_LEARNED = 0, 1, 2
 PRECISION_FP64, PRECISION_MIXED = 0, 1
+FORMULATION_REFERENCE, FORMULATION_TESTLAB, FORMULATION_MINIMAL = 0, 1, 2
 
 
 class AfemError(RuntimeError):
@@ -59,6 +60,8 @@ SIGNATURES = {
     "afem_context_set_stream": (C.c_int, [_P, _P]),
     "afem_context_synchronize": (C.c_int, [_P]),
     "afem_context_launch_count": (C.c_int, [_P, _I64P]),
+    "afem_context_set_element_formulation": (C.c_int, [_P, C.c_int]),
+    "afem_context_get_element_formulation": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "afem_device_fp64_fma_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "afem_node_cell_build": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P]),
     "afem_sparsity_rows": (C.c_int, [_P, C.c_int, C.c_int, _P, _P, _P, _P, _I64P]),
@@ -87,6 +90,7 @@ SIGNATURES = {
     "afem_ls_destroy": (C.c_int, [_P]),
     "afem_ls_set_csr_values": (C.c_int, [_P, _P, _P, _P, C.c_int64]),
     "afem_ls_get_csr_values": (C.c_int, [_P, _PP, _PP, _PP, _I64P]),
+    "afem_ls_set_csr_view": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, _P, _P]),
     "afem_ls_dof_variables": (C.c_int, [_P, _PP, _PP, _PP, _PP, _PP, _PP]),
     "afem_ls_clear_values": (C.c_int, [_P]),
     "afem_ls_matrix_add_value": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double]),

@@ -25,9 +25,11 @@
 //   Diagonals use the zero row sum of a P1 stiffness: K_ii = -sum_{j!=i} K_ij.
 // Results agree with the reference formulas to rounding (tests check 1e-12).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <mutex>
 
+#include "afem_elem_ref.cuh"
 #include "afem_internal.cuh"
 
 namespace afem {
@@ -50,21 +52,6 @@ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
 }
 __device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
-// Tetrahedron geometry: cofactor vectors c[0..3] and s = 1 / (6 |det|).
-__device__ __forceinline__ void tet_cofactors(const double* __restrict__ xyz, const int32_t* __restrict__ cn,
-                                              int64_t c, d3 cf[4], double* s, double* vol) {
-  const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
-  d3 p0 = ld_node(xyz, q.x);
-  d3 v1 = sub(ld_node(xyz, q.y), p0), v2 = sub(ld_node(xyz, q.z), p0), v3 = sub(ld_node(xyz, q.w), p0);
-  cf[1] = cross(v2, v3);
-  cf[2] = cross(v3, v1);
-  cf[3] = cross(v1, v2);
-  cf[0] = d3{-(cf[1].x + cf[2].x + cf[3].x), -(cf[1].y + cf[2].y + cf[3].y), -(cf[1].z + cf[2].z + cf[3].z)};
-  double det = fabs(dot(v1, cf[1]));
-  *vol = det / 6.0;
-  *s = 1.0 / (6.0 * det);
-}
-
 // 32-byte row stores / loads as two 16-byte vector accesses (rows are 32-byte aligned)
 __device__ __forceinline__ void st4(double* p, double a, double b, double c, double d) {
   reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
@@ -79,6 +66,7 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double v[4]) {
 // ---------------------------------------------------------------------------
 // Element kernels (one thread per cell).
 
+// AFEM_FORMULATION_MINIMAL.
 // Poisson tetrahedron: 4 rows of 4 values, row i at er[inv[c][i] * 4] as
 // (K_ii, then K_ij for j != i increasing).  FP64 issue is the binding limit
 // on GB300, so the element is computed with few FP64 instructions (72 per
@@ -91,13 +79,16 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double v[4]) {
 __global__ void __launch_bounds__(256) k_elem_poisson_tet(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
                                                           const int32_t* __restrict__ inv,
-                                                          const double* __restrict__ coeff, double* __restrict__ er) {
+                                                          const double* __restrict__ coeff, double* __restrict__ er,
+                                                          int* __restrict__ bad) {
   for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
     const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
     const d3 p0 = ld_node(xyz, q.x);
     const d3 v1 = sub(ld_node(xyz, q.y), p0), v2 = sub(ld_node(xyz, q.z), p0), v3 = sub(ld_node(xyz, q.w), p0);
     const d3 c1 = cross(v2, v3), c2 = cross(v3, v1), c3 = cross(v1, v2);
-    double s = __drcp_rn(6.0 * fabs(dot(v1, c1)));
+    const double v6 = 6.0 * fabs(dot(v1, c1));
+    if (bad && !ref::measure_ok(v6)) atomicOr(bad, kFlagDegenerateCell);
+    double s = __drcp_rn(v6);
     if (coeff) s *= __ldg(coeff + c);
     const double k11 = s * dot(c1, c1), k22 = s * dot(c2, c2), k33 = s * dot(c3, c3);
     const double k12 = s * dot(c1, c2), k13 = s * dot(c1, c3), k23 = s * dot(c2, c3);
@@ -114,7 +105,8 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tet(int cell0, int nb_cell
 __global__ void __launch_bounds__(256) k_elem_poisson_tri(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                           const int32_t* __restrict__ cn,
                                                           const int32_t* __restrict__ inv,
-                                                          const double* __restrict__ coeff, double* __restrict__ er) {
+                                                          const double* __restrict__ coeff, double* __restrict__ er,
+                                                          int* __restrict__ bad) {
   for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
     const int32_t* q = cn + 3 * c;
     const double* a0 = xyz + 3 * (int64_t)__ldg(q);
@@ -124,6 +116,7 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tri(int cell0, int nb_cell
     double v1x = __ldg(a1) - x0, v1y = __ldg(a1 + 1) - y0;
     double v2x = __ldg(a2) - x0, v2y = __ldg(a2 + 1) - y0;
     double A2 = v1x * v2y - v1y * v2x;
+    if (bad && !ref::measure_ok(A2)) atomicOr(bad, kFlagDegenerateCell);
     double s = 1.0 / (2.0 * fabs(A2));
     if (coeff) s *= __ldg(coeff + c);
     // c1 = (v2y, -v2x), c2 = (-v1y, v1x), c0 = -(c1 + c2)
@@ -138,6 +131,90 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tri(int cell0, int nb_cell
     r0[0] = -(k01 + k02); r0[1] = k01; r0[2] = k02;
     r1[0] = -(k01 + k12); r1[1] = k01; r1[2] = k12;
     r2[0] = -(k02 + k12); r2[1] = k02; r2[2] = k12;
+  }
+}
+
+// AFEM_FORMULATION_REFERENCE / _TESTLAB, Poisson P1 (NPC = 3 triangles, 4
+// tetrahedra): the element in the reference's own rounding (afem_elem_ref.cuh).
+// Rows are laid out as above (row i at er[inv[c][i] * NPC], diagonal first,
+// then the other cell nodes increasing); each row is the reference's element
+// vector of its own node, which in the module formulation is not the
+// transpose of the column bit for bit ((vol dx_i) dx_k against (vol dx_k) dx_i),
+// so every row is formed: 4 x 23 + ~130 FP64 instructions per tetrahedron
+// (divisions included) against 72 for the minimal form.  A cell coefficient
+// multiplies each entry as the node-wise loop does (coeff * v).
+template <int NPC, int F>
+__global__ void __launch_bounds__(128) k_elem_poisson_p1_ref(int cell0, int nb_cell, const double* __restrict__ xyz,
+                                                             const int32_t* __restrict__ cn,
+                                                             const int32_t* __restrict__ inv,
+                                                             const double* __restrict__ coeff,
+                                                             double* __restrict__ er, int* __restrict__ bad) {
+  for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int32_t nid[NPC], pos[NPC];
+    if constexpr (NPC == 4) {
+      const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
+      const int4 p = __ldg(reinterpret_cast<const int4*>(inv) + c);
+      nid[0] = q.x; nid[1] = q.y; nid[2] = q.z; nid[3] = q.w;
+      pos[0] = p.x; pos[1] = p.y; pos[2] = p.z; pos[3] = p.w;
+    } else {
+#pragma unroll
+      for (int a = 0; a < NPC; ++a) {
+        nid[a] = __ldg(cn + NPC * c + a);
+        pos[a] = __ldg(inv + NPC * c + a);
+      }
+    }
+    double n[NPC][3];
+#pragma unroll
+    for (int a = 0; a < NPC; ++a) {
+      const double* p = xyz + 3 * (int64_t)nid[a];
+      n[a][0] = __ldg(p);
+      n[a][1] = __ldg(p + 1);
+      n[a][2] = __ldg(p + 2);
+    }
+    double K[NPC][NPC], meas;
+    if constexpr (F == AFEM_FORMULATION_TESTLAB) {
+      if constexpr (NPC == 4) meas = ref::testlab_tet(n, K);
+      else meas = ref::testlab_tri(n, K);
+#pragma unroll
+      for (int i = 0; i < NPC; ++i)
+#pragma unroll
+        for (int k = 0; k < i; ++k) K[i][k] = K[k][i];
+    } else if constexpr (NPC == 4) {
+      double g[3][4], vol;
+      meas = ref::tet_gradients(n, g, &vol);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) ref::tet_row(g, vol, i, K[i]);
+    } else {
+      double dx[3], dy[3], area;
+      meas = ref::tri_gradients(n, dx, dy, &area);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) ref::tri_row(dx, dy, area, i, K[i]);
+    }
+    if (bad && !ref::measure_ok(meas)) atomicOr(bad, kFlagDegenerateCell);
+    if (coeff) {
+      const double k = __ldg(coeff + c);
+#pragma unroll
+      for (int i = 0; i < NPC; ++i)
+#pragma unroll
+        for (int j = 0; j < NPC; ++j) K[i][j] = ref::mul(k, K[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < NPC; ++i) {
+      double r[NPC];
+      r[0] = K[i][i];
+      int q = 1;
+#pragma unroll
+      for (int j = 0; j < NPC; ++j)
+        if (j != i) r[q++] = K[i][j];
+      double* dst = er + NPC * (int64_t)pos[i];
+      if constexpr (NPC == 4) {
+        st4(dst, r[0], r[1], r[2], r[3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < NPC; ++j) dst[j] = r[j];
+      }
+    }
   }
 }
 
@@ -169,11 +246,31 @@ __device__ __forceinline__ int elast_packed(int i, int m, int a, int b) {
   return pair * 9 + (i < m ? a * 3 + b : b * 3 + a);
 }
 
+// One entry of the reference's elasticity row block (modules/elasticity/
+// ElementMatrix.h:216-301) for row component a, column component b, with
+// P[x][y] = dN_row/dx_x * dN_col/dx_y: of the reference's twelve-vector sums
+// ne + ce + se, every term with a zero factor is an exact zero, which leaves
+//   a == b: (l2m P_aa) vol + (mu (P_bb + P_cc)) vol  (b, c the two other axes,
+//           summed in the reference's order)
+//   a != b: (lambda P_ab) vol + (mu P_ba) vol
+// with each product rounded as the reference rounds it.  The products commute,
+// so K is symmetric bit for bit.
+__device__ __forceinline__ double elast_ref_entry(int a, int b, const double P[3][3], double l2m, double lambda,
+                                                  double mu, double vol) {
+  using namespace ref;
+  if (a == b) {
+    const double z = a == 0 ? add(P[1][1], P[2][2]) : (a == 1 ? add(P[0][0], P[2][2]) : add(P[1][1], P[0][0]));
+    return add(mul(mul(l2m, P[a][a]), vol), mul(mul(mu, z), vol));
+  }
+  return add(mul(mul(lambda, P[a][b]), vol), mul(mul(mu, P[b][a]), vol));
+}
+
+template <int F>
 __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                                          const int32_t* __restrict__ cn,
                                                                          const int32_t* __restrict__ inv,
                                                                          double lambda, double mu,
-                                                                         double* __restrict__ er) {
+                                                                         double* __restrict__ er, int* __restrict__ bad) {
   __shared__ double stage[kElastElemBlock][kElastPacked + 1];
   __shared__ int4 stage_p[kElastElemBlock];
   // src_tab[n][q]: packed positions of entries 2q and 2q + 1 of node n's row block
@@ -196,7 +293,53 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
   for (int64_t base = cell0 + blockIdx.x * (int64_t)blockDim.x; base < nb_cell; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = base + threadIdx.x;
     double* my = stage[threadIdx.x];
-    if (c < nb_cell) {
+    if (c < nb_cell && F != AFEM_FORMULATION_MINIMAL) {
+      // reference rounding: gradients and volume of the reference, then the 78
+      // distinct entries (6 node-pair blocks, 4 symmetric diagonal blocks)
+      const int4 q = __ldg(reinterpret_cast<const int4*>(cn) + c);
+      const int32_t nid[4] = {q.x, q.y, q.z, q.w};
+      double n[4][3];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const double* p = xyz + 3 * (int64_t)nid[a];
+        n[a][0] = __ldg(p);
+        n[a][1] = __ldg(p + 1);
+        n[a][2] = __ldg(p + 2);
+      }
+      double g[3][4], vol;
+      const double v6 = ref::tet_gradients(n, g, &vol);
+      if (bad && !ref::measure_ok(v6)) atomicOr(bad, kFlagDegenerateCell);
+      stage_p[threadIdx.x] = __ldg(reinterpret_cast<const int4*>(inv) + c);
+      const double l2m = ref::add(lambda, 2.0 * mu);
+#pragma unroll
+      for (int lo = 0; lo < 4; ++lo)
+#pragma unroll
+        for (int hi = lo + 1; hi < 4; ++hi) {
+          const int pair = lo * (7 - lo) / 2 + (hi - lo - 1);
+          double P[3][3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) P[a][b] = ref::mul(g[a][lo], g[b][hi]);
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) my[pair * 9 + a * 3 + b] = elast_ref_entry(a, b, P, l2m, lambda, mu, vol);
+        }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        double P[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = a; b < 3; ++b) P[a][b] = P[b][a] = ref::mul(g[a][i], g[b][i]);
+        int k = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = a; b < 3; ++b, ++k) my[54 + i * 6 + k] = elast_ref_entry(a, b, P, l2m, lambda, mu, vol);
+      }
+    } else if (c < nb_cell) {
       // cofactors c_1..c_3 of the edges from node 0 and s = 1 / (6 |det|);
       // with G_n = s c_n the block of nodes (n, m) is
       //   K_nm = lambda G_n G_m^T + mu G_m G_n^T + mu (G_n . G_m) I  (times 6 |det| s = 1 here)
@@ -206,7 +349,9 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
       const d3 p0 = ld_node(xyz, q.x);
       const d3 v1 = sub(ld_node(xyz, q.y), p0), v2 = sub(ld_node(xyz, q.z), p0), v3 = sub(ld_node(xyz, q.w), p0);
       const d3 c1 = cross(v2, v3), c2 = cross(v3, v1), c3 = cross(v1, v2);
-      const double s = __drcp_rn(6.0 * fabs(dot(v1, c1)));
+      const double v6 = 6.0 * fabs(dot(v1, c1));
+      if (bad && !ref::measure_ok(v6)) atomicOr(bad, kFlagDegenerateCell);
+      const double s = __drcp_rn(v6);
       const double ls = lambda * s, ms = mu * s, lms = (lambda + mu) * s;
       stage_p[threadIdx.x] = __ldg(reinterpret_cast<const int4*>(inv) + c);
       const double cv[3][3] = {{c1.x, c1.y, c1.z}, {c2.x, c2.y, c2.z}, {c3.x, c3.y, c3.z}};
@@ -505,10 +650,26 @@ __device__ __forceinline__ void write_rows_q1(const double (&K)[N][N], const int
   }
 }
 
+// Reference-rounding derivative tables (compile-time, the reference's expressions).
+__constant__ ref::QuadDN kQuadDnRef = ref::make_quad_dn();
+__constant__ ref::HexDN kHexDnRef = ref::make_hex_dn();
+
+template <int N>
+__device__ __forceinline__ void scale_upper(double (&K)[N][N], double k) {
+#pragma unroll
+  for (int a = 0; a < N; ++a)
+#pragma unroll
+    for (int b = a; b < N; ++b) K[a][b] = ref::mul(k, K[a][b]);
+}
+
+// F = AFEM_FORMULATION_MINIMAL: the fewest FP64 instructions (below);
+// otherwise the reference's own rounding (ref::quad4_matrix / hexa8_matrix).
+template <int F>
 __global__ void __launch_bounds__(128) k_elem_poisson_quad4(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                             const int32_t* __restrict__ cn,
                                                             const int32_t* __restrict__ inv,
-                                                            const double* __restrict__ coeff, double* __restrict__ er) {
+                                                            const double* __restrict__ coeff, double* __restrict__ er,
+                                                            int* __restrict__ bad) {
   for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell;
        c += (int64_t)gridDim.x * blockDim.x) {
     double x[4], y[4];
@@ -519,6 +680,13 @@ __global__ void __launch_bounds__(128) k_elem_poisson_quad4(int cell0, int nb_ce
       y[a] = __ldg(p + 1);
     }
     double K[4][4];
+    if constexpr (F != AFEM_FORMULATION_MINIMAL) {
+      const bool ok = ref::quad4_matrix(x, y, kQuadDnRef, K);
+      if (bad && !ok) atomicOr(bad, kFlagDegenerateCell);
+      if (coeff) scale_upper<4>(K, __ldg(coeff + c));
+      write_rows_q1<4>(K, inv + 4 * c, er);
+      continue;
+    }
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -537,6 +705,7 @@ __global__ void __launch_bounds__(128) k_elem_poisson_quad4(int cell0, int nb_ce
         j11 += deta[a] * y[a];
       }
       const double det = j00 * j11 - j01 * j10;
+      if (bad && !ref::measure_ok(det)) atomicOr(bad, kFlagDegenerateCell);
       const double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
       double dx[4], dy[4];
 #pragma unroll
@@ -577,10 +746,12 @@ __constant__ double kHexDN[8][3][8] = {
     {{-kHpm, kHpm, kHpp, -kHpp, -kHmm, kHmm, kHpm, -kHpm}, {-kHpm, -kHpp, kHpp, kHpm, -kHmm, -kHpm, kHpm, kHmm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}},
     {{-kHmm, kHmm, kHpm, -kHpm, -kHpm, kHpm, kHpp, -kHpp}, {-kHmm, -kHpm, kHpm, kHmm, -kHpm, -kHpp, kHpp, kHpm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}}};
 
+template <int F>
 __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                             const int32_t* __restrict__ cn,
                                                             const int32_t* __restrict__ inv,
-                                                            const double* __restrict__ coeff, double* __restrict__ er) {
+                                                            const double* __restrict__ coeff, double* __restrict__ er,
+                                                            int* __restrict__ bad) {
   for (int64_t c = cell0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell;
        c += (int64_t)gridDim.x * blockDim.x) {
     double x[8], y[8], z[8];
@@ -592,6 +763,13 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_ce
       z[a] = __ldg(p + 2);
     }
     double K[8][8];
+    if constexpr (F != AFEM_FORMULATION_MINIMAL) {
+      const bool ok = ref::hexa8_matrix(x, y, z, kHexDnRef, K);
+      if (bad && !ok) atomicOr(bad, kFlagDegenerateCell);
+      if (coeff) scale_upper<8>(K, __ldg(coeff + c));
+      write_rows_q1<8>(K, inv + 8 * c, er);
+      continue;
+    }
 #pragma unroll
     for (int a = 0; a < 8; ++a)
 #pragma unroll
@@ -646,6 +824,7 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_ce
       const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
       const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
       const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+      if (bad && !ref::measure_ok(det)) atomicOr(bad, kFlagDegenerateCell);
       const double id = 1.0 / det;
       const double v00 = c00 * id, v10 = c01 * id, v20 = c02 * id;
       const double v01 = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
@@ -681,83 +860,58 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_ce
   }
 }
 
-// Constant source on Quad4 / Hexa8 cells, 2 x 2 (x 2) Gauss points: each
-// (cell, local node) term sum_gp N_i qdot w detJ goes to its incidence slot
+// Constant source on Quad4 / Hexa8 cells, 2 x 2 (x 2) Gauss points
 // (applyConstantSourceToRhsQuad4 / Hexa8, femutils/ArcaneFemFunctionsGpu.cc:
-// 393-458,875-960, which adds per Gauss point with atomics).
+// 393-458,875-960, which adds every Gauss-point term with an atomic).  Each
+// (cell, local node, Gauss point) term N_a qdot (w detJ), w = 1, rounded as
+// the reference rounds it, goes to its incidence slot term[inv[c][a] * NG + g];
+// k_incidence_gp_sum then adds a node's terms in increasing cell order and, per
+// cell, in Gauss-point order: the deterministic order of a sequential cell
+// loop.  Jacobians in the reference's rounding (afem_elem_ref.cuh).
 template <int N>
 __global__ void __launch_bounds__(128) k_cell_source_q1(int nb_cell, const double* __restrict__ xyz,
                                                         const int32_t* __restrict__ cn,
                                                         const int32_t* __restrict__ inv, double qdot,
                                                         double* __restrict__ term) {
+  constexpr int NG = N;   // 4 Gauss points for Quad4, 8 for Hexa8
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
-    double x[N], y[N], z[N], acc[N];
+    double x[N], y[N], z[N];
+    int32_t pos[N];
 #pragma unroll
     for (int a = 0; a < N; ++a) {
       const double* p = xyz + 3 * (int64_t)__ldg(cn + N * c + a);
       x[a] = __ldg(p);
       y[a] = __ldg(p + 1);
       z[a] = __ldg(p + 2);
-      acc[a] = 0.0;
+      pos[a] = __ldg(inv + N * c + a);
     }
 #pragma unroll 1
-    for (int g = 0; g < (N == 4 ? 4 : 8); ++g) {
-      double det, Nf[N];
+    for (int g = 0; g < NG; ++g) {
+      double det;
+      const double* Nf;
       if constexpr (N == 4) {
-        const double xi = (g >> 1) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
-        Nf[0] = 0.25 * (1.0 - xi) * (1.0 - eta);
-        Nf[1] = 0.25 * (1.0 + xi) * (1.0 - eta);
-        Nf[2] = 0.25 * (1.0 + xi) * (1.0 + eta);
-        Nf[3] = 0.25 * (1.0 - xi) * (1.0 + eta);
-        const double dxi[4] = {-0.25 * (1.0 - eta), 0.25 * (1.0 - eta), 0.25 * (1.0 + eta), -0.25 * (1.0 + eta)};
-        const double deta[4] = {-0.25 * (1.0 - xi), -0.25 * (1.0 + xi), 0.25 * (1.0 + xi), 0.25 * (1.0 - xi)};
-        double j00 = 0.0, j01 = 0.0, j10 = 0.0, j11 = 0.0;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          j00 += dxi[a] * x[a];
-          j01 += dxi[a] * y[a];
-          j10 += deta[a] * x[a];
-          j11 += deta[a] * y[a];
-        }
-        det = j00 * j11 - j01 * j10;
+        double J[2][2];
+        det = ref::quad4_jacobian(x, y, kQuadDnRef, g, J);
+        Nf = kQuadDnRef.N[g];
       } else {
-        const double xi = (g >> 2) ? kGauss : -kGauss, eta = ((g >> 1) & 1) ? kGauss : -kGauss,
-                     zeta = (g & 1) ? kGauss : -kGauss;
-        const double mx = 1.0 - xi, px = 1.0 + xi, me = 1.0 - eta, pe = 1.0 + eta, mz = 1.0 - zeta, pz = 1.0 + zeta;
-        Nf[0] = 0.125 * mx * me * mz; Nf[1] = 0.125 * px * me * mz; Nf[2] = 0.125 * px * pe * mz;
-        Nf[3] = 0.125 * mx * pe * mz; Nf[4] = 0.125 * mx * me * pz; Nf[5] = 0.125 * px * me * pz;
-        Nf[6] = 0.125 * px * pe * pz; Nf[7] = 0.125 * mx * pe * pz;
-        const double dxi[8] = {-0.125 * me * mz, 0.125 * me * mz, 0.125 * pe * mz, -0.125 * pe * mz,
-                               -0.125 * me * pz, 0.125 * me * pz, 0.125 * pe * pz, -0.125 * pe * pz};
-        const double deta[8] = {-0.125 * mx * mz, -0.125 * px * mz, 0.125 * px * mz, 0.125 * mx * mz,
-                                -0.125 * mx * pz, -0.125 * px * pz, 0.125 * px * pz, 0.125 * mx * pz};
-        const double dzeta[8] = {-0.125 * mx * me, -0.125 * px * me, -0.125 * px * pe, -0.125 * mx * pe,
-                                 0.125 * mx * me, 0.125 * px * me, 0.125 * px * pe, 0.125 * mx * pe};
-        double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          J[0][0] += dxi[a] * x[a]; J[0][1] += dxi[a] * y[a]; J[0][2] += dxi[a] * z[a];
-          J[1][0] += deta[a] * x[a]; J[1][1] += deta[a] * y[a]; J[1][2] += deta[a] * z[a];
-          J[2][0] += dzeta[a] * x[a]; J[2][1] += dzeta[a] * y[a]; J[2][2] += dzeta[a] * z[a];
-        }
-        det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-              J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        double J[3][3], mm[3];
+        det = ref::hexa8_jacobian(x, y, z, kHexDnRef, g, J, mm);
+        Nf = kHexDnRef.N[g];
       }
 #pragma unroll
-      for (int a = 0; a < N; ++a) acc[a] += Nf[a] * qdot * det;
+      for (int a = 0; a < N; ++a) term[(int64_t)pos[a] * NG + g] = ref::mul(ref::mul(Nf[a], qdot), det);
     }
-    const int32_t* ip = inv + N * c;
-#pragma unroll
-    for (int a = 0; a < N; ++a) term[__ldg(ip + a)] = acc[a];
   }
 }
 
-// rhs[n * nb_dof] = sum of the node's incidence terms (increasing cell order)
+// rhs[n * nb_dof] = sum of the node's incidence terms, `per` consecutive
+// terms per incidence (increasing cell order, then term order)
 __global__ void k_incidence_sum(int nb_node, const int32_t* __restrict__ nc_ptr, const double* __restrict__ term,
-                                int nb_dof, double* __restrict__ rhs) {
+                                int per, int nb_dof, double* __restrict__ rhs) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb_node; n += gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int32_t p = nc_ptr[n]; p < nc_ptr[n + 1]; ++p) s += term[p];
+    const int64_t t1 = (int64_t)nc_ptr[n + 1] * per;
+    for (int64_t t = (int64_t)nc_ptr[n] * per; t < t1; ++t) s = __dadd_rn(s, term[t]);
     rhs[(int64_t)n * nb_dof] = s;
   }
 }
@@ -833,27 +987,31 @@ __global__ void k_face_gather(int nb_node, const int32_t* __restrict__ ptr, cons
   }
 }
 
+// Cell measure in the reference's rounding: computeAreaTria3 /
+// computeVolumeTetra4 (femutils/ArcaneFemFunctionsGpu.h:76-86,113-128).
+__device__ __forceinline__ double cell_measure_ref(int dim, const double* __restrict__ xyz,
+                                                   const int32_t* __restrict__ cn, int64_t c) {
+  const int npc = dim + 1;
+  double n[4][3];
+  for (int a = 0; a < npc; ++a) {
+    const double* p = xyz + 3 * (int64_t)__ldg(cn + npc * c + a);
+    n[a][0] = __ldg(p);
+    n[a][1] = __ldg(p + 1);
+    n[a][2] = __ldg(p + 2);
+  }
+  if (dim == 2) {
+    const double t[3][3] = {{n[0][0], n[0][1], n[0][2]}, {n[1][0], n[1][1], n[1][2]}, {n[2][0], n[2][1], n[2][2]}};
+    return ref::tri_area(t);
+  }
+  return ref::tet_volume(n);
+}
+
+// w_c = (qdot * measure) / npc, each operation rounded as the reference's
+// sum += qdot * domain / nbItem rounds it.
 __global__ void k_cell_source_weight(int nb_cell, int dim, const double* __restrict__ xyz,
                                      const int32_t* __restrict__ cn, double qdot, double* __restrict__ w) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
-    double meas;
-    int npc;
-    if (dim == 2) {
-      const int32_t* q = cn + 3 * c;
-      const double* a0 = xyz + 3 * (int64_t)q[0];
-      const double* a1 = xyz + 3 * (int64_t)q[1];
-      const double* a2 = xyz + 3 * (int64_t)q[2];
-      double v1x = a1[0] - a0[0], v1y = a1[1] - a0[1], v2x = a2[0] - a0[0], v2y = a2[1] - a0[1];
-      meas = fabs(v1x * v2y - v1y * v2x) / 2.0;
-      npc = 3;
-    } else {
-      d3 cf[4];
-      double s;
-      tet_cofactors(xyz, cn, c, cf, &s, &meas);
-      npc = 4;
-    }
-    w[c] = qdot * meas / npc;
-  }
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x)
+    w[c] = __ddiv_rn(__dmul_rn(qdot, cell_measure_ref(dim, xyz, cn, c)), (double)(dim + 1));
 }
 
 // rhs[node * stride + off] = sum_{cells, increasing} w_c                 (body = 0)
@@ -866,8 +1024,8 @@ __global__ void k_node_sum(int nb_node, const int32_t* __restrict__ nc_ptr, cons
     int64_t d = (int64_t)n * stride + off;
     double sum = body ? rhs[d] : 0.0;
     for (int32_t p = nc_ptr[n]; p < nc_ptr[n + 1]; ++p) {
-      double wc = w[nc_cell[p]];
-      sum += body ? f * wc / 4 : wc;
+      const double wc = w[nc_cell[p]];
+      sum = __dadd_rn(sum, body ? __dmul_rn(__dmul_rn(f, wc), 0.25) : wc);   // f * volume / 4 (exact quarter)
     }
     rhs[d] = sum;
   }
@@ -875,12 +1033,8 @@ __global__ void k_node_sum(int nb_node, const int32_t* __restrict__ nc_ptr, cons
 
 __global__ void k_cell_volume(int nb_cell, const double* __restrict__ xyz, const int32_t* __restrict__ cn,
                               double* __restrict__ vol) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
-    d3 cf[4];
-    double s, v;
-    tet_cofactors(xyz, cn, c, cf, &s, &v);
-    vol[c] = v;
-  }
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x)
+    vol[c] = cell_measure_ref(3, xyz, cn, c);
 }
 
 static afem_status check_mesh(const afem_mesh_view* m, const char* who) {
@@ -915,14 +1069,75 @@ namespace afem {
 // tetrahedra 1.28 / 0.59 / 0.56 / 0.57 / 0.62 / 1.02 (default 1.00), Hexa8
 // 0.50 / 0.38 / 0.37 / 0.36 / 0.37 / 0.50 (default 0.50).  The elasticity
 // gather is best at its default (1.90 ms; 1.92 at 75 %, 2.48 at 50 %).
+// The attribute belongs to the device that is current when it is set, so it
+// is set once per device (bit d of g_gather_attrs_set), on first use there.
+static std::atomic<uint64_t> g_gather_attrs_set{0};
 static void gather_attrs() {
-  static const bool done = [] {
-    cudaFuncSetAttribute(k_gather_scalar<3>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
-    cudaFuncSetAttribute(k_gather_scalar<4>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
-    cudaFuncSetAttribute(k_gather_scalar<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
-    return true;
-  }();
-  (void)done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  const uint64_t bit = uint64_t(1) << dev;
+  if (g_gather_attrs_set.load(std::memory_order_acquire) & bit) return;
+  cudaFuncSetAttribute(k_gather_scalar<3>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
+  cudaFuncSetAttribute(k_gather_scalar<4>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
+  cudaFuncSetAttribute(k_gather_scalar<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
+  g_gather_attrs_set.fetch_or(bit, std::memory_order_acq_rel);
+}
+}  // namespace afem
+
+namespace afem {
+// Element-kernel launches over cells [c0, c1), by the context's formulation.
+// The reference-rounding kernels hold more live values (about 130 registers
+// per thread), so they run 128-thread blocks.
+static afem_status launch_elem_p1(afem_context ctx, const afem_mesh_view* m, int c0, int c1, const double* coeff,
+                                  double* ke) {
+  const int f = ctx->formulation;
+  int* bad = ctx->flags_d;
+  if (f == AFEM_FORMULATION_MINIMAL) {
+    const unsigned ge = grid_for(ctx, c1 - c0, 256, 16);
+    if (m->dim == 3)
+      return launch(ctx, k_elem_poisson_tet, ge, 256, 0, c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d, coeff,
+                    ke, bad);
+    return launch(ctx, k_elem_poisson_tri, ge, 256, 0, c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d, coeff, ke,
+                  bad);
+  }
+  const unsigned ge = grid_for(ctx, c1 - c0, 128, 32);
+  if (m->dim == 3)
+    return f == AFEM_FORMULATION_TESTLAB
+               ? launch(ctx, k_elem_poisson_p1_ref<4, AFEM_FORMULATION_TESTLAB>, ge, 128, 0, c0, c1, m->coords_d,
+                        m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad)
+               : launch(ctx, k_elem_poisson_p1_ref<4, AFEM_FORMULATION_REFERENCE>, ge, 128, 0, c0, c1, m->coords_d,
+                        m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad);
+  return f == AFEM_FORMULATION_TESTLAB
+             ? launch(ctx, k_elem_poisson_p1_ref<3, AFEM_FORMULATION_TESTLAB>, ge, 128, 0, c0, c1, m->coords_d,
+                      m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad)
+             : launch(ctx, k_elem_poisson_p1_ref<3, AFEM_FORMULATION_REFERENCE>, ge, 128, 0, c0, c1, m->coords_d,
+                      m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad);
+}
+
+static afem_status launch_elem_q1(afem_context ctx, const afem_mesh_view* m, int c0, int c1, const double* coeff,
+                                  double* ke) {
+  const bool minimal = ctx->formulation == AFEM_FORMULATION_MINIMAL;
+  int* bad = ctx->flags_d;
+  const unsigned ge = grid_for(ctx, c1 - c0, 128, 16);
+  if (m->dim == 3)
+    return minimal ? launch(ctx, k_elem_poisson_hexa8<AFEM_FORMULATION_MINIMAL>, ge, 128, 0, c0, c1, m->coords_d,
+                            m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad)
+                   : launch(ctx, k_elem_poisson_hexa8<AFEM_FORMULATION_REFERENCE>, ge, 128, 0, c0, c1, m->coords_d,
+                            m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad);
+  return minimal ? launch(ctx, k_elem_poisson_quad4<AFEM_FORMULATION_MINIMAL>, ge, 128, 0, c0, c1, m->coords_d,
+                          m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad)
+                 : launch(ctx, k_elem_poisson_quad4<AFEM_FORMULATION_REFERENCE>, ge, 128, 0, c0, c1, m->coords_d,
+                          m->cell_nodes_d, m->nc_inverse_d, coeff, ke, bad);
+}
+
+static afem_status launch_elem_elasticity(afem_context ctx, const afem_mesh_view* m, int c0, int c1, double lambda,
+                                          double mu, double* ke) {
+  const unsigned ge = grid_for(ctx, c1 - c0, kElastElemBlock, 32);
+  if (ctx->formulation == AFEM_FORMULATION_MINIMAL)
+    return launch(ctx, k_elem_elasticity_tet<AFEM_FORMULATION_MINIMAL>, ge, kElastElemBlock, 0, c0, c1, m->coords_d,
+                  m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke, ctx->flags_d);
+  return launch(ctx, k_elem_elasticity_tet<AFEM_FORMULATION_REFERENCE>, ge, kElastElemBlock, 0, c0, c1, m->coords_d,
+                m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke, ctx->flags_d);
 }
 }  // namespace afem
 
@@ -935,12 +1150,7 @@ afem_status afem_element_matrices_poisson_p1(afem_context ctx, const afem_mesh_v
   AFEM_CHECK_ARG(ctx, "afem_element_matrices_poisson_p1: null context");
   AFEM_TRY(check_assembly(m, "afem_element_matrices_poisson_p1"));
   AFEM_CHECK_ARG(ke && ((uintptr_t)ke & 31) == 0, "afem_element_matrices_poisson_p1: ke null or not 32-byte aligned");
-  unsigned ge = grid_for(ctx, m->nb_cell, 256, 16);
-  if (m->dim == 3)
-    return launch(ctx, k_elem_poisson_tet, ge, 256, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                  cell_coeff_d, ke);
-  return launch(ctx, k_elem_poisson_tri, ge, 256, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                cell_coeff_d, ke);
+  return launch_elem_p1(ctx, m, 0, m->nb_cell, cell_coeff_d, ke);
 }
 
 afem_status afem_gather_poisson_p1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
@@ -1030,7 +1240,7 @@ afem_status afem_gather_to_host(afem_context ctx, const afem_mesh_view* m, int k
                                 cudaMemcpyDeviceToHost, cs));
   }
   AFEM_CUDA(cudaStreamSynchronize(cs));
-  return AFEM_OK;
+  return check_flags(ctx);
 }
 
 }  // extern "C"
@@ -1141,26 +1351,12 @@ static afem_status assemble_to_host_impl(afem_context ctx, const afem_mesh_view*
     if (coords_h && h2d_at[k] >= 0 && (k == 0 || h2d_at[k] != h2d_at[k - 1]))
       AFEM_CUDA(cudaStreamWaitEvent(s, ctx->h2d_ev[h2d_at[k]], 0));
     if (c1 > c0) {
-      if (kind == AFEM_GATHER_ELASTICITY_TET4) {
-        AFEM_TRY(launch(ctx, k_elem_elasticity_tet, grid_for(ctx, c1 - c0, kElastElemBlock, 32), kElastElemBlock, 0,
-                        c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke));
-      } else if (kind == AFEM_GATHER_POISSON_Q1) {
-        const unsigned ge = grid_for(ctx, c1 - c0, 128, 16);
-        if (m->dim == 3)
-          AFEM_TRY(launch(ctx, k_elem_poisson_hexa8, ge, 128, 0, c0, c1, m->coords_d, m->cell_nodes_d,
-                          m->nc_inverse_d, cell_coeff_d, ke));
-        else
-          AFEM_TRY(launch(ctx, k_elem_poisson_quad4, ge, 128, 0, c0, c1, m->coords_d, m->cell_nodes_d,
-                          m->nc_inverse_d, cell_coeff_d, ke));
-      } else {
-        const unsigned ge = grid_for(ctx, c1 - c0, 256, 16);
-        if (m->dim == 3)
-          AFEM_TRY(launch(ctx, k_elem_poisson_tet, ge, 256, 0, c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                          cell_coeff_d, ke));
-        else
-          AFEM_TRY(launch(ctx, k_elem_poisson_tri, ge, 256, 0, c0, c1, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                          cell_coeff_d, ke));
-      }
+      if (kind == AFEM_GATHER_ELASTICITY_TET4)
+        AFEM_TRY(launch_elem_elasticity(ctx, m, c0, c1, lambda, mu, ke));
+      else if (kind == AFEM_GATHER_POISSON_Q1)
+        AFEM_TRY(launch_elem_q1(ctx, m, c0, c1, cell_coeff_d, ke));
+      else
+        AFEM_TRY(launch_elem_p1(ctx, m, c0, c1, cell_coeff_d, ke));
     }
     const int n0 = nb[k], n1 = nb[k + 1];
     if (n1 > n0) {
@@ -1183,7 +1379,7 @@ static afem_status assemble_to_host_impl(afem_context ctx, const afem_mesh_view*
   }
   AFEM_CUDA(cudaStreamSynchronize(cs));
   AFEM_CUDA(cudaStreamSynchronize(s));
-  return AFEM_OK;
+  return check_flags(ctx);
 }
 
 extern "C" {
@@ -1208,12 +1404,7 @@ afem_status afem_element_matrices_poisson_q1(afem_context ctx, const afem_mesh_v
   AFEM_CHECK_ARG(ctx, "afem_element_matrices_poisson_q1: null context");
   AFEM_TRY(check_mesh(m, "afem_element_matrices_poisson_q1"));
   AFEM_CHECK_ARG(m->nc_inverse_d && ke, "afem_element_matrices_poisson_q1: null nc_inverse / element buffer");
-  const unsigned ge = grid_for(ctx, m->nb_cell, 128, 16);
-  if (m->dim == 3)
-    return launch(ctx, k_elem_poisson_hexa8, ge, 128, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                  cell_coeff_d, ke);
-  return launch(ctx, k_elem_poisson_quad4, ge, 128, 0, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                cell_coeff_d, ke);
+  return launch_elem_q1(ctx, m, 0, m->nb_cell, cell_coeff_d, ke);
 }
 
 afem_status afem_gather_poisson_q1(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
@@ -1264,9 +1455,7 @@ afem_status afem_element_matrices_elasticity_tet4(afem_context ctx, const afem_m
   AFEM_TRY(check_assembly(m, "afem_element_matrices_elasticity_tet4"));
   AFEM_CHECK_ARG(m->dim == 3, "afem_element_matrices_elasticity_tet4: tetrahedra only (dim 3)");
   AFEM_CHECK_ARG(ke && ((uintptr_t)ke & 31) == 0, "afem_element_matrices_elasticity_tet4: ke null or misaligned");
-  return launch(ctx, k_elem_elasticity_tet, grid_for(ctx, m->nb_cell, kElastElemBlock, 32), kElastElemBlock, 0, 0,
-                m->nb_cell, m->coords_d,
-                m->cell_nodes_d, m->nc_inverse_d, lambda, mu, ke);
+  return launch_elem_elasticity(ctx, m, 0, m->nb_cell, lambda, mu, ke);
 }
 
 afem_status afem_gather_elasticity_tet4(afem_context ctx, const afem_mesh_view* m, const int32_t* row_ptr_d,
@@ -1314,10 +1503,10 @@ afem_status afem_rhs_constant_source_q1(afem_context ctx, const afem_mesh_view* 
   AFEM_CHECK_ARG(ctx, "afem_rhs_constant_source_q1: null context");
   AFEM_TRY(check_mesh(m, "afem_rhs_constant_source_q1"));
   AFEM_CHECK_ARG(m->nc_inverse_d && nb_dof >= 1 && rhs_d, "afem_rhs_constant_source_q1: bad arguments");
-  const size_t npc = (size_t)1 << m->dim;
-  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * npc * (size_t)m->nb_cell)));
+  const size_t npc = (size_t)1 << m->dim;   // also the Gauss points per cell
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(double) * npc * npc * (size_t)m->nb_cell)));
   double* term;
-  AFEM_TRY(scratch_take(ctx, npc * (size_t)m->nb_cell, &term));
+  AFEM_TRY(scratch_take(ctx, npc * npc * (size_t)m->nb_cell, &term));
   if (m->dim == 3)
     AFEM_TRY(launch(ctx, k_cell_source_q1<8>, grid_for(ctx, m->nb_cell, 128, 16), 128, 0, m->nb_cell, m->coords_d,
                     m->cell_nodes_d, m->nc_inverse_d, qdot, term));
@@ -1325,7 +1514,7 @@ afem_status afem_rhs_constant_source_q1(afem_context ctx, const afem_mesh_view* 
     AFEM_TRY(launch(ctx, k_cell_source_q1<4>, grid_for(ctx, m->nb_cell, 128, 16), 128, 0, m->nb_cell, m->coords_d,
                     m->cell_nodes_d, m->nc_inverse_d, qdot, term));
   return launch(ctx, k_incidence_sum, grid_for(ctx, m->nb_node, 256), 256, 0, m->nb_node, m->nc_ptr_d,
-                (const double*)term, nb_dof, rhs_d);
+                (const double*)term, (int)npc, nb_dof, rhs_d);
 }
 
 afem_status afem_rhs_body_force_tet4(afem_context ctx, const afem_mesh_view* m, double fx, double fy, double fz,
@@ -1435,6 +1624,12 @@ static afem_status noalloc_rows_address(int dev, double** out) {
 
 template <class Kernel, class... Args>
 static afem_status launch_on(cudaStream_t s, Kernel k, unsigned grid, unsigned block, Args... args) {
+  // an error left by the caller's own earlier CUDA work is reported as such,
+  // not as a failure of this launch
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess)
+    return cuda_fail(pending, "error pending before the launch (from earlier CUDA work of the caller)", __FILE__,
+                     __LINE__);
   k<<<grid, block, 0, s>>>(args...);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? AFEM_OK : cuda_fail(e, "kernel launch", __FILE__, __LINE__);
@@ -1455,26 +1650,34 @@ extern "C" afem_status afem_assemble_poisson_p1_noalloc(void* cuda_stream, const
                 "afem_assemble_poisson_p1_noalloc: %d cells need %zu doubles of element rows, above the fixed "
                 "%zu (at most %zu tetrahedra or %zu triangles); use afem_assemble_poisson_p1",
                 m->nb_cell, need, kNoAllocRows, kNoAllocRows / 16, kNoAllocRows / 9);
-  int dev = 0, sms = 0;
+  int dev = 0, sms = 0, stream_dev = 0;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
   AFEM_CUDA(cudaGetDevice(&dev));
+  AFEM_CUDA(cudaStreamGetDevice(s, &stream_dev));
+  AFEM_CHECK_ARG(stream_dev == dev,
+                 "afem_assemble_poisson_p1_noalloc: cuda_stream belongs to device %d while device %d is current; "
+                 "make the stream's device current",
+                 stream_dev, dev);
   AFEM_CHECK_ARG(dev >= 0 && dev < kNoAllocMaxDevices, "afem_assemble_poisson_p1_noalloc: device %d unsupported", dev);
   AFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   double* rows = nullptr;
   AFEM_TRY(noalloc_rows_address(dev, &rows));
   // every element row is rewritten by the element kernel before the gather
   // reads it, so nothing left by a previous call needs clearing
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
-  const int64_t eblocks = ((int64_t)m->nb_cell + 255) / 256;
-  const unsigned ge = (unsigned)std::max<int64_t>(1, std::min<int64_t>(eblocks, (int64_t)sms * 16));
+  // the element rows in the reference's rounding (AFEM_FORMULATION_REFERENCE,
+  // the default of a context); no context, so no degenerate-cell flag
+  const int64_t eblocks = ((int64_t)m->nb_cell + 127) / 128;
+  const unsigned ge = (unsigned)std::max<int64_t>(1, std::min<int64_t>(eblocks, (int64_t)sms * 32));
   const unsigned gg = (unsigned)((m->nb_node + kGatherBlock - 1) / kGatherBlock);
+  int* no_flags = nullptr;
   if (m->dim == 3) {
-    AFEM_TRY(launch_on(s, k_elem_poisson_tet, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                       cell_coeff_d, rows));
+    AFEM_TRY(launch_on(s, k_elem_poisson_p1_ref<4, AFEM_FORMULATION_REFERENCE>, ge, 128, 0, m->nb_cell, m->coords_d,
+                       m->cell_nodes_d, m->nc_inverse_d, cell_coeff_d, rows, no_flags));
     return launch_on(s, k_gather_scalar<4>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
                      (const double*)rows, values_d);
   }
-  AFEM_TRY(launch_on(s, k_elem_poisson_tri, ge, 256, 0, m->nb_cell, m->coords_d, m->cell_nodes_d, m->nc_inverse_d,
-                     cell_coeff_d, rows));
+  AFEM_TRY(launch_on(s, k_elem_poisson_p1_ref<3, AFEM_FORMULATION_REFERENCE>, ge, 128, 0, m->nb_cell, m->coords_d,
+                     m->cell_nodes_d, m->nc_inverse_d, cell_coeff_d, rows, no_flags));
   return launch_on(s, k_gather_scalar<3>, gg, kGatherBlock, 0, m->nb_node, m->nc_ptr_d, m->nc_slot_d, row_ptr_d,
                    (const double*)rows, values_d);
 }

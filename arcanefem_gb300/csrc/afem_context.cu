@@ -28,6 +28,20 @@ afem_status cuda_fail(cudaError_t e, const char* what, const char* file, int lin
   return e == cudaErrorMemoryAllocation ? AFEM_ERR_OOM : AFEM_ERR_CUDA;
 }
 
+afem_status check_flags(afem_context ctx) {
+  int* h = reinterpret_cast<int*>(static_cast<char*>(ctx->pinned) + 256);
+  AFEM_CUDA(cudaMemcpyAsync(h, ctx->flags_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int flags = *h;
+  if (flags == 0) return AFEM_OK;
+  AFEM_CUDA(cudaMemsetAsync(ctx->flags_d, 0, sizeof(int), ctx->stream));
+  AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (flags & kFlagDegenerateCell)
+    return fail(AFEM_ERR_MESH, "degenerate cell: an element kernel met a cell of zero or non-finite measure "
+                               "(volume, area or Jacobian determinant); its matrix entries are not finite");
+  return fail(AFEM_ERR_CUDA, "unknown device flag 0x%x", flags);
+}
+
 afem_status scratch_reserve(afem_context ctx, size_t bytes) {
   ctx->scratch_used = 0;
   if (bytes <= ctx->scratch_cap) return AFEM_OK;
@@ -151,8 +165,12 @@ afem_status afem_context_create(afem_context* out, void* stream) {
   ctx->stream = reinterpret_cast<cudaStream_t>(stream);
   cudaError_t e = cudaGetDevice(&ctx->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
-  if (e == cudaSuccess) e = cudaMallocHost(&ctx->pinned, 256);
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->pinned, 512);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->flags_d, 256);
+  if (e == cudaSuccess) e = cudaMemset(ctx->flags_d, 0, 256);
   if (e != cudaSuccess) {
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->flags_d) cudaFree(ctx->flags_d);
     delete ctx;
     return cuda_fail(e, "afem_context_create", __FILE__, __LINE__);
   }
@@ -178,6 +196,7 @@ afem_status afem_context_destroy(afem_context ctx) {
   for (cudaEvent_t ev : ctx->h2d_ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  if (ctx->flags_d) cudaFree(ctx->flags_d);
   delete ctx;
   if (e != cudaSuccess) return cuda_fail(e, "afem_context_destroy", __FILE__, __LINE__);
   if (e2 != cudaSuccess) return cuda_fail(e2, "afem_context_destroy", __FILE__, __LINE__);
@@ -195,6 +214,21 @@ afem_status afem_context_set_stream(afem_context ctx, void* stream) {
 afem_status afem_context_synchronize(afem_context ctx) {
   AFEM_CHECK_ARG(ctx != nullptr, "afem_context_synchronize: null context");
   AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+  return check_flags(ctx);
+}
+
+afem_status afem_context_set_element_formulation(afem_context ctx, int formulation) {
+  AFEM_CHECK_ARG(ctx != nullptr, "afem_context_set_element_formulation: null context");
+  AFEM_CHECK_ARG(formulation == AFEM_FORMULATION_REFERENCE || formulation == AFEM_FORMULATION_TESTLAB ||
+                     formulation == AFEM_FORMULATION_MINIMAL,
+                 "afem_context_set_element_formulation: unknown formulation %d", formulation);
+  ctx->formulation = formulation;
+  return AFEM_OK;
+}
+
+afem_status afem_context_get_element_formulation(afem_context ctx, int* formulation_h) {
+  AFEM_CHECK_ARG(ctx != nullptr && formulation_h != nullptr, "afem_context_get_element_formulation: null argument");
+  *formulation_h = ctx->formulation;
   return AFEM_OK;
 }
 

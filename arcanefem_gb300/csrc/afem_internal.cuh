@@ -15,6 +15,10 @@ namespace afem {
 
 constexpr int kSmCountDefault = 152;
 
+// Bits of the context's device flag word (afem_context_s::flags_d), set by
+// kernels and reported by the next synchronous call (check_flags).
+constexpr int kFlagDegenerateCell = 1;   // an element kernel met a zero / non-finite cell measure
+
 // ---------------------------------------------------------------------------
 // Error reporting: the last message per host thread, status codes returned.
 void set_error(const char* fmt, ...);
@@ -62,6 +66,10 @@ struct afem_context_s {
   // host -> device coordinate uploads overlapped with kernels (afem_assemble_host_io), created on first use
   cudaStream_t h2d_stream = nullptr;
   cudaEvent_t h2d_ev[17] = {};
+  // element arithmetic of the assembly kernels (AFEM_FORMULATION_*)
+  int formulation = AFEM_FORMULATION_REFERENCE;
+  // device flag word (afem::kFlag*), set by kernels, read and cleared by check_flags
+  int* flags_d = nullptr;
 };
 
 namespace afem {
@@ -105,6 +113,10 @@ inline unsigned grid_for(afem_context ctx, int64_t work_items, int block, int ma
   if (need < 1) need = 1;
   return (unsigned)need;
 }
+
+// Report (and clear) the flags kernels set since the last check: waits for the
+// context stream.  AFEM_ERR_MESH for a degenerate cell.
+afem_status check_flags(afem_context ctx);
 
 // Read one device value into host memory (synchronous on the stream).
 template <class T>

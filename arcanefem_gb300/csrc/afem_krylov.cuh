@@ -17,6 +17,9 @@ constexpr int kSolveBlock = 256;
 // column and value loads are all issued before their gathers (predicated past
 // the row end with a zero weight on the row's own entry), so a thread keeps
 // kRowChunk loads in flight.  Entries are summed in increasing k order.
+// A negative column marks an unused slot of a reference CSR view
+// (femutils/CsrFormatMatrix.cc:49-50): it gets the same zero weight, so the
+// row's sum is that of its used entries.
 constexpr int kRowChunk = 8;
 
 template <class Acc, class T, class V>
@@ -30,8 +33,9 @@ __device__ __forceinline__ Acc row_dot_chunked(int row, const int32_t* __restric
     T a[kRowChunk];
 #pragma unroll
     for (int u = 0; u < kRowChunk; ++u) {
-      const bool in = k + u < e;
-      c[u] = in ? __ldg(cols + k + u) : row;
+      const int32_t cc = k + u < e ? __ldg(cols + k + u) : -1;
+      const bool in = cc >= 0;
+      c[u] = in ? cc : row;
       a[u] = in ? __ldg(vals + k + u) : T(0);
     }
 #pragma unroll
@@ -46,7 +50,10 @@ __device__ __forceinline__ double row_dot(int row, const int32_t* __restrict__ r
   if constexpr (G == 1) return row_dot_chunked<double>(row, rp, cols, vals, x);
   double s = 0.0;
   const int32_t e = __ldg(rp + row + 1);
-  for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) s += (double)__ldg(vals + k) * (double)__ldg(x + __ldg(cols + k));
+  for (int32_t k = __ldg(rp + row) + lane; k < e; k += G) {
+    const int32_t c = __ldg(cols + k);
+    if (c >= 0) s += (double)__ldg(vals + k) * (double)__ldg(x + c);
+  }
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
   return s;
@@ -205,8 +212,9 @@ __global__ void k_slice_fill(int n, const int32_t* __restrict__ rp, const int32_
     const int64_t base = (int64_t)kSlice * soff[sl] + (row & (kSlice - 1));
     const int32_t b = row < n ? rp[row] : 0, e = row < n ? rp[row + 1] : 0;
     for (int k = 0; k < m; ++k) {
-      const bool in = b + k < e;
-      if (scols) scols[base + (int64_t)kSlice * k] = in ? cols[b + k] : (row < n ? (int32_t)row : 0);
+      const int32_t c = b + k < e ? cols[b + k] : -1;   // -1: past the row, or an unused slot
+      const bool in = c >= 0;
+      if (scols) scols[base + (int64_t)kSlice * k] = in ? c : (row < n ? (int32_t)row : 0);
       svals[base + (int64_t)kSlice * k] = in ? (T)vals[b + k] : T(0);
     }
   }

@@ -24,6 +24,10 @@ struct afem_linear_system_s {
   const int32_t* cols = nullptr;
   double* values = nullptr;
   int64_t nnz = 0;
+  // row offsets [n + 1] owned by the system when the matrix came as a
+  // reference CSR view (afem_ls_set_csr_view); 1 if that view has unused slots
+  int32_t* view_row_ptr = nullptr;
+  int padded = 0;
   // row-column elimination bookkeeping
   int has_rc = 0;
   double* rc_saved = nullptr;
@@ -146,6 +150,42 @@ __global__ void k_entry(const int32_t* __restrict__ rp, const int32_t* __restric
   *flag = 1;
 }
 
+// Row offsets of a reference CSR view (rows without the trailing entry, the
+// last row ending at nb_column) and its checks: flags bit 0 = a bad row start
+// or count, bit 1 = a column out of range, bit 2 = a slot past a row's count
+// that is not -1, bit 3 = the view has unused (-1) slots.
+__global__ void k_view_rows(int n, const int32_t* __restrict__ rows, const int32_t* __restrict__ nb_col,
+                            int64_t nb_column, const int32_t* __restrict__ cols, int32_t* __restrict__ rp,
+                            int* __restrict__ flags) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+    if (i == n) {
+      rp[n] = (int32_t)nb_column;
+      continue;
+    }
+    const int32_t b = rows[i];
+    const int64_t e = i + 1 < n ? (int64_t)rows[i + 1] : nb_column;
+    rp[i] = b;
+    if (b < 0 || (int64_t)b > e) {
+      atomicOr(flags, 1);
+      continue;
+    }
+    const int64_t used = nb_col ? (int64_t)nb_col[i] : e - b;
+    if (used < 0 || b + used > e) {
+      atomicOr(flags, 1);
+      continue;
+    }
+    int f = 0;
+    for (int64_t k = b; k < e; ++k) {
+      const int32_t c = cols[k];
+      if (c >= n) f |= 2;
+      if (c < -1) f |= 2;
+      if (c == -1) f |= 8;
+      if (k >= b + used && c != -1) f |= 4;
+    }
+    if (f) atomicOr(flags, f);
+  }
+}
+
 afem_status solve_csr(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
                       const double* b, double* x, const uint8_t* forced, const afem_solver_options* opt,
                       afem_solve_info* info);
@@ -197,7 +237,7 @@ afem_status afem_ls_destroy(afem_linear_system ls) {
   if (!ls) return AFEM_OK;
   cudaStream_t s = ls->ctx->stream;
   void* ptrs[] = {ls->rhs, ls->sol, ls->forced_value, ls->elim_value, ls->forced_info, ls->elim_info, ls->flag,
-                  ls->rc_saved};
+                  ls->rc_saved, ls->view_row_ptr};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, s);
   cudaStreamSynchronize(s);
@@ -212,6 +252,36 @@ afem_status afem_ls_set_csr_values(afem_linear_system ls, const int32_t* row_ptr
   ls->cols = cols_d;
   ls->values = values_d;
   ls->nnz = nnz;
+  ls->padded = 0;
+  return AFEM_OK;
+}
+
+afem_status afem_ls_set_csr_view(afem_linear_system ls, int32_t nb_row, const int32_t* rows_d,
+                                 const int32_t* rows_nb_column_d, int64_t nb_column, const int32_t* columns_d,
+                                 double* values_d) {
+  AFEM_CHECK_ARG(ls && rows_d && columns_d && values_d && nb_column > 0 && nb_column <= INT32_MAX,
+                 "afem_ls_set_csr_view: bad arguments");
+  AFEM_CHECK_ARG(nb_row == ls->n, "afem_ls_set_csr_view: %d rows for a system of %d DoFs (the DoF family must be "
+                                  "compacted, one row per DoF)", nb_row, ls->n);
+  afem_context ctx = ls->ctx;
+  if (!ls->view_row_ptr)
+    AFEM_CUDA(cudaMallocAsync((void**)&ls->view_row_ptr, sizeof(int32_t) * ((size_t)ls->n + 1), ctx->stream));
+  AFEM_CUDA(cudaMemsetAsync(ls->flag, 0, sizeof(int), ctx->stream));
+  AFEM_TRY(launch(ctx, k_view_rows, grid_for(ctx, (int64_t)ls->n + 1, 256), 256, 0, ls->n, rows_d, rows_nb_column_d,
+                  nb_column, columns_d, ls->view_row_ptr, ls->flag));
+  int f = 0;
+  AFEM_TRY(read_scalar(ctx, ls->flag, &f));
+  if (f & 1)
+    return fail(AFEM_ERR_BAD_ARG, "afem_ls_set_csr_view: a row start is negative, decreasing or past nb_column, or "
+                                  "a row's column count overruns its range");
+  if (f & 2) return fail(AFEM_ERR_BAD_ARG, "afem_ls_set_csr_view: a column index is below -1 or not a DoF");
+  if (f & 4)
+    return fail(AFEM_ERR_BAD_ARG, "afem_ls_set_csr_view: a slot past a row's column count holds a column (not -1)");
+  ls->row_ptr = ls->view_row_ptr;
+  ls->cols = columns_d;
+  ls->values = values_d;
+  ls->nnz = nb_column;
+  ls->padded = (f & 8) ? 1 : 0;
   return AFEM_OK;
 }
 
@@ -247,6 +317,7 @@ afem_status afem_ls_clear_values(afem_linear_system ls) {
   ls->cols = nullptr;
   ls->values = nullptr;
   ls->nnz = 0;
+  ls->padded = 0;
   ls->has_rc = 0;
   return AFEM_OK;
 }

@@ -29,8 +29,9 @@ import torch
 
 from . import _capi
 from ._capi import (AfemError, COLS_ASCENDING, COLS_SELF_LAST, ELIMINATE_ROW, ELIMINATE_ROW_COLUMN,  # noqa: F401
-                    LAYOUT_PER_BLOCK, LAYOUT_PER_ROW, PRECISION_FP64, PRECISION_MIXED, PRECOND_JACOBI,
-                    PRECOND_NONE, MeshView, SolveInfo, SolverOptions, call)
+                    FORMULATION_MINIMAL, FORMULATION_REFERENCE, FORMULATION_TESTLAB, LAYOUT_PER_BLOCK,
+                    LAYOUT_PER_ROW, PRECISION_FP64, PRECISION_MIXED, PRECOND_JACOBI, PRECOND_NONE, MeshView,
+                    SolveInfo, SolverOptions, call)
 
 
 def _ptr(t) -> C.c_void_p:
@@ -60,7 +61,20 @@ class Context:
         self.handle = h
 
     def synchronize(self) -> None:
+        """Wait for the stream; raises AFEM_ERR_MESH if an element kernel met a degenerate cell."""
         call("afem_context_synchronize", self.handle)
+
+    @property
+    def formulation(self) -> int:
+        """Element arithmetic of the assembly kernels: FORMULATION_REFERENCE (default, bit-identical
+        to the reference), FORMULATION_TESTLAB or FORMULATION_MINIMAL (fewest FP64 instructions)."""
+        v = C.c_int()
+        call("afem_context_get_element_formulation", self.handle, C.byref(v))
+        return int(v.value)
+
+    @formulation.setter
+    def formulation(self, f: int) -> None:
+        call("afem_context_set_element_formulation", self.handle, int(f))
 
     @property
     def launches(self) -> int:
@@ -340,6 +354,16 @@ class DoFLinearSystem:
     def set_csr_values(self, row_ptr: torch.Tensor, cols: torch.Tensor, values: torch.Tensor):
         self._keep = (row_ptr, cols, values)   # the view is non-owning: keep the tensors alive
         call("afem_ls_set_csr_values", self.handle, _ptr(row_ptr), _ptr(cols), _ptr(values), int(cols.numel()))
+
+    def set_csr_view(self, rows: torch.Tensor, columns: torch.Tensor, values: torch.Tensor,
+                     rows_nb_column: torch.Tensor | None = None):
+        """setCSRValues with the reference's CsrFormatMatrixView layout: `rows` holds
+        one start per row (no trailing entry, the last row ends at columns.numel()),
+        `columns` may hold -1 in unused slots; `rows_nb_column` (optional) the slot
+        count of each row.  Non-owning, like set_csr_values."""
+        self._keep = (rows, columns, values, rows_nb_column)   # non-owning view: keep the tensors alive
+        call("afem_ls_set_csr_view", self.handle, int(rows.numel()), _ptr(rows), _ptr(rows_nb_column),
+             int(columns.numel()), _ptr(columns), _ptr(values))
 
     def clear_values(self):
         call("afem_ls_clear_values", self.handle)

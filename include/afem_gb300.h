@@ -137,6 +137,38 @@ typedef struct {
   const int32_t* nc_inverse_d;   /* [nb_cell*(dim+1)] from afem_node_cell_build */
 } afem_mesh_view;
 
+/* Element arithmetic of the assembly kernels (per context; default
+ * AFEM_FORMULATION_REFERENCE).
+ *   REFERENCE: the reference's element functions in their own operation order,
+ *     every product and sum rounded separately as its CPU build evaluates them
+ *     (modules/poisson/ElementMatrix.h:54-63,107-118,
+ *     modules/poisson/ElementMatrixHexQuad.h:63-91,239-266,
+ *     modules/elasticity/ElementMatrix.h:216-301, with the geometry of
+ *     femutils/ArcaneFemFunctionsGpu.h:76-128,241-281,414-610).  Assembled
+ *     values are bit-identical to the reference's node-wise assembly.
+ *   TESTLAB: the testlab B-matrix form of the P1 Poisson element
+ *     (modules/testlab/FemModule.h:469-538, NodeWiseCsrBiliAssembly.cc:
+ *     194-211,269-290), bit-identical to testlab's nwcsr path; the other
+ *     element kinds use REFERENCE.
+ *   MINIMAL: the same matrices with the fewest FP64 instructions (edge-vector
+ *     cofactors, zero row sums, per-cell Jacobian moments): 2-3x faster on
+ *     GB300's narrow FP64 pipe and about 25x closer to exact arithmetic than
+ *     the reference's own formula, so NOT bit-identical to it (within
+ *     1e-11 of an entry near 1e-3 of its row maximum on 128^3 meshes).
+ * No reference counterpart (the reference has one formulation per path). */
+enum { AFEM_FORMULATION_REFERENCE = 0, AFEM_FORMULATION_TESTLAB = 1, AFEM_FORMULATION_MINIMAL = 2 };
+afem_status afem_context_set_element_formulation(afem_context ctx, int formulation);
+afem_status afem_context_get_element_formulation(afem_context ctx, int* formulation_h);
+
+/* Degenerate cells.  Every element kernel checks its cell's measure (tet 6V,
+ * triangle 2A, Jacobian determinant at each Gauss point); a zero, subnormal or
+ * non-finite one sets a flag in the context, and the next synchronous call
+ * (afem_context_synchronize, afem_assemble_to_host, afem_assemble_host_io,
+ * afem_gather_to_host) returns AFEM_ERR_MESH and clears it.  The reference
+ * divides by the measure without a check (ArcaneFemFunctionsGpu.h:113-128,
+ * 414-535) and yields non-finite entries; the values here are the same, but
+ * the status says so. */
+
 /* Scalar Poisson P1 stiffness, -div(k grad u): values_d[nnz] (CSR) receives
  * sum_cells k_c vol grad N_i . grad N_j.  cell_coeff_d (nullable) holds k_c.
  * Replaces assembleBilinearAtomicFree with _computeElementVectorTria3Gpu /
@@ -314,6 +346,28 @@ afem_status afem_ls_destroy(afem_linear_system ls);
 /* setCSRValues (CsrDoFLinearSystemImpl.h:98-101). */
 afem_status afem_ls_set_csr_values(afem_linear_system ls, const int32_t* row_ptr_d, const int32_t* cols_d,
                                    double* values_d, int64_t nnz);
+/* setCSRValues(const CSRFormatView&) with the reference's view as it is
+ * (femutils/CsrFormatMatrixView.h:135-210, filled by
+ * femutils/CsrFormatMatrix.cc:35-95): rows_d[nb_row] holds each row's first
+ * slot, with NO trailing entry (the last row ends at nb_column, the view's
+ * nbColumn(), :181-187); rows_nb_column_d[nb_row] (nullable) holds each row's
+ * slot count (nbColumnForRow); columns_d[nb_column] may hold -1 in unused
+ * slots (CsrFormatMatrix.cc:49-50), which every kernel of the library skips:
+ * the transformations as the reference's (column_index > 0 / >= 0 tests,
+ * CsrDoFLinearSystemImpl.cc:111,217), the SpMVs and solves as absent
+ * entries.  Rows must start at non-decreasing offsets; slots past a row's
+ * count up to the next row's start must be -1.  No copy of the matrix is
+ * made: the library keeps a device array of the nb_row + 1 row offsets
+ * (checked when set; synchronous) and a non-owning view of columns and
+ * values, valid until afem_ls_solve.  nb_row must equal the system's DoF
+ * count (the compacted DoF family of CsrDoFLinearSystemImpl.cc:27-29).
+ * rows_nb_column_d = NULL takes each row's count as its range size, which is
+ * what CsrFormat::translateToLinearSystem stores.  The learned
+ * preconditioner and block_size = 3 need a view without unused slots
+ * (AFEM_ERR_NOT_IMPLEMENTED / AFEM_ERR_BAD_ARG otherwise). */
+afem_status afem_ls_set_csr_view(afem_linear_system ls, int32_t nb_row, const int32_t* rows_d,
+                                 const int32_t* rows_nb_column_d, int64_t nb_column, const int32_t* columns_d,
+                                 double* values_d);
 /* hasSetCSRValues / getCSRValues. */
 afem_status afem_ls_get_csr_values(afem_linear_system ls, const int32_t** row_ptr_d, const int32_t** cols_d,
                                    double** values_d, int64_t* nnz);

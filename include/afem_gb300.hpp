@@ -9,9 +9,9 @@
 //
 // Errors are thrown as afem::Error (the counterpart of ARCANE_FATAL /
 // ARCANE_THROW); device memory is allocated with cudaMallocAsync on the
-// context's stream and released by the destructors.  An Arcane service
-// (GB300LinearSystem) wraps CsrDoFLinearSystem; the glue is shown in
-// INTEGRATION.md.
+// context's stream and released by the destructors.  The Arcane service
+// (GB300LinearSystem) that plugs the library behind IDoFLinearSystemImpl is
+// arcanefem_gb300/arcane/GB300DoFLinearSystem.{h,cc}.
 #pragma once
 
 #include <cuda_runtime.h>

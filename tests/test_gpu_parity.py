@@ -2,9 +2,13 @@
 
 Tolerances:
   * structure (node->cell adjacency, row pointers, columns): bit-exact;
-  * matrix values: |a - b| <= 1e-12 * max(|b|, 1e-3 * max|row of b|) per
-    entry (the element math is regrouped for FP64 throughput, so the last
-    bits may differ; the guard covers entries that cancel to ~0);
+  * matrix values in the default (reference-rounding) and testlab
+    formulations: bit-exact (np.array_equal) against the oracle, which
+    restates the reference's operation order;
+  * matrix values in the minimal-instruction formulation: |a - b| <= 1e-12 *
+    max(|b|, 1e-3 * max|row of b|) per entry on these small meshes (its
+    element math is regrouped for FP64 throughput, so the last bits differ;
+    the guard covers entries that cancel to ~0);
   * Dirichlet transformations on equal inputs: bit-exact;
   * solutions: true FP64 relative residual below the requested tolerance and
     the reference check files within their own tolerance.
@@ -16,22 +20,9 @@ import torch
 import golden_cases as G
 from arcanefem_gb300 import fem, meshgen
 from oracle import oracle as O
+from parity_helpers import REL, assert_bit_exact, rel_err_rows
 
 pytestmark = pytest.mark.gpu
-
-REL = 1e-12
-
-
-def rel_err_rows(got, ref, rp, b=1):
-    """Max over entries of |got - ref| / max(|ref|, 1e-3 * max|row|); an
-    all-zero row (a node in no cell) is compared absolutely."""
-    ref = np.asarray(ref)
-    got = np.asarray(got)
-    row_of = np.repeat(np.arange(rp.size - 1), np.diff(rp) * b * b)
-    rowmax = np.zeros(rp.size - 1)
-    np.maximum.at(rowmax, row_of, np.abs(ref))
-    denom = np.maximum(np.abs(ref), 1e-3 * rowmax[row_of])
-    return float(np.max(np.abs(got - ref) / np.where(denom > 0, denom, 1.0)))
 
 
 def build_format(ctx, mesh, nb_dof=1, use_csr=True, col_order=fem.COLS_ASCENDING):
@@ -82,47 +73,75 @@ def test_sparsity_bit_exact(cuda_ctx, name, self_last):
     assert np.array_equal(got_cols, expected)
 
 
+@pytest.fixture
+def formulation_ctx(cuda_ctx):
+    """The shared context; the formulation a test sets is put back afterwards."""
+    yield cuda_ctx
+    cuda_ctx.formulation = fem.FORMULATION_REFERENCE
+
+
 @pytest.mark.parametrize("name", list(MESHES))
 @pytest.mark.parametrize("self_last", [False, True])
-def test_poisson_values_match_oracle(cuda_ctx, name, self_last):
+def test_poisson_values_match_oracle(formulation_ctx, name, self_last):
+    ctx = formulation_ctx
     m = MESHES[name]()
-    f = build_format(cuda_ctx, m, col_order=fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING)
-    f.assemble_poisson()
+    f = build_format(ctx, m, col_order=fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING)
     ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
     rp, cols = O.sparsity(m.nb_node, m.cells, self_last=self_last)
     kind = O.POISSON_TRI3 if m.dim == 2 else O.POISSON_TET4
+    kind_t = O.TESTLAB_TRI3 if m.dim == 2 else O.TESTLAB_TET4
     ref = O.assemble(kind, m.coords, m.cells, ptr, nc, rp, cols)
+    ref_t = O.assemble(kind_t, m.coords, m.cells, ptr, nc, rp, cols)
+    # default: the module formulation in the reference's rounding, bit for bit
+    assert ctx.formulation == fem.FORMULATION_REFERENCE
+    f.assemble_poisson()
+    assert_bit_exact(f.values.cpu().numpy(), ref, "reference formulation")
+    # testlab B-matrix formulation (signed measure), bit for bit
+    ctx.formulation = fem.FORMULATION_TESTLAB
+    f.assemble_poisson()
+    assert_bit_exact(f.values.cpu().numpy(), ref_t, "testlab formulation")
+    # minimal-instruction formulation: within the guard of both
+    ctx.formulation = fem.FORMULATION_MINIMAL
+    f.assemble_poisson()
     got = f.values.cpu().numpy()
     assert rel_err_rows(got, ref, rp) < REL
-    # the testlab formulation (B matrix, signed measure) agrees too
-    kind_t = O.TESTLAB_TRI3 if m.dim == 2 else O.TESTLAB_TET4
-    ref_t = O.assemble(kind_t, m.coords, m.cells, ptr, nc, rp, cols)
     assert rel_err_rows(got, ref_t, rp) < REL
 
 
-def test_poisson_variable_coefficient(cuda_ctx):
-    m = meshgen.unit_square_tri(20, seed=9)
+@pytest.mark.parametrize("formulation", [fem.FORMULATION_REFERENCE, fem.FORMULATION_MINIMAL])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_poisson_variable_coefficient(formulation_ctx, formulation, dim):
+    m = meshgen.unit_square_tri(20, seed=9) if dim == 2 else meshgen.unit_cube_tet(6, seed=9)
     k = np.exp(np.random.default_rng(0).standard_normal(m.nb_cell))
-    f = build_format(cuda_ctx, m)
+    formulation_ctx.formulation = formulation
+    f = build_format(formulation_ctx, m)
     f.assemble_poisson(torch.as_tensor(k, device="cuda"))
     ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
     rp, cols = O.sparsity(m.nb_node, m.cells)
-    ref = O.assemble(O.POISSON_TRI3, m.coords, m.cells, ptr, nc, rp, cols, cell_coeff=k)
-    assert rel_err_rows(f.values.cpu().numpy(), ref, rp) < REL
+    ref = O.assemble(O.POISSON_TRI3 if dim == 2 else O.POISSON_TET4, m.coords, m.cells, ptr, nc, rp, cols,
+                     cell_coeff=k)
+    if formulation == fem.FORMULATION_REFERENCE:
+        assert_bit_exact(f.values.cpu().numpy(), ref, "coefficient")
+    else:
+        assert rel_err_rows(f.values.cpu().numpy(), ref, rp) < REL
 
 
+@pytest.mark.parametrize("formulation", [fem.FORMULATION_REFERENCE, fem.FORMULATION_MINIMAL])
 @pytest.mark.parametrize("use_csr", [True, False])
-def test_elasticity_values_match_oracle(cuda_ctx, use_csr):
+def test_elasticity_values_match_oracle(formulation_ctx, use_csr, formulation):
     m = meshgen.unit_cube_tet(5, seed=6)
     lam, mu = fem.lame(21e5, 0.28)
-    f = build_format(cuda_ctx, m, nb_dof=3, use_csr=use_csr)
+    formulation_ctx.formulation = formulation
+    f = build_format(formulation_ctx, m, nb_dof=3, use_csr=use_csr)
     f.assemble_elasticity(lam, mu)
     ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
     rp, cols = O.sparsity(m.nb_node, m.cells)
     ref = O.assemble(O.ELASTICITY_TET4, m.coords, m.cells, ptr, nc, rp, cols, per_block_layout=not use_csr,
                      lam=lam, mu=mu)
     got = f.values.cpu().numpy()
-    if use_csr:
+    if formulation == fem.FORMULATION_REFERENCE:
+        assert_bit_exact(got, ref, "elasticity")
+    elif use_csr:
         srp, _ = G.scalar_csr_from_block(rp, cols, 3)
         assert rel_err_rows(got, ref, srp) < REL
     else:
@@ -156,7 +175,7 @@ def test_rhs_constant_source(cuda_ctx, dim):
     f.rhs_constant_source(-5.5, rhs)
     ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
     ref = O.rhs_constant_source(dim, m.coords, m.cells, ptr, nc, -5.5)
-    np.testing.assert_allclose(rhs.cpu().numpy(), ref, rtol=1e-13, atol=0)
+    assert_bit_exact(rhs.cpu().numpy(), ref, "constant source")
 
 
 def test_rhs_body_force(cuda_ctx):
@@ -165,7 +184,7 @@ def test_rhs_body_force(cuda_ctx):
     rhs = torch.zeros(3 * m.nb_node, dtype=torch.float64, device="cuda")
     f.rhs_body_force([0.0, 0.5, -1.0], rhs)
     ref = O.rhs_body_force_tet4(m.coords, m.cells, [0.0, 0.5, -1.0])
-    np.testing.assert_allclose(rhs.cpu().numpy(), ref, rtol=1e-13, atol=1e-300)
+    assert_bit_exact(rhs.cpu().numpy(), ref, "body force")
 
 
 def test_dirichlet_transformations_bit_exact(cuda_ctx):
@@ -391,8 +410,9 @@ Q1_MESHES = {
 @pytest.mark.parametrize("name", list(Q1_MESHES))
 def test_q1_structure_and_values_match_oracle(cuda_ctx, name):
     """Quad4 / Hexa8 (bilinear / trilinear Lagrange, 2x2(x2) Gauss points):
-    node -> cell incidence and sparsity bit-exact, values within 1e-12 per
-    entry of the oracle's node-wise assembly of the reference element vectors."""
+    node -> cell incidence and sparsity bit-exact; values bit-exact in the
+    reference formulation, within 1e-12 per entry in the minimal one, against
+    the oracle's node-wise assembly of the reference element vectors."""
     m = Q1_MESHES[name]()
     f = build_format(cuda_ctx, m)
     ptr, nc, loc = O.node_cell(m.nb_node, m.cells)
@@ -404,6 +424,12 @@ def test_q1_structure_and_values_match_oracle(cuda_ctx, name):
     f.assemble_poisson(k)
     kind = O.POISSON_QUAD4 if m.dim == 2 else O.POISSON_HEXA8
     ref = O.assemble(kind, m.coords, m.cells, ptr, nc, rp, cols, cell_coeff=k.cpu().numpy())
+    assert_bit_exact(f.values.cpu().numpy(), ref, "Q1 reference formulation")
+    cuda_ctx.formulation = fem.FORMULATION_MINIMAL
+    try:
+        f.assemble_poisson(k)
+    finally:
+        cuda_ctx.formulation = fem.FORMULATION_REFERENCE
     assert rel_err_rows(f.values.cpu().numpy(), ref, rp) < REL
 
 
@@ -415,7 +441,7 @@ def test_q1_constant_source(cuda_ctx, dim):
     f.rhs_constant_source(-5.5, rhs)
     ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
     ref = O.rhs_constant_source_q1(dim, m.coords, m.cells, ptr, nc, -5.5)
-    np.testing.assert_allclose(rhs.cpu().numpy(), ref, rtol=1e-13, atol=0)
+    assert_bit_exact(rhs.cpu().numpy(), ref, "Q1 constant source")
 
 
 def test_q1_poisson_solve(cuda_ctx):
@@ -579,7 +605,7 @@ def fan_mesh(k, isolated=0):
 def test_fan_rows_and_isolated_nodes_match_oracle(cuda_ctx, k, isolated):
     """Rows longer than the gather's shared-memory accumulators (the direct
     path: 41 and 101 entries) and nodes in no cell (a diagonal-only row, as
-    the reference's deg + 1 rows): structure bit-exact, values 1e-12."""
+    the reference's deg + 1 rows): structure and values bit-exact."""
     coords, cells = fan_mesh(k, isolated)
     n = coords.shape[0]
     f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
@@ -590,7 +616,50 @@ def test_fan_rows_and_isolated_nodes_match_oracle(cuda_ctx, k, isolated):
     f.assemble_poisson()
     ptr, nc, _ = O.node_cell(n, cells)
     ref = O.assemble(O.POISSON_TRI3, coords, cells, ptr, nc, rp, cols)
-    assert rel_err_rows(f.values.cpu().numpy(), ref, rp) < REL
+    assert_bit_exact(f.values.cpu().numpy(), ref, "fan rows")
+
+
+@pytest.mark.parametrize("formulation", [fem.FORMULATION_REFERENCE, fem.FORMULATION_TESTLAB,
+                                         fem.FORMULATION_MINIMAL])
+@pytest.mark.parametrize("kind", ["tet", "tri", "hex", "elasticity"])
+def test_degenerate_cell_is_reported(formulation_ctx, formulation, kind):
+    """A cell of zero measure (a flattened tetrahedron / triangle / hexahedron)
+    makes its element matrix non-finite; the element kernel flags it and the
+    next synchronous call returns AFEM_ERR_MESH, after which the context is
+    usable again.  The flag is raised on the host side of the API, not by a
+    device fault."""
+    ctx = formulation_ctx
+    ctx.formulation = formulation
+    if kind in ("tet", "elasticity"):
+        m = meshgen.unit_cube_tet(3, seed=1)
+    elif kind == "tri":
+        m = meshgen.unit_square_tri(4, seed=1)
+    else:
+        m = meshgen.unit_cube_hex(3, seed=1)
+    bad = m.coords.copy()
+    # move every node of cell 0 onto the plane z = 0 (3D) or the line y = y_0 (2D):
+    # its measure is then exactly zero in every formulation
+    cn = m.cells[0]
+    if m.dim == 3:
+        bad[cn, 2] = 0.0
+    else:
+        bad[cn, 1] = bad[cn[0], 1]
+    f = build_format(ctx, meshgen.Mesh(m.dim, bad, m.cells), nb_dof=3 if kind == "elasticity" else 1)
+    if kind == "elasticity":
+        f.assemble_elasticity(*fem.lame(21e5, 0.28))
+    else:
+        f.assemble_poisson()
+    with pytest.raises(fem.AfemError) as e:
+        ctx.synchronize()
+    assert e.value.status == 7 and "degenerate cell" in str(e.value)
+    ctx.synchronize()   # the flag was cleared
+    g = build_format(ctx, m, nb_dof=3 if kind == "elasticity" else 1)
+    if kind == "elasticity":
+        g.assemble_elasticity(*fem.lame(21e5, 0.28))
+    else:
+        g.assemble_poisson()
+    ctx.synchronize()
+    assert torch.isfinite(g.values).all()
 
 
 def test_row_above_the_candidate_capacity_is_reported(cuda_ctx):
