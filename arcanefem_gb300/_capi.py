@@ -105,6 +105,7 @@ SIGNATURES = {
     "afem_cg_solve_csr": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, C.POINTER(SolverOptions),
                                     C.POINTER(SolveInfo)]),
     "afem_ls_solve": (C.c_int, [_P, C.POINTER(SolverOptions), C.POINTER(SolveInfo)]),
+    "afem_ls_set_learned_preconditioner": (C.c_int, [_P, _P]),
     "afem_spmv_csr": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P]),
     "afem_mpnn_create": (C.c_int, None),
     "afem_mpnn_destroy": (C.c_int, [_P]),

@@ -101,6 +101,7 @@ class Batch:
         h = C.c_void_p()
         call("afem_batch_create", ctx.handle, len(sizes), descs, C.byref(h))
         self.handle = h
+        ctx.adopt(self)
         self.nb_node = sum(m.nb_node for m in self.meshes)
         self.nnz = sum(f.nnzb for f in self.fmts)
 
@@ -122,21 +123,31 @@ class Batch:
         arr = None if weights is None else (C.c_double * len(self.sizes))(*[float(w) for w in weights])
         call("afem_batch_set_weights", self.handle, arr)
 
-    def rebalance(self, options=None, rounds: int = 3):
-        """Feedback partitioning: weight each instance by its measured work
-        (finish time x CTAs) and resize the teams; keep the fastest split."""
+    def rebalance(self, options=None, rounds: int = 6, damping: float = 0.5):
+        """Feedback partitioning.  Each round estimates every instance's work as
+        its measured finish time x its CTAs and moves the weights part of the way
+        towards it, w <- w * (work / w)^damping (a full step overshoots: a team's
+        speed does not grow in proportion to its CTAs, its barriers cost more);
+        all rounds run and the fastest split is kept.  Returns the best launch
+        time, its weights (None: the cost model was best) and the finish-time
+        spread (min, median, max ms) before and after."""
         opt = options or fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000)
+        self.set_weights(None)
         res, best_ms = self.solve(opt)
+        spread = lambda rr: [float(np.min([r.finish_ms for r in rr])), float(np.median([r.finish_ms for r in rr])),
+                             float(np.max([r.finish_ms for r in rr]))]
+        before = after = spread(res)
         best_w = None
+        w = None
         for _ in range(rounds):
-            w = [max(float(res[i].finish_ms), 1e-3) * self.team(i)[1] for i in range(len(self.sizes))]
+            work = [max(float(res[i].finish_ms), 1e-3) * self.team(i)[1] for i in range(len(self.sizes))]
+            w = work if w is None else [wi * (ki / wi) ** damping for wi, ki in zip(w, work)]
             self.set_weights(w)
-            res2, ms = self.solve(opt)
+            res, ms = self.solve(opt)
             if ms < best_ms:
-                best_ms, best_w, res = ms, w, res2
-            else:
-                break
+                best_ms, best_w, after = ms, list(w), spread(res)
         self.set_weights(best_w)
+        self.last_spread = {"before_ms": before, "after_ms": after}
         return best_ms, best_w
 
     def team(self, inst: int):
@@ -148,7 +159,11 @@ class Batch:
         res = (BatchResult * len(self.sizes))()
         ms = C.c_float()
         opt = options or fem.solver_options(rtol=1e-8, inner_rtol=0.1, max_iter=20000)
-        call("afem_batch_solve", self.handle, C.byref(opt), res, C.byref(ms))
+        try:
+            call("afem_batch_solve", self.handle, C.byref(opt), res, C.byref(ms))
+        except _capi.AfemError as e:   # per-instance statuses and residuals ride on the error
+            e.results = list(res)
+            raise
         return list(res), float(ms.value)
 
     def autotune(self, candidates=None, options=None, reps: int = 2, cache: str | None = None, log=None,
@@ -182,6 +197,7 @@ class Batch:
             ms, w = self.rebalance(opt)
             chosen["weights"] = w
             chosen["rebalanced_ms"] = ms
+            chosen["team_finish_spread"] = self.last_spread
         table[key] = chosen
         os.makedirs(os.path.dirname(cache) or ".", exist_ok=True)
         tmp = cache + ".tmp"

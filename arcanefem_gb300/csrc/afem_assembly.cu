@@ -143,6 +143,18 @@ __global__ void __launch_bounds__(256) k_elem_poisson_tri(int cell0, int nb_cell
 // so every row is formed: 4 x 23 + ~130 FP64 instructions per tetrahedron
 // (divisions included) against 72 for the minimal form.  A cell coefficient
 // multiplies each entry as the node-wise loop does (coeff * v).
+// Which stages of the reference-rounding tetrahedron run their products and
+// sums on the integer pipe (afem_fp64_int.cuh) instead of the FP64 pipe, so
+// that both pipes work at once: bit 0 the element rows, bit 1 the gradient
+// numerators, bit 2 the coordinate differences.  The values are the same bit
+// for bit whatever the choice; it is a throughput tuning constant.
+#ifndef AFEM_REF_INT_STAGES
+#define AFEM_REF_INT_STAGES 0
+#endif
+constexpr bool kIntRows = (AFEM_REF_INT_STAGES & 1) != 0;
+constexpr bool kIntNumerators = (AFEM_REF_INT_STAGES & 2) != 0;
+constexpr bool kIntDifferences = (AFEM_REF_INT_STAGES & 4) != 0;
+
 template <int NPC, int F>
 __global__ void __launch_bounds__(128) k_elem_poisson_p1_ref(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                              const int32_t* __restrict__ cn,
@@ -182,9 +194,9 @@ __global__ void __launch_bounds__(128) k_elem_poisson_p1_ref(int cell0, int nb_c
         for (int k = 0; k < i; ++k) K[i][k] = K[k][i];
     } else if constexpr (NPC == 4) {
       double g[3][4], vol;
-      meas = ref::tet_gradients(n, g, &vol);
+      meas = ref::tet_gradients<kIntDifferences, kIntNumerators>(n, g, &vol);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) ref::tet_row(g, vol, i, K[i]);
+      for (int i = 0; i < 4; ++i) ref::tet_row<kIntRows>(g, vol, i, K[i]);
     } else {
       double dx[3], dy[3], area;
       meas = ref::tri_gradients(n, dx, dy, &area);
@@ -255,15 +267,32 @@ __device__ __forceinline__ int elast_packed(int i, int m, int a, int b) {
 //   a != b: (lambda P_ab) vol + (mu P_ba) vol
 // with each product rounded as the reference rounds it.  The products commute,
 // so K is symmetric bit for bit.
+// INT: 0 all on the FP64 pipe, 1 all on the integer pipe, 2 the mu (shear)
+// terms and the final sum on the integer pipe, the rest on the FP64 pipe.
+template <int INT>
 __device__ __forceinline__ double elast_ref_entry(int a, int b, const double P[3][3], double l2m, double lambda,
                                                   double mu, double vol) {
-  using namespace ref;
+  auto add1 = [](double x, double y) { return ref::xadd<INT == 1>(x, y); };
+  auto mul1 = [](double x, double y) { return ref::xmul<INT == 1>(x, y); };
+  auto add2 = [](double x, double y) { return ref::xadd<INT != 0>(x, y); };
+  auto mul2 = [](double x, double y) { return ref::xmul<INT != 0>(x, y); };
   if (a == b) {
-    const double z = a == 0 ? add(P[1][1], P[2][2]) : (a == 1 ? add(P[0][0], P[2][2]) : add(P[1][1], P[0][0]));
-    return add(mul(mul(l2m, P[a][a]), vol), mul(mul(mu, z), vol));
+    const double z = a == 0 ? add2(P[1][1], P[2][2]) : (a == 1 ? add2(P[0][0], P[2][2]) : add2(P[1][1], P[0][0]));
+    return add2(mul1(mul1(l2m, P[a][a]), vol), mul2(mul2(mu, z), vol));
   }
-  return add(mul(mul(lambda, P[a][b]), vol), mul(mul(mu, P[b][a]), vol));
+  return add2(mul1(mul1(lambda, P[a][b]), vol), mul2(mul2(mu, P[b][a]), vol));
 }
+
+// Integer-pipe stages of the reference-rounding elasticity element (as
+// AFEM_REF_INT_STAGES for the Poisson tetrahedron): bit 0 the block entries,
+// bit 1 the gradient products P, bit 2 the gradient numerators, bit 3 only
+// the shear terms of the block entries (when bit 0 is clear).
+#ifndef AFEM_ELAST_INT_STAGES
+#define AFEM_ELAST_INT_STAGES 0
+#endif
+constexpr int kElastIntEntries = (AFEM_ELAST_INT_STAGES & 1) ? 1 : ((AFEM_ELAST_INT_STAGES & 8) ? 2 : 0);
+constexpr bool kElastIntProducts = (AFEM_ELAST_INT_STAGES & 2) != 0;
+constexpr bool kElastIntNumerators = (AFEM_ELAST_INT_STAGES & 4) != 0;
 
 template <int F>
 __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cell0, int nb_cell, const double* __restrict__ xyz,
@@ -307,7 +336,7 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
         n[a][2] = __ldg(p + 2);
       }
       double g[3][4], vol;
-      const double v6 = ref::tet_gradients(n, g, &vol);
+      const double v6 = ref::tet_gradients<false, kElastIntNumerators>(n, g, &vol);
       if (bad && !ref::measure_ok(v6)) atomicOr(bad, kFlagDegenerateCell);
       stage_p[threadIdx.x] = __ldg(reinterpret_cast<const int4*>(inv) + c);
       const double l2m = ref::add(lambda, 2.0 * mu);
@@ -320,11 +349,12 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
 #pragma unroll
           for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) P[a][b] = ref::mul(g[a][lo], g[b][hi]);
+            for (int b = 0; b < 3; ++b) P[a][b] = ref::xmul<kElastIntProducts>(g[a][lo], g[b][hi]);
 #pragma unroll
           for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) my[pair * 9 + a * 3 + b] = elast_ref_entry(a, b, P, l2m, lambda, mu, vol);
+            for (int b = 0; b < 3; ++b)
+              my[pair * 9 + a * 3 + b] = elast_ref_entry<kElastIntEntries>(a, b, P, l2m, lambda, mu, vol);
         }
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -332,12 +362,13 @@ __global__ void __launch_bounds__(kElastElemBlock) k_elem_elasticity_tet(int cel
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
-          for (int b = a; b < 3; ++b) P[a][b] = P[b][a] = ref::mul(g[a][i], g[b][i]);
+          for (int b = a; b < 3; ++b) P[a][b] = P[b][a] = ref::xmul<kElastIntProducts>(g[a][i], g[b][i]);
         int k = 0;
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
-          for (int b = a; b < 3; ++b, ++k) my[54 + i * 6 + k] = elast_ref_entry(a, b, P, l2m, lambda, mu, vol);
+          for (int b = a; b < 3; ++b, ++k)
+            my[54 + i * 6 + k] = elast_ref_entry<kElastIntEntries>(a, b, P, l2m, lambda, mu, vol);
       }
     } else if (c < nb_cell) {
       // cofactors c_1..c_3 of the edges from node 0 and s = 1 / (6 |det|);
@@ -746,6 +777,14 @@ __constant__ double kHexDN[8][3][8] = {
     {{-kHpm, kHpm, kHpp, -kHpp, -kHmm, kHmm, kHpm, -kHpm}, {-kHpm, -kHpp, kHpp, kHpm, -kHmm, -kHpm, kHpm, kHmm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}},
     {{-kHmm, kHmm, kHpm, -kHpm, -kHpm, kHpm, kHpp, -kHpp}, {-kHmm, -kHpm, kHpm, kHmm, -kHpm, -kHpp, kHpp, kHpm}, {-kHmm, -kHpm, -kHpp, -kHpm, kHmm, kHpm, kHpp, kHpm}}};
 
+// Integer-pipe stages of the reference-rounding Hexa8 element: bit 0 the
+// matrix accumulation, bit 1 the Jacobians.
+#ifndef AFEM_HEX_INT_STAGES
+#define AFEM_HEX_INT_STAGES 0
+#endif
+constexpr bool kHexIntRows = (AFEM_HEX_INT_STAGES & 1) != 0;
+constexpr bool kHexIntJacobian = (AFEM_HEX_INT_STAGES & 2) != 0;
+
 template <int F>
 __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_cell, const double* __restrict__ xyz,
                                                             const int32_t* __restrict__ cn,
@@ -764,7 +803,7 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_ce
     }
     double K[8][8];
     if constexpr (F != AFEM_FORMULATION_MINIMAL) {
-      const bool ok = ref::hexa8_matrix(x, y, z, kHexDnRef, K);
+      const bool ok = ref::hexa8_matrix<kHexIntJacobian, kHexIntRows>(x, y, z, kHexDnRef, K);
       if (bad && !ok) atomicOr(bad, kFlagDegenerateCell);
       if (coeff) scale_upper<8>(K, __ldg(coeff + c));
       write_rows_q1<8>(K, inv + 8 * c, er);

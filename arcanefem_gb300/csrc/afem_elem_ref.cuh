@@ -29,12 +29,40 @@
 
 #include <cstdint>
 
+#include "afem_fp64_int.cuh"
+
 namespace afem {
 namespace ref {
 
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+
+// The same operations, bit for bit, on the integer pipe (afem_fp64_int.cuh),
+// with the FP64 unit for the operands and results the integer path leaves out.
+__device__ __forceinline__ double iadd(double a, double b) {
+  uint64_t r;
+  if (i64fp::add(__double_as_longlong(a), __double_as_longlong(b), &r)) return __longlong_as_double(r);
+  return __dadd_rn(a, b);
+}
+__device__ __forceinline__ double isub(double a, double b) { return iadd(a, -b); }
+__device__ __forceinline__ double imul(double a, double b) {
+  uint64_t r;
+  if (i64fp::mul(__double_as_longlong(a), __double_as_longlong(b), &r)) return __longlong_as_double(r);
+  return __dmul_rn(a, b);
+}
+
+// Add / multiply on the FP64 pipe (INT = false) or the integer pipe (INT = true).
+template <bool INT>
+__device__ __forceinline__ double xadd(double a, double b) {
+  if constexpr (INT) return iadd(a, b);
+  else return __dadd_rn(a, b);
+}
+template <bool INT>
+__device__ __forceinline__ double xmul(double a, double b) {
+  if constexpr (INT) return imul(a, b);
+  else return __dmul_rn(a, b);
+}
 
 // Biased binary exponent of x (0 for zero and subnormals, 2047 for inf / NaN).
 __device__ __forceinline__ int bexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
@@ -108,26 +136,31 @@ __device__ __forceinline__ double tet_v6(const double v0[3], const double v1[3],
 // (computeGradient{X,Y,Z}Tetra4).  e[] holds the six differences
 // e10 e20 e30 e21 e31 e32 (e_ij = n_i.b - n_j.b); the reverse ones are their
 // negatives exactly.
+template <bool INT = false>
 __device__ __forceinline__ void tet_grad_numerators(const double na[4], const double e[6], double g[4]) {
   const double e10 = e[0], e20 = e[1], e30 = e[2], e21 = e[3], e31 = e[4], e32 = e[5];
-  g[0] = add(add(mul(na[1], e32), mul(na[2], -e31)), mul(na[3], e21));
-  g[1] = add(add(mul(na[0], -e32), mul(na[2], e30)), mul(na[3], -e20));
-  g[2] = add(add(mul(na[0], e31), mul(na[1], -e30)), mul(na[3], e10));
-  g[3] = add(add(mul(na[0], -e21), mul(na[1], e20)), mul(na[2], -e10));
+  auto A = [](double x, double y) { return xadd<INT>(x, y); };
+  auto M = [](double x, double y) { return xmul<INT>(x, y); };
+  g[0] = A(A(M(na[1], e32), M(na[2], -e31)), M(na[3], e21));
+  g[1] = A(A(M(na[0], -e32), M(na[2], e30)), M(na[3], -e20));
+  g[2] = A(A(M(na[0], e31), M(na[1], -e30)), M(na[3], e10));
+  g[3] = A(A(M(na[0], -e21), M(na[1], e20)), M(na[2], -e10));
 }
 
 // The reference's P1 tetrahedron geometry: gradients g[d][i] = dN_i/dx_d and
 // the volume V6 / 6.  Returns V6 (zero or non-finite for a degenerate cell).
+template <bool INT_DIFF = false, bool INT_NUM = false>
 __device__ __forceinline__ double tet_gradients(const double n[4][3], double g[3][4], double* vol) {
   double e[3][6];
+  auto D = [](double x, double y) { return xadd<INT_DIFF>(x, -y); };
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    e[k][0] = sub(n[1][k], n[0][k]);
-    e[k][1] = sub(n[2][k], n[0][k]);
-    e[k][2] = sub(n[3][k], n[0][k]);
-    e[k][3] = sub(n[2][k], n[1][k]);
-    e[k][4] = sub(n[3][k], n[1][k]);
-    e[k][5] = sub(n[3][k], n[2][k]);
+    e[k][0] = D(n[1][k], n[0][k]);
+    e[k][1] = D(n[2][k], n[0][k]);
+    e[k][2] = D(n[3][k], n[0][k]);
+    e[k][3] = D(n[2][k], n[1][k]);
+    e[k][4] = D(n[3][k], n[1][k]);
+    e[k][5] = D(n[3][k], n[2][k]);
   }
   const double v0[3] = {e[0][0], e[1][0], e[2][0]};
   const double v1[3] = {e[0][1], e[1][1], e[2][1]};
@@ -142,7 +175,7 @@ __device__ __forceinline__ double tet_gradients(const double n[4][3], double g[3
     const int a = (d + 1) % 3, b = (d + 2) % 3;
     const double na[4] = {n[0][a], n[1][a], n[2][a], n[3][a]};
     double num[4];
-    tet_grad_numerators(na, e[b], num);
+    tet_grad_numerators<INT_NUM>(na, e[b], num);
 #pragma unroll
     for (int i = 0; i < 4; ++i) g[d][i] = div(num[i], v6, rv6, ok);
   }
@@ -164,10 +197,13 @@ __device__ __forceinline__ double tet_volume(const double n[4][3]) {
 // Row i of the Poisson P1 tetrahedron (_computeElementVectorTetra4Gpu,
 // modules/poisson/ElementMatrix.h:107-118):
 //   out_k = (vol dx_i) dx_k + (vol dy_i) dy_k + (vol dz_i) dz_k.
+template <bool INT = false>
 __device__ __forceinline__ void tet_row(const double g[3][4], double vol, int i, double out[4]) {
-  const double sx = mul(vol, g[0][i]), sy = mul(vol, g[1][i]), sz = mul(vol, g[2][i]);
+  auto A = [](double x, double y) { return xadd<INT>(x, y); };
+  auto M = [](double x, double y) { return xmul<INT>(x, y); };
+  const double sx = M(vol, g[0][i]), sy = M(vol, g[1][i]), sz = M(vol, g[2][i]);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) out[k] = add(add(mul(sx, g[0][k]), mul(sy, g[1][k])), mul(sz, g[2][k]));
+  for (int k = 0; k < 4; ++k) out[k] = A(A(M(sx, g[0][k]), M(sy, g[1][k])), M(sz, g[2][k]));
 }
 
 // Triangle: area |(n1 - n0) x (n2 - n0)| / 2 (computeAreaTria3, the Real3
@@ -406,17 +442,20 @@ __device__ __forceinline__ bool quad4_matrix(const double x[4], const double y[4
 // coordinate from zero, in node order) and the determinant by the first row,
 // J00 (J11 J22 - J12 J21) - J01 (J10 J22 - J12 J20) + J02 (J10 J21 - J11 J20);
 // m[] returns those three minors.
+template <bool INT = false>
 __device__ __forceinline__ double hexa8_jacobian(const double x[8], const double y[8], const double z[8],
                                                  const HexDN& dn, int g, double J[3][3], double m[3]) {
+  auto A = [](double p, double q) { return xadd<INT>(p, q); };
+  auto M = [](double p, double q) { return xmul<INT>(p, q); };
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     const double* d = dn.v[g][r];
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-      s0 = add(s0, mul(d[a], x[a]));
-      s1 = add(s1, mul(d[a], y[a]));
-      s2 = add(s2, mul(d[a], z[a]));
+      s0 = A(s0, M(d[a], x[a]));
+      s1 = A(s1, M(d[a], y[a]));
+      s2 = A(s2, M(d[a], z[a]));
     }
     J[r][0] = s0;
     J[r][1] = s1;
@@ -435,8 +474,9 @@ __device__ __forceinline__ double hexa8_jacobian(const double x[8], const double
 // determinant already formed are its minors, negated where the reference
 // writes the difference the other way round.  Returns false if a Gauss point
 // has a degenerate Jacobian (measure_ok).
+template <bool INT_J = false, bool INT_ROWS = false>
 __device__ __forceinline__ bool hexa8_matrix(const double x[8], const double y[8], const double z[8], const HexDN& dn,
-                                               double K[8][8]) {
+                                             double K[8][8]) {
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -445,7 +485,7 @@ __device__ __forceinline__ bool hexa8_matrix(const double x[8], const double y[8
 #pragma unroll 1
   for (int g = 0; g < 8; ++g) {
     double J[3][3], mm[3];
-    const double det = hexa8_jacobian(x, y, z, dn, g, J, mm);
+    const double det = hexa8_jacobian<INT_J>(x, y, z, dn, g, J, mm);
     const double mA = mm[0], mB = mm[1], mC = mm[2];
     all_ok &= measure_ok(det);
     const double rd = __drcp_rn(det);
@@ -469,11 +509,12 @@ __device__ __forceinline__ bool hexa8_matrix(const double x[8], const double y[8
       dy[a] = add(add(mul(v10, dxi[a]), mul(v11, deta[a])), mul(v12, dzeta[a]));
       dz[a] = add(add(mul(v20, dxi[a]), mul(v21, deta[a])), mul(v22, dzeta[a]));
     }
+    auto A = [](double p, double q) { return xadd<INT_ROWS>(p, q); };
+    auto M = [](double p, double q) { return xmul<INT_ROWS>(p, q); };
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-      for (int k = i; k < 8; ++k)
-        K[i][k] = add(K[i][k], mul(add(add(mul(dx[i], dx[k]), mul(dy[i], dy[k])), mul(dz[i], dz[k])), det));
+      for (int k = i; k < 8; ++k) K[i][k] = A(K[i][k], M(A(A(M(dx[i], dx[k]), M(dy[i], dy[k])), M(dz[i], dz[k])), det));
   }
   return all_ok;
 }

@@ -131,6 +131,12 @@ afem_status read_scalar(afem_context ctx, const T* d, T* h) {
 afem_status spmv_fp64(afem_context ctx, int n, int64_t nnz, const int32_t* rp, const int32_t* cols,
                       const double* vals, const double* x, double* y);
 
+// afem_fcg_solve with a forced-row mask (nullable) for the stop test's norms
+// (afem_mpnn.cu); the linear system's learned-preconditioner solve.
+afem_status fcg_solve(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                      const double* b, double* x, const uint8_t* skip, afem_mpnn net,
+                      const afem_solver_options* opt, afem_solve_info* info);
+
 // Exclusive scan of int32 counts into int32 offsets out[0..n] (out[n] = total),
 // three-phase (tile sums, scan of sums, add-back), deterministic.
 // Needs scan_scratch_bytes(n) bytes of scratch.

@@ -28,6 +28,11 @@ struct afem_linear_system_s {
   // reference CSR view (afem_ls_set_csr_view); 1 if that view has unused slots
   int32_t* view_row_ptr = nullptr;
   int padded = 0;
+  // the learned preconditioner (precond = AFEM_PRECOND_LEARNED) and the
+  // version of the matrix values its operator was last set from
+  afem_mpnn learned = nullptr;
+  int64_t values_version = 1;
+  int64_t learned_version = 0;
   // row-column elimination bookkeeping
   int has_rc = 0;
   double* rc_saved = nullptr;
@@ -248,6 +253,7 @@ afem_status afem_ls_destroy(afem_linear_system ls) {
 afem_status afem_ls_set_csr_values(afem_linear_system ls, const int32_t* row_ptr_d, const int32_t* cols_d,
                                    double* values_d, int64_t nnz) {
   AFEM_CHECK_ARG(ls && row_ptr_d && cols_d && values_d && nnz > 0, "afem_ls_set_csr_values: bad arguments");
+  ++ls->values_version;
   ls->row_ptr = row_ptr_d;
   ls->cols = cols_d;
   ls->values = values_d;
@@ -277,6 +283,7 @@ afem_status afem_ls_set_csr_view(afem_linear_system ls, int32_t nb_row, const in
   if (f & 2) return fail(AFEM_ERR_BAD_ARG, "afem_ls_set_csr_view: a column index is below -1 or not a DoF");
   if (f & 4)
     return fail(AFEM_ERR_BAD_ARG, "afem_ls_set_csr_view: a slot past a row's column count holds a column (not -1)");
+  ++ls->values_version;
   ls->row_ptr = ls->view_row_ptr;
   ls->cols = columns_d;
   ls->values = values_d;
@@ -324,6 +331,7 @@ afem_status afem_ls_clear_values(afem_linear_system ls) {
 
 static afem_status entry(afem_linear_system ls, int32_t row, int32_t col, double value, int add, const char* who) {
   AFEM_TRY(need_view(ls, who));
+  ++ls->values_version;
   AFEM_CHECK_ARG(row >= 0 && row < ls->n && col >= 0 && col < ls->n, "%s: (%d, %d) out of range", who, row, col);
   afem_context ctx = ls->ctx;
   AFEM_CUDA(cudaMemsetAsync(ls->flag, 0, sizeof(int), ctx->stream));
@@ -391,6 +399,7 @@ afem_status afem_dirichlet_elimination(afem_linear_system ls, int type, int nb_s
 
 afem_status afem_ls_apply_matrix_transformation(afem_linear_system ls) {
   AFEM_TRY(need_view(ls, "afem_ls_apply_matrix_transformation"));
+  ++ls->values_version;
   afem_context ctx = ls->ctx;
   // _fillRowColumnEliminationInfos: is any DoF RowColumn-eliminated?
   AFEM_CUDA(cudaMemsetAsync(ls->flag, 0, sizeof(int), ctx->stream));
@@ -423,8 +432,29 @@ afem_status afem_ls_apply_rhs_transformation(afem_linear_system ls) {
                 (const double*)ls->elim_value, ls->rhs);
 }
 
+afem_status afem_ls_set_learned_preconditioner(afem_linear_system ls, afem_mpnn net) {
+  AFEM_CHECK_ARG(ls, "afem_ls_set_learned_preconditioner: null linear system");
+  ls->learned = net;
+  ls->learned_version = 0;
+  return AFEM_OK;
+}
+
 afem_status afem_ls_solve(afem_linear_system ls, const afem_solver_options* opt, afem_solve_info* info) {
   AFEM_TRY(need_view(ls, "afem_ls_solve"));
+  if (opt && opt->precond == AFEM_PRECOND_LEARNED) {
+    if (!ls->learned)
+      return fail(AFEM_ERR_BAD_ARG, "afem_ls_solve: precond = learned needs a network "
+                                    "(afem_ls_set_learned_preconditioner)");
+    if (ls->padded)
+      return fail(AFEM_ERR_NOT_IMPLEMENTED, "afem_ls_solve: the learned preconditioner needs a CSR view without "
+                                            "unused slots");
+    if (ls->learned_version != ls->values_version) {   // the matrix changed: new Galerkin values and weights
+      AFEM_TRY(afem_mpnn_set_operator(ls->learned, ls->n, ls->row_ptr, ls->cols, ls->values));
+      ls->learned_version = ls->values_version;
+    }
+    return fcg_solve(ls->ctx, ls->n, ls->row_ptr, ls->cols, ls->values, ls->rhs, ls->sol,
+                     opt->skip_forced_rows ? ls->forced_info : nullptr, ls->learned, opt, info);
+  }
   return solve_csr(ls->ctx, ls->n, ls->row_ptr, ls->cols, ls->values, ls->rhs, ls->sol, ls->forced_info, opt, info);
 }
 

@@ -9,12 +9,14 @@
 //   their order, so the output is deterministic.
 //
 // node -> node sparsity (rows of the assembled matrix):
-//   one warp per node stages the nodes of its incident cells in shared memory
-//   and extracts their distinct values in increasing order (one warp-wide
-//   minimum per distinct value): row length = 1 + number of neighbours
-//   (femutils/BSRFormat.cc:445-557, row = deg + 1).  The second pass writes
-//   the columns (ascending or self-last) and, for every cell-node incidence,
-//   its position in the row (the slot map used by the assembly kernels).
+//   one warp per node inserts the nodes of its incident cells into a hash
+//   table in shared memory; the number of distinct values is the row length
+//   = 1 + number of neighbours (femutils/BSRFormat.cc:445-557, row = deg + 1).
+//   The second pass sorts the distinct values and writes the columns
+//   (ascending or self-last) and, for every cell-node incidence, its position
+//   in the row (the slot map used by the assembly kernels).  Rows too long
+//   for the table path extract their distinct values in increasing order by
+//   warp-wide minima instead.
 #include <algorithm>
 #include <climits>
 
@@ -163,10 +165,111 @@ __device__ __forceinline__ int row_select(int n, int npc, int m, const int32_t* 
   return it;
 }
 
+// Fast path for rows of at most kHashRow candidates and 32 distinct columns
+// (every interior row of a tetrahedral, triangular or hexahedral mesh): each
+// candidate is inserted once into a per-warp open-addressing table in shared
+// memory (atomicCAS, linear probing), so the row length is the number of
+// first insertions -- one pass over the candidates instead of one sweep per
+// distinct value.  The column pass compacts the first insertions (ballot
+// prefix) into a list, sorts it (one value per lane, a 32-key bitonic network
+// on shuffles), records each value's position in the row in its table entry,
+// and every candidate reads its slot byte from there.  Rows with more
+// candidates, and column passes with more than 32 distinct values, take
+// row_select.  Returns the row length, or -1 when the row needs row_select.
+constexpr int kHashRow = 128;      // candidates per row on the fast path (R = 4)
+constexpr int kHashSlots = 256;    // table entries per warp (load factor <= 1/8 for 32 distinct values)
+
+__device__ __forceinline__ uint32_t hash_slot(int32_t v) { return ((uint32_t)v * 2654435761u) >> 24; }
+
+template <bool FILL>
+__device__ __forceinline__ int row_hash(int n, int npc, int m, const int32_t* __restrict__ cn,
+                                        const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ local,
+                                        int len, int self_last, int32_t* __restrict__ cols,
+                                        uint8_t* __restrict__ slot, int32_t* __restrict__ key,
+                                        uint8_t* __restrict__ rank, uint64_t* __restrict__ list) {
+  constexpr int R = kHashRow / 32;
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = lane; k < kHashSlots; k += 32) key[k] = -1;
+  __syncwarp();
+  int16_t si[R];
+  int16_t hs[R];
+  int distinct = 0;   // uniform across the warp
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int i = r * 32 + lane;
+    si[r] = 0;
+    hs[r] = 0;
+    bool fresh = false;
+    int32_t v = -1;
+    if (i < m) {
+      const int k = i / npc, j = i - k * npc;
+      v = __ldg(cn + (int64_t)__ldg(nc_cell + k) * npc + j);
+      if (FILL) {
+        const int li = __ldg(local + k);
+        si[r] = (int16_t)(k * npc + (j == li ? 0 : (j < li ? j + 1 : j)));
+      }
+      uint32_t h = hash_slot(v);
+      for (int probe = 0; probe < kHashSlots; ++probe, h = (h + 1) & (kHashSlots - 1)) {
+        const int32_t old = atomicCAS(key + h, -1, v);
+        if (old == -1) {
+          fresh = true;
+          break;
+        }
+        if (old == v) break;
+      }
+      hs[r] = (int16_t)h;
+    }
+    const unsigned fb = __ballot_sync(0xffffffffu, fresh);
+    if (FILL && fresh) {
+      const int at = distinct + __popc(fb & below);
+      if (at < 32) list[at] = ((uint64_t)(uint32_t)v << 32) | (uint32_t)hs[r];
+    }
+    distinct += __popc(fb);
+  }
+  if (!FILL) return distinct;   // the table counts any number of distinct values
+  if (distinct > 32) return -1;
+  __syncwarp();
+  // the distinct values, one per lane, sorted by a 32-key bitonic network;
+  // each carries its table slot
+  uint64_t kv = lane < distinct ? list[lane] : ~uint64_t(0);
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint64_t o = __shfl_xor_sync(0xffffffffu, kv, j);
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      kv = keep_min ? (o < kv ? o : kv) : (o > kv ? o : kv);
+    }
+  }
+  // lane t < distinct now holds the t-th smallest column; a row_ptr that
+  // disagrees is reported by the caller, not written past
+  if (distinct == len) {
+    if (lane < distinct) {
+      const int32_t col = (int32_t)(kv >> 32);
+      // self-last: the neighbours keep their ascending order, the row's own node goes last
+      const int pos = !self_last ? lane : (col < n ? lane : (col == n ? len - 1 : lane - 1));
+      cols[pos] = col;
+      rank[(uint32_t)kv & 0xffffu] = (uint8_t)pos;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (r * 32 + lane < m) slot[si[r]] = rank[hs[r]];
+  }
+  __syncwarp();
+  return distinct;
+}
+
 template <bool FILL>
 __device__ __forceinline__ int row_dispatch(int n, int npc, int m, const int32_t* cn, const int32_t* nc_cell,
                                             const uint8_t* local, int len, int self_last, int32_t* cols,
-                                            uint8_t* slot) {
+                                            uint8_t* slot, int32_t* key, uint8_t* rank, uint64_t* list) {
+  if (m <= kHashRow) {
+    const int got = row_hash<FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot, key, rank, list);
+    if (got >= 0) return got;
+  }
   if (m <= 32) return row_select<1, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
   if (m <= 64) return row_select<2, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
   if (m <= 128) return row_select<4, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
@@ -179,16 +282,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, in
                                                                  const int32_t* __restrict__ nc_cell,
                                                                  int32_t* __restrict__ row_len,
                                                                  int* __restrict__ err) {
+  __shared__ int32_t tab_key[kWarpsPerBlock][kHashSlots];
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  int32_t* const key = tab_key[threadIdx.x >> 5];
   for (int n = wid; n < nb_node; n += nwarps) {
     const int32_t b = __ldg(nc_ptr + n);
     const int m = (__ldg(nc_ptr + n + 1) - b) * npc;
     // a node in no cell keeps its diagonal (the reference's rows hold deg + 1 entries)
     int len = m > kRowCap ? -1
               : m == 0    ? 1
-                          : row_dispatch<false>(n, npc, m, cn, nc_cell + b, nullptr, 0, 0, nullptr, nullptr);
+                          : row_dispatch<false>(n, npc, m, cn, nc_cell + b, nullptr, 0, 0, nullptr, nullptr, key,
+                                                nullptr, nullptr);
     if (lane == 0) {
       if (len < 0 || len > kMaxRowLen) {
         atomicOr(err, 2);
@@ -206,9 +312,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, i
                                                                   const int32_t* __restrict__ row_ptr, int self_last,
                                                                   int32_t* __restrict__ cols,
                                                                   uint8_t* __restrict__ slot, int* __restrict__ err) {
+  __shared__ int32_t tab_key[kWarpsPerBlock][kHashSlots];
+  __shared__ uint8_t tab_rank[kWarpsPerBlock][kHashSlots];
+  __shared__ uint64_t tab_list[kWarpsPerBlock][32];
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  int32_t* const key = tab_key[threadIdx.x >> 5];
+  uint8_t* const rank = tab_rank[threadIdx.x >> 5];
+  uint64_t* const list = tab_list[threadIdx.x >> 5];
   for (int n = wid; n < nb_node; n += nwarps) {
     const int32_t rb = __ldg(row_ptr + n);
     const int len = __ldg(row_ptr + n + 1) - rb;
@@ -220,7 +332,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, i
       if (lane == 0 && len == 1) cols[rb] = n;
     } else if (m <= kRowCap) {
       got = row_dispatch<true>(n, npc, m, cn, nc_cell + b, nc_local + b, len, self_last, cols + rb,
-                               slot + (int64_t)b * npc);
+                               slot + (int64_t)b * npc, key, rank, list);
     }
     if (lane == 0 && got != len) atomicOr(err, 4);
   }

@@ -1766,7 +1766,8 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_init(int n, const int32_t* 
                                                           const double* __restrict__ vals, const double* __restrict__ b,
                                                           const double* __restrict__ x, double* __restrict__ r,
                                                           float* __restrict__ r32, double* partials, FcgState* st,
-                                                          double rtol, double atol, int max_iter) {
+                                                          double rtol, double atol, int max_iter,
+                                                          const uint8_t* __restrict__ skip) {
   __shared__ double sh[kSolveBlock / 32];
   const int lane = threadIdx.x & (G - 1);
   const int groups = gridDim.x * (blockDim.x / G);
@@ -1783,8 +1784,10 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_init(int n, const int32_t* 
       const double bi = b[row], ri = bi - s;
       r[row] = ri;
       r32[row] = (float)ri;
-      rr += ri * ri;
-      bb += bi * bi;
+      if (!(skip && skip[row])) {   // forced (penalty) rows stay out of both norms when skip is given
+        rr += ri * ri;
+        bb += bi * bi;
+      }
     }
   }
   rr = block_sum(rr, sh);
@@ -1864,7 +1867,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_spmv(int n, const int32_t* 
 __global__ void __launch_bounds__(kSolveBlock) k_fcg_update(int n, double* __restrict__ x, double* __restrict__ r,
                                                             float* __restrict__ r32, const double* __restrict__ p,
                                                             const double* __restrict__ q, double* partials,
-                                                            FcgState* st) {
+                                                            FcgState* st, const uint8_t* __restrict__ skip) {
   pdl_trigger();
   pdl_wait();
   if (((volatile FcgState*)st)->done) return;
@@ -1876,7 +1879,7 @@ __global__ void __launch_bounds__(kSolveBlock) k_fcg_update(int n, double* __res
     const double ri = r[i] - alpha * q[i];
     r[i] = ri;
     r32[i] = (float)ri;
-    rr += ri * ri;
+    if (!(skip && skip[i])) rr += ri * ri;
   }
   rr = block_sum(rr, sh);
   if (threadIdx.x == 0) partials[blockIdx.x * 2] = rr;
@@ -1945,7 +1948,7 @@ struct FcgWork {
   double *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *partials = nullptr;
   FcgState* st = nullptr;
   int nparts = 0;
-  const void* key[4] = {};
+  const void* key[5] = {};
   int key_chunk = 0;
   GraphChunk* graph = nullptr;
   ~FcgWork() { delete graph; }
@@ -1990,6 +1993,14 @@ static afem_status apply_on(afem_mpnn net, cudaStream_t stream) {
 extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp, const int32_t* cols,
                                       const double* vals, const double* b, double* x, afem_mpnn net,
                                       const afem_solver_options* opt_in, afem_solve_info* info) {
+  return afem::fcg_solve(ctx, n, rp, cols, vals, b, x, nullptr, net, opt_in, info);
+}
+
+// afem_fcg_solve with the forced-row mask `skip` (nullable) of a linear
+// system: its rows stay out of the stop test's norms (skip_forced_rows).
+afem_status afem::fcg_solve(afem_context ctx, int n, const int32_t* rp, const int32_t* cols, const double* vals,
+                            const double* b, double* x, const uint8_t* skip, afem_mpnn net,
+                            const afem_solver_options* opt_in, afem_solve_info* info) {
   AFEM_CHECK_ARG(ctx && n > 0 && rp && cols && vals && b && x && net, "afem_fcg_solve: bad arguments");
   AFEM_CHECK_ARG(net->ctx == ctx, "afem_fcg_solve: the network belongs to another context");
   AFEM_CHECK_ARG(net->n0 == n && net->have_operator, "afem_fcg_solve: network not set for this operator");
@@ -2006,12 +2017,12 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
   FcgWork* w = nullptr;
   AFEM_TRY(fcg_work(net, &w));
   if (!net->scalings_valid) AFEM_TRY(features_forward(net));
-  const void* key[4] = {rp, cols, vals, x};
-  if (!w->graph || w->key_chunk != chunk || !std::equal(key, key + 4, w->key)) {
+  const void* key[5] = {rp, cols, vals, x, skip};
+  if (!w->graph || w->key_chunk != chunk || !std::equal(key, key + 5, w->key)) {
     delete w->graph;
     w->graph = new (std::nothrow) GraphChunk();
     if (!w->graph) return fail(AFEM_ERR_OOM, "afem_fcg_solve: host allocation");
-    std::copy(key, key + 4, w->key);
+    std::copy(key, key + 5, w->key);
     w->key_chunk = chunk;
     afem_status cst = capture(ctx, *w->graph, [&](cudaStream_t s) -> afem_status {
       for (int k = 0; k < chunk; ++k) {
@@ -2020,7 +2031,7 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
                             (const double*)w->p, (const double*)w->r, w->q, w->partials, w->st);
         }));
         AFEM_TRY(launch_pdl(ctx, s, k_fcg_update, dim3(grid_vec), kSolveBlock, n, x, w->r, net->r32,
-                            (const double*)w->p, (const double*)w->q, w->partials, w->st));
+                            (const double*)w->p, (const double*)w->q, w->partials, w->st, skip));
         AFEM_TRY(apply_on(net, s));
         AFEM_TRY(launch_pdl(ctx, s, k_fcg_widen, dim3(grid_vec), kSolveBlock, n, (const float*)net->z32, w->z,
                             (const double*)w->q, w->p, 0, w->partials, w->st));
@@ -2041,7 +2052,7 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
   AFEM_CUDA(cudaEventRecord(e0, ctx->stream));
   afem_status st = dispatch_g(G, [&](auto g) {
     return launch(ctx, k_fcg_init<decltype(g)::value>, grid_rows, kSolveBlock, 0, n, rp, cols, vals, b,
-                  (const double*)x, w->r, net->r32, w->partials, w->st, opt.rtol, opt.atol, max_iter);
+                  (const double*)x, w->r, net->r32, w->partials, w->st, opt.rtol, opt.atol, max_iter, skip);
   });
   if (st == AFEM_OK) st = apply(net, 1, net->r32, net->z32);
   if (st == AFEM_OK)
@@ -2073,7 +2084,7 @@ extern "C" afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* rp
   cudaEventDestroy(e1);
   if (st != AFEM_OK) return st;
   double rel = 0.0;
-  AFEM_TRY(true_relres(ctx, n, rp, cols, vals, nnz32, b, x, nullptr, &rel));
+  AFEM_TRY(true_relres(ctx, n, rp, cols, vals, nnz32, b, x, skip, &rel));
   if (info) {
     info->iterations = hs.iter;
     info->refinements = 0;

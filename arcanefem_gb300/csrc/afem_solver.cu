@@ -784,10 +784,13 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
   double rr_prev = 0.0;      // true ||r||^2 at the previous update
   bool restart = true;
   for (;; ++outer_steps) {
+    // max_iter bounds the inner iterations of the whole solve (the reference's
+    // max-iter, HypreDoFLinearSystem.cc:182): each cycle gets what remains
+    const int remaining = std::max(1, max_iter - total_inner);
     AFEM_TRY(dispatch_g(G64, [&](auto g) {
       return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows64, kSolveBlock, 0, n, rp, cols, vals, b,
                     (const double*)x, (const float*)dinv32, skip, r32, x32, z32, partials, outer, inner,
-                    inner_rtol, max_iter, restart ? 1 : 0);
+                    inner_rtol, remaining, restart ? 1 : 0);
     }));
     CgState ho{};
     AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, outer, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
@@ -799,7 +802,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
       AFEM_TRY(dispatch_g(G64, [&](auto g) {
         return launch(ctx, k_ir_residual<decltype(g)::value>, grid_rows64, kSolveBlock, 0, n, rp, cols, vals, b,
                       (const double*)x, (const float*)dinv32, skip, r32, x32, z32, partials, outer, inner,
-                      inner_rtol, max_iter, 1);
+                      inner_rtol, remaining, 1);
       }));
       AFEM_CUDA(cudaMemcpyAsync(ctx->pinned, outer, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
       AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -818,7 +821,7 @@ afem_status cg_mixed(afem_context ctx, int n, const int32_t* rp, const int32_t* 
     } else if (ho.done) {
       break;
     }
-    if (outer_steps >= max_outer || total_inner >= 50 * max_iter) {
+    if (outer_steps >= max_outer || total_inner >= max_iter) {
       status = AFEM_ERR_NOT_CONVERGED;
       break;
     }

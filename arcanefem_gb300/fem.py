@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import ctypes as C
 import sys
+import weakref
 from dataclasses import dataclass
 
 import torch
@@ -30,12 +31,24 @@ import torch
 from . import _capi
 from ._capi import (AfemError, COLS_ASCENDING, COLS_SELF_LAST, ELIMINATE_ROW, ELIMINATE_ROW_COLUMN,  # noqa: F401
                     FORMULATION_MINIMAL, FORMULATION_REFERENCE, FORMULATION_TESTLAB, LAYOUT_PER_BLOCK,
-                    LAYOUT_PER_ROW, PRECISION_FP64, PRECISION_MIXED, PRECOND_JACOBI, PRECOND_NONE, MeshView,
-                    SolveInfo, SolverOptions, call)
+                    LAYOUT_PER_ROW, PRECISION_FP64, PRECISION_MIXED, PRECOND_JACOBI, PRECOND_LEARNED, PRECOND_NONE,
+                    MeshView, SolveInfo, SolverOptions, call)
 
 
 def _ptr(t) -> C.c_void_p:
     return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+def solve_call(name: str, info: SolveInfo, *args) -> SolveInfo:
+    """Call a solver entry point; on a failure status (not converged, breakdown)
+    the raised AfemError carries the filled SolveInfo as ``.info`` (the
+    solution argument then holds the last iterate)."""
+    try:
+        call(name, *args)
+    except AfemError as e:
+        e.info = info
+        raise
+    return info
 
 
 class _DeviceArray:
@@ -59,6 +72,13 @@ class Context:
         h = C.c_void_p()
         call("afem_context_create", C.byref(h), C.c_void_p(self.stream.cuda_stream))
         self.handle = h
+        # handles created on this context (linear systems, networks, batches):
+        # closed before it, since the library's objects use their context's stream
+        self._children = weakref.WeakSet()
+
+    def adopt(self, child) -> None:
+        """Register an object with a close() that must run before the context's."""
+        self._children.add(child)
 
     def synchronize(self) -> None:
         """Wait for the stream; raises AFEM_ERR_MESH if an element kernel met a degenerate cell."""
@@ -90,6 +110,8 @@ class Context:
 
     def close(self) -> None:
         if self.handle:
+            for child in list(self._children):
+                child.close()
             call("afem_context_destroy", self.handle)
             self.handle = None
 
@@ -320,6 +342,7 @@ class DoFLinearSystem:
         h = C.c_void_p()
         call("afem_ls_create", ctx.handle, nb_dof, C.byref(h))
         self.handle = h
+        ctx.adopt(self)
         ptrs = [C.c_void_p() for _ in range(6)]
         call("afem_ls_dof_variables", h, *[C.byref(p) for p in ptrs])
         self._rhs = device_view(ptrs[0].value, nb_dof, torch.float64)
@@ -365,6 +388,12 @@ class DoFLinearSystem:
         call("afem_ls_set_csr_view", self.handle, int(rows.numel()), _ptr(rows), _ptr(rows_nb_column),
              int(columns.numel()), _ptr(columns), _ptr(values))
 
+    def set_learned_preconditioner(self, net):
+        """Attach the learned preconditioner (a learned.MPNN built on this system's
+        matrix graph) for solves with precond = PRECOND_LEARNED; None detaches it."""
+        self._learned = net
+        call("afem_ls_set_learned_preconditioner", self.handle, None if net is None else net.handle)
+
     def clear_values(self):
         call("afem_ls_clear_values", self.handle)
         self._keep = None
@@ -395,8 +424,7 @@ class DoFLinearSystem:
         if opt.block_size == 0 and getattr(self, "block_size", 1) == 3:
             opt = SolverOptions.from_buffer_copy(opt)
             opt.block_size = 3
-        call("afem_ls_solve", self.handle, C.byref(opt), C.byref(info))
-        return info
+        return solve_call("afem_ls_solve", info, self.handle, C.byref(opt), C.byref(info))
 
     # DoFLinearSystem::applyLinearSystemTransformationAndSolve (DoFLinearSystem.cc:487-493)
     def apply_linear_system_transformation_and_solve(self, options: SolverOptions | None = None) -> SolveInfo:
@@ -433,9 +461,8 @@ def cg_solve_csr(ctx: Context, row_ptr, cols, values, b, x, forced_info=None, op
     info = SolveInfo()
     opt = options or solver_options()
     n = int(row_ptr.numel()) - 1
-    call("afem_cg_solve_csr", ctx.handle, n, _ptr(row_ptr), _ptr(cols), _ptr(values), _ptr(b), _ptr(x),
-         _ptr(forced_info), C.byref(opt), C.byref(info))
-    return info
+    return solve_call("afem_cg_solve_csr", info, ctx.handle, n, _ptr(row_ptr), _ptr(cols), _ptr(values), _ptr(b),
+                      _ptr(x), _ptr(forced_info), C.byref(opt), C.byref(info))
 
 
 FACE_SCALAR, FACE_NORMAL, FACE_VECTOR = 0, 1, 2

@@ -158,6 +158,137 @@ class Hierarchy:
             self.coarse.append(dcsr(G))
 
 
+class AlgebraicHierarchy:
+    """The level hierarchy built from the matrix alone, for any mesh (the
+    unstructured triangle and tetrahedron meshes of the reference included):
+    smoothed aggregation.
+
+    Per level: strong connections |A_ij| >= theta sqrt(A_ii A_jj); aggregates
+    by a greedy pass (a node none of whose strong neighbours is aggregated
+    seeds an aggregate with them), then every left-over node joins the
+    aggregate of a strong neighbour, or starts its own; the tentative
+    prolongation T (1 where a node belongs to an aggregate) is smoothed once,
+    P = (I - (4/3) / rho(D^-1 A) D^-1 A) T, with rho estimated by power
+    iteration.  Rows with no off-diagonal entry -- the eliminated Dirichlet
+    rows, whose matrix row is the identity -- join no aggregate, so P vanishes
+    there and the coarse spaces satisfy the boundary condition.  Levels stop
+    at `min_coarse` rows.  The network's coarse graphs are the patterns of
+    the Galerkin operators with row-normalised weights; its features restrict
+    by aggregate averages.  Same attributes as Hierarchy (structure only: the
+    library recomputes the coarse values on the device from the matrix).
+    Node ids are taken in the matrix's order, so the result is deterministic."""
+
+    def __init__(self, row_ptr0: torch.Tensor, cols0: torch.Tensor, values0: torch.Tensor, levels: int = 12,
+                 min_coarse: int = 64, theta: float = 0.08):
+        rp = row_ptr0.cpu().numpy()
+        c0 = cols0.cpu().numpy()
+        v0 = values0.cpu().numpy().astype(np.float64)
+        n0 = rp.size - 1
+        A = sp.csr_matrix((v0, c0, rp), shape=(n0, n0))
+        self.keep = []
+        dev = "cuda"
+
+        def dcsr(M):
+            M = sp.csr_matrix(M)
+            M.sort_indices()
+            t = (torch.as_tensor(M.indptr.astype(np.int32), device=dev),
+                 torch.as_tensor(M.indices.astype(np.int32), device=dev),
+                 torch.as_tensor(M.data.astype(np.float32), device=dev))
+            self.keep.append(t)
+            return t
+
+        Ps, Ts = [], []
+        Al = A
+        while Al.shape[0] > min_coarse and len(Ps) + 1 < levels:
+            P, T = self._level(Al, theta)
+            if P.shape[1] == 0 or P.shape[1] >= Al.shape[0]:
+                break
+            Ps.append(P)
+            Ts.append(T)
+            Al = sp.csr_matrix(P.T @ Al @ P)
+        self.levels = len(Ps) + 1
+        self.rows = [n0] + [P.shape[1] for P in Ps]
+        self.sizes = list(self.rows)
+        # host copies (scipy) of the transfers and the network's graphs
+        self.host_prol, self.host_restr, self.host_graph = list(Ps), [], [None]
+        self.graph = [(row_ptr0, cols0, None)]
+        self.restr, self.restrT, self.prol, self.prolT = [], [], [], []
+        self.coarse = [None]
+        G = sp.csr_matrix((np.ones(c0.size), c0, rp), shape=(n0, n0))
+        for P, T in zip(Ps, Ts):
+            # feature restriction: the average over each aggregate
+            cnt = np.asarray(T.sum(axis=0)).ravel()
+            R = sp.csr_matrix(sp.diags(1.0 / np.maximum(cnt, 1.0)) @ T.T)
+            self.host_restr.append(R)
+            self.restr.append(dcsr(R))
+            self.restrT.append(dcsr(R.T))
+            self.prol.append(dcsr(P))
+            self.prolT.append(dcsr(P.T))
+            G = sp.csr_matrix(abs(P).T @ G @ abs(P))
+            G.data[:] = 1.0
+            G.sort_indices()
+            self.coarse.append(dcsr(G))
+            # the network's graph on this level: the Galerkin pattern without the
+            # diagonal, each row averaging its neighbours
+            S = sp.csr_matrix(G - sp.diags(G.diagonal()))
+            S.eliminate_zeros()
+            deg = np.diff(S.indptr)
+            S.data = np.repeat(1.0 / np.maximum(deg, 1), deg)
+            self.host_graph.append(S)
+            self.graph.append(dcsr(S))
+
+    @staticmethod
+    def _level(A: sp.csr_matrix, theta: float):
+        n = A.shape[0]
+        d = A.diagonal()
+        C = sp.coo_matrix(A)
+        offd = C.row != C.col
+        nonzero_offd = np.bincount(C.row[offd & (C.data != 0)], minlength=n)
+        dirichlet = nonzero_offd == 0
+        strong = offd & (np.abs(C.data) >= theta * np.sqrt(np.abs(d[C.row] * d[C.col])))
+        S = sp.csr_matrix((np.ones(int(strong.sum())), (C.row[strong], C.col[strong])), shape=(n, n))
+        ind, ptr = S.indices, S.indptr
+        agg = np.full(n, -1, np.int64)
+        agg[dirichlet] = -2
+        na = 0
+        for i in range(n):                      # seeds: a node with no aggregated strong neighbour
+            if agg[i] != -1:
+                continue
+            nb = ind[ptr[i]:ptr[i + 1]]
+            nb = nb[agg[nb] != -2]
+            if np.all(agg[nb] == -1):
+                agg[i] = na
+                agg[nb] = na
+                na += 1
+        for i in range(n):                      # left-overs join a strong neighbour's aggregate
+            if agg[i] != -1:
+                continue
+            nb = ind[ptr[i]:ptr[i + 1]]
+            cand = agg[nb][agg[nb] >= 0]
+            if cand.size:
+                agg[i] = cand[0]
+        for i in range(n):                      # or start their own
+            if agg[i] == -1:
+                agg[i] = na
+                na += 1
+        rows = np.flatnonzero(agg >= 0)
+        T = sp.csr_matrix((np.ones(rows.size), (rows, agg[rows])), shape=(n, na))
+        dinv = np.where(dirichlet | (d == 0), 0.0, 1.0 / np.where(d != 0, d, 1.0))
+        Dinv = sp.diags(dinv)
+        x = np.random.default_rng(1).random(n) * (~dirichlet)
+        lam = 1.0
+        for _ in range(20):                     # rho(D^-1 A) by power iteration
+            x = Dinv @ (A @ x)
+            lam = float(np.linalg.norm(x))
+            if lam == 0.0:
+                lam = 1.0
+                break
+            x /= lam
+        P = sp.csr_matrix(T - (4.0 / 3.0 / lam) * (Dinv @ (A @ T)))
+        P.eliminate_zeros()
+        return P, T
+
+
 def param_count(layers: int, levels: int) -> int:
     """W_in[2][64], b_in[64]; per layer W1, W2 [64][64], b[64]; per level head w[64], beta."""
     return 3 * F + layers * (2 * F * F + F) + levels * (F + 1)
@@ -203,6 +334,7 @@ class MPNN:
                                  C.byref(h))
         _capi.check(rc, "afem_mpnn_create")
         self.handle = h
+        ctx.adopt(self)
         self.max_batch = max_batch
         self.nparam = int(_capi.lib().afem_mpnn_param_count(h))
         self.n0 = hier.rows[0]
@@ -254,9 +386,8 @@ class MPNN:
     def fcg(self, row_ptr, cols, values, b, x, options=None) -> _capi.SolveInfo:
         info = _capi.SolveInfo()
         opt = options or fem.solver_options()
-        call("afem_fcg_solve", self.ctx.handle, int(row_ptr.numel()) - 1, _ptr(row_ptr), _ptr(cols), _ptr(values),
-             _ptr(b), _ptr(x), self.handle, C.byref(opt), C.byref(info))
-        return info
+        return fem.solve_call("afem_fcg_solve", info, self.ctx.handle, int(row_ptr.numel()) - 1, _ptr(row_ptr),
+                              _ptr(cols), _ptr(values), _ptr(b), _ptr(x), self.handle, C.byref(opt), C.byref(info))
 
     def close(self):
         if self.handle:

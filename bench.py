@@ -37,7 +37,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -52,18 +51,21 @@ HBM_FALLBACK_GBS = 6800.0
 
 WORKLOADS = {
     "poisson3d": dict(dim=3, n=128, jitter=0.15, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 3D Poisson P1)",
-                      dp_elem=72, dp_gather=16, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
+                      dp_gather=16, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
     "elasticity3d": dict(dim=3, n=96, jitter=0.15, nb_dof=3,
                          metric="assembled nnz/s (node-wise 3x3 BSR, 3D linear elasticity P1)",
-                         dp_elem=238, dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
+                         dp_gather=144, rtol=1e-8, precision="mixed", dirichlet="zmin",
                          E=21e5, nu=0.28, body=(0.0, 0.0, -1.0)),
     "poisson2d": dict(dim=2, n=256, jitter=0.2, nb_dof=1, metric="assembled nnz/s (node-wise CSR, 2D Poisson P1)",
-                      dp_elem=29, dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
+                      dp_gather=9, rtol=1e-10, precision="fp64", dirichlet="boundary", source=-1.0),
     # Q1 widening: trilinear hexahedra (2x2x2 Gauss points), Q1 source, FP64 / mixed CG
     "poisson3d_hex": dict(dim=3, cell="hex", n=96, jitter=0.15, nb_dof=1,
                           metric="assembled nnz/s (node-wise CSR, 3D Poisson Q1 Hexa8)",
-                          dp_elem=2218, dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
+                          dp_gather=64, rtol=1e-8, precision="fp64", dirichlet="x_faces", source=1.0),
 }
+# the workloads that ride along on the default line, after the main one
+EXTRA_WORKLOADS = ("elasticity3d", "poisson2d", "poisson3d_hex")
+FORMULATIONS = ("reference", "minimal")
 
 
 def parse_args():
@@ -90,6 +92,8 @@ def parse_args():
     p.add_argument("--batched-sides", type=int, nargs=2, default=(64, 512), metavar=("MIN", "MAX"))
     p.add_argument("--batched-tune", choices=["auto", "none"], default="auto",
                    help="auto: autotune (JSON cache); none: the library's default configuration")
+    p.add_argument("--no-extra-workloads", action="store_true",
+                   help="measure the main workload only (skip " + ", ".join(EXTRA_WORKLOADS) + ")")
     a = p.parse_args()
     if a.n <= 0:
         a.n = WORKLOADS[a.workload]["n"]
@@ -113,30 +117,31 @@ def replica_value(total_ms: float, world: int, units_per_rank: int, steps: int, 
     return ms_per_step, world * units_per_rank / (ms_per_step * 1e-3)
 
 
-def make_mesh(args):
+def make_mesh(name, n, seed):
     from arcanefem_gb300 import meshgen
-    w = WORKLOADS[args.workload]
+    w = WORKLOADS[name]
     if w.get("cell") == "hex":
-        return meshgen.unit_cube_hex(args.n, jitter=w["jitter"], seed=args.seed)
+        return meshgen.unit_cube_hex(n, jitter=w["jitter"], seed=seed)
     if w["dim"] == 3:
-        return meshgen.unit_cube_tet(args.n, jitter=w["jitter"], seed=args.seed)
-    return meshgen.unit_square_tri(args.n, jitter=w["jitter"], seed=args.seed)
+        return meshgen.unit_cube_tet(n, jitter=w["jitter"], seed=seed)
+    return meshgen.unit_square_tri(n, jitter=w["jitter"], seed=seed)
 
 
-def config(args, world):
-    w = WORKLOADS[args.workload]
+def config(name, n, seed, world):
+    w = WORKLOADS[name]
     if w.get("cell") == "hex":
-        desc = f"unit cube {args.n}^3 trilinear hexahedra, jitter {w['jitter']}h"
-        elements, nodes = args.n ** 3, (args.n + 1) ** 3
+        desc = f"unit cube {n}^3 trilinear hexahedra, jitter {w['jitter']}h"
+        elements, nodes = n ** 3, (n + 1) ** 3
     elif w["dim"] == 3:
-        desc = f"unit cube {args.n}^3 hexahedra x 6 Kuhn tetrahedra, jitter {w['jitter']}h"
-        elements, nodes = 6 * args.n ** 3, (args.n + 1) ** 3
+        desc = f"unit cube {n}^3 hexahedra x 6 Kuhn tetrahedra, jitter {w['jitter']}h"
+        elements, nodes = 6 * n ** 3, (n + 1) ** 3
     else:
-        desc = f"unit square {args.n}^2 quads x 2 triangles, jitter {w['jitter']}h"
-        elements, nodes = 2 * args.n ** 2, (args.n + 1) ** 2
-    return {"workload": f"{args.workload} ({desc})", "elements": elements, "nodes": nodes,
-            "dof_per_node": w["nb_dof"], "seed": args.seed,
+        desc = f"unit square {n}^2 quads x 2 triangles, jitter {w['jitter']}h"
+        elements, nodes = 2 * n ** 2, (n + 1) ** 2
+    return {"workload": f"{name} ({desc})", "elements": elements, "nodes": nodes,
+            "dof_per_node": w["nb_dof"], "seed": seed,
             "step": "values assembly (element matrices + node-wise gather), sparsity reused",
+            "element_arithmetic": "reference rounding (bit-identical to the reference's node-wise assembly)",
             "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"}
 
 
@@ -204,16 +209,16 @@ def read_peaks():
         return HBM_FALLBACK_GBS, "fallback"
 
 
-def read_traffic(name: str):
-    """Per-assembly DRAM bytes from the committed ncu summary (profiles/), or None."""
+def read_counters(name: str, n: int, formulation: str):
+    """ncu counters of one assembly of this workload (profiles/assembly_counters.json,
+    machine-readable; the capture commands are recorded in it): DRAM bytes per
+    assembly and FP64 instructions per cell, or {} when not captured."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", name)):
-            m = re.match(r"\s*traffic_bytes_per_assembly\s*[:=]\s*([0-9.eE+]+)", line)
-            if m:
-                return float(m.group(1))
-    except OSError:
-        pass
-    return None
+        with open(os.path.join(ROOT, "profiles", "assembly_counters.json")) as f:
+            table = json.load(f)
+        return dict(table["workloads"][f"{name}_n{n}"][formulation])
+    except (OSError, KeyError, ValueError, TypeError):
+        return {}
 
 
 def algorithmic_bytes(mesh, nnz_scalar):
@@ -223,20 +228,102 @@ def algorithmic_bytes(mesh, nnz_scalar):
 
 
 # ---------------------------------------------------------------------------
-def run_gpu(args):
+def time_assembly(fmt, ke, lam, mu, steps, warmup, flush, clk_index=None):
+    """Device time of the values assembly (element matrices, then the node-wise
+    gather), CUDA events on the launching stream around each stage, L2 flushed
+    before every step; nvidia-smi clocks sampled over the timed region when
+    clk_index is given."""
+    import contextlib
+
     import torch
-    import torch.distributed as dist
+
+    def step(ev=None):
+        if ev:
+            ev[0].record()
+        fmt.element_matrices(ke, lam=lam, mu=mu)
+        if ev:
+            ev[1].record()
+        fmt.gather(ke)
+        if ev:
+            ev[2].record()
+
+    for _ in range(max(warmup, 3)):
+        flush.fill_(1.0)
+        step()
+    torch.cuda.synchronize()
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    launches0 = fmt.ctx.launches
+    clk = ClockSampler(clk_index) if clk_index is not None else contextlib.nullcontext()
+    with clk:
+        t0 = time.perf_counter()
+        for k in range(steps):
+            flush.fill_(float(k))
+            step(events[k])
+        torch.cuda.synchronize()
+        wall_s = time.perf_counter() - t0
+    fmt.ctx.synchronize()   # raises on a degenerate cell
+    elem = [e[0].elapsed_time(e[1]) for e in events]
+    gath = [e[1].elapsed_time(e[2]) for e in events]
+    return {"element_ms": elem, "gather_ms": gath, "total_ms": sum(a + b for a, b in zip(elem, gath)),
+            "launches": fmt.ctx.launches - launches0, "wall_s": wall_s,
+            "clocks": clk.summary() if clk_index is not None else None}
+
+
+def time_structure(fmt, reps=3):
+    """Warm device time (CUDA events) of the structure build on the existing
+    buffers: node -> cell lists, row lengths + scan, columns + slot map."""
+    import ctypes as C
+
+    import torch
+
+    from arcanefem_gb300._capi import call
+    m = fmt.mesh
+    p = lambda t: C.c_void_p(t.data_ptr())
+    nnz = C.c_int64()
+    res = {"node_cell_ms": [], "rows_ms": [], "cols_ms": []}
+    for _ in range(reps + 1):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record()
+        call("afem_node_cell_build", fmt.ctx.handle, m.nb_node, m.nb_cell, m.npc, p(m.cells), p(fmt.nc_ptr),
+             p(fmt.nc_cell), p(fmt.nc_local), p(fmt.nc_inverse))
+        ev[1].record()
+        call("afem_sparsity_rows", fmt.ctx.handle, m.nb_node, m.npc, p(m.cells), p(fmt.nc_ptr), p(fmt.nc_cell),
+             p(fmt.row_ptr), C.byref(nnz))
+        ev[2].record()
+        call("afem_sparsity_cols", fmt.ctx.handle, m.nb_node, m.npc, p(m.cells), p(fmt.nc_ptr), p(fmt.nc_cell),
+             p(fmt.nc_local), p(fmt.row_ptr), fmt.col_order, p(fmt.cols), p(fmt.nc_slot))
+        ev[3].record()
+        torch.cuda.synchronize()
+        for k, key in enumerate(("node_cell_ms", "rows_ms", "cols_ms")):
+            res[key].append(ev[k].elapsed_time(ev[k + 1]))
+    out = {k: statistics.median(v[1:]) for k, v in res.items()}
+    out["sparsity_ms"] = out["rows_ms"] + out["cols_ms"]
+    out["note"] = "warm, device time; rows_ms includes the host read of nnz"
+    return out
+
+
+def kernel_names(name, mesh, formulation):
+    w = WORKLOADS[name]
+    if w["nb_dof"] == 3:
+        return "k_elem_elasticity_tet + k_gather_elasticity"
+    if w.get("cell") == "hex":
+        return "k_elem_poisson_hexa8 + k_gather_scalar<8>"
+    if formulation == "minimal":
+        return f"k_elem_poisson_{'tet' if mesh.dim == 3 else 'tri'} + k_gather_scalar<{mesh.npc}>"
+    return f"k_elem_poisson_p1_ref<{mesh.npc}> + k_gather_scalar<{mesh.npc}>"
+
+
+def measure_workload(args, name, n, ctx, rank, world, local, main):
+    """One workload: structure once, then the timed values assembly in the
+    reference rounding (the headline) and in the minimal-instruction
+    formulation, each checked against the oracle; e2e through the public API
+    with host buffers; the solves."""
+    import torch
 
     from arcanefem_gb300 import fem
 
-    w = WORKLOADS[args.workload]
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    mesh = make_mesh(args)
-    ctx = fem.Context()
+    w = WORKLOADS[name]
+    mesh = make_mesh(name, n, args.seed)
     dm = fem.Mesh.from_host(mesh.dim, mesh.coords, mesh.cells)
     fmt = fem.BSRFormat(ctx, dm)
     torch.cuda.synchronize()
@@ -249,81 +336,120 @@ def run_gpu(args):
     lam, mu = fem.lame(w["E"], w["nu"]) if w["nb_dof"] == 3 else (0.0, 0.0)
     ke = torch.empty(fmt.element_buffer_size(), dtype=torch.float64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    steps = args.steps if main else min(args.steps, 10)
 
-    def step(ev=None):
-        if ev:
-            ev[0].record()
-        fmt.element_matrices(ke, lam=lam, mu=mu)
-        if ev:
-            ev[1].record()
-        fmt.gather(ke)
-        if ev:
-            ev[2].record()
-
-    for _ in range(max(args.warmup, 3)):
-        flush.fill_(1.0)
-        step()
-    torch.cuda.synchronize()
-    events = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    launches0 = ctx.launches
     if world > 1:
+        import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        for k in range(args.steps):
-            flush.fill_(float(k))
-            step(events[k])
-        torch.cuda.synchronize()
-        wall_s = time.perf_counter() - t0
-    launches = ctx.launches - launches0
-    elem_ms = [e[0].elapsed_time(e[1]) for e in events]
-    gath_ms = [e[1].elapsed_time(e[2]) for e in events]
-    total_ms = sum(a + b for a, b in zip(elem_ms, gath_ms))
-    ms_per_step, value = replica_value(total_ms, world, nnz, args.steps, "cuda")
+    ctx.formulation = fem.FORMULATION_REFERENCE
+    t_ref = time_assembly(fmt, ke, lam, mu, steps, args.warmup, flush, clk_index=local)
+    ms_per_step, value = replica_value(t_ref["total_ms"], world, nnz, steps, "cuda")
 
     hbm_peak, peak_kind = read_peaks()
     alg = algorithmic_bytes(mesh, nnz)
-    achieved = alg / (ms_per_step * 1e-3) / 1e9
-    traffic = read_traffic(f"assembly_{args.workload}_n{args.n}.md")
     fma_rate = ctx.fp64_fma_rate()
-    dp_cell = w["dp_elem"] + w["dp_gather"]
-    dp_achieved = dp_cell * mesh.nb_cell / (ms_per_step * 1e-3) / 1e9
-    kernel = ("k_elem_elasticity_tet + k_gather_elasticity" if w["nb_dof"] == 3 else
-              f"k_elem_poisson_hexa8 + k_gather_scalar<8>" if w.get("cell") == "hex" else
-              f"k_elem_poisson_{'tet' if mesh.dim == 3 else 'tri'} + k_gather_scalar<{mesh.npc}>")
 
-    e2e = None if args.no_e2e else run_e2e(args, mesh, fmt, lam, mu)
-    cpu = None
+    def rooflines(ms, formulation):
+        counters = read_counters(name, n, formulation)
+        achieved = alg / (ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": counters.get("traffic_bytes_per_assembly"), "peak_source": peak_kind,
+                "algorithmic_bytes": alg, "kernel": kernel_names(name, mesh, formulation),
+                "limiter": "fp64 issue (fp64_roofline): the element arithmetic is FP64 on a part with a "
+                           "narrow FP64 pipe"}
+        dp_cell = counters.get("fp64_instructions_per_cell")
+        fp = None
+        if dp_cell:
+            dp_achieved = dp_cell * mesh.nb_cell / (ms * 1e-3) / 1e9
+            fp = {"achieved_g_fp64_instr_s": dp_achieved, "peak_g_fma_s": fma_rate, "frac": dp_achieved / fma_rate,
+                  "fp64_instructions_per_cell": dp_cell, "source": "ncu sm__inst_executed_pipe_fp64 (profiles/)"}
+        return roof, fp
+
+    roof, fp64 = rooflines(ms_per_step, "reference")
+    out = {"value": value, "unit": UNIT, "ms_per_step": ms_per_step, "steps": steps, "nnz": nnz,
+           "config": config(name, n, args.seed, world),
+           "element_ms": statistics.mean(t_ref["element_ms"]), "gather_ms": statistics.mean(t_ref["gather_ms"]),
+           "structure_ms_once": structure_ms, "wall_s_timed_loop": t_ref["wall_s"],
+           "gpu_launches": t_ref["launches"], "roofline": roof, "fp64_roofline": fp64, "clocks": t_ref["clocks"]}
+
+    oracle_values = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, mesh, fmt, lam, mu)
-    solve = None if args.no_solve else run_solve(args, ctx, mesh, fmt)
+        out["cpu_baseline"], oracle_values = cpu_baseline(name, mesh, fmt, lam, mu)
+        if main or name == "poisson2d":
+            plan = cpu_plan_baselines(name, mesh, fmt, lam, mu)
+            if "B5_sparsity" in plan:
+                plan["B5_sparsity"]["gpu_structure_ms_once"] = structure_ms
+            out["cpu_baseline"]["plan_baselines"] = plan
+
+    # the opt-in minimal-instruction formulation, same mesh and steps
+    ctx.formulation = fem.FORMULATION_MINIMAL
+    t_min = time_assembly(fmt, ke, lam, mu, steps, 3, flush)
+    ms_min = t_min["total_ms"] / steps
+    roof_m, fp64_m = rooflines(ms_min, "minimal")
+    mini = {"value": world * nnz / (ms_min * 1e-3), "ms_per_step": ms_min,
+            "element_ms": statistics.mean(t_min["element_ms"]), "gather_ms": statistics.mean(t_min["gather_ms"]),
+            "roofline_frac": roof_m["frac"], "fp64_roofline": fp64_m,
+            "note": "AFEM_FORMULATION_MINIMAL: fewest FP64 instructions, closer to exact arithmetic than the "
+                    "reference's formula, not bit-identical to it"}
+    if oracle_values is not None:
+        mini["max_rel_diff_vs_oracle"] = guard_error(fmt.values.cpu().numpy(), oracle_values, fmt.row_ptr.cpu().numpy(),
+                                                     w["nb_dof"])
+    out["minimal_formulation"] = mini
+    ctx.formulation = fem.FORMULATION_REFERENCE
+    fmt.element_matrices(ke, lam=lam, mu=mu)
+    fmt.gather(ke)
+    del ke, flush
+
+    out["structure"] = time_structure(fmt)
+    if not args.no_e2e:
+        out["e2e"] = run_e2e(args, name, mesh, fmt, lam, mu)
+    if not args.no_solve:
+        out["solve"] = run_solve(args, name, ctx, mesh, fmt)
+    return out
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    from arcanefem_gb300 import fem
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ctx = fem.Context()
+    main = measure_workload(args, args.workload, args.n, ctx, rank, world, local, main=True)
+    extras = {}
+    if not args.no_extra_workloads:
+        for name in EXTRA_WORKLOADS:
+            if name != args.workload:
+                extras[name] = measure_workload(args, name, WORKLOADS[name]["n"], ctx, rank, world, local, main=False)
     learned = None if (args.no_learned or rank != 0) else run_learned(args)
     batched = None if (args.no_batched or rank != 0) else run_batched(args)
 
     if rank == 0:
+        w = WORKLOADS[args.workload]
         out = {
-            "metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
+            "metric": w["metric"], "value": main.pop("value"), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": main.pop("ms_per_step"), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered mesh)",
-            "config": config(args, world),
-            "nnz": nnz, "element_ms": statistics.mean(elem_ms), "gather_ms": statistics.mean(gath_ms),
-            "structure_ms_once": structure_ms, "wall_s_timed_loop": wall_s, "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
-                         "algorithmic_bytes": alg, "kernel": kernel},
-            "fp64_roofline": {"achieved_g_fp64_instr_s": dp_achieved, "peak_g_fma_s": fma_rate,
-                              "frac": dp_achieved / fma_rate, "fp64_instr_per_cell": dp_cell,
-                              "note": "FP64 issue rate is the binding limit of the element kernel on GB300"},
-            "e2e": e2e, "cpu_baseline": cpu, "solve": solve, "learned": learned, "batched": batched,
-            "clocks": clk.summary(),
+            "config": main.pop("config"), "gpu_launches": main.pop("gpu_launches"), "clocks": main.pop("clocks"),
         }
+        main.pop("unit")
+        out.update(main)
+        for v in extras.values():
+            v["metric"] = "assembled nnz/s"
+        out["workloads"] = extras
+        out["learned"] = learned
+        out["batched"] = batched
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
 
-def run_e2e(args, mesh, fmt0, lam, mu):
+def run_e2e(args, name, mesh, fmt0, lam, mu):
     """Same metric through the public API with host buffers (transfers timed).
 
     The step of the headline metric reuses the sparsity, so the e2e step does
@@ -336,7 +462,7 @@ def run_e2e(args, mesh, fmt0, lam, mu):
 
     from arcanefem_gb300 import fem
 
-    w = WORKLOADS[args.workload]
+    w = WORKLOADS[name]
     nnz = fmt0.nnzb * w["nb_dof"] ** 2
     coords_h = torch.from_numpy(mesh.coords).pin_memory()
     cells_h = torch.from_numpy(mesh.cells).pin_memory()
@@ -393,10 +519,20 @@ def run_e2e(args, mesh, fmt0, lam, mu):
         torch.cuda.current_stream().synchronize()
 
     dt = timed(values_step)
-    assert torch.equal(vals_h, fs.values.cpu()), "host values differ from the device's"
+    assert torch.equal(vals_h, fmt0.values.cpu()), "host values differ from the device assembly's"
     dt_r = timed(rebuild_step)
     assert torch.equal(rp_h, fs.row_ptr.cpu()) and torch.equal(cols_h, fs.cols.cpu()), "rebuilt structure differs"
-    assert torch.equal(vals_h, fs.values.cpu()), "rebuilt values differ"
+    assert torch.equal(vals_h, fmt0.values.cpu()), "rebuilt values differ"
+    # the coordinates do come from the host in every step: with the device copy
+    # poisoned, one more step of each kind still gives the same values
+    dco.fill_(float("nan"))
+    vals_h.fill_(0.0)
+    values_step()
+    assert torch.equal(vals_h, fmt0.values.cpu()), "values step did not upload the coordinates"
+    dco.fill_(float("nan"))
+    vals_h.fill_(0.0)
+    rebuild_step()
+    assert torch.equal(vals_h, fmt0.values.cpu()), "rebuild step did not upload the coordinates"
     h2d = coords_h.numel() * 8
     d2h = nnz * 8
     return {"value": nnz / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -412,9 +548,9 @@ def run_e2e(args, mesh, fmt0, lam, mu):
                                      "H2D in node prefixes, values D2H behind the node ranges)")}}
 
 
-def oracle_kind(args):
+def oracle_kind(name):
     from oracle import oracle as O
-    w = WORKLOADS[args.workload]
+    w = WORKLOADS[name]
     if w["nb_dof"] == 3:
         return O.ELASTICITY_TET4
     if w.get("cell") == "hex":
@@ -422,9 +558,21 @@ def oracle_kind(args):
     return O.POISSON_TET4 if w["dim"] == 3 else O.POISSON_TRI3
 
 
-def cpu_baseline(args, mesh, fmt, lam, mu):
+def guard_error(got, ref, rp, b):
+    """max |got - ref| / max(|ref|, 1e-3 max|row|) per (block) row: the parity
+    tests' guard for the minimal formulation."""
+    import numpy as np
+    row_of = np.repeat(np.arange(rp.size - 1), np.diff(rp) * b * b)
+    rowmax = np.zeros(rp.size - 1)
+    np.maximum.at(rowmax, row_of, np.abs(ref))
+    return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), np.where(rowmax[row_of] > 0,
+                                                                             1e-3 * rowmax[row_of], 1.0))))
+
+
+def cpu_baseline(name, mesh, fmt, lam, mu):
     """The oracle's node-wise assembly (CPU restatement of BSRFormat.h:473-537 with
-    the reference element vectors) on all host cores, same mesh and sparsity."""
+    the reference element vectors) on all host cores, same mesh and sparsity,
+    and the GPU values compared with it entry by entry."""
     import numpy as np
 
     from oracle import oracle as O
@@ -432,31 +580,75 @@ def cpu_baseline(args, mesh, fmt, lam, mu):
     threads = O.max_threads()
     ptr, nc = fmt.nc_ptr.cpu().numpy(), fmt.nc_cell.cpu().numpy()
     rp, cols = fmt.row_ptr.cpu().numpy(), fmt.cols.cpu().numpy()
-    nnz = fmt.nnzb * WORKLOADS[args.workload]["nb_dof"] ** 2
+    b = WORKLOADS[name]["nb_dof"]
+    nnz = fmt.nnzb * b * b
     t0 = time.perf_counter()
-    v = O.assemble(oracle_kind(args), mesh.coords, mesh.cells, ptr, nc, rp, cols, lam=lam, mu=mu, nb_threads=threads)
+    v = O.assemble(oracle_kind(name), mesh.coords, mesh.cells, ptr, nc, rp, cols, lam=lam, mu=mu, nb_threads=threads)
     dt = time.perf_counter() - t0
     gpu = fmt.values.cpu().numpy()
-    # the parity tests' guard: |gpu - cpu| / max(|cpu|, 1e-3 max |row|), per (block) row
-    b = WORKLOADS[args.workload]["nb_dof"]
-    row_of = np.repeat(np.arange(rp.size - 1), np.diff(rp) * b * b)
-    rowmax = np.zeros(rp.size - 1)
-    np.maximum.at(rowmax, row_of, np.abs(v))
-    err = float(np.max(np.abs(gpu - v) / np.maximum(np.abs(v), 1e-3 * rowmax[row_of])))
-    err_row = float(np.max(np.abs(gpu - v) / np.where(rowmax[row_of] > 0, rowmax[row_of], 1.0)))
     return {"value": nnz / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"one full values assembly of the same mesh ({mesh.nb_cell} cells), {dt:.2f} s",
-            "max_rel_diff_vs_gpu": err, "max_diff_over_row_max": err_row}
+            "bit_exact_vs_gpu": bool(np.array_equal(gpu, v)),
+            "entries_differing_from_gpu": int(np.count_nonzero(gpu != v)),
+            "max_rel_diff_vs_gpu": guard_error(gpu, v, rp, b)}, v
 
 
-def run_solve(args, ctx, mesh, fmt):
+def cpu_plan_baselines(name, mesh, fmt, lam, mu, budget_s=5.0):
+    """The CPU baselines of the plan beside the all-core node-wise assembly:
+    B1 the reference's DOK assembly (ordered map, zeros skipped; Poisson only),
+    1 core, on the first cells that fit the budget, scaled to the whole mesh;
+    B2 the node-wise assembly on 1 core; B5 the sparsity build, node-wise on
+    all cores and edge-sort on 1 core."""
+    from oracle import oracle as O
+
+    w = WORKLOADS[name]
+    b = w["nb_dof"]
+    nnz = fmt.nnzb * b * b
+    threads = O.max_threads()
+    ptr, nc = fmt.nc_ptr.cpu().numpy(), fmt.nc_cell.cpu().numpy()
+    rp, cols = fmt.row_ptr.cpu().numpy(), fmt.cols.cpu().numpy()
+    out = {}
+    if b == 1 and w.get("cell") != "hex":
+        kind = oracle_kind(name)
+        probe = min(mesh.nb_cell, 20000)
+        t0 = time.perf_counter()
+        O.assemble_dok(kind, mesh.nb_node, mesh.coords, mesh.cells, nb_cell=probe)
+        per_cell = (time.perf_counter() - t0) / probe
+        sample = int(min(mesh.nb_cell, max(probe, budget_s / max(per_cell, 1e-9))))
+        t0 = time.perf_counter()
+        O.assemble_dok(kind, mesh.nb_node, mesh.coords, mesh.cells, nb_cell=sample)
+        dt = time.perf_counter() - t0
+        est = dt * mesh.nb_cell / sample
+        out["B1_dok_1core"] = {"value": nnz / est, "unit": UNIT, "cores": 1, "kind": "port",
+                               "estimated_full_s": est,
+                               "sample": f"the first {sample} of {mesh.nb_cell} cells into the ordered map, {dt:.2f} s, "
+                                         "scaled by the cell count"}
+    t0 = time.perf_counter()
+    O.assemble(oracle_kind(name), mesh.coords, mesh.cells, ptr, nc, rp, cols, lam=lam, mu=mu, nb_threads=1)
+    dt = time.perf_counter() - t0
+    out["B2_nodewise_1core"] = {"value": nnz / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"one full values assembly, {dt:.2f} s"}
+    if b == 1:
+        t0 = time.perf_counter()
+        O.sparsity_nodewise(mesh.nb_node, mesh.cells, ptr, nc, nb_threads=threads)
+        t_nw = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.sparsity(mesh.nb_node, mesh.cells)
+        t_es = time.perf_counter() - t0
+        out["B5_sparsity"] = {"nodewise_all_cores_ms": t_nw * 1e3, "cores": threads,
+                              "edge_sort_1core_ms": t_es * 1e3, "kind": "port",
+                              "gpu_structure_ms_once": None}
+    return out
+
+
+def run_solve(args, name, ctx, mesh, fmt):
     """Time to the target relative residual on the assembled system (RowColumn
     elimination Dirichlet, source / body force), FP64 CG and mixed precision."""
     import torch
 
     from arcanefem_gb300 import fem
 
-    w = WORKLOADS[args.workload]
+    w = WORKLOADS[name]
     nd = mesh.nb_node * w["nb_dof"]
     nodes = torch.as_tensor(mesh.groups[w["dirichlet"]], device="cuda")
     res = {"target_relres": w["rtol"], "dirichlet": f"row-column elimination on {w['dirichlet']}"}
@@ -521,9 +713,14 @@ def cpu_solve_baseline(fmt, ls, gpu_iterations, rtol, cap=300, budget_s=20.0):
     _, it, rel = O.pcg_jacobi(rp, cols, vals, b, rtol=1e-300, max_iter=iters, nb_threads=threads)
     dt = time.perf_counter() - t0
     per_it = dt / max(it, 1)
+    t0 = time.perf_counter()
+    _, it1, _ = O.pcg_jacobi(rp, cols, vals, b, rtol=1e-300, max_iter=min(iters, 50), nb_threads=1)
+    per_it1 = (time.perf_counter() - t0) / max(it1, 1)
     out = {"ms_per_iteration": per_it * 1e3, "iterations_sampled": it, "cores": threads, "kind": "port",
            "estimated_solve_ms": per_it * gpu_iterations * 1e3,
-           "sample": f"{it} Jacobi-PCG iterations on the same system, {dt:.2f} s"}
+           "sample": f"{it} Jacobi-PCG iterations on the same system, {dt:.2f} s",
+           "B4_1core": {"ms_per_iteration": per_it1 * 1e3, "estimated_solve_ms": per_it1 * gpu_iterations * 1e3,
+                        "cores": 1, "sample": f"{it1} iterations"}}
     x_oracle = None
     if per_it * gpu_iterations <= budget_s:
         t0 = time.perf_counter()
@@ -670,7 +867,8 @@ def run_batched(args):
         "refinements_max": max(r.refinements for r in res),
         "team_finish_ms": {"min": min(fin), "median": float(np.median(fin)), "max": max(fin)},
         "config": {**cfg.as_dict(), "grid_ctas": grid, "rebalanced": tune["config"].get("weights") is not None,
-                   "from_cache": tune["cached"]},
+                   "from_cache": tune["cached"],
+                   "team_finish_spread_ms": tune["config"].get("team_finish_spread")},
         "autotune_s": tune_s, "setup_s": setup_s,
         "single_system_fp64_cg_ms_one_rhs": single_ms,
         "speedup_vs_single_system_4_rhs": 4 * single_ms / ms,
@@ -691,13 +889,13 @@ def run_reference(args):
     from oracle import oracle as O
 
     w = WORKLOADS[args.workload]
-    mesh = make_mesh(args)
+    mesh = make_mesh(args.workload, args.n, args.seed)
     ptr, nc, _ = O.node_cell(mesh.nb_node, mesh.cells)
     rp, cols = O.sparsity(mesh.nb_node, mesh.cells)
     nnz = int(rp[-1]) * w["nb_dof"] ** 2
     lam, mu = fem.lame(w["E"], w["nu"]) if w["nb_dof"] == 3 else (0.0, 0.0)
     threads = O.max_threads()
-    kind = oracle_kind(args)
+    kind = oracle_kind(args.workload)
     for _ in range(args.warmup):
         O.assemble(kind, mesh.coords, mesh.cells, ptr, nc, rp, cols, lam=lam, mu=mu, nb_threads=threads)
     times = []
@@ -710,7 +908,7 @@ def run_reference(args):
     out = {"metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered mesh)",
-           "config": config(args, 1), "impl": "reference",
+           "config": config(args.workload, args.n, args.seed, 1), "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": f"full values assembly of the same mesh per step ({mesh.nb_cell} cells)"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -274,7 +274,10 @@ afem_status afem_assemble_host_io(afem_context ctx, const afem_mesh_view* mesh, 
  * array's device address (cudaGetSymbolAddress) for that device: make that
  * first call before any stream capture.  All calls share the one array, so
  * calls that can overlap on the GPU (different streams, or different host
- * threads without ordering) race and must be serialised by the caller. */
+ * threads without ordering) race and must be serialised by the caller.  The
+ * stream's device must be the current device (AFEM_ERR_BAD_ARG otherwise).
+ * Element arithmetic: AFEM_FORMULATION_REFERENCE; no context, hence no
+ * degenerate-cell status. */
 afem_status afem_assemble_poisson_p1_noalloc(void* cuda_stream, const afem_mesh_view* mesh,
                                              const int32_t* row_ptr_d, const double* cell_coeff_d,
                                              double* values_d);
@@ -450,7 +453,13 @@ afem_status afem_cg_solve_csr(afem_context ctx, int n, const int32_t* row_ptr_d,
 
 /* IDoFLinearSystemImpl::solve: solves the linear system's matrix view for
  * its rhs into its solution variable (applyLinearSystemTransformationAndSolve
- * calls the two transformations first, femutils/DoFLinearSystem.cc:487-493). */
+ * calls the two transformations first, femutils/DoFLinearSystem.cc:487-493).
+ * opt->precond = AFEM_PRECOND_LEARNED runs the flexible CG with the network
+ * attached by afem_ls_set_learned_preconditioner (its operator is refreshed
+ * from the system's matrix whenever the values changed since its last use);
+ * the other preconditioners run the CG of afem_cg_solve_csr.  Failure
+ * statuses (AFEM_ERR_NOT_CONVERGED with the last iterate in the solution,
+ * AFEM_ERR_BREAKDOWN) fill *info too. */
 afem_status afem_ls_solve(afem_linear_system ls, const afem_solver_options* opt, afem_solve_info* info);
 
 /* y = A x, FP64 CSR. */
@@ -543,6 +552,14 @@ afem_status afem_tc_weight_grad(afem_context ctx, int64_t M, const void* X1_d, c
 afem_status afem_fcg_solve(afem_context ctx, int n, const int32_t* row_ptr_d, const int32_t* cols_d,
                            const double* values_d, const double* b_d, double* x_d, afem_mpnn net,
                            const afem_solver_options* opt, afem_solve_info* info);
+
+/* precond = learned of the linear-system service: the network whose
+ * level-0 graph is this system's matrix pattern (afem_mpnn_create with the
+ * system's row_ptr / cols, on the same context), used by afem_ls_solve when
+ * opt->precond = AFEM_PRECOND_LEARNED (NULL detaches it).  The system does
+ * not own it.  No reference counterpart (the reference hands the solve to
+ * HYPRE / PETSc / Aleph, femutils/HypreDoFLinearSystem.cc:596-751). */
+afem_status afem_ls_set_learned_preconditioner(afem_linear_system ls, afem_mpnn net);
 
 /* ---------------------------------------------------------------------- */
 /* Batched 2D Poisson P1: many independent instances (the Poisson module's

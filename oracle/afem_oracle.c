@@ -139,6 +139,64 @@ int64_t afo_sparsity(int nb_node, int nb_cell, int npc, const int32_t* cell_node
   return nnz;
 }
 
+/* Node-wise sparsity for the all-core CPU baseline: rows in parallel, each
+ * the sorted distinct nodes of the row node's incident cells (self included),
+ * the atomic-free construction of femutils/BSRFormat.cc:445-557 with
+ * ascending columns.  Two passes (lengths, then columns) around a scan. */
+static int row_candidates(int node, int npc, const int32_t* cell_nodes, const int32_t* nc_ptr,
+                          const int32_t* nc_cell, int32_t* buf) {
+  int m = 0;
+  for (int32_t p = nc_ptr[node]; p < nc_ptr[node + 1]; ++p) {
+    const int32_t* cn = cell_nodes + (int64_t)nc_cell[p] * npc;
+    for (int j = 0; j < npc; ++j) buf[m++] = cn[j];
+  }
+  buf[m++] = node;   /* a node in no cell keeps its diagonal */
+  qsort(buf, (size_t)m, sizeof(int32_t), cmp_i32);
+  int u = 0;
+  for (int k = 0; k < m; ++k)
+    if (k == 0 || buf[k] != buf[k - 1]) buf[u++] = buf[k];
+  return u;
+}
+
+int64_t afo_sparsity_nodewise(int nb_node, int npc, const int32_t* cell_nodes, const int32_t* nc_ptr,
+                              const int32_t* nc_cell, int32_t* row_ptr, int32_t* cols, int64_t cap,
+                              int nb_threads) {
+  int maxdeg = 0;
+  for (int i = 0; i < nb_node; ++i)
+    if (nc_ptr[i + 1] - nc_ptr[i] > maxdeg) maxdeg = nc_ptr[i + 1] - nc_ptr[i];
+  const size_t bufsz = (size_t)maxdeg * npc + 1;
+  if (nb_threads < 1) nb_threads = 1;
+  row_ptr[0] = 0;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nb_threads)
+#endif
+  {
+    int32_t* buf = (int32_t*)malloc(sizeof(int32_t) * bufsz);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (int i = 0; i < nb_node; ++i) row_ptr[i + 1] = row_candidates(i, npc, cell_nodes, nc_ptr, nc_cell, buf);
+    free(buf);
+  }
+  for (int i = 0; i < nb_node; ++i) row_ptr[i + 1] += row_ptr[i];
+  if (row_ptr[nb_node] > cap) return -1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nb_threads)
+#endif
+  {
+    int32_t* buf = (int32_t*)malloc(sizeof(int32_t) * bufsz);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (int i = 0; i < nb_node; ++i) {
+      const int u = row_candidates(i, npc, cell_nodes, nc_ptr, nc_cell, buf);
+      memcpy(cols + row_ptr[i], buf, sizeof(int32_t) * (size_t)u);
+    }
+    free(buf);
+  }
+  return row_ptr[nb_node];
+}
+
 /* ------------------------------------------------------------------------ */
 /* Geometry (femutils/ArcaneFemFunctionsGpu.h)                               */
 /* ------------------------------------------------------------------------ */

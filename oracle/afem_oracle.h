@@ -123,6 +123,16 @@ int afo_pcg_jacobi(int n, const int32_t* row_ptr, const int32_t* cols, const dou
 double afo_wtime(void);
 int afo_max_threads(void);
 
+/* CPU baselines (afem_oracle_dok.cc, afem_oracle.c): the reference's DOK
+ * assembly (ordered map, zeros skipped) of cells [0, nb_cell), Poisson P1;
+ * returns the stored entries or -1 when cap is too small.  And the node-wise
+ * sparsity on nb_threads threads (ascending columns): per node, the nodes of
+ * its incident cells, sorted and deduplicated; returns nnz or -1 (cap). */
+int64_t afo_assemble_dok(int kind, int nb_node, int nb_cell, const double* coords, const int32_t* cell_nodes,
+                         int32_t* row_ptr, int32_t* cols, double* values, int64_t cap);
+int64_t afo_sparsity_nodewise(int nb_node, int npc, const int32_t* cell_nodes, const int32_t* nc_ptr,
+                              const int32_t* nc_cell, int32_t* row_ptr, int32_t* cols, int64_t cap, int nb_threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -75,6 +75,10 @@ def _declare(L):
     L.afo_spmv.restype = None
     L.afo_pcg_jacobi.argtypes = [C.c_int, _P, _P, _P, _P, _P, C.c_double, C.c_int, _P, _P, C.c_int]
     L.afo_pcg_jacobi.restype = C.c_int
+    L.afo_assemble_dok.argtypes = [C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int64]
+    L.afo_assemble_dok.restype = C.c_int64
+    L.afo_sparsity_nodewise.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int64, C.c_int]
+    L.afo_sparsity_nodewise.restype = C.c_int64
     L.afo_wtime.argtypes = []
     L.afo_wtime.restype = C.c_double
     L.afo_max_threads.argtypes = []
@@ -233,6 +237,33 @@ def pcg_jacobi(row_ptr, cols, values, b, rtol=1e-12, max_iter=100000, x0=None, n
                               _p(_c(b, np.float64)), _p(x), rtol, max_iter, _p(skip), C.byref(relres),
                               int(nb_threads))
     return x, int(it), float(relres.value)
+
+
+def assemble_dok(kind, nb_node, coords, cell_nodes, nb_cell=None):
+    """The reference's DOK assembly (ordered (row, col) map, zeros skipped) of
+    the first nb_cell cells, as CSR (row_ptr, cols, values).  Poisson P1."""
+    cn = _c(cell_nodes, np.int32)
+    nc = cn.shape[0] if nb_cell is None else int(nb_cell)
+    cap = nc * cn.shape[1] ** 2
+    rp = np.zeros(nb_node + 1, np.int32)
+    cols = np.zeros(max(cap, 1), np.int32)
+    vals = np.zeros(max(cap, 1))
+    nnz = lib().afo_assemble_dok(kind, nb_node, nc, _p(_c(coords, np.float64)), _p(cn), _p(rp), _p(cols), _p(vals),
+                                 cap)
+    assert nnz >= 0
+    return rp, cols[:nnz].copy(), vals[:nnz].copy()
+
+
+def sparsity_nodewise(nb_node, cell_nodes, nc_ptr, nc_cell, nb_threads=1):
+    """Node-wise sparsity (ascending columns) on nb_threads threads."""
+    cn = _c(cell_nodes, np.int32)
+    rp = np.zeros(nb_node + 1, np.int32)
+    cap = int(np.diff(nc_ptr).sum()) * cn.shape[1] + nb_node
+    cols = np.zeros(cap, np.int32)
+    nnz = lib().afo_sparsity_nodewise(nb_node, cn.shape[1], _p(cn), _p(_c(nc_ptr, np.int32)),
+                                      _p(_c(nc_cell, np.int32)), _p(rp), _p(cols), cap, int(nb_threads))
+    assert nnz >= 0
+    return rp, cols[:nnz].copy()
 
 
 def wtime() -> float:

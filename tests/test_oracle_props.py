@@ -178,3 +178,26 @@ def test_q1_source_integrates_the_domain(dim):
     ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
     r = O.rhs_constant_source_q1(dim, m.coords, m.cells, ptr, nc, 2.5)
     assert abs(r.sum() - 2.5) < 1e-12
+
+
+def test_cpu_baselines_compute_the_same_matrix():
+    """The timed CPU baselines are the same computation: the DOK assembly
+    (ordered map, zeros skipped) gives the node-wise matrix to rounding, and the
+    all-core node-wise sparsity equals the edge-sort sparsity."""
+    from arcanefem_gb300 import meshgen
+    for m, kind in ((meshgen.unit_square_tri(9, seed=3), O.POISSON_TRI3), (meshgen.unit_cube_tet(4, seed=3),
+                                                                           O.POISSON_TET4)):
+        ptr, nc, _ = O.node_cell(m.nb_node, m.cells)
+        rp, cols = O.sparsity(m.nb_node, m.cells)
+        ref = O.assemble(kind, m.coords, m.cells, ptr, nc, rp, cols)
+        drp, dcols, dvals = O.assemble_dok(kind, m.nb_node, m.coords, m.cells)
+        full = np.zeros(cols.size)
+        row = np.repeat(np.arange(m.nb_node), np.diff(drp))
+        for r, c, v in zip(row, dcols, dvals):
+            k = rp[r] + int(np.searchsorted(cols[rp[r]:rp[r + 1]], c))
+            assert cols[k] == c
+            full[k] = v
+        assert np.allclose(full, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
+        for t in (1, 4):
+            nrp, ncols = O.sparsity_nodewise(m.nb_node, m.cells, ptr, nc, nb_threads=t)
+            assert np.array_equal(nrp, rp) and np.array_equal(ncols, cols)
