@@ -76,4 +76,7 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ARCANEFEM_REFERENCE")
+    if not root:
+        sys.exit("usage: make_fixtures.py <reference source tree>  (or set ARCANEFEM_REFERENCE)")
+    main(root)

@@ -11,7 +11,8 @@ import pytest
 
 from arcanefem_gb300 import meshgen, meshio
 
-REF = "/root/reference/meshes/msh"
+# the reference source tree, when a checkout is at hand: ARCANEFEM_REFERENCE=<tree>
+REF = os.path.join(os.environ.get("ARCANEFEM_REFERENCE", ""), "meshes", "msh")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -30,7 +31,8 @@ def test_msh_round_trip(tmp_path, make):
     assert np.array_equal(d.node_tags, np.arange(1, m.nb_node + 1))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference meshes not present")
+@pytest.mark.skipif(not os.environ.get("ARCANEFEM_REFERENCE") or not os.path.isdir(REF),
+                    reason="ARCANEFEM_REFERENCE does not name a reference tree with meshes/msh")
 @pytest.mark.parametrize("name,fixture", [("L-shape.msh", "testlab_lshape_2d.npz"),
                                           ("circle_cut.msh", "poisson_circle_2d.npz"),
                                           ("bar_dynamic_3D.msh", "elasticity_bar_3d.npz")])
