@@ -9,16 +9,19 @@
 //   their order, so the output is deterministic.
 //
 // node -> node sparsity (rows of the assembled matrix):
-//   one warp per node inserts the nodes of its incident cells into a hash
-//   table in shared memory; the number of distinct values is the row length
-//   = 1 + number of neighbours (femutils/BSRFormat.cc:445-557, row = deg + 1).
-//   The second pass sorts the distinct values and writes the columns
-//   (ascending or self-last) and, for every cell-node incidence, its position
-//   in the row (the slot map used by the assembly kernels).  Rows too long
-//   for the table path extract their distinct values in increasing order by
-//   warp-wide minima instead.
+//   one warp per node, one lane per incidence (chunks of 32): the nodes of
+//   the node's incident cells go into a hash set in shared memory; the
+//   number of distinct values is the row length = 1 + number of neighbours
+//   (femutils/BSRFormat.cc:445-557, row = deg + 1).  The second pass builds
+//   the same set, ranks each neighbour by counting the smaller ones in the
+//   set (broadcast reads, no sort), writes the columns (ascending or
+//   self-last) and, for every cell-node incidence, its position in the row
+//   (the slot map used by the assembly kernels) in one packed store.  Rows
+//   may hold up to 255 entries (the slot map is uint8); longer rows are
+//   reported as mesh errors.
 #include <algorithm>
 #include <climits>
+#include <type_traits>
 
 #include "afem_internal.cuh"
 
@@ -106,235 +109,361 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_nc_sort(int nb_node, in
 // ---------------------------------------------------------------------------
 // node -> node
 
-constexpr int kRowCap = 512;        // candidates per node (deg * npc), e.g. 128 tetrahedra
-constexpr int kMaxRowLen = 255;     // slot map entries are uint8
+constexpr int kMaxRowLen = 255;   // slot map entries are uint8
+constexpr int kTabSlots = 256;    // hash table entries per warp: every distinct neighbour of a row fits
 
-// One warp per node.  The candidates (the nodes of the node's incident
-// cells, m = deg * npc of them) are held in registers, R per lane (candidate
-// i in lane i % 32, register i / 32), with, for the column pass, the slot-map
-// index of each: k * npc + q for candidate i = cell node j of incidence
-// k = i / npc, q = 0 for the row's own node (local index li) and q = 1.. for
-// the other cell nodes in increasing local index -- the order of the element
-// rows.  The distinct candidates come out in increasing order, one warp-wide
-// minimum per distinct value; the sweep that finds value t + 1 also writes
-// the slot bytes of value t, so each distinct value costs one sweep of R
-// registers.  Returns the row length; with `fill`, writes the columns
-// (ascending or self-last) at cols[0..len) and the slot map.
-template <int R, bool FILL>
-__device__ __forceinline__ int row_select(int n, int npc, int m, const int32_t* __restrict__ cn,
-                                          const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ local,
-                                          int len, int self_last, int32_t* __restrict__ cols,
-                                          uint8_t* __restrict__ slot) {
-  const int lane = threadIdx.x & 31;
-  int32_t v[R];
-  int16_t si[R];
+__device__ __forceinline__ int tab_hash(int32_t v) { return (int)(((uint32_t)v * 2654435761u) >> 24); }
+
+// Per-warp tables in shared memory.  key: open-addressing hash set of the
+// row's neighbours (-1 = empty; linear probing); at: the table slot of each
+// distinct neighbour in order of first insertion (for the ranks and to clear
+// the table afterwards); val: the neighbours in that order, padded with
+// INT_MAX for the 4-wide rank loop; pos: the position in the row of the
+// neighbour held in each table slot.
+struct RowTables {
+  int32_t* key;
+  int16_t* at;
+  int32_t* val;
+  uint8_t* pos;
+};
+
+// The incidences of node n in chunks of 32, one per lane: the lane holds its
+// cell's NPC nodes, of which local index li is n itself (read with the slot
+// map only).
+template <int NPC, bool LOCAL>
+__device__ __forceinline__ bool load_incidence(const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_cell,
+                                               const uint8_t* __restrict__ nc_local, int k, int deg, int32_t (&v)[NPC],
+                                               int& li) {
+  if (k >= deg) return false;
+  const int64_t c = __ldg(nc_cell + k);
+  if (LOCAL) li = __ldg(nc_local + k);
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int i = r * 32 + lane;
-    v[r] = INT_MAX;
-    si[r] = 0;
-    if (i < m) {
-      const int k = i / npc, j = i - k * npc;
-      v[r] = __ldg(cn + (int64_t)__ldg(nc_cell + k) * npc + j);
-      if (FILL) {
-        const int li = __ldg(local + k);
-        si[r] = (int16_t)(k * npc + (j == li ? 0 : (j < li ? j + 1 : j)));
-      }
-    }
-  }
-  int32_t last = INT_MIN;
-  int pos_last = -1, it = 0;
-  for (;;) {
-    int32_t loc = INT_MAX;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      if (FILL && v[r] == last && pos_last >= 0) slot[si[r]] = (uint8_t)pos_last;
-      if (v[r] > last && v[r] < loc) loc = v[r];
-    }
-    const int32_t mn = __reduce_min_sync(0xffffffffu, loc);
-    if (mn == INT_MAX) break;
-    if (FILL) {
-      const int pos = self_last ? (mn < n ? it : (mn == n ? len - 1 : it - 1)) : it;
-      // a row_ptr that disagrees is reported by the caller, not written past
-      pos_last = (pos >= 0 && pos < len) ? pos : -1;
-      if (lane == 0 && pos_last >= 0) cols[pos_last] = mn;
-    }
-    last = mn;
-    ++it;
-  }
-  return it;
+  for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
+  return true;
 }
 
-// Fast path for rows of at most kHashRow candidates and 32 distinct columns
-// (every interior row of a tetrahedral, triangular or hexahedral mesh): each
-// candidate is inserted once into a per-warp open-addressing table in shared
-// memory (atomicCAS, linear probing), so the row length is the number of
-// first insertions -- one pass over the candidates instead of one sweep per
-// distinct value.  The column pass compacts the first insertions (ballot
-// prefix) into a list, sorts it (one value per lane, a 32-key bitonic network
-// on shuffles), records each value's position in the row in its table entry,
-// and every candidate reads its slot byte from there.  Rows with more
-// candidates, and column passes with more than 32 distinct values, take
-// row_select.  Returns the row length, or -1 when the row needs row_select.
-constexpr int kHashRow = 128;      // candidates per row on the fast path (R = 4)
-constexpr int kHashSlots = 256;    // table entries per warp (load factor <= 1/8 for 32 distinct values)
+// Inserts v; returns its table slot (fresh: first insertion), or -1 when
+// the table is full.
+__device__ __forceinline__ int tab_insert(int32_t* key, int32_t v, bool& fresh) {
+  int h = tab_hash(v);
+  for (int p = 0; p < kTabSlots; ++p, h = (h + 1) & (kTabSlots - 1)) {
+    const int32_t old = atomicCAS(key + h, -1, v);
+    if (old == -1) {
+      fresh = true;
+      return h;
+    }
+    if (old == v) return h;
+  }
+  return -1;
+}
 
-__device__ __forceinline__ uint32_t hash_slot(int32_t v) { return ((uint32_t)v * 2654435761u) >> 24; }
+// v[j] for a run-time j in [0, NPC), by selects (no local-memory array)
+template <int NPC>
+__device__ __forceinline__ int32_t pick(const int32_t (&v)[NPC], int j) {
+  int32_t x = v[0];
+#pragma unroll
+  for (int q = 1; q < NPC; ++q)
+    if (j == q) x = v[q];
+  return x;
+}
 
-template <bool FILL>
-__device__ __forceinline__ int row_hash(int n, int npc, int m, const int32_t* __restrict__ cn,
-                                        const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ local,
-                                        int len, int self_last, int32_t* __restrict__ cols,
-                                        uint8_t* __restrict__ slot, int32_t* __restrict__ key,
-                                        uint8_t* __restrict__ rank, uint64_t* __restrict__ list) {
-  constexpr int R = kHashRow / 32;
+__device__ __forceinline__ int tab_find(const int32_t* key, int32_t v) {
+  int h = tab_hash(v);
+  for (int p = 0; p < kTabSlots; ++p, h = (h + 1) & (kTabSlots - 1))
+    if (key[h] == v) return h;
+  return 0;   // not reached: every neighbour was inserted
+}
+
+// One thread per node.  Its hash set of neighbours lives in shared memory,
+// interleaved across the block's threads (slot h of thread t at key[h][t]),
+// so that the 32 probes of a warp fall in 32 distinct banks whatever their
+// slots.  The thread streams its node's incidences in increasing order and
+// inserts the nodes other than n of each cell: the number of first insertions
+// D is the number of distinct neighbours and the row holds D + 1 entries (the
+// node itself included, as the reference's deg + 1 rows,
+// femutils/BSRFormat.cc:445-557).  With FILL the row is then written: the
+// rank of each neighbour among the others (counted against the thread's list
+// of them; no sort) gives its column position in either order, and every
+// incidence writes its NPC slot bytes (its own column first, then the other
+// cell nodes in increasing local index) in one packed store.  A row with more
+// neighbours than the table's 3/4 is appended to `defer` for
+// k_sparsity_rows_warp.
+// Errors: bit 2 a row of more than kMaxRowLen entries, bit 4 a row_ptr that
+// does not match, bit 8 a node id out of range.
+constexpr int kThreadBlock = 128;
+// Nodes in more cells than this go to k_sparsity_rows_warp, whose lanes then
+// stay at least half busy (tetrahedral meshes: about 24 cells per node);
+// lower degrees (triangles, hexahedra, boundary nodes) stay here.
+constexpr int kThreadMaxDeg = 16;
+
+template <int NPC>
+struct ThreadTable {
+  static constexpr int slots = NPC == 8 ? 64 : 32;   // power of two
+  static constexpr int max_d = slots * 3 / 4;        // load factor at most 3/4
+};
+
+__device__ __forceinline__ void defer_node(int n, int32_t* defer, int32_t* defer_count) {
+  defer[atomicAdd(defer_count, 1)] = n;
+}
+
+template <int NPC, bool FILL>
+__global__ void __launch_bounds__(kThreadBlock)
+    k_sparsity_thread(int nb_node, const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_ptr,
+                      const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ nc_local,
+                      const int32_t* __restrict__ row_ptr, int self_last, int packed_slots,
+                      int32_t* __restrict__ row_len, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
+                      int32_t* __restrict__ defer, int32_t* __restrict__ defer_count, int* __restrict__ err) {
+  constexpr int TS = ThreadTable<NPC>::slots, DMAX = ThreadTable<NPC>::max_d;
+  __shared__ int32_t s_key[TS][kThreadBlock];
+  __shared__ int32_t s_val[FILL ? DMAX : 1][kThreadBlock];   // the neighbours in order of insertion
+  __shared__ uint8_t s_at[FILL ? DMAX : 1][kThreadBlock];    // their table slots
+  __shared__ uint8_t s_pos[FILL ? TS : 1][kThreadBlock];     // position in the row, by table slot
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int h = 0; h < TS; ++h) s_key[h][t] = -1;
+  for (int n = blockIdx.x * kThreadBlock + t; n < nb_node; n += gridDim.x * kThreadBlock) {
+    const int32_t b = __ldg(nc_ptr + n), e = __ldg(nc_ptr + n + 1);
+    if (e - b > kThreadMaxDeg) continue;   // k_sparsity_rows_warp's
+    int D = 0;
+    bool over = false, bad = false;
+    for (int32_t p = b; p < e && !over; ++p) {
+      const int64_t c = __ldg(nc_cell + p);
+      int32_t v[NPC];
+#pragma unroll
+      for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
+#pragma unroll
+      for (int j = 0; j < NPC; ++j) {
+        const int32_t x = v[j];
+        if (x == n || over) continue;
+        if ((unsigned)x >= (unsigned)nb_node) {
+          bad = true;
+          continue;
+        }
+        int h = tab_hash(x) & (TS - 1);
+#pragma unroll 1
+        for (int q = 0; q < TS; ++q, h = (h + 1) & (TS - 1)) {
+          const int32_t k = s_key[h][t];
+          if (k == x) break;
+          if (k == -1) {
+            if (D == DMAX) {
+              over = true;
+              break;
+            }
+            s_key[h][t] = x;
+            if (FILL) {
+              s_val[D][t] = x;
+              s_at[D][t] = (uint8_t)h;
+            }
+            ++D;
+            break;
+          }
+        }
+      }
+    }
+    if (bad) {
+      atomicOr(err, 8);
+      if (!FILL) row_len[n] = 0;
+    } else if (over) {
+      defer_node(n, defer, defer_count);
+    } else if (!FILL) {
+      row_len[n] = D + 1;
+    } else {
+      const int32_t rb = __ldg(row_ptr + n);
+      if (__ldg(row_ptr + n + 1) - rb != D + 1) {
+        atomicOr(err, 4);
+      } else {
+        int own = 0;   // neighbours below n
+        for (int i = 0; i < D; ++i) {
+          const int32_t x = s_val[i][t];
+          int r = 0;
+          for (int u = 0; u < D; ++u) r += s_val[u][t] < x;
+          const int pos = self_last ? r : r + (n < x);
+          cols[rb + pos] = x;
+          s_pos[s_at[i][t]][t] = (uint8_t)pos;
+          own += x < n;
+        }
+        const int pn = self_last ? D : own;
+        cols[rb + pn] = n;
+        for (int32_t p = b; p < e; ++p) {
+          const int64_t c = __ldg(nc_cell + p);
+          const int li = __ldg(nc_local + p);
+          using Word = typename std::conditional<(NPC > 4), uint64_t, uint32_t>::type;
+          Word word = (Word)pn;
+#pragma unroll
+          for (int j = 0; j < NPC; ++j) {
+            if (j == li) continue;
+            const int32_t x = __ldg(cn + c * NPC + j);
+            Word q = (Word)pn;
+            if (x != n) {
+              int h = tab_hash(x) & (TS - 1);
+#pragma unroll 1
+              for (int k = 0; k < TS && s_key[h][t] != x; ++k) h = (h + 1) & (TS - 1);
+              q = (Word)s_pos[h][t];
+            }
+            word |= q << (8 * (j < li ? j + 1 : j));
+          }
+          uint8_t* dst = slot + (int64_t)p * NPC;
+          if (NPC == 4 && packed_slots) {
+            *reinterpret_cast<uint32_t*>(dst) = (uint32_t)word;
+          } else if (NPC == 8 && packed_slots) {
+            *reinterpret_cast<uint2*>(dst) = make_uint2((uint32_t)word, (uint32_t)((uint64_t)word >> 32));
+          } else {
+#pragma unroll
+            for (int q = 0; q < NPC; ++q) dst[q] = (uint8_t)((uint64_t)word >> (8 * q));
+          }
+        }
+      }
+    }
+    // empty the table for the next node
+#pragma unroll
+    for (int h = 0; h < TS; ++h) s_key[h][t] = -1;
+  }
+}
+
+// The nodes in more than kThreadMaxDeg cells, and the rows k_sparsity_thread
+// deferred (more distinct neighbours than its per-thread table holds), listed
+// in `list[0 .. *list_count)`: one warp per node, lanes over its incidences
+// (chunks of 32), the nodes other than n of each incident cell inserted into
+// the warp's hash set.  Round r inserts, in every lane, the cell node r + 1
+// places after the lane's own, so that the lanes of one atomic rarely target
+// the same table slot (cells around a node share nodes at equal local
+// indices) and the own node takes no round.  The number
+// of first insertions D is the number of distinct neighbours and the row
+// holds D + 1 entries.  With FILL the row is then written: the rank of each
+// neighbour among the others is counted against the list (broadcast reads of
+// shared memory; no sort), which gives its column position in either order,
+// and every incidence writes its NPC slot bytes in one packed store.  Errors
+// as k_sparsity_thread.
+template <int NPC, bool FILL>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    k_sparsity_rows_warp(int nb_node, const int32_t* __restrict__ list, const int32_t* __restrict__ list_count,
+                         const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_ptr,
+                         const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ nc_local,
+                         const int32_t* __restrict__ row_ptr, int self_last, int packed_slots,
+                         int32_t* __restrict__ row_len, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
+                         int* __restrict__ err) {
+  __shared__ int32_t s_key[kWarpsPerBlock][kTabSlots];
+  __shared__ int16_t s_at[kWarpsPerBlock][kTabSlots];
+  __shared__ __align__(16) int32_t s_val[kWarpsPerBlock][FILL ? kTabSlots + 4 : 1];
+  __shared__ uint8_t s_pos[kWarpsPerBlock][FILL ? kTabSlots : 1];
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
-#pragma unroll
-  for (int k = lane; k < kHashSlots; k += 32) key[k] = -1;
+  const int w = threadIdx.x >> 5;
+  RowTables t{s_key[w], s_at[w], s_val[w], s_pos[w]};
+  for (int i = lane; i < kTabSlots; i += 32) t.key[i] = -1;
   __syncwarp();
-  int16_t si[R];
-  int16_t hs[R];
-  int distinct = 0;   // uniform across the warp
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int i = r * 32 + lane;
-    si[r] = 0;
-    hs[r] = 0;
-    bool fresh = false;
-    int32_t v = -1;
-    if (i < m) {
-      const int k = i / npc, j = i - k * npc;
-      v = __ldg(cn + (int64_t)__ldg(nc_cell + k) * npc + j);
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int count = nb_node + *list_count;
+  for (int it = wid; it < count; it += nwarps) {
+    const int n = it < nb_node ? it : __ldg(list + (it - nb_node));
+    const int32_t b = __ldg(nc_ptr + n);
+    const int deg = __ldg(nc_ptr + n + 1) - b;
+    if (it < nb_node && deg <= kThreadMaxDeg) continue;   // k_sparsity_thread's
+    int32_t v[NPC];
+    int16_t hs[NPC - 1];   // table slot of each round's candidate (the last chunk's)
+    int me = 0;            // local index of n in the lane's cell
+    int li = 0;
+    bool act = false, bad_id = false, full = false;
+    int D = 0;   // distinct neighbours so far, uniform across the warp
+    for (int kb = 0; kb < deg || kb == 0; kb += 32) {
+      act = load_incidence<NPC, FILL>(cn, nc_cell + b, nc_local + b, kb + lane, deg, v, li);
       if (FILL) {
-        const int li = __ldg(local + k);
-        si[r] = (int16_t)(k * npc + (j == li ? 0 : (j < li ? j + 1 : j)));
+        me = li;
+      } else {
+        me = 0;
+#pragma unroll
+        for (int j = NPC - 1; j >= 0; --j)
+          if (v[j] == n) me = j;
       }
-      uint32_t h = hash_slot(v);
-      for (int probe = 0; probe < kHashSlots; ++probe, h = (h + 1) & (kHashSlots - 1)) {
-        const int32_t old = atomicCAS(key + h, -1, v);
-        if (old == -1) {
-          fresh = true;
-          break;
+#pragma unroll
+      for (int r = 0; r + 1 < NPC; ++r) {
+        int j = me + 1 + r;
+        j -= j >= NPC ? NPC : 0;
+        const int32_t x = pick<NPC>(v, j);
+        bool fresh = false;
+        int h = 0;
+        if (act && x != n) {
+          if ((unsigned)x >= (unsigned)nb_node) {
+            bad_id = true;
+          } else {
+            h = tab_insert(t.key, x, fresh);
+            full |= h < 0;
+          }
         }
-        if (old == v) break;
+        hs[r] = (int16_t)h;
+        const unsigned fb = __ballot_sync(0xffffffffu, fresh);
+        if (fresh) {
+          const int at = D + __popc(fb & below);   // < kTabSlots: each first insertion took a table slot
+          t.at[at] = (int16_t)h;
+          if (FILL) t.val[at] = x;
+        }
+        D += __popc(fb);
       }
-      hs[r] = (int16_t)h;
     }
-    const unsigned fb = __ballot_sync(0xffffffffu, fresh);
-    if (FILL && fresh) {
-      const int at = distinct + __popc(fb & below);
-      if (at < 32) list[at] = ((uint64_t)(uint32_t)v << 32) | (uint32_t)hs[r];
-    }
-    distinct += __popc(fb);
-  }
-  if (!FILL) return distinct;   // the table counts any number of distinct values
-  if (distinct > 32) return -1;
-  __syncwarp();
-  // the distinct values, one per lane, sorted by a 32-key bitonic network;
-  // each carries its table slot
-  uint64_t kv = lane < distinct ? list[lane] : ~uint64_t(0);
+    const bool bad = __any_sync(0xffffffffu, bad_id), overflow = __any_sync(0xffffffffu, full);
+    const int len = D + 1;
+    const bool too_long = overflow || len > kMaxRowLen;
+    __syncwarp();
+    if (!FILL) {
+      if (lane == 0) {
+        if (bad || too_long) atomicOr(err, bad ? 8 : 2);
+        row_len[n] = (bad || too_long) ? 0 : len;
+      }
+    } else {
+      const int32_t rb = __ldg(row_ptr + n);
+      const bool ok = !bad && !too_long && __ldg(row_ptr + n + 1) - rb == len;
+      if (lane == 0 && !ok) atomicOr(err, bad ? 8 : too_long ? 2 : 4);
+      if (ok) {
+        if (lane < 4) t.val[D + lane] = INT_MAX;
+        __syncwarp();
+        int own = 0;   // neighbours below n
+        for (int i = lane; i < D; i += 32) {
+          const int32_t x = t.val[i];
+          int r = 0;
+          for (int u = 0; u < D; u += 4) {
+            const int4 q = *reinterpret_cast<const int4*>(t.val + u);
+            r += (q.x < x) + (q.y < x) + (q.z < x) + (q.w < x);
+          }
+          const int p = self_last ? r : r + (n < x);
+          cols[rb + p] = x;
+          t.pos[t.at[i]] = (uint8_t)p;
+          own += x < n;
+        }
+        own = __reduce_add_sync(0xffffffffu, own);
+        const int pn = self_last ? D : own;
+        if (lane == 0) cols[rb + pn] = n;
+        __syncwarp();
+        for (int kb = 0; kb < deg; kb += 32) {
+          if (deg > 32) act = load_incidence<NPC, true>(cn, nc_cell + b, nc_local + b, kb + lane, deg, v, li);
+          if (!act) continue;
+          // slot byte q of the incidence at bits 8q: its own column, then the
+          // other cell nodes in increasing local index
+          using Word = typename std::conditional<(NPC > 4), uint64_t, uint32_t>::type;
+          Word word = (Word)pn;
 #pragma unroll
-  for (int k = 2; k <= 32; k <<= 1) {
+          for (int r = 0; r + 1 < NPC; ++r) {
+            int j = li + 1 + r;
+            j -= j >= NPC ? NPC : 0;
+            const int32_t x = pick<NPC>(v, j);
+            const Word p = x == n ? (Word)pn : (Word)t.pos[deg > 32 ? tab_find(t.key, x) : hs[r]];
+            word |= p << (8 * (j < li ? j + 1 : j));
+          }
+          uint8_t* dst = slot + (int64_t)(b + kb + lane) * NPC;
+          if (NPC == 4 && packed_slots) {
+            *reinterpret_cast<uint32_t*>(dst) = (uint32_t)word;
+          } else if (NPC == 8 && packed_slots) {
+            *reinterpret_cast<uint2*>(dst) = make_uint2((uint32_t)word, (uint32_t)((uint64_t)word >> 32));
+          } else {
 #pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      const uint64_t o = __shfl_xor_sync(0xffffffffu, kv, j);
-      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
-      kv = keep_min ? (o < kv ? o : kv) : (o > kv ? o : kv);
-    }
-  }
-  // lane t < distinct now holds the t-th smallest column; a row_ptr that
-  // disagrees is reported by the caller, not written past
-  if (distinct == len) {
-    if (lane < distinct) {
-      const int32_t col = (int32_t)(kv >> 32);
-      // self-last: the neighbours keep their ascending order, the row's own node goes last
-      const int pos = !self_last ? lane : (col < n ? lane : (col == n ? len - 1 : lane - 1));
-      cols[pos] = col;
-      rank[(uint32_t)kv & 0xffffu] = (uint8_t)pos;
+            for (int q = 0; q < NPC; ++q) dst[q] = (uint8_t)((uint64_t)word >> (8 * q));
+          }
+        }
+      }
     }
     __syncwarp();
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-      if (r * 32 + lane < m) slot[si[r]] = rank[hs[r]];
-  }
-  __syncwarp();
-  return distinct;
-}
-
-template <bool FILL>
-__device__ __forceinline__ int row_dispatch(int n, int npc, int m, const int32_t* cn, const int32_t* nc_cell,
-                                            const uint8_t* local, int len, int self_last, int32_t* cols,
-                                            uint8_t* slot, int32_t* key, uint8_t* rank, uint64_t* list) {
-  if (m <= kHashRow) {
-    const int got = row_hash<FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot, key, rank, list);
-    if (got >= 0) return got;
-  }
-  if (m <= 32) return row_select<1, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
-  if (m <= 64) return row_select<2, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
-  if (m <= 128) return row_select<4, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
-  if (m <= 256) return row_select<8, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
-  return row_select<16, FILL>(n, npc, m, cn, nc_cell, local, len, self_last, cols, slot);
-}
-
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_len(int nb_node, int npc, const int32_t* __restrict__ cn,
-                                                                 const int32_t* __restrict__ nc_ptr,
-                                                                 const int32_t* __restrict__ nc_cell,
-                                                                 int32_t* __restrict__ row_len,
-                                                                 int* __restrict__ err) {
-  __shared__ int32_t tab_key[kWarpsPerBlock][kHashSlots];
-  const int lane = threadIdx.x & 31;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  int32_t* const key = tab_key[threadIdx.x >> 5];
-  for (int n = wid; n < nb_node; n += nwarps) {
-    const int32_t b = __ldg(nc_ptr + n);
-    const int m = (__ldg(nc_ptr + n + 1) - b) * npc;
-    // a node in no cell keeps its diagonal (the reference's rows hold deg + 1 entries)
-    int len = m > kRowCap ? -1
-              : m == 0    ? 1
-                          : row_dispatch<false>(n, npc, m, cn, nc_cell + b, nullptr, 0, 0, nullptr, nullptr, key,
-                                                nullptr, nullptr);
-    if (lane == 0) {
-      if (len < 0 || len > kMaxRowLen) {
-        atomicOr(err, 2);
-        len = 0;
-      }
-      row_len[n] = len;
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_row_fill(int nb_node, int npc, const int32_t* __restrict__ cn,
-                                                                  const int32_t* __restrict__ nc_ptr,
-                                                                  const int32_t* __restrict__ nc_cell,
-                                                                  const uint8_t* __restrict__ nc_local,
-                                                                  const int32_t* __restrict__ row_ptr, int self_last,
-                                                                  int32_t* __restrict__ cols,
-                                                                  uint8_t* __restrict__ slot, int* __restrict__ err) {
-  __shared__ int32_t tab_key[kWarpsPerBlock][kHashSlots];
-  __shared__ uint8_t tab_rank[kWarpsPerBlock][kHashSlots];
-  __shared__ uint64_t tab_list[kWarpsPerBlock][32];
-  const int lane = threadIdx.x & 31;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  int32_t* const key = tab_key[threadIdx.x >> 5];
-  uint8_t* const rank = tab_rank[threadIdx.x >> 5];
-  uint64_t* const list = tab_list[threadIdx.x >> 5];
-  for (int n = wid; n < nb_node; n += nwarps) {
-    const int32_t rb = __ldg(row_ptr + n);
-    const int len = __ldg(row_ptr + n + 1) - rb;
-    const int32_t b = __ldg(nc_ptr + n);
-    const int m = (__ldg(nc_ptr + n + 1) - b) * npc;
-    int got = -1;
-    if (m == 0) {   // a node in no cell: its diagonal only
-      got = 1;
-      if (lane == 0 && len == 1) cols[rb] = n;
-    } else if (m <= kRowCap) {
-      got = row_dispatch<true>(n, npc, m, cn, nc_cell + b, nc_local + b, len, self_last, cols + rb,
-                               slot + (int64_t)b * npc, key, rank, list);
-    }
-    if (lane == 0 && got != len) atomicOr(err, 4);
+    for (int i = lane; i < D && i < kTabSlots; i += 32) t.key[t.at[i]] = -1;
+    __syncwarp();
   }
 }
 
@@ -403,29 +532,90 @@ afem_status afem_node_cell_build(afem_context ctx, int nb_node, int nb_cell, int
   return AFEM_OK;
 }
 
+}  // extern "C"
+
+namespace afem {
+
+// Resident blocks of a kernel on one SM: the grid-stride kernels below are
+// launched with exactly that many blocks per SM, since a larger grid leaves
+// its last blocks to a second, mostly idle wave.
+template <typename Kernel>
+static int resident_blocks(Kernel k, int block) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, block, 0) != cudaSuccess) {
+    (void)cudaGetLastError();
+    b = 0;
+  }
+  return b > 0 ? b : 1;
+}
+
+template <int NPC, bool FILL>
+static afem_status launch_rows(afem_context ctx, int nb_node, const int32_t* cn, const int32_t* nc_ptr,
+                               const int32_t* nc_cell, const uint8_t* nc_local, const int32_t* row_ptr, int self_last,
+                               int packed, int32_t* row_len, int32_t* cols, uint8_t* slot, int32_t* defer,
+                               int32_t* defer_count, int* err) {
+  static const int per_sm_thread = resident_blocks(k_sparsity_thread<NPC, FILL>, kThreadBlock);
+  static const int per_sm_warp = resident_blocks(k_sparsity_rows_warp<NPC, FILL>, kWarpsPerBlock * 32);
+  const unsigned g1 = (unsigned)std::min<int64_t>((nb_node + kThreadBlock - 1) / kThreadBlock,
+                                                  (int64_t)ctx->sm_count * per_sm_thread);
+  AFEM_TRY(launch(ctx, k_sparsity_thread<NPC, FILL>, g1, kThreadBlock, 0, nb_node, cn, nc_ptr, nc_cell, nc_local,
+                  row_ptr, self_last, packed, row_len, cols, slot, defer, defer_count, err));
+  // the deferred long rows (usually none): the grid covers the worst case and
+  // each warp reads the list's length on the device
+  const unsigned g2 = (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock,
+                                                  (int64_t)ctx->sm_count * per_sm_warp);
+  return launch(ctx, k_sparsity_rows_warp<NPC, FILL>, g2, kWarpsPerBlock * 32, 0, nb_node, (const int32_t*)defer,
+                (const int32_t*)defer_count, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed, row_len, cols,
+                slot, err);
+}
+
+static afem_status launch_sparsity_rows(afem_context ctx, bool fill, int nb_node, int npc, const int32_t* cn,
+                                        const int32_t* nc_ptr, const int32_t* nc_cell, const uint8_t* nc_local,
+                                        const int32_t* row_ptr, int self_last, int32_t* row_len, int32_t* cols,
+                                        uint8_t* slot, int32_t* defer, int32_t* defer_count, int* err) {
+  // one packed store per incidence when the slot map is aligned to its rows
+  const int packed = (reinterpret_cast<uintptr_t>(slot) % (npc == 8 ? 8 : 4)) == 0;
+#define AFEM_ROWS_LAUNCH(NPC)                                                                                    \
+  return fill ? launch_rows<NPC, true>(ctx, nb_node, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed,    \
+                                       row_len, cols, slot, defer, defer_count, err)                              \
+              : launch_rows<NPC, false>(ctx, nb_node, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed,   \
+                                        row_len, cols, slot, defer, defer_count, err)
+  if (npc == 3) AFEM_ROWS_LAUNCH(3);
+  if (npc == 4) AFEM_ROWS_LAUNCH(4);
+  AFEM_ROWS_LAUNCH(8);
+#undef AFEM_ROWS_LAUNCH
+}
+
+static afem_status sparsity_error(int herr, const char* fn) {
+  if (herr & 8) return fail(AFEM_ERR_MESH, "%s: node id out of range in cell_nodes", fn);
+  if (herr & 2)
+    return fail(AFEM_ERR_MESH, "%s: a row has more than %d entries (%d neighbours)", fn, kMaxRowLen, kMaxRowLen - 1);
+  return fail(AFEM_ERR_MESH, "%s: row_ptr does not match the mesh", fn);
+}
+
+}  // namespace afem
+
+extern "C" {
+
 afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int32_t* cell_nodes_d,
                                const int32_t* nc_ptr_d, const int32_t* nc_cell_d, int32_t* row_ptr_d, int64_t* nnz_h) {
   AFEM_CHECK_ARG(ctx, "afem_sparsity_rows: null context");
   AFEM_CHECK_ARG(nb_node > 0 && (npc == 3 || npc == 4 || npc == 8), "afem_sparsity_rows: bad sizes");
   AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && row_ptr_d, "afem_sparsity_rows: null buffer");
-  size_t need = align256(sizeof(int32_t) * ((size_t)nb_node + 1)) + 256 + scan_scratch_bytes(nb_node);
+  size_t need = 2 * align256(sizeof(int32_t) * ((size_t)nb_node + 1)) + 256 + scan_scratch_bytes(nb_node);
   AFEM_TRY(scratch_reserve(ctx, need));
-  int32_t* len;
-  int* err;
+  int32_t *len, *defer;
+  int* err;   // err[0] error bits, err[1] deferred rows
   AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &len));
-  AFEM_TRY(scratch_take(ctx, 1, &err));
-  AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
-  unsigned grid =
-      (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock, (int64_t)ctx->sm_count * 8);
-  AFEM_TRY(launch(ctx, k_row_len, grid, kWarpsPerBlock * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, len,
-                  err));
+  AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &defer));
+  AFEM_TRY(scratch_take(ctx, 2, &err));
+  AFEM_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), ctx->stream));
+  AFEM_TRY(launch_sparsity_rows(ctx, false, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, nullptr, nullptr, 0, len,
+                                nullptr, nullptr, defer, err + 1, err));
   AFEM_TRY(exclusive_scan_i32(ctx, len, row_ptr_d, nb_node));
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
-  if (herr)
-    return fail(AFEM_ERR_MESH,
-                "afem_sparsity_rows: a node has more than %d cell-node incidences or more than %d neighbours",
-                kRowCap, kMaxRowLen);
+  if (herr) return sparsity_error(herr, "afem_sparsity_rows");
   if (nnz_h) {
     int32_t nnz = 0;
     AFEM_TRY(read_scalar(ctx, row_ptr_d + nb_node, &nnz));
@@ -443,17 +633,17 @@ afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int
                  "afem_sparsity_cols: bad col_order %d", col_order);
   AFEM_CHECK_ARG(cell_nodes_d && nc_ptr_d && nc_cell_d && nc_local_d && row_ptr_d && cols_d && nc_slot_d,
                  "afem_sparsity_cols: null buffer");
-  AFEM_TRY(scratch_reserve(ctx, 256));
-  int* err;
-  AFEM_TRY(scratch_take(ctx, 1, &err));
-  AFEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
-  unsigned grid =
-      (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock, (int64_t)ctx->sm_count * 8);
-  AFEM_TRY(launch(ctx, k_row_fill, grid, kWarpsPerBlock * 32, 0, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d,
-                  nc_local_d, row_ptr_d, col_order, cols_d, nc_slot_d, err));
+  AFEM_TRY(scratch_reserve(ctx, align256(sizeof(int32_t) * ((size_t)nb_node + 1)) + 256));
+  int32_t* defer;
+  int* err;   // err[0] error bits, err[1] deferred rows
+  AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &defer));
+  AFEM_TRY(scratch_take(ctx, 2, &err));
+  AFEM_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), ctx->stream));
+  AFEM_TRY(launch_sparsity_rows(ctx, true, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, nc_local_d, row_ptr_d,
+                                col_order == AFEM_COLS_SELF_LAST, nullptr, cols_d, nc_slot_d, defer, err + 1, err));
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
-  if (herr) return fail(AFEM_ERR_MESH, "afem_sparsity_cols: row_ptr does not match the mesh");
+  if (herr) return sparsity_error(herr, "afem_sparsity_cols");
   return AFEM_OK;
 }
 

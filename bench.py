@@ -363,7 +363,16 @@ def measure_workload(args, name, n, ctx, rank, world, local, main):
         if dp_cell:
             dp_achieved = dp_cell * mesh.nb_cell / (ms * 1e-3) / 1e9
             fp = {"achieved_g_fp64_instr_s": dp_achieved, "peak_g_fma_s": fma_rate, "frac": dp_achieved / fma_rate,
-                  "fp64_instructions_per_cell": dp_cell, "source": "ncu sm__inst_executed_pipe_fp64 (profiles/)"}
+                  "fp64_instructions_per_cell": dp_cell,
+                  "source": "ncu thread-level DADD+DFMA+DMUL per cell (profiles/assembly_counters.json); peak: "
+                            "afem_device_fp64_fma_rate measured on this GPU in this run"}
+            if fp["frac"] > roof["frac"]:
+                # the FP64 pipe binds: it is the line's roofline, the HBM figures stay beside it
+                hbm = {k: roof[k] for k in ("achieved", "peak", "unit", "frac", "peak_source")}
+                roof = {"bound": "fp64", "achieved": dp_achieved, "peak": fma_rate, "unit": "G FP64 instr/s",
+                        "frac": fp["frac"], "traffic": roof["traffic"], "peak_source": "measured (FP64 FMA loop)",
+                        "algorithmic_bytes": alg, "kernel": roof["kernel"], "hbm": hbm,
+                        "fp64_instructions_per_cell": dp_cell}
         return roof, fp
 
     roof, fp64 = rooflines(ms_per_step, "reference")

@@ -98,6 +98,8 @@ enum {
 
 /* Node-to-node sparsity, step 1: row_ptr_d[nb_node+1] (row length = 1 +
  * number of distinct neighbours) and the total in *nnz_h (host, synchronous).
+ * A row of more than 255 entries (the slot map below is uint8) or a node id
+ * outside [0, nb_node) returns AFEM_ERR_MESH. nodes_per_cell: 3, 4 or 8.
  * Replaces computeRowIndexAtomicFree / computeRowIndex (BSRFormat.cc:562-573,
  * 912-924) and _buildOffsetsNodeWiseCsr (NodeWiseCsrBiliAssembly.cc:90-112). */
 afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int nodes_per_cell, const int32_t* cell_nodes_d,

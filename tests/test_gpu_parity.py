@@ -601,11 +601,13 @@ def fan_mesh(k, isolated=0):
     return coords, cells
 
 
-@pytest.mark.parametrize("k,isolated", [(12, 0), (40, 0), (100, 2)])
+@pytest.mark.parametrize("k,isolated", [(12, 0), (40, 0), (100, 2), (200, 1), (254, 0)])
 def test_fan_rows_and_isolated_nodes_match_oracle(cuda_ctx, k, isolated):
     """Rows longer than the gather's shared-memory accumulators (the direct
-    path: 41 and 101 entries) and nodes in no cell (a diagonal-only row, as
-    the reference's deg + 1 rows): structure and values bit-exact."""
+    path: 41 to 255 entries; the hub's incidences span several chunks of 32 in
+    the sparsity kernels, and 255 entries is the longest row the uint8 slot map
+    addresses) and nodes in no cell (a diagonal-only row, as the reference's
+    deg + 1 rows): structure and values bit-exact."""
     coords, cells = fan_mesh(k, isolated)
     n = coords.shape[0]
     f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
@@ -662,16 +664,51 @@ def test_degenerate_cell_is_reported(formulation_ctx, formulation, kind):
     assert torch.isfinite(g.values).all()
 
 
-def test_row_above_the_candidate_capacity_is_reported(cuda_ctx):
-    """A node in 200 triangles (600 candidate entries, above the per-node
-    capacity of the sparsity kernels) is reported as a mesh error, not
-    truncated."""
-    coords, cells = fan_mesh(200)
+def star_mesh(k):
+    """k triangles that share only node 0 (a non-manifold star): node 0 is in
+    k cells and has 2k distinct neighbours."""
+    t = np.linspace(0.0, 2 * np.pi, 2 * k, endpoint=False)
+    ring = np.stack([np.cos(t), np.sin(t), np.zeros(2 * k)], 1)
+    coords = np.concatenate([np.zeros((1, 3)), ring], 0)
+    cells = np.array([[0, 1 + 2 * i, 2 + 2 * i] for i in range(k)], np.int32)
+    return coords, cells
+
+
+@pytest.mark.parametrize("k,self_last", [(8, False), (16, False), (16, True)])
+def test_rows_with_many_neighbours_per_cell_match_oracle(cuda_ctx, k, self_last):
+    """A node in at most 16 cells goes to the thread-per-node sparsity kernel;
+    with 2k > 24 distinct neighbours (k = 16) its row overflows that kernel's
+    table and is deferred to the warp kernel through the node list.  Structure,
+    slot map and values bit-exact in both column orders."""
+    coords, cells = star_mesh(k)
+    n = coords.shape[0]
+    f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
+    f.initialize(1, col_order=fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING)
+    f.compute_sparsity()
+    rp, cols = O.sparsity(n, cells, self_last=self_last)
+    assert np.array_equal(f.row_ptr.cpu().numpy(), rp) and np.array_equal(f.cols.cpu().numpy(), cols)
+    f.assemble_poisson()
+    ptr, nc, _ = O.node_cell(n, cells)
+    ref = O.assemble(O.POISSON_TRI3, coords, cells, ptr, nc, rp, cols)
+    assert_bit_exact(f.values.cpu().numpy(), ref, "star rows")
+
+
+@pytest.mark.parametrize("k", [255, 300])
+def test_row_above_the_slot_map_capacity_is_reported(cuda_ctx, k):
+    """A node in k triangles has a row of k + 1 entries; above 255 (the uint8
+    slot map) it is reported as a mesh error, not truncated, and the context
+    stays usable."""
+    coords, cells = fan_mesh(k)
     f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
     f.initialize(1)
     with pytest.raises(fem.AfemError) as e:
         f.compute_sparsity()
-    assert e.value.status == 7
+    assert e.value.status == 7 and "more than 255 entries" in str(e.value)
+    coords, cells = fan_mesh(12)
+    g = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
+    g.initialize(1)
+    g.compute_sparsity()
+    assert g.nnzb == 13 + 12 * 4   # the hub row, then 12 rows of 4
 
 
 def hub_laplacian(n, hubs, seed):
