@@ -127,21 +127,6 @@ struct RowTables {
   uint8_t* pos;
 };
 
-// The incidences of node n in chunks of 32, one per lane: the lane holds its
-// cell's NPC nodes, of which local index li is n itself (read with the slot
-// map only).
-template <int NPC, bool LOCAL>
-__device__ __forceinline__ bool load_incidence(const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_cell,
-                                               const uint8_t* __restrict__ nc_local, int k, int deg, int32_t (&v)[NPC],
-                                               int& li) {
-  if (k >= deg) return false;
-  const int64_t c = __ldg(nc_cell + k);
-  if (LOCAL) li = __ldg(nc_local + k);
-#pragma unroll
-  for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
-  return true;
-}
-
 // Inserts v; returns its table slot (fresh: first insertion), or -1 when
 // the table is full.
 __device__ __forceinline__ int tab_insert(int32_t* key, int32_t v, bool& fresh) {
@@ -187,7 +172,8 @@ __device__ __forceinline__ int tab_find(const int32_t* key, int32_t v) {
 // incidence writes its NPC slot bytes (its own column first, then the other
 // cell nodes in increasing local index) in one packed store.  A row with more
 // neighbours than the table's 3/4 is appended to `defer` for
-// k_sparsity_rows_warp.
+// k_sparsity_rows_warp, and so are the light nodes of a warp that holds too
+// few of them.
 // Errors: bit 2 a row of more than kMaxRowLen entries, bit 4 a row_ptr that
 // does not match, bit 8 a node id out of range.
 constexpr int kThreadBlock = 128;
@@ -195,6 +181,8 @@ constexpr int kThreadBlock = 128;
 // stay at least half busy (tetrahedral meshes: about 24 cells per node);
 // lower degrees (triangles, hexahedra, boundary nodes) stay here.
 constexpr int kThreadMaxDeg = 16;
+// A warp of k_sparsity_thread with fewer light nodes than this passes them on.
+constexpr int kThreadMinLanes = 12;
 
 template <int NPC>
 struct ThreadTable {
@@ -221,9 +209,26 @@ __global__ void __launch_bounds__(kThreadBlock)
   const int t = threadIdx.x;
 #pragma unroll
   for (int h = 0; h < TS; ++h) s_key[h][t] = -1;
-  for (int n = blockIdx.x * kThreadBlock + t; n < nb_node; n += gridDim.x * kThreadBlock) {
-    const int32_t b = __ldg(nc_ptr + n), e = __ldg(nc_ptr + n + 1);
-    if (e - b > kThreadMaxDeg) continue;   // k_sparsity_rows_warp's
+  const int lane = t & 31;
+  for (int n0 = blockIdx.x * kThreadBlock + (t & ~31); n0 < nb_node; n0 += gridDim.x * kThreadBlock) {
+    const int n = n0 + lane;
+    int32_t b = 0, e = 0;
+    if (n < nb_node) {
+      b = __ldg(nc_ptr + n);
+      e = __ldg(nc_ptr + n + 1);
+    }
+    const bool light = n < nb_node && e - b <= kThreadMaxDeg;   // the others are k_sparsity_rows_warp's
+    const unsigned lights = __ballot_sync(0xffffffffu, light);
+    if (__popc(lights) < kThreadMinLanes) {
+      // too few light nodes to keep this warp's lanes busy (the boundary of a
+      // dense mesh): they go to the warp kernel's list
+      int base = 0;
+      if (lane == 0 && lights) base = atomicAdd(defer_count, __popc(lights));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (light) defer[base + __popc(lights & ((1u << lane) - 1u))] = n;
+      continue;
+    }
+    if (!light) continue;
     int D = 0;
     bool over = false, bad = false;
     for (int32_t p = b; p < e && !over; ++p) {
@@ -320,23 +325,25 @@ __global__ void __launch_bounds__(kThreadBlock)
   }
 }
 
-// The nodes in more than kThreadMaxDeg cells, and the rows k_sparsity_thread
-// deferred (more distinct neighbours than its per-thread table holds), listed
+// The nodes in more than `min_deg` cells (every node when -1), and the rows
+// k_sparsity_thread deferred (more distinct neighbours than its per-thread table holds), listed
 // in `list[0 .. *list_count)`: one warp per node, lanes over its incidences
-// (chunks of 32), the nodes other than n of each incident cell inserted into
-// the warp's hash set.  Round r inserts, in every lane, the cell node r + 1
-// places after the lane's own, so that the lanes of one atomic rarely target
-// the same table slot (cells around a node share nodes at equal local
-// indices) and the own node takes no round.  The number
-// of first insertions D is the number of distinct neighbours and the row
-// holds D + 1 entries.  With FILL the row is then written: the rank of each
-// neighbour among the others is counted against the list (broadcast reads of
-// shared memory; no sort), which gives its column position in either order,
-// and every incidence writes its NPC slot bytes in one packed store.  Errors
-// as k_sparsity_thread.
+// (chunks of 32).  The row's own node is inserted into the warp's hash set
+// first, then every lane inserts the nodes of its cell: a node met again
+// (the row's own included) finds its slot, so the number of first insertions
+// D is the row length (the reference's deg + 1 entries,
+// femutils/BSRFormat.cc:445-557).  Round r inserts, in every lane, the cell
+// node r + 1 places after the lane's own, so that the lanes of one atomic
+// rarely target the same slot (cells around a node share nodes at equal
+// local indices).  With FILL the row is then written: the rank of each
+// column among the row's (counted against the list with broadcast reads of
+// shared memory; no sort) gives its position in either order, and every
+// incidence writes its NPC slot bytes in one packed store.  Errors as
+// k_sparsity_thread.
 template <int NPC, bool FILL>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
-    k_sparsity_rows_warp(int nb_node, const int32_t* __restrict__ list, const int32_t* __restrict__ list_count,
+    k_sparsity_rows_warp(int nb_node, int min_deg, const int32_t* __restrict__ list,
+                         const int32_t* __restrict__ list_count,
                          const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_ptr,
                          const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ nc_local,
                          const int32_t* __restrict__ row_ptr, int self_last, int packed_slots,
@@ -359,37 +366,46 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     const int n = it < nb_node ? it : __ldg(list + (it - nb_node));
     const int32_t b = __ldg(nc_ptr + n);
     const int deg = __ldg(nc_ptr + n + 1) - b;
-    if (it < nb_node && deg <= kThreadMaxDeg) continue;   // k_sparsity_thread's
+    if (it < nb_node && deg <= min_deg) continue;   // k_sparsity_thread's
+    if (lane == 0) {
+      const int h = tab_hash(n);
+      t.key[h] = n;
+      t.at[0] = (int16_t)h;
+      if (FILL) t.val[0] = n;
+    }
+    __syncwarp();
     int32_t v[NPC];
     int16_t hs[NPC - 1];   // table slot of each round's candidate (the last chunk's)
-    int me = 0;            // local index of n in the lane's cell
-    int li = 0;
-    bool act = false, bad_id = false, full = false;
-    int D = 0;   // distinct neighbours so far, uniform across the warp
-    for (int kb = 0; kb < deg || kb == 0; kb += 32) {
-      act = load_incidence<NPC, FILL>(cn, nc_cell + b, nc_local + b, kb + lane, deg, v, li);
-      if (FILL) {
-        me = li;
-      } else {
-        me = 0;
+    int li = 0;            // local index of n in the lane's cell
+    bool act = false, bad = false, full = false;
+    int D = 1;             // distinct columns so far, uniform across the warp
+    for (int kb = 0; kb < deg; kb += 32) {
+      act = kb + lane < deg;
+      if (act) {
+        const int64_t c = __ldg(nc_cell + b + kb + lane);
 #pragma unroll
-        for (int j = NPC - 1; j >= 0; --j)
-          if (v[j] == n) me = j;
+        for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
+        if (FILL) {
+          li = __ldg(nc_local + b + kb + lane);
+        } else {
+          li = 0;
+#pragma unroll
+          for (int j = NPC - 1; j > 0; --j)
+            if (v[j] == n) li = j;
+        }
+#pragma unroll
+        for (int j = 0; j < NPC; ++j) bad |= (unsigned)v[j] >= (unsigned)nb_node;
       }
 #pragma unroll
       for (int r = 0; r + 1 < NPC; ++r) {
-        int j = me + 1 + r;
+        int j = li + 1 + r;
         j -= j >= NPC ? NPC : 0;
         const int32_t x = pick<NPC>(v, j);
         bool fresh = false;
         int h = 0;
-        if (act && x != n) {
-          if ((unsigned)x >= (unsigned)nb_node) {
-            bad_id = true;
-          } else {
-            h = tab_insert(t.key, x, fresh);
-            full |= h < 0;
-          }
+        if (act) {
+          h = tab_insert(t.key, x, fresh);
+          full |= h < 0;
         }
         hs[r] = (int16_t)h;
         const unsigned fb = __ballot_sync(0xffffffffu, fresh);
@@ -401,23 +417,21 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         D += __popc(fb);
       }
     }
-    const bool bad = __any_sync(0xffffffffu, bad_id), overflow = __any_sync(0xffffffffu, full);
-    const int len = D + 1;
-    const bool too_long = overflow || len > kMaxRowLen;
+    const bool bad_w = __any_sync(0xffffffffu, bad), overflow = __any_sync(0xffffffffu, full);
+    const bool too_long = overflow || D > kMaxRowLen;
     __syncwarp();
     if (!FILL) {
       if (lane == 0) {
-        if (bad || too_long) atomicOr(err, bad ? 8 : 2);
-        row_len[n] = (bad || too_long) ? 0 : len;
+        if (bad_w || too_long) atomicOr(err, bad_w ? 8 : 2);
+        row_len[n] = (bad_w || too_long) ? 0 : D;
       }
     } else {
       const int32_t rb = __ldg(row_ptr + n);
-      const bool ok = !bad && !too_long && __ldg(row_ptr + n + 1) - rb == len;
-      if (lane == 0 && !ok) atomicOr(err, bad ? 8 : too_long ? 2 : 4);
+      const bool ok = !bad_w && !too_long && __ldg(row_ptr + n + 1) - rb == D;
+      if (lane == 0 && !ok) atomicOr(err, bad_w ? 8 : too_long ? 2 : 4);
       if (ok) {
         if (lane < 4) t.val[D + lane] = INT_MAX;
         __syncwarp();
-        int own = 0;   // neighbours below n
         for (int i = lane; i < D; i += 32) {
           const int32_t x = t.val[i];
           int r = 0;
@@ -425,17 +439,23 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             const int4 q = *reinterpret_cast<const int4*>(t.val + u);
             r += (q.x < x) + (q.y < x) + (q.z < x) + (q.w < x);
           }
-          const int p = self_last ? r : r + (n < x);
+          // self-last: the neighbours keep their ascending order, the row's own node goes last
+          const int p = !self_last ? r : (x == n ? D - 1 : r - (x > n));
           cols[rb + p] = x;
           t.pos[t.at[i]] = (uint8_t)p;
-          own += x < n;
         }
-        own = __reduce_add_sync(0xffffffffu, own);
-        const int pn = self_last ? D : own;
-        if (lane == 0) cols[rb + pn] = n;
         __syncwarp();
+        const int pn = t.pos[t.at[0]];
         for (int kb = 0; kb < deg; kb += 32) {
-          if (deg > 32) act = load_incidence<NPC, true>(cn, nc_cell + b, nc_local + b, kb + lane, deg, v, li);
+          if (deg > 32) {
+            act = kb + lane < deg;
+            if (act) {
+              const int64_t c = __ldg(nc_cell + b + kb + lane);
+              li = __ldg(nc_local + b + kb + lane);
+#pragma unroll
+              for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
+            }
+          }
           if (!act) continue;
           // slot byte q of the incidence at bits 8q: its own column, then the
           // other cell nodes in increasing local index
@@ -445,8 +465,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           for (int r = 0; r + 1 < NPC; ++r) {
             int j = li + 1 + r;
             j -= j >= NPC ? NPC : 0;
-            const int32_t x = pick<NPC>(v, j);
-            const Word p = x == n ? (Word)pn : (Word)t.pos[deg > 32 ? tab_find(t.key, x) : hs[r]];
+            const Word p = (Word)t.pos[deg > 32 ? tab_find(t.key, pick<NPC>(v, j)) : hs[r]];
             word |= p << (8 * (j < li ? j + 1 : j));
           }
           uint8_t* dst = slot + (int64_t)(b + kb + lane) * NPC;
@@ -550,36 +569,44 @@ static int resident_blocks(Kernel k, int block) {
 }
 
 template <int NPC, bool FILL>
-static afem_status launch_rows(afem_context ctx, int nb_node, const int32_t* cn, const int32_t* nc_ptr,
+static afem_status launch_rows(afem_context ctx, bool dense, int nb_node, const int32_t* cn, const int32_t* nc_ptr,
                                const int32_t* nc_cell, const uint8_t* nc_local, const int32_t* row_ptr, int self_last,
                                int packed, int32_t* row_len, int32_t* cols, uint8_t* slot, int32_t* defer,
                                int32_t* defer_count, int* err) {
   static const int per_sm_thread = resident_blocks(k_sparsity_thread<NPC, FILL>, kThreadBlock);
   static const int per_sm_warp = resident_blocks(k_sparsity_rows_warp<NPC, FILL>, kWarpsPerBlock * 32);
-  const unsigned g1 = (unsigned)std::min<int64_t>((nb_node + kThreadBlock - 1) / kThreadBlock,
-                                                  (int64_t)ctx->sm_count * per_sm_thread);
-  AFEM_TRY(launch(ctx, k_sparsity_thread<NPC, FILL>, g1, kThreadBlock, 0, nb_node, cn, nc_ptr, nc_cell, nc_local,
-                  row_ptr, self_last, packed, row_len, cols, slot, defer, defer_count, err));
-  // the deferred long rows (usually none): the grid covers the worst case and
-  // each warp reads the list's length on the device
+  if (!dense) {
+    const unsigned g1 = (unsigned)std::min<int64_t>((nb_node + kThreadBlock - 1) / kThreadBlock,
+                                                    (int64_t)ctx->sm_count * per_sm_thread);
+    AFEM_TRY(launch(ctx, k_sparsity_thread<NPC, FILL>, g1, kThreadBlock, 0, nb_node, cn, nc_ptr, nc_cell, nc_local,
+                    row_ptr, self_last, packed, row_len, cols, slot, defer, defer_count, err));
+  }
+  // the dense rows, and the rows k_sparsity_thread passed on: the grid covers
+  // the worst case and each warp reads the list's length on the device
   const unsigned g2 = (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock,
                                                   (int64_t)ctx->sm_count * per_sm_warp);
-  return launch(ctx, k_sparsity_rows_warp<NPC, FILL>, g2, kWarpsPerBlock * 32, 0, nb_node, (const int32_t*)defer,
-                (const int32_t*)defer_count, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed, row_len, cols,
-                slot, err);
+  return launch(ctx, k_sparsity_rows_warp<NPC, FILL>, g2, kWarpsPerBlock * 32, 0, nb_node,
+                dense ? -1 : kThreadMaxDeg, (const int32_t*)defer, (const int32_t*)defer_count, cn, nc_ptr, nc_cell,
+                nc_local, row_ptr, self_last, packed, row_len, cols, slot, err);
 }
 
 static afem_status launch_sparsity_rows(afem_context ctx, bool fill, int nb_node, int npc, const int32_t* cn,
                                         const int32_t* nc_ptr, const int32_t* nc_cell, const uint8_t* nc_local,
                                         const int32_t* row_ptr, int self_last, int32_t* row_len, int32_t* cols,
                                         uint8_t* slot, int32_t* defer, int32_t* defer_count, int* err) {
+  // Meshes whose nodes lie in more than kThreadMaxDeg cells on average
+  // (tetrahedra: about 24) run the warp kernel alone: in the thread kernel
+  // their few light nodes would only leave its lanes idle.
+  int32_t incidences = 0;
+  AFEM_TRY(read_scalar(ctx, nc_ptr + nb_node, &incidences));
+  const bool dense = incidences > (int64_t)kThreadMaxDeg * nb_node;
   // one packed store per incidence when the slot map is aligned to its rows
   const int packed = (reinterpret_cast<uintptr_t>(slot) % (npc == 8 ? 8 : 4)) == 0;
 #define AFEM_ROWS_LAUNCH(NPC)                                                                                    \
-  return fill ? launch_rows<NPC, true>(ctx, nb_node, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed,    \
-                                       row_len, cols, slot, defer, defer_count, err)                              \
-              : launch_rows<NPC, false>(ctx, nb_node, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed,   \
-                                        row_len, cols, slot, defer, defer_count, err)
+  return fill ? launch_rows<NPC, true>(ctx, dense, nb_node, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last,     \
+                                       packed, row_len, cols, slot, defer, defer_count, err)                      \
+              : launch_rows<NPC, false>(ctx, dense, nb_node, cn, nc_ptr, nc_cell, nc_local, row_ptr, self_last,    \
+                                        packed, row_len, cols, slot, defer, defer_count, err)
   if (npc == 3) AFEM_ROWS_LAUNCH(3);
   if (npc == 4) AFEM_ROWS_LAUNCH(4);
   AFEM_ROWS_LAUNCH(8);
