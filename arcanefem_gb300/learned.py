@@ -289,22 +289,34 @@ class AlgebraicHierarchy:
         return P, T
 
 
-def param_count(layers: int, levels: int) -> int:
-    """W_in[2][64], b_in[64]; per layer W1, W2 [64][64], b[64]; per level head w[64], beta."""
-    return 3 * F + layers * (2 * F * F + F) + levels * (F + 1)
+FACT_ROWS = 2048   # the finest level and the levels of at most this many rows get the factored smoother
 
 
-def init_params(layers: int, levels: int, seed: int = 0, head_scale: float = 0.01) -> np.ndarray:
-    """He-style hidden weights; heads near zero, so that the initial
-    preconditioner is the V-cycle with l1-Jacobi smoothing (c_l ~ 0)."""
+def fact_levels(sizes) -> list:
+    """The levels whose smoother is the learned factored sparse approximate inverse."""
+    return [l for l, n in enumerate(sizes) if l == 0 or n <= FACT_ROWS]
+
+
+def param_count(layers: int, levels: int, nfact: int = 0) -> int:
+    """W_in[2][64], b_in[64]; per layer W1, W2 [64][64], b[64]; per level head
+    w[64], beta; per factored level edge head ew[64], eb."""
+    return 3 * F + layers * (2 * F * F + F) + levels * (F + 1) + nfact * (F + 1)
+
+
+def init_params(layers: int, levels: int, seed: int = 0, head_scale: float = 0.01, nfact: int = 0) -> np.ndarray:
+    """He-style hidden weights; node heads near zero and edge heads at zero, so
+    that the initial preconditioner is the V-cycle with l1-Jacobi smoothing
+    (c_l ~ 0, N_l = 0)."""
     rng = np.random.default_rng(seed)
     parts = [rng.normal(0, 1.0, (2, F)), np.zeros(F)]
     for _ in range(layers):
         parts += [rng.normal(0, np.sqrt(1.0 / F), (F, F)), rng.normal(0, np.sqrt(1.0 / F), (F, F)), np.zeros(F)]
     for _ in range(levels):
         parts += [rng.normal(0, head_scale, F), np.zeros(1)]
+    for _ in range(nfact):
+        parts += [np.zeros(F), np.zeros(1)]
     p = np.concatenate([p.ravel() for p in parts]).astype(np.float32)
-    assert p.size == param_count(layers, levels)
+    assert p.size == param_count(layers, levels, nfact)
     return p
 
 

@@ -21,6 +21,21 @@ with weighted-Jacobi smoothers whose per-node weights come from the network:
     c_l = o_l . w_l + beta_l  (o_l the level-l output of the message-passing
     network on the coefficient features x0 = [1, log A_ii - mean log A_ii])
 
+On the factored levels (the finest level and every level of at most
+FACT_ROWS rows) the smoother is a learned factored sparse approximate
+inverse instead of d_l * x:
+
+    G_l = theta_l L_l^T L_l,   L_l = (I + N_l) T_l^1/2,   T_l = diag(d_l),
+    N_l,ij = m_ij s_i s_j A_l,ij   (strictly lower pattern of A_l; s = sqrt(d_l)),
+    m_ij = 2 tanh(o_i . (ew_l * o_j) + eb_l)   (an edge head on the level output),
+    theta_l = 1.9 / max(1.9, max_i sum_j |(L_l^T L_l A_l)_ij|),
+
+SPD by construction (L_l lower triangular with a positive diagonal) and with
+lambda_max(G_l A_l) < 2 by the row-sum bound, so the V-cycle stays SPD for any
+network output; with ew = eb = 0 it is the weighted Jacobi smoother above.
+theta_l takes part in the gradient (through the row that attains the
+maximum) on every factored level but the finest, where it is held constant.
+
 trained on the relative energy norm of the error propagation
 ||(I - M A) e||_A^2 / ||e||_A^2, with the gradient -2 A (e - M r) of a
 symmetric A (as the GPU computes it); the backward pass is the adjoint of
@@ -38,6 +53,8 @@ import scipy.sparse as sp
 
 F = 64
 THETA = 0.8          # untrained smoother weight, as a fraction of the l1-Jacobi cap
+FACT_ROWS = 2048     # levels of at most this many rows (and the finest) get the factored smoother
+SAFE = 1.9           # the row-sum bound of theta_l G_l A_l
 
 
 def bf16(x):
@@ -48,11 +65,19 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def param_count(NL, L):
-    return 3 * F + NL * (2 * F * F + F) + L * (F + 1)
+def fact_levels(sizes, fact_rows=FACT_ROWS):
+    """The levels that get the factored smoother: the finest and every level of
+    at most fact_rows rows (none when fact_rows is None: diagonal smoothers only)."""
+    if fact_rows is None:
+        return []
+    return [l for l, n in enumerate(sizes) if l == 0 or n <= fact_rows]
 
 
-def unpack(params, NL, L):
+def param_count(NL, L, nfact=0):
+    return 3 * F + NL * (2 * F * F + F) + L * (F + 1) + nfact * (F + 1)
+
+
+def unpack(params, NL, L, nfact=0):
     p = np.asarray(params, np.float64)
     o = 0
     Win = p[o:o + 2 * F].reshape(2, F); o += 2 * F
@@ -66,8 +91,11 @@ def unpack(params, NL, L):
     heads = []
     for _ in range(L):
         heads.append((p[o:o + F], p[o + F])); o += F + 1
+    edges = []
+    for _ in range(nfact):
+        edges.append((p[o:o + F], p[o + F])); o += F + 1
     assert o == p.size, (o, p.size)
-    return Win, bin_, layers, heads
+    return Win, bin_, layers, heads, edges
 
 
 def level0_graph(A: sp.csr_matrix):
@@ -79,7 +107,7 @@ def level0_graph(A: sp.csr_matrix):
 
 
 class Net:
-    def __init__(self, A, graphs, restr, prol, layers=None, bf16_round=False):
+    def __init__(self, A, graphs, restr, prol, layers=None, bf16_round=False, fact_rows=None):
         self.A = sp.csr_matrix(A)
         self.S0, self.d = level0_graph(A)
         self.S = [self.S0] + list(graphs[1:])
@@ -98,13 +126,44 @@ class Net:
             self.base.append(np.where(l1 > 0, 2.0 / np.where(l1 > 0, l1, 1.0), 0.0))
         logd = np.log(self.d)
         self.x0 = np.stack([np.ones_like(logd), (logd - logd.mean()).astype(np.float32).astype(np.float64)], 1)
+        # factored levels: the strictly lower pattern of A_l (row i, column j < i, value A_ij)
+        self.fact = fact_levels([Al.shape[0] for Al in self.Al], fact_rows)
+        self.low = {}
+        for l in self.fact:
+            lo = sp.tril(self.Al[l], k=-1).tocoo()
+            keep = lo.data != 0
+            self.low[l] = (lo.row[keep], lo.col[keep], lo.data[keep])
+
+    @property
+    def nfact(self):
+        return len(self.fact)
+
+    def factor(self, l, d, o, ew, eb):
+        """The factored smoother of level l: L_l, theta_l and what the backward needs."""
+        i, j, a = self.low[l]
+        n = self.Al[l].shape[0]
+        z = np.einsum("ef,ef,f->e", o[i], o[j], ew) + eb if i.size else np.zeros(0)
+        m = 2 * np.tanh(z)
+        s = np.sqrt(d[l])
+        lval = m * s[i] * s[j] * s[j] * a                       # L_ij = N_ij s_j
+        ar = np.arange(n)
+        Lf = sp.csr_matrix((np.concatenate([s, lval]), (np.concatenate([ar, i]), np.concatenate([ar, j]))),
+                           shape=(n, n))
+        LA = sp.csr_matrix(Lf @ self.Al[l])
+        GA = sp.csr_matrix(Lf.T @ LA)
+        rows = np.asarray(abs(GA).sum(axis=1)).ravel()
+        istar = int(np.argmax(rows))
+        bound = float(rows[istar])
+        theta = SAFE / max(SAFE, bound)
+        return {"z": z, "m": m, "s": s, "Lf": Lf, "LA": LA, "GA": GA, "istar": istar, "bound": bound,
+                "theta": theta}
 
     def features(self, params):
-        """Network forward: per-level scalings d_l and the activations."""
+        """Network forward: per-level weights d_l, the factored smoothers, and the activations."""
         q = self.q
-        Win, bin_, layers, heads = unpack(params, self.NL, self.L)
+        Win, bin_, layers, heads, edges = unpack(params, self.NL, self.L, self.nfact)
         a = q(np.maximum(self.x0 @ Win + bin_, 0))
-        c = {"a": a, "h": [a], "m": [], "o": [], "d": []}
+        c = {"a": a, "h": [a], "m": [], "o": [], "d": [], "f": {}}
         h = a
         for l in range(self.L):
             if l < self.NL:
@@ -118,12 +177,22 @@ class Net:
             w, beta = heads[l]
             z = np.clip(o @ w + beta + np.log(THETA / (1 - THETA)), -30, 30)
             c["d"].append(self.base[l] / (1 + np.exp(-z)))
+            if l in self.low:
+                ew, eb = edges[self.fact.index(l)]
+                c["f"][l] = self.factor(l, c["d"], o, ew, eb)
             if l + 1 < self.L:
                 h = q(self.R[l] @ o)
                 c["h"].append(h)
         return c
 
-    def apply(self, d, r):
+    def smooth(self, c, l, x):
+        """The level-l smoother applied to x: d_l * x, or theta_l L_l^T L_l x."""
+        f = c["f"].get(l)
+        if f is None:
+            return c["d"][l] * x
+        return f["theta"] * (f["Lf"].T @ (f["Lf"] @ x))
+
+    def apply(self, c, r):
         """z = M r (one V(1,1)-cycle) and the per-level states (r_l, u_l) the
         backward pass needs."""
         L = self.L
@@ -132,41 +201,53 @@ class Net:
         def V(l, r):
             if l == L - 1:
                 st[l] = (r, None)
-                return d[l] * r
+                return self.smooth(c, l, r)
             A = self.Al[l]
-            x1 = d[l] * r
+            x1 = self.smooth(c, l, r)
             s = r - A @ x1
             x2 = x1 + self.P[l] @ V(l + 1, self.P[l].T @ s)
             u = r - A @ x2
             st[l] = (r, u)
-            return x2 + d[l] * u
+            return x2 + self.smooth(c, l, u)
 
         return V(0, r), st
 
-    def adjoint(self, d, st, g):
-        """dL/dd_l for dL/dz = g through the V-cycle with states st."""
+    def adjoint(self, c, st, g, acc):
+        """Accumulates into acc the gradient of <g, M r> with respect to the
+        smoothers: acc["dd"][l] (diagonal levels: dL/dd_l) and, on factored
+        levels, acc["gL"][l] (dL/dL_l on its diagonal and lower pattern, as a
+        matrix) and acc["dth"][l] (dL/dtheta_l)."""
         L = self.L
-        dd = [np.zeros_like(x) for x in d]
+
+        def use(l, a, gbar):
+            f = c["f"].get(l)
+            if f is None:
+                acc["dd"][l] += gbar * a
+                return
+            wa, wg = f["Lf"] @ a, f["Lf"] @ gbar
+            acc["dth"][l] += wg @ wa
+            # dL/dL_ij = theta (wg_i a_j + wa_i gbar_j) on the pattern of L
+            Lf = sp.coo_matrix(f["Lf"])
+            acc["gL"][l] += f["theta"] * (wg[Lf.row] * a[Lf.col] + wa[Lf.row] * gbar[Lf.col])
 
         def B(l, g):
             r, u = st[l]
             if l == L - 1:
-                dd[l] += g * r
-                return d[l] * g
+                use(l, r, g)
+                return self.smooth(c, l, g)
             A = self.Al[l]
-            dd[l] += g * u                       # post-smoothing weight
-            x2b = g - A @ (d[l] * g)
+            use(l, u, g)                              # post-smoothing
+            x2b = g - A @ self.smooth(c, l, g)
             sb = self.P[l] @ B(l + 1, self.P[l].T @ x2b)
             x1b = x2b - A @ sb
-            dd[l] += x1b * r                     # pre-smoothing weight
-            return d[l] * g + sb + d[l] * x1b
+            use(l, r, x1b)                            # pre-smoothing
+            return self.smooth(c, l, g + x1b) + sb
 
         B(0, g)
-        return dd
 
     def forward(self, params, r):
         c = self.features(params)
-        return self.apply(c["d"], r)[0]
+        return self.apply(c, r)[0]
 
     def loss_and_grad(self, params, rs, es):
         """Mean relative energy norm of the error propagation,
@@ -176,7 +257,7 @@ class Net:
         loss = 0.0
         ts, seeds = [], []
         for r, e in zip(rs, es):
-            z, t = self.apply(c["d"], r)
+            z, t = self.apply(c, r)
             ee = np.dot(e, self.A @ e) + 1e-300
             Av = self.A @ (e - z)
             loss += np.dot(e - z, Av) / ee / B
@@ -184,15 +265,68 @@ class Net:
             seeds.append(-2 * Av / (ee * B))
         return loss, self.backward(params, c, ts, seeds)
 
+    def factor_backward(self, l, c, gL, dth, ew):
+        """From dL/dL_l (coo order of L_l) and dL/dtheta_l to dL/dd_l, the edge
+        head's parameter gradient and its contribution to dL/do_l."""
+        f = c["f"][l]
+        i, j, a = self.low[l]
+        o = c["o"][l]
+        Lf = sp.coo_matrix(f["Lf"])
+        G = sp.csr_matrix((gL, (Lf.row, Lf.col)), shape=Lf.shape)   # duplicates summed: none on a pattern
+        if l != 0 and f["bound"] > SAFE:
+            # theta = SAFE / bound: through the row i* that attains the bound
+            db = dth * (-SAFE / f["bound"] ** 2)
+            ist = f["istar"]
+            sign = np.sign(f["GA"].getrow(ist).toarray().ravel())
+            Lcsc = sp.csc_matrix(f["Lf"])
+            col = Lcsc.getcol(ist).tocoo()                  # entries L_{k i*}
+            dG = sp.lil_matrix(Lf.shape)
+            LAs = f["LA"] @ sign                            # (L A sign)_k
+            As = self.Al[l] @ sign                          # (A sign)_m
+            Lcsr = sp.csr_matrix(f["Lf"])
+            for k, lk in zip(col.row, col.data):
+                dG[k, ist] += LAs[k]
+                row = Lcsr.getrow(k).tocoo()
+                for mcol in row.col:
+                    dG[k, mcol] += lk * As[mcol]
+            G = G + db * sp.csr_matrix(dG)
+        gd = np.asarray(G.diagonal()).ravel()                # dL/dL_ii = dL/ds_i
+        gl = np.asarray(G[i, j]).ravel() if i.size else np.zeros(0)
+        s, m = f["s"], f["m"]
+        ds = gd.copy()
+        # L_ij = m_ij a_ij s_i s_j^2
+        if i.size:
+            dm = gl * a * s[i] * s[j] ** 2
+            np.add.at(ds, i, gl * m * a * s[j] ** 2)
+            np.add.at(ds, j, gl * m * a * s[i] * 2 * s[j])
+            dz = dm * 2 * (1 - np.tanh(f["z"]) ** 2)
+            oij = o[i] * o[j]
+            gew = oij.T @ dz
+            geb = dz.sum()
+            dO = np.zeros_like(o)
+            np.add.at(dO, i, dz[:, None] * (ew * o[j]))
+            np.add.at(dO, j, dz[:, None] * (ew * o[i]))
+        else:
+            gew, geb, dO = np.zeros(F), 0.0, np.zeros_like(o)
+        dd = np.where(s > 0, ds / (2 * np.where(s > 0, s, 1.0)), 0.0)
+        return dd, (gew, geb), dO
+
     def backward(self, params, c, ts, seeds):
         """Parameter gradient from dL/dz_b (seeds) for z_b = M r_b with V-cycle states ts."""
         q = self.q
-        Win, bin_, layers, heads = unpack(params, self.NL, self.L)
+        Win, bin_, layers, heads, edges = unpack(params, self.NL, self.L, self.nfact)
         L = self.L
-        dd = [np.zeros_like(x) for x in c["d"]]
+        acc = {"dd": [np.zeros_like(x) for x in c["d"]],
+               "gL": {l: np.zeros(c["f"][l]["Lf"].nnz) for l in self.fact}, "dth": {l: 0.0 for l in self.fact}}
         for t, s in zip(ts, seeds):
-            for l, x in enumerate(self.adjoint(c["d"], t, s)):
-                dd[l] += x
+            self.adjoint(c, t, s, acc)
+        dd = acc["dd"]
+        gedges = [None] * self.nfact
+        dOe = {}
+        for k, l in enumerate(self.fact):
+            ew, _ = edges[k]
+            ddl, gedges[k], dOe[l] = self.factor_backward(l, c, acc["gL"][l], acc["dth"][l], ew)
+            dd[l] = dd[l] + ddl
         gheads = []
         dO = [None] * L
         for l in range(L):
@@ -200,7 +334,7 @@ class Net:
             dc = dd[l] * dl * (1 - np.where(cap > 0, dl / np.where(cap > 0, cap, 1.0), 0.0))
             w, _ = heads[l]
             gheads.append((c["o"][l].T @ dc, dc.sum()))
-            dO[l] = np.outer(dc, w)
+            dO[l] = np.outer(dc, w) + dOe.get(l, 0.0)
         gl = [None] * self.NL
         dh0 = None
         for l in range(L - 1, -1, -1):
@@ -220,5 +354,7 @@ class Net:
         for g1, g2, gb in gl:
             parts += [g1.ravel(), g2.ravel(), gb]
         for gw, gb in gheads:
+            parts += [gw, [gb]]
+        for gw, gb in gedges:
             parts += [gw, [gb]]
         return np.concatenate(parts)
