@@ -572,12 +572,12 @@ __global__ void k_head(int n, const bf16* __restrict__ o, const float* __restric
 // scalar CSR SpMV over a batch (grid.y): y[b][i] = (d ? d[i] t[b][i] : 0) + sum_k w_k x[b][col_k]
 __global__ void k_sweep(int nrow, int ncol, const int32_t* __restrict__ rp, const int32_t* __restrict__ cols,
                         const float* __restrict__ w, const float* __restrict__ x, const float* __restrict__ d,
-                        const float* __restrict__ t, float* __restrict__ y) {
+                        const float* __restrict__ t, const float* __restrict__ add, float* __restrict__ y) {
   pdl_trigger();
   pdl_wait();
   const int64_t b = blockIdx.y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nrow; i += gridDim.x * blockDim.x) {
-    float s = d ? d[i] * t[b * nrow + i] : 0.f;
+    float s = d ? d[i] * t[b * nrow + i] : (add ? add[b * nrow + i] : 0.f);
     if (x)
       for (int32_t k = rp[i]; k < rp[i + 1]; ++k) s = fmaf(w[k], x[b * ncol + cols[k]], s);
     y[b * nrow + i] = s;
@@ -612,6 +612,18 @@ __device__ __forceinline__ void vc_spmv(int i0, int st, int n, const int32_t* __
                                         const float* __restrict__ t, float* __restrict__ y) {
   for (int i = i0; i < n; i += st) {
     float acc = d ? d[i] * t[i] : 0.f;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) acc = fmaf(w[k], x[cols[k]], acc);
+    y[i] = acc;
+  }
+}
+
+// y = add + M x
+__device__ __forceinline__ void vc_spmv_add(int i0, int st, int n, const int32_t* __restrict__ rp,
+                                            const int32_t* __restrict__ cols, const float* __restrict__ w,
+                                            const float* __restrict__ x, const float* __restrict__ add,
+                                            float* __restrict__ y) {
+  for (int i = i0; i < n; i += st) {
+    float acc = add[i];
     for (int32_t k = rp[i]; k < rp[i + 1]; ++k) acc = fmaf(w[k], x[cols[k]], acc);
     y[i] = acc;
   }
@@ -672,6 +684,12 @@ __global__ void k_vc_pre_adjoint(int n, const int32_t* __restrict__ rp, const in
                  sb + o, x1b + o, rb ? rb + o : nullptr);
 }
 
+}  // namespace afem
+
+#include "afem_fact.cuh"
+
+namespace afem {
+
 // The coarse end of the V-cycle in ONE block per vector: levels lo..L-1 are
 // small (<= kCoarseRows rows each), so their steps run back to back with
 // block barriers instead of one launch each.
@@ -685,13 +703,19 @@ struct CoarseLevel {
   // [B][n] buffers: t = the level's input r (l > lo), vs = s / sb, x2 = x2 / x2b,
   // u, w = the level's output x / rb (l > lo), g = the adjoint input, x1b
   float *t, *vs, *x2, *u, *w, *g, *x1b;
+  // factored smoother (fact != 0): x1 = G r kept for the post-smoothing, wpre = L r,
+  // wpost = L u, gpre = L x1b, gpost = L g, tmp = G g
+  int fact;
+  FactView f;
+  float *x1, *wpre, *wpost, *gpre, *gpost, *tmp;
 };
 struct CoarsePlan {
   int lo, L;
   CoarseLevel lev[kMaxLevels];
 };
 
-// forward: x_lo = V_lo(r_lo), keeping t, u per level for the backward
+// forward: x_lo = V_lo(r_lo), keeping t, u (and the factored smoothers' L r,
+// L u) per level for the backward
 __global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse(CoarsePlan plan, const float* __restrict__ r_lo,
                                                             float* __restrict__ x_lo) {
   pdl_trigger();
@@ -701,34 +725,63 @@ __global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse(CoarsePlan plan, con
   for (int l = lo; l + 1 < L; ++l) {   // pre-smoothing residual, restriction
     const CoarseLevel& A = plan.lev[l];
     const CoarseLevel& C = plan.lev[l + 1];
-    const float* r = (l == lo ? r_lo : A.t) + b * A.n;
-    float* s = A.vs + b * A.n;
-    vc_smooth_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, r, s);
+    const int64_t o = b * A.n;
+    const float* r = (l == lo ? r_lo : A.t) + o;
+    float* s = A.vs + o;
+    if (A.fact) {   // x1 = G r, s = r - A x1
+      fact_lower(i0, st, A.f, r, A.wpre + o);
+      __syncthreads();
+      fact_upper(i0, st, A.f, A.wpre + o, nullptr, nullptr, A.x1 + o);
+      __syncthreads();
+      vc_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, r, A.x1 + o, s);
+    } else {
+      vc_smooth_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, r, s);
+    }
     __syncthreads();
     vc_spmv(i0, st, C.n, A.pt_rp, A.pt_cols, A.pt_w, s, nullptr, nullptr, C.t + b * C.n);
     __syncthreads();
   }
   {
     const CoarseLevel& C = plan.lev[L - 1];
-    const float* r = (L - 1 == lo ? r_lo : C.t) + b * C.n;
-    float* x = (L - 1 == lo ? x_lo : C.w) + b * C.n;
-    for (int i = i0; i < C.n; i += st) x[i] = C.d[i] * r[i];
+    const int64_t o = b * C.n;
+    const float* r = (L - 1 == lo ? r_lo : C.t) + o;
+    float* x = (L - 1 == lo ? x_lo : C.w) + o;
+    if (C.fact) {
+      fact_lower(i0, st, C.f, r, C.wpre + o);
+      __syncthreads();
+      fact_upper(i0, st, C.f, C.wpre + o, nullptr, nullptr, x);
+    } else {
+      for (int i = i0; i < C.n; i += st) x[i] = C.d[i] * r[i];
+    }
     __syncthreads();
   }
-  for (int l = L - 2; l >= lo; --l) {   // prolongation + d r, post-smoothing
+  for (int l = L - 2; l >= lo; --l) {   // prolongation + x1, post-smoothing
     const CoarseLevel& A = plan.lev[l];
     const CoarseLevel& C = plan.lev[l + 1];
-    const float* r = (l == lo ? r_lo : A.t) + b * A.n;
-    float* x2 = A.x2 + b * A.n;
-    vc_spmv(i0, st, A.n, A.p_rp, A.p_cols, A.p_w, C.w + b * C.n, A.d, r, x2);
-    __syncthreads();
-    vc_post(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, r, x2, A.u + b * A.n, (l == lo ? x_lo : A.w) + b * A.n);
+    const int64_t o = b * A.n;
+    const float* r = (l == lo ? r_lo : A.t) + o;
+    float* x2 = A.x2 + o;
+    float* y = (l == lo ? x_lo : A.w) + o;
+    if (A.fact) {   // x2 = x1 + P x_{l+1}; u = r - A x2; y = x2 + G u
+      vc_spmv_add(i0, st, A.n, A.p_rp, A.p_cols, A.p_w, C.w + b * C.n, A.x1 + o, x2);
+      __syncthreads();
+      vc_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, r, x2, A.u + o);
+      __syncthreads();
+      fact_lower(i0, st, A.f, A.u + o, A.wpost + o);
+      __syncthreads();
+      fact_upper(i0, st, A.f, A.wpost + o, nullptr, x2, y);
+    } else {
+      vc_spmv(i0, st, A.n, A.p_rp, A.p_cols, A.p_w, C.w + b * C.n, A.d, r, x2);
+      __syncthreads();
+      vc_post(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, r, x2, A.u + o, y);
+    }
     __syncthreads();
   }
 }
 
 // backward: from the adjoint g_lo of x_lo, rb_lo (the adjoint of r_lo), and
-// per level g (the adjoint of the level's output) and x1b for the weights
+// per level g (the adjoint of the level's output) and x1b for the weights;
+// on factored levels also L g (gpost) and L x1b (gpre)
 __global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse_adjoint(CoarsePlan plan, const float* __restrict__ g_lo,
                                                                     float* __restrict__ rb_lo) {
   const int64_t b = blockIdx.y;
@@ -736,29 +789,55 @@ __global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse_adjoint(CoarsePlan p
   for (int l = lo; l + 1 < L; ++l) {   // adjoint of the post-smoothing, then of the prolongation
     const CoarseLevel& A = plan.lev[l];
     const CoarseLevel& C = plan.lev[l + 1];
-    const float* g = (l == lo ? g_lo : A.g) + b * A.n;
-    float* x2b = A.x2 + b * A.n;
-    vc_smooth_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, g, x2b);
+    const int64_t o = b * A.n;
+    const float* g = (l == lo ? g_lo : A.g) + o;
+    float* x2b = A.x2 + o;
+    if (A.fact) {   // x2b = g - A G g
+      fact_lower(i0, st, A.f, g, A.gpost + o);
+      __syncthreads();
+      fact_upper(i0, st, A.f, A.gpost + o, nullptr, nullptr, A.tmp + o);
+      __syncthreads();
+      vc_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, g, A.tmp + o, x2b);
+    } else {
+      vc_smooth_res(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, g, x2b);
+    }
     __syncthreads();
     vc_spmv(i0, st, C.n, A.pt_rp, A.pt_cols, A.pt_w, x2b, nullptr, nullptr, C.g + b * C.n);
     __syncthreads();
   }
   {
     const CoarseLevel& C = plan.lev[L - 1];
-    const float* g = (L - 1 == lo ? g_lo : C.g) + b * C.n;
-    float* rb = (L - 1 == lo ? rb_lo : C.w) + b * C.n;
-    for (int i = i0; i < C.n; i += st) rb[i] = C.d[i] * g[i];
+    const int64_t o = b * C.n;
+    const float* g = (L - 1 == lo ? g_lo : C.g) + o;
+    float* rb = (L - 1 == lo ? rb_lo : C.w) + o;
+    if (C.fact) {   // one use, out = G r: its adjoint terms as a pre-smoothing with x1b = g
+      fact_lower(i0, st, C.f, g, C.gpre + o);
+      __syncthreads();
+      fact_upper(i0, st, C.f, C.gpre + o, nullptr, nullptr, rb);
+    } else {
+      for (int i = i0; i < C.n; i += st) rb[i] = C.d[i] * g[i];
+    }
     __syncthreads();
   }
   for (int l = L - 2; l >= lo; --l) {   // adjoint of the restriction, then of the pre-smoothing
     const CoarseLevel& A = plan.lev[l];
     const CoarseLevel& C = plan.lev[l + 1];
-    const float* g = (l == lo ? g_lo : A.g) + b * A.n;
-    float* sb = A.vs + b * A.n;
+    const int64_t o = b * A.n;
+    const float* g = (l == lo ? g_lo : A.g) + o;
+    float* sb = A.vs + o;
+    float* rb = (l == lo ? rb_lo : A.w) + o;
     vc_spmv(i0, st, A.n, A.p_rp, A.p_cols, A.p_w, C.w + b * C.n, nullptr, nullptr, sb);
     __syncthreads();
-    vc_pre_adjoint(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, g, A.x2 + b * A.n, sb, A.x1b + b * A.n,
-                   (l == lo ? rb_lo : A.w) + b * A.n);
+    if (A.fact) {   // x1b = x2b - A sb ; rb = sb + G (g + x1b)
+      vc_pre_adjoint(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, g, A.x2 + o, sb, A.x1b + o, nullptr);
+      __syncthreads();
+      fact_lower(i0, st, A.f, A.x1b + o, A.gpre + o);
+      __syncthreads();
+      if (rb_lo || l != lo) fact_upper(i0, st, A.f, A.gpost + o, A.gpre + o, sb, rb);
+    } else {
+      vc_pre_adjoint(i0, st, A.n, A.a_rp, A.a_cols, A.a_w, A.d, g, A.x2 + o, sb, A.x1b + o,
+                     (l == lo && !rb_lo) ? nullptr : rb);
+    }
     __syncthreads();
   }
 }
@@ -1067,6 +1146,21 @@ struct afem_mpnn_s {
   float* tmpB = nullptr;                     // [B][n0]
   float* r32 = nullptr;                      // FCG staging [n0]
   float* z32 = nullptr;                      // FCG staging [n0]
+  // factored smoothers (the finest level and the levels of at most kFactRows rows)
+  struct Fact {
+    bool on = false;
+    int k = -1;                                // edge head index
+    int nlow = 0;
+    int32_t *low_rp = nullptr, *lo_col = nullptr, *lo_row = nullptr, *up_rp = nullptr, *up_e = nullptr;
+    int32_t* aidx = nullptr;                   // position of each lower edge in A_l's values
+    float *a_low = nullptr, *lval = nullptr, *sq = nullptr, *z = nullptr, *m = nullptr, *dz = nullptr;
+    float *gl_diag = nullptr, *gl_low = nullptr;
+    float* scal = nullptr;                     // theta, bound, dL/dtheta
+    int* istar = nullptr;
+    unsigned long long* packed = nullptr;
+    float *x1 = nullptr, *wpre = nullptr, *wpost = nullptr, *gpre = nullptr, *gpost = nullptr, *tmp = nullptr;
+  } fl[kMaxLevels];
+  int nfact = 0;
   afem::FcgWork* fcg = nullptr;              // FCG buffers and graph (created on first solve)
   bool pdl = false;                          // V-cycle kernels launched with programmatic dependent launch
   std::vector<void*> owned;
@@ -1110,6 +1204,80 @@ static int off_w1(int l) { return 3 * kF + l * (2 * kF * kF + kF); }
 static int off_w2(int l) { return off_w1(l) + kF * kF; }
 static int off_b(int l) { return off_w1(l) + 2 * kF * kF; }
 static int off_head(int NL, int l) { return 3 * kF + NL * (2 * kF * kF + kF) + l * (kF + 1); }
+static int off_edge(int NL, int L, int k) { return off_head(NL, L) + k * (kF + 1); }
+
+// The factored smoother's index structures of level l from the pattern of
+// A_l (host side, once): the strict lower entries in row order, their
+// positions in A_l's values, and the transposed index by column.
+static afem_status fact_setup(afem_mpnn net, int l, const CsrLevel& pat) {
+  auto& f = net->fl[l];
+  const int n = pat.nrow;
+  cudaStream_t s = net->ctx->stream;
+  std::vector<int32_t> rp(n + 1), cols(std::max<int64_t>(pat.nnz, 1));
+  AFEM_CUDA(cudaMemcpyAsync(rp.data(), pat.rp, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+  if (pat.nnz) AFEM_CUDA(cudaMemcpyAsync(cols.data(), pat.cols, sizeof(int32_t) * pat.nnz, cudaMemcpyDeviceToHost, s));
+  AFEM_CUDA(cudaStreamSynchronize(s));
+  std::vector<int32_t> low_rp(n + 1, 0), lo_col, lo_row, aidx;
+  for (int i = 0; i < n; ++i) {
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+      if (cols[k] < i) {
+        lo_col.push_back(cols[k]);
+        lo_row.push_back(i);
+        aidx.push_back(k);
+      }
+    low_rp[i + 1] = (int32_t)lo_col.size();
+  }
+  const int nlow = (int)lo_col.size();
+  std::vector<int32_t> up_rp(n + 1, 0), up_e(std::max(nlow, 1));
+  for (int e = 0; e < nlow; ++e) ++up_rp[lo_col[e] + 1];
+  for (int j = 0; j < n; ++j) up_rp[j + 1] += up_rp[j];
+  {
+    std::vector<int32_t> cur(up_rp.begin(), up_rp.end() - 1);
+    for (int e = 0; e < nlow; ++e) up_e[cur[lo_col[e]]++] = e;   // rows ascending within a column
+  }
+  const size_t ne = std::max(nlow, 1), B = net->max_batch;
+  f.on = true;
+  f.nlow = nlow;
+  AFEM_TRY(dalloc(net, (size_t)n + 1, &f.low_rp));
+  AFEM_TRY(dalloc(net, (size_t)n + 1, &f.up_rp));
+  AFEM_TRY(dalloc(net, ne, &f.lo_col));
+  AFEM_TRY(dalloc(net, ne, &f.lo_row));
+  AFEM_TRY(dalloc(net, ne, &f.up_e));
+  AFEM_TRY(dalloc(net, ne, &f.aidx));
+  for (float** p : {&f.a_low, &f.lval, &f.z, &f.m, &f.dz, &f.gl_low}) AFEM_TRY(dalloc(net, ne, p));
+  for (float** p : {&f.sq, &f.gl_diag}) AFEM_TRY(dalloc(net, (size_t)n, p));
+  for (float** p : {&f.x1, &f.wpre, &f.wpost, &f.gpre, &f.gpost, &f.tmp}) AFEM_TRY(dalloc(net, B * n, p));
+  AFEM_TRY(dalloc(net, 4, &f.scal));
+  AFEM_TRY(dalloc(net, 1, &f.istar));
+  AFEM_TRY(dalloc(net, 1, &f.packed));
+  AFEM_CUDA(cudaMemcpyAsync(f.low_rp, low_rp.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, s));
+  AFEM_CUDA(cudaMemcpyAsync(f.up_rp, up_rp.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, s));
+  if (nlow) {
+    AFEM_CUDA(cudaMemcpyAsync(f.lo_col, lo_col.data(), sizeof(int32_t) * nlow, cudaMemcpyHostToDevice, s));
+    AFEM_CUDA(cudaMemcpyAsync(f.lo_row, lo_row.data(), sizeof(int32_t) * nlow, cudaMemcpyHostToDevice, s));
+    AFEM_CUDA(cudaMemcpyAsync(f.up_e, up_e.data(), sizeof(int32_t) * nlow, cudaMemcpyHostToDevice, s));
+    AFEM_CUDA(cudaMemcpyAsync(f.aidx, aidx.data(), sizeof(int32_t) * nlow, cudaMemcpyHostToDevice, s));
+  }
+  AFEM_CUDA(cudaMemsetAsync(f.scal, 0, sizeof(float) * 4, s));
+  AFEM_CUDA(cudaStreamSynchronize(s));   // the host vectors go out of scope
+  return AFEM_OK;
+}
+
+static FactView fact_view(afem_mpnn net, int l) {
+  const auto& f = net->fl[l];
+  FactView v;
+  v.n = net->n[l];
+  v.nlow = f.nlow;
+  v.low_rp = f.low_rp;
+  v.lo_col = f.lo_col;
+  v.lo_row = f.lo_row;
+  v.up_rp = f.up_rp;
+  v.up_e = f.up_e;
+  v.lval = f.lval;
+  v.sq = f.sq;
+  v.theta = f.scal;
+  return v;
+}
 
 static afem_status refresh_weights(afem_mpnn net) {
   afem_context ctx = net->ctx;
@@ -1139,18 +1307,19 @@ static afem_status spmm(afem_mpnn net, const CsrLevel& S, const TIn* X, TOut* Y,
   return AFEM_OK;
 }
 
+// y = (dsc ? dsc .* tv : add, or 0) + M x, per vector of the batch
 static afem_status sweep(afem_mpnn net, const CsrLevel* M, int batch, const float* x, const float* dsc,
-                         const float* tv, float* y, int nrow) {
+                         const float* tv, float* y, int nrow, const float* add = nullptr) {
   dim3 grid(grid_for(net->ctx, nrow, 256, 8), batch);
   if (net->pdl)
     return M ? launch_pdl(net->ctx, net->ctx->stream, k_sweep, grid, 256, M->nrow, M->ncol, M->rp, M->cols, M->w, x,
-                          dsc, tv, y)
+                          dsc, tv, add, y)
              : launch_pdl(net->ctx, net->ctx->stream, k_sweep, grid, 256, nrow, 0, nullptr, nullptr, nullptr,
-                          nullptr, dsc, tv, y);
+                          nullptr, dsc, tv, add, y);
   if (M)
-    k_sweep<<<grid, 256, 0, net->ctx->stream>>>(M->nrow, M->ncol, M->rp, M->cols, M->w, x, dsc, tv, y);
+    k_sweep<<<grid, 256, 0, net->ctx->stream>>>(M->nrow, M->ncol, M->rp, M->cols, M->w, x, dsc, tv, add, y);
   else
-    k_sweep<<<grid, 256, 0, net->ctx->stream>>>(nrow, 0, nullptr, nullptr, nullptr, nullptr, dsc, tv, y);
+    k_sweep<<<grid, 256, 0, net->ctx->stream>>>(nrow, 0, nullptr, nullptr, nullptr, nullptr, dsc, tv, add, y);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "k_sweep", __FILE__, __LINE__);
   ++net->ctx->launches;
@@ -1224,6 +1393,26 @@ static afem_status check_tc(afem_mpnn net) {
 }
 
 // network forward on the coefficient features -> scalings d_l
+// The factored smoother of level l from the level's weights d_l and output
+// o_l: s = sqrt(d), the edge head and L's lower entries, then theta from the
+// row sums of |L^T L A_l|.
+static afem_status fact_values(afem_mpnn net, int l) {
+  afem_context ctx = net->ctx;
+  auto& f = net->fl[l];
+  const int nl = net->n[l];
+  const CsrLevel& A = net->Ac[l];
+  AFEM_TRY(launch(ctx, k_fact_sq, grid_for(ctx, nl, 256, 8), 256, 0, nl, (const float*)net->d[l], f.sq));
+  if (f.nlow)
+    AFEM_TRY(launch(ctx, k_fact_edges, grid_for(ctx, f.nlow, 256, 8), 256, 0, f.nlow, (const int32_t*)f.lo_row,
+                    (const int32_t*)f.lo_col, (const float*)f.a_low, (const bf16*)net->o[l],
+                    (const float*)(net->params + off_edge(net->NL, net->L, f.k)), (const float*)f.sq, f.z, f.m,
+                    f.lval));
+  AFEM_CUDA(cudaMemsetAsync(f.packed, 0, sizeof(unsigned long long), ctx->stream));
+  AFEM_TRY(launch(ctx, k_fact_rows, grid_for(ctx, nl, kFactRowBlock, 16), kFactRowBlock, 0, fact_view(net, l),
+                  (const int32_t*)A.rp, (const int32_t*)A.cols, (const float*)A.w, f.packed));
+  return launch(ctx, k_fact_theta, 1, 32, 0, (const unsigned long long*)f.packed, f.scal, f.scal + 1, f.istar);
+}
+
 static afem_status features_forward(afem_mpnn net) {
   afem_context ctx = net->ctx;
   const int n0 = net->n0, L = net->L;
@@ -1240,6 +1429,7 @@ static afem_status features_forward(afem_mpnn net) {
     if (l + 1 < L) AFEM_TRY(spmm<bf16, bf16>(net, net->R[l], net->o[l], net->h[l + 1], 0));
     AFEM_TRY(launch(ctx, k_head, grid_for(ctx, nl, 256, 8), 256, 0, nl, (const bf16*)net->o[l],
                     (const float*)(net->params + off_head(net->NL, l)), (const float*)net->base[l], net->d[l]));
+    if (net->fl[l].on) AFEM_TRY(fact_values(net, l));
   }
   AFEM_TRY(check_tc(net));
   net->scalings_valid = true;
@@ -1275,6 +1465,17 @@ static CoarsePlan coarse_plan(afem_mpnn net) {
     c.w = net->w[l];
     c.g = net->s[l];
     c.x1b = net->x1b[l];
+    const auto& f = net->fl[l];
+    c.fact = f.on;
+    if (f.on) {
+      c.f = fact_view(net, l);
+      c.x1 = f.x1;
+      c.wpre = f.wpre;
+      c.wpost = f.wpost;
+      c.gpre = f.gpre;
+      c.gpost = f.gpost;
+      c.tmp = f.tmp;
+    }
     if (l + 1 < net->L) {
       c.pt_rp = net->Pt[l].rp;
       c.pt_cols = net->Pt[l].cols;
@@ -1295,12 +1496,22 @@ static afem_status apply(afem_mpnn net, int batch, const float* r, float* z) {
   const bool keep = z == nullptr;
   if (!net->scalings_valid) AFEM_TRY(features_forward(net));
   net->t0 = r;
-  for (int l = 0; l < lo; ++l) {   // fine levels down: s = r - A (d r), r_{l+1} = P^T s
+  for (int l = 0; l < lo; ++l) {   // fine levels down: s = r - A (G r), r_{l+1} = P^T s
     const CsrLevel& A = net->Ac[l];
     const int nl = net->n[l];
     const float* rl = l == 0 ? r : net->t[l];
-    AFEM_TRY(launch_batch(net, k_vc_smooth_res, "k_vc_smooth_res", nl, batch, nl, (const int32_t*)A.rp,
-                          (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], rl, net->vs[l]));
+    const auto& f = net->fl[l];
+    if (f.on) {   // x1 = G r = theta L^T (L r), s = r - A x1
+      const FactView fv = fact_view(net, l);
+      AFEM_TRY(launch_batch(net, k_fact_lower, "k_fact_lower", nl, batch, fv, rl, f.wpre));
+      AFEM_TRY(launch_batch(net, k_fact_upper, "k_fact_upper", nl, batch, fv, (const float*)f.wpre,
+                            (const float*)nullptr, (const float*)nullptr, f.x1));
+      AFEM_TRY(launch_batch(net, k_vc_res, "k_vc_res", nl, batch, nl, (const int32_t*)A.rp, (const int32_t*)A.cols,
+                            (const float*)A.w, rl, (const float*)f.x1, net->vs[l]));
+    } else {
+      AFEM_TRY(launch_batch(net, k_vc_smooth_res, "k_vc_smooth_res", nl, batch, nl, (const int32_t*)A.rp,
+                            (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], rl, net->vs[l]));
+    }
     AFEM_TRY(sweep(net, &net->Pt[l], batch, net->vs[l], nullptr, nullptr, net->t[l + 1], net->n[l + 1]));
   }
   float* x0 = z ? z : net->w[0];
@@ -1314,14 +1525,26 @@ static afem_status apply(afem_mpnn net, int batch, const float* r, float* z) {
     if (e != cudaSuccess) return cuda_fail(e, "k_vc_coarse", __FILE__, __LINE__);
     ++net->ctx->launches;
   }
-  for (int l = lo - 1; l >= 0; --l) {   // fine levels up: x2 = d r + P x_{l+1}, post-smoothing
+  for (int l = lo - 1; l >= 0; --l) {   // fine levels up: x2 = x1 + P x_{l+1}, post-smoothing
     const CsrLevel& A = net->Ac[l];
     const int nl = net->n[l];
     const float* rl = l == 0 ? r : net->t[l];
-    AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], net->d[l], rl, net->x2[l], nl));
-    AFEM_TRY(launch_batch(net, k_vc_post, "k_vc_post", nl, batch, nl, (const int32_t*)A.rp, (const int32_t*)A.cols,
-                          (const float*)A.w, (const float*)net->d[l], rl, (const float*)net->x2[l],
-                          keep ? net->u[l] : (float*)nullptr, l == 0 ? x0 : net->w[l]));
+    float* y = l == 0 ? x0 : net->w[l];
+    const auto& f = net->fl[l];
+    if (f.on) {   // u = r - A x2, y = x2 + theta L^T (L u)
+      const FactView fv = fact_view(net, l);
+      AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], nullptr, nullptr, net->x2[l], nl, f.x1));
+      AFEM_TRY(launch_batch(net, k_vc_res, "k_vc_res", nl, batch, nl, (const int32_t*)A.rp, (const int32_t*)A.cols,
+                            (const float*)A.w, rl, (const float*)net->x2[l], net->u[l]));
+      AFEM_TRY(launch_batch(net, k_fact_lower, "k_fact_lower", nl, batch, fv, (const float*)net->u[l], f.wpost));
+      AFEM_TRY(launch_batch(net, k_fact_upper, "k_fact_upper", nl, batch, fv, (const float*)f.wpost,
+                            (const float*)nullptr, (const float*)net->x2[l], y));
+    } else {
+      AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], net->d[l], rl, net->x2[l], nl));
+      AFEM_TRY(launch_batch(net, k_vc_post, "k_vc_post", nl, batch, nl, (const int32_t*)A.rp,
+                            (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], rl,
+                            (const float*)net->x2[l], keep ? net->u[l] : (float*)nullptr, y));
+    }
   }
   return AFEM_OK;
 }
@@ -1333,9 +1556,19 @@ static afem_status apply_adjoint(afem_mpnn net, int batch) {
   for (int l = 0; l < lo; ++l) {   // adjoint of the post-smoothing, then of the prolongation
     const CsrLevel& A = net->Ac[l];
     const int nl = net->n[l];
-    AFEM_TRY(launch_batch(net, k_vc_smooth_res, "k_vc_smooth_res", nl, batch, nl, (const int32_t*)A.rp,
-                          (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], (const float*)net->s[l],
-                          net->x2[l]));
+    const auto& f = net->fl[l];
+    if (f.on) {   // x2b = g - A G g, keeping L g
+      const FactView fv = fact_view(net, l);
+      AFEM_TRY(launch_batch(net, k_fact_lower, "k_fact_lower", nl, batch, fv, (const float*)net->s[l], f.gpost));
+      AFEM_TRY(launch_batch(net, k_fact_upper, "k_fact_upper", nl, batch, fv, (const float*)f.gpost,
+                            (const float*)nullptr, (const float*)nullptr, f.tmp));
+      AFEM_TRY(launch_batch(net, k_vc_res, "k_vc_res", nl, batch, nl, (const int32_t*)A.rp, (const int32_t*)A.cols,
+                            (const float*)A.w, (const float*)net->s[l], (const float*)f.tmp, net->x2[l]));
+    } else {
+      AFEM_TRY(launch_batch(net, k_vc_smooth_res, "k_vc_smooth_res", nl, batch, nl, (const int32_t*)A.rp,
+                            (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l],
+                            (const float*)net->s[l], net->x2[l]));
+    }
     AFEM_TRY(sweep(net, &net->Pt[l], batch, net->x2[l], nullptr, nullptr, net->s[l + 1], net->n[l + 1]));
   }
   {
@@ -1347,13 +1580,22 @@ static afem_status apply_adjoint(afem_mpnn net, int batch) {
   for (int l = lo - 1; l >= 0; --l) {   // adjoint of the restriction, then of the pre-smoothing
     const CsrLevel& A = net->Ac[l];
     const int nl = net->n[l];
+    const auto& f = net->fl[l];
     AFEM_TRY(sweep(net, &net->P[l], batch, net->w[l + 1], nullptr, nullptr, net->vs[l], nl));
     AFEM_TRY(launch_batch(net, k_vc_pre_adjoint, "k_vc_pre_adjoint", nl, batch, nl, (const int32_t*)A.rp,
                           (const int32_t*)A.cols, (const float*)A.w, (const float*)net->d[l], (const float*)net->s[l],
                           (const float*)net->x2[l], (const float*)net->vs[l], net->x1b[l],
-                          l == 0 ? (float*)nullptr : net->w[l]));
+                          (l == 0 || f.on) ? (float*)nullptr : net->w[l]));
+    if (f.on) {   // L x1b, and rb = sb + theta L^T (L g + L x1b) above the finest level
+      const FactView fv = fact_view(net, l);
+      AFEM_TRY(launch_batch(net, k_fact_lower, "k_fact_lower", nl, batch, fv, (const float*)net->x1b[l], f.gpre));
+      if (l > 0)
+        AFEM_TRY(launch_batch(net, k_fact_upper, "k_fact_upper", nl, batch, fv, (const float*)f.gpost,
+                              (const float*)f.gpre, (const float*)net->vs[l], net->w[l]));
+    }
   }
   for (int l = 0; l < L; ++l) {
+    if (net->fl[l].on) continue;   // fact_backward
     const int nl = net->n[l];
     const bool last = l == L - 1;
     AFEM_TRY(launch(ctx, k_dc_vcycle, grid_for(ctx, nl, 256, 8), 256, 0, nl, batch, (const float*)net->d[l],
@@ -1408,6 +1650,46 @@ static afem_status dw_gemm2(afem_mpnn net, int64_t M, const bf16* X1, const bf16
 }
 
 // loss and gradients of the mean relative squared error over (r, e)
+// The factored levels' backward, after apply_adjoint: dL/dL (diagonal and
+// lower entries) and dL/dtheta from the stored vectors, theta's term through
+// its maximal row, then dL/dc of the level's weights, dz of the edge head and
+// its parameter gradient.
+static afem_status fact_backward(afem_mpnn net, int batch) {
+  afem_context ctx = net->ctx;
+  const int L = net->L;
+  for (int l = 0; l < L; ++l) {
+    auto& f = net->fl[l];
+    if (!f.on) continue;
+    const int nl = net->n[l];
+    const bool last = l == L - 1;
+    const FactView fv = fact_view(net, l);
+    const float* rl = l == 0 ? net->t0 : net->t[l];
+    const CsrLevel& A = net->Ac[l];
+    const unsigned nbk = grid_for(ctx, nl, 256, 2);
+    AFEM_TRY(ensure_part(net, std::max<int64_t>(nbk, (int64_t)grid_for(ctx, std::max(f.nlow, 1), 256, 2) * (kF + 1))));
+    // the coarsest level's single use out = G r enters as a pre-smoothing with x1b = g
+    AFEM_TRY(launch(ctx, k_fact_grad, nbk, 256, 0, fv, batch, rl, last ? (const float*)net->s[l] : net->x1b[l],
+                    (const float*)f.wpre, (const float*)f.gpre, last ? (const float*)nullptr : net->u[l],
+                    (const float*)net->s[l], (const float*)f.wpost, (const float*)f.gpost, f.gl_diag, f.gl_low,
+                    net->part));
+    AFEM_TRY(sum_partials(ctx, (int)nbk, 1, (const float*)net->part, f.scal + 2, 0));
+    AFEM_TRY(launch(ctx, k_fact_theta_grad, 1, 32, 0, fv, (const int32_t*)A.rp, (const int32_t*)A.cols,
+                    (const float*)A.w, (const float*)(f.scal + 1), (const int*)f.istar, (const float*)(f.scal + 2),
+                    f.gl_diag, f.gl_low));
+    AFEM_TRY(launch(ctx, k_fact_dc, grid_for(ctx, nl, 256, 8), 256, 0, fv, (const float*)f.m, (const float*)f.a_low,
+                    (const float*)f.gl_diag, (const float*)f.gl_low, (const float*)net->d[l],
+                    (const float*)net->base[l], net->dc[l]));
+    float* gedge = net->grads + off_edge(net->NL, L, f.k);
+    if (f.nlow) {
+      const unsigned nbe = grid_for(ctx, f.nlow, 256, 2);
+      AFEM_TRY(launch(ctx, k_fact_edge_backward, nbe, 256, 0, fv, (const float*)f.z, (const float*)f.a_low,
+                      (const float*)f.gl_low, (const bf16*)net->o[l], f.dz, net->part));
+      AFEM_TRY(sum_partials(ctx, (int)nbe, kF + 1, (const float*)net->part, gedge, 0));
+    }
+  }
+  return AFEM_OK;
+}
+
 static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, const float* e, double* loss_h) {
   afem_context ctx = net->ctx;
   cudaStream_t s = ctx->stream;
@@ -1429,8 +1711,9 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
     if (ce != cudaSuccess) return cuda_fail(ce, "k_energy", __FILE__, __LINE__);
     ctx->launches += 2;
   }
-  // adjoint V-cycle -> dL/dc_l per level ; heads
+  // adjoint V-cycle -> dL/dc_l per level (and the factored levels' edge heads) ; heads
   AFEM_TRY(apply_adjoint(net, batch));
+  AFEM_TRY(fact_backward(net, batch));
   for (int l = 0; l < L; ++l) {
     const int nl = net->n[l];
     const unsigned nbk = grid_for(ctx, nl, 256, 2);
@@ -1439,6 +1722,11 @@ static afem_status loss_and_gradients(afem_mpnn net, int batch, const float* r, 
                     (const float*)(net->params + off_head(net->NL, l)), net->dO[l], net->part));
     AFEM_TRY(sum_partials(ctx, (int)nbk, kF + 1, (const float*)net->part,
                     net->grads + off_head(net->NL, l), 0));
+    const auto& f = net->fl[l];
+    if (f.on && f.nlow)   // + the edge head's d o
+      AFEM_TRY(launch(ctx, k_fact_dO, grid_for(ctx, (int64_t)nl * 32, 256, 8), 256, 0, fact_view(net, l),
+                      (const float*)f.dz, (const bf16*)net->o[l],
+                      (const float*)(net->params + off_edge(net->NL, L, f.k)), net->dO[l]));
   }
   // network backward, coarsest level first: o_l gets its head gradient plus R_l^T dh_{l+1}
   for (int l = L - 1; l >= 0; --l) {
@@ -1535,7 +1823,12 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
   net->n0 = level_rows[0];
   net->coarse_lo = nb_levels - 1;
   while (net->coarse_lo > 0 && level_rows[net->coarse_lo - 1] <= kCoarseRows) --net->coarse_lo;
-  net->nparam = off_head(nb_layers, nb_levels);
+  for (int l = 0; l < nb_levels; ++l) {
+    if (l != 0 && level_rows[l] > kFactRows) continue;
+    if ((st = fact_setup(net, l, l == 0 ? net->S[0] : net->Ac[l])) != AFEM_OK) return cleanup(st);
+    net->fl[l].k = net->nfact++;
+  }
+  net->nparam = off_edge(nb_layers, nb_levels, net->nfact);
   const size_t B = max_batch;
   const size_t n0 = net->n0;
   if ((st = dalloc(net, (size_t)net->nparam, &net->params)) || (st = dalloc(net, (size_t)net->nparam, &net->grads)) ||
@@ -1647,6 +1940,12 @@ afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* rp, cons
     AFEM_CUDA(cudaMemcpyAsync(&missing, net->missing, sizeof(int), cudaMemcpyDeviceToHost, s));
     AFEM_CUDA(cudaStreamSynchronize(s));
     AFEM_CHECK_ARG(!missing, "afem_mpnn_set_operator: a coarse operator pattern misses entries of P^T A P");
+  }
+  for (int l = 0; l < net->L; ++l) {   // the factored levels' lower entries of A_l (FP32)
+    const auto& f = net->fl[l];
+    if (!f.on || !f.nlow) continue;
+    AFEM_TRY(launch(ctx, k_fact_gather, grid_for(ctx, f.nlow, 256), 256, 0, f.nlow, (const int32_t*)f.aidx,
+                    (const float*)net->Ac[l].w, f.a_low));
   }
   net->have_operator = true;
   net->scalings_valid = false;

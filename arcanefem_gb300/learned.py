@@ -352,6 +352,18 @@ class MPNN:
         self.n0 = hier.rows[0]
         self.levels = L
         self.layers = layers
+        # edge heads of the factored levels (the finest and those of at most FACT_ROWS rows)
+        self.nfact = (self.nparam - param_count(layers, L)) // (F + 1)
+        assert self.nfact == len(fact_levels(hier.rows)), (self.nfact, hier.rows)
+
+    def init_params(self, seed: int = 0, head_scale: float = 0.01, edge_scale: float = 0.0) -> np.ndarray:
+        """Initial parameters of this network (init_params); with edge_scale > 0
+        the edge heads get N(0, edge_scale) weights and biases instead of zeros."""
+        p = init_params(self.layers, self.levels, seed=seed, head_scale=head_scale, nfact=self.nfact)
+        if edge_scale > 0:
+            k = param_count(self.layers, self.levels)
+            p[k:] = np.random.default_rng(seed + 1).normal(0, edge_scale, p.size - k).astype(np.float32)
+        return p
 
     def set_params(self, p):
         t = torch.as_tensor(np.asarray(p, np.float32), device="cuda")
@@ -599,6 +611,6 @@ def setup(ctx: fem.Context, n=512, levels=9, layers=6, seed=7, max_batch=8):
     prob = DiffusionProblem(ctx, n=n, seed=seed)
     hier = Hierarchy(n, levels, prob.row_ptr, prob.cols)
     net = MPNN(ctx, hier, layers=layers, max_batch=max_batch)
-    net.set_params(init_params(net.layers, levels, seed))
+    net.set_params(net.init_params(seed))
     net.set_operator(prob.row_ptr, prob.cols, prob.values)
     return prob, hier, net

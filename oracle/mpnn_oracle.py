@@ -33,8 +33,7 @@ inverse instead of d_l * x:
 SPD by construction (L_l lower triangular with a positive diagonal) and with
 lambda_max(G_l A_l) < 2 by the row-sum bound, so the V-cycle stays SPD for any
 network output; with ew = eb = 0 it is the weighted Jacobi smoother above.
-theta_l takes part in the gradient (through the row that attains the
-maximum) on every factored level but the finest, where it is held constant.
+theta_l takes part in the gradient through the row that attains the maximum.
 
 trained on the relative energy norm of the error propagation
 ||(I - M A) e||_A^2 / ||e||_A^2, with the gradient -2 A (e - M r) of a
@@ -273,7 +272,7 @@ class Net:
         o = c["o"][l]
         Lf = sp.coo_matrix(f["Lf"])
         G = sp.csr_matrix((gL, (Lf.row, Lf.col)), shape=Lf.shape)   # duplicates summed: none on a pattern
-        if l != 0 and f["bound"] > SAFE:
+        if f["bound"] > SAFE:
             # theta = SAFE / bound: through the row i* that attains the bound
             db = dth * (-SAFE / f["bound"] ** 2)
             ist = f["istar"]

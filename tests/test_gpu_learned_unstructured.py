@@ -53,12 +53,13 @@ def test_algebraic_hierarchy_forward_and_gradient_match_oracle(cuda_ctx):
     layers = min(3, hier.levels)
     net = learned.MPNN(cuda_ctx, hier, layers=layers, max_batch=2)
     try:
-        params = learned.init_params(net.layers, hier.levels, seed=3, head_scale=0.1)
+        params = net.init_params(seed=3, head_scale=0.1, edge_scale=0.3)
         net.set_params(params)
         net.set_operator(rp, cols, vals)
         n = rp.numel() - 1
         A = sp.csr_matrix((vals.cpu().numpy(), cols.cpu().numpy(), rp.cpu().numpy()), shape=(n, n))
-        onet = MO.Net(A, hier.host_graph, hier.host_restr, hier.host_prol, layers=net.layers, bf16_round=True)
+        onet = MO.Net(A, hier.host_graph, hier.host_restr, hier.host_prol, layers=net.layers, bf16_round=True,
+                      fact_rows=MO.FACT_ROWS)
         rng = np.random.default_rng(1)
         free = (A.diagonal() < 1e20).astype(np.float64)   # errors on the free nodes only
         E = rng.standard_normal((2, n)) * free
@@ -87,7 +88,7 @@ def test_learned_solve_through_the_linear_system_matches_the_check_file(cuda_ctx
     hier = learned.AlgebraicHierarchy(rp, cols, vals, min_coarse=16)
     net = learned.MPNN(cuda_ctx, hier, layers=min(6, hier.levels), max_batch=8)
     try:
-        net.set_params(learned.init_params(net.layers, hier.levels, seed=7))
+        net.set_params(net.init_params(seed=7))
         ls.set_learned_preconditioner(net)
         opt = fem.solver_options(rtol=1e-12, max_iter=500, precond=fem.PRECOND_LEARNED, skip_forced_rows=True)
         info = ls.solve(opt)

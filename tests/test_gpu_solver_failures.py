@@ -126,7 +126,7 @@ def test_linear_system_solve_statuses(cuda_ctx):
 def test_learned_fcg_statuses(cuda_ctx):
     prob, hier, net = learned.setup(cuda_ctx, n=16, levels=3, layers=2, seed=1, max_batch=1)
     try:
-        net.set_params(learned.init_params(2, 3, seed=2, head_scale=0.1))
+        net.set_params(net.init_params(seed=2, head_scale=0.1))
         b = prob.rhs(np.random.default_rng(3))
         x = torch.zeros_like(b)
         with pytest.raises(fem.AfemError) as e:
