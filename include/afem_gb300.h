@@ -482,6 +482,15 @@ afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* row_ptr_d, con
  * the call that ran the network.
  * The cap keeps the V-cycle symmetric positive definite for any network
  * output; with c = 0 the smoother is l1-Jacobi at 0.8 of the cap.
+ * On the finest level and on every level of at most 2048 rows the smoother
+ * is a learned factored sparse approximate inverse instead of d_l * x:
+ *   G_l = theta_l L_l^T L_l,  L_l = (I + N_l) diag(sqrt d_l),
+ *   N_l,ij = m_ij sqrt(d_i d_j) A_l,ij  (strictly lower pattern of A_l),
+ *   m_ij = 2 tanh(ew_l . (o_i * o_j) + eb_l)  (an edge head on the level's
+ *   network output), theta_l = 1.9 / max(1.9, max_i sum_j |(L^T L A_l)_ij|):
+ * SPD by construction and with lambda_max(G_l A_l) < 2, so the V-cycle stays
+ * SPD; theta_l takes part in the gradient through the row that attains the
+ * bound.  Zero edge heads give the weighted-Jacobi smoother exactly.
  *
  * The caller provides the level hierarchy as device CSR matrices (FP32
  * weights): graph[l] (level l adjacency, symmetric; level 0 = the matrix
@@ -508,7 +517,9 @@ afem_status afem_mpnn_destroy(afem_mpnn net);
 /* nb_layers (1..nb_levels) message-passing layers run on levels
  * 0..nb_layers-1; deeper levels take the restricted output of the last layer.
  * Number of FP32 parameters.  Flat layout: W_in[2][64], b_in[64]; per layer
- * W1[64][64], W2[64][64], b[64]; then per level a head w[64], beta. */
+ * W1[64][64], W2[64][64], b[64]; then per level a head w[64], beta; then per
+ * factored level (level 0 and the levels of at most 2048 rows, in level
+ * order) an edge head ew[64], eb. */
 int afem_mpnn_param_count(afem_mpnn net);
 afem_status afem_mpnn_set_params(afem_mpnn net, const float* params_d);
 afem_status afem_mpnn_get_params(afem_mpnn net, float* params_d);
