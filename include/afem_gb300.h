@@ -266,8 +266,9 @@ afem_status afem_assemble_host_io(afem_context ctx, const afem_mesh_view* mesh, 
 /* Allocation-free assembly of the scalar Poisson P1 matrix.  No counterpart
  * in the reference: it serves callers that cannot let a library allocate
  * device memory (a host framework that owns all device allocations through
- * its own pool, or code running while a stream is captured into a CUDA
- * graph).  Same arguments and results as afem_assemble_poisson_p1, but no
+ * its own pool and budgets them, or a step loop that cannot afford the
+ * synchronisation a device allocation implies).  Same arguments and results
+ * as afem_assemble_poisson_p1, but no
  * context: the work runs on cuda_stream, and the element-row scratch is a
  * fixed 32 MiB device array inside the library, held by every GPU that loads
  * the library until the process exits.  Limit: 4,194,304 doubles of scratch,

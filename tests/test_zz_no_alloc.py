@@ -1,6 +1,7 @@
 """The allocation-free assembly entry point, for callers that cannot let the
-library allocate device memory (a framework that owns every device
-allocation through its own pool, or code running under stream capture).
+library allocate device memory (a framework that owns and budgets every
+device allocation through its own pool, or a step loop that cannot afford
+the synchronisation a device allocation implies).
 
 afem_assemble_poisson_p1_noalloc keeps its element rows in a fixed device
 array inside the library instead of a context's scratch arena.  This test
