@@ -5,10 +5,11 @@
 -div(k grad u) = f on an n x n triangle grid of the unit square (k = exp of a
 Gaussian random field, bump source, u = 0 on the boundary), solved to a 1e-8
 FP64 relative residual by flexible CG preconditioned with one V(1,1)-cycle
-whose smoother weights come from the message-passing network.  With --train
-the network is first trained on 2000 solver-generated pairs (the solver keeps
-the better parameter set); without it the network predicts its initial
-weights (l1-Jacobi smoothing).
+whose smoothers come from the message-passing network (per-node weights, and
+learned factored sparse approximate inverses on the finest and the coarse
+levels).  With --train the network is first trained on 2000 solver-generated
+pairs (the solver keeps the better parameter set); without it the network
+gives its initial smoothers (l1-Jacobi).
 """
 from __future__ import annotations
 

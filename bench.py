@@ -821,7 +821,8 @@ def run_learned(args):
         "speedup_vs_plain_fp64_cg_jacobi": cg_jac.solve_ms / kept.solve_ms,
         "speedup_vs_plain_fp64_cg_none": cg_none.solve_ms / kept.solve_ms,
         "network": ("6 message-passing layers, width 64, BF16 tcgen05 GEMMs (TMA-fed, FP32 accumulate in TMEM); predicts the "
-                    "per-node smoother weights of a V(1,1)-cycle on a 9-level Galerkin hierarchy"),
+                    "smoothers of a V(1,1)-cycle on a 9-level Galerkin hierarchy: per-node weights, and factored sparse "
+                    "approximate inverses theta L^T L (edge heads) on the finest and the coarse levels"),
         "training": {"pairs": 2000, "pair_generation_s": pairs_s, "train_s": train_s, "loss": rep["loss"],
                      "fcg_iterations_untrained": rep["iterations_untrained"],
                      "fcg_iterations_trained": rep["iterations_trained"], "kept": rep["kept"]},
