@@ -382,9 +382,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int kb = 0; kb < deg; kb += 32) {
       act = kb + lane < deg;
       if (act) {
-        const int64_t c = __ldg(nc_cell + b + kb + lane);
+        const int32_t* cp = cn + (int64_t)__ldg(nc_cell + b + kb + lane) * NPC;
 #pragma unroll
-        for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
+        for (int j = 0; j < NPC; ++j) v[j] = __ldg(cp + j);
         if (FILL) {
           li = __ldg(nc_local + b + kb + lane);
         } else {
@@ -404,8 +404,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         bool fresh = false;
         int h = 0;
         if (act) {
-          h = tab_insert(t.key, x, fresh);
-          full |= h < 0;
+          // one atomic settles the common case (an empty slot, or x already there);
+          // a slot held by another node sends the lane on to the probing loop
+          h = tab_hash(x);
+          const int32_t old = atomicCAS(t.key + h, -1, x);
+          fresh = old == -1;
+          if (!fresh && old != x) {
+            h = tab_insert(t.key, x, fresh);
+            full |= h < 0;
+          }
         }
         hs[r] = (int16_t)h;
         const unsigned fb = __ballot_sync(0xffffffffu, fresh);
