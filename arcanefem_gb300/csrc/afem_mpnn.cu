@@ -694,6 +694,7 @@ namespace afem {
 // small (<= kCoarseRows rows each), so their steps run back to back with
 // block barriers instead of one launch each.
 constexpr int kCoarseRows = 2048;
+constexpr int kExactRows = 320;   // the first level below the finest of at most this many rows is solved exactly
 constexpr int kCoarseBlock = 1024;
 
 struct CoarseLevel {
@@ -711,8 +712,23 @@ struct CoarseLevel {
 };
 struct CoarsePlan {
   int lo, L;
+  const float* minv;   // level L-1 solved exactly: x = minv r (row-major, symmetric), or nullptr
   CoarseLevel lev[kMaxLevels];
 };
+
+// y = M x for a dense row-major n x n M, one warp per row
+__device__ __forceinline__ void dense_matvec(int n, const float* __restrict__ M, const float* __restrict__ x,
+                                             float* __restrict__ y) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = w; i < n; i += nw) {
+    const float* row = M + (int64_t)i * n;
+    float acc = 0.f;
+    for (int j = lane; j < n; j += 32) acc = fmaf(row[j], x[j], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[i] = acc;
+  }
+}
 
 // forward: x_lo = V_lo(r_lo), keeping t, u (and the factored smoothers' L r,
 // L u) per level for the backward
@@ -746,7 +762,9 @@ __global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse(CoarsePlan plan, con
     const int64_t o = b * C.n;
     const float* r = (L - 1 == lo ? r_lo : C.t) + o;
     float* x = (L - 1 == lo ? x_lo : C.w) + o;
-    if (C.fact) {
+    if (plan.minv) {   // the exact level
+      dense_matvec(C.n, plan.minv, r, x);
+    } else if (C.fact) {
       fact_lower(i0, st, C.f, r, C.wpre + o);
       __syncthreads();
       fact_upper(i0, st, C.f, C.wpre + o, nullptr, nullptr, x);
@@ -810,7 +828,9 @@ __global__ void __launch_bounds__(kCoarseBlock) k_vc_coarse_adjoint(CoarsePlan p
     const int64_t o = b * C.n;
     const float* g = (L - 1 == lo ? g_lo : C.g) + o;
     float* rb = (L - 1 == lo ? rb_lo : C.w) + o;
-    if (C.fact) {   // one use, out = G r: its adjoint terms as a pre-smoothing with x1b = g
+    if (plan.minv) {   // the exact level: rb = minv g (symmetric), no parameter
+      dense_matvec(C.n, plan.minv, g, rb);
+    } else if (C.fact) {   // one use, out = G r: its adjoint terms as a pre-smoothing with x1b = g
       fact_lower(i0, st, C.f, g, C.gpre + o);
       __syncthreads();
       fact_upper(i0, st, C.f, C.gpre + o, nullptr, nullptr, rb);
@@ -1131,7 +1151,10 @@ struct afem_mpnn_s {
   float* dc[kMaxLevels] = {};                // dL/dc per level [n_l]
   float* t[kMaxLevels] = {};                 // level input r_l [B][n_l] (level 0: the caller's r, t0)
   const float* t0 = nullptr;
-  int coarse_lo = 0;                         // levels coarse_lo..L-1 run in the coarse-levels kernels
+  int coarse_lo = 0;                         // levels coarse_lo..Lv-1 run in the coarse-levels kernels
+  int ex = -1;                               // the level solved exactly (-1: none)
+  int Lv = 0;                                // levels the V-cycle uses: ex + 1, or L
+  float* minv = nullptr;                     // FP32 inverse of A_ex's nonzero rows' block [n_ex][n_ex]
   float* w[kMaxLevels] = {};                 // level output x_l (w[0] = M r in training); backward: rb_l
   float* s[kMaxLevels] = {};                 // adjoint g_l of the level output (s[0] = dL/dz)
   float* vs[kMaxLevels] = {};                // pre-smoothing residual s_l; backward: sb_l
@@ -1450,8 +1473,9 @@ static afem_status launch_batch(afem_mpnn net, Kernel k, const char* name, int n
 static CoarsePlan coarse_plan(afem_mpnn net) {
   CoarsePlan plan{};
   plan.lo = net->coarse_lo;
-  plan.L = net->L;
-  for (int l = plan.lo; l < net->L; ++l) {
+  plan.L = net->Lv;
+  plan.minv = net->ex >= 0 ? net->minv : nullptr;
+  for (int l = plan.lo; l < net->Lv; ++l) {
     CoarseLevel& c = plan.lev[l];
     c.n = net->n[l];
     c.a_rp = net->Ac[l].rp;
@@ -1476,7 +1500,7 @@ static CoarsePlan coarse_plan(afem_mpnn net) {
       c.gpost = f.gpost;
       c.tmp = f.tmp;
     }
-    if (l + 1 < net->L) {
+    if (l + 1 < net->Lv) {
       c.pt_rp = net->Pt[l].rp;
       c.pt_cols = net->Pt[l].cols;
       c.pt_w = net->Pt[l].w;
@@ -1597,7 +1621,11 @@ static afem_status apply_adjoint(afem_mpnn net, int batch) {
   for (int l = 0; l < L; ++l) {
     if (net->fl[l].on) continue;   // fact_backward
     const int nl = net->n[l];
-    const bool last = l == L - 1;
+    if (l >= net->Lv || l == net->ex) {   // no smoother of the network on this level
+      AFEM_CUDA(cudaMemsetAsync(net->dc[l], 0, sizeof(float) * nl, ctx->stream));
+      continue;
+    }
+    const bool last = l == net->Lv - 1;
     AFEM_TRY(launch(ctx, k_dc_vcycle, grid_for(ctx, nl, 256, 8), 256, 0, nl, batch, (const float*)net->d[l],
                     (const float*)net->base[l], (const float*)net->s[l], last ? (const float*)nullptr : net->u[l],
                     last ? (const float*)nullptr : net->x1b[l], l == 0 ? net->t0 : (const float*)net->t[l],
@@ -1661,7 +1689,7 @@ static afem_status fact_backward(afem_mpnn net, int batch) {
     auto& f = net->fl[l];
     if (!f.on) continue;
     const int nl = net->n[l];
-    const bool last = l == L - 1;
+    const bool last = l == net->Lv - 1;
     const FactView fv = fact_view(net, l);
     const float* rl = l == 0 ? net->t0 : net->t[l];
     const CsrLevel& A = net->Ac[l];
@@ -1821,10 +1849,15 @@ afem_status afem_mpnn_create(afem_context ctx, int nb_levels, int nb_layers, con
     }
   }
   net->n0 = level_rows[0];
-  net->coarse_lo = nb_levels - 1;
+  for (int l = 1; l < nb_levels && net->ex < 0; ++l)
+    if (level_rows[l] <= kExactRows) net->ex = l;
+  net->Lv = net->ex >= 0 ? net->ex + 1 : nb_levels;
+  net->coarse_lo = net->Lv - 1;
   while (net->coarse_lo > 0 && level_rows[net->coarse_lo - 1] <= kCoarseRows) --net->coarse_lo;
-  for (int l = 0; l < nb_levels; ++l) {
-    if (l != 0 && level_rows[l] > kFactRows) continue;
+  if (net->ex >= 0 && (st = dalloc(net, (size_t)level_rows[net->ex] * level_rows[net->ex], &net->minv)) != AFEM_OK)
+    return cleanup(st);
+  for (int l = 0; l < net->Lv; ++l) {
+    if (l == net->ex || (l != 0 && level_rows[l] > kFactRows)) continue;
     if ((st = fact_setup(net, l, l == 0 ? net->S[0] : net->Ac[l])) != AFEM_OK) return cleanup(st);
     net->fl[l].k = net->nfact++;
   }
@@ -1897,6 +1930,78 @@ afem_status afem_mpnn_get_params(afem_mpnn net, float* params_d) {
   return AFEM_OK;
 }
 
+namespace afem {
+
+// The exact level's inverse, on the host in FP64 once per operator: the block
+// of A_ex's nonzero rows (the rows of coarse Dirichlet nodes are empty) by a
+// Cholesky factorisation, inverted column by column, stored in FP32 with
+// zeros on the empty rows and columns.
+static afem_status exact_inverse(afem_mpnn net) {
+  const int l = net->ex, n = net->n[l];
+  const CsrLevel& A = net->Ac[l];
+  cudaStream_t s = net->ctx->stream;
+  std::vector<int32_t> rp(n + 1), cols(std::max<int64_t>(A.nnz, 1));
+  std::vector<double> v(std::max<int64_t>(A.nnz, 1));
+  AFEM_CUDA(cudaMemcpyAsync(rp.data(), A.rp, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+  if (A.nnz) {
+    AFEM_CUDA(cudaMemcpyAsync(cols.data(), A.cols, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToHost, s));
+    AFEM_CUDA(cudaMemcpyAsync(v.data(), net->ac64[l], sizeof(double) * A.nnz, cudaMemcpyDeviceToHost, s));
+  }
+  AFEM_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> act;   // the nonzero rows
+  std::vector<int> pos(n, -1);
+  for (int i = 0; i < n; ++i) {
+    bool nz = false;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) nz |= v[k] != 0.0;
+    if (nz) {
+      pos[i] = (int)act.size();
+      act.push_back(i);
+    }
+  }
+  const int m = (int)act.size();
+  std::vector<double> B((size_t)m * m, 0.0);
+  for (int i = 0; i < n; ++i) {
+    if (pos[i] < 0) continue;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+      if (pos[cols[k]] >= 0) B[(size_t)pos[i] * m + pos[cols[k]]] += v[k];
+  }
+  // B = C C^T (lower C in place)
+  for (int j = 0; j < m; ++j) {
+    double dj = B[(size_t)j * m + j];
+    for (int k = 0; k < j; ++k) dj -= B[(size_t)j * m + k] * B[(size_t)j * m + k];
+    if (!(dj > 0.0))
+      return fail(AFEM_ERR_BREAKDOWN, "afem_mpnn_set_operator: the operator of level %d (solved exactly) is not "
+                                      "positive definite", l);
+    const double cj = std::sqrt(dj);
+    B[(size_t)j * m + j] = cj;
+    for (int i = j + 1; i < m; ++i) {
+      double a = B[(size_t)i * m + j];
+      for (int k = 0; k < j; ++k) a -= B[(size_t)i * m + k] * B[(size_t)j * m + k];
+      B[(size_t)i * m + j] = a / cj;
+    }
+  }
+  std::vector<float> out((size_t)n * n, 0.f);
+  std::vector<double> y(m);
+  for (int c = 0; c < m; ++c) {   // column c of B^-1: C y = e_c, C^T x = y
+    for (int i = 0; i < m; ++i) {
+      double a = i == c ? 1.0 : 0.0;
+      for (int k = 0; k < i; ++k) a -= B[(size_t)i * m + k] * y[k];
+      y[i] = a / B[(size_t)i * m + i];
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      double a = y[i];
+      for (int k = i + 1; k < m; ++k) a -= B[(size_t)k * m + i] * y[k];
+      y[i] = a / B[(size_t)i * m + i];
+    }
+    for (int i = 0; i < m; ++i) out[(size_t)act[i] * n + act[c]] = (float)y[i];
+  }
+  AFEM_CUDA(cudaMemcpyAsync(net->minv, out.data(), sizeof(float) * out.size(), cudaMemcpyHostToDevice, s));
+  AFEM_CUDA(cudaStreamSynchronize(s));   // out goes out of scope
+  return AFEM_OK;
+}
+
+}  // namespace afem
+
 afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* rp, const int32_t* cols, const double* vals) {
   AFEM_CHECK_ARG(net && rp && cols && vals, "afem_mpnn_set_operator: null argument");
   AFEM_CHECK_ARG(n == net->n0, "afem_mpnn_set_operator: %d rows, network level 0 has %d", n, net->n0);
@@ -1941,6 +2046,7 @@ afem_status afem_mpnn_set_operator(afem_mpnn net, int n, const int32_t* rp, cons
     AFEM_CUDA(cudaStreamSynchronize(s));
     AFEM_CHECK_ARG(!missing, "afem_mpnn_set_operator: a coarse operator pattern misses entries of P^T A P");
   }
+  if (net->ex >= 0) AFEM_TRY(exact_inverse(net));
   for (int l = 0; l < net->L; ++l) {   // the factored levels' lower entries of A_l (FP32)
     const auto& f = net->fl[l];
     if (!f.on || !f.nlow) continue;
@@ -2249,8 +2355,13 @@ struct FcgWork {
   int nparts = 0;
   const void* key[5] = {};
   int key_chunk = 0;
-  GraphChunk* graph = nullptr;
-  ~FcgWork() { delete graph; }
+  GraphChunk* graph = nullptr;    // `chunk` iterations
+  GraphChunk* graph1 = nullptr;   // one iteration (the tail of a solve)
+  int64_t launches_chunk = 0, launches_one = 0;   // kernels per replay of each
+  ~FcgWork() {
+    delete graph;
+    delete graph1;
+  }
 };
 
 static void free_fcg_work(FcgWork* w) { delete w; }
@@ -2317,14 +2428,21 @@ afem_status afem::fcg_solve(afem_context ctx, int n, const int32_t* rp, const in
   AFEM_TRY(fcg_work(net, &w));
   if (!net->scalings_valid) AFEM_TRY(features_forward(net));
   const void* key[5] = {rp, cols, vals, x, skip};
-  if (!w->graph || w->key_chunk != chunk || !std::equal(key, key + 5, w->key)) {
+  if (!w->graph || !w->graph1 || w->key_chunk != chunk || !std::equal(key, key + 5, w->key)) {
     delete w->graph;
+    delete w->graph1;
     w->graph = new (std::nothrow) GraphChunk();
-    if (!w->graph) return fail(AFEM_ERR_OOM, "afem_fcg_solve: host allocation");
+    w->graph1 = new (std::nothrow) GraphChunk();
+    if (!w->graph || !w->graph1) return fail(AFEM_ERR_OOM, "afem_fcg_solve: host allocation");
     std::copy(key, key + 5, w->key);
     w->key_chunk = chunk;
-    afem_status cst = capture(ctx, *w->graph, [&](cudaStream_t s) -> afem_status {
-      for (int k = 0; k < chunk; ++k) {
+    afem_status cst = AFEM_OK;
+    const int64_t launches_start = ctx->launches;
+    int64_t launches0 = launches_start;
+    for (int gi = 0; gi < 2 && cst == AFEM_OK; ++gi) {
+      const int iters = gi == 0 ? chunk : 1;
+      cst = capture(ctx, gi == 0 ? *w->graph : *w->graph1, [&](cudaStream_t s) -> afem_status {
+      for (int k = 0; k < iters; ++k) {
         AFEM_TRY(dispatch_g(G, [&](auto g) {
           return launch_pdl(ctx, s, k_fcg_spmv<decltype(g)::value>, dim3(grid_rows), kSolveBlock, n, rp, cols, vals,
                             (const double*)w->p, (const double*)w->r, w->q, w->partials, w->st);
@@ -2339,9 +2457,14 @@ afem_status afem::fcg_solve(afem_context ctx, int n, const int32_t* rp, const in
       }
       return AFEM_OK;
     });
+      (gi == 0 ? w->launches_chunk : w->launches_one) = ctx->launches - launches0;
+      launches0 = ctx->launches;
+    }
+    ctx->launches = launches_start;   // counted when the graphs run
     if (cst != AFEM_OK) {
       delete w->graph;
-      w->graph = nullptr;
+      delete w->graph1;
+      w->graph = w->graph1 = nullptr;
       return cst;
     }
   }
@@ -2357,8 +2480,13 @@ afem_status afem::fcg_solve(afem_context ctx, int n, const int32_t* rp, const in
   if (st == AFEM_OK)
     st = launch(ctx, k_fcg_widen, grid_vec, kSolveBlock, 0, n, (const float*)net->z32, w->z, (const double*)w->q,
                 w->p, 1, w->partials, w->st);
-  const int per_iteration = 4 + 4 * net->coarse_lo + 1;
+  // Chunks of `chunk` iterations while at least that many remain, then single
+  // iterations: the remaining count is predicted from the residual's
+  // reduction since the previous read-back (iterations past convergence
+  // still launch their kernels, which only test the stop flag).
   FcgState hs{};
+  double rr_prev = 0.0;
+  int it_prev = 0;
   while (st == AFEM_OK) {
     cudaError_t ce = cudaMemcpyAsync(ctx->pinned, w->st, sizeof(FcgState), cudaMemcpyDeviceToHost, ctx->stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
@@ -2368,12 +2496,27 @@ afem_status afem::fcg_solve(afem_context ctx, int n, const int32_t* rp, const in
     }
     hs = *reinterpret_cast<FcgState*>(ctx->pinned);
     if (hs.done) break;
-    ce = cudaGraphLaunch(w->graph->exec, ctx->stream);
+    int left = chunk;   // launch a whole chunk unless fewer iterations are predicted
+    if (hs.iter > it_prev && rr_prev > 0.0 && hs.rr > 0.0 && hs.rr < rr_prev && hs.tol2 > 0.0) {
+      const double per_it = std::log(hs.rr / rr_prev) / (hs.iter - it_prev);   // log reduction of rr per iteration
+      const double need = std::log(hs.tol2 / hs.rr) / per_it;
+      if (need < chunk) left = std::max(1, (int)std::ceil(need - 1e-9));
+    }
+    rr_prev = hs.rr;
+    it_prev = hs.iter;
+    if (left >= chunk) {
+      ce = cudaGraphLaunch(w->graph->exec, ctx->stream);
+      ctx->launches += w->launches_chunk;
+    } else {
+      for (int k = 0; k < left && ce == cudaSuccess; ++k) {
+        ce = cudaGraphLaunch(w->graph1->exec, ctx->stream);
+        ctx->launches += w->launches_one;
+      }
+    }
     if (ce != cudaSuccess) {
       st = cuda_fail(ce, "cudaGraphLaunch", __FILE__, __LINE__);
       break;
     }
-    ctx->launches += (int64_t)per_iteration * chunk;
   }
   cudaEventRecord(e1, ctx->stream);
   cudaEventSynchronize(e1);
@@ -2401,7 +2544,7 @@ afem_status afem::fcg_solve(afem_context ctx, int n, const int32_t* rp, const in
 // per vector); the others one launch per V-cycle step.
 extern "C" afem_status afem_mpnn_set_coarse_rows(afem_mpnn net, int rows) {
   AFEM_CHECK_ARG(net && rows >= 0, "afem_mpnn_set_coarse_rows: bad arguments");
-  net->coarse_lo = net->L - 1;
+  net->coarse_lo = net->Lv - 1;
   while (net->coarse_lo > 0 && net->n[net->coarse_lo - 1] <= rows) --net->coarse_lo;
   if (net->fcg) {   // the captured FCG iteration depends on the split
     delete net->fcg->graph;

@@ -290,11 +290,23 @@ class AlgebraicHierarchy:
 
 
 FACT_ROWS = 2048   # the finest level and the levels of at most this many rows get the factored smoother
+EXACT_ROWS = 320   # the first level below the finest of at most this many rows is solved exactly
+
+
+def exact_level(sizes):
+    """The level the V-cycle solves exactly (and stops at), or None."""
+    for l, n in enumerate(sizes):
+        if l > 0 and n <= EXACT_ROWS:
+            return l
+    return None
 
 
 def fact_levels(sizes) -> list:
-    """The levels whose smoother is the learned factored sparse approximate inverse."""
-    return [l for l, n in enumerate(sizes) if l == 0 or n <= FACT_ROWS]
+    """The levels whose smoother is the learned factored sparse approximate
+    inverse: the finest and those of at most FACT_ROWS rows, above the exact level."""
+    ex = exact_level(sizes)
+    top = len(sizes) if ex is None else ex
+    return [l for l, n in enumerate(sizes[:top]) if l == 0 or n <= FACT_ROWS]
 
 
 def param_count(layers: int, levels: int, nfact: int = 0) -> int:

@@ -35,6 +35,10 @@ lambda_max(G_l A_l) < 2 by the row-sum bound, so the V-cycle stays SPD for any
 network output; with ew = eb = 0 it is the weighted Jacobi smoother above.
 theta_l takes part in the gradient through the row that attains the maximum.
 
+With an exact level (the first level below the finest of at most EXACT_ROWS
+rows), the V-cycle stops there and solves it with the inverse of the block of
+its nonzero rows (V_ex(r) = A_ex^+ r); the levels below are not used.
+
 trained on the relative energy norm of the error propagation
 ||(I - M A) e||_A^2 / ||e||_A^2, with the gradient -2 A (e - M r) of a
 symmetric A (as the GPU computes it); the backward pass is the adjoint of
@@ -53,6 +57,7 @@ import scipy.sparse as sp
 F = 64
 THETA = 0.8          # untrained smoother weight, as a fraction of the l1-Jacobi cap
 FACT_ROWS = 2048     # levels of at most this many rows (and the finest) get the factored smoother
+EXACT_ROWS = 320     # the first level (below the finest) of at most this many rows is solved exactly
 SAFE = 1.9           # the row-sum bound of theta_l G_l A_l
 
 
@@ -64,12 +69,24 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def fact_levels(sizes, fact_rows=FACT_ROWS):
+def exact_level(sizes, exact_rows=EXACT_ROWS):
+    """The level solved exactly (the V-cycle stops there), or None: the first
+    level below the finest of at most exact_rows rows."""
+    if exact_rows is None:
+        return None
+    for l, n in enumerate(sizes):
+        if l > 0 and n <= exact_rows:
+            return l
+    return None
+
+
+def fact_levels(sizes, fact_rows=FACT_ROWS, exact=None):
     """The levels that get the factored smoother: the finest and every level of
     at most fact_rows rows (none when fact_rows is None: diagonal smoothers only)."""
     if fact_rows is None:
         return []
-    return [l for l, n in enumerate(sizes) if l == 0 or n <= fact_rows]
+    top = len(sizes) if exact is None else exact
+    return [l for l, n in enumerate(sizes[:top]) if l == 0 or n <= fact_rows]
 
 
 def param_count(NL, L, nfact=0):
@@ -106,7 +123,7 @@ def level0_graph(A: sp.csr_matrix):
 
 
 class Net:
-    def __init__(self, A, graphs, restr, prol, layers=None, bf16_round=False, fact_rows=None):
+    def __init__(self, A, graphs, restr, prol, layers=None, bf16_round=False, fact_rows=None, exact_rows=None):
         self.A = sp.csr_matrix(A)
         self.S0, self.d = level0_graph(A)
         self.S = [self.S0] + list(graphs[1:])
@@ -125,8 +142,19 @@ class Net:
             self.base.append(np.where(l1 > 0, 2.0 / np.where(l1 > 0, l1, 1.0), 0.0))
         logd = np.log(self.d)
         self.x0 = np.stack([np.ones_like(logd), (logd - logd.mean()).astype(np.float32).astype(np.float64)], 1)
+        # exact level: the V-cycle uses levels 0 .. ex and solves level ex with the
+        # inverse of its nonzero rows' block (the rows of coarse Dirichlet nodes are empty)
+        sizes = [Al.shape[0] for Al in self.Al]
+        self.ex = exact_level(sizes, exact_rows)
+        self.Lv = self.L if self.ex is None else self.ex + 1
+        self.minv = None
+        if self.ex is not None:
+            Ae = self.Al[self.ex].toarray()
+            act = np.abs(Ae).sum(axis=1) > 0
+            self.minv = np.zeros_like(Ae)
+            self.minv[np.ix_(act, act)] = np.linalg.inv(Ae[np.ix_(act, act)])
         # factored levels: the strictly lower pattern of A_l (row i, column j < i, value A_ij)
-        self.fact = fact_levels([Al.shape[0] for Al in self.Al], fact_rows)
+        self.fact = fact_levels(sizes, fact_rows, self.ex)
         self.low = {}
         for l in self.fact:
             lo = sp.tril(self.Al[l], k=-1).tocoo()
@@ -194,10 +222,13 @@ class Net:
     def apply(self, c, r):
         """z = M r (one V(1,1)-cycle) and the per-level states (r_l, u_l) the
         backward pass needs."""
-        L = self.L
+        L = self.Lv
         st = [None] * L
 
         def V(l, r):
+            if l == self.ex:
+                st[l] = (r, None)
+                return self.minv @ r
             if l == L - 1:
                 st[l] = (r, None)
                 return self.smooth(c, l, r)
@@ -216,7 +247,7 @@ class Net:
         smoothers: acc["dd"][l] (diagonal levels: dL/dd_l) and, on factored
         levels, acc["gL"][l] (dL/dL_l on its diagonal and lower pattern, as a
         matrix) and acc["dth"][l] (dL/dtheta_l)."""
-        L = self.L
+        L = self.Lv
 
         def use(l, a, gbar):
             f = c["f"].get(l)
@@ -231,6 +262,8 @@ class Net:
 
         def B(l, g):
             r, u = st[l]
+            if l == self.ex:
+                return self.minv @ g                  # no parameter on the exact level
             if l == L - 1:
                 use(l, r, g)
                 return self.smooth(c, l, g)

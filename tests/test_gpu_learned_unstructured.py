@@ -59,7 +59,7 @@ def test_algebraic_hierarchy_forward_and_gradient_match_oracle(cuda_ctx):
         n = rp.numel() - 1
         A = sp.csr_matrix((vals.cpu().numpy(), cols.cpu().numpy(), rp.cpu().numpy()), shape=(n, n))
         onet = MO.Net(A, hier.host_graph, hier.host_restr, hier.host_prol, layers=net.layers, bf16_round=True,
-                      fact_rows=MO.FACT_ROWS)
+                      fact_rows=MO.FACT_ROWS, exact_rows=MO.EXACT_ROWS)
         rng = np.random.default_rng(1)
         free = (A.diagonal() < 1e20).astype(np.float64)   # errors on the free nodes only
         E = rng.standard_normal((2, n)) * free

@@ -150,3 +150,35 @@ def test_hierarchy_operators():
     G = learned.grid_graph(5)
     # 8-neighbour graph of a 5 x 5 grid: 2 x (20 horizontal + 20 vertical + 32 diagonal) directed edges
     assert abs(G - G.T).max() == 0 and G.nnz == 144
+
+
+def test_exact_coarse_level_gradient_and_spd():
+    """With an exact level (the first level below the finest of at most 320
+    rows: here level 1, 289 rows), the V-cycle stops there and solves it with
+    the inverse of its nonzero rows' block; the gradient (no parameter on that
+    level) still matches central finite differences, and M stays SPD."""
+    A, graphs, R, P, m = small_problem(n=32, levels=5)
+    A = symmetric_elimination(A, m)
+    net = MO.Net(A, graphs, R, P, layers=3, fact_rows=MO.FACT_ROWS, exact_rows=MO.EXACT_ROWS)
+    assert net.ex == 1 and net.Lv == 2 and net.fact == [0]
+    rng = np.random.default_rng(1)
+    params = learned.init_params(net.NL, net.L, seed=3, head_scale=0.2, nfact=net.nfact).astype(np.float64)
+    params[2 * 64:3 * 64] = 0.1
+    edges = MO.param_count(net.NL, net.L)
+    params[edges:] = rng.normal(0, 0.3, params.size - edges)
+    n = A.shape[0]
+    es = [rng.standard_normal(n) for _ in range(2)]
+    rs = [A @ e for e in es]
+    loss, g = net.loss_and_grad(params, rs, es)
+    idx = np.concatenate([rng.choice(edges, 30, replace=False), edges + np.arange(params.size - edges)])
+    eps = 1e-6
+    for i in idx:
+        p1, p2 = params.copy(), params.copy()
+        p1[i] += eps
+        p2[i] -= eps
+        fd = (net.loss_and_grad(p1, rs, es)[0] - net.loss_and_grad(p2, rs, es)[0]) / (2 * eps)
+        assert abs(fd - g[i]) <= 1e-4 * abs(fd) + 1e-8, (i, fd, g[i])
+    c = net.features(params)
+    M = operator_matrix(net, c, n)
+    assert np.abs(M - M.T).max() <= 1e-12 * np.abs(M).max()
+    assert np.linalg.eigvalsh(0.5 * (M + M.T)).min() > 0
