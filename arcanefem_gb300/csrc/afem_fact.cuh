@@ -1,7 +1,7 @@
 // Factored sparse-approximate-inverse smoothers of the learned V-cycle.
 //
-// On the finest level and on every level of at most kFactRows rows, the
-// V-cycle smooths with
+// On the finest level and on every level of at most kFactRows rows above the
+// level that is solved exactly, the V-cycle smooths with
 //
 //   G = theta L^T L,   L = (I + N) S,   S = diag(s),  s_i = sqrt(d_i),
 //   L_ii = s_i,  L_ij = N_ij s_j = m_ij A_ij s_i s_j^2   (j < i, A_ij != 0),

@@ -492,6 +492,12 @@ afem_status afem_spmv_csr(afem_context ctx, int n, const int32_t* row_ptr_d, con
  * SPD by construction and with lambda_max(G_l A_l) < 2, so the V-cycle stays
  * SPD; theta_l takes part in the gradient through the row that attains the
  * bound.  Zero edge heads give the weighted-Jacobi smoother exactly.
+ * The first level below the finest of at most 320 rows is solved exactly:
+ * the V-cycle stops there and applies the inverse of the block of that
+ * level's nonzero rows (FP64 Cholesky on the host in afem_mpnn_set_operator,
+ * applied in FP32); the levels below it are not used, and afem_mpnn_set_operator
+ * returns AFEM_ERR_BREAKDOWN if that block is not positive definite.  The
+ * factored levels are the finest and those of at most 2048 rows above it.
  *
  * The caller provides the level hierarchy as device CSR matrices (FP32
  * weights): graph[l] (level l adjacency, symmetric; level 0 = the matrix
@@ -519,8 +525,9 @@ afem_status afem_mpnn_destroy(afem_mpnn net);
  * 0..nb_layers-1; deeper levels take the restricted output of the last layer.
  * Number of FP32 parameters.  Flat layout: W_in[2][64], b_in[64]; per layer
  * W1[64][64], W2[64][64], b[64]; then per level a head w[64], beta; then per
- * factored level (level 0 and the levels of at most 2048 rows, in level
- * order) an edge head ew[64], eb. */
+ * factored level (level 0 and the levels of at most 2048 rows above the
+ * exact level, in level order) an edge head ew[64], eb.  Heads of levels at
+ * or below the exact level stay in the layout with zero gradients. */
 int afem_mpnn_param_count(afem_mpnn net);
 afem_status afem_mpnn_set_params(afem_mpnn net, const float* params_d);
 afem_status afem_mpnn_get_params(afem_mpnn net, float* params_d);
