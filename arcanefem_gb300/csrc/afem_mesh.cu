@@ -162,25 +162,23 @@ __device__ __forceinline__ int tab_find(const int32_t* key, int32_t v) {
 // One thread per node.  Its hash set of neighbours lives in shared memory,
 // interleaved across the block's threads (slot h of thread t at key[h][t]),
 // so that the 32 probes of a warp fall in 32 distinct banks whatever their
-// slots.  The thread streams its node's incidences in increasing order and
-// inserts the nodes other than n of each cell: the number of first insertions
-// D is the number of distinct neighbours and the row holds D + 1 entries (the
+// slots.  The thread streams its node's incidences in increasing order, the
+// cell nodes of each loaded two incidences ahead (CellStream), and inserts
+// the nodes other than n of each cell: the number of first insertions D is
+// the number of distinct neighbours and the row holds D + 1 entries (the
 // node itself included, as the reference's deg + 1 rows,
 // femutils/BSRFormat.cc:445-557).  With FILL the row is then written: the
-// rank of each neighbour among the others (counted against the thread's list
-// of them; no sort) gives its column position in either order, and every
-// incidence writes its NPC slot bytes (its own column first, then the other
-// cell nodes in increasing local index) in one packed store.  A row with more
-// neighbours than the table's 3/4 is appended to `defer` for
-// k_sparsity_rows_warp, and so are the light nodes of a warp that holds too
-// few of them.
+// neighbours, tagged with their insertion index, are sorted by a bitonic
+// network in registers (rows of up to 16 neighbours, 32 for hexahedra;
+// longer ones rank each neighbour by counting the smaller ones), which gives
+// each column's position in either order, and every incidence writes its
+// NPC slot bytes (its own column first, then the other cell nodes in
+// increasing local index) in one packed store.  A row with more neighbours
+// than the table's 3/4 is appended to `defer` for k_sparsity_rows_warp, and
+// so are the light nodes of a warp that holds too few of them.
 // Errors: bit 2 a row of more than kMaxRowLen entries, bit 4 a row_ptr that
 // does not match, bit 8 a node id out of range.
 constexpr int kThreadBlock = 128;
-// Nodes in more cells than this go to k_sparsity_rows_warp, whose lanes then
-// stay at least half busy (tetrahedral meshes: about 24 cells per node);
-// lower degrees (triangles, hexahedra, boundary nodes) stay here.
-constexpr int kThreadMaxDeg = 16;
 // A warp of k_sparsity_thread with fewer light nodes than this passes them on.
 constexpr int kThreadMinLanes = 12;
 
@@ -188,10 +186,102 @@ template <int NPC>
 struct ThreadTable {
   static constexpr int slots = NPC == 8 ? 64 : 32;   // power of two
   static constexpr int max_d = slots * 3 / 4;        // load factor at most 3/4
+  // Nodes in more cells than this go to k_sparsity_rows_warp, whose lanes
+  // then stay at least half busy and read the cells of one node together
+  // (tetrahedral meshes: about 24 cells per node, the others 4 to 8).
+  static constexpr int max_deg = 16;
+  // rows of at most sort_m neighbours are ranked by the sorting network, the
+  // insertion index in the low sort_bits bits of each key
+  static constexpr int sort_m = NPC == 8 ? 32 : 16;
+  static constexpr int sort_bits = NPC == 8 ? 5 : 4;
 };
 
 __device__ __forceinline__ void defer_node(int n, int32_t* defer, int32_t* defer_count) {
   defer[atomicAdd(defer_count, 1)] = n;
+}
+
+// The nodes of cell c (one or two 16-byte loads when cn is 16-byte aligned).
+template <int NPC>
+__device__ __forceinline__ void load_cell(const int32_t* __restrict__ cn, bool vec, int32_t c, int32_t (&v)[NPC]) {
+  const int32_t* cp = cn + (int64_t)c * NPC;
+  if constexpr (NPC == 4 || NPC == 8) {
+    if (vec) {
+#pragma unroll
+      for (int k = 0; k < NPC / 4; ++k) {
+        const int4 q = __ldg(reinterpret_cast<const int4*>(cp) + k);
+        v[4 * k] = q.x;
+        v[4 * k + 1] = q.y;
+        v[4 * k + 2] = q.z;
+        v[4 * k + 3] = q.w;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NPC; ++j) v[j] = __ldg(cp + j);
+}
+
+// The cells of incidences b, b + 1, ... < e in order: the nodes (and the
+// local index of the row's node) two incidences ahead, the cell ids three
+// ahead, so that a thread's dependent loads overlap its work on the earlier
+// incidences.
+template <int NPC>
+struct CellStream {
+  int32_t v0[NPC], v1[NPC];
+  int32_t c2, l0, l1;
+  __device__ __forceinline__ void start(const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_cell,
+                                        const uint8_t* __restrict__ nc_local, bool vec, int32_t b, int32_t e) {
+#pragma unroll
+    for (int j = 0; j < NPC; ++j) v0[j] = v1[j] = 0;
+    l0 = l1 = 0;
+    const int32_t c0 = b < e ? __ldg(nc_cell + b) : 0;
+    const int32_t c1 = b + 1 < e ? __ldg(nc_cell + b + 1) : 0;
+    c2 = b + 2 < e ? __ldg(nc_cell + b + 2) : 0;
+    if (b < e) load_cell<NPC>(cn, vec, c0, v0);
+    if (b + 1 < e) load_cell<NPC>(cn, vec, c1, v1);
+    if (nc_local) {
+      if (b < e) l0 = __ldg(nc_local + b);
+      if (b + 1 < e) l1 = __ldg(nc_local + b + 1);
+    }
+  }
+  // incidence p (b <= p < e): its cell nodes into v and its local index
+  __device__ __forceinline__ int next(const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_cell,
+                                      const uint8_t* __restrict__ nc_local, bool vec, int32_t p, int32_t e,
+                                      int32_t (&v)[NPC]) {
+    const int li = l0;
+#pragma unroll
+    for (int j = 0; j < NPC; ++j) {
+      v[j] = v0[j];
+      v0[j] = v1[j];
+    }
+    l0 = l1;
+    if (p + 2 < e) {
+      load_cell<NPC>(cn, vec, c2, v1);
+      if (nc_local) l1 = __ldg(nc_local + p + 2);
+    }
+    if (p + 3 < e) c2 = __ldg(nc_cell + p + 3);
+    return li;
+  }
+};
+
+// Ascending sort of M keys in registers (bitonic network, M a power of two).
+template <int M>
+__device__ __forceinline__ void bitonic_sort(uint32_t (&a)[M]) {
+#pragma unroll
+  for (int k = 2; k <= M; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        const int l = i ^ j;
+        if (l > i) {
+          const uint32_t lo = min(a[i], a[l]), hi = max(a[i], a[l]);
+          a[i] = (i & k) == 0 ? lo : hi;
+          a[l] = (i & k) == 0 ? hi : lo;
+        }
+      }
+    }
+  }
 }
 
 template <int NPC, bool FILL>
@@ -201,15 +291,18 @@ __global__ void __launch_bounds__(kThreadBlock)
                       const int32_t* __restrict__ row_ptr, int self_last, int packed_slots,
                       int32_t* __restrict__ row_len, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
                       int32_t* __restrict__ defer, int32_t* __restrict__ defer_count, int* __restrict__ err) {
-  constexpr int TS = ThreadTable<NPC>::slots, DMAX = ThreadTable<NPC>::max_d;
+  using TT = ThreadTable<NPC>;
+  constexpr int TS = TT::slots, DMAX = TT::max_d, M = TT::sort_m, SB = TT::sort_bits;
   __shared__ int32_t s_key[TS][kThreadBlock];
-  __shared__ int32_t s_val[FILL ? DMAX : 1][kThreadBlock];   // the neighbours in order of insertion
-  __shared__ uint8_t s_at[FILL ? DMAX : 1][kThreadBlock];    // their table slots
+  __shared__ uint8_t s_at[DMAX][kThreadBlock];              // table slot of each neighbour, in order of insertion
   __shared__ uint8_t s_pos[FILL ? TS : 1][kThreadBlock];     // position in the row, by table slot
   const int t = threadIdx.x;
 #pragma unroll
   for (int h = 0; h < TS; ++h) s_key[h][t] = -1;
   const int lane = t & 31;
+  const bool vec = (reinterpret_cast<uintptr_t>(cn) & 15) == 0;
+  // node ids below 2^(31 - SB) leave room for the insertion index in a sort key
+  const bool small_ids = nb_node <= (1 << (31 - SB));
   for (int n0 = blockIdx.x * kThreadBlock + (t & ~31); n0 < nb_node; n0 += gridDim.x * kThreadBlock) {
     const int n = n0 + lane;
     int32_t b = 0, e = 0;
@@ -217,7 +310,7 @@ __global__ void __launch_bounds__(kThreadBlock)
       b = __ldg(nc_ptr + n);
       e = __ldg(nc_ptr + n + 1);
     }
-    const bool light = n < nb_node && e - b <= kThreadMaxDeg;   // the others are k_sparsity_rows_warp's
+    const bool light = n < nb_node && e - b <= TT::max_deg;   // the others are k_sparsity_rows_warp's
     const unsigned lights = __ballot_sync(0xffffffffu, light);
     if (__popc(lights) < kThreadMinLanes) {
       // too few light nodes to keep this warp's lanes busy (the boundary of a
@@ -229,46 +322,45 @@ __global__ void __launch_bounds__(kThreadBlock)
       continue;
     }
     if (!light) continue;
-    int D = 0;
-    bool over = false, bad = false;
-    for (int32_t p = b; p < e && !over; ++p) {
-      const int64_t c = __ldg(nc_cell + p);
-      int32_t v[NPC];
+    int D = 0;   // distinct neighbours; above DMAX the row is deferred
+    bool bad = false;
+    {
+      CellStream<NPC> cs;
+      cs.start(cn, nc_cell, nullptr, vec, b, e);
+      for (int32_t p = b; p < e && D <= DMAX; ++p) {
+        int32_t v[NPC];
+        cs.next(cn, nc_cell, nullptr, vec, p, e, v);
 #pragma unroll
-      for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
-#pragma unroll
-      for (int j = 0; j < NPC; ++j) {
-        const int32_t x = v[j];
-        if (x == n || over) continue;
-        if ((unsigned)x >= (unsigned)nb_node) {
-          bad = true;
-          continue;
-        }
-        int h = tab_hash(x) & (TS - 1);
+        for (int j = 0; j < NPC; ++j) {
+          const int32_t x = v[j];
+          if (x == n) continue;
+          if ((unsigned)x >= (unsigned)nb_node) {
+            bad = true;
+            continue;
+          }
+          // the table never holds more than DMAX < TS keys: the probe meets x or an empty slot
+          int h = tab_hash(x) & (TS - 1);
 #pragma unroll 1
-        for (int q = 0; q < TS; ++q, h = (h + 1) & (TS - 1)) {
-          const int32_t k = s_key[h][t];
-          if (k == x) break;
-          if (k == -1) {
-            if (D == DMAX) {
-              over = true;
+          for (int q = 0; q < TS; ++q, h = (h + 1) & (TS - 1)) {
+            const int32_t k = s_key[h][t];
+            if (k == x) break;
+            if (k == -1) {
+              if (D < DMAX) {
+                s_key[h][t] = x;
+                s_at[D][t] = (uint8_t)h;
+              }
+              ++D;
               break;
             }
-            s_key[h][t] = x;
-            if (FILL) {
-              s_val[D][t] = x;
-              s_at[D][t] = (uint8_t)h;
-            }
-            ++D;
-            break;
           }
         }
       }
     }
+    const int stored = min(D, DMAX);
     if (bad) {
       atomicOr(err, 8);
       if (!FILL) row_len[n] = 0;
-    } else if (over) {
+    } else if (D > DMAX) {
       defer_node(n, defer, defer_count);
     } else if (!FILL) {
       row_len[n] = D + 1;
@@ -278,26 +370,46 @@ __global__ void __launch_bounds__(kThreadBlock)
         atomicOr(err, 4);
       } else {
         int own = 0;   // neighbours below n
-        for (int i = 0; i < D; ++i) {
-          const int32_t x = s_val[i][t];
-          int r = 0;
-          for (int u = 0; u < D; ++u) r += s_val[u][t] < x;
-          const int pos = self_last ? r : r + (n < x);
-          cols[rb + pos] = x;
-          s_pos[s_at[i][t]][t] = (uint8_t)pos;
-          own += x < n;
+        if (D <= M && small_ids) {
+          uint32_t a[M];
+#pragma unroll
+          for (int i = 0; i < M; ++i)
+            a[i] = i < D ? ((uint32_t)s_key[s_at[i][t]][t] << SB) | (uint32_t)i : 0xffffffffu;
+          bitonic_sort<M>(a);
+#pragma unroll
+          for (int i = 0; i < M; ++i) {
+            if (i < D) {
+              const int32_t x = (int32_t)(a[i] >> SB);
+              const int pos = self_last ? i : i + (n < x);
+              cols[rb + pos] = x;
+              s_pos[s_at[a[i] & (M - 1)][t]][t] = (uint8_t)pos;
+              own += x < n;
+            }
+          }
+        } else {
+          for (int i = 0; i < D; ++i) {
+            const int32_t x = s_key[s_at[i][t]][t];
+            int r = 0;
+            for (int u = 0; u < D; ++u) r += s_key[s_at[u][t]][t] < x;
+            const int pos = self_last ? r : r + (n < x);
+            cols[rb + pos] = x;
+            s_pos[s_at[i][t]][t] = (uint8_t)pos;
+            own += x < n;
+          }
         }
         const int pn = self_last ? D : own;
         cols[rb + pn] = n;
+        CellStream<NPC> cs;
+        cs.start(cn, nc_cell, nc_local, vec, b, e);
         for (int32_t p = b; p < e; ++p) {
-          const int64_t c = __ldg(nc_cell + p);
-          const int li = __ldg(nc_local + p);
+          int32_t v[NPC];
+          const int li = cs.next(cn, nc_cell, nc_local, vec, p, e, v);
           using Word = typename std::conditional<(NPC > 4), uint64_t, uint32_t>::type;
           Word word = (Word)pn;
 #pragma unroll
           for (int j = 0; j < NPC; ++j) {
             if (j == li) continue;
-            const int32_t x = __ldg(cn + c * NPC + j);
+            const int32_t x = v[j];
             Word q = (Word)pn;
             if (x != n) {
               int h = tab_hash(x) & (TS - 1);
@@ -320,13 +432,13 @@ __global__ void __launch_bounds__(kThreadBlock)
       }
     }
     // empty the table for the next node
-#pragma unroll
-    for (int h = 0; h < TS; ++h) s_key[h][t] = -1;
+    for (int i = 0; i < stored; ++i) s_key[s_at[i][t]][t] = -1;
   }
 }
 
 // The nodes in more than `min_deg` cells (every node when -1), and the rows
-// k_sparsity_thread deferred (more distinct neighbours than its per-thread table holds), listed
+// k_sparsity_thread deferred (more distinct neighbours than its per-thread
+// table holds), listed
 // in `list[0 .. *list_count)`: one warp per node, lanes over its incidences
 // (chunks of 32).  The row's own node is inserted into the warp's hash set
 // first, then every lane inserts the nodes of its cell: a node met again
@@ -361,6 +473,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   __syncwarp();
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool vec = (reinterpret_cast<uintptr_t>(cn) & 15) == 0;
   const int count = nb_node + *list_count;
   for (int it = wid; it < count; it += nwarps) {
     const int n = it < nb_node ? it : __ldg(list + (it - nb_node));
@@ -382,9 +495,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int kb = 0; kb < deg; kb += 32) {
       act = kb + lane < deg;
       if (act) {
-        const int32_t* cp = cn + (int64_t)__ldg(nc_cell + b + kb + lane) * NPC;
-#pragma unroll
-        for (int j = 0; j < NPC; ++j) v[j] = __ldg(cp + j);
+        load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + lane), v);
         if (FILL) {
           li = __ldg(nc_local + b + kb + lane);
         } else {
@@ -457,10 +568,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           if (deg > 32) {
             act = kb + lane < deg;
             if (act) {
-              const int64_t c = __ldg(nc_cell + b + kb + lane);
               li = __ldg(nc_local + b + kb + lane);
-#pragma unroll
-              for (int j = 0; j < NPC; ++j) v[j] = __ldg(cn + c * NPC + j);
+              load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + lane), v);
             }
           }
           if (!act) continue;
@@ -593,20 +702,21 @@ static afem_status launch_rows(afem_context ctx, bool dense, int nb_node, const 
   const unsigned g2 = (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock,
                                                   (int64_t)ctx->sm_count * per_sm_warp);
   return launch(ctx, k_sparsity_rows_warp<NPC, FILL>, g2, kWarpsPerBlock * 32, 0, nb_node,
-                dense ? -1 : kThreadMaxDeg, (const int32_t*)defer, (const int32_t*)defer_count, cn, nc_ptr, nc_cell,
-                nc_local, row_ptr, self_last, packed, row_len, cols, slot, err);
+                dense ? -1 : ThreadTable<NPC>::max_deg, (const int32_t*)defer, (const int32_t*)defer_count, cn,
+                nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed, row_len, cols, slot, err);
 }
 
 static afem_status launch_sparsity_rows(afem_context ctx, bool fill, int nb_node, int npc, const int32_t* cn,
                                         const int32_t* nc_ptr, const int32_t* nc_cell, const uint8_t* nc_local,
                                         const int32_t* row_ptr, int self_last, int32_t* row_len, int32_t* cols,
                                         uint8_t* slot, int32_t* defer, int32_t* defer_count, int* err) {
-  // Meshes whose nodes lie in more than kThreadMaxDeg cells on average
-  // (tetrahedra: about 24) run the warp kernel alone: in the thread kernel
-  // their few light nodes would only leave its lanes idle.
+  // Meshes whose nodes lie on average in more cells than the thread kernel
+  // takes (tetrahedra: about 24) run the warp kernel alone: in the thread
+  // kernel their few light nodes would only leave its lanes idle.
   int32_t incidences = 0;
   AFEM_TRY(read_scalar(ctx, nc_ptr + nb_node, &incidences));
-  const bool dense = incidences > (int64_t)kThreadMaxDeg * nb_node;
+  const int max_deg = npc == 3 ? ThreadTable<3>::max_deg : npc == 4 ? ThreadTable<4>::max_deg : ThreadTable<8>::max_deg;
+  const bool dense = incidences > (int64_t)max_deg * nb_node;
   // one packed store per incidence when the slot map is aligned to its rows
   const int packed = (reinterpret_cast<uintptr_t>(slot) % (npc == 8 ? 8 : 4)) == 0;
 #define AFEM_ROWS_LAUNCH(NPC)                                                                                    \

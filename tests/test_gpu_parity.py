@@ -674,12 +674,14 @@ def star_mesh(k):
     return coords, cells
 
 
-@pytest.mark.parametrize("k,self_last", [(8, False), (16, False), (16, True)])
+@pytest.mark.parametrize("k,self_last", [(8, False), (10, False), (10, True), (16, False), (16, True)])
 def test_rows_with_many_neighbours_per_cell_match_oracle(cuda_ctx, k, self_last):
-    """A node in at most 16 cells goes to the thread-per-node sparsity kernel;
-    with 2k > 24 distinct neighbours (k = 16) its row overflows that kernel's
-    table and is deferred to the warp kernel through the node list.  Structure,
-    slot map and values bit-exact in both column orders."""
+    """A node in at most 16 cells goes to the thread-per-node sparsity kernel,
+    which ranks up to 16 neighbours by a sorting network (k = 8) and 17 to 24
+    by counting (k = 10: 20 neighbours); with 2k > 24 distinct neighbours
+    (k = 16) its row overflows that kernel's table and is deferred to the warp
+    kernel through the node list.  Structure, slot map and values bit-exact in
+    both column orders."""
     coords, cells = star_mesh(k)
     n = coords.shape[0]
     f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
@@ -691,6 +693,56 @@ def test_rows_with_many_neighbours_per_cell_match_oracle(cuda_ctx, k, self_last)
     ptr, nc, _ = O.node_cell(n, cells)
     ref = O.assemble(O.POISSON_TRI3, coords, cells, ptr, nc, rp, cols)
     assert_bit_exact(f.values.cpu().numpy(), ref, "star rows")
+
+
+def delaunay_mesh(dim, npts, seed):
+    """Delaunay triangles / tetrahedra of random points in the unit square /
+    cube, nodes renumbered at random: uneven degrees (tetrahedra: 8 to over
+    60 cells per node, rows of 7 to over 30 entries)."""
+    spatial = pytest.importorskip("scipy.spatial")
+    rng = np.random.default_rng(seed)
+    pts = rng.random((npts, dim))
+    cells = spatial.Delaunay(pts).simplices.astype(np.int32)
+    perm = rng.permutation(npts).astype(np.int32)
+    coords = np.zeros((npts, 3))
+    coords[perm, :dim] = pts
+    return coords, perm[cells]
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("self_last", [False, True])
+@pytest.mark.parametrize("aligned", [True, False])
+def test_unstructured_sparsity_matches_oracle(cuda_ctx, dim, self_last, aligned):
+    """Unstructured meshes with randomly numbered nodes through both sparsity
+    kernels (triangles: a thread per node; tetrahedra, about 26 cells per
+    node: a warp per node).  With aligned=False the cell array starts 4 bytes
+    past a 16-byte boundary, so the cell nodes are read one by one instead of
+    in 16-byte loads.  Structure and slot map bit-exact; values bit-exact with
+    the aligned array (the assembly kernels require 16-byte aligned
+    cell_nodes)."""
+    coords, cells = delaunay_mesh(dim, 4000, seed=21)
+    n, npc = coords.shape[0], dim + 1
+    rp, cols = O.sparsity(n, cells, self_last=self_last)
+    ptr, nc, loc = O.node_cell(n, cells)
+    deg = np.diff(ptr)
+    buf = torch.zeros(cells.size + 4, dtype=torch.int32, device="cuda")
+    off = 0 if aligned else 1
+    buf[off:off + cells.size] = torch.as_tensor(cells.reshape(-1), device="cuda")
+    ce = buf[off:off + cells.size].view(-1, npc)
+    assert (ce.data_ptr() % 16 == 0) == aligned
+    mesh = fem.Mesh(dim, torch.as_tensor(coords, device="cuda"), ce)
+    f = fem.BSRFormat(cuda_ctx, mesh)
+    f.initialize(1, col_order=fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING)
+    f.compute_sparsity()
+    assert np.array_equal(f.row_ptr.cpu().numpy(), rp) and np.array_equal(f.cols.cpu().numpy(), cols)
+    slot = f.nc_slot.cpu().numpy().reshape(-1, npc)
+    node_of = np.repeat(np.arange(n), deg)
+    others = np.array([np.delete(row, li) for row, li in zip(cells[nc], loc)])
+    assert np.array_equal(cols[rp[node_of][:, None] + slot], np.concatenate([node_of[:, None], others], axis=1))
+    if aligned:
+        f.assemble_poisson()
+        ref = O.assemble(O.POISSON_TET4 if dim == 3 else O.POISSON_TRI3, coords, cells, ptr, nc, rp, cols)
+        assert_bit_exact(f.values.cpu().numpy(), ref, "unstructured mesh")
 
 
 @pytest.mark.parametrize("k", [255, 300])
