@@ -182,6 +182,7 @@ afem_status afem_context_destroy(afem_context ctx) {
   if (!ctx) return AFEM_OK;
   cudaError_t e = cudaSuccess;
   if (ctx->scratch) e = cudaFreeAsync(ctx->scratch, ctx->stream);
+  if (ctx->sp.buf) cudaFreeAsync(ctx->sp.buf, ctx->stream);
   cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
   if (ctx->copy_stream) {
     cudaStreamSynchronize(ctx->copy_stream);

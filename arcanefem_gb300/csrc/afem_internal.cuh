@@ -66,6 +66,22 @@ struct afem_context_s {
   // host -> device coordinate uploads overlapped with kernels (afem_assemble_host_io), created on first use
   cudaStream_t h2d_stream = nullptr;
   cudaEvent_t h2d_ev[17] = {};
+  // The rows, ascending and at padded offsets, and the slot map that
+  // afem_sparsity_rows found, kept for the next afem_sparsity_cols on the same
+  // mesh arrays (which then only copies them into place).
+  struct SparsityRows {
+    void* buf = nullptr;
+    size_t cap = 0;
+    int32_t* cols = nullptr;   // row n at (npc - 1) * nc_ptr[n] + n
+    int32_t* len = nullptr;    // [nb_node + 1] row lengths
+    uint8_t* slot = nullptr;   // [incidences * npc]
+    const int32_t* cn = nullptr;
+    const int32_t* nc_ptr = nullptr;
+    const int32_t* nc_cell = nullptr;
+    int nb_node = 0, npc = 0;
+    int64_t incidences = 0;
+    bool valid = false;
+  } sp;
   // element arithmetic of the assembly kernels (AFEM_FORMULATION_*)
   int formulation = AFEM_FORMULATION_REFERENCE;
   // device flag word (afem::kFlag*), set by kernels, read and cleared by check_flags

@@ -9,15 +9,19 @@
 //   their order, so the output is deterministic.
 //
 // node -> node sparsity (rows of the assembled matrix):
-//   one warp per node, one lane per incidence (chunks of 32): the nodes of
-//   the node's incident cells go into a hash set in shared memory; the
-//   number of distinct values is the row length = 1 + number of neighbours
-//   (femutils/BSRFormat.cc:445-557, row = deg + 1).  The second pass builds
-//   the same set, ranks each neighbour by counting the smaller ones in the
-//   set (broadcast reads, no sort), writes the columns (ascending or
-//   self-last) and, for every cell-node incidence, its position in the row
-//   (the slot map used by the assembly kernels) in one packed store.  Rows
-//   may hold up to 255 entries (the slot map is uint8); longer rows are
+//   one warp per node, one lane per incidence (chunks of 32), or one thread
+//   per node on meshes of few cells per node: the nodes of the node's
+//   incident cells go into a hash set in shared memory; the number of
+//   distinct values is the row length = 1 + number of neighbours
+//   (femutils/BSRFormat.cc:445-557, row = deg + 1).  The same pass ranks
+//   each neighbour, writes the columns (ascending or self-last) and, for
+//   every cell-node incidence, its position in the row (the slot map used by
+//   the assembly kernels) in one packed store.  afem_sparsity_rows runs it
+//   before the row starts are known, with each row at a padded offset
+//   ((npc - 1) * nc_ptr[n] + n bounds the rows before n), into a buffer the
+//   context keeps; afem_sparsity_cols then copies the rows into place, or,
+//   for other mesh arrays, runs the pass again with the real row starts.
+//   Rows may hold up to 255 entries (the slot map is uint8); longer rows are
 //   reported as mesh errors.
 #include <algorithm>
 #include <climits>
@@ -284,6 +288,23 @@ __device__ __forceinline__ void bitonic_sort(uint32_t (&a)[M]) {
   }
 }
 
+// Local index of node n in a cell (its first occurrence).  Without the
+// node -> cell local indices (afem_sparsity_rows) the slot bytes take n's
+// place from the cell itself; a cell that holds n twice is flagged (bit 16),
+// since there the two ways of numbering differ.
+template <int NPC>
+__device__ __forceinline__ int local_index(const int32_t (&v)[NPC], int32_t n, int* err) {
+  int li = -1, hits = 0;
+#pragma unroll
+  for (int j = NPC - 1; j >= 0; --j)
+    if (v[j] == n) {
+      li = j;
+      ++hits;
+    }
+  if (hits != 1) atomicOr(err, 16);
+  return li < 0 ? 0 : li;
+}
+
 template <int NPC, bool FILL>
 __global__ void __launch_bounds__(kThreadBlock)
     k_sparsity_thread(int nb_node, const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_ptr,
@@ -365,10 +386,17 @@ __global__ void __launch_bounds__(kThreadBlock)
     } else if (!FILL) {
       row_len[n] = D + 1;
     } else {
-      const int32_t rb = __ldg(row_ptr + n);
-      if (__ldg(row_ptr + n + 1) - rb != D + 1) {
-        atomicOr(err, 4);
+      // row_ptr null: the row goes to its padded place (afem_sparsity_rows)
+      int64_t rb = (int64_t)(NPC - 1) * b + n;
+      bool ok = true;
+      if (row_ptr) {
+        rb = __ldg(row_ptr + n);
+        ok = __ldg(row_ptr + n + 1) - (int32_t)rb == D + 1;
+        if (!ok) atomicOr(err, 4);
       } else {
+        row_len[n] = D + 1;
+      }
+      if (ok) {
         int own = 0;   // neighbours below n
         if (D <= M && small_ids) {
           uint32_t a[M];
@@ -403,7 +431,8 @@ __global__ void __launch_bounds__(kThreadBlock)
         cs.start(cn, nc_cell, nc_local, vec, b, e);
         for (int32_t p = b; p < e; ++p) {
           int32_t v[NPC];
-          const int li = cs.next(cn, nc_cell, nc_local, vec, p, e, v);
+          int li = cs.next(cn, nc_cell, nc_local, vec, p, e, v);
+          if (!nc_local) li = local_index<NPC>(v, n, err);
           using Word = typename std::conditional<(NPC > 4), uint64_t, uint32_t>::type;
           Word word = (Word)pn;
 #pragma unroll
@@ -496,8 +525,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       act = kb + lane < deg;
       if (act) {
         load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + lane), v);
-        if (FILL) {
+        if (FILL && nc_local) {
           li = __ldg(nc_local + b + kb + lane);
+        } else if (FILL) {
+          li = local_index<NPC>(v, n, err);
         } else {
           li = 0;
 #pragma unroll
@@ -544,9 +575,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         row_len[n] = (bad_w || too_long) ? 0 : D;
       }
     } else {
-      const int32_t rb = __ldg(row_ptr + n);
-      const bool ok = !bad_w && !too_long && __ldg(row_ptr + n + 1) - rb == D;
+      // row_ptr null: the row goes to its padded place (afem_sparsity_rows)
+      const int64_t rb = row_ptr ? (int64_t)__ldg(row_ptr + n) : (int64_t)(NPC - 1) * b + n;
+      const bool ok = !bad_w && !too_long && (!row_ptr || __ldg(row_ptr + n + 1) - (int32_t)rb == D);
       if (lane == 0 && !ok) atomicOr(err, bad_w ? 8 : too_long ? 2 : 4);
+      if (lane == 0 && !row_ptr) row_len[n] = ok ? D : 0;
       if (ok) {
         if (lane < 4) t.val[D + lane] = INT_MAX;
         __syncwarp();
@@ -568,8 +601,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           if (deg > 32) {
             act = kb + lane < deg;
             if (act) {
-              li = __ldg(nc_local + b + kb + lane);
               load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + lane), v);
+              li = nc_local ? __ldg(nc_local + b + kb + lane) : local_index<NPC>(v, n, err);
             }
           }
           if (!act) continue;
@@ -706,15 +739,14 @@ static afem_status launch_rows(afem_context ctx, bool dense, int nb_node, const 
                 nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed, row_len, cols, slot, err);
 }
 
-static afem_status launch_sparsity_rows(afem_context ctx, bool fill, int nb_node, int npc, const int32_t* cn,
-                                        const int32_t* nc_ptr, const int32_t* nc_cell, const uint8_t* nc_local,
-                                        const int32_t* row_ptr, int self_last, int32_t* row_len, int32_t* cols,
-                                        uint8_t* slot, int32_t* defer, int32_t* defer_count, int* err) {
+static afem_status launch_sparsity_rows(afem_context ctx, bool fill, int nb_node, int npc, int64_t incidences,
+                                        const int32_t* cn, const int32_t* nc_ptr, const int32_t* nc_cell,
+                                        const uint8_t* nc_local, const int32_t* row_ptr, int self_last,
+                                        int32_t* row_len, int32_t* cols, uint8_t* slot, int32_t* defer,
+                                        int32_t* defer_count, int* err) {
   // Meshes whose nodes lie on average in more cells than the thread kernel
   // takes (tetrahedra: about 24) run the warp kernel alone: in the thread
   // kernel their few light nodes would only leave its lanes idle.
-  int32_t incidences = 0;
-  AFEM_TRY(read_scalar(ctx, nc_ptr + nb_node, &incidences));
   const int max_deg = npc == 3 ? ThreadTable<3>::max_deg : npc == 4 ? ThreadTable<4>::max_deg : ThreadTable<8>::max_deg;
   const bool dense = incidences > (int64_t)max_deg * nb_node;
   // one packed store per incidence when the slot map is aligned to its rows
@@ -728,6 +760,94 @@ static afem_status launch_sparsity_rows(afem_context ctx, bool fill, int nb_node
   if (npc == 4) AFEM_ROWS_LAUNCH(4);
   AFEM_ROWS_LAUNCH(8);
 #undef AFEM_ROWS_LAUNCH
+}
+
+// afem_sparsity_cols after afem_sparsity_rows on the same mesh: each row,
+// found ascending at its padded offset, copied into place (self-last: the
+// row's own node moved to the end and its slot bytes renumbered to match).
+// Error bit 4: a row_ptr that does not match.
+// One thread per node (rows of ~7 to ~15 entries: triangles, tetrahedra).
+template <int NPC>
+__global__ void k_sparsity_place_thread(int nb_node, const int32_t* __restrict__ nc_ptr,
+                                        const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ pcols,
+                                        const int32_t* __restrict__ plen, const uint8_t* __restrict__ pslot,
+                                        int self_last, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
+                                        int* __restrict__ err) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb_node; n += gridDim.x * blockDim.x) {
+    const int32_t rb = __ldg(row_ptr + n);
+    const int len = __ldg(row_ptr + n + 1) - rb;
+    if (len != __ldg(plen + n)) {
+      atomicOr(err, 4);
+      continue;
+    }
+    const int32_t b = __ldg(nc_ptr + n);
+    const int32_t* src = pcols + (int64_t)(NPC - 1) * b + n;
+    if (!self_last) {
+      for (int i = 0; i < len; ++i) cols[rb + i] = __ldg(src + i);
+      continue;
+    }
+    int pn = 0;   // the node's own position in the ascending row
+    for (int i = 0; i < len; ++i)
+      if (__ldg(src + i) == n) pn = i;
+    for (int i = 0; i < len; ++i) cols[rb + (i == pn ? len - 1 : i - (i > pn))] = __ldg(src + i);
+    const int32_t e = __ldg(nc_ptr + n + 1);
+    for (int64_t q = (int64_t)NPC * b; q < (int64_t)NPC * e; ++q) {
+      const int v = __ldg(pslot + q);
+      slot[q] = (uint8_t)(v == pn ? len - 1 : v - (v > pn));
+    }
+  }
+}
+
+// A warp per 32 consecutive nodes, their rows copied one at a time across
+// the lanes so that reads and writes move in contiguous segments (hexahedra:
+// rows of ~27 entries, 64 slot bytes per incidence).
+template <int NPC>
+__global__ void k_sparsity_place_warp(int nb_node, const int32_t* __restrict__ nc_ptr, const int32_t* __restrict__ row_ptr,
+                                 const int32_t* __restrict__ pcols, const int32_t* __restrict__ plen,
+                                 const uint8_t* __restrict__ pslot, int self_last, int32_t* __restrict__ cols,
+                                 uint8_t* __restrict__ slot, int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < nb_node;
+       base += nwarps * 32) {
+    const int n = (int)base + lane;
+    int32_t rb = 0, b = 0, e = 0;
+    int len = 0;
+    if (n < nb_node) {
+      rb = __ldg(row_ptr + n);
+      len = __ldg(row_ptr + n + 1) - rb;
+      b = __ldg(nc_ptr + n);
+      e = __ldg(nc_ptr + n + 1);
+      if (len != __ldg(plen + n)) {
+        atomicOr(err, 4);
+        len = 0;
+      }
+    }
+    const int64_t src = (int64_t)(NPC - 1) * b + n;
+    const int rows = min(32, nb_node - (int)base);
+    for (int t = 0; t < rows; ++t) {
+      const int32_t rbt = __shfl_sync(0xffffffffu, rb, t);
+      const int lent = __shfl_sync(0xffffffffu, len, t);
+      const int64_t st = __shfl_sync(0xffffffffu, src, t);
+      if (!self_last) {
+        for (int i = lane; i < lent; i += 32) cols[rbt + i] = __ldg(pcols + st + i);
+        continue;
+      }
+      const int nt = (int)base + t;
+      int pn = 0;   // the node's own position in its ascending row
+      for (int i0 = 0; i0 < lent; i0 += 32) {
+        const unsigned hit = __ballot_sync(0xffffffffu, i0 + lane < lent && __ldg(pcols + st + i0 + lane) == nt);
+        if (hit) pn = i0 + __ffs(hit) - 1;
+      }
+      for (int i = lane; i < lent; i += 32) cols[rbt + (i == pn ? lent - 1 : i - (i > pn))] = __ldg(pcols + st + i);
+      const int64_t q0 = (int64_t)NPC * __shfl_sync(0xffffffffu, b, t);
+      const int64_t q1 = lent ? (int64_t)NPC * __shfl_sync(0xffffffffu, e, t) : q0;
+      for (int64_t q = q0 + lane; q < q1; q += 32) {
+        const int v = __ldg(pslot + q);
+        slot[q] = (uint8_t)(v == pn ? lent - 1 : v - (v > pn));
+      }
+    }
+  }
 }
 
 static afem_status sparsity_error(int herr, const char* fn) {
@@ -753,13 +873,55 @@ afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int
   AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &len));
   AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &defer));
   AFEM_TRY(scratch_take(ctx, 2, &err));
+  int32_t incidences = 0;
+  AFEM_TRY(read_scalar(ctx, nc_ptr_d + nb_node, &incidences));
   AFEM_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), ctx->stream));
-  AFEM_TRY(launch_sparsity_rows(ctx, false, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, nullptr, nullptr, 0, len,
-                                nullptr, nullptr, defer, err + 1, err));
-  AFEM_TRY(exclusive_scan_i32(ctx, len, row_ptr_d, nb_node));
+  // The whole rows (columns and slot map) in one pass, kept for
+  // afem_sparsity_cols, when the device has room for them; else the row
+  // lengths alone and afem_sparsity_cols finds the rows again.
+  auto& sp = ctx->sp;
+  sp.valid = false;
+  const size_t pcols = (size_t)(npc - 1) * incidences + nb_node;
+  const size_t bytes = align256(sizeof(int32_t) * pcols) + align256(sizeof(int32_t) * ((size_t)nb_node + 1)) +
+                       align256((size_t)npc * incidences);
+  if (bytes > sp.cap) {   // grows, kept until the context goes
+    if (sp.buf) AFEM_CUDA(cudaFreeAsync(sp.buf, ctx->stream));
+    sp.buf = nullptr;
+    sp.cap = 0;
+    if (cudaMallocAsync(&sp.buf, bytes, ctx->stream) == cudaSuccess) {
+      sp.cap = bytes;
+    } else {
+      (void)cudaGetLastError();
+      sp.buf = nullptr;
+    }
+  }
+  if (sp.buf) {
+    char* q = static_cast<char*>(sp.buf);
+    sp.cols = reinterpret_cast<int32_t*>(q);
+    sp.len = reinterpret_cast<int32_t*>(q + align256(sizeof(int32_t) * pcols));
+    sp.slot = reinterpret_cast<uint8_t*>(q + align256(sizeof(int32_t) * pcols) +
+                                         align256(sizeof(int32_t) * ((size_t)nb_node + 1)));
+    AFEM_TRY(launch_sparsity_rows(ctx, true, nb_node, npc, incidences, cell_nodes_d, nc_ptr_d, nc_cell_d, nullptr,
+                                  nullptr, 0, sp.len, sp.cols, sp.slot, defer, err + 1, err));
+    AFEM_TRY(exclusive_scan_i32(ctx, sp.len, row_ptr_d, nb_node));
+  } else {
+    AFEM_TRY(launch_sparsity_rows(ctx, false, nb_node, npc, incidences, cell_nodes_d, nc_ptr_d, nc_cell_d, nullptr,
+                                  nullptr, 0, len, nullptr, nullptr, defer, err + 1, err));
+    AFEM_TRY(exclusive_scan_i32(ctx, len, row_ptr_d, nb_node));
+  }
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
-  if (herr) return sparsity_error(herr, "afem_sparsity_rows");
+  if (herr & ~16) return sparsity_error(herr, "afem_sparsity_rows");
+  if (sp.buf) {
+    // a cell holding a node twice (bit 16): its slot bytes need the node -> cell local indices
+    sp.valid = (herr & 16) == 0;
+    sp.cn = cell_nodes_d;
+    sp.nc_ptr = nc_ptr_d;
+    sp.nc_cell = nc_cell_d;
+    sp.nb_node = nb_node;
+    sp.npc = npc;
+    sp.incidences = incidences;
+  }
   if (nnz_h) {
     int32_t nnz = 0;
     AFEM_TRY(read_scalar(ctx, row_ptr_d + nb_node, &nnz));
@@ -783,8 +945,25 @@ afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int
   AFEM_TRY(scratch_take(ctx, (size_t)nb_node + 1, &defer));
   AFEM_TRY(scratch_take(ctx, 2, &err));
   AFEM_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), ctx->stream));
-  AFEM_TRY(launch_sparsity_rows(ctx, true, nb_node, npc, cell_nodes_d, nc_ptr_d, nc_cell_d, nc_local_d, row_ptr_d,
-                                col_order == AFEM_COLS_SELF_LAST, nullptr, cols_d, nc_slot_d, defer, err + 1, err));
+  auto& sp = ctx->sp;
+  const bool self_last = col_order == AFEM_COLS_SELF_LAST;
+  if (sp.buf && sp.valid && sp.cn == cell_nodes_d && sp.nc_ptr == nc_ptr_d && sp.nc_cell == nc_cell_d &&
+      sp.nb_node == nb_node && sp.npc == npc) {
+    // the rows afem_sparsity_rows found on these mesh arrays, copied into place
+    auto kern = npc == 3 ? k_sparsity_place_thread<3> : npc == 4 ? k_sparsity_place_thread<4> : k_sparsity_place_warp<8>;
+    AFEM_TRY(launch(ctx, kern, grid_for(ctx, (int64_t)nb_node, 256), 256, 0, nb_node, nc_ptr_d, row_ptr_d,
+                    (const int32_t*)sp.cols, (const int32_t*)sp.len, (const uint8_t*)sp.slot, (int)self_last,
+                    cols_d, nc_slot_d, err));
+    if (!self_last)
+      AFEM_CUDA(cudaMemcpyAsync(nc_slot_d, sp.slot, (size_t)npc * sp.incidences, cudaMemcpyDeviceToDevice,
+                                ctx->stream));
+    sp.valid = false;
+  } else {
+    int32_t incidences = 0;
+    AFEM_TRY(read_scalar(ctx, nc_ptr_d + nb_node, &incidences));
+    AFEM_TRY(launch_sparsity_rows(ctx, true, nb_node, npc, incidences, cell_nodes_d, nc_ptr_d, nc_cell_d, nc_local_d,
+                                  row_ptr_d, (int)self_last, nullptr, cols_d, nc_slot_d, defer, err + 1, err));
+  }
   int herr = 0;
   AFEM_TRY(read_scalar(ctx, err, &herr));
   if (herr) return sparsity_error(herr, "afem_sparsity_cols");

@@ -100,6 +100,15 @@ enum {
  * number of distinct neighbours) and the total in *nnz_h (host, synchronous).
  * A row of more than 255 entries (the slot map below is uint8) or a node id
  * outside [0, nb_node) returns AFEM_ERR_MESH. nodes_per_cell: 3, 4 or 8.
+ * The pass that counts the rows also finds their columns and the slot map;
+ * the context keeps them for the next afem_sparsity_cols on the same
+ * cell_nodes_d / nc_ptr_d / nc_cell_d, which then only copies them into
+ * place.  Their buffer (about 4 (nodes_per_cell - 1) + nodes_per_cell bytes
+ * per incidence: 0.8 GB for 12.6 M tetrahedra) grows as needed and stays
+ * with the context until afem_context_destroy; without room for it the
+ * rows are counted alone and afem_sparsity_cols finds them again.  The mesh
+ * arrays must not change between the two calls (as row_ptr_d already
+ * requires).
  * Replaces computeRowIndexAtomicFree / computeRowIndex (BSRFormat.cc:562-573,
  * 912-924) and _buildOffsetsNodeWiseCsr (NodeWiseCsrBiliAssembly.cc:90-112). */
 afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int nodes_per_cell, const int32_t* cell_nodes_d,
@@ -109,9 +118,10 @@ afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int nodes_per_cell
  * nodes_per_cell * nodes_per_cell] (uint8): for incidence p of node n and
  * cell node j, the position inside row n of column cell_nodes[c][j].  The
  * slot map lets the assembly skip the reference's linear column search
- * (BSRFormat.h:449-462).  Replaces computeColumnsAtomicFree / computeColumns
- * (BSRFormat.cc:578-772, 929-971) and _buildMatrixNodeWiseCsr
- * (NodeWiseCsrBiliAssembly.cc:115-152). */
+ * (BSRFormat.h:449-462).  After afem_sparsity_rows on other mesh arrays (or
+ * without the kept rows) the columns are found again here.  Replaces
+ * computeColumnsAtomicFree / computeColumns (BSRFormat.cc:578-772, 929-971)
+ * and _buildMatrixNodeWiseCsr (NodeWiseCsrBiliAssembly.cc:115-152). */
 afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int nodes_per_cell, const int32_t* cell_nodes_d,
                                const int32_t* nc_ptr_d, const int32_t* nc_cell_d, const uint8_t* nc_local_d,
                                const int32_t* row_ptr_d, int col_order, int32_t* cols_d, uint8_t* nc_slot_d);

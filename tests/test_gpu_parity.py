@@ -73,6 +73,44 @@ def test_sparsity_bit_exact(cuda_ctx, name, self_last):
     assert np.array_equal(got_cols, expected)
 
 
+@pytest.mark.parametrize("self_last", [False, True])
+def test_sparsity_cols_finds_rows_itself_after_another_meshs_rows(cuda_ctx, self_last):
+    """afem_sparsity_cols copies the rows that afem_sparsity_rows kept only when
+    it is given the same mesh arrays; after a rows call on another mesh it runs
+    the full pass on its own.  Structure and slot map bit-exact both ways, and
+    again for the second mesh, whose kept rows the first call left alone."""
+    import ctypes as C
+
+    from arcanefem_gb300._capi import call
+    order = fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING
+    ms = [MESHES["tet_9"](), MESHES["tet_3"]()]
+    fs = []
+    for m in ms:
+        f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(m.dim, m.coords, m.cells))
+        f.initialize(1, col_order=order)
+        f.row_ptr = torch.empty(m.nb_node + 1, dtype=torch.int32, device="cuda")
+        fs.append(f)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    nnz = []
+    for f in fs:
+        k = C.c_int64()
+        call("afem_sparsity_rows", cuda_ctx.handle, f.mesh.nb_node, f.mesh.npc, p(f.mesh.cells), p(f.nc_ptr),
+             p(f.nc_cell), p(f.row_ptr), C.byref(k))
+        nnz.append(int(k.value))
+    for f, k, m in zip(fs, nnz, ms):   # the first mesh's rows are no longer kept
+        cols = torch.empty(k, dtype=torch.int32, device="cuda")
+        slot = torch.empty(m.nb_cell * m.npc * m.npc, dtype=torch.uint8, device="cuda")
+        call("afem_sparsity_cols", cuda_ctx.handle, m.nb_node, m.npc, p(f.mesh.cells), p(f.nc_ptr), p(f.nc_cell),
+             p(f.nc_local), p(f.row_ptr), order, p(cols), p(slot))
+        rp, ref = O.sparsity(m.nb_node, m.cells, self_last=self_last)
+        assert np.array_equal(f.row_ptr.cpu().numpy(), rp) and np.array_equal(cols.cpu().numpy(), ref)
+        ptr, nc, loc = O.node_cell(m.nb_node, m.cells)
+        node_of = np.repeat(np.arange(m.nb_node), np.diff(ptr))
+        got = ref[rp[node_of][:, None] + slot.cpu().numpy().reshape(-1, m.npc)]
+        others = np.array([np.delete(row, li) for row, li in zip(m.cells[nc], loc)])
+        assert np.array_equal(got, np.concatenate([node_of[:, None], others], axis=1))
+
+
 @pytest.fixture
 def formulation_ctx(cuda_ctx):
     """The shared context; the formulation a test sets is put back afterwards."""
