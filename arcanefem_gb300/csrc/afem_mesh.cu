@@ -767,12 +767,16 @@ static afem_status launch_sparsity_rows(afem_context ctx, bool fill, int nb_node
 // row's own node moved to the end and its slot bytes renumbered to match).
 // Error bit 4: a row_ptr that does not match.
 // One thread per node (rows of ~7 to ~15 entries: triangles, tetrahedra).
+// With n16 > 0 (ascending order, both slot maps 16-byte aligned) the same
+// launch also copies the slot map's first n16 16-byte chunks.
 template <int NPC>
 __global__ void k_sparsity_place_thread(int nb_node, const int32_t* __restrict__ nc_ptr,
                                         const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ pcols,
                                         const int32_t* __restrict__ plen, const uint8_t* __restrict__ pslot,
                                         int self_last, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
-                                        int* __restrict__ err) {
+                                        int* __restrict__ err, int64_t n16) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
+    reinterpret_cast<int4*>(slot)[i] = __ldg(reinterpret_cast<const int4*>(pslot) + i);
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb_node; n += gridDim.x * blockDim.x) {
     const int32_t rb = __ldg(row_ptr + n);
     const int len = __ldg(row_ptr + n + 1) - rb;
@@ -803,9 +807,11 @@ __global__ void k_sparsity_place_thread(int nb_node, const int32_t* __restrict__
 // rows of ~27 entries, 64 slot bytes per incidence).
 template <int NPC>
 __global__ void k_sparsity_place_warp(int nb_node, const int32_t* __restrict__ nc_ptr, const int32_t* __restrict__ row_ptr,
-                                 const int32_t* __restrict__ pcols, const int32_t* __restrict__ plen,
-                                 const uint8_t* __restrict__ pslot, int self_last, int32_t* __restrict__ cols,
-                                 uint8_t* __restrict__ slot, int* __restrict__ err) {
+                                      const int32_t* __restrict__ pcols, const int32_t* __restrict__ plen,
+                                      const uint8_t* __restrict__ pslot, int self_last, int32_t* __restrict__ cols,
+                                      uint8_t* __restrict__ slot, int* __restrict__ err, int64_t n16) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
+    reinterpret_cast<int4*>(slot)[i] = __ldg(reinterpret_cast<const int4*>(pslot) + i);
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t base = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < nb_node;
@@ -909,8 +915,12 @@ afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int
                                   nullptr, 0, len, nullptr, nullptr, defer, err + 1, err));
     AFEM_TRY(exclusive_scan_i32(ctx, len, row_ptr_d, nb_node));
   }
-  int herr = 0;
-  AFEM_TRY(read_scalar(ctx, err, &herr));
+  // the error bits and the total in one read-back
+  int32_t* hb = reinterpret_cast<int32_t*>(ctx->pinned);
+  AFEM_CUDA(cudaMemcpyAsync(hb, err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  AFEM_CUDA(cudaMemcpyAsync(hb + 1, row_ptr_d + nb_node, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  AFEM_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int herr = hb[0];
   if (herr & ~16) return sparsity_error(herr, "afem_sparsity_rows");
   if (sp.buf) {
     // a cell holding a node twice (bit 16): its slot bytes need the node -> cell local indices
@@ -922,11 +932,7 @@ afem_status afem_sparsity_rows(afem_context ctx, int nb_node, int npc, const int
     sp.npc = npc;
     sp.incidences = incidences;
   }
-  if (nnz_h) {
-    int32_t nnz = 0;
-    AFEM_TRY(read_scalar(ctx, row_ptr_d + nb_node, &nnz));
-    *nnz_h = nnz;
-  }
+  if (nnz_h) *nnz_h = hb[1];
   return AFEM_OK;
 }
 
@@ -951,12 +957,18 @@ afem_status afem_sparsity_cols(afem_context ctx, int nb_node, int npc, const int
       sp.nb_node == nb_node && sp.npc == npc) {
     // the rows afem_sparsity_rows found on these mesh arrays, copied into place
     auto kern = npc == 3 ? k_sparsity_place_thread<3> : npc == 4 ? k_sparsity_place_thread<4> : k_sparsity_place_warp<8>;
+    // ascending order: the slot map is copied as it is, by the thread-per-node
+    // launch when aligned (measured: 2D 0.071 -> 0.062 ms; the hexahedral
+    // warp copy is faster beside a separate copy of its 64-byte slot words)
+    const size_t sbytes = (size_t)npc * sp.incidences;
+    const int64_t n16 =
+        (!self_last && npc != 8 && ((uintptr_t)nc_slot_d & 15) == 0) ? (int64_t)(sbytes / 16) : 0;
     AFEM_TRY(launch(ctx, kern, grid_for(ctx, (int64_t)nb_node, 256), 256, 0, nb_node, nc_ptr_d, row_ptr_d,
                     (const int32_t*)sp.cols, (const int32_t*)sp.len, (const uint8_t*)sp.slot, (int)self_last,
-                    cols_d, nc_slot_d, err));
-    if (!self_last)
-      AFEM_CUDA(cudaMemcpyAsync(nc_slot_d, sp.slot, (size_t)npc * sp.incidences, cudaMemcpyDeviceToDevice,
-                                ctx->stream));
+                    cols_d, nc_slot_d, err, n16));
+    if (!self_last && sbytes > (size_t)n16 * 16)
+      AFEM_CUDA(cudaMemcpyAsync(nc_slot_d + n16 * 16, sp.slot + n16 * 16, sbytes - (size_t)n16 * 16,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
     sp.valid = false;
   } else {
     int32_t incidences = 0;
