@@ -111,6 +111,27 @@ def test_sparsity_cols_finds_rows_itself_after_another_meshs_rows(cuda_ctx, self
         assert np.array_equal(got, np.concatenate([node_of[:, None], others], axis=1))
 
 
+def test_cell_repeating_a_node_gives_the_oracles_structure(cuda_ctx):
+    """A cell that lists a node twice: its two incidences of that node number
+    their slot bytes by their own local index, which only the node -> cell
+    local indices tell apart; the rows pass flags it and the columns pass
+    finds the rows again with those indices.  Structure and slot map equal to
+    the oracle's."""
+    m = MESHES["tet_3"]()
+    cells = m.cells.copy()
+    cells[5, 2] = cells[5, 1]
+    f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(3, m.coords, cells))
+    f.initialize(1)
+    f.compute_sparsity()
+    rp, cols = O.sparsity(m.nb_node, cells)
+    assert np.array_equal(f.row_ptr.cpu().numpy(), rp) and np.array_equal(f.cols.cpu().numpy(), cols)
+    ptr, nc, loc = O.node_cell(m.nb_node, cells)
+    node_of = np.repeat(np.arange(m.nb_node), np.diff(ptr))
+    got = cols[rp[node_of][:, None] + f.nc_slot.cpu().numpy().reshape(-1, 4)]
+    others = np.array([np.delete(row, li) for row, li in zip(cells[nc], loc)])
+    assert np.array_equal(got, np.concatenate([node_of[:, None], others], axis=1))
+
+
 @pytest.fixture
 def formulation_ctx(cuda_ctx):
     """The shared context; the formulation a test sets is put back afterwards."""
