@@ -111,20 +111,28 @@ def test_sparsity_cols_finds_rows_itself_after_another_meshs_rows(cuda_ctx, self
         assert np.array_equal(got, np.concatenate([node_of[:, None], others], axis=1))
 
 
-def test_cell_repeating_a_node_gives_the_oracles_structure(cuda_ctx):
-    """A cell that lists a node twice: its two incidences of that node number
-    their slot bytes by their own local index, which only the node -> cell
-    local indices tell apart; the rows pass flags it and the columns pass
-    finds the rows again with those indices.  Structure and slot map equal to
-    the oracle's."""
+def test_cell_repeating_a_node_keeps_distinct_columns(cuda_ctx):
+    """A cell that lists a node twice (a degenerate cell, which the assembly
+    reports as such).  Its two incidences of that node number their slot bytes
+    by their own local index, which only the node -> cell local indices tell
+    apart: the rows pass flags the cell and the columns pass finds the rows
+    again with those indices.  Each row holds its node and the distinct nodes
+    of its cells; the reference's edge sort (the oracle) would also count the
+    repeated node's self-edge, two more entries here."""
     m = MESHES["tet_3"]()
     cells = m.cells.copy()
     cells[5, 2] = cells[5, 1]
     f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(3, m.coords, cells))
     f.initialize(1)
     f.compute_sparsity()
-    rp, cols = O.sparsity(m.nb_node, cells)
+    rows = [set([n]) for n in range(m.nb_node)]
+    for c in cells:
+        for a in c:
+            rows[a].update(int(x) for x in c)
+    rp = np.concatenate([[0], np.cumsum([len(r) for r in rows])])
+    cols = np.concatenate([sorted(r) for r in rows])
     assert np.array_equal(f.row_ptr.cpu().numpy(), rp) and np.array_equal(f.cols.cpu().numpy(), cols)
+    assert rp[-1] + 2 == O.sparsity(m.nb_node, cells)[0][-1]
     ptr, nc, loc = O.node_cell(m.nb_node, cells)
     node_of = np.repeat(np.arange(m.nb_node), np.diff(ptr))
     got = cols[rp[node_of][:, None] + f.nc_slot.cpu().numpy().reshape(-1, 4)]
