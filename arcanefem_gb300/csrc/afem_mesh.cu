@@ -633,13 +633,22 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       if (lane == 0 && !row_ptr) row_len[n] = ok ? D : 0;
       if (ok) {
         if (lane < 4) t.val[D + lane] = INT_MAX;
+        if (lane >= D && lane < 16) t.val[lane] = INT_MAX;
         __syncwarp();
         for (int i = lane; i < D; i += 32) {
           const int32_t x = t.val[i];
           int r = 0;
-          for (int u = 0; u < D; u += 4) {
-            const int4 q = *reinterpret_cast<const int4*>(t.val + u);
-            r += (q.x < x) + (q.y < x) + (q.z < x) + (q.w < x);
+          if (D <= 16) {   // tetrahedral rows (15 entries): four broadcast reads, no loop
+#pragma unroll
+            for (int u = 0; u < 16; u += 4) {
+              const int4 q = *reinterpret_cast<const int4*>(t.val + u);
+              r += (q.x < x) + (q.y < x) + (q.z < x) + (q.w < x);
+            }
+          } else {
+            for (int u = 0; u < D; u += 4) {
+              const int4 q = *reinterpret_cast<const int4*>(t.val + u);
+              r += (q.x < x) + (q.y < x) + (q.z < x) + (q.w < x);
+            }
           }
           // self-last: the neighbours keep their ascending order, the row's own node goes last
           const int p = !self_last ? r : (x == n ? D - 1 : r - (x > n));
