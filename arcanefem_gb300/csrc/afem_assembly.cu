@@ -1046,11 +1046,14 @@ __device__ __forceinline__ double cell_measure_ref(int dim, const double* __rest
 }
 
 // w_c = (qdot * measure) / npc, each operation rounded as the reference's
-// sum += qdot * domain / nbItem rounds it.
+// sum += qdot * domain / nbItem rounds it (the division by 4 an exact
+// scaling, by 3 the corrected constant-reciprocal product).
 __global__ void k_cell_source_weight(int nb_cell, int dim, const double* __restrict__ xyz,
                                      const int32_t* __restrict__ cn, double qdot, double* __restrict__ w) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x)
-    w[c] = __ddiv_rn(__dmul_rn(qdot, cell_measure_ref(dim, xyz, cn, c)), (double)(dim + 1));
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nb_cell; c += (int64_t)gridDim.x * blockDim.x) {
+    const double qm = __dmul_rn(qdot, cell_measure_ref(dim, xyz, cn, c));
+    w[c] = dim == 3 ? ref::div_const<4>(qm) : ref::div_const<3>(qm);
+  }
 }
 
 // rhs[node * stride + off] = sum_{cells, increasing} w_c                 (body = 0)

@@ -104,17 +104,26 @@ __device__ __forceinline__ double div(double a, double b, double rb, bool b_ok) 
   return __ddiv_rn(a, b);
 }
 
-// x / 6.0 rounded to nearest (the volume of computeVolumeTetra4): the same
-// correction with the constant RN(1 / 6).
-__device__ __forceinline__ double div6(double x) {
-  constexpr double r6 = 1.0 / 6.0;
-  if (in_window(x)) {
-    const double q = __dmul_rn(x, r6);
-    const double r = __fma_rn(-q, 6.0, x);
-    return __fma_rn(r, r6, q);
+// x / D rounded to nearest for a small integer constant D: for a power of
+// two the product by 1 / D is the same exact scaling; otherwise the same
+// correction as above with the constant RN(1 / D).
+template <int D>
+__device__ __forceinline__ double div_const(double x) {
+  constexpr double rd = 1.0 / D;
+  if constexpr ((D & (D - 1)) == 0) {
+    return __dmul_rn(x, rd);
+  } else {
+    if (in_window(x)) {
+      const double q = __dmul_rn(x, rd);
+      const double r = __fma_rn(-q, (double)D, x);
+      return __fma_rn(r, rd, q);
+    }
+    return __ddiv_rn(x, (double)D);
   }
-  return __ddiv_rn(x, 6.0);
 }
+
+// x / 6.0 rounded to nearest (the volume of computeVolumeTetra4).
+__device__ __forceinline__ double div6(double x) { return div_const<6>(x); }
 
 // V6 = |v0 . (v1 x v2)| with v_k = n_{k+1} - n_0 (computeVolumeTetra4,
 // femutils/ArcaneFemFunctionsGpu.h:113-128; math::cross / math::dot in their

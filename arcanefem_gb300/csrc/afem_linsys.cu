@@ -111,6 +111,16 @@ __global__ void k_transform(int n, const int32_t* __restrict__ rp, const int32_t
   }
 }
 
+// The pre-elimination values of the row-column eliminated rows (the only
+// ones k_rc_rhs reads), at their own positions of `saved`.
+__global__ void k_save_rc_rows(int n, const int32_t* __restrict__ rp, const double* __restrict__ vals,
+                               const uint8_t* __restrict__ ei, double* __restrict__ saved) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (ei[i] != AFEM_ELIMINATE_ROW_COLUMN) continue;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k) saved[k] = vals[k];
+  }
+}
+
 // rhs_j -= A_ij g_i for stored (i, j), i != j, i row-column eliminated, in
 // increasing i (DoFLinearSystemImplBase.cc:55-88); unfused multiply and
 // subtract as the reference's host code.  A_ij is read from the saved
@@ -413,8 +423,8 @@ afem_status afem_ls_apply_matrix_transformation(afem_linear_system ls) {
       AFEM_CUDA(cudaMallocAsync((void**)&ls->rc_saved, sizeof(double) * ls->nnz, ctx->stream));
       ls->rc_cap = ls->nnz;
     }
-    AFEM_CUDA(cudaMemcpyAsync(ls->rc_saved, ls->values, sizeof(double) * ls->nnz, cudaMemcpyDeviceToDevice,
-                              ctx->stream));
+    AFEM_TRY(launch(ctx, k_save_rc_rows, grid_for(ctx, ls->n, 256), 256, 0, ls->n, ls->row_ptr,
+                    (const double*)ls->values, (const uint8_t*)ls->elim_info, ls->rc_saved));
   }
   return launch(ctx, k_transform, grid_for(ctx, ls->n, 256), 256, 0, ls->n, ls->row_ptr, ls->cols, ls->values,
                 (const uint8_t*)ls->forced_info, (const double*)ls->forced_value, (const uint8_t*)ls->elim_info,
