@@ -716,47 +716,47 @@ __global__ void __launch_bounds__(128) k_elem_poisson_quad4(int cell0, int nb_ce
       if (bad && !ok) atomicOr(bad, kFlagDegenerateCell);
       if (coeff) scale_upper<4>(K, __ldg(coeff + c));
       write_rows_q1<4>(K, inv + 4 * c, er);
-      continue;
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int b = 0; b < 4; ++b) K[a][b] = 0.0;
-#pragma unroll
-    for (int g = 0; g < 4; ++g) {
-      const double xi = (g >> 1) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
-      const double dxi[4] = {-0.25 * (1.0 - eta), 0.25 * (1.0 - eta), 0.25 * (1.0 + eta), -0.25 * (1.0 + eta)};
-      const double deta[4] = {-0.25 * (1.0 - xi), -0.25 * (1.0 + xi), 0.25 * (1.0 + xi), 0.25 * (1.0 - xi)};
-      double j00 = 0.0, j01 = 0.0, j10 = 0.0, j11 = 0.0;
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        j00 += dxi[a] * x[a];
-        j01 += dxi[a] * y[a];
-        j10 += deta[a] * x[a];
-        j11 += deta[a] * y[a];
-      }
-      const double det = j00 * j11 - j01 * j10;
-      if (bad && !ref::measure_ok(det)) atomicOr(bad, kFlagDegenerateCell);
-      const double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
-      double dx[4], dy[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        dx[a] = i00 * dxi[a] + i01 * deta[a];
-        dy[a] = i10 * dxi[a] + i11 * deta[a];
-      }
+    } else {
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = a; b < 4; ++b) K[a][b] += (dx[a] * dx[b]) * det + (dy[a] * dy[b]) * det;
-    }
-    if (coeff) {
-      const double k = __ldg(coeff + c);
+        for (int b = 0; b < 4; ++b) K[a][b] = 0.0;
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+      for (int g = 0; g < 4; ++g) {
+        const double xi = (g >> 1) ? kGauss : -kGauss, eta = (g & 1) ? kGauss : -kGauss;
+        const double dxi[4] = {-0.25 * (1.0 - eta), 0.25 * (1.0 - eta), 0.25 * (1.0 + eta), -0.25 * (1.0 + eta)};
+        const double deta[4] = {-0.25 * (1.0 - xi), -0.25 * (1.0 + xi), 0.25 * (1.0 + xi), 0.25 * (1.0 - xi)};
+        double j00 = 0.0, j01 = 0.0, j10 = 0.0, j11 = 0.0;
 #pragma unroll
-        for (int b = a; b < 4; ++b) K[a][b] *= k;
+        for (int a = 0; a < 4; ++a) {
+          j00 += dxi[a] * x[a];
+          j01 += dxi[a] * y[a];
+          j10 += deta[a] * x[a];
+          j11 += deta[a] * y[a];
+        }
+        const double det = j00 * j11 - j01 * j10;
+        if (bad && !ref::measure_ok(det)) atomicOr(bad, kFlagDegenerateCell);
+        const double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
+        double dx[4], dy[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          dx[a] = i00 * dxi[a] + i01 * deta[a];
+          dy[a] = i10 * dxi[a] + i11 * deta[a];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = a; b < 4; ++b) K[a][b] += (dx[a] * dx[b]) * det + (dy[a] * dy[b]) * det;
+      }
+      if (coeff) {
+        const double k = __ldg(coeff + c);
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = a; b < 4; ++b) K[a][b] *= k;
+      }
+      write_rows_q1<4>(K, inv + 4 * c, er);
     }
-    write_rows_q1<4>(K, inv + 4 * c, er);
   }
 }
 
@@ -807,95 +807,95 @@ __global__ void __launch_bounds__(128) k_elem_poisson_hexa8(int cell0, int nb_ce
       if (bad && !ok) atomicOr(bad, kFlagDegenerateCell);
       if (coeff) scale_upper<8>(K, __ldg(coeff + c));
       write_rows_q1<8>(K, inv + 8 * c, er);
-      continue;
-    }
+    } else {
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
+      for (int a = 0; a < 8; ++a)
 #pragma unroll
-      for (int b = 0; b < 8; ++b) K[a][b] = 0.0;
-    // The trilinear map's derivatives are bilinear in the other two reference
-    // coordinates: d x / d xi = m_xi + eta m_xieta + zeta m_xizeta + eta zeta m_xietazeta,
-    // and so on, with the moments m (signed sums of the 8 nodal coordinates, / 8)
-    // formed once per cell by a Walsh-Hadamard butterfly: 3 FMAs per Jacobian
-    // entry per Gauss point instead of 8.  Node a has reference signs
-    // (s_xi, s_eta, s_zeta) = (-,-,-) (+,-,-) (+,+,-) (-,+,-) (-,-,+) (+,-,+) (+,+,+) (-,+,+).
-    double mo[3][8];   // per component: [1, xi, eta, xi eta, zeta, xi zeta, eta zeta, xi eta zeta]
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const double* v = q == 0 ? x : (q == 1 ? y : z);
-      // reorder to the binary order (xi bit 0, eta bit 1, zeta bit 2): nodes 0 1 3 2 4 5 7 6
-      const double u0 = v[0], u1 = v[1], u2 = v[3], u3 = v[2], u4 = v[4], u5 = v[5], u6 = v[7], u7 = v[6];
-      // stage xi
-      const double a0 = u1 + u0, a1 = u1 - u0, a2 = u3 + u2, a3 = u3 - u2;
-      const double a4 = u5 + u4, a5 = u5 - u4, a6 = u7 + u6, a7 = u7 - u6;
-      // stage eta
-      const double b0 = a2 + a0, b1 = a3 + a1, b2 = a2 - a0, b3 = a3 - a1;
-      const double b4 = a6 + a4, b5 = a7 + a5, b6 = a6 - a4, b7 = a7 - a5;
-      // stage zeta
-      mo[q][0] = 0.125 * (b4 + b0);
-      mo[q][1] = 0.125 * (b5 + b1);
-      mo[q][2] = 0.125 * (b6 + b2);
-      mo[q][3] = 0.125 * (b7 + b3);
-      mo[q][4] = 0.125 * (b4 - b0);
-      mo[q][5] = 0.125 * (b5 - b1);
-      mo[q][6] = 0.125 * (b6 - b2);
-      mo[q][7] = 0.125 * (b7 - b3);
-    }
-#pragma unroll 1
-    for (int g = 0; g < 8; ++g) {
-      const double* dxi = kHexDN[g][0];
-      const double* deta = kHexDN[g][1];
-      const double* dzeta = kHexDN[g][2];
-      const double xi = (g >> 2) ? kGauss : -kGauss, eta = ((g >> 1) & 1) ? kGauss : -kGauss,
-                   zeta = (g & 1) ? kGauss : -kGauss;
-      const double xe = (g >> 2) == ((g >> 1) & 1) ? kGauss * kGauss : -(kGauss * kGauss);
-      const double xz = (g >> 2) == (g & 1) ? kGauss * kGauss : -(kGauss * kGauss);
-      const double ez = ((g >> 1) & 1) == (g & 1) ? kGauss * kGauss : -(kGauss * kGauss);
-      double J[3][3];
+        for (int b = 0; b < 8; ++b) K[a][b] = 0.0;
+      // The trilinear map's derivatives are bilinear in the other two reference
+      // coordinates: d x / d xi = m_xi + eta m_xieta + zeta m_xizeta + eta zeta m_xietazeta,
+      // and so on, with the moments m (signed sums of the 8 nodal coordinates, / 8)
+      // formed once per cell by a Walsh-Hadamard butterfly: 3 FMAs per Jacobian
+      // entry per Gauss point instead of 8.  Node a has reference signs
+      // (s_xi, s_eta, s_zeta) = (-,-,-) (+,-,-) (+,+,-) (-,+,-) (-,-,+) (+,-,+) (+,+,+) (-,+,+).
+      double mo[3][8];   // per component: [1, xi, eta, xi eta, zeta, xi zeta, eta zeta, xi eta zeta]
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        J[0][q] = fma(ez, mo[q][7], fma(zeta, mo[q][5], fma(eta, mo[q][3], mo[q][1])));
-        J[1][q] = fma(xz, mo[q][7], fma(zeta, mo[q][6], fma(xi, mo[q][3], mo[q][2])));
-        J[2][q] = fma(xe, mo[q][7], fma(eta, mo[q][6], fma(xi, mo[q][5], mo[q][4])));
+        const double* v = q == 0 ? x : (q == 1 ? y : z);
+        // reorder to the binary order (xi bit 0, eta bit 1, zeta bit 2): nodes 0 1 3 2 4 5 7 6
+        const double u0 = v[0], u1 = v[1], u2 = v[3], u3 = v[2], u4 = v[4], u5 = v[5], u6 = v[7], u7 = v[6];
+        // stage xi
+        const double a0 = u1 + u0, a1 = u1 - u0, a2 = u3 + u2, a3 = u3 - u2;
+        const double a4 = u5 + u4, a5 = u5 - u4, a6 = u7 + u6, a7 = u7 - u6;
+        // stage eta
+        const double b0 = a2 + a0, b1 = a3 + a1, b2 = a2 - a0, b3 = a3 - a1;
+        const double b4 = a6 + a4, b5 = a7 + a5, b6 = a6 - a4, b7 = a7 - a5;
+        // stage zeta
+        mo[q][0] = 0.125 * (b4 + b0);
+        mo[q][1] = 0.125 * (b5 + b1);
+        mo[q][2] = 0.125 * (b6 + b2);
+        mo[q][3] = 0.125 * (b7 + b3);
+        mo[q][4] = 0.125 * (b4 - b0);
+        mo[q][5] = 0.125 * (b5 - b1);
+        mo[q][6] = 0.125 * (b6 - b2);
+        mo[q][7] = 0.125 * (b7 - b3);
       }
-      // determinant by the first row, inverse = adjugate / det
-      const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-      const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-      const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-      const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-      if (bad && !ref::measure_ok(det)) atomicOr(bad, kFlagDegenerateCell);
-      const double id = 1.0 / det;
-      const double v00 = c00 * id, v10 = c01 * id, v20 = c02 * id;
-      const double v01 = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-      const double v11 = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-      const double v21 = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-      const double v02 = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-      const double v12 = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-      const double v22 = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-      // physical gradients, and the same scaled by det for the weighted products
-      double dx[8], dy[8], dz[8], sx[8], sy[8], sz[8];
+#pragma unroll 1
+      for (int g = 0; g < 8; ++g) {
+        const double* dxi = kHexDN[g][0];
+        const double* deta = kHexDN[g][1];
+        const double* dzeta = kHexDN[g][2];
+        const double xi = (g >> 2) ? kGauss : -kGauss, eta = ((g >> 1) & 1) ? kGauss : -kGauss,
+                     zeta = (g & 1) ? kGauss : -kGauss;
+        const double xe = (g >> 2) == ((g >> 1) & 1) ? kGauss * kGauss : -(kGauss * kGauss);
+        const double xz = (g >> 2) == (g & 1) ? kGauss * kGauss : -(kGauss * kGauss);
+        const double ez = ((g >> 1) & 1) == (g & 1) ? kGauss * kGauss : -(kGauss * kGauss);
+        double J[3][3];
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
-        dx[a] = v00 * dxi[a] + v01 * deta[a] + v02 * dzeta[a];
-        dy[a] = v10 * dxi[a] + v11 * deta[a] + v12 * dzeta[a];
-        dz[a] = v20 * dxi[a] + v21 * deta[a] + v22 * dzeta[a];
-        sx[a] = dx[a] * det;
-        sy[a] = dy[a] * det;
-        sz[a] = dz[a] * det;
+        for (int q = 0; q < 3; ++q) {
+          J[0][q] = fma(ez, mo[q][7], fma(zeta, mo[q][5], fma(eta, mo[q][3], mo[q][1])));
+          J[1][q] = fma(xz, mo[q][7], fma(zeta, mo[q][6], fma(xi, mo[q][3], mo[q][2])));
+          J[2][q] = fma(xe, mo[q][7], fma(eta, mo[q][6], fma(xi, mo[q][5], mo[q][4])));
+        }
+        // determinant by the first row, inverse = adjugate / det
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        if (bad && !ref::measure_ok(det)) atomicOr(bad, kFlagDegenerateCell);
+        const double id = 1.0 / det;
+        const double v00 = c00 * id, v10 = c01 * id, v20 = c02 * id;
+        const double v01 = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        const double v11 = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        const double v21 = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        const double v02 = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        const double v12 = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        const double v22 = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        // physical gradients, and the same scaled by det for the weighted products
+        double dx[8], dy[8], dz[8], sx[8], sy[8], sz[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          dx[a] = v00 * dxi[a] + v01 * deta[a] + v02 * dzeta[a];
+          dy[a] = v10 * dxi[a] + v11 * deta[a] + v12 * dzeta[a];
+          dz[a] = v20 * dxi[a] + v21 * deta[a] + v22 * dzeta[a];
+          sx[a] = dx[a] * det;
+          sy[a] = dy[a] * det;
+          sz[a] = dz[a] * det;
+        }
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int b = a; b < 8; ++b) K[a][b] = fma(sx[a], dx[b], fma(sy[a], dy[b], fma(sz[a], dz[b], K[a][b])));
       }
+      if (coeff) {
+        const double k = __ldg(coeff + c);
 #pragma unroll
-      for (int a = 0; a < 8; ++a)
+        for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = a; b < 8; ++b) K[a][b] = fma(sx[a], dx[b], fma(sy[a], dy[b], fma(sz[a], dz[b], K[a][b])));
+          for (int b = a; b < 8; ++b) K[a][b] *= k;
+      }
+      write_rows_q1<8>(K, inv + 8 * c, er);
     }
-    if (coeff) {
-      const double k = __ldg(coeff + c);
-#pragma unroll
-      for (int a = 0; a < 8; ++a)
-#pragma unroll
-        for (int b = a; b < 8; ++b) K[a][b] *= k;
-    }
-    write_rows_q1<8>(K, inv + 8 * c, er);
   }
 }
 
