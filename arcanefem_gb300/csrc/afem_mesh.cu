@@ -516,9 +516,9 @@ __global__ void __launch_bounds__(kThreadBlock)
   }
 }
 
-// The nodes in more than `min_deg` cells (every node when -1), and the rows
-// k_sparsity_thread deferred (more distinct neighbours than its per-thread
-// table holds), listed
+// The nodes in more than `min_deg` cells (every node when -1, none when
+// INT_MAX), and the rows k_sparsity_thread or k_sparsity_rows_sub deferred
+// (more distinct neighbours than their tables hold), listed
 // in `list[0 .. *list_count)`: one warp per node, lanes over its incidences
 // (chunks of 32).  The row's own node is inserted into the warp's hash set
 // first, then every lane inserts the nodes of its cell: a node met again
@@ -554,12 +554,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const bool vec = (reinterpret_cast<uintptr_t>(cn) & 15) == 0;
-  const int count = nb_node + *list_count;
+  const int direct = min_deg == INT_MAX ? 0 : nb_node;   // INT_MAX: the list alone
+  const int count = direct + *list_count;
   for (int it = wid; it < count; it += nwarps) {
-    const int n = it < nb_node ? it : __ldg(list + (it - nb_node));
+    const int n = it < direct ? it : __ldg(list + (it - direct));
     const int32_t b = __ldg(nc_ptr + n);
     const int deg = __ldg(nc_ptr + n + 1) - b;
-    if (it < nb_node && deg <= min_deg) continue;   // k_sparsity_thread's
+    if (it < direct && deg <= min_deg) continue;   // k_sparsity_thread's
     if (lane == 0) {
       const int h = tab_hash(n);
       t.key[h] = n;
@@ -695,6 +696,225 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   }
 }
 
+// Dense meshes (tetrahedra, about 24 cells per node): a warp per 32 / G
+// nodes, G lanes per node over its incidences in chunks of G, so that the
+// lanes stay busy (24 incidences fill 3 chunks of 8 exactly, where a whole
+// warp per node leaves 8 of its 32 lanes idle) and each node's fixed costs
+// and ranking are shared by the warp's nodes.  The same hash sets as
+// k_sparsity_rows_warp, one of SubTable::slots keys per node; the same
+// rounds, ranks and slot bytes.  Nodes in more than 4 G cells, or with more
+// than 3/4 of a table's slots in distinct neighbours, go to
+// k_sparsity_rows_warp through the node list.  Errors as k_sparsity_thread.
+constexpr int kSubLanes = 8;   // lanes per node of k_sparsity_rows_sub
+
+template <int G>
+struct SubTable {
+  static constexpr int slots = G == 16 ? 256 : 128;
+  static constexpr int bits = G == 16 ? 8 : 7;
+  static constexpr int max_d = slots * 3 / 4;
+  static constexpr int max_deg = 4 * G;
+};
+
+template <int TS, int BITS>
+__device__ __forceinline__ int sub_hash(int32_t v) { return (int)(((uint32_t)v * 2654435761u) >> (32 - BITS)); }
+
+template <int NPC, bool FILL, int G>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    k_sparsity_rows_sub(int nb_node, const int32_t* __restrict__ cn, const int32_t* __restrict__ nc_ptr,
+                        const int32_t* __restrict__ nc_cell, const uint8_t* __restrict__ nc_local,
+                        const int32_t* __restrict__ row_ptr, int self_last, int packed_slots,
+                        int32_t* __restrict__ row_len, int32_t* __restrict__ cols, uint8_t* __restrict__ slot,
+                        int32_t* __restrict__ defer, int32_t* __restrict__ defer_count, int* __restrict__ err) {
+  using ST = SubTable<G>;
+  constexpr int NG = 32 / G, TS = ST::slots, BITS = ST::bits, DMAX = ST::max_d;
+  __shared__ int32_t s_key[kWarpsPerBlock][NG][TS];
+  __shared__ int16_t s_at[kWarpsPerBlock][NG][DMAX];
+  __shared__ __align__(16) int32_t s_val[kWarpsPerBlock][NG][FILL ? DMAX + 4 : 4];
+  __shared__ uint8_t s_pos[kWarpsPerBlock][NG][FILL ? TS : 1];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int g = lane / G, gl = lane - g * G;
+  const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (g * G);
+  const unsigned gbelow = gmask & ((1u << lane) - 1u);
+  int32_t* const key = s_key[w][g];
+  int16_t* const at = s_at[w][g];
+  int32_t* const val = s_val[w][g];
+  uint8_t* const pos = s_pos[w][g];
+  for (int i = gl; i < TS; i += G) key[i] = -1;
+  __syncwarp();
+  const bool vec = (reinterpret_cast<uintptr_t>(cn) & 15) == 0;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int ngroups = (nb_node + NG - 1) / NG;
+  for (int grp = wid; grp < ngroups; grp += nwarps) {
+    const int n = grp * NG + g;
+    int32_t b = 0;
+    int deg = 0;
+    if (n < nb_node) {
+      b = __ldg(nc_ptr + n);
+      deg = __ldg(nc_ptr + n + 1) - b;
+    }
+    const bool heavy = n < nb_node && deg > ST::max_deg;
+    if (heavy && gl == 0) defer_node(n, defer, defer_count);
+    const bool mine = n < nb_node && !heavy;
+    if (mine && gl == 0) {
+      const int h = sub_hash<TS, BITS>(n);
+      key[h] = n;
+      at[0] = (int16_t)h;
+      if (FILL) val[0] = n;
+    }
+    __syncwarp();
+    const int maxdeg = __reduce_max_sync(0xffffffffu, mine ? deg : 0);
+    int D = 1;   // distinct columns so far, uniform across the node's lanes
+    bool bad = false, full = false;
+    for (int kb = 0; kb < maxdeg; kb += G) {
+      const bool act = mine && kb + gl < deg;
+      int32_t v[NPC];
+      int li = 0;
+      if (act) {
+        load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + gl), v);
+        if (FILL && nc_local) {
+          li = __ldg(nc_local + b + kb + gl);
+        } else if (FILL) {
+          li = local_index<NPC>(v, n, err);
+        } else {
+#pragma unroll
+          for (int j = NPC - 1; j > 0; --j)
+            if (v[j] == n) li = j;
+        }
+#pragma unroll
+        for (int j = 0; j < NPC; ++j) bad |= (unsigned)v[j] >= (unsigned)nb_node;
+      }
+#pragma unroll
+      for (int r = 0; r + 1 < NPC; ++r) {
+        int j = li + 1 + r;
+        j -= j >= NPC ? NPC : 0;
+        bool fresh = false;
+        int h = 0;
+        if (act) {
+          const int32_t x = pick<NPC>(v, j);
+          h = sub_hash<TS, BITS>(x);
+          const int32_t old = atomicCAS(key + h, -1, x);
+          fresh = old == -1;
+          if (!fresh && old != x) {
+            h = -1;
+#pragma unroll 1
+            for (int p = 1; p < TS; ++p) {
+              const int hp = (sub_hash<TS, BITS>(x) + p) & (TS - 1);
+              const int32_t o = atomicCAS(key + hp, -1, x);
+              if (o == -1 || o == x) {
+                fresh = o == -1;
+                h = hp;
+                break;
+              }
+            }
+            full |= h < 0;
+          }
+        }
+        const unsigned fb = __ballot_sync(0xffffffffu, fresh);
+        if (fresh) {
+          const int a = D + __popc(fb & gbelow);
+          if (a < DMAX) {
+            at[a] = (int16_t)h;
+            if (FILL) val[a] = pick<NPC>(v, j);
+          } else {
+            full = true;
+          }
+        }
+        D += __popc(fb & gmask);
+      }
+    }
+    const unsigned badm = __ballot_sync(0xffffffffu, bad), fullm = __ballot_sync(0xffffffffu, full);
+    const bool bad_g = (badm & gmask) != 0;
+    const bool spill = (fullm & gmask) != 0 || D > DMAX;   // keys past the slot list: clear the whole table
+    const bool over_g = mine && !bad_g && spill;
+    if (over_g && gl == 0) defer_node(n, defer, defer_count);
+    if (!FILL) {
+      if (mine && gl == 0) {
+        if (bad_g) atomicOr(err, 8);
+        if (bad_g || !over_g) row_len[n] = bad_g ? 0 : D;
+      }
+    } else {
+      bool ok = mine && !bad_g && !over_g;
+      int64_t rb = (int64_t)(NPC - 1) * b + n;
+      if (mine && bad_g && gl == 0) atomicOr(err, 8);
+      if (ok) {
+        if (row_ptr) {
+          rb = __ldg(row_ptr + n);
+          ok = __ldg(row_ptr + n + 1) - (int32_t)rb == D;
+          if (!ok && gl == 0) atomicOr(err, 4);
+        } else if (gl == 0) {
+          row_len[n] = D;
+        }
+      }
+      if (ok)
+        for (int i = D + gl; i < max(D + 4, 16); i += G) val[i] = INT_MAX;
+      __syncwarp();
+      if (ok) {
+        for (int i = gl; i < D; i += G) {
+          const int32_t x = val[i];
+          int r = 0;
+          if (D <= 16) {
+#pragma unroll
+            for (int u = 0; u < 16; u += 4) {
+              const int4 q = *reinterpret_cast<const int4*>(val + u);
+              r += (q.x < x) + (q.y < x) + (q.z < x) + (q.w < x);
+            }
+          } else {
+            for (int u = 0; u < D; u += 4) {
+              const int4 q = *reinterpret_cast<const int4*>(val + u);
+              r += (q.x < x) + (q.y < x) + (q.z < x) + (q.w < x);
+            }
+          }
+          // self-last: the neighbours keep their ascending order, the row's own node goes last
+          const int p = !self_last ? r : (x == n ? D - 1 : r - (x > n));
+          cols[rb + p] = x;
+          pos[at[i]] = (uint8_t)p;
+        }
+      }
+      __syncwarp();
+      const int pn = ok ? pos[at[0]] : 0;
+      for (int kb = 0; kb < maxdeg; kb += G) {
+        if (!ok || kb + gl >= deg) continue;
+        int32_t v[NPC];
+        load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + gl), v);
+        const int li = nc_local ? __ldg(nc_local + b + kb + gl) : local_index<NPC>(v, n, err);
+        // slot byte q of the incidence at bits 8q: its own column, then the
+        // other cell nodes in increasing local index
+        using Word = typename std::conditional<(NPC > 4), uint64_t, uint32_t>::type;
+        Word word = (Word)pn;
+#pragma unroll
+        for (int r = 0; r + 1 < NPC; ++r) {
+          int j = li + 1 + r;
+          j -= j >= NPC ? NPC : 0;
+          const int32_t x = pick<NPC>(v, j);
+          int h = sub_hash<TS, BITS>(x);
+#pragma unroll 1
+          for (int q = 0; q < TS && key[h] != x; ++q) h = (h + 1) & (TS - 1);
+          word |= (Word)pos[h] << (8 * (j < li ? j + 1 : j));
+        }
+        uint8_t* dst = slot + (int64_t)(b + kb + gl) * NPC;
+        if (NPC == 4 && packed_slots) {
+          *reinterpret_cast<uint32_t*>(dst) = (uint32_t)word;
+        } else if (NPC == 8 && packed_slots) {
+          *reinterpret_cast<uint2*>(dst) = make_uint2((uint32_t)word, (uint32_t)((uint64_t)word >> 32));
+        } else {
+#pragma unroll
+          for (int q = 0; q < NPC; ++q) dst[q] = (uint8_t)((uint64_t)word >> (8 * q));
+        }
+      }
+    }
+    __syncwarp();
+    // empty the table: the recorded slots, or all of it after an overflow
+    if (spill) {
+      for (int i = gl; i < TS; i += G) key[i] = -1;
+    } else if (mine) {
+      for (int i = gl; i < D; i += G) key[at[i]] = -1;
+    }
+    __syncwarp();
+  }
+}
+
 // Block CSR -> scalar CSR structure (BSRMatrix::toCsr, femutils/BSRFormat.cc:110-172).
 __global__ void k_bsr_rows(int nb_brow, int b, const int32_t* __restrict__ brow_ptr, int32_t* __restrict__ row_ptr) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r <= nb_brow * b; r += gridDim.x * blockDim.x) {
@@ -790,18 +1010,26 @@ static afem_status launch_rows(afem_context ctx, bool dense, int nb_node, const 
                                int32_t* defer_count, int* err) {
   static const int per_sm_thread = resident_blocks(k_sparsity_thread<NPC, FILL>, kThreadBlock);
   static const int per_sm_warp = resident_blocks(k_sparsity_rows_warp<NPC, FILL>, kWarpsPerBlock * 32);
+  static const int per_sm_sub = resident_blocks(k_sparsity_rows_sub<NPC, FILL, kSubLanes>, kWarpsPerBlock * 32);
   if (!dense) {
     const unsigned g1 = (unsigned)std::min<int64_t>((nb_node + kThreadBlock - 1) / kThreadBlock,
                                                     (int64_t)ctx->sm_count * per_sm_thread);
     AFEM_TRY(launch(ctx, k_sparsity_thread<NPC, FILL>, g1, kThreadBlock, 0, nb_node, cn, nc_ptr, nc_cell, nc_local,
                     row_ptr, self_last, packed, row_len, cols, slot, defer, defer_count, err));
+  } else {
+    const int64_t groups = ((int64_t)nb_node + 32 / kSubLanes - 1) / (32 / kSubLanes);
+    const unsigned g1 = (unsigned)std::min<int64_t>((groups + kWarpsPerBlock - 1) / kWarpsPerBlock,
+                                                    (int64_t)ctx->sm_count * per_sm_sub);
+    AFEM_TRY(launch(ctx, k_sparsity_rows_sub<NPC, FILL, kSubLanes>, g1, kWarpsPerBlock * 32, 0, nb_node, cn, nc_ptr,
+                    nc_cell, nc_local, row_ptr, self_last, packed, row_len, cols, slot, defer, defer_count, err));
   }
-  // the dense rows, and the rows k_sparsity_thread passed on: the grid covers
-  // the worst case and each warp reads the list's length on the device
+  // the rows the thread or sub-warp kernel passed on (and, after the thread
+  // kernel, the heavy ones): the grid covers the worst case and each warp
+  // reads the list's length on the device
   const unsigned g2 = (unsigned)std::min<int64_t>((nb_node + kWarpsPerBlock - 1) / kWarpsPerBlock,
                                                   (int64_t)ctx->sm_count * per_sm_warp);
   return launch(ctx, k_sparsity_rows_warp<NPC, FILL>, g2, kWarpsPerBlock * 32, 0, nb_node,
-                dense ? -1 : ThreadTable<NPC>::max_deg, (const int32_t*)defer, (const int32_t*)defer_count, cn,
+                dense ? INT_MAX : ThreadTable<NPC>::max_deg, (const int32_t*)defer, (const int32_t*)defer_count, cn,
                 nc_ptr, nc_cell, nc_local, row_ptr, self_last, packed, row_len, cols, slot, err);
 }
 
