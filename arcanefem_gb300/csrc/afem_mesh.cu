@@ -715,6 +715,11 @@ struct SubTable {
   static constexpr int max_deg = 4 * G;
 };
 
+// Whether the insertion's table slots (one byte per round) and the local
+// index fit one 32-bit word per chunk: three rounds (tetrahedra).
+template <int NPC>
+constexpr bool kKeepSlots = NPC <= 4;
+
 template <int TS, int BITS>
 __device__ __forceinline__ int sub_hash(int32_t v) { return (int)(((uint32_t)v * 2654435761u) >> (32 - BITS)); }
 
@@ -767,7 +772,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     const int maxdeg = __reduce_max_sync(0xffffffffu, mine ? deg : 0);
     int D = 1;   // distinct columns so far, uniform across the node's lanes
     bool bad = false, full = false;
-    for (int kb = 0; kb < maxdeg; kb += G) {
+    // per chunk (at most 4: a node here has at most 4 G incidences), the
+    // table slot of each round's candidate and the local index, one byte
+    // each, for the slot bytes below (tetrahedra: 3 rounds)
+    uint32_t kept[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int kb = c * G;
+      if (kb >= maxdeg) break;
       const bool act = mine && kb + gl < deg;
       int32_t v[NPC];
       int li = 0;
@@ -822,7 +834,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           }
         }
         D += __popc(fb & gmask);
+        if (kKeepSlots<NPC>) kept[c] |= (uint32_t)(h & 0xff) << (8 * r);
       }
+      if (kKeepSlots<NPC>) kept[c] |= (uint32_t)li << 24;
     }
     const unsigned badm = __ballot_sync(0xffffffffu, bad), fullm = __ballot_sync(0xffffffffu, full);
     const bool bad_g = (badm & gmask) != 0;
@@ -874,24 +888,37 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       }
       __syncwarp();
       const int pn = ok ? pos[at[0]] : 0;
-      for (int kb = 0; kb < maxdeg; kb += G) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int kb = c * G;
+        if (kb >= maxdeg) break;
         if (!ok || kb + gl >= deg) continue;
-        int32_t v[NPC];
-        load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + gl), v);
-        const int li = nc_local ? __ldg(nc_local + b + kb + gl) : local_index<NPC>(v, n, err);
         // slot byte q of the incidence at bits 8q: its own column, then the
         // other cell nodes in increasing local index
         using Word = typename std::conditional<(NPC > 4), uint64_t, uint32_t>::type;
         Word word = (Word)pn;
+        if constexpr (kKeepSlots<NPC>) {
+          const int li = (int)(kept[c] >> 24);
 #pragma unroll
-        for (int r = 0; r + 1 < NPC; ++r) {
-          int j = li + 1 + r;
-          j -= j >= NPC ? NPC : 0;
-          const int32_t x = pick<NPC>(v, j);
-          int h = sub_hash<TS, BITS>(x);
+          for (int r = 0; r + 1 < NPC; ++r) {
+            int j = li + 1 + r;
+            j -= j >= NPC ? NPC : 0;
+            word |= (Word)pos[(kept[c] >> (8 * r)) & 0xffu] << (8 * (j < li ? j + 1 : j));
+          }
+        } else {
+          int32_t v[NPC];
+          load_cell<NPC>(cn, vec, __ldg(nc_cell + b + kb + gl), v);
+          const int li = nc_local ? __ldg(nc_local + b + kb + gl) : local_index<NPC>(v, n, err);
+#pragma unroll
+          for (int r = 0; r + 1 < NPC; ++r) {
+            int j = li + 1 + r;
+            j -= j >= NPC ? NPC : 0;
+            const int32_t x = pick<NPC>(v, j);
+            int h = sub_hash<TS, BITS>(x);
 #pragma unroll 1
-          for (int q = 0; q < TS && key[h] != x; ++q) h = (h + 1) & (TS - 1);
-          word |= (Word)pos[h] << (8 * (j < li ? j + 1 : j));
+            for (int q = 0; q < TS && key[h] != x; ++q) h = (h + 1) & (TS - 1);
+            word |= (Word)pos[h] << (8 * (j < li ? j + 1 : j));
+          }
         }
         uint8_t* dst = slot + (int64_t)(b + kb + gl) * NPC;
         if (NPC == 4 && packed_slots) {
