@@ -182,3 +182,29 @@ def test_exact_coarse_level_gradient_and_spd():
     M = operator_matrix(net, c, n)
     assert np.abs(M - M.T).max() <= 1e-12 * np.abs(M).max()
     assert np.linalg.eigvalsh(0.5 * (M + M.T)).min() > 0
+
+
+@pytest.mark.parametrize("sizes", [
+    [263169, 66049, 16641, 4225, 1089, 289, 81, 25, 9],   # 513^2, 9 levels (the bench)
+    [66049, 16641, 4225, 1089, 289, 81, 25, 9],           # 257^2 (the learned test)
+    [4225, 1089, 289, 81],
+    [5000, 3000, 2100, 2048, 400, 321, 320, 12],          # the thresholds themselves
+    [700, 330, 200],
+    [200, 90],
+    [9000, 4000],                                          # no exact level
+])
+def test_level_rules_agree_with_the_oracle(sizes):
+    """The library's host rules for the exactly solved level, the factored
+    levels and the parameter count (arcanefem_gb300/learned.py, mirrored by the
+    device code) are the oracle's: the parameter vector one side packs is the
+    one the other unpacks."""
+    from arcanefem_gb300 import learned
+    assert learned.FACT_ROWS == MO.FACT_ROWS and learned.EXACT_ROWS == MO.EXACT_ROWS
+    ex = MO.exact_level(sizes)
+    assert learned.exact_level(sizes) == ex
+    fl = MO.fact_levels(sizes, MO.FACT_ROWS, ex)
+    assert learned.fact_levels(sizes) == fl
+    assert 0 in fl and (ex is None or all(l < ex for l in fl))
+    for layers in (1, 3, 6):
+        assert learned.param_count(layers, len(sizes), len(fl)) == MO.param_count(layers, len(sizes), len(fl))
+
