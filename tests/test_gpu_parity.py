@@ -111,6 +111,30 @@ def test_sparsity_cols_finds_rows_itself_after_another_meshs_rows(cuda_ctx, self
         assert np.array_equal(got, np.concatenate([node_of[:, None], others], axis=1))
 
 
+@pytest.mark.parametrize("self_last", [False, True])
+def test_dense_triangle_sparsity_matches_oracle(cuda_ctx, self_last):
+    """700 random triangles on 100 nodes: about 21 cells per node, so the
+    triangle mesh takes the dense path (8 lanes per node, the nodes in more
+    than 32 cells passed on to the warp kernel), with rows of 30 to 50 entries
+    (the ranking's general path).  Structure and slot map bit-exact."""
+    rng = np.random.default_rng(33)
+    n = 100
+    cells = np.array([rng.choice(n, 3, replace=False) for _ in range(700)], dtype=np.int32)
+    coords = np.concatenate([rng.random((n, 2)), np.zeros((n, 1))], axis=1)
+    ptr, nc, loc = O.node_cell(n, cells)
+    deg = np.diff(ptr)
+    assert deg.mean() > 16 and (deg > 32).any() and (deg <= 32).any()
+    f = fem.BSRFormat(cuda_ctx, fem.Mesh.from_host(2, coords, cells))
+    f.initialize(1, col_order=fem.COLS_SELF_LAST if self_last else fem.COLS_ASCENDING)
+    f.compute_sparsity()
+    rp, cols = O.sparsity(n, cells, self_last=self_last)
+    assert np.array_equal(f.row_ptr.cpu().numpy(), rp) and np.array_equal(f.cols.cpu().numpy(), cols)
+    node_of = np.repeat(np.arange(n), deg)
+    got = cols[rp[node_of][:, None] + f.nc_slot.cpu().numpy().reshape(-1, 3)]
+    others = np.array([np.delete(row, li) for row, li in zip(cells[nc], loc)])
+    assert np.array_equal(got, np.concatenate([node_of[:, None], others], axis=1))
+
+
 def test_cell_repeating_a_node_keeps_distinct_columns(cuda_ctx):
     """A cell that lists a node twice (a degenerate cell, which the assembly
     reports as such).  Its two incidences of that node number their slot bytes
