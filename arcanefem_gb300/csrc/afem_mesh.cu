@@ -11,9 +11,10 @@
 //   the output is deterministic.
 //
 // node -> node sparsity (rows of the assembled matrix):
-//   one warp per node, one lane per incidence (chunks of 32), or one thread
-//   per node on meshes of few cells per node: the nodes of the node's
-//   incident cells go into a hash set in shared memory; the number of
+//   8 lanes per node (4 nodes per warp) on meshes of many cells per node,
+//   one thread per node on meshes of few, one warp per node for the rows
+//   either passes on: the nodes of the node's incident cells go into a hash
+//   set in shared memory; the number of
 //   distinct values is the row length = 1 + number of neighbours
 //   (femutils/BSRFormat.cc:445-557, row = deg + 1).  The same pass ranks
 //   each neighbour, writes the columns (ascending or self-last) and, for
