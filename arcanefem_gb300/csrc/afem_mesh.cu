@@ -956,14 +956,23 @@ __global__ void k_bsr_rows(int nb_brow, int b, const int32_t* __restrict__ brow_
   }
 }
 
+// The scalar columns of block row br fill one contiguous range,
+// [s b^2, (s + len) b^2) with s = brow_ptr[br]: entry idx of it is scalar row
+// i = idx / (len b), block x, component k.  A warp per block row writes the
+// range with consecutive lanes on consecutive entries.
 __global__ void k_bsr_cols(int nb_brow, int b, const int32_t* __restrict__ brow_ptr, const int32_t* __restrict__ bcols,
                            int32_t* __restrict__ cols) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nb_brow * b; r += gridDim.x * blockDim.x) {
-    int br = r / b, i = r - br * b;
-    int32_t s = brow_ptr[br], len = brow_ptr[br + 1] - s;
-    int64_t o = (int64_t)s * b * b + (int64_t)i * len * b;
-    for (int32_t x = 0; x < len; ++x)
-      for (int k = 0; k < b; ++k) cols[o + (int64_t)x * b + k] = bcols[s + x] * b + k;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t br = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; br < nb_brow; br += nwarps) {
+    const int32_t s = __ldg(brow_ptr + br), len = __ldg(brow_ptr + br + 1) - s;
+    const int row_len = len * b, total = row_len * b;
+    int32_t* out = cols + (int64_t)s * b * b;
+    for (int idx = lane; idx < total; idx += 32) {
+      const int rem = idx % row_len;   // position within scalar row idx / row_len
+      const int x = rem / b, k = rem - x * b;
+      out[idx] = __ldg(bcols + s + x) * b + k;
+    }
   }
 }
 
@@ -1311,7 +1320,7 @@ afem_status afem_bsr_to_csr_structure(afem_context ctx, int nb_brow, int b, cons
   scratch_reset(ctx);
   AFEM_TRY(launch(ctx, k_bsr_rows, grid_for(ctx, (int64_t)nb_brow * b + 1, 256), 256, 0, nb_brow, b, brow_ptr_d,
                   row_ptr_d));
-  return launch(ctx, k_bsr_cols, grid_for(ctx, (int64_t)nb_brow * b, 256), 256, 0, nb_brow, b, brow_ptr_d, bcols_d,
+  return launch(ctx, k_bsr_cols, grid_for(ctx, (int64_t)nb_brow * 32, 256), 256, 0, nb_brow, b, brow_ptr_d, bcols_d,
                 cols_d);
 }
 

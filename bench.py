@@ -299,6 +299,16 @@ def time_structure(fmt, reps=3):
     out = {k: statistics.median(v[1:]) for k, v in res.items()}
     out["sparsity_ms"] = out["rows_ms"] + out["cols_ms"]
     out["note"] = "warm, device time; rows_ms includes the host read of nnz"
+    if fmt.nb_dof > 1:   # BSRMatrix::toCsr: the block structure expanded to scalar rows on the device
+        times = []
+        for _ in range(reps + 1):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            fmt.to_csr()
+            ev[1].record()
+            torch.cuda.synchronize()
+            times.append(ev[0].elapsed_time(ev[1]))
+        out["bsr_to_csr_ms"] = statistics.median(times[1:])
     return out
 
 
